@@ -1,0 +1,356 @@
+"""Benchmark: simulated ECGs per second on one GB300 (replicas on N GPUs), JSON line on stdout.
+
+Workload (default): the batched configuration -- one resident 160^3 ellipsoid heart (wall 14,
+3 layers, delays {1,2,2}), 12 leads on a radius-120 sphere, 600 steps of 1 ms, 256 seeded
+16-gene parameter vectors per step.  A step is one batched evaluation of those 256 vectors.
+
+  value      simulations/s from CUDA events around the device passes, inputs resident in HBM
+  e2e        simulations/s through the public C ABI (ekg_eval_batch): host genes in, host
+             criteria + ECGs out, host<->device copies and host gene mapping inside the timed region
+  plain      the plain single-simulation form (ekg_eval, one call per simulation) on the same heart
+  roofline   the lead-contraction kernel against the measured bf16 peak (algorithmic flops
+             2 x L x 3V x T per simulation)
+  cpu_baseline  the reference's CPU algorithm (FP64 port with the reference's cost structure,
+             bit-identical results) run as one independent simulation per host core, on a bounded
+             sample of the same heart (the first few time steps; cost is linear in steps)
+
+--impl reference runs only that CPU farm (rank 0), on the same workload, metric and unit.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ECG sims/sec & p99 latency, batched vs plain on GB300, ECG rel-L2<=1e-4 vs FP64"
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Dist:
+    """Barrier and max-over-ranks for replica runs (torch.distributed gloo on host tensors)."""
+
+    def __init__(self):
+        self.rank, self.world, self.local = dist_info()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_heart_spec(name: str):
+    from ekgsim_gb300 import synth
+    if name == "batched":
+        c = synth.config(2)
+        return c["spec"], c["steps"], c["batch"], 2, c["name"]
+    c = synth.config(1)
+    return c["spec"], c["steps"], 64, 1, c["name"]
+
+
+def build_inputs(spec, steps, batch, cfg_index):
+    from ekgsim_gb300 import synth
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    rng = np.random.Generator(np.random.PCG64(spec.seed))
+    leads_zyx = synth.leads(spec, rng)[:, ::-1].copy()
+    genes = np.stack([synth.genes_for(spec, r, cfg_index) for r in range(batch)])
+    target = synth.analytic_target(spec.n_leads, steps, spec.seed + 999)
+    return grid, tm, leads_zyx, genes, target
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("bf16_tflops", 1900.0), d.get("hbm_gbs", 6800.0), "measured"
+    return 1900.0, 6800.0, "fallback"
+
+
+def profiled_traffic(workload: str):
+    """DRAM bytes per simulation of the contraction kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", f"contract_{workload}.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_sim:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_farm(spec, steps, genes, sample_steps: int, threads: int):
+    """The reference's CPU algorithm as a farm of independent single-threaded simulations, one per
+    host core, each on the first `sample_steps` steps.  Returns (sims/s, seconds, sample text)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from ekgsim_gb300 import synth
+    from oracle import oracle as O
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    rng = np.random.Generator(np.random.PCG64(spec.seed))
+    leads_zyx = synth.leads(spec, rng)[:, ::-1].copy()
+    at, layer = O.activation(grid, tm)
+    jobs = []
+    for i in range(threads):
+        g = genes[i % len(genes)]
+        lk, _, _ = O.layer_aps(spec.n_layers, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX,
+                               [5, 6, 7, 8], "endo-mid-epi", 0.6, g[:12])
+        moved = O.move_leads(leads_zyx, g[12:12 + 2 * spec.n_leads].reshape(-1, 2))
+        jobs.append((lk, moved))
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda j: O.run_naive(layer, at, j[0], j[1], "3D4", 0.0, float(steps), 1.0, sample_steps), jobs))
+    dt = time.perf_counter() - t0
+    per_sim = dt * steps / sample_steps
+    sims_per_s = threads / per_sim
+    sample = (f"{threads} concurrent single-thread simulations of the {spec.n}^3 heart, first {sample_steps} of "
+              f"{steps} steps each ({dt:.1f} s wall), scaled by {steps}/{sample_steps}")
+    return sims_per_s, dt, sample
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_reference(args):
+    d = Dist()
+    if d.rank != 0:
+        d.close()
+        return
+    spec, steps, batch, cfg_index, wname = make_heart_spec(args.workload)
+    from ekgsim_gb300 import synth
+    genes = np.stack([synth.genes_for(spec, r, cfg_index) for r in range(max(1, host_cores()))])
+    cores = host_cores()
+    sample_steps = max(1, int(args.ref_sample_steps))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, dt, sample = cpu_farm(spec, steps, genes, sample_steps, cores)
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.mean(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "sims/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * cores / value if value else None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": wname, "grid": spec.n, "leads": spec.n_leads, "steps": steps},
+        "cpu_baseline": {"value": value, "unit": "sims/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "sims/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    d.close()
+
+
+def run_ours(args):
+    d = Dist()
+    from ekgsim_gb300 import engine as E
+    from ekgsim_gb300 import synth
+    spec, steps, batch, cfg_index, wname = make_heart_spec(args.workload)
+    if args.batch:
+        batch = args.batch
+    grid, tm, leads_zyx, genes, target = build_inputs(spec, steps, batch, cfg_index)
+    eng = E.Engine(d.local)
+    t0 = time.perf_counter()
+    heart = E.Heart.create(eng, grid, tm, leads_zyx, "3D4", 0.0, float(steps), 1.0)
+    setup_s = time.perf_counter() - t0
+    heart.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], [t for t in target],
+                   mid_position=0.6, optimize_points=True, comparison_mode=2)
+    info = heart.info
+    # per-simulation layer APs and moved leads (host, as the evaluation does)
+    cfg = heart._cfg
+    lk = np.stack([E.layer_aps(cfg, 3, g[:12])[0] for g in genes])
+    moved = np.stack([E.move_leads(leads_zyx, g[12:].reshape(-1, 2)) for g in genes])
+
+    # device-only throughput (inputs resident)
+    for _ in range(1):
+        heart.benchmark(lk, moved, warmup=args.warmup, iters=1)
+    d.barrier()
+    clocks = ClockSampler(d.local)
+    clocks.start()
+    bm = heart.benchmark(lk, moved, warmup=0, iters=args.steps)
+    clk = clocks.stop()
+    dev_s = d.max(bm["total_ms"] / 1000.0)
+    d.barrier()
+    value = d.world * batch * args.steps / dev_s
+
+    # end to end through the public API (host buffers)
+    for _ in range(args.warmup):
+        heart.eval_batch(genes, want_ecg=True)
+    d.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        crit, viol, ecg = heart.eval_batch(genes, want_ecg=True)
+    e2e_s = d.max(time.perf_counter() - t0)
+    e2e = d.world * batch * args.steps / e2e_s
+    ng, nc = heart.eval_shape()
+    h2d = batch * (info.n_layers * 9 + info.n_leads * 3) * 8
+    d2h = batch * (info.n_leads * steps * 8 + min(info.n_leads, len(target)) * 2 * 8)
+
+    # plain form: one simulation per call, latency distribution
+    lat = []
+    for i in range(args.warmup + max(20, args.plain_calls)):
+        t1 = time.perf_counter()
+        heart.eval(genes[i % batch])
+        if i >= args.warmup:
+            lat.append(time.perf_counter() - t1)
+    lat = np.array(lat) * 1000.0
+    plain = {"sims_per_s": float(1000.0 / lat.mean()), "p50_ms": float(np.percentile(lat, 50)),
+             "p99_ms": float(np.percentile(lat, 99)), "calls": int(lat.size)}
+
+    # roofline of the contraction kernel
+    bf16, hbm, src = peaks()
+    contract_s = bm["contract_ms"] / 1000.0 / args.steps  # one launch per step
+    alg_flops = 2.0 * info.n_leads * 3 * info.n_voxels * steps * batch
+    achieved = alg_flops / contract_s / 1e12
+    mufu = 3.0 * info.n_aps * steps * batch / contract_s / 1e12
+    tr = profiled_traffic(wname)
+    roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
+            "traffic": tr * batch if tr is not None else None, "peak_source": src,
+            "kernel": "k_contract_umma", "launch_ms": contract_s * 1000.0,
+            "sfu_tops": mufu, "note": "algorithmic flops 2 x L x 3V x T per simulation"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "sims/s", "n_gpus": d.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": bm["total_ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16x3", "data": "synthetic",
+        "config": {"workload": wname, "grid": spec.n, "voxels": int(info.n_voxels), "aps": int(info.n_aps),
+                   "leads": info.n_leads, "steps": steps, "batch": batch, "layers": info.n_layers,
+                   "l2": "inputs larger than L2 (per-step lead fields and partials exceed 129 MB)",
+                   "parallelism": f"replicas{d.world}", "heart_setup_s": setup_s, "ca_rounds": info.ca_rounds},
+        "e2e": {"value": e2e, "unit": "sims/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "plain": plain,
+        "batched_over_plain": value / plain["sims_per_s"],
+        "roofline": roof,
+        "gpu_launches": int(bm["launches"]) * args.steps,
+        "clocks": clk,
+    }
+    if d.rank == 0 and not args.no_check:
+        # parity of a sample of results against the FP64 oracle, and activation-time mismatch
+        from oracle import oracle as O
+        at_ref, layer = O.activation(grid, tm)
+        at_gpu = heart.activation()
+        mism = int(np.count_nonzero(at_gpu.view(np.int64) != at_ref.view(np.int64)))
+        rels = []
+        for i in range(min(2, batch)):
+            ref = O.run(layer, at_ref, lk[i], moved[i], "3D4", 0.0, float(steps), 1.0)
+            rels.append(float(np.linalg.norm(ecg[i] - ref) / np.linalg.norm(ref)))
+        line["parity"] = {"ecg_rel_l2_max": max(rels), "checked_sims": len(rels), "at_mismatch": mism}
+    if d.rank == 0 and d.world == 1 and not args.no_cpu:
+        v, dt, sample = cpu_farm(spec, steps, genes, args.cpu_sample_steps, host_cores())
+        line["cpu_baseline"] = {"value": v, "unit": "sims/s", "cores": host_cores(), "kind": "port",
+                                "sample": sample}
+    if d.rank == 0:
+        print(json.dumps(line), flush=True)
+    heart.close()
+    eng.close()
+    d.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "single"])
+    ap.add_argument("--batch", type=int, default=0)
+    ap.add_argument("--plain-calls", type=int, default=50)
+    ap.add_argument("--cpu-sample-steps", type=int, default=16)
+    ap.add_argument("--ref-sample-steps", type=int, default=6)
+    ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

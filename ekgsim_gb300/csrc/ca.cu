@@ -1,0 +1,233 @@
+// ca.cu -- activation times of the excitation-sequence cellular automaton on the device.
+//
+// The reference runs a Dijkstra search over the 26-neighbour cube (simlib/simulator.cpp:212-286):
+// start voxels get time 1.0; a popped voxel u offers time(u) + lag to each unexcited non-empty
+// neighbour v, lag = T[L(u)][L(v)] * sqrt(|u - v|^2), each step rounded in FP64.  With positive
+// lags that search returns the unique fixed point of
+//     at(v) = min(init(v), min_u fl(at(u) + fl(T[L(u)][L(v)] * sqrt(k))))
+// (every offered time is >= the offering voxel's own time), so a chaotic min-relaxation from
+// +inf converges to the same doubles bit for bit, in any order.  Products and sums use
+// __dmul_rn / __dadd_rn so the compiler cannot fuse them into an FMA.
+//
+// Layout: the grid is cut into 8x8x8 tiles.  A round processes the active tiles, one CTA each:
+// the tile and a one-voxel halo are staged in shared memory (FP64 times + uint8 layers), the
+// tile relaxes locally until a block-wide vote (__syncthreads_or) finds no change, the changed
+// interior voxels are written back, and the neighbour tiles that touch a changed face, edge or
+// corner are flagged.  A compaction kernel turns the flags into the next round's tile list with
+// warp ballots and one atomic per warp.  The host loops until no tile is active.
+#include <cstdio>
+#include <vector>
+
+#include "ekg_internal.h"
+
+namespace ekg {
+
+namespace {
+
+constexpr int TS = 8;            // tile edge
+constexpr int HS = TS + 2;       // tile + halo
+constexpr int CA_THREADS = 256;  // 2 voxels per thread
+constexpr int MAX_LOCAL_ITERS = 64;
+
+__global__ void k_ca_round(int nz, int ny, int nx, int ntz, int nty, int ntx, const uint8_t *__restrict__ layers,
+                           const double *__restrict__ lag, int nl1, double *__restrict__ at,
+                           const int32_t *__restrict__ active, uint8_t *__restrict__ next_flag) {
+    __shared__ double s_at[HS][HS][HS];
+    __shared__ uint8_t s_l[HS][HS][HS];
+    __shared__ uint32_t s_mark;  // 27-bit mask of neighbour tiles to flag (bit = (dz+1)*9+(dy+1)*3+(dx+1))
+
+    const int tile = active[blockIdx.x];
+    const int tx0 = (tile % ntx) * TS;
+    const int ty0 = ((tile / ntx) % nty) * TS;
+    const int tz0 = (tile / (ntx * nty)) * TS;
+    const int tid = threadIdx.x;
+    if (tid == 0) s_mark = 0;
+
+    // stage tile + halo
+    for (int i = tid; i < HS * HS * HS; i += CA_THREADS) {
+        int hx = i % HS, hy = (i / HS) % HS, hz = i / (HS * HS);
+        int gx = tx0 + hx - 1, gy = ty0 + hy - 1, gz = tz0 + hz - 1;
+        double a = __longlong_as_double(0x7ff0000000000000LL);  // +inf
+        uint8_t l = 0;
+        if (gx >= 0 && gx < nx && gy >= 0 && gy < ny && gz >= 0 && gz < nz) {
+            size_t g = ((size_t)gz * ny + gy) * nx + gx;
+            l = layers[g];
+            if (l) a = at[g];
+        }
+        s_at[hz][hy][hx] = a;
+        s_l[hz][hy][hx] = l;
+    }
+    __syncthreads();
+
+    const int lx = (tid & 7) + 1, ly = ((tid >> 3) & 7) + 1, lz0 = (tid >> 6) + 1;
+    double orig[2];
+    uint8_t myl[2];
+    bool inside[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        int lz = lz0 + 4 * r;
+        orig[r] = s_at[lz][ly][lx];
+        myl[r] = s_l[lz][ly][lx];
+        inside[r] = (tx0 + lx - 1 < nx) && (ty0 + ly - 1 < ny) && (tz0 + lz - 1 < nz);
+    }
+
+    int iters = 0;
+    bool again = true;
+    while (again && iters < MAX_LOCAL_ITERS) {
+        bool changed = false;
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            if (!inside[r] || myl[r] == 0) continue;
+            const int lz = lz0 + 4 * r;
+            double best = s_at[lz][ly][lx];
+            const double *lagd = lag + (size_t)myl[r] * 3;  // lag[src][dst=myl][k]
+#pragma unroll
+            for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+                for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        if (dz == 0 && dy == 0 && dx == 0) continue;
+                        const uint8_t lu = s_l[lz + dz][ly + dy][lx + dx];
+                        if (lu == 0) continue;
+                        const double au = s_at[lz + dz][ly + dy][lx + dx];
+                        const int k = (dz != 0) + (dy != 0) + (dx != 0);
+                        const double c = __dadd_rn(au, __ldg(lagd + (size_t)lu * nl1 * 3 + (k - 1)));
+                        if (c < best) best = c;
+                    }
+            if (best < s_at[lz][ly][lx]) {
+                s_at[lz][ly][lx] = best;
+                changed = true;
+            }
+        }
+        again = __syncthreads_or(changed);
+        ++iters;
+    }
+
+    // write back and flag neighbour tiles touched by changed boundary voxels
+    uint32_t mark = 0;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int lz = lz0 + 4 * r;
+        if (!inside[r] || myl[r] == 0) continue;
+        const double v = s_at[lz][ly][lx];
+        if (v < orig[r]) {
+            size_t g = ((size_t)(tz0 + lz - 1) * ny + (ty0 + ly - 1)) * nx + (tx0 + lx - 1);
+            at[g] = v;
+            const int fz = (lz == 1) ? -1 : (lz == TS ? 1 : 0);
+            const int fy = (ly == 1) ? -1 : (ly == TS ? 1 : 0);
+            const int fx = (lx == 1) ? -1 : (lx == TS ? 1 : 0);
+            for (int a = 0; a <= (fz != 0); ++a)
+                for (int b = 0; b <= (fy != 0); ++b)
+                    for (int c = 0; c <= (fx != 0); ++c) {
+                        int dz = a ? fz : 0, dy = b ? fy : 0, dx = c ? fx : 0;
+                        if (dz || dy || dx) mark |= 1u << ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1));
+                    }
+        }
+    }
+    if (again) mark |= 1u << 13;  // local iteration cap hit: run this tile again
+    // warp-level OR, then one shared atomic per warp
+    for (int o = 16; o > 0; o >>= 1) mark |= __shfl_xor_sync(0xffffffffu, mark, o);
+    if ((tid & 31) == 0 && mark) atomicOr(&s_mark, mark);
+    __syncthreads();
+    if (tid < 27) {
+        const uint32_t m = s_mark;
+        if (m & (1u << tid)) {
+            int dz = tid / 9 - 1, dy = (tid / 3) % 3 - 1, dx = tid % 3 - 1;
+            int tzz = tz0 / TS + dz, tyy = ty0 / TS + dy, txx = tx0 / TS + dx;
+            if (tzz >= 0 && tzz < ntz && tyy >= 0 && tyy < nty && txx >= 0 && txx < ntx)
+                next_flag[((size_t)tzz * nty + tyy) * ntx + txx] = 1;
+        }
+    }
+}
+
+// next_flag -> compact list (order irrelevant); clears the flags.
+__global__ void k_ca_compact(int ntiles, uint8_t *__restrict__ flag, int32_t *__restrict__ list,
+                             int32_t *__restrict__ count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool f = (i < ntiles) && flag[i];
+    const unsigned b = __ballot_sync(0xffffffffu, f);
+    int base = 0;
+    if ((threadIdx.x & 31) == 0 && b) base = atomicAdd(count, __popc(b));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (f) {
+        list[base + __popc(b & ((1u << (threadIdx.x & 31)) - 1))] = i;
+        flag[i] = 0;
+    }
+}
+
+__global__ void k_ca_init(size_t n, const uint8_t *__restrict__ layers, const uint8_t *__restrict__ start,
+                          double *__restrict__ at) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        double v = 0.0;
+        if (layers[i]) v = start[i] ? 1.0 : __longlong_as_double(0x7ff0000000000000LL);
+        at[i] = v;
+    }
+}
+
+__global__ void k_ca_finish(size_t n, double *__restrict__ at) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        if (isinf(at[i])) at[i] = 0.0;  // unreachable voxels keep excitationDelay 0
+}
+
+}  // namespace
+
+CaResult ca_run(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_layers, const uint8_t *d_start,
+                const std::vector<int32_t> &start_tiles, int nl1, const double *d_lag, double *d_at,
+                uint32_t *d_err) {
+    (void)d_err;
+    CaResult res;
+    const int ntz = (nz + TS - 1) / TS, nty = (ny + TS - 1) / TS, ntx = (nx + TS - 1) / TS;
+    const int ntiles = ntz * nty * ntx;
+    const size_t n = (size_t)nz * ny * nx;
+    DBuf<int32_t> list_a, list_b, count;
+    DBuf<uint8_t> flag;
+    list_a.alloc(ntiles);
+    list_b.alloc(ntiles);
+    count.alloc(2);
+    flag.alloc(ntiles);
+    EKG_CUDA(cudaMemsetAsync(flag.p, 0, ntiles, s));
+    EKG_CUDA(cudaMemcpyAsync(list_a.p, start_tiles.data(), start_tiles.size() * sizeof(int32_t),
+                             cudaMemcpyHostToDevice, s));
+    cudaEvent_t e0, e1;
+    EKG_CUDA(cudaEventCreate(&e0));
+    EKG_CUDA(cudaEventCreate(&e1));
+    EKG_CUDA(cudaEventRecord(e0, s));
+    k_ca_init<<<1024, 256, 0, s>>>(n, d_layers, d_start, d_at);
+    EKG_CUDA(cudaGetLastError());
+    int n_active = (int)start_tiles.size();
+    // Every round finalises at least the next tile along each shortest path; a path can
+    // cross a tile boundary at most once per hop, so this cap is far above any real heart.
+    const int cap = 16 * (ntz + nty + ntx) + 4 * ntiles + 64;
+    int32_t *cur = list_a.p, *nxt = list_b.p;
+    int32_t *h_count = nullptr;
+    EKG_CUDA(cudaMallocHost(&h_count, sizeof(int32_t)));
+    while (n_active > 0) {
+        if (res.rounds >= cap) {
+            cudaFreeHost(h_count);
+            throw Error{EKG_ERR_CA_NOT_CONVERGED, "activation-time relaxation did not converge"};
+        }
+        k_ca_round<<<n_active, CA_THREADS, 0, s>>>(nz, ny, nx, ntz, nty, ntx, d_layers, d_lag, nl1, d_at, cur,
+                                                  flag.p);
+        EKG_CUDA(cudaGetLastError());
+        EKG_CUDA(cudaMemsetAsync(count.p, 0, sizeof(int32_t), s));
+        k_ca_compact<<<(ntiles + 255) / 256, 256, 0, s>>>(ntiles, flag.p, nxt, count.p);
+        EKG_CUDA(cudaGetLastError());
+        EKG_CUDA(cudaMemcpyAsync(h_count, count.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        EKG_CUDA(cudaStreamSynchronize(s));
+        n_active = *h_count;
+        std::swap(cur, nxt);
+        ++res.rounds;
+    }
+    cudaFreeHost(h_count);
+    k_ca_finish<<<1024, 256, 0, s>>>(n, d_at);
+    EKG_CUDA(cudaGetLastError());
+    EKG_CUDA(cudaEventRecord(e1, s));
+    EKG_CUDA(cudaEventSynchronize(e1));
+    EKG_CUDA(cudaEventElapsedTime(&res.ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return res;
+}
+
+}  // namespace ekg

@@ -1,0 +1,406 @@
+// ecg.cu -- simulated ECG of one heart: lead field, AP factors, contraction, FP64 reduction,
+// criteria.
+//
+// The reference forms, per non-empty voxel x, the dipole D_x(t) = sum_n d_n (AP(x-d_n,t) - AP(x,t))
+// and adds g_l(x) . D_x(t) to lead l, g_l(x) = (r_l - x)/|r_l - x|^3 (simlib/simulator.cpp:489-537).
+// The same sum regrouped by cell AP (the reference's apIndex, simlib/simulator.cpp:561-621) is a
+// contraction over the de-duplicated APs:
+//     ECG_l(t) = sum_a W[l,a] AP_a(t),   W[l,a] = sum_{voxels y of AP a} w_l(y),
+//     w_l(y)   = sum_{n: y+d_n non-empty} g_l(y+d_n).d_n  -  g_l(y) . sum_{n: y-d_n non-empty} d_n.
+// The Wohlfart AP (simlib/Wohlfart.h:195-203) with k8 shifted by the activation time
+// (simlib/simulator.cpp:154-170) factors, with tau = t - at, as
+//     AP_a(t) - k0 = H_a(t) * F_L(t) * exp(k5 at),
+//     H_a(t) = sigma(k1 tau) ((1-k3) exp(-k4 tau) + k3)                (per AP and step, FP32)
+//     F_L(t) = k2 exp(-k5 t) (1 - (1 + exp(-k7 (t-k8)) (2^(k7/k6) - 1))^(-k6/k7))   (per layer, FP64)
+// so the device evaluates H on the fly, folds exp(k5 at) into the lead field (W' = W exp(k5 at)),
+// and applies F_L in FP64 to each layer's partial sums.  k0 cancels inside every AP difference of
+// one layer; across layers it leaves the constant sum_L k0_L sum_{a in L} W[l,a].
+#include <cmath>
+#include <cstdio>
+
+#include "ekg_internal.h"
+
+namespace ekg {
+
+namespace {
+
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// H_a(t) in FP32; c = {k1*log2(e), k4*log2(e), 1-k3, k3}
+__device__ __forceinline__ float h_value(float tau, float4 c) {
+    const float e1 = ex2_approx(-c.x * tau);
+    const float s = rcp_approx(1.0f + e1);
+    const float e4 = ex2_approx(-c.y * tau);
+    const float h = s * fmaf(c.z, e4, c.w);
+    return s == 0.0f ? 0.0f : h;
+}
+
+// ------------------------------------------------------------------ lead field
+// One thread per (AP a, lead l, sim s).  Lead positions FP64 [S][lead_stride][3] (z,y,x);
+// W [S][w_lead_stride][apad].
+__global__ void k_lead_field(int64_t apad, const int64_t *__restrict__ a_vox_begin,
+                             const int32_t *__restrict__ vox_zyx, const uint32_t *__restrict__ nb_in,
+                             const uint32_t *__restrict__ nb_out, int nnb, const int8_t *__restrict__ difs,
+                             const double *__restrict__ leads, int nleads, int lead_stride,
+                             float *__restrict__ W, int w_lead_stride) {
+    __shared__ int8_t s_dif[26 * 3];
+    __shared__ float s_sout[3];
+    if (threadIdx.x < nnb * 3) s_dif[threadIdx.x] = difs[threadIdx.x];
+    __syncthreads();
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int l = blockIdx.y, s = blockIdx.z;
+    (void)s_sout;
+    if (a >= apad || l >= nleads) return;
+    const double *r = leads + ((size_t)s * lead_stride + l) * 3;
+    const float rz = (float)r[0], ry = (float)r[1], rx = (float)r[2];
+    const float rzl = (float)(r[0] - (double)rz), ryl = (float)(r[1] - (double)ry), rxl = (float)(r[2] - (double)rx);
+    double acc = 0.0;
+    const int64_t v0 = a_vox_begin[a], v1 = a_vox_begin[a + 1];
+    for (int64_t v = v0; v < v1; ++v) {
+        const int32_t p = vox_zyx[v];
+        // bordered coordinates (simlib/simulator.cpp:458-463, 487)
+        const float pz = (float)((p >> 20) + 1), py = (float)(((p >> 10) & 1023) + 1), px = (float)((p & 1023) + 1);
+        const uint32_t mi = nb_in[v], mo = nb_out[v];
+        float w = 0.f;
+        float sz = 0.f, sy = 0.f, sx = 0.f;
+        for (int n = 0; n < nnb; ++n) {
+            const float dz = s_dif[3 * n], dy = s_dif[3 * n + 1], dx = s_dif[3 * n + 2];
+            if (mi & (1u << n)) {
+                const float mz = (rz - (pz + dz)) + rzl, my = (ry - (py + dy)) + ryl, mx = (rx - (px + dx)) + rxl;
+                const float ss = fmaf(mz, mz, fmaf(my, my, mx * mx));
+                const float rs = rsqrtf(ss);
+                const float f = rs * rs * rs;
+                w = fmaf(f, fmaf(mz, dz, fmaf(my, dy, mx * dx)), w);
+            }
+            if (mo & (1u << n)) {
+                sz += dz;
+                sy += dy;
+                sx += dx;
+            }
+        }
+        if (mo) {
+            const float mz = (rz - pz) + rzl, my = (ry - py) + ryl, mx = (rx - px) + rxl;
+            const float ss = fmaf(mz, mz, fmaf(my, my, mx * mx));
+            const float rs = rsqrtf(ss);
+            const float f = rs * rs * rs;
+            w = fmaf(-f, fmaf(mz, sz, fmaf(my, sy, mx * sx)), w);
+        }
+        acc += (double)w;
+    }
+    W[((size_t)s * w_lead_stride + l) * apad + a] = (float)acc;
+}
+
+// ------------------------------------------------------------------ per-layer factors
+// One thread per (sim, layer, step).  layer_k: [S][nl][9].
+__global__ void k_layer_factors(int nl, int steps, const double *__restrict__ t, const double *__restrict__ layer_k,
+                                int n_sims, double *__restrict__ F, float *__restrict__ layer_c) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)n_sims * nl * steps;
+    if (i >= total) return;
+    const int step = (int)(i % steps);
+    const int64_t sl = i / steps;  // sim * nl + layer
+    const double *k = layer_k + sl * 9;
+    const double tt = t[step];
+    const double R = 1 - pow((1 + exp(-k[7] * (tt - k[8]) + log(pow(2.0, (k[7] / k[6])) - 1))), -(k[6] / k[7]));
+    F[i] = k[2] * exp(-k[5] * tt) * R;
+    if (step == 0) {
+        const double L2E = 1.4426950408889634;
+        float4 c = make_float4((float)(k[1] * L2E), (float)(k[4] * L2E), (float)(1.0 - k[3]), (float)k[3]);
+        reinterpret_cast<float4 *>(layer_c)[sl] = c;
+    }
+}
+
+// W' = W * exp(k5_L(a) at_a); one thread per (a, sim), looping leads.
+__global__ void k_scale_w(int64_t apad, int nleads, const float *__restrict__ W, const double *__restrict__ at,
+                          const int32_t *__restrict__ a_layer, const double *__restrict__ layer_k, int nl,
+                          int n_sims, float *__restrict__ Wp) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int s = blockIdx.y;
+    if (a >= apad) return;
+    const double aa = at[a];
+    float f = 0.f;
+    if (!isinf(aa)) f = expf((float)(layer_k[((size_t)s * nl + a_layer[a]) * 9 + 5] * aa));
+    for (int l = 0; l < nleads; ++l) {
+        const size_t o = ((size_t)s * nleads + l) * apad + a;
+        Wp[o] = W[o] * f;
+    }
+}
+
+// k0 term: k0w[s][l] = sum_L k0_L sum_{a in L} W[s][l][a]; one block per (l, s).
+__global__ void k_k0_term(int64_t apad, int nleads, const float *__restrict__ W, const int32_t *__restrict__ a_layer,
+                          const double *__restrict__ layer_k, int nl, double *__restrict__ k0w) {
+    const int l = blockIdx.x, s = blockIdx.y;
+    __shared__ double red[256];
+    double acc = 0.0;
+    const float *w = W + ((size_t)s * nleads + l) * apad;
+    for (int64_t a = threadIdx.x; a < apad; a += blockDim.x)
+        acc += layer_k[((size_t)s * nl + a_layer[a]) * 9 + 0] * (double)w[a];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) k0w[(size_t)s * nleads + l] = red[0];
+}
+
+// ------------------------------------------------------------------ contraction (CUDA cores)
+// grid (t tiles of 128, K chunks, sims * lead blocks of 16); block 128 threads, one step each.
+constexpr int CC_T = 128, CC_LB = 16, CC_STAGE = 256;
+__global__ void __launch_bounds__(CC_T) k_contract_cuda(int steps, int nleads, int64_t apad, int nl,
+                                                        const float2 *__restrict__ t_hilo,
+                                                        const float2 *__restrict__ at_hilo,
+                                                        const int32_t *__restrict__ chunk_a0,
+                                                        const int32_t *__restrict__ chunk_a1,
+                                                        const int32_t *__restrict__ chunk_layer,
+                                                        const float *__restrict__ Wp, const float *__restrict__ layer_c,
+                                                        const double *__restrict__ F, int nchunks, int nlb,
+                                                        double *__restrict__ partial) {
+    __shared__ float s_w[CC_LB][CC_STAGE];
+    __shared__ float2 s_at[CC_STAGE];
+    const int c = blockIdx.y;
+    const int s = blockIdx.z / nlb, lb = blockIdx.z % nlb;
+    const int t = blockIdx.x * CC_T + threadIdx.x;
+    const int a0 = chunk_a0[c], a1 = chunk_a1[c], L = chunk_layer[c];
+    const float4 kc = reinterpret_cast<const float4 *>(layer_c)[(size_t)s * nl + L];
+    const float2 th = t_hilo[t < steps ? t : steps - 1];
+    const int l0 = lb * CC_LB;
+    const int nlh = min(CC_LB, nleads - l0);
+    float acc[CC_LB];
+#pragma unroll
+    for (int j = 0; j < CC_LB; ++j) acc[j] = 0.f;
+    for (int b = a0; b < a1; b += CC_STAGE) {
+        const int nb = min(CC_STAGE, a1 - b);
+        __syncthreads();
+        for (int i = threadIdx.x; i < CC_STAGE; i += CC_T) {
+            s_at[i] = i < nb ? at_hilo[b + i] : make_float2(INFINITY, 0.f);
+            for (int j = 0; j < CC_LB; ++j)
+                s_w[j][i] = (i < nb && j < nlh) ? Wp[((size_t)s * nleads + l0 + j) * apad + b + i] : 0.f;
+        }
+        __syncthreads();
+        for (int i = 0; i < nb; ++i) {
+            const float2 at = s_at[i];
+            const float tau = (th.x - at.x) + (th.y - at.y);
+            const float h = h_value(tau, kc);
+#pragma unroll
+            for (int j = 0; j < CC_LB; ++j) acc[j] = fmaf(s_w[j][i], h, acc[j]);
+        }
+    }
+    if (t < steps) {
+        const double f = F[((size_t)s * nl + L) * steps + t];
+        for (int j = 0; j < nlh; ++j)
+            partial[(((size_t)s * nchunks + c) * nleads + l0 + j) * steps + t] = (double)acc[j] * f;
+    }
+}
+
+// ecg[s][l][t] = k0w[s][l] + sum_c partial[s][c][l][t]   (fixed order over c)
+__global__ void k_reduce_ecg(int steps, int nleads, int nchunks, const double *__restrict__ partial,
+                             const double *__restrict__ k0w, int n_sims, double *__restrict__ ecg) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)n_sims * nleads * steps;
+    if (i >= total) return;
+    const int t = (int)(i % steps);
+    const int64_t sl = i / steps;
+    const int s = (int)(sl / nleads), l = (int)(sl % nleads);
+    double acc = k0w[sl];
+    for (int c = 0; c < nchunks; ++c) acc += partial[(((size_t)s * nchunks + c) * nleads + l) * steps + t];
+    ecg[i] = acc;
+}
+
+// ------------------------------------------------------------------ criteria (FP64)
+// One block (256 threads) per (sim, criterion lead).  Output per (s, i): value and argmax.
+template <int NT>
+__device__ double block_sum(double v, double *red) {
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = NT / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    const double r = red[0];
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_criteria(int steps, int nleads, int ncl, int mode, const double *__restrict__ ecg,
+                           const double *__restrict__ targets, const int64_t *__restrict__ tlen,
+                           const double *__restrict__ toff, int crit_stride, double *__restrict__ crit) {
+    constexpr int NT = 256;
+    __shared__ double red[NT];
+    __shared__ double s_min[NT], s_max[NT];
+    __shared__ int s_arg[NT];
+    const int i = blockIdx.x, s = blockIdx.y;
+    const double *a = ecg + ((size_t)s * nleads + i) * steps;
+    int64_t off = 0;
+    for (int j = 0; j < i; ++j) off += tlen[j];
+    const double *b = targets + off;
+    const int64_t nb = tlen[i];
+    const int64_t len = steps < nb ? steps : nb;
+    double value = 0.0;
+    if (mode == 2) {
+        double sa = 0, sb = 0;
+        for (int64_t j = threadIdx.x; j < len; j += NT) {
+            sa += a[j];
+            sb += b[j];
+        }
+        const double inv = 1.0 / (double)len;
+        const double ma = block_sum<NT>(sa, red) * inv, mb = block_sum<NT>(sb, red) * inv;
+        double va = 0, vb = 0, cv = 0;
+        for (int64_t j = threadIdx.x; j < len; j += NT) {
+            const double x = a[j] - ma, y = b[j] - mb;
+            va += x * x;
+            vb += y * y;
+            cv += x * y;
+        }
+        va = block_sum<NT>(va, red) * inv;
+        vb = block_sum<NT>(vb, red) * inv;
+        cv = block_sum<NT>(cv, red) / (double)len;
+        value = 1.0 - cv / (sqrt(va) * sqrt(vb));
+    } else if (mode == 4) {
+        double ab = 0, aa = 0, bb = 0;
+        for (int64_t j = threadIdx.x; j < len; j += NT) {
+            ab += a[j] * b[j];
+            aa += a[j] * a[j];
+            bb += b[j] * b[j];
+        }
+        ab = block_sum<NT>(ab, red);
+        aa = block_sum<NT>(aa, red);
+        bb = block_sum<NT>(bb, red);
+        value = 1.0 - ab / (sqrt(aa) * sqrt(bb));
+    } else if (mode == 1) {
+        double q = 0;
+        for (int64_t j = threadIdx.x; j < len; j += NT) {
+            const double x = a[j] - b[j];
+            q += x * x;
+        }
+        value = sqrt(block_sum<NT>(q, red) / (double)len);
+    } else {
+        // devFromLinear (vectorMath.h:373-404): min/max over the whole simulated lead
+        double mn = INFINITY, mx = -INFINITY;
+        for (int64_t j = threadIdx.x; j < steps; j += NT) {
+            mn = fmin(mn, a[j]);
+            mx = fmax(mx, a[j]);
+        }
+        s_min[threadIdx.x] = mn;
+        s_max[threadIdx.x] = mx;
+        __syncthreads();
+        for (int o = NT / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) {
+                s_min[threadIdx.x] = fmin(s_min[threadIdx.x], s_min[threadIdx.x + o]);
+                s_max[threadIdx.x] = fmax(s_max[threadIdx.x], s_max[threadIdx.x + o]);
+            }
+            __syncthreads();
+        }
+        const double amult = 1.0 / (s_max[0] - s_min[0]);
+        const double bofs = toff[i];
+        double sd = 0;
+        for (int64_t j = threadIdx.x; j < len; j += NT) sd += (a[j] * amult + bofs) / (b[j] + bofs);
+        const double inv = 1.0 / (double)len;
+        const double mean = block_sum<NT>(sd, red) * inv;
+        double var = 0;
+        for (int64_t j = threadIdx.x; j < len; j += NT) {
+            const double d = (a[j] * amult + bofs) / (b[j] + bofs) - mean;
+            var += d * d;
+        }
+        var = block_sum<NT>(var, red) * inv;
+        value = (var == 0) ? 1.0 / 1e-30 : sqrt(var);
+    }
+    // argmax of the simulated lead (first maximum), for the peak-position criterion
+    double best = -INFINITY;
+    int arg = 0x7fffffff;
+    for (int j = threadIdx.x; j < steps; j += NT)
+        if (a[j] > best) {
+            best = a[j];
+            arg = j;
+        }
+    s_max[threadIdx.x] = best;
+    s_arg[threadIdx.x] = arg;
+    __syncthreads();
+    for (int o = NT / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            const double v2 = s_max[threadIdx.x + o];
+            const int a2 = s_arg[threadIdx.x + o];
+            if (v2 > s_max[threadIdx.x] || (v2 == s_max[threadIdx.x] && a2 < s_arg[threadIdx.x])) {
+                s_max[threadIdx.x] = v2;
+                s_arg[threadIdx.x] = a2;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        crit[((size_t)s * crit_stride + i) * 2 + 0] = value;
+        crit[((size_t)s * crit_stride + i) * 2 + 1] = (double)s_arg[0];
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+void launch_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads, int nleads_in, int lead_stride,
+                       int n_sims, float *d_W, int w_lead_stride) {
+    dim3 grid((unsigned)((h.apad + 127) / 128), (unsigned)nleads_in, (unsigned)n_sims);
+    k_lead_field<<<grid, 128, 0, s>>>(h.apad, h.a_vox_begin.p, h.vox_zyx.p, h.vox_nb.p, h.vox_nbo.p, h.nnb,
+                                      h.difs.p, d_leads, nleads_in, lead_stride, d_W, w_lead_stride);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_layer_k, int n_sims, double *d_F,
+                          float *d_layer_c) {
+    const int64_t total = (int64_t)n_sims * h.nlayers * h.steps;
+    k_layer_factors<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(h.nlayers, h.steps, h.t.p, d_layer_k, n_sims,
+                                                                   d_F, d_layer_c);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_scale_w(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
+                    float *d_Wp) {
+    dim3 grid((unsigned)((h.apad + 255) / 256), (unsigned)n_sims);
+    k_scale_w<<<grid, 256, 0, s>>>(h.apad, h.nleads, d_W, h.at.p, h.a_layer.p, d_layer_k, h.nlayers, n_sims, d_Wp);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_k0_term(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
+                    double *d_k0w) {
+    dim3 grid((unsigned)h.nleads, (unsigned)n_sims);
+    k_k0_term<<<grid, 256, 0, s>>>(h.apad, h.nleads, d_W, h.a_layer.p, d_layer_k, h.nlayers, d_k0w);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_contract_cuda(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,
+                          const double *d_F, int n_sims, double *d_partial) {
+    const int nlb = (h.nleads + CC_LB - 1) / CC_LB;
+    dim3 grid((unsigned)((h.steps + CC_T - 1) / CC_T), (unsigned)h.nchunks, (unsigned)(n_sims * nlb));
+    k_contract_cuda<<<grid, CC_T, 0, s>>>(h.steps, h.nleads, h.apad, h.nlayers, h.t_hilo.p, h.at_hilo.p,
+                                          h.chunk_a0.p, h.chunk_a1.p, h.chunk_layer.p, d_Wp, d_layer_c, d_F,
+                                          h.nchunks, nlb, d_partial);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_reduce_ecg(cudaStream_t s, const HeartDev &h, const double *d_partial, const double *d_k0w,
+                       int n_sims, double *d_ecg) {
+    const int64_t total = (int64_t)n_sims * h.nleads * h.steps;
+    k_reduce_ecg<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(h.steps, h.nleads, h.nchunks, d_partial, d_k0w,
+                                                                n_sims, d_ecg);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_criteria(cudaStream_t s, const HeartDev &h, const double *d_ecg, int n_sims, int ncrit_stride,
+                     int n_crit_leads, int mode, const double *d_targets, const int64_t *d_tlen,
+                     const double *d_toff, double *d_crit) {
+    if (n_crit_leads <= 0) return;
+    dim3 grid((unsigned)n_crit_leads, (unsigned)n_sims);
+    k_criteria<<<grid, 256, 0, s>>>(h.steps, h.nleads, n_crit_leads, mode, d_ecg, d_targets, d_tlen, d_toff,
+                                    ncrit_stride, d_crit);
+    EKG_CUDA(cudaGetLastError());
+}
+
+}  // namespace ekg

@@ -1,0 +1,57 @@
+// Engine and heart objects behind the C ABI.
+#pragma once
+
+#include <functional>
+
+#include "ekg_internal.h"
+#include "host_model.h"
+
+struct ekg_engine {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int chunk_len = 512;  // APs per K chunk of the contraction (multiple of 64)
+    bool umma = true;     // tensor-core contraction (EKG_CONTRACT=cuda selects the CUDA-core kernel)
+};
+
+namespace ekg {
+struct EvalSettings {
+    GeneModel gm;
+    bool optimize_points = false, peak = false, fast_is_crit = false;
+    int criteria_mode = 1, comparison_mode = 2;
+    double fast_delay = 0, fast_limit = 2, endo_epi_delay = -1;
+    std::vector<std::vector<double>> targets;
+    std::vector<double> target_offsets;
+    std::vector<int> target_peak;
+    std::vector<double> disp_min_v, disp_max_v;
+    int n_crit_leads = 0, n_criteria = 0, n_genes = 0;
+};
+int guard(const std::function<void()> &f);
+}  // namespace ekg
+
+struct ekg_heart {
+    ekg_engine *eng = nullptr;
+    cudaStream_t stream = nullptr;    // this heart's device passes run here
+    uint32_t *err_host = nullptr;     // pinned copy of the kernels' error word
+    ~ekg_heart() {
+        if (stream) cudaStreamDestroy(stream);
+        if (err_host) cudaFreeHost(err_host);
+    }
+    std::mutex mu;
+    int nz = 0, ny = 0, nx = 0, nhood = 0;
+    int64_t ncell = 0, nvox = 0, naps = 0;
+    double start = 0, length = 0, dt = 1;
+    int ca_rounds = 0;
+    double ca_ms = 0, setup_ms = 0;
+    std::vector<double> t;            // time axis
+    std::vector<double> leads0;       // loaded lead positions (z,y,x)
+    std::vector<double> at_host;      // activation time per cell
+    std::vector<int64_t> ap_index_ref;
+    ekg::HeartDev dev;
+    ekg::EvalDev ev;
+    ekg::DBuf<double> at_cells;       // device activation times per cell
+    ekg::DBuf<double> leads0_dev;
+    ekg::DBuf<float> W0;              // [L][apad] lead field at the loaded positions
+    ekg::EvalSettings es;
+    bool has_eval = false;
+    ekg::SimConfig cfg;
+};

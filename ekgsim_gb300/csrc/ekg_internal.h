@@ -1,0 +1,146 @@
+// Internal declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/ekgsim.h"
+
+namespace ekg {
+
+// ------------------------------------------------------------------ errors
+void set_error(const std::string &msg);
+struct Error {
+    int code;
+    std::string msg;
+};
+#define EKG_CUDA(call)                                                                      \
+    do {                                                                                    \
+        cudaError_t err_ = (call);                                                          \
+        if (err_ != cudaSuccess)                                                            \
+            throw ::ekg::Error{EKG_ERR_DEVICE, std::string(#call) + ": " + cudaGetErrorString(err_)}; \
+    } while (0)
+#define EKG_CHECK(cond, code, msg)                                                          \
+    do {                                                                                    \
+        if (!(cond)) throw ::ekg::Error{(code), (msg)};                                     \
+    } while (0)
+
+// Kernel error word bits (written by bounded device waits, read by the host after a pass).
+enum : uint32_t { KERR_MBAR_TIMEOUT = 1u, KERR_TMEM = 2u };
+
+// device buffer owning helper
+template <class T>
+struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count) {
+        if (count == n && p) return;
+        release();
+        if (count == 0) return;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+            throw Error{EKG_ERR_OUT_OF_MEMORY, std::string("cudaMalloc failed: ") + cudaGetErrorString(e)};
+        }
+        n = count;
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+// ------------------------------------------------------------------ CA (ca.cu)
+struct CaResult {
+    int rounds = 0;
+    float ms = 0.f;
+};
+// layers_u8: stripped layer per cell; start flags in `is_start`; lag: [nl1][nl1][3] FP64 with
+// lag[s][d][k-1] = T[s][d] * sqrt(k).  at_out: FP64 per cell (0 for empty / unreachable).
+CaResult ca_run(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_layers, const uint8_t *d_start,
+                const std::vector<int32_t> &start_tiles, int nl1, const double *d_lag, double *d_at,
+                uint32_t *d_err);
+
+// ------------------------------------------------------------------ ECG kernels (ecg.cu)
+// Heart-resident device arrays used by the simulation kernels.
+struct HeartDev {
+    int nz = 0, ny = 0, nx = 0;
+    int64_t nvox = 0, naps = 0, apad = 0;  // apad: A rounded to a multiple of 64 per layer (K tiles)
+    int nlayers = 0, nleads = 0, steps = 0, nhood = 0;
+    int nchunks = 0;                        // K chunks (each inside one layer)
+    // per-AP (ordered by (layer, at), padded per layer to a multiple of 64)
+    DBuf<float2> at_hilo;   // [apad] activation time split hi+lo (pad: +inf -> H = 0)
+    DBuf<double> at;        // [apad]
+    DBuf<int32_t> a_layer;  // [apad] layer index 0-based (pad: layer of its chunk)
+    DBuf<int64_t> a_vox_begin;  // [apad + 1] voxel ranges (voxels sorted by AP)
+    // per voxel (sorted by AP)
+    DBuf<int32_t> vox_zyx;  // [nvox] packed z<<20 | y<<10 | x  (each < 1024)
+    DBuf<uint32_t> vox_nb;  // [nvox] bits 0..25: in-neighbour mask, (unused high bits)
+    DBuf<uint32_t> vox_nbo; // [nvox] out-neighbour mask
+    // K chunks
+    DBuf<int32_t> chunk_a0, chunk_a1, chunk_layer;  // [nchunks]
+    // neighbourhood offsets (z,y,x) as int8 triples
+    int nnb = 0;
+    int8_t nb_dif[26 * 3];
+    DBuf<int8_t> difs;      // [nnb*3] device copy of nb_dif
+    // time axis
+    DBuf<double> t;         // [steps]
+    DBuf<float2> t_hilo;    // [steps]
+};
+
+// Per-evaluation scratch (sized for n_sims simulations).
+struct EvalDev {
+    int cap_sims = 0;
+    DBuf<double> layer_k;   // [S][nl][9]
+    DBuf<double> leads;     // [S][L][3]
+    DBuf<float> layer_c;    // [S][nl][4]: k1*log2e, k4*log2e, 1-k3, k3 (FP32 H constants)
+    DBuf<double> F;         // [S][nl][steps]
+    DBuf<double> k0w;       // [S][L] constant k0 term
+    DBuf<float> W;          // [S][L][apad] lead field for this eval's positions
+    DBuf<float> Wp;         // [S][L][apad] W * exp(k5 at)
+    DBuf<double> partial;   // [S][nchunks][L][steps]
+    DBuf<double> ecg;       // [S][L][steps]
+    DBuf<double> crit;      // [S][ncrit]
+    DBuf<double> targets;   // concatenated targets
+    DBuf<int64_t> target_len;
+    DBuf<double> target_off;
+    DBuf<uint32_t> err;     // [1]
+};
+
+void launch_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads, int nleads_in, int lead_stride,
+                       int n_sims, float *d_W, int w_lead_stride);
+void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_layer_k, int n_sims, double *d_F,
+                          float *d_layer_c);
+void launch_scale_w(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
+                    float *d_Wp);
+void launch_k0_term(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
+                    double *d_k0w);
+void launch_contract_cuda(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,
+                          const double *d_F, int n_sims, double *d_partial);
+void launch_contract_umma(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,
+                          const double *d_F, int n_sims, double *d_partial, uint32_t *d_err);
+void launch_reduce_ecg(cudaStream_t s, const HeartDev &h, const double *d_partial, const double *d_k0w,
+                       int n_sims, double *d_ecg);
+void launch_criteria(cudaStream_t s, const HeartDev &h, const double *d_ecg, int n_sims, int ncrit_stride,
+                     int n_crit_leads, int mode, const double *d_targets, const int64_t *d_tlen,
+                     const double *d_toff, double *d_crit);
+
+}  // namespace ekg

@@ -1,0 +1,974 @@
+// engine.cpp -- C ABI of the engine: engine and heart lifetime, plain and batched evaluation,
+// simulator.ini front end.
+#include <algorithm>
+#include <chrono>
+#include <cstdlib>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <numeric>
+#include <sstream>
+#include <stdexcept>
+
+#include "ekg_engine.h"
+
+namespace ekg {
+
+static thread_local std::string g_last_error;
+void set_error(const std::string &m) { g_last_error = m; }
+
+int guard(const std::function<void()> &f) {
+    try {
+        f();
+        g_last_error.clear();
+        return EKG_OK;
+    } catch (const Error &e) {
+        set_error(e.msg);
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        set_error("host allocation failed");
+        return EKG_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return EKG_ERR_BAD_INPUT;
+    }
+}
+
+// neighbour offsets (z,y,x) in the reference's creation order (simlib/simulator.h:334-384)
+int neighbourhood(int code, int8_t *dif) {
+    int cnt = 0;
+    for (int a0 = 0; a0 < 3; ++a0)
+        for (int a1 = 0; a1 < 3; ++a1)
+            for (int a2 = 0; a2 < 3; ++a2) {
+                const int d0 = std::abs(a0 - 1), d1 = std::abs(a1 - 1), d2 = std::abs(a2 - 1);
+                bool ok = false;
+                if (code == EKG_NHOOD_3D4) ok = std::min({d0, d1, d2}) == 1 && std::max({d0, d1, d2}) == 1;
+                else if (code == EKG_NHOOD_CUBE) ok = std::max({d0, d1, d2}) == 1;
+                else if (code == EKG_NHOOD_2D4) ok = std::min(d1, d2) == 1 && std::max(d1, d2) == 1 && d0 == 0;
+                else if (code == EKG_NHOOD_2D8) ok = std::max(d1, d2) == 1 && d0 == 0;
+                if (ok) {
+                    dif[3 * cnt] = (int8_t)(a0 - 1);
+                    dif[3 * cnt + 1] = (int8_t)(a1 - 1);
+                    dif[3 * cnt + 2] = (int8_t)(a2 - 1);
+                    ++cnt;
+                }
+            }
+    return cnt;
+}
+
+// ------------------------------------------------------------------ heart setup
+void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
+    auto t0 = std::chrono::steady_clock::now();
+    EKG_CHECK(d && d->layers && d->transfer && d->leads_zyx, EKG_ERR_BAD_INPUT, "null heart description field");
+    EKG_CHECK(d->nz >= 1 && d->ny >= 1 && d->nx >= 1 && d->nz < 1024 && d->ny < 1024 && d->nx < 1024,
+              EKG_ERR_BAD_INPUT, "grid extents must be in 1..1023");
+    EKG_CHECK(d->n_leads >= 1 && d->n_leads <= 1024, EKG_ERR_BAD_INPUT, "n_leads must be in 1..1024");
+    EKG_CHECK(d->dt > 0 && d->length > 0, EKG_ERR_BAD_INPUT, "time step and length must be positive");
+    h->nz = d->nz;
+    h->ny = d->ny;
+    h->nx = d->nx;
+    const int64_t n = (int64_t)d->nz * d->ny * d->nx;
+    h->ncell = n;
+    h->start = d->start;
+    h->length = d->length;
+    h->dt = d->dt;
+    h->nhood = d->nhood;
+    h->leads0.assign(d->leads_zyx, d->leads_zyx + 3 * d->n_leads);
+    HeartDev &D = h->dev;
+    D.nz = d->nz;
+    D.ny = d->ny;
+    D.nx = d->nx;
+    D.nleads = d->n_leads;
+    D.nnb = neighbourhood(d->nhood, D.nb_dif);
+    EKG_CHECK(D.nnb > 0, EKG_ERR_BAD_INPUT, "unknown neighbourhood (only know of these: 2D4, 3D4, 2D8, 3D8 (cube))");
+
+    // time axis: simTime accumulated by += dt from start (simlib/simulator.cpp:496-500, 519)
+    const int64_t steps = (int64_t)std::ceil(d->length / d->dt);
+    {
+        int64_t cnt = 0;
+        const double total = d->length + d->start;
+        for (double s = d->start; s < total; s += d->dt) ++cnt;
+        EKG_CHECK(cnt == steps && steps > 0 && steps < (1 << 24), EKG_ERR_BAD_INPUT,
+                  "time step does not divide the simulation length into ceil(length/dt) steps");
+    }
+    D.steps = (int)steps;
+    h->t.resize(steps);
+    {
+        double s = d->start;
+        for (int64_t i = 0; i < steps; ++i) {
+            h->t[i] = s;
+            s += d->dt;
+        }
+    }
+
+    // layers, stimulus, validation
+    std::vector<uint8_t> lay(n), st(n);
+    int nl = 0;
+    int64_t nstart = 0;
+    std::vector<char> present(256, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        int32_t v = d->layers[i];
+        int32_t a = v < 0 ? -v : v;
+        EKG_CHECK(a <= 254, EKG_ERR_BAD_INPUT, "layer ids must be at most 254");
+        lay[i] = (uint8_t)a;
+        st[i] = v < 0;
+        nstart += v < 0;
+        nl = std::max(nl, a);
+        present[a] = 1;
+    }
+    EKG_CHECK(nstart > 0, EKG_ERR_NO_START, "Could not find starting point for excitation sequence");
+    EKG_CHECK(nl >= 1, EKG_ERR_BAD_INPUT, "model has no non-empty voxel");
+    D.nlayers = nl;
+    const int nt = d->n_transfer;
+    for (int a = 1; a <= nl; ++a)
+        if (present[a] && a >= nt)
+            throw Error{EKG_ERR_TRANSFER, "transfer (conduction) matrix does not define layer " + std::to_string(a)};
+    for (int s = 1; s <= nl; ++s)
+        for (int t = 1; t <= nl; ++t)
+            if (present[s] && present[t]) {
+                const double v = d->transfer[(size_t)s * nt + t];
+                EKG_CHECK(v >= 0 && std::isfinite(v), EKG_ERR_BAD_INPUT,
+                          "conduction delays between present layers must be finite and non-negative");
+            }
+    const int nl1 = nl + 1;
+    std::vector<double> lag((size_t)nl1 * nl1 * 3, 0.0);
+    for (int s = 1; s <= nl; ++s)
+        for (int t = 1; t <= nl; ++t)
+            for (int k = 1; k <= 3; ++k) {
+                double l = d->transfer[(size_t)s * nt + t];
+                l *= std::sqrt((double)k);  // simlib/simulator.cpp:239-240
+                lag[((size_t)s * nl1 + t) * 3 + (k - 1)] = l;
+            }
+    std::vector<int32_t> start_tiles;
+    {
+        const int ntx = (d->nx + 7) / 8, nty = (d->ny + 7) / 8;
+        std::vector<char> seen((size_t)ntx * nty * ((d->nz + 7) / 8), 0);
+        for (int64_t i = 0; i < n; ++i)
+            if (st[i]) {
+                const int64_t z = i / ((int64_t)d->ny * d->nx), y = (i / d->nx) % d->ny, x = i % d->nx;
+                const int64_t tile = ((z / 8) * nty + (y / 8)) * ntx + (x / 8);
+                if (!seen[tile]) {
+                    seen[tile] = 1;
+                    start_tiles.push_back((int32_t)tile);
+                }
+            }
+    }
+
+    // activation times on the device
+    EKG_CUDA(cudaSetDevice(h->eng->device));
+    if (!h->stream) EKG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    if (!h->err_host) EKG_CUDA(cudaMallocHost(&h->err_host, sizeof(uint32_t)));
+    cudaStream_t s = h->stream;
+    {
+        DBuf<uint8_t> dl, ds;
+        DBuf<double> dlag;
+        dl.alloc(n);
+        ds.alloc(n);
+        dlag.alloc(lag.size());
+        h->at_cells.alloc(n);
+        EKG_CUDA(cudaMemcpyAsync(dl.p, lay.data(), n, cudaMemcpyHostToDevice, s));
+        EKG_CUDA(cudaMemcpyAsync(ds.p, st.data(), n, cudaMemcpyHostToDevice, s));
+        EKG_CUDA(cudaMemcpyAsync(dlag.p, lag.data(), lag.size() * 8, cudaMemcpyHostToDevice, s));
+        CaResult r = ca_run(s, d->nz, d->ny, d->nx, dl.p, ds.p, start_tiles, nl1, dlag.p, h->at_cells.p, nullptr);
+        h->ca_rounds = r.rounds;
+        h->ca_ms = r.ms;
+        h->at_host.resize(n);
+        EKG_CUDA(cudaMemcpyAsync(h->at_host.data(), h->at_cells.p, n * 8, cudaMemcpyDeviceToHost, s));
+        EKG_CUDA(cudaStreamSynchronize(s));
+    }
+
+    // de-duplicate (layer, at) pairs: sorted by (layer, at); the reference numbers them by first
+    // appearance in raster order (simlib/simulator.cpp:570-590), kept for ekg_heart_ap_index
+    std::vector<int64_t> vox;
+    vox.reserve(n / 4);
+    for (int64_t i = 0; i < n; ++i)
+        if (lay[i]) vox.push_back(i);
+    const int64_t nv = (int64_t)vox.size();
+    h->nvox = nv;
+    D.nvox = nv;
+    std::vector<int64_t> ord(vox);
+    std::sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) {
+        if (lay[a] != lay[b]) return lay[a] < lay[b];
+        if (h->at_host[a] != h->at_host[b]) return h->at_host[a] < h->at_host[b];
+        return a < b;
+    });
+    // groups
+    std::vector<int64_t> gstart;  // index into ord
+    for (int64_t i = 0; i < nv; ++i)
+        if (i == 0 || lay[ord[i]] != lay[ord[i - 1]] || h->at_host[ord[i]] != h->at_host[ord[i - 1]]) gstart.push_back(i);
+    const int64_t na = (int64_t)gstart.size();
+    h->naps = na;
+    D.naps = na;
+    gstart.push_back(nv);
+    // reference numbering
+    {
+        std::vector<int64_t> g_of_cell(n, -1);
+        for (int64_t g = 0; g < na; ++g)
+            for (int64_t i = gstart[g]; i < gstart[g + 1]; ++i) g_of_cell[ord[i]] = g;
+        std::vector<int64_t> g2ref(na, -1);
+        int64_t next = 0;
+        h->ap_index_ref.assign(n, -1);
+        for (int64_t i = 0; i < n; ++i) {
+            const int64_t g = g_of_cell[i];
+            if (g < 0) continue;
+            if (g2ref[g] < 0) g2ref[g] = next++;
+            h->ap_index_ref[i] = g2ref[g];
+        }
+    }
+    // padded per-layer K layout, tiles of KT APs, chunks of up to chunk_len APs inside one layer
+    const int KT = 64;
+    const int chunk_len = h->eng->chunk_len;
+    std::vector<double> a_at;
+    std::vector<float2> a_hilo;
+    std::vector<int32_t> a_layer;
+    std::vector<int64_t> a_vb;
+    std::vector<int32_t> c0, c1, cl;
+    std::vector<int32_t> vzyx(nv);
+    std::vector<uint32_t> vin(nv), vout(nv);
+    int64_t vpos = 0;
+    {
+        int64_t g = 0;
+        for (int L = 1; L <= nl; ++L) {
+            const int64_t gb = g;
+            while (g < na && lay[ord[gstart[g]]] == L) ++g;
+            const int64_t cnt = g - gb;
+            if (cnt == 0) continue;
+            const int64_t base = (int64_t)a_at.size();
+            const int64_t padded = (cnt + KT - 1) / KT * KT;
+            for (int64_t j = 0; j < padded; ++j) {
+                a_layer.push_back(L - 1);
+                a_vb.push_back(vpos);
+                if (j < cnt) {
+                    const int64_t gg = gb + j;
+                    const double at = h->at_host[ord[gstart[gg]]];
+                    a_at.push_back(at);
+                    const float hi = (float)at;
+                    a_hilo.push_back(make_float2(hi, (float)(at - (double)hi)));
+                    for (int64_t i = gstart[gg]; i < gstart[gg + 1]; ++i) {
+                        const int64_t c = ord[i];
+                        const int z = (int)(c / ((int64_t)d->ny * d->nx)), y = (int)((c / d->nx) % d->ny),
+                                  x = (int)(c % d->nx);
+                        vzyx[vpos] = (z << 20) | (y << 10) | x;
+                        uint32_t mi = 0, mo = 0;
+                        for (int q = 0; q < D.nnb; ++q) {
+                            const int dz = D.nb_dif[3 * q], dy = D.nb_dif[3 * q + 1], dx = D.nb_dif[3 * q + 2];
+                            int z2 = z + dz, y2 = y + dy, x2 = x + dx;
+                            if (z2 >= 0 && z2 < d->nz && y2 >= 0 && y2 < d->ny && x2 >= 0 && x2 < d->nx &&
+                                lay[((int64_t)z2 * d->ny + y2) * d->nx + x2])
+                                mi |= 1u << q;
+                            z2 = z - dz;
+                            y2 = y - dy;
+                            x2 = x - dx;
+                            if (z2 >= 0 && z2 < d->nz && y2 >= 0 && y2 < d->ny && x2 >= 0 && x2 < d->nx &&
+                                lay[((int64_t)z2 * d->ny + y2) * d->nx + x2])
+                                mo |= 1u << q;
+                        }
+                        vin[vpos] = mi;
+                        vout[vpos] = mo;
+                        ++vpos;
+                    }
+                } else {
+                    a_at.push_back(INFINITY);
+                    a_hilo.push_back(make_float2(INFINITY, 0.f));
+                }
+            }
+            for (int64_t j = 0; j < padded; j += chunk_len) {
+                c0.push_back((int32_t)(base + j));
+                c1.push_back((int32_t)(base + std::min<int64_t>(padded, j + chunk_len)));
+                cl.push_back(L - 1);
+            }
+        }
+        a_vb.push_back(vpos);
+    }
+    const int64_t apad = (int64_t)a_at.size();
+    EKG_CHECK(apad < (int64_t)1 << 31, EKG_ERR_BAD_INPUT, "too many distinct activation times");
+    D.apad = apad;
+    D.nchunks = (int)c0.size();
+    D.at.alloc(apad);
+    D.at_hilo.alloc(apad);
+    D.a_layer.alloc(apad);
+    D.a_vox_begin.alloc(apad + 1);
+    D.vox_zyx.alloc(nv);
+    D.vox_nb.alloc(nv);
+    D.vox_nbo.alloc(nv);
+    D.chunk_a0.alloc(c0.size());
+    D.chunk_a1.alloc(c0.size());
+    D.chunk_layer.alloc(c0.size());
+    D.difs.alloc(3 * D.nnb);
+    D.t.alloc(steps);
+    D.t_hilo.alloc(steps);
+    std::vector<float2> th(steps);
+    for (int64_t i = 0; i < steps; ++i) {
+        const float hi = (float)h->t[i];
+        th[i] = make_float2(hi, (float)(h->t[i] - (double)hi));
+    }
+    EKG_CUDA(cudaMemcpyAsync(D.at.p, a_at.data(), apad * 8, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.at_hilo.p, a_hilo.data(), apad * 8, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.a_layer.p, a_layer.data(), apad * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.a_vox_begin.p, a_vb.data(), (apad + 1) * 8, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.vox_zyx.p, vzyx.data(), nv * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.vox_nb.p, vin.data(), nv * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.vox_nbo.p, vout.data(), nv * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.chunk_a0.p, c0.data(), c0.size() * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.chunk_a1.p, c1.data(), c0.size() * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.chunk_layer.p, cl.data(), c0.size() * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.difs.p, D.nb_dif, 3 * D.nnb, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.t.p, h->t.data(), steps * 8, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.t_hilo.p, th.data(), steps * 8, cudaMemcpyHostToDevice, s));
+    // resident lead field for the loaded lead positions
+    h->leads0_dev.alloc(3 * D.nleads);
+    EKG_CUDA(cudaMemcpyAsync(h->leads0_dev.p, h->leads0.data(), h->leads0.size() * 8, cudaMemcpyHostToDevice, s));
+    h->W0.alloc((size_t)D.nleads * apad);
+    launch_lead_field(s, D, h->leads0_dev.p, D.nleads, D.nleads, 1, h->W0.p, D.nleads);
+    EKG_CUDA(cudaStreamSynchronize(s));
+    h->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+int64_t heart_device_bytes(const ekg_heart *h) {
+    const HeartDev &D = h->dev;
+    int64_t b = D.at.bytes() + D.at_hilo.bytes() + D.a_layer.bytes() + D.a_vox_begin.bytes() + D.vox_zyx.bytes() +
+                D.vox_nb.bytes() + D.vox_nbo.bytes() + D.chunk_a0.bytes() * 3 + D.t.bytes() + D.t_hilo.bytes() +
+                h->W0.bytes() + h->at_cells.bytes();
+    const EvalDev &E = h->ev;
+    b += E.layer_k.bytes() + E.leads.bytes() + E.layer_c.bytes() + E.F.bytes() + E.k0w.bytes() + E.W.bytes() +
+         E.Wp.bytes() + E.partial.bytes() + E.ecg.bytes() + E.crit.bytes() + E.targets.bytes();
+    return b;
+}
+
+// ------------------------------------------------------------------ evaluation
+int64_t eval_bytes_per_sim(const ekg_heart *h) {
+    const HeartDev &D = h->dev;
+    const int64_t L = D.nleads, nl = D.nlayers;
+    return nl * 9 * 8 + L * 3 * 8 + nl * 4 * 4 + nl * D.steps * 8 + L * 8 + 2 * L * D.apad * 4 +
+           (int64_t)D.nchunks * L * D.steps * 8 + L * D.steps * 8 + std::max<int64_t>(1, L) * 2 * 8;
+}
+int64_t eval_bytes_held(const ekg_heart *h) { return (int64_t)h->ev.cap_sims * eval_bytes_per_sim(h); }
+
+void ensure_eval_capacity(ekg_heart *h, int n_sims) {
+    EvalDev &E = h->ev;
+    const HeartDev &D = h->dev;
+    if (E.cap_sims >= n_sims) return;
+    const size_t S = (size_t)n_sims;
+    E.layer_k.alloc(S * D.nlayers * 9);
+    E.leads.alloc(S * D.nleads * 3);
+    E.layer_c.alloc(S * D.nlayers * 4);
+    E.F.alloc(S * D.nlayers * D.steps);
+    E.k0w.alloc(S * D.nleads);
+    E.W.alloc(S * D.nleads * D.apad);
+    E.Wp.alloc(S * D.nleads * D.apad);
+    E.partial.alloc(S * D.nchunks * D.nleads * D.steps);
+    E.ecg.alloc(S * D.nleads * D.steps);
+    E.crit.alloc(S * std::max(1, D.nleads) * 2);
+    E.err.alloc(1);
+    E.cap_sims = n_sims;
+}
+
+// Device pass for n_sims simulations, split into upload / compute / download so the benchmark
+// can time the compute part with its inputs resident.  layer_k [S][nl][9], leads [S][L][3] (host).
+struct PassTiming {
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // start, after lead field, after contraction, end
+    bool on = false;
+};
+static int g_launch_count = 0;
+
+int upload_inputs(ekg_heart *h, int n_sims, const double *layer_k, const double *leads) {
+    HeartDev &D = h->dev;
+    EvalDev &E = h->ev;
+    cudaStream_t s = h->stream;
+    ensure_eval_capacity(h, n_sims);
+    const size_t L = D.nleads, S = n_sims;
+    EKG_CUDA(cudaMemcpyAsync(E.layer_k.p, layer_k, S * D.nlayers * 9 * 8, cudaMemcpyHostToDevice, s));
+    // number of leading leads that move in any simulation (lead displacement genes come first)
+    int nmove = 0;
+    for (size_t si = 0; si < S; ++si) {
+        const double *p = leads + si * L * 3;
+        for (size_t l = 0; l < L; ++l)
+            if (p[3 * l] != h->leads0[3 * l] || p[3 * l + 1] != h->leads0[3 * l + 1] || p[3 * l + 2] != h->leads0[3 * l + 2])
+                nmove = std::max(nmove, (int)l + 1);
+    }
+    if (nmove > 0) EKG_CUDA(cudaMemcpyAsync(E.leads.p, leads, S * L * 3 * 8, cudaMemcpyHostToDevice, s));
+    return nmove;
+}
+
+void compute(ekg_heart *h, int n_sims, int nmove, int n_crit_leads, int mode, PassTiming *tm) {
+    HeartDev &D = h->dev;
+    EvalDev &E = h->ev;
+    cudaStream_t s = h->stream;
+    const size_t L = D.nleads, S = n_sims;
+    int launches = 0;
+    if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[0], s));
+    // lead field: resident rows for leads at their loaded position, recomputed rows for moved ones
+    for (size_t si = 0; si < S; ++si)
+        EKG_CUDA(cudaMemcpyAsync(E.W.p + si * L * D.apad, h->W0.p, L * D.apad * 4, cudaMemcpyDeviceToDevice, s));
+    if (nmove > 0) {
+        launch_lead_field(s, D, E.leads.p, nmove, (int)L, n_sims, E.W.p, (int)L);
+        ++launches;
+    }
+    launch_layer_factors(s, D, E.layer_k.p, n_sims, E.F.p, E.layer_c.p);
+    launch_scale_w(s, D, E.W.p, E.layer_k.p, n_sims, E.Wp.p);
+    launch_k0_term(s, D, E.W.p, E.layer_k.p, n_sims, E.k0w.p);
+    launches += 3;
+    EKG_CUDA(cudaMemsetAsync(E.err.p, 0, sizeof(uint32_t), s));
+    if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[1], s));
+    if (h->eng->umma) launch_contract_umma(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p, E.err.p);
+    else launch_contract_cuda(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p);
+    if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[2], s));
+    launch_reduce_ecg(s, D, E.partial.p, E.k0w.p, n_sims, E.ecg.p);
+    launches += 2;
+    if (n_crit_leads > 0) {
+        launch_criteria(s, D, E.ecg.p, n_sims, n_crit_leads, n_crit_leads, mode, E.targets.p, E.target_len.p,
+                        E.target_off.p, E.crit.p);
+        ++launches;
+    }
+    if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[3], s));
+    g_launch_count = launches;
+}
+
+void device_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *leads, double *ecg_host,
+                 double *crit_host, int n_crit_leads, int mode) {
+    HeartDev &D = h->dev;
+    EvalDev &E = h->ev;
+    cudaStream_t s = h->stream;
+    EKG_CUDA(cudaSetDevice(h->eng->device));
+    const int nmove = upload_inputs(h, n_sims, layer_k, leads);
+    compute(h, n_sims, nmove, crit_host ? n_crit_leads : 0, mode, nullptr);
+    const size_t L = D.nleads, S = n_sims;
+    EKG_CUDA(cudaMemcpyAsync(h->err_host, E.err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    if (crit_host && n_crit_leads > 0)
+        EKG_CUDA(cudaMemcpyAsync(crit_host, E.crit.p, S * n_crit_leads * 2 * 8, cudaMemcpyDeviceToHost, s));
+    if (ecg_host) EKG_CUDA(cudaMemcpyAsync(ecg_host, E.ecg.p, S * L * D.steps * 8, cudaMemcpyDeviceToHost, s));
+    EKG_CUDA(cudaStreamSynchronize(s));
+    if (*h->err_host) throw Error{EKG_ERR_TIMEOUT, "a bounded device wait ran out (error word " +
+                                                       std::to_string(*h->err_host) + ")"};
+}
+
+// Device-only timing of `iters` passes with inputs resident (after `warmup` untimed passes).
+void benchmark(ekg_heart *h, int n_sims, const double *layer_k, const double *leads, int warmup, int iters,
+               double *out, int n_out) {
+    std::lock_guard<std::mutex> lk(h->mu);
+    EKG_CUDA(cudaSetDevice(h->eng->device));
+    cudaStream_t s = h->stream;
+    const int nmove = upload_inputs(h, n_sims, layer_k, leads);
+    const int ncl = h->has_eval ? h->es.n_crit_leads : 0;
+    const int mode = h->has_eval ? h->es.comparison_mode : 2;
+    for (int i = 0; i < warmup; ++i) compute(h, n_sims, nmove, ncl, mode, nullptr);
+    PassTiming tm;
+    tm.on = true;
+    for (auto &e : tm.ev) EKG_CUDA(cudaEventCreate(&e));
+    cudaEvent_t t0, t1;
+    EKG_CUDA(cudaEventCreate(&t0));
+    EKG_CUDA(cudaEventCreate(&t1));
+    EKG_CUDA(cudaStreamSynchronize(s));
+    double contract = 0, prep = 0, tail = 0;
+    EKG_CUDA(cudaEventRecord(t0, s));
+    for (int i = 0; i < iters; ++i) {
+        compute(h, n_sims, nmove, ncl, mode, &tm);
+        EKG_CUDA(cudaEventSynchronize(tm.ev[3]));
+        float a = 0, b = 0, c = 0;
+        EKG_CUDA(cudaEventElapsedTime(&a, tm.ev[0], tm.ev[1]));
+        EKG_CUDA(cudaEventElapsedTime(&b, tm.ev[1], tm.ev[2]));
+        EKG_CUDA(cudaEventElapsedTime(&c, tm.ev[2], tm.ev[3]));
+        prep += a;
+        contract += b;
+        tail += c;
+    }
+    EKG_CUDA(cudaEventRecord(t1, s));
+    EKG_CUDA(cudaEventSynchronize(t1));
+    float total = 0;
+    EKG_CUDA(cudaEventElapsedTime(&total, t0, t1));
+    const double vals[6] = {total, contract, prep, tail, (double)g_launch_count, (double)nmove};
+    for (int i = 0; i < n_out && i < 6; ++i) out[i] = vals[i];
+    for (auto &e : tm.ev) cudaEventDestroy(e);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    EKG_CUDA(cudaMemcpy(h->err_host, h->ev.err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (*h->err_host) throw Error{EKG_ERR_TIMEOUT, "a bounded device wait ran out"};
+}
+
+// Per-simulation host part of SimImplementation::eval (sim.cpp:443-492): genes -> layer APs and
+// lead positions.
+void prepare_sim(ekg_heart *h, const double *genes, int n_genes, double *layer_k, double *leads, double *violation) {
+    const EvalSettings &es = h->es;
+    EKG_CHECK(h->has_eval, EKG_ERR_BAD_INPUT, "evaluation settings not set for this heart");
+    const int nw = es.gm.n_free() * (es.gm.interpolation == 2 ? 3 : 2);
+    const int nd = es.optimize_points ? 2 * h->dev.nleads : 0;
+    if (n_genes < nw + nd) throw Error{EKG_ERR_BAD_INPUT, "Solution does not contain enough values"};
+    if (n_genes != nw + nd) {
+        std::ostringstream m;
+        m << "chromosome size does not agree with the combination of the number of free Wohlfart parameters and "
+             "the selected interpolation procedure ("
+          << n_genes << " != " << nd << "+" << nw << ")";
+        throw Error{EKG_ERR_BAD_INPUT, m.str()};
+    }
+    for (int i = 0; i < n_genes; ++i)
+        EKG_CHECK(std::isfinite(genes[i]), EKG_ERR_BAD_INPUT, "gene values must be finite");
+    if (es.optimize_points) {
+        std::vector<double> disp(2 * h->dev.nleads);
+        for (int i = 0; i < h->dev.nleads; ++i) {
+            disp[2 * i] = genes[nw + 2 * i];
+            disp[2 * i + 1] = genes[nw + 2 * i + 1];
+        }
+        move_leads(h->dev.nleads, h->leads0.data(), disp.data(), leads);
+    } else {
+        std::copy(h->leads0.begin(), h->leads0.end(), leads);
+    }
+    layer_aps_from_genes(es.gm, h->dev.nlayers, genes, layer_k, violation);
+}
+
+// SimImplementation::calculateFitness (sim.cpp:600-702) from the device's per-lead comparison
+// values and peak positions, plus the host-side fast approximation and endo-epi terms.
+void assemble_criteria(const ekg_heart *h, const double *layer_k, const double *crit2, bool done,
+                       double approx_crit, const std::vector<double> &approx, double *out) {
+    const EvalSettings &es = h->es;
+    EKG_CHECK(es.criteria_mode == 1, EKG_ERR_BAD_INPUT, "selected criteria mode is either not implemented yet or invalid");
+    const int nm = es.n_crit_leads;
+    const int nc = es.n_criteria;
+    for (int i = 0; i < nc; ++i) out[i] = 0.0;
+    if (es.fast_is_crit) out[nm] = approx_crit;
+    for (int i = 0; i < nm; ++i) {
+        double value;
+        int peak;
+        if (done) {
+            value = crit2[2 * i];
+            peak = (int)crit2[2 * i + 1];
+        } else {
+            value = approx_crit;
+            peak = (int)(std::max_element(approx.begin(), approx.end()) - approx.begin());
+        }
+        int ci = i;
+        if (es.peak) {
+            ci = 2 * i;
+            out[ci + 1] = std::abs(peak - es.target_peak[i]);
+        }
+        out[ci] = value;
+        if (out[ci] < 0 || !std::isfinite(out[ci]) || !std::isnormal(out[ci])) out[ci] = 2e10;
+    }
+    if (es.endo_epi_delay >= 0) {
+        const int nl = h->dev.nlayers;
+        double sd = 0.0;
+        for (double t = 1.0; t < 700.0; t += 1.0) {
+            const double dd = wohlfart(layer_k, t + es.endo_epi_delay) - wohlfart(layer_k + 9 * (nl - 1), t);
+            sd += dd * dd;
+        }
+        out[nc - 1] = sd;
+    }
+}
+
+// host comparison for the fast approximation (same formulas as the device criteria)
+double compare_host(int mode, const std::vector<double> &a, const std::vector<double> &b, double bofs) {
+    const size_t len = std::min(a.size(), b.size());
+    if (mode == 2) {
+        double sa = 0, sb = 0;
+        for (size_t i = 0; i < len; ++i) sa += a[i];
+        for (size_t i = 0; i < len; ++i) sb += b[i];
+        const double inv = 1.0 / (double)len, ma = sa * inv, mb = sb * inv;
+        double va = 0, vb = 0, cv = 0;
+        for (size_t i = 0; i < len; ++i) {
+            va += (a[i] - ma) * (a[i] - ma);
+            vb += (b[i] - mb) * (b[i] - mb);
+            cv += (a[i] - ma) * (b[i] - mb);
+        }
+        return 1.0 - (cv / (double)len) / (std::sqrt(va * inv) * std::sqrt(vb * inv));
+    } else if (mode == 4) {
+        double ab = 0, aa = 0, bb = 0;
+        for (size_t i = 0; i < len; ++i) {
+            ab += a[i] * b[i];
+            aa += a[i] * a[i];
+            bb += b[i] * b[i];
+        }
+        return 1.0 - ab / (std::sqrt(aa) * std::sqrt(bb));
+    } else if (mode == 1) {
+        double q = 0;
+        for (size_t i = 0; i < len; ++i) q += (a[i] - b[i]) * (a[i] - b[i]);
+        return std::sqrt(q / (double)len);
+    }
+    double mn = a[0], mx = a[0];
+    for (size_t i = 1; i < a.size(); ++i) {
+        if (a[i] < mn) mn = a[i];
+        else if (a[i] > mx) mx = a[i];
+    }
+    const double am = 1.0 / (mx - mn);
+    double mean = 0;
+    for (size_t i = 0; i < len; ++i) mean += (a[i] * am + bofs) / (b[i] + bofs);
+    mean /= (double)len;
+    double var = 0;
+    for (size_t i = 0; i < len; ++i) {
+        const double d = (a[i] * am + bofs) / (b[i] + bofs) - mean;
+        var += d * d;
+    }
+    var /= (double)len;
+    return var == 0 ? 1e30 : std::sqrt(var);
+}
+
+// fast approximation gate (sim.cpp:712-747; simlib/simulator.cpp:552-559)
+bool approx_gate(const ekg_heart *h, const double *layer_k, double &approx_crit, std::vector<double> &approx) {
+    const EvalSettings &es = h->es;
+    approx_crit = 2;
+    if (!(es.fast_is_crit || es.fast_limit < 2)) return true;
+    const int nl = h->dev.nlayers;
+    const size_t n = (size_t)(h->length / h->dt);
+    approx.resize(n);
+    for (size_t i = 0; i < n; ++i) {
+        const double t = h->start + i * h->dt;
+        approx[i] = wohlfart(layer_k, t + es.fast_delay) - wohlfart(layer_k + 9 * (nl - 1), t);
+    }
+    approx_crit = compare_host(es.comparison_mode, approx, es.targets[0], es.target_offsets[0]);
+    return !(approx_crit > es.fast_limit);
+}
+
+void eval_many(ekg_heart *h, int n_sims, const double *genes, int n_genes, double *criteria, double *violation,
+               double *ecg, double *layer_k_out, double *leads_out) {
+    std::lock_guard<std::mutex> lk(h->mu);
+    const int nl = h->dev.nlayers, L = h->dev.nleads;
+    std::vector<double> lk_all((size_t)n_sims * nl * 9), leads_all((size_t)n_sims * L * 3), viol(n_sims);
+    std::vector<char> done(n_sims, 1);
+    std::vector<double> acrit(n_sims, 2.0);
+    std::vector<std::vector<double>> approx(n_sims);
+    for (int s = 0; s < n_sims; ++s) {
+        prepare_sim(h, genes + (size_t)s * n_genes, n_genes, &lk_all[(size_t)s * nl * 9], &leads_all[(size_t)s * L * 3],
+                    &viol[s]);
+        done[s] = approx_gate(h, &lk_all[(size_t)s * nl * 9], acrit[s], approx[s]);
+    }
+    const int ncl = h->es.n_crit_leads;
+    std::vector<double> crit2((size_t)n_sims * std::max(1, ncl) * 2);
+    device_pass(h, n_sims, lk_all.data(), leads_all.data(), ecg, crit2.data(), ncl, h->es.comparison_mode);
+    for (int s = 0; s < n_sims; ++s) {
+        assemble_criteria(h, &lk_all[(size_t)s * nl * 9], &crit2[(size_t)s * ncl * 2], done[s], acrit[s], approx[s],
+                          criteria + (size_t)s * h->es.n_criteria);
+        violation[s] = viol[s];
+    }
+    if (layer_k_out) std::copy(lk_all.begin(), lk_all.end(), layer_k_out);
+    if (leads_out) std::copy(leads_all.begin(), leads_all.end(), leads_out);
+}
+
+void set_eval(ekg_heart *h, const ekg_eval_config *c) {
+    EKG_CHECK(c, EKG_ERR_BAD_INPUT, "null eval config");
+    EKG_CHECK(c->interpolation == 1 || c->interpolation == 2, EKG_ERR_BAD_INPUT,
+              "unknown interpolation type (endo-epi or endo-mid-epi)");
+    EKG_CHECK(c->n_base_aps >= 2 && c->base_aps && c->k_min && c->k_max, EKG_ERR_BAD_INPUT, "need at least 2 base APs");
+    EKG_CHECK(c->comparison_mode >= 1 && c->comparison_mode <= 4, EKG_ERR_BAD_INPUT, "invalid comparison mode");
+    EKG_CHECK(c->criteria_mode == 1 || c->criteria_mode == 9, EKG_ERR_BAD_INPUT, "invalid optimization mode");
+    EKG_CHECK(c->n_targets >= 1 && c->targets && c->target_len, EKG_ERR_BAD_INPUT, "no targets");
+    EvalSettings es;
+    es.gm.interpolation = c->interpolation;
+    es.gm.mid_position = c->mid_position;
+    for (int i = 0; i < c->n_base_aps; ++i) es.gm.base.emplace_back(c->base_aps + 9 * i, c->base_aps + 9 * i + 9);
+    es.gm.k_min.assign(c->k_min, c->k_min + 9);
+    es.gm.k_max.assign(c->k_max, c->k_max + 9);
+    es.gm.free_mask = c->free_k_mask & 0x1ffu;
+    es.optimize_points = c->optimize_points != 0;
+    es.criteria_mode = c->criteria_mode;
+    es.comparison_mode = c->comparison_mode;
+    es.peak = c->peak_is_criterion != 0;
+    es.fast_is_crit = c->fast_is_criterion != 0;
+    es.fast_delay = c->fast_delay;
+    es.fast_limit = c->fast_limit;
+    es.endo_epi_delay = c->endo_epi_delay;
+    size_t off = 0;
+    for (int i = 0; i < c->n_targets; ++i) {
+        EKG_CHECK(c->target_len[i] >= 1, EKG_ERR_BAD_INPUT, "empty target");
+        es.targets.emplace_back(c->targets + off, c->targets + off + c->target_len[i]);
+        off += c->target_len[i];
+        es.target_offsets.push_back(c->target_offsets ? c->target_offsets[i] : 0.0);
+        es.target_peak.push_back((int)(std::max_element(es.targets.back().begin(), es.targets.back().end()) -
+                                       es.targets.back().begin()));
+    }
+    // SimImplementation constructor: number of criteria (sim.cpp:403-429)
+    const int base = c->criteria_mode == 1 ? std::min(h->dev.nleads, c->n_targets) : 1;
+    es.n_crit_leads = std::min(h->dev.nleads, c->n_targets);
+    es.n_criteria = base + (es.peak ? base : 0) + (es.fast_is_crit ? 1 : 0) + (es.endo_epi_delay >= 0 ? 1 : 0);
+    es.n_genes = es.gm.n_free() * (es.gm.interpolation == 2 ? 3 : 2) + (es.optimize_points ? 2 * h->dev.nleads : 0);
+    if (c->disp_min && c->n_disp_min > 0) es.disp_min_v.assign(c->disp_min, c->disp_min + c->n_disp_min);
+    if (c->disp_max && c->n_disp_max > 0) es.disp_max_v.assign(c->disp_max, c->disp_max + c->n_disp_max);
+    std::lock_guard<std::mutex> lk(h->mu);
+    // device copies of the targets
+    EvalDev &E = h->ev;
+    E.targets.alloc(off);
+    E.target_len.alloc(c->n_targets);
+    E.target_off.alloc(c->n_targets);
+    EKG_CUDA(cudaSetDevice(h->eng->device));
+    EKG_CUDA(cudaMemcpy(E.targets.p, c->targets, off * 8, cudaMemcpyHostToDevice));
+    EKG_CUDA(cudaMemcpy(E.target_len.p, c->target_len, c->n_targets * 8, cudaMemcpyHostToDevice));
+    EKG_CUDA(cudaMemcpy(E.target_off.p, es.target_offsets.data(), c->n_targets * 8, cudaMemcpyHostToDevice));
+    h->es = es;
+    h->has_eval = true;
+}
+
+}  // namespace ekg
+
+using namespace ekg;
+
+extern "C" {
+
+const char *ekg_last_error(void) { return g_last_error.c_str(); }
+
+int ekg_engine_create(int device, ekg_engine **out) {
+    return guard([&] {
+        EKG_CHECK(out, EKG_ERR_BAD_INPUT, "null output pointer");
+        int n = 0;
+        EKG_CUDA(cudaGetDeviceCount(&n));
+        EKG_CHECK(device >= 0 && device < n, EKG_ERR_BAD_INPUT, "no such CUDA device");
+        std::unique_ptr<ekg_engine> e(new ekg_engine());
+        e->device = device;
+        if (const char *v = std::getenv("EKG_CONTRACT")) e->umma = std::string(v) != "cuda";
+        if (const char *v = std::getenv("EKG_CHUNK")) e->chunk_len = std::max(64, std::atoi(v) / 64 * 64);
+        EKG_CUDA(cudaSetDevice(device));
+        EKG_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+        *out = e.release();
+    });
+}
+
+int ekg_engine_destroy(ekg_engine *e) {
+    return guard([&] {
+        if (!e) return;
+        cudaSetDevice(e->device);
+        if (e->stream) cudaStreamDestroy(e->stream);
+        delete e;
+    });
+}
+
+int ekg_engine_free_bytes(ekg_engine *e, uint64_t *free_bytes) {
+    return guard([&] {
+        EKG_CHECK(e && free_bytes, EKG_ERR_BAD_INPUT, "null argument");
+        size_t f = 0, t = 0;
+        EKG_CUDA(cudaSetDevice(e->device));
+        EKG_CUDA(cudaMemGetInfo(&f, &t));
+        *free_bytes = f;
+    });
+}
+
+int ekg_heart_create(ekg_engine *e, const ekg_heart_desc *desc, ekg_heart **out) {
+    return guard([&] {
+        EKG_CHECK(e && desc && out, EKG_ERR_BAD_INPUT, "null argument");
+        std::unique_ptr<ekg_heart> h(new ekg_heart());
+        h->eng = e;
+        heart_setup(h.get(), desc);
+        *out = h.release();
+    });
+}
+
+int ekg_heart_destroy(ekg_heart *h) {
+    return guard([&] {
+        if (!h) return;
+        cudaSetDevice(h->eng->device);
+        delete h;
+    });
+}
+
+int ekg_heart_get_info(ekg_heart *h, ekg_heart_info *info) {
+    return guard([&] {
+        EKG_CHECK(h && info, EKG_ERR_BAD_INPUT, "null argument");
+        info->n_cells = h->ncell;
+        info->n_voxels = h->nvox;
+        info->n_aps = h->naps;
+        info->n_layers = h->dev.nlayers;
+        info->n_leads = h->dev.nleads;
+        info->steps = h->dev.steps;
+        info->ca_rounds = h->ca_rounds;
+        info->device_bytes = heart_device_bytes(h);
+        info->ca_ms = h->ca_ms;
+        info->setup_ms = h->setup_ms;
+    });
+}
+
+int ekg_heart_activation(ekg_heart *h, double *at_out) {
+    return guard([&] {
+        EKG_CHECK(h && at_out, EKG_ERR_BAD_INPUT, "null argument");
+        std::copy(h->at_host.begin(), h->at_host.end(), at_out);
+    });
+}
+
+int ekg_heart_ap_index(ekg_heart *h, int64_t *out) {
+    return guard([&] {
+        EKG_CHECK(h && out, EKG_ERR_BAD_INPUT, "null argument");
+        std::copy(h->ap_index_ref.begin(), h->ap_index_ref.end(), out);
+    });
+}
+
+int ekg_simulate(ekg_heart *h, const double *layer_k, const double *leads_zyx, double *ecg_out) {
+    return guard([&] {
+        EKG_CHECK(h && layer_k && ecg_out, EKG_ERR_BAD_INPUT, "null argument");
+        for (int i = 0; i < 9 * h->dev.nlayers; ++i)
+            EKG_CHECK(std::isfinite(layer_k[i]), EKG_ERR_BAD_INPUT, "AP coefficients must be finite");
+        std::lock_guard<std::mutex> lk(h->mu);
+        device_pass(h, 1, layer_k, leads_zyx ? leads_zyx : h->leads0.data(), ecg_out, nullptr, 0, 2);
+    });
+}
+
+int ekg_heart_set_eval(ekg_heart *h, const ekg_eval_config *cfg) {
+    return guard([&] {
+        EKG_CHECK(h, EKG_ERR_BAD_INPUT, "null heart");
+        set_eval(h, cfg);
+    });
+}
+
+int ekg_eval_shape(ekg_heart *h, int32_t *n_genes, int32_t *n_criteria) {
+    return guard([&] {
+        EKG_CHECK(h && h->has_eval, EKG_ERR_BAD_INPUT, "evaluation settings not set for this heart");
+        if (n_genes) *n_genes = h->es.n_genes;
+        if (n_criteria) *n_criteria = h->es.n_criteria;
+    });
+}
+
+int ekg_eval_gene_bounds(ekg_heart *h, double *gmin, double *gmax) {
+    return guard([&] {
+        EKG_CHECK(h && h->has_eval && gmin && gmax, EKG_ERR_BAD_INPUT, "evaluation settings not set for this heart");
+        const EvalSettings &es = h->es;
+        // SimImplementation::getGeneParams (sim.cpp:523-580)
+        const int nf = es.gm.n_free(), nsets = es.gm.interpolation == 2 ? 3 : 2;
+        int g = 0;
+        for (int i = 0; i < 9; ++i)
+            if (es.gm.free_mask & (1u << i)) {
+                for (int s = 0; s < nsets; ++s) {
+                    gmin[g + s * nf] = es.gm.k_min[i];
+                    gmax[g + s * nf] = es.gm.k_max[i];
+                }
+                ++g;
+            }
+        int pos = nf * nsets;
+        if (es.optimize_points) {
+            std::vector<double> dmin = es.disp_min_v, dmax = es.disp_max_v;
+            if (dmin.empty()) dmin.push_back(0);
+            if (dmax.empty()) dmax.push_back(0);
+            for (int i = 0; i < 2 * h->dev.nleads; ++i) {
+                gmin[pos + i] = dmin[std::min<size_t>(i, dmin.size() - 1)];
+                gmax[pos + i] = dmax[std::min<size_t>(i, dmax.size() - 1)];
+            }
+        }
+    });
+}
+
+int ekg_eval(ekg_heart *h, const double *genes, int32_t n_genes, double *criteria_out, double *violation_out,
+             double *ecg_out, double *layer_k_out, double *leads_out) {
+    return guard([&] {
+        EKG_CHECK(h && genes && criteria_out && violation_out, EKG_ERR_BAD_INPUT, "null argument");
+        eval_many(h, 1, genes, n_genes, criteria_out, violation_out, ecg_out, layer_k_out, leads_out);
+    });
+}
+
+int ekg_eval_batch(ekg_heart *h, int32_t n_sims, const double *genes, int32_t n_genes, double *criteria_out,
+                   double *violation_out, double *ecg_out) {
+    return guard([&] {
+        EKG_CHECK(h && genes && criteria_out && violation_out && n_sims >= 1, EKG_ERR_BAD_INPUT, "bad argument");
+        eval_many(h, n_sims, genes, n_genes, criteria_out, violation_out, ecg_out, nullptr, nullptr);
+    });
+}
+
+int ekg_heart_benchmark(ekg_heart *h, int32_t n_sims, const double *layer_k, const double *leads, int32_t warmup,
+                        int32_t iters, double *out, int32_t n_out) {
+    return guard([&] {
+        EKG_CHECK(h && layer_k && out && n_sims >= 1 && iters >= 1 && warmup >= 0, EKG_ERR_BAD_INPUT, "bad argument");
+        std::vector<double> lds;
+        if (!leads) {
+            for (int i = 0; i < n_sims; ++i) lds.insert(lds.end(), h->leads0.begin(), h->leads0.end());
+            leads = lds.data();
+        }
+        benchmark(h, n_sims, layer_k, leads, warmup, iters, out, n_out);
+    });
+}
+
+int ekg_move_leads(int32_t n, const double *orig, const double *disp, double *out) {
+    return guard([&] {
+        EKG_CHECK(n >= 0 && orig && out, EKG_ERR_BAD_INPUT, "null argument");
+        move_leads(n, orig, disp, out);
+    });
+}
+
+int ekg_layer_aps(const ekg_eval_config *c, int32_t n_layers, const double *genes, double *layer_k_out,
+                  double *violation_out) {
+    return guard([&] {
+        EKG_CHECK(c && genes && layer_k_out && violation_out && n_layers >= 1, EKG_ERR_BAD_INPUT, "bad argument");
+        EKG_CHECK(c->n_base_aps >= 2 && c->base_aps && c->k_min && c->k_max, EKG_ERR_BAD_INPUT, "need at least 2 base APs");
+        GeneModel gm;
+        gm.interpolation = c->interpolation;
+        gm.mid_position = c->mid_position;
+        for (int i = 0; i < c->n_base_aps; ++i) gm.base.emplace_back(c->base_aps + 9 * i, c->base_aps + 9 * i + 9);
+        gm.k_min.assign(c->k_min, c->k_min + 9);
+        gm.k_max.assign(c->k_max, c->k_max + 9);
+        gm.free_mask = c->free_k_mask & 0x1ffu;
+        layer_aps_from_genes(gm, n_layers, genes, layer_k_out, violation_out);
+    });
+}
+
+int ekg_heart_from_ini(ekg_engine *e, const char *ini_path, const char *out_dir, ekg_heart **out) {
+    return guard([&] {
+        EKG_CHECK(e && ini_path && out, EKG_ERR_BAD_INPUT, "null argument");
+        SimConfig c = load_config(ini_path);
+        // SimImplementation constructor order (sim.cpp:368-379): the conduction matrix is loaded
+        // before the shape, against the simulator's default of 12 layers (simlib/simulator.cpp:201-206)
+        int nt = 0;
+        std::vector<double> tm;
+        read_transfer(c.transfer, nt, tm);
+        if (nt < 12) throw Error{EKG_ERR_TRANSFER, "loaded transfer matrix too small"};
+        std::vector<double> pts;
+        read_points(c.points, pts);
+        int nz, ny, nx;
+        std::vector<int32_t> lay;
+        read_shape(c.shape, nz, ny, nx, lay);
+        EKG_CHECK(c.excitation_in.empty(), EKG_ERR_BAD_INPUT,
+                  "loading a precomputed excitation sequence is not supported; remove [model] excitation sequence");
+        const int nh = nhood_code(c.nhood);
+        if (nh < 0) throw Error{EKG_ERR_BAD_INPUT, "\n   unknown neighbourhood (only know of these: 2D4, 3D4, 2D8, 3D8 (cube))"};
+        ekg_heart_desc d{};
+        d.nz = nz;
+        d.ny = ny;
+        d.nx = nx;
+        d.layers = lay.data();
+        d.n_transfer = nt;
+        d.transfer = tm.data();
+        d.n_leads = (int32_t)(pts.size() / 3);
+        d.leads_zyx = pts.data();
+        d.nhood = nh;
+        d.start = c.start;
+        d.length = c.length;
+        d.dt = c.dt;
+        std::unique_ptr<ekg_heart> h(new ekg_heart());
+        h->eng = e;
+        heart_setup(h.get(), &d);
+        if (c.interpolation != "endo-epi" && c.interpolation != "endo-mid-epi")
+            throw Error{EKG_ERR_BAD_INPUT, "unknown interpolation type [" + c.interpolation + "]"};
+        std::vector<std::vector<double>> targets;
+        std::vector<double> offs;
+        load_targets(c, c.targets_file, out_dir ? std::string(out_dir) : std::string(), targets, offs);
+        std::vector<double> flat, base;
+        std::vector<int64_t> tl;
+        for (auto &t : targets) {
+            flat.insert(flat.end(), t.begin(), t.end());
+            tl.push_back((int64_t)t.size());
+        }
+        for (auto &b : c.base_aps) base.insert(base.end(), b.begin(), b.end());
+        std::vector<double> dmin(c.disp_min.begin(), c.disp_min.end()), dmax(c.disp_max.begin(), c.disp_max.end());
+        ekg_eval_config ec{};
+        ec.interpolation = c.interpolation == "endo-epi" ? 1 : 2;
+        ec.mid_position = c.mid_position;
+        ec.n_base_aps = (int32_t)c.base_aps.size();
+        ec.base_aps = base.data();
+        ec.k_min = c.k_min.data();
+        ec.k_max = c.k_max.data();
+        uint32_t mask = 0;
+        for (int k : c.free_k)
+            if (k >= 0 && k < 9) mask |= 1u << k;
+        ec.free_k_mask = mask;
+        ec.optimize_points = c.optimize_points;
+        ec.criteria_mode = c.criteria_mode;
+        ec.comparison_mode = c.comparison_mode;
+        ec.peak_is_criterion = c.peak;
+        ec.fast_is_criterion = c.fast_is_crit;
+        ec.fast_delay = c.fast_delay;
+        ec.fast_limit = c.fast_limit;
+        ec.endo_epi_delay = c.endo_epi_delay;
+        ec.n_targets = (int32_t)targets.size();
+        ec.target_len = tl.data();
+        ec.targets = flat.data();
+        ec.target_offsets = offs.data();
+        ec.n_disp_min = (int32_t)dmin.size();
+        ec.disp_min = dmin.data();
+        ec.n_disp_max = (int32_t)dmax.size();
+        ec.disp_max = dmax.data();
+        set_eval(h.get(), &ec);
+        h->cfg = c;
+        *out = h.release();
+    });
+}
+
+}  // extern "C"

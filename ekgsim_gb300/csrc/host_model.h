@@ -1,0 +1,92 @@
+// host_model.h -- host-side parts of one evaluation: simulator.ini settings, the reference's file
+// formats, gene -> layer AP construction, lead displacement.  FP64 throughout; this is per-
+// evaluation bookkeeping (microseconds for three layers), not the simulation itself, which runs
+// on the device.
+#pragma once
+
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+namespace ekg {
+
+// ------------------------------------------------------------------ INI (copyOfLibs/Ini.h semantics)
+// Sections "[name]"; "name = value" lines (name and value trimmed of blanks/tabs); lines whose
+// name starts with ';' are comments; a repeated name keeps its last value (copyOfLibs/Ini.cpp:171-200).
+struct Ini {
+    std::map<std::string, std::map<std::string, std::string>> sec;
+    bool ok = false;
+    bool load(const std::string &path);
+    bool has(const std::string &s, const std::string &k) const;
+    std::string str(const std::string &s, const std::string &k, const std::string &def = "") const;
+    double num(const std::string &s, const std::string &k, double def) const;
+    std::vector<double> vec(const std::string &s, const std::string &k) const;
+};
+
+// ------------------------------------------------------------------ settings
+struct SimConfig {
+    // [model] / [output files] / [simulation]  (simlib/simulator.h:107-145)
+    std::string shape, transfer, points, excitation_in, excitation_out, results = "result.column";
+    double start = 0, length = 800, dt = 1.0 / 3.0;
+    std::string nhood;
+    // [wohlfart ap] / [measuring points] / [optimization]  (SimSettings.h:158-356)
+    std::vector<std::vector<double>> base_aps;
+    std::vector<double> k_min, k_max;
+    std::string interpolation;
+    double mid_position = 0.5;
+    std::vector<int> free_k;
+    std::vector<int> disp_min, disp_max;
+    std::string targets_file;
+    int criteria_mode = 1, comparison_mode = 2;
+    double endo_epi_delay = -1;
+    bool peak = false, optimize_points = false, fast_is_crit = false;
+    double fast_delay = 0, fast_limit = 2;
+    size_t generations = 100, population = 0;
+    int queue_size = 1;
+    double ap_time_step = 1;  // [action potentials] resample time step (sim.cpp:1008)
+};
+// Parses the keys both SimLib::Settings and SimSettings read; throws std::runtime_error with the
+// reference's messages on the errors the reference throws on.
+SimConfig load_config(const std::string &ini_path);
+int nhood_code(const std::string &name);  // EKG_NHOOD_* or -1
+
+// ------------------------------------------------------------------ files
+// importMatrix with shapeLoad (simlib/matrix.h:125-248): signed layer grid [z][y][x].
+void read_shape(const std::string &path, int &nz, int &ny, int &nx, std::vector<int32_t> &layers);
+// importMatrix with the default loader for the conduction matrix: n x n row-major.
+void read_transfer(const std::string &path, int &n, std::vector<double> &t);
+// Simulation::loadMeasuringPoints (simlib/simulator.cpp:369-397): returns (z,y,x) triples.
+void read_points(const std::string &path, std::vector<double> &zyx);
+// ColumnFile::load (simlib/columnFile.h:115-165).
+void read_columns(const std::string &path, std::vector<std::vector<double>> &cols);
+// SimImplementation::loadTargets (sim.cpp:999-1042); writes target_chk.column into out_dir
+// unless out_dir is empty.
+void load_targets(const SimConfig &c, const std::string &path, const std::string &out_dir,
+                  std::vector<std::vector<double>> &targets, std::vector<double> &offsets);
+// vectorMath.h:210-227
+void resample(const std::vector<double> &src, std::vector<double> &dest, double factor, int start_offset);
+// exportVectors for .column files (simlib/simulator.h:196-240).
+void write_columns(const std::string &path, const std::vector<std::string> &names,
+                   const std::vector<std::string> &comments, const std::vector<const std::vector<double> *> &data,
+                   double start, double dt, const std::string &comment);
+
+// ------------------------------------------------------------------ APs and genes
+double wohlfart(const double *k, double t);  // WohlfartPlus::operator[] (simlib/Wohlfart.h:195-203)
+
+struct GeneModel {
+    int interpolation = 2;  // 1 endo-epi, 2 endo-mid-epi
+    double mid_position = 0.5;
+    std::vector<std::vector<double>> base;  // base APs (9 each)
+    std::vector<double> k_min, k_max;
+    uint32_t free_mask = 0;
+    int n_free() const;
+};
+// simUsingBorderAps / simUsingBorderAndMidAps (sim.cpp:751-916): layer APs [nl][9] and the
+// violation of the gene-set APs (sim.cpp:582-596).
+void layer_aps_from_genes(const GeneModel &m, int n_layers, const double *genes, double *out_k, double *violation);
+// EkgSim::loadMeasuringPoints basis + moveMeasuringPoints (simlib/sim_lib.h:167-208).
+void move_leads(int n, const double *orig_zyx, const double *disp_uv, double *out_zyx);
+
+}  // namespace ekg

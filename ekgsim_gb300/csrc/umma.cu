@@ -1,0 +1,328 @@
+// umma.cu -- the lead contraction on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// For one simulation, one K chunk (a range of de-duplicated APs inside one layer L) and one tile
+// of 128 time steps the CTA computes
+//     P[t, l] = sum_a H_a(t) W'[l, a]        (M = 128 steps, N = leads padded to 16..256, K = APs)
+// and writes partial[s][chunk][l][t] = P[t, l] * F_L(t) in FP64.  H_a(t) (see ecg.cu) is evaluated
+// in FP32 by all 256 threads straight into shared memory, split into BF16 hi + lo parts, as the A
+// operand; W' (FP32 in HBM) is split the same way as the B operand.  One elected thread issues
+// three MMAs per 16-wide K step (hi*hi, hi*lo, lo*hi) into an FP32 accumulator in tensor memory;
+// a two-stage shared-memory ring lets the producers fill stage k+1 while the tensor core consumes
+// stage k, tracked by an mbarrier per stage that tcgen05.commit arrives on.
+//
+// Operand layout: K-major, no swizzle.  A core matrix is 8 rows x 16 bytes (8 BF16 along K),
+// stored contiguously; core matrix (row group g, K chunk c) sits at byte (c * G + g) * 128 for a
+// tile of G row groups, so the descriptor's leading byte offset (next core matrix along K) is
+// G * 128 and its stride byte offset (next 8-row group) is 128.
+//
+// Every mbarrier wait is bounded: on timeout the CTA records KERR_MBAR_TIMEOUT in the error word,
+// waits (bounded) for the last commit, releases its tensor memory and skips its output.
+#include <cuda_bf16.h>
+#include <cstdio>
+
+#include "ekg_internal.h"
+
+namespace ekg {
+
+namespace {
+
+constexpr int UM_M = 128;       // time steps per tile
+constexpr int UM_KT = 64;       // APs per pipeline stage (4 MMA K steps)
+constexpr int UM_THREADS = 256;
+constexpr uint32_t WAIT_LIMIT = 1u << 22;  // try_wait rounds before giving up (~seconds)
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait; returns false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    for (uint32_t i = 0; i < WAIT_LIMIT; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void fence_barrier_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// tcgen05 shared-memory matrix descriptor: start, leading and stride byte offsets (>>4),
+// descriptor version 1, no swizzle, base offset 0.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+// instruction descriptor, kind::f16: FP32 accumulate, BF16 A and B, both K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float h_value(float tau, float4 c) {
+    const float e1 = ex2_approx(-c.x * tau);
+    const float s = rcp_approx(1.0f + e1);
+    const float e4 = ex2_approx(-c.y * tau);
+    const float h = s * fmaf(c.z, e4, c.w);
+    return s == 0.0f ? 0.0f : h;
+}
+// x -> (bf16 hi, bf16 lo) packed pairs for elements (x0, x1)
+__device__ __forceinline__ void split2(float x0, float x1, uint32_t &hi, uint32_t &lo) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+    const float r0 = x0 - __bfloat162float(h.x), r1 = x1 - __bfloat162float(h.y);
+    __nv_bfloat162 l = __floats2bfloat162_rn(r0, r1);
+    hi = *reinterpret_cast<uint32_t *>(&h);
+    lo = *reinterpret_cast<uint32_t *>(&l);
+}
+
+template <int N>
+struct UmmaSmem {
+    // two stages; A: 128 x 64 BF16 = 16 KB per part; B: N x 64 BF16 per part
+    alignas(1024) uint8_t a_hi[2][UM_M * UM_KT * 2];
+    alignas(1024) uint8_t a_lo[2][UM_M * UM_KT * 2];
+    alignas(1024) uint8_t b_hi[2][N * UM_KT * 2];
+    alignas(1024) uint8_t b_lo[2][N * UM_KT * 2];
+    float2 at[2][UM_KT];
+    alignas(8) uint64_t bar[2];
+    uint32_t tmem_base;
+    int abort;
+};
+
+template <int N>
+__global__ void __launch_bounds__(UM_THREADS, 1) k_contract_umma(
+    int steps, int nleads, int64_t apad, int nl, const float2 *__restrict__ t_hilo, const float2 *__restrict__ at_hilo,
+    const int32_t *__restrict__ chunk_a0, const int32_t *__restrict__ chunk_a1, const int32_t *__restrict__ chunk_layer,
+    const float *__restrict__ Wp, const float *__restrict__ layer_c, const double *__restrict__ F, int nchunks,
+    int nlb, double *__restrict__ partial, uint32_t *__restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    UmmaSmem<N> &S = *reinterpret_cast<UmmaSmem<N> *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    constexpr uint32_t TCOLS = N < 32 ? 32 : N;
+    constexpr uint32_t IDESC = idesc_bf16(UM_M, N);
+    constexpr uint32_t A_LBO = (UM_M / 8) * 128, A_SBO = 128;
+    constexpr uint32_t B_LBO = (N / 8) * 128, B_SBO = 128;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int c = blockIdx.y;
+    const int s = blockIdx.z / nlb, lb = blockIdx.z % nlb;
+    const int t0 = blockIdx.x * UM_M;
+    const int a0 = chunk_a0[c], a1 = chunk_a1[c], L = chunk_layer[c];
+    const int l0 = lb * N;
+    const float4 kc = reinterpret_cast<const float4 *>(layer_c)[(size_t)s * nl + L];
+
+    if (tid == 0) {
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+        S.abort = 0;
+        fence_barrier_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(&S.tmem_base, TCOLS);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+
+    // producer roles: row (time step) and half of the 64-wide K stage
+    const int row = tid & (UM_M - 1), half = tid >> 7;
+    const int trow = min(t0 + row, steps - 1);
+    const float2 th = t_hilo[trow];
+    const int nkt = (a1 - a0) / UM_KT;
+    uint32_t phase_bits = 0;  // expected parity per stage
+    bool ok = true;
+
+    for (int kt = 0; kt < nkt; ++kt) {
+        const int b = kt & 1;
+        if (kt >= 2) {
+            if (!mbar_wait(&S.bar[b], (phase_bits >> b) & 1u)) ok = false;
+            phase_bits ^= 1u << b;
+            if (__syncthreads_or(!ok)) {
+                ok = false;
+                break;
+            }
+        }
+        const int abase = a0 + kt * UM_KT;
+        if (tid < UM_KT) S.at[b][tid] = at_hilo[abase + tid];
+        // B operand: W'[l][a] rows l (N), 64 a's; thread -> (row n, 8-wide K chunk)
+        for (int i = tid; i < N * (UM_KT / 8); i += UM_THREADS) {
+            const int n = i % N, kcn = i / N;
+            const int l = l0 + n;
+            float w[8];
+            if (l < nleads) {
+                const float4 *src = reinterpret_cast<const float4 *>(Wp + ((size_t)s * nleads + l) * apad + abase + kcn * 8);
+                const float4 p0 = __ldg(src), p1 = __ldg(src + 1);
+                w[0] = p0.x; w[1] = p0.y; w[2] = p0.z; w[3] = p0.w;
+                w[4] = p1.x; w[5] = p1.y; w[6] = p1.z; w[7] = p1.w;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) w[j] = 0.f;
+            }
+            uint4 hv, lv;
+            split2(w[0], w[1], hv.x, lv.x);
+            split2(w[2], w[3], hv.y, lv.y);
+            split2(w[4], w[5], hv.z, lv.z);
+            split2(w[6], w[7], hv.w, lv.w);
+            const uint32_t off = (uint32_t)((kcn * (N / 8) + n / 8) * 128 + (n % 8) * 16);
+            *reinterpret_cast<uint4 *>(S.b_hi[b] + off) = hv;
+            *reinterpret_cast<uint4 *>(S.b_lo[b] + off) = lv;
+        }
+        __syncthreads();  // S.at visible
+        // A operand: H_a(t) for this thread's row and 32 K columns
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int kc8 = half * 4 + j;
+            float hv8[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const float2 at = S.at[b][kc8 * 8 + e];
+                const float tau = (th.x - at.x) + (th.y - at.y);
+                hv8[e] = h_value(tau, kc);
+            }
+            uint4 hv, lv;
+            split2(hv8[0], hv8[1], hv.x, lv.x);
+            split2(hv8[2], hv8[3], hv.y, lv.y);
+            split2(hv8[4], hv8[5], hv.z, lv.z);
+            split2(hv8[6], hv8[7], hv.w, lv.w);
+            const uint32_t off = (uint32_t)((kc8 * (UM_M / 8) + row / 8) * 128 + (row % 8) * 16);
+            *reinterpret_cast<uint4 *>(S.a_hi[b] + off) = hv;
+            *reinterpret_cast<uint4 *>(S.a_lo[b] + off) = lv;
+        }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t ah = smem_u32(S.a_hi[b]), al = smem_u32(S.a_lo[b]);
+            const uint32_t bh = smem_u32(S.b_hi[b]), bl = smem_u32(S.b_lo[b]);
+#pragma unroll
+            for (int j = 0; j < UM_KT / 16; ++j) {
+                const uint64_t dah = sdesc(ah + j * 2 * A_LBO, A_LBO, A_SBO);
+                const uint64_t dal = sdesc(al + j * 2 * A_LBO, A_LBO, A_SBO);
+                const uint64_t dbh = sdesc(bh + j * 2 * B_LBO, B_LBO, B_SBO);
+                const uint64_t dbl = sdesc(bl + j * 2 * B_LBO, B_LBO, B_SBO);
+                mma_bf16(tmem, dah, dbh, IDESC, (kt > 0 || j > 0) ? 1u : 0u);
+                mma_bf16(tmem, dah, dbl, IDESC, 1u);
+                mma_bf16(tmem, dal, dbh, IDESC, 1u);
+            }
+            mma_commit(&S.bar[b]);
+        }
+    }
+    // wait for the last commit (MMAs complete in issue order)
+    if (nkt > 0) {
+        const int last = (nkt - 1) & 1;
+        // parity of the last use of stage `last`
+        const uint32_t par = (uint32_t)(((nkt - 1) >> 1) & 1);
+        if (!mbar_wait(&S.bar[last], par)) ok = false;
+    }
+    ok = !__syncthreads_or(!ok);
+    tc_fence_after();
+    if (ok && nkt > 0) {
+        // epilogue: warp quadrant q reads TMEM lanes 32q..32q+31, column half (warp >> 2)
+        const int q = warp & 3, ch = warp >> 2;
+        const int t = t0 + 32 * q + lane;
+        const double f = (t < steps) ? F[((size_t)s * nl + L) * steps + t] : 0.0;
+        for (int cb = ch * (N / 2); cb < (ch + 1) * (N / 2); cb += 8) {
+            if (N / 2 < 8 && ch == 1) break;
+            float v[8];
+            tmem_ld8(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)cb, v);
+            if (t < steps) {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const int l = l0 + cb + j;
+                    if (l < nleads)
+                        partial[(((size_t)s * nchunks + c) * nleads + l) * steps + t] = (double)v[j] * f;
+                }
+            }
+        }
+    } else if (!ok && tid == 0) {
+        atomicOr(err, KERR_MBAR_TIMEOUT);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, TCOLS);
+}
+
+template <int N>
+void launch_n(cudaStream_t st, const HeartDev &h, const float *d_Wp, const float *d_layer_c, const double *d_F,
+              int n_sims, double *d_partial, uint32_t *d_err) {
+    const int nlb = (h.nleads + N - 1) / N;
+    const size_t smem = sizeof(UmmaSmem<N>) + 1024;
+    static bool attr = false;
+    if (!attr) {
+        EKG_CUDA(cudaFuncSetAttribute(k_contract_umma<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr = true;
+    }
+    dim3 grid((unsigned)((h.steps + UM_M - 1) / UM_M), (unsigned)h.nchunks, (unsigned)(n_sims * nlb));
+    k_contract_umma<N><<<grid, UM_THREADS, smem, st>>>(h.steps, h.nleads, h.apad, h.nlayers, h.t_hilo.p, h.at_hilo.p,
+                                                       h.chunk_a0.p, h.chunk_a1.p, h.chunk_layer.p, d_Wp, d_layer_c,
+                                                       d_F, h.nchunks, nlb, d_partial, d_err);
+    EKG_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+// N (padded leads) chosen from the lead count: 16, 32, 64, 128 or 256 per lead block.
+void launch_contract_umma(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,
+                          const double *d_F, int n_sims, double *d_partial, uint32_t *d_err) {
+    if (h.nleads <= 16) launch_n<16>(s, h, d_Wp, d_layer_c, d_F, n_sims, d_partial, d_err);
+    else if (h.nleads <= 32) launch_n<32>(s, h, d_Wp, d_layer_c, d_F, n_sims, d_partial, d_err);
+    else if (h.nleads <= 64) launch_n<64>(s, h, d_Wp, d_layer_c, d_F, n_sims, d_partial, d_err);
+    else if (h.nleads <= 128) launch_n<128>(s, h, d_Wp, d_layer_c, d_F, n_sims, d_partial, d_err);
+    else launch_n<256>(s, h, d_Wp, d_layer_c, d_F, n_sims, d_partial, d_err);
+}
+
+}  // namespace ekg

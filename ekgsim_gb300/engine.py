@@ -1,0 +1,282 @@
+"""Python handles over the C ABI: Engine, Heart and Server.
+
+These wrap include/ekgsim.h one to one; numpy arrays cross the boundary as plain pointers.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import EkgError, check, dptr, i32ptr, i64ptr
+
+
+class Engine:
+    """One engine per process and GPU (ekg_engine_create)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = L.load()
+        h = ctypes.c_void_p()
+        check(self._lib.ekg_engine_create(device, ctypes.byref(h)))
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def free_bytes(self) -> int:
+        v = ctypes.c_uint64()
+        check(self._lib.ekg_engine_free_bytes(self._h, ctypes.byref(v)))
+        return int(v.value)
+
+    def close(self):
+        if self._h:
+            check(self._lib.ekg_engine_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Heart:
+    """A resident heart: activation times, de-duplicated APs and lead field live on the device."""
+
+    def __init__(self, engine: Engine, handle):
+        self.engine = engine
+        self._lib = engine._lib
+        self._h = handle
+        self.info = self._info()
+
+    @classmethod
+    def create(cls, engine: Engine, layers: np.ndarray, transfer: np.ndarray, leads_zyx: np.ndarray,
+               nhood: str = "3D4", start: float = 0.0, length: float = 600.0, dt: float = 1.0) -> "Heart":
+        layers = np.ascontiguousarray(layers, dtype=np.int32)
+        if layers.ndim == 2:
+            layers = layers[None]
+        transfer = np.ascontiguousarray(transfer, dtype=np.float64)
+        leads_zyx = np.ascontiguousarray(np.atleast_2d(leads_zyx), dtype=np.float64)
+        d = L.HeartDesc(layers.shape[0], layers.shape[1], layers.shape[2], i32ptr(layers), transfer.shape[0],
+                        dptr(transfer), leads_zyx.shape[0], dptr(leads_zyx), L.NHOOD[nhood], float(start),
+                        float(length), float(dt))
+        h = ctypes.c_void_p()
+        check(engine._lib.ekg_heart_create(engine.handle, ctypes.byref(d), ctypes.byref(h)))
+        heart = cls(engine, h)
+        heart.shape = layers.shape
+        return heart
+
+    @classmethod
+    def from_ini(cls, engine: Engine, ini_path: str, out_dir: Optional[str] = None) -> "Heart":
+        h = ctypes.c_void_p()
+        check(engine._lib.ekg_heart_from_ini(engine.handle, ini_path.encode(),
+                                             out_dir.encode() if out_dir else None, ctypes.byref(h)))
+        heart = cls(engine, h)
+        heart.shape = None
+        return heart
+
+    def _info(self) -> L.HeartInfo:
+        i = L.HeartInfo()
+        check(self._lib.ekg_heart_get_info(self._h, ctypes.byref(i)))
+        return i
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def n_leads(self) -> int:
+        return self.info.n_leads
+
+    @property
+    def steps(self) -> int:
+        return self.info.steps
+
+    def activation(self) -> np.ndarray:
+        out = np.zeros(self.info.n_cells, dtype=np.float64)
+        check(self._lib.ekg_heart_activation(self._h, dptr(out)))
+        return out.reshape(self.shape) if self.shape is not None else out
+
+    def ap_index(self) -> np.ndarray:
+        out = np.zeros(self.info.n_cells, dtype=np.int64)
+        check(self._lib.ekg_heart_ap_index(self._h, i64ptr(out)))
+        return out.reshape(self.shape) if self.shape is not None else out
+
+    def simulate(self, layer_k: np.ndarray, leads_zyx: Optional[np.ndarray] = None) -> np.ndarray:
+        """ECG [n_leads, steps] for the given layer APs (and optionally moved leads)."""
+        layer_k = np.ascontiguousarray(layer_k, dtype=np.float64)
+        if layer_k.shape != (self.info.n_layers, 9):
+            raise ValueError(f"layer_k must be ({self.info.n_layers}, 9)")
+        lp = None
+        if leads_zyx is not None:
+            lp = np.ascontiguousarray(leads_zyx, dtype=np.float64)
+            if lp.shape != (self.n_leads, 3):
+                raise ValueError(f"leads must be ({self.n_leads}, 3)")
+        out = np.zeros((self.n_leads, self.steps), dtype=np.float64)
+        check(self._lib.ekg_simulate(self._h, dptr(layer_k), dptr(lp), dptr(out)))
+        return out
+
+    def benchmark(self, layer_k: np.ndarray, leads_zyx: Optional[np.ndarray] = None, warmup: int = 3,
+                  iters: int = 10) -> dict:
+        """Device-only timing with resident inputs (ekg_heart_benchmark)."""
+        lk = np.ascontiguousarray(layer_k, dtype=np.float64)
+        n = lk.shape[0] if lk.ndim == 3 else 1
+        lp = None if leads_zyx is None else np.ascontiguousarray(leads_zyx, dtype=np.float64)
+        out = np.zeros(6)
+        check(self._lib.ekg_heart_benchmark(self._h, n, dptr(lk), dptr(lp), warmup, iters, dptr(out), 6))
+        return dict(total_ms=out[0], contract_ms=out[1], prep_ms=out[2], tail_ms=out[3], launches=int(out[4]),
+                    moved_leads=int(out[5]), iters=iters, n_sims=n)
+
+    # ------------------------------------------------------------------ evaluation
+    def set_eval(self, base_aps, k_min, k_max, free_k, targets, target_offsets=None, **kw):
+        """Evaluation settings (ekg_heart_set_eval); keyword arguments as ``eval_config``."""
+        self._cfg = eval_config(base_aps, k_min, k_max, free_k, targets, target_offsets, **kw)
+        check(self._lib.ekg_heart_set_eval(self._h, ctypes.byref(self._cfg)))
+
+    def eval_shape(self):
+        g, c = ctypes.c_int32(), ctypes.c_int32()
+        check(self._lib.ekg_eval_shape(self._h, ctypes.byref(g), ctypes.byref(c)))
+        return g.value, c.value
+
+    def gene_bounds(self):
+        g, _ = self.eval_shape()
+        lo, hi = np.zeros(g), np.zeros(g)
+        check(self._lib.ekg_eval_gene_bounds(self._h, dptr(lo), dptr(hi)))
+        return lo, hi
+
+    def eval(self, genes, want_ecg: bool = False):
+        """One evaluation: (criteria, violation[, ecg, layer_k, leads])."""
+        genes = np.ascontiguousarray(genes, dtype=np.float64)
+        ng, nc = self.eval_shape()
+        crit = np.zeros(nc)
+        viol = np.zeros(1)
+        ecg = np.zeros((self.n_leads, self.steps)) if want_ecg else None
+        lk = np.zeros((self.info.n_layers, 9)) if want_ecg else None
+        leads = np.zeros((self.n_leads, 3)) if want_ecg else None
+        check(self._lib.ekg_eval(self._h, dptr(genes), genes.size, dptr(crit), dptr(viol), dptr(ecg), dptr(lk),
+                                 dptr(leads)))
+        if want_ecg:
+            return crit, float(viol[0]), ecg, lk, leads
+        return crit, float(viol[0])
+
+    def eval_batch(self, genes: np.ndarray, want_ecg: bool = False):
+        genes = np.ascontiguousarray(np.atleast_2d(genes), dtype=np.float64)
+        n, g = genes.shape
+        _, nc = self.eval_shape()
+        crit = np.zeros((n, nc))
+        viol = np.zeros(n)
+        ecg = np.zeros((n, self.n_leads, self.steps)) if want_ecg else None
+        check(self._lib.ekg_eval_batch(self._h, n, dptr(genes), g, dptr(crit), dptr(viol), dptr(ecg)))
+        return (crit, viol, ecg) if want_ecg else (crit, viol)
+
+    def close(self):
+        if self._h:
+            check(self._lib.ekg_heart_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def eval_config(base_aps, k_min, k_max, free_k, targets=(np.zeros(1),), target_offsets=None,
+                interpolation="endo-mid-epi", mid_position=0.5, optimize_points=True, comparison_mode=2,
+                criteria_mode=1, peak=False, fast_is_criterion=False, fast_delay=0.0, fast_limit=2.0,
+                endo_epi_delay=-1.0, disp_min=(-50,), disp_max=(50,)):
+    """An ekg_eval_config plus the arrays it points into (kept alive in ``cfg._keep``)."""
+    keep = dict(
+        base=np.ascontiguousarray(np.atleast_2d(base_aps), dtype=np.float64),
+        kmin=np.ascontiguousarray(k_min, dtype=np.float64), kmax=np.ascontiguousarray(k_max, dtype=np.float64),
+        tl=np.array([len(t) for t in targets], dtype=np.int64),
+        tg=np.ascontiguousarray(np.concatenate([np.asarray(t, dtype=np.float64) for t in targets])),
+        to=np.ascontiguousarray(target_offsets if target_offsets is not None else np.zeros(len(targets)),
+                                dtype=np.float64),
+        dmin=np.ascontiguousarray(disp_min, dtype=np.float64), dmax=np.ascontiguousarray(disp_max, dtype=np.float64))
+    mask = 0
+    for f in free_k:
+        mask |= 1 << int(f)
+    k = keep
+    c = L.EvalConfig(1 if interpolation == "endo-epi" else 2, mid_position, k["base"].shape[0], dptr(k["base"]),
+                     dptr(k["kmin"]), dptr(k["kmax"]), mask, int(optimize_points), criteria_mode, comparison_mode,
+                     int(peak), int(fast_is_criterion), fast_delay, fast_limit, endo_epi_delay, len(targets),
+                     i64ptr(k["tl"]), dptr(k["tg"]), dptr(k["to"]), len(k["dmin"]), dptr(k["dmin"]),
+                     len(k["dmax"]), dptr(k["dmax"]))
+    c._keep = keep
+    return c
+
+
+def layer_aps(cfg, n_layers: int, wohlfart_genes) -> tuple:
+    """Layer APs [n_layers, 9] and violation from the Wohlfart genes (host only)."""
+    lib = L.load()
+    g = np.ascontiguousarray(wohlfart_genes, dtype=np.float64)
+    out = np.zeros((n_layers, 9))
+    v = np.zeros(1)
+    check(lib.ekg_layer_aps(ctypes.byref(cfg), n_layers, dptr(g), dptr(out), dptr(v)))
+    return out, float(v[0])
+
+
+def move_leads(orig_zyx: np.ndarray, disp_uv: Optional[np.ndarray]) -> np.ndarray:
+    lib = L.load()
+    o = np.ascontiguousarray(np.atleast_2d(orig_zyx), dtype=np.float64)
+    out = np.zeros_like(o)
+    d = None if disp_uv is None else np.ascontiguousarray(disp_uv, dtype=np.float64)
+    check(lib.ekg_move_leads(o.shape[0], dptr(o), dptr(d), dptr(out)))
+    return out
+
+
+class Server:
+    """Served form: request loop with continuous batching over resident hearts."""
+
+    def __init__(self, engine: Engine, max_batch: int = 256, max_wait_us: int = 200, hbm_reserve_bytes: int = 2 << 30):
+        self.engine = engine
+        self._lib = engine._lib
+        o = L.ServerOpts(max_batch, max_wait_us, hbm_reserve_bytes)
+        h = ctypes.c_void_p()
+        check(self._lib.ekg_server_create(engine.handle, ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+        self._hearts = {}
+
+    def add_heart(self, heart: Heart) -> int:
+        i = ctypes.c_int32()
+        check(self._lib.ekg_server_add_heart(self._h, heart.handle, ctypes.byref(i)))
+        self._hearts[i.value] = heart
+        return i.value
+
+    def submit(self, heart_id: int, genes) -> int:
+        g = np.ascontiguousarray(genes, dtype=np.float64)
+        rid = ctypes.c_uint64()
+        check(self._lib.ekg_server_submit(self._h, heart_id, dptr(g), g.size, ctypes.byref(rid)))
+        return rid.value
+
+    def poll(self, request_id: int, heart_id: int, wait_ms: int = 0, want_ecg: bool = False):
+        """(criteria, violation, ecg or None, stats dict) or None when not ready."""
+        heart = self._hearts[heart_id]
+        _, nc = heart.eval_shape()
+        crit = np.zeros(nc)
+        viol = np.zeros(1)
+        ecg = np.zeros((heart.n_leads, heart.steps)) if want_ecg else None
+        st = L.RequestStats()
+        rc = self._lib.ekg_server_poll(self._h, request_id, wait_ms, dptr(crit), dptr(viol), dptr(ecg),
+                                       ctypes.byref(st))
+        if rc == -10:
+            return None
+        check(rc)
+        return crit, float(viol[0]), ecg, dict(queue_ms=st.queue_ms, total_ms=st.total_ms, batch=st.batch_size)
+
+    def close(self):
+        if self._h:
+            check(self._lib.ekg_server_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

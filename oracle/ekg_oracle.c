@@ -614,3 +614,68 @@ double ekgo_clamp(double c) {
     if ((c < 0) || !isfinite(c) || !isnormal(c)) return 2e10;
     return c;
 }
+
+/* ------------------------------------------------------ reference-cost CPU baseline */
+/*
+ * Simulation::run with the reference's own cost structure (simlib/simulator.cpp:452-550): every
+ * cell AP and every neighbour AP is evaluated in place, once per step, exactly as the reference
+ * does (about nine Wohlfart evaluations per voxel-step), single-threaded, including the apIndex
+ * build (setApIndices, :561-621).  Used only to time the CPU baseline; results are bit-identical
+ * to ekgo_run.  `steps_limit` > 0 runs only the first steps_limit steps (a bounded sample).
+ */
+int ekgo_run_naive(int nz, int ny, int nx, const int32_t *layer, const double *at, int nlayers,
+                   const double *layer_k, int nlead, const double *lead_zyx, int nhood_code, double start,
+                   double length, double dt, int steps_limit, double *ecg) {
+    int64_t n = (int64_t)nz * ny * nx;
+    int64_t steps = (int64_t)ceil(length / dt);
+    if (steps_limit > 0 && steps_limit < steps) steps = steps_limit;
+    int64_t *api = (int64_t *)malloc((size_t)n * sizeof(int64_t));
+    int32_t *apl = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    double *apat = (double *)malloc((size_t)n * sizeof(double));
+    int64_t na = ekgo_ap_indices(n, layer, at, api, apl, apat);
+    ap_t *aps = (ap_t *)malloc((size_t)(na ? na : 1) * sizeof(ap_t));
+    for (int64_t a = 0; a < na; ++a) ap_init(&aps[a], layer_k + 9 * (apl[a] - 1), apat[a]);
+    int dif[26 * 3];
+    int nnb = ekgo_neighbourhood(nhood_code, dif);
+    double *cell = (double *)malloc((size_t)steps * sizeof(double));
+    double *dip = (double *)malloc((size_t)steps * 3 * sizeof(double));
+    for (int64_t i = 0; i < (int64_t)nlead * steps; ++i) ecg[i] = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        if (layer[i] <= 0) continue;
+        int64_t z = i / ((int64_t)ny * nx), y = (i / nx) % ny, x = i % nx;
+        const ap_t *ap = &aps[api[i]];
+        double st = start;
+        for (int64_t k = 0; k < steps; ++k) { cell[k] = ap_eval(ap, st); st += dt; }
+        for (int64_t k = 0; k < 3 * steps; ++k) dip[k] = 0.0;
+        for (int q = 0; q < nnb; ++q) {
+            int64_t z2 = z - dif[3 * q], y2 = y - dif[3 * q + 1], x2 = x - dif[3 * q + 2];
+            if (z2 < 0 || z2 >= nz || y2 < 0 || y2 >= ny || x2 < 0 || x2 >= nx) continue;
+            int64_t j = (z2 * ny + y2) * nx + x2;
+            if (layer[j] <= 0) continue;
+            const ap_t *ap2 = &aps[api[j]];
+            double st2 = start;
+            for (int64_t k = 0; k < steps; ++k) {
+                double vd = ap_eval(ap2, st2) - cell[k];
+                dip[3 * k + 0] += (double)dif[3 * q + 0] * vd;
+                dip[3 * k + 1] += (double)dif[3 * q + 1] * vd;
+                dip[3 * k + 2] += (double)dif[3 * q + 2] * vd;
+                st2 += dt;
+            }
+        }
+        for (int l = 0; l < nlead; ++l) {
+            double m0 = lead_zyx[3 * l + 0] - (double)(z + 1);
+            double m1 = lead_zyx[3 * l + 1] - (double)(y + 1);
+            double m2 = lead_zyx[3 * l + 2] - (double)(x + 1);
+            double s = m0 * m0; s += m1 * m1; s += m2 * m2;
+            double f = 1.0 / (s * sqrt(s));
+            m0 *= f; m1 *= f; m2 *= f;
+            for (int64_t k = 0; k < steps; ++k) {
+                double r = 0.0;
+                r += m0 * dip[3 * k]; r += m1 * dip[3 * k + 1]; r += m2 * dip[3 * k + 2];
+                ecg[l * steps + k] += r;
+            }
+        }
+    }
+    free(dip); free(cell); free(aps); free(apat); free(apl); free(api);
+    return EKGO_OK;
+}

@@ -16,6 +16,7 @@ from __future__ import annotations
 import ctypes
 import math
 import os
+import platform
 import subprocess
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional
@@ -23,7 +24,7 @@ from typing import Dict, List, Optional
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-_LIB_PATH = os.path.join(_HERE, "_build", "libekg_oracle.so")
+_LIB_PATH = os.path.join(_HERE, "_build", platform.machine(), "libekg_oracle.so")
 _lib = None
 
 
@@ -49,6 +50,8 @@ def lib():
         L.ekgo_activation.argtypes = [ctypes.c_int] * 3 + [P(i32), ctypes.c_int, P(d), P(d), P(i32)]
         L.ekgo_run.argtypes = [ctypes.c_int] * 3 + [P(i32), P(d), ctypes.c_int, P(d), ctypes.c_int, P(d),
                                                     ctypes.c_int, d, d, d, P(d), ctypes.c_int]
+        L.ekgo_run_naive.argtypes = [ctypes.c_int] * 3 + [P(i32), P(d), ctypes.c_int, P(d), ctypes.c_int, P(d),
+                                                          ctypes.c_int, d, d, d, ctypes.c_int, P(d)]
         L.ekgo_ap_indices.argtypes = [i64, P(i32), P(d), P(i64), P(i32), P(d)]
         L.ekgo_ap_indices.restype = i64
         L.ekgo_layer_aps.argtypes = [ctypes.c_int, ctypes.c_int, P(d), P(d), P(d), ctypes.c_uint,
@@ -115,6 +118,25 @@ def run(layer: np.ndarray, at: np.ndarray, layer_k: np.ndarray, leads_zyx: np.nd
                         NHOOD[nhood], float(start), float(length), float(dt), _p(ecg, ctypes.c_double), threads)
     if rc != 0:
         raise RuntimeError(f"oracle run error {rc}")
+    return ecg
+
+
+def run_naive(layer, at, layer_k, leads_zyx, nhood="3D4", start=0.0, length=600.0, dt=1.0, steps_limit=0):
+    """ECG with the reference's per-voxel AP evaluation cost (single thread), optionally only the
+    first ``steps_limit`` steps."""
+    layer = np.ascontiguousarray(layer, dtype=np.int32)
+    at = np.ascontiguousarray(at, dtype=np.float64)
+    layer_k = np.ascontiguousarray(layer_k, dtype=np.float64)
+    leads_zyx = np.ascontiguousarray(np.atleast_2d(leads_zyx), dtype=np.float64)
+    steps = int(math.ceil(length / dt))
+    if 0 < steps_limit < steps:
+        steps = steps_limit
+    ecg = np.zeros((leads_zyx.shape[0], steps), dtype=np.float64)
+    nz, ny, nx = layer.shape
+    lib().ekgo_run_naive(nz, ny, nx, _p(layer, ctypes.c_int32), _p(at, ctypes.c_double), layer_k.shape[0],
+                         _p(layer_k, ctypes.c_double), leads_zyx.shape[0], _p(leads_zyx, ctypes.c_double),
+                         NHOOD[nhood], float(start), float(length), float(dt), int(steps_limit),
+                         _p(ecg, ctypes.c_double))
     return ecg
 
 

@@ -1,0 +1,221 @@
+"""GPU parity: the engine (through the C ABI) against the FP64 oracle.
+
+Bars: activation times bit-exact (FP64 equality); ECG relative L2 over leads x steps <= 1e-4
+(the FP32-AP / BF16 hi+lo contraction tolerance); criteria within 1e-4 absolute of the oracle's.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from ekgsim_gb300 import synth
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+ECG_TOL = 1e-4
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def make_heart(engine, spec, steps=300, nhood="3D4", start=0.0, dt=1.0):
+    from ekgsim_gb300.engine import Heart
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    rng = np.random.Generator(np.random.PCG64(spec.seed))
+    leads_zyx = synth.leads(spec, rng)[:, ::-1].copy()
+    h = Heart.create(engine, grid, tm, leads_zyx, nhood, start, steps * dt, dt)
+    return h, grid, tm, leads_zyx
+
+
+def layer_k_for(spec, request=0):
+    g = synth.genes_for(spec, request, 0)
+    lk, _, _ = O.layer_aps(spec.n_layers, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8],
+                           "endo-mid-epi", 0.6, g[:12])
+    return lk
+
+
+@pytest.mark.parametrize("n", [8, 16, 24, 40, 64])
+def test_activation_bit_exact(engine, n):
+    spec = synth.small_spec(n) if n < 64 else synth.config(0)["spec"]
+    h, grid, tm, _ = make_heart(engine, spec, steps=10)
+    at_ref, _ = O.activation(grid, tm)
+    at = h.activation()
+    assert np.array_equal(at.view(np.int64), at_ref.view(np.int64))
+    idx_ref, _, _ = O.ap_indices(np.abs(grid), at_ref)
+    assert np.array_equal(h.ap_index().ravel(), idx_ref)
+    assert h.info.n_aps == idx_ref.max() + 1
+
+
+def test_activation_bit_exact_128(engine):
+    spec = synth.config(1)["spec"]
+    h, grid, tm, _ = make_heart(engine, spec, steps=10)
+    at_ref, _ = O.activation(grid, tm)
+    assert np.array_equal(h.activation().view(np.int64), at_ref.view(np.int64))
+
+
+def test_activation_unreachable_and_multilayer(engine):
+    # two separate blobs, stimulus only in one; 5 layers with mixed delays
+    rng = np.random.Generator(np.random.PCG64(5))
+    g = np.zeros((20, 22, 18), dtype=np.int32)
+    g[2:9, 3:12, 2:10] = rng.integers(1, 6, size=(7, 9, 8))
+    g[12:18, 10:20, 8:16] = rng.integers(1, 6, size=(6, 10, 8))
+    g[3, 4, 3] = -abs(g[3, 4, 3])
+    tm = np.full((12, 12), -1.0)
+    tm[1:6, 1:6] = rng.integers(1, 4, size=(5, 5)).astype(float) * 0.5
+    from ekgsim_gb300.engine import Heart
+    h = Heart.create(engine, g, tm, np.array([[40.0, 40.0, 40.0]]), "3D4", 0.0, 50.0, 1.0)
+    at_ref, _ = O.activation(g, tm)
+    at = h.activation()
+    assert np.array_equal(at.view(np.int64), at_ref.view(np.int64))
+    assert (at[12:18, 10:20, 8:16] == 0).all()
+
+
+def test_activation_2d_grid(engine):
+    spec = synth.small_spec(32)
+    grid = synth.ellipsoid_heart(spec)[16:17].copy()
+    grid[0][grid[0] != 0] = np.abs(grid[0][grid[0] != 0])
+    nz = np.argwhere(grid[0] == 1)
+    grid[0, nz[0][0], nz[0][1]] = -1
+    tm = synth.transfer_matrix(3, [1, 2, 2])
+    from ekgsim_gb300.engine import Heart
+    h = Heart.create(engine, grid, tm, np.array([[0.0, 40.0, 40.0]]), "2D8", 0.0, 50.0, 1.0)
+    at_ref, layer = O.activation(grid, tm)
+    assert np.array_equal(h.activation().view(np.int64), at_ref.view(np.int64))
+    lk = layer_k_for(spec)
+    ecg = h.simulate(lk)
+    ref = O.run(layer, at_ref, lk, np.array([[0.0, 40.0, 40.0]]), "2D8", 0.0, 50.0, 1.0)
+    assert rel_l2(ecg, ref) <= ECG_TOL
+
+
+@pytest.mark.parametrize("nhood", ["3D4", "cube", "2D4", "2D8"])
+def test_ecg_neighbourhoods(engine, nhood):
+    spec = synth.small_spec(24, n_leads=3)
+    h, grid, tm, leads = make_heart(engine, spec, steps=250, nhood=nhood)
+    at, layer = O.activation(grid, tm)
+    lk = layer_k_for(spec, 1)
+    ecg = h.simulate(lk)
+    ref = O.run(layer, at, lk, leads, nhood, 0.0, 250.0, 1.0)
+    assert rel_l2(ecg, ref) <= ECG_TOL
+
+
+def test_ecg_64_full(engine):
+    c = synth.config(0)
+    spec = c["spec"]
+    h, grid, tm, leads = make_heart(engine, spec, steps=c["steps"])
+    at, layer = O.activation(grid, tm)
+    for req in range(3):
+        g = synth.genes_for(spec, req, 0)
+        lk = layer_k_for(spec, req)
+        moved = O.move_leads(leads, g[12:16].reshape(2, 2))
+        ecg = h.simulate(lk, moved)
+        ref = O.run(layer, at, lk, moved, "3D4", 0.0, float(c["steps"]), 1.0)
+        assert rel_l2(ecg, ref) <= ECG_TOL, req
+
+
+def test_ecg_k0_offsets_and_start(engine):
+    """Distinct k0 per layer leave a constant term; start != 0 and dt = 0.5 shift the time axis."""
+    spec = synth.small_spec(24, n_leads=2)
+    h, grid, tm, leads = make_heart(engine, spec, steps=240, start=100.0, dt=0.5)
+    at, layer = O.activation(grid, tm)
+    lk = layer_k_for(spec, 2)
+    lk[:, 0] = [-86.0, -80.0, -90.0]
+    ecg = h.simulate(lk)
+    ref = O.run(layer, at, lk, leads, "3D4", 100.0, 120.0, 0.5)
+    assert rel_l2(ecg, ref) <= ECG_TOL
+
+
+def _workload(tmp_path, cfg_index, target=None):
+    c = synth.config(cfg_index)
+    return synth.make_workload(str(tmp_path), c["spec"], c["steps"], target=target), c
+
+
+def test_eval_matches_oracle_64(engine, tmp_path):
+    from ekgsim_gb300.engine import Heart
+    w, c = _workload(tmp_path, 0)
+    s = O.load_setup(str(tmp_path))
+    h = Heart.from_ini(engine, os.path.join(str(tmp_path), "simulator.ini"))
+    for req in range(2):
+        g = synth.genes_for(c["spec"], req, 0)
+        crit_ref, viol_ref, ecg_ref, lk_ref, leads_ref = O.evaluate(s, g)
+        crit, viol, ecg, lk, leads = h.eval(g, want_ecg=True)
+        assert np.array_equal(lk, lk_ref)
+        assert np.array_equal(leads, leads_ref)
+        assert viol == viol_ref
+        assert rel_l2(ecg, ecg_ref) <= ECG_TOL
+        assert np.allclose(crit, crit_ref, rtol=0, atol=1e-4)
+
+
+def test_batch_matches_single(engine, tmp_path):
+    from ekgsim_gb300.engine import Heart
+    w, c = _workload(tmp_path, 0)
+    h = Heart.from_ini(engine, os.path.join(str(tmp_path), "simulator.ini"))
+    genes = np.stack([synth.genes_for(c["spec"], r, 0) for r in range(5)])
+    crit_b, viol_b, ecg_b = h.eval_batch(genes, want_ecg=True)
+    for i in range(5):
+        crit, viol, ecg, _, _ = h.eval(genes[i], want_ecg=True)
+        assert np.allclose(ecg_b[i], ecg, rtol=0, atol=1e-9 * np.abs(ecg).max())
+        assert np.allclose(crit_b[i], crit, rtol=0, atol=1e-9)
+        assert viol_b[i] == viol
+
+
+def test_eval_128_twelve_leads(engine, tmp_path):
+    from ekgsim_gb300.engine import Heart
+    w, c = _workload(tmp_path, 1)
+    s = O.load_setup(str(tmp_path))
+    h = Heart.from_ini(engine, os.path.join(str(tmp_path), "simulator.ini"))
+    g = synth.genes_for(c["spec"], 1, 1)
+    crit_ref, viol_ref, ecg_ref, _, _ = O.evaluate(s, g)
+    crit, viol, ecg, _, _ = h.eval(g, want_ecg=True)
+    assert ecg.shape == (12, 600)
+    assert rel_l2(ecg, ecg_ref) <= ECG_TOL
+    assert np.allclose(crit, crit_ref, rtol=0, atol=1e-4)
+
+
+def test_bad_inputs(engine, tmp_path):
+    from ekgsim_gb300.engine import EkgError, Heart
+    spec = synth.small_spec(16)
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(3, [1, 2, 2])
+    with pytest.raises(EkgError) as e:
+        Heart.create(engine, np.abs(grid), tm, np.array([[30.0, 30, 30]]))
+    assert e.value.code == -6  # no stimulus voxel
+    with pytest.raises(EkgError) as e:
+        Heart.create(engine, grid, tm[:3, :3], np.array([[30.0, 30, 30]]))
+    assert e.value.code == -7  # conduction matrix misses layer 3
+    w, c = _workload(tmp_path, 0)
+    h = Heart.from_ini(engine, os.path.join(str(tmp_path), "simulator.ini"))
+    with pytest.raises(EkgError):
+        h.eval(np.zeros(5))
+    g = synth.genes_for(c["spec"], 0, 0)
+    g[3] = np.nan
+    with pytest.raises(EkgError):
+        h.eval(g)
+
+
+def test_contract_kernels_agree(tmp_path):
+    """The tensor-core and CUDA-core contractions give the same ECG within the split tolerance."""
+    from ekgsim_gb300.engine import Engine, Heart
+    spec = synth.config(0)["spec"]
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    lk = layer_k_for(spec, 3)
+    out = {}
+    for impl in ("umma", "cuda"):
+        os.environ["EKG_CONTRACT"] = impl
+        try:
+            e = Engine(0)
+            h = Heart.create(e, grid, tm, leads, "3D4", 0.0, 600.0, 1.0)
+            out[impl] = h.simulate(lk)
+            h.close()
+            e.close()
+        finally:
+            os.environ.pop("EKG_CONTRACT", None)
+    at, layer = O.activation(grid, tm)
+    ref = O.run(layer, at, lk, leads, "3D4", 0.0, 600.0, 1.0)
+    assert rel_l2(out["umma"], ref) <= ECG_TOL
+    assert rel_l2(out["cuda"], ref) <= ECG_TOL
+    assert rel_l2(out["umma"], out["cuda"]) <= ECG_TOL
