@@ -1,0 +1,451 @@
+// batch.cu -- the batched form: many parameter vectors on one resident heart.
+//
+// Within a batch every simulation shares the heart (activation times, de-duplicated APs) and the
+// per-layer AP shape coefficients k1 and k4, which the genes never change (they are interpolated
+// between base APs, sim.cpp:705-709, and left alone by the steepest-descent fit, whose step vector
+// is zero for them, sim.cpp:873-874).  With tau = t - at_a the cell AP factors as
+//     AP_a(t) - k0 = F_L(t) exp(k5 at_a) [(1 - k3) B1_a(t) + k3 B2_a(t)],
+//     B1_a(t) = sigma(k1 tau) exp(-k4 tau),   B2_a(t) = sigma(k1 tau),
+// where only F_L (per layer and step), k5 and k3 depend on the simulation.  Hence:
+//
+// * Leads at their loaded position (the same lead field W0 for every simulation): exp(k5 at) is
+//   expanded around the layer's mid activation time c_L, with u_a = (at_a - c_L)/s_L in [-1, 1]:
+//       exp(k5 at_a) = exp(k5 c_L) sum_{j<J} (k5 s_L)^j / j! u_a^j   (truncation bound <= 1e-12),
+//   so per heart the basis Q_{b,L,j}[l,t] = sum_{a in L} W0[l,a] u_a^j B_b,a(t) is contracted once
+//   (tensor cores, ecg path), and each simulation's static-lead ECG is a short FP64 combination.
+// * Moved leads (lead genes): one GEMM per batch on the tensor cores,
+//       Y_b[(s,l), t] = sum_{a in L} W'_s[l,a] B_b,a(t),   W'_s = W_s exp(k5_s at_a),
+//   with M = 128 steps, N = 256 (or 128) rows (simulation, moved lead), K = APs of one layer.
+//   The B operand W' is written per batch in BF16 hi+lo, already tiled in the UMMA canonical
+//   layout, and streamed into shared memory with 1-D bulk copies (TMA engine, mbarrier tx
+//   counts); the A operand B_b,a(t) is evaluated by all 256 threads in FP32 per K stage.  The
+//   epilogue forms ((1-k3) Y1 + k3 Y2) F_L(t) per row in FP64.  With a batch-uniform k3 the two
+//   bases collapse into one (N = 256, three MMAs per K step instead of six).
+#include <cmath>
+#include <cstdio>
+
+#include "ekg_internal.h"
+#include "umma_ptx.h"
+
+namespace ekg {
+
+using namespace ptx;
+
+namespace {
+
+constexpr int BM = 128, BKT = 64, BTHREADS = 256;
+
+__device__ __forceinline__ float ex2a(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcpa(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ void split2(float x0, float x1, uint32_t &hi, uint32_t &lo) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+    const float r0 = x0 - __bfloat162float(h.x), r1 = x1 - __bfloat162float(h.y);
+    __nv_bfloat162 l = __floats2bfloat162_rn(r0, r1);
+    hi = *reinterpret_cast<uint32_t *>(&h);
+    lo = *reinterpret_cast<uint32_t *>(&l);
+}
+
+// ------------------------------------------------------------------ Taylor basis weights
+// Wt[(l*J + j)][a] = W0[l][a] * u_a^j, u_a = (at_a - c_L) / s_L  (0 for padding APs)
+__global__ void k_taylor_w(int64_t apad, int nleads, int J, const float *__restrict__ W0,
+                           const double *__restrict__ at, const int32_t *__restrict__ a_layer,
+                           const double *__restrict__ centre, const double *__restrict__ scale, float *__restrict__ Wt) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int l = blockIdx.y;
+    if (a >= apad) return;
+    const double aa = at[a];
+    const int L = a_layer[a];
+    const double u = isinf(aa) ? 0.0 : (aa - centre[L]) / scale[L];
+    const float w = W0[(size_t)l * apad + a];
+    double p = 1.0;
+    for (int j = 0; j < J; ++j) {
+        Wt[((size_t)l * J + j) * apad + a] = isinf(aa) ? 0.f : (float)((double)w * p);
+        p *= u;
+    }
+}
+
+// Q[L][row][t] = sum over the chunks of layer L of partial[c][row][t] (chunks of a layer are
+// contiguous, [lc0[L], lc1[L])); block per (row, 32 steps), warps split chunks, fixed order.
+__global__ void k_reduce_layers(int steps, int rows, int nl, const int32_t *__restrict__ lc0,
+                                const int32_t *__restrict__ lc1, const double *__restrict__ partial,
+                                double *__restrict__ Q) {
+    __shared__ double red[8][33];
+    const int tt = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int w = threadIdx.x >> 5;
+    const int row = blockIdx.y;
+    for (int L = 0; L < nl; ++L) {
+        double acc = 0.0;
+        if (tt < steps)
+            for (int c = lc0[L] + w; c < lc1[L]; c += 8) acc += partial[((size_t)c * rows + row) * steps + tt];
+        red[w][threadIdx.x & 31] = acc;
+        __syncthreads();
+        if (w == 0 && tt < steps) {
+            double r = 0.0;
+            for (int i = 0; i < 8; ++i) r += red[i][threadIdx.x];
+            Q[((size_t)L * rows + row) * steps + tt] = r;
+        }
+        __syncthreads();
+    }
+}
+
+// Static leads: ecg[s][l][t] = sum_L F[s][L][t] sum_j coef[s][L][j] ((1-k3) Q1 + k3 Q2)[L][l*J+j][t]
+__global__ void k_static_combine(int steps, int nleads, int nl, int J, int Jb, int nmove, int n_sims,
+                                 const double *__restrict__ F, const double *__restrict__ coef,
+                                 const double *__restrict__ k3, const double *__restrict__ Q1,
+                                 const double *__restrict__ Q2, double *__restrict__ ecg) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int l = nmove + blockIdx.y, s = blockIdx.z;
+    if (t >= steps || l >= nleads) return;
+    const int rows = nleads * Jb;  // the basis stores Jb terms per lead
+    double acc = 0.0;
+    for (int L = 0; L < nl; ++L) {
+        const double kk = k3[(size_t)s * nl + L];
+        const double *c = coef + ((size_t)s * nl + L) * J;
+        double v = 0.0;
+        for (int j = 0; j < J; ++j) {
+            const size_t q = ((size_t)L * rows + (size_t)l * Jb + j) * steps + t;
+            v += c[j] * ((1.0 - kk) * Q1[q] + kk * Q2[q]);
+        }
+        acc += F[((size_t)s * nl + L) * steps + t] * v;
+    }
+    ecg[((size_t)s * nleads + l) * steps + t] = acc;
+}
+
+// ------------------------------------------------------------------ moved-lead operand
+// W'_s[l][a] for the moved leads l < nmove, written as BF16 hi/lo into the tiled B layout:
+// [N tile][K tile][part hi/lo][N*128 bytes], element (row n, k) of a tile at byte
+// ((k/8) * (N/8) + n/8) * 128 + (n%8) * 16 + (k%8) * 2.  One thread per (AP a, simulation s).
+template <int N>
+__global__ void k_batch_lead_field(int64_t apad, int nkt, const int64_t *__restrict__ a_vox_begin,
+                                   const int32_t *__restrict__ vox_zyx, const uint32_t *__restrict__ nb_in,
+                                   const uint32_t *__restrict__ nb_out, int nnb, const int8_t *__restrict__ difs,
+                                   const double *__restrict__ at, const int32_t *__restrict__ a_layer,
+                                   const double *__restrict__ layer_k, int nl, const double *__restrict__ leads,
+                                   int nleads, int nmove, uint8_t *__restrict__ Bt) {
+    __shared__ int8_t s_dif[26 * 3];
+    if (threadIdx.x < nnb * 3) s_dif[threadIdx.x] = difs[threadIdx.x];
+    __syncthreads();
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int s = blockIdx.y;
+    if (a >= apad) return;
+    const double aa = at[a];
+    const bool pad = isinf(aa);
+    const float e = pad ? 0.f : expf((float)(layer_k[((size_t)s * nl + a_layer[a]) * 9 + 5] * aa));
+    const int64_t v0 = a_vox_begin[a], v1 = a_vox_begin[a + 1];
+    const int kt = (int)(a / BKT), k = (int)(a % BKT);
+    for (int l = 0; l < nmove; ++l) {
+        const double *r = leads + ((size_t)s * nleads + l) * 3;
+        const float rz = (float)r[0], ry = (float)r[1], rx = (float)r[2];
+        const float rzl = (float)(r[0] - (double)rz), ryl = (float)(r[1] - (double)ry), rxl = (float)(r[2] - (double)rx);
+        double acc = 0.0;
+        for (int64_t v = v0; v < v1; ++v) {
+            const int32_t p = vox_zyx[v];
+            const float pz = (float)((p >> 20) + 1), py = (float)(((p >> 10) & 1023) + 1), px = (float)((p & 1023) + 1);
+            const uint32_t mi = nb_in[v], mo = nb_out[v];
+            float w = 0.f, sz = 0.f, sy = 0.f, sx = 0.f;
+            for (int n = 0; n < nnb; ++n) {
+                const float dz = s_dif[3 * n], dy = s_dif[3 * n + 1], dx = s_dif[3 * n + 2];
+                if (mi & (1u << n)) {
+                    const float mz = (rz - (pz + dz)) + rzl, my = (ry - (py + dy)) + ryl, mx = (rx - (px + dx)) + rxl;
+                    const float ss = fmaf(mz, mz, fmaf(my, my, mx * mx));
+                    const float rs = rsqrtf(ss);
+                    w = fmaf(rs * rs * rs, fmaf(mz, dz, fmaf(my, dy, mx * dx)), w);
+                }
+                if (mo & (1u << n)) {
+                    sz += dz;
+                    sy += dy;
+                    sx += dx;
+                }
+            }
+            if (mo) {
+                const float mz = (rz - pz) + rzl, my = (ry - py) + ryl, mx = (rx - px) + rxl;
+                const float ss = fmaf(mz, mz, fmaf(my, my, mx * mx));
+                const float rs = rsqrtf(ss);
+                w = fmaf(-(rs * rs * rs), fmaf(mz, sz, fmaf(my, sy, mx * sx)), w);
+            }
+            acc += (double)w;
+        }
+        const float wv = pad ? 0.f : (float)acc * e;
+        const __nv_bfloat16 hi = __float2bfloat16_rn(wv);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(wv - __bfloat162float(hi));
+        const int row = s * nmove + l;
+        const int nt = row / N, n = row % N;
+        const size_t tile = ((size_t)nt * nkt + kt) * 2;
+        const size_t off = (size_t)((k / 8) * (N / 8) + n / 8) * 128 + (n % 8) * 16 + (k % 8) * 2;
+        *reinterpret_cast<__nv_bfloat16 *>(Bt + tile * (N * 128) + off) = hi;
+        *reinterpret_cast<__nv_bfloat16 *>(Bt + (tile + 1) * (N * 128) + off) = lo;
+    }
+}
+
+// ------------------------------------------------------------------ batch GEMM
+template <int NB, int N>
+struct BatchSmem {
+    alignas(1024) uint8_t a[2][NB][2][BM * BKT * 2];  // [stage][basis][hi/lo]
+    alignas(1024) uint8_t b[2][2][N * BKT * 2];       // [stage][hi/lo]
+    float2 at[2][BKT];
+    alignas(8) uint64_t full[2];
+    alignas(8) uint64_t done[2];
+    uint32_t tmem_base;
+};
+
+// grid (t tiles, N tiles, K chunks).  Chunk c covers K tiles [ck0[c], ck1[c]) inside layer cl[c].
+template <int NB, int N>
+__global__ void __launch_bounds__(BTHREADS, 1) k_batch_umma(
+    int steps, int nl, int nkt, int rows, int nmove, int n_sims, const float2 *__restrict__ t_hilo,
+    const float2 *__restrict__ at_hilo, const int32_t *__restrict__ ck0, const int32_t *__restrict__ ck1,
+    const int32_t *__restrict__ cl, const float4 *__restrict__ hconst, const double *__restrict__ k3,
+    const double *__restrict__ F, const uint8_t *__restrict__ Bt, double *__restrict__ partial,
+    uint32_t *__restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    BatchSmem<NB, N> &S =
+        *reinterpret_cast<BatchSmem<NB, N> *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    constexpr uint32_t TCOLS = NB * N;  // 256
+    constexpr uint32_t IDESC = idesc_bf16(BM, N);
+    constexpr uint32_t A_LBO = (BM / 8) * 128, A_SBO = 128;
+    constexpr uint32_t B_LBO = (N / 8) * 128, B_SBO = 128;
+    constexpr uint32_t BPART = N * BKT * 2;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int t0 = blockIdx.x * BM, nt = blockIdx.y, c = blockIdx.z;
+    const int kt0 = ck0[c], kt1 = ck1[c], L = cl[c];
+    const float4 hc = hconst[L];  // k1*log2e, k4*log2e, 1-k3, k3 (the last two unused with two bases)
+
+    if (tid == 0) {
+        mbar_init(&S.full[0], 1);
+        mbar_init(&S.full[1], 1);
+        mbar_init(&S.done[0], 1);
+        mbar_init(&S.done[1], 1);
+        fence_barrier_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(&S.tmem_base, TCOLS);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+
+    const int row = tid & (BM - 1), half = tid >> 7;
+    const float2 th = t_hilo[min(t0 + row, steps - 1)];
+    const int nk = kt1 - kt0;
+    bool ok = true;
+    for (int i = 0; i < nk; ++i) {
+        const int b = i & 1;
+        const int kt = kt0 + i;
+        if (i >= 2) {
+            if (!mbar_wait(&S.done[b], (uint32_t)(((i >> 1) + 1) & 1))) ok = false;
+            if (__syncthreads_or(!ok)) {
+                ok = false;
+                break;
+            }
+        }
+        if (tid == 0) {
+            const uint8_t *src = Bt + ((size_t)nt * nkt + kt) * 2 * BPART;
+            mbar_expect_tx(&S.full[b], 2 * BPART);
+            bulk_g2s(S.b[b][0], src, BPART, &S.full[b]);
+            bulk_g2s(S.b[b][1], src + BPART, BPART, &S.full[b]);
+        }
+        if (tid < BKT) S.at[b][tid] = at_hilo[(size_t)kt * BKT + tid];
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int kc8 = half * 4 + j;
+            float v1[8], v2[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const float2 at = S.at[b][kc8 * 8 + e];
+                const float tau = (th.x - at.x) + (th.y - at.y);
+                const float e1 = ex2a(-hc.x * tau);
+                const float sg = rcpa(1.0f + e1);
+                const float e4 = ex2a(-hc.y * tau);
+                if (NB == 1) {
+                    const float h = sg * fmaf(hc.z, e4, hc.w);
+                    v1[e] = sg == 0.f ? 0.f : h;
+                } else {
+                    const float h = sg * e4;
+                    v1[e] = sg == 0.f ? 0.f : h;
+                    v2[e] = sg;
+                }
+            }
+            const uint32_t off = (uint32_t)((kc8 * (BM / 8) + row / 8) * 128 + (row % 8) * 16);
+            uint4 hv, lv;
+            split2(v1[0], v1[1], hv.x, lv.x);
+            split2(v1[2], v1[3], hv.y, lv.y);
+            split2(v1[4], v1[5], hv.z, lv.z);
+            split2(v1[6], v1[7], hv.w, lv.w);
+            *reinterpret_cast<uint4 *>(S.a[b][0][0] + off) = hv;
+            *reinterpret_cast<uint4 *>(S.a[b][0][1] + off) = lv;
+            if (NB == 2) {
+                split2(v2[0], v2[1], hv.x, lv.x);
+                split2(v2[2], v2[3], hv.y, lv.y);
+                split2(v2[4], v2[5], hv.z, lv.z);
+                split2(v2[6], v2[7], hv.w, lv.w);
+                *reinterpret_cast<uint4 *>(S.a[b][NB - 1][0] + off) = hv;
+                *reinterpret_cast<uint4 *>(S.a[b][NB - 1][1] + off) = lv;
+            }
+        }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            if (!mbar_wait(&S.full[b], (uint32_t)((i >> 1) & 1))) {
+                atomicOr(err, KERR_MBAR_TIMEOUT);
+            } else {
+                tc_fence_after();
+                const uint32_t bh = smem_u32(S.b[b][0]), bl = smem_u32(S.b[b][1]);
+#pragma unroll
+                for (int j = 0; j < BKT / 16; ++j) {
+                    const uint64_t dbh = sdesc(bh + j * 2 * B_LBO, B_LBO, B_SBO);
+                    const uint64_t dbl = sdesc(bl + j * 2 * B_LBO, B_LBO, B_SBO);
+#pragma unroll
+                    for (int q = 0; q < NB; ++q) {
+                        const uint32_t ah = smem_u32(S.a[b][q][0]), al = smem_u32(S.a[b][q][1]);
+                        const uint64_t dah = sdesc(ah + j * 2 * A_LBO, A_LBO, A_SBO);
+                        const uint64_t dal = sdesc(al + j * 2 * A_LBO, A_LBO, A_SBO);
+                        const uint32_t d = tmem + (uint32_t)(q * N);
+                        mma_bf16(d, dah, dbh, IDESC, (i > 0 || j > 0) ? 1u : 0u);
+                        mma_bf16(d, dah, dbl, IDESC, 1u);
+                        mma_bf16(d, dal, dbh, IDESC, 1u);
+                    }
+                }
+            }
+            mma_commit(&S.done[b]);
+        }
+    }
+    if (nk > 0) {
+        const int last = (nk - 1) & 1;
+        if (!mbar_wait(&S.done[last], (uint32_t)(((nk - 1) >> 1) & 1))) ok = false;
+    }
+    ok = !__syncthreads_or(!ok);
+    tc_fence_after();
+    if (ok && nk > 0 && *err == 0) {
+        const int q = warp & 3, ch = warp >> 2;
+        const int t = t0 + 32 * q + lane;
+        for (int cb = ch * (N / 2); cb < (ch + 1) * (N / 2); cb += 16) {
+            float y1[16], y2[16];
+            tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)cb, y1);
+            if (NB == 2) tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(N + cb), y2);
+            if (t < steps) {
+#pragma unroll
+                for (int jj = 0; jj < 16; ++jj) {
+                    const int r = nt * N + cb + jj;
+                    const int s = r / nmove;
+                    if (s >= n_sims) continue;
+                    const double f = F[((size_t)s * nl + L) * steps + t];
+                    double v;
+                    if (NB == 2) {
+                        const double kk = k3[(size_t)s * nl + L];
+                        v = ((1.0 - kk) * (double)y1[jj] + kk * (double)y2[jj]) * f;
+                    } else {
+                        v = (double)y1[jj] * f;
+                    }
+                    partial[((size_t)c * rows + r) * steps + t] = v;
+                }
+            }
+        }
+    } else if (!ok && tid == 0) {
+        atomicOr(err, KERR_MBAR_TIMEOUT);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, TCOLS);
+}
+
+// ecg[s][l][t] (l < nmove) = sum_c partial[c][s*nmove + l][t]; block per (row, 32 steps)
+__global__ void k_reduce_rows(int steps, int rows, int nchunks, int nmove, int nleads, const double *__restrict__ partial,
+                              const double *__restrict__ k0w, double *__restrict__ ecg) {
+    __shared__ double red[8][33];
+    const int tt = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int w = threadIdx.x >> 5;
+    const int r = blockIdx.y;
+    const int s = r / nmove, l = r % nmove;
+    double acc = 0.0;
+    if (tt < steps)
+        for (int c = w; c < nchunks; c += 8) acc += partial[((size_t)c * rows + r) * steps + tt];
+    red[w][threadIdx.x & 31] = acc;
+    __syncthreads();
+    if (w == 0 && tt < steps) {
+        double v = k0w ? k0w[(size_t)s * nleads + l] : 0.0;
+        for (int i = 0; i < 8; ++i) v += red[i][threadIdx.x];
+        ecg[((size_t)s * nleads + l) * steps + tt] = v;
+    }
+}
+
+template <int NB, int N>
+void launch_gemm(cudaStream_t st, const BatchArgs &A) {
+    const size_t smem = sizeof(BatchSmem<NB, N>) + 1024;
+    static bool attr = false;
+    if (!attr) {
+        EKG_CUDA(cudaFuncSetAttribute(k_batch_umma<NB, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr = true;
+    }
+    dim3 grid((unsigned)((A.steps + BM - 1) / BM), (unsigned)A.ntiles, (unsigned)A.nchunks);
+    k_batch_umma<NB, N><<<grid, BTHREADS, smem, st>>>(A.steps, A.nl, A.nkt, A.rows, A.nmove, A.n_sims, A.t_hilo,
+                                                      A.at_hilo, A.ck0, A.ck1, A.cl, A.hconst, A.k3, A.F, A.Bt,
+                                                      A.partial, A.err);
+    EKG_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+int batch_tile_rows(int two_bases) { return two_bases ? 128 : 256; }
+
+void launch_taylor_w(cudaStream_t s, const HeartDev &h, const float *W0, int J, const double *centre,
+                     const double *scale, float *Wt) {
+    dim3 grid((unsigned)((h.apad + 255) / 256), (unsigned)h.nleads);
+    k_taylor_w<<<grid, 256, 0, s>>>(h.apad, h.nleads, J, W0, h.at.p, h.a_layer.p, centre, scale, Wt);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int32_t *lc0, const int32_t *lc1,
+                          const double *partial, double *Q) {
+    dim3 grid((unsigned)((steps + 31) / 32), (unsigned)rows);
+    k_reduce_layers<<<grid, 256, 0, s>>>(steps, rows, nl, lc0, lc1, partial, Q);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const double *F,
+                           const double *coef, const double *k3, const double *Q1, const double *Q2, double *ecg) {
+    if (nmove >= h.nleads) return;
+    dim3 grid((unsigned)((h.steps + 127) / 128), (unsigned)(h.nleads - nmove), (unsigned)n_sims);
+    k_static_combine<<<grid, 128, 0, s>>>(h.steps, h.nleads, h.nlayers, J, Jb, nmove, n_sims, F, coef, k3, Q1, Q2,
+                                          ecg);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const double *layer_k,
+                             const double *leads, int nmove, int n_sims, uint8_t *Bt) {
+    dim3 grid((unsigned)((h.apad + 127) / 128), (unsigned)n_sims);
+    const int nkt = (int)(h.apad / BKT);
+    if (two_bases)
+        k_batch_lead_field<128><<<grid, 128, 0, s>>>(h.apad, nkt, h.a_vox_begin.p, h.vox_zyx.p, h.vox_nb.p,
+                                                     h.vox_nbo.p, h.nnb, h.difs.p, h.at.p, h.a_layer.p, layer_k,
+                                                     h.nlayers, leads, h.nleads, nmove, Bt);
+    else
+        k_batch_lead_field<256><<<grid, 128, 0, s>>>(h.apad, nkt, h.a_vox_begin.p, h.vox_zyx.p, h.vox_nb.p,
+                                                     h.vox_nbo.p, h.nnb, h.difs.p, h.at.p, h.a_layer.p, layer_k,
+                                                     h.nlayers, leads, h.nleads, nmove, Bt);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_batch_gemm(cudaStream_t s, const BatchArgs &A) {
+    if (A.two_bases) launch_gemm<2, 128>(s, A);
+    else launch_gemm<1, 256>(s, A);
+}
+
+void launch_reduce_rows(cudaStream_t s, int steps, int rows_used, int rows, int nchunks, int nmove, int nleads,
+                        const double *partial, const double *k0w, double *ecg) {
+    dim3 grid((unsigned)((steps + 31) / 32), (unsigned)rows_used);
+    k_reduce_rows<<<grid, 256, 0, s>>>(steps, rows, nchunks, nmove, nleads, partial, k0w, ecg);
+    EKG_CUDA(cudaGetLastError());
+}
+
+}  // namespace ekg

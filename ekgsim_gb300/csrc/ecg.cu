@@ -202,18 +202,26 @@ __global__ void __launch_bounds__(CC_T) k_contract_cuda(int steps, int nleads, i
     }
 }
 
-// ecg[s][l][t] = k0w[s][l] + sum_c partial[s][c][l][t]   (fixed order over c)
-__global__ void k_reduce_ecg(int steps, int nleads, int nchunks, const double *__restrict__ partial,
-                             const double *__restrict__ k0w, int n_sims, double *__restrict__ ecg) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t total = (int64_t)n_sims * nleads * steps;
-    if (i >= total) return;
-    const int t = (int)(i % steps);
-    const int64_t sl = i / steps;
-    const int s = (int)(sl / nleads), l = (int)(sl % nleads);
-    double acc = k0w[sl];
-    for (int c = 0; c < nchunks; ++c) acc += partial[(((size_t)s * nchunks + c) * nleads + l) * steps + t];
-    ecg[i] = acc;
+// ecg[s][l][t] = k0w[s][l] + sum_c partial[s][c][l][t]: one block per (s, l, 32 steps); warp w
+// sums chunks c = w, w+8, ... for 32 consecutive steps (coalesced), then the 8 warp sums are added
+// in warp order, so the result does not depend on scheduling.
+__global__ void __launch_bounds__(256) k_reduce_ecg(int steps, int nleads, int nchunks,
+                                                    const double *__restrict__ partial,
+                                                    const double *__restrict__ k0w, double *__restrict__ ecg) {
+    __shared__ double red[8][33];
+    const int tt = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int w = threadIdx.x >> 5;
+    const int l = blockIdx.y, s = blockIdx.z;
+    double acc = 0.0;
+    if (tt < steps)
+        for (int c = w; c < nchunks; c += 8) acc += partial[(((size_t)s * nchunks + c) * nleads + l) * steps + tt];
+    red[w][threadIdx.x & 31] = acc;
+    __syncthreads();
+    if (w == 0 && tt < steps) {
+        double r = k0w[(size_t)s * nleads + l];
+        for (int i = 0; i < 8; ++i) r += red[i][threadIdx.x];
+        ecg[((size_t)s * nleads + l) * steps + tt] = r;
+    }
 }
 
 // ------------------------------------------------------------------ criteria (FP64)
@@ -387,9 +395,8 @@ void launch_contract_cuda(cudaStream_t s, const HeartDev &h, const float *d_Wp, 
 
 void launch_reduce_ecg(cudaStream_t s, const HeartDev &h, const double *d_partial, const double *d_k0w,
                        int n_sims, double *d_ecg) {
-    const int64_t total = (int64_t)n_sims * h.nleads * h.steps;
-    k_reduce_ecg<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(h.steps, h.nleads, h.nchunks, d_partial, d_k0w,
-                                                                n_sims, d_ecg);
+    dim3 grid((unsigned)((h.steps + 31) / 32), (unsigned)h.nleads, (unsigned)n_sims);
+    k_reduce_ecg<<<grid, 256, 0, s>>>(h.steps, h.nleads, h.nchunks, d_partial, d_k0w, d_ecg);
     EKG_CUDA(cudaGetLastError());
 }
 

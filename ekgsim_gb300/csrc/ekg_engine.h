@@ -11,6 +11,7 @@ struct ekg_engine {
     cudaStream_t stream = nullptr;
     int chunk_len = 512;  // APs per K chunk of the contraction (multiple of 64)
     bool umma = true;     // tensor-core contraction (EKG_CONTRACT=cuda selects the CUDA-core kernel)
+    bool batched = true;  // separable batched form for multi-simulation passes (EKG_BATCHED=0 disables)
 };
 
 namespace ekg {
@@ -26,6 +27,34 @@ struct EvalSettings {
     int n_crit_leads = 0, n_criteria = 0, n_genes = 0;
 };
 int guard(const std::function<void()> &f);
+}  // namespace ekg
+
+namespace ekg {
+// Per-heart state of the batched form: the static-lead Taylor basis (cached per set of per-layer
+// k1, k4) and per-batch buffers.
+struct BatchState {
+    bool basis_ok = false;
+    std::vector<double> key;               // k1, k4 per layer the basis was built for
+    int J = 0;                             // Taylor terms stored
+    std::vector<double> centre, scale;     // per layer
+    DBuf<double> Q1, Q2;                   // [nl][L*J][steps]
+    DBuf<double> d_centre, d_scale;
+    DBuf<int32_t> lc0, lc1;                // chunk range of each layer
+    DBuf<uint8_t> Bt;                      // tiled BF16 hi/lo moved-lead weights
+    DBuf<double> partial;                  // [chunks][rows][steps]
+    DBuf<int32_t> ck0, ck1, cl;            // GEMM K chunks
+    DBuf<float4> hconst;
+    DBuf<double> k3, coef;
+};
+// What one device pass does, decided on the host from the batch's layer APs and lead positions.
+struct PassPlan {
+    bool batch = false;                    // separable batched form
+    int n_sims = 0, nmove = 0, J = 0, two_bases = 0;
+    int rows_used = 0, rows = 0, ntiles = 0, nchunks = 0;
+    std::vector<double> coef, k3;          // [S][nl][J], [S][nl]
+    std::vector<int32_t> ck0, ck1, cl;
+    float4 hc[256];
+};
 }  // namespace ekg
 
 struct ekg_heart {
@@ -52,6 +81,9 @@ struct ekg_heart {
     ekg::DBuf<double> leads0_dev;
     ekg::DBuf<float> W0;              // [L][apad] lead field at the loaded positions
     ekg::EvalSettings es;
+    ekg::BatchState bs;
+    int sm_count = 152;
     bool has_eval = false;
+    bool any_k0 = false;              // some layer AP of the current pass has k0 != 0
     ekg::SimConfig cfg;
 };

@@ -137,6 +137,43 @@ void launch_contract_cuda(cudaStream_t s, const HeartDev &h, const float *d_Wp, 
                           const double *d_F, int n_sims, double *d_partial);
 void launch_contract_umma(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,
                           const double *d_F, int n_sims, double *d_partial, uint32_t *d_err);
+// Explicit-argument form: `rows` weight rows (leads) per simulation, Wp [S][rows][apad],
+// layer_c [S][nl] float4, F [S][nl][steps], partial [S][nchunks][rows][steps].
+struct ContractArgs {
+    int steps = 0, rows = 0, nl = 0, nchunks = 0, n_sims = 1;
+    int64_t apad = 0;
+    const float2 *t_hilo = nullptr, *at_hilo = nullptr;
+    const int32_t *chunk_a0 = nullptr, *chunk_a1 = nullptr, *chunk_layer = nullptr;
+    const float *Wp = nullptr, *layer_c = nullptr;
+    const double *F = nullptr;
+    double *partial = nullptr;
+    uint32_t *err = nullptr;
+};
+void launch_contract_umma_args(cudaStream_t s, const ContractArgs &a);
+
+// ------------------------------------------------------------------ batched form (batch.cu)
+struct BatchArgs {
+    int steps = 0, nl = 0, nkt = 0, rows = 0, nmove = 0, n_sims = 0, ntiles = 0, nchunks = 0, two_bases = 0;
+    const float2 *t_hilo = nullptr, *at_hilo = nullptr;
+    const int32_t *ck0 = nullptr, *ck1 = nullptr, *cl = nullptr;
+    const float4 *hconst = nullptr;
+    const double *k3 = nullptr, *F = nullptr;
+    const uint8_t *Bt = nullptr;
+    double *partial = nullptr;
+    uint32_t *err = nullptr;
+};
+int batch_tile_rows(int two_bases);
+void launch_taylor_w(cudaStream_t s, const HeartDev &h, const float *W0, int J, const double *centre,
+                     const double *scale, float *Wt);
+void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int32_t *lc0, const int32_t *lc1,
+                          const double *partial, double *Q);
+void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const double *F,
+                           const double *coef, const double *k3, const double *Q1, const double *Q2, double *ecg);
+void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const double *layer_k,
+                             const double *leads, int nmove, int n_sims, uint8_t *Bt);
+void launch_batch_gemm(cudaStream_t s, const BatchArgs &a);
+void launch_reduce_rows(cudaStream_t s, int steps, int rows_used, int rows, int nchunks, int nmove, int nleads,
+                        const double *partial, const double *k0w, double *ecg);
 void launch_reduce_ecg(cudaStream_t s, const HeartDev &h, const double *d_partial, const double *d_k0w,
                        int n_sims, double *d_ecg);
 void launch_criteria(cudaStream_t s, const HeartDev &h, const double *d_ecg, int n_sims, int ncrit_stride,

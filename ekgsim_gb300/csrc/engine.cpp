@@ -158,6 +158,8 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     EKG_CUDA(cudaSetDevice(h->eng->device));
     if (!h->stream) EKG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     if (!h->err_host) EKG_CUDA(cudaMallocHost(&h->err_host, sizeof(uint32_t)));
+    EKG_CUDA(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->eng->device));
+    h->ev.err.alloc(1);
     cudaStream_t s = h->stream;
     {
         DBuf<uint8_t> dl, ds;
@@ -354,13 +356,20 @@ void ensure_eval_capacity(ekg_heart *h, int n_sims) {
     E.layer_c.alloc(S * D.nlayers * 4);
     E.F.alloc(S * D.nlayers * D.steps);
     E.k0w.alloc(S * D.nleads);
-    E.W.alloc(S * D.nleads * D.apad);
-    E.Wp.alloc(S * D.nleads * D.apad);
-    E.partial.alloc(S * D.nchunks * D.nleads * D.steps);
     E.ecg.alloc(S * D.nleads * D.steps);
     E.crit.alloc(S * std::max(1, D.nleads) * 2);
     E.err.alloc(1);
     E.cap_sims = n_sims;
+}
+// buffers of the general (per-simulation AP) form
+void ensure_general_capacity(ekg_heart *h, int n_sims) {
+    EvalDev &E = h->ev;
+    const HeartDev &D = h->dev;
+    const size_t S = (size_t)n_sims;
+    if (E.W.n >= S * D.nleads * D.apad && E.partial.n >= S * D.nchunks * D.nleads * D.steps) return;
+    E.W.alloc(S * D.nleads * D.apad);
+    E.Wp.alloc(S * D.nleads * D.apad);
+    E.partial.alloc(S * D.nchunks * D.nleads * D.steps);
 }
 
 // Device pass for n_sims simulations, split into upload / compute / download so the benchmark
@@ -371,50 +380,317 @@ struct PassTiming {
 };
 static int g_launch_count = 0;
 
-int upload_inputs(ekg_heart *h, int n_sims, const double *layer_k, const double *leads) {
+// Taylor order for exp(x) on |x| <= xmax with truncation bound xmax^J / J! * e^xmax <= 1e-12.
+int taylor_terms(double xmax, int jmax) {
+    double term = 1.0;  // xmax^J / J!
+    for (int J = 1; J <= jmax; ++J) {
+        term *= xmax / J;
+        if (term * std::exp(xmax) <= 1e-12) return J;
+    }
+    return -1;
+}
+
+// Build (or reuse) the static-lead Taylor basis for per-layer (k1, k4) = key.
+void ensure_basis(ekg_heart *h, const std::vector<double> &key) {
+    BatchState &B = h->bs;
+    HeartDev &D = h->dev;
+    if (B.basis_ok && B.key == key) return;
+    cudaStream_t s = h->stream;
+    const int nl = D.nlayers, L = D.nleads, J = 10;
+    // centre and half-range of the activation times of each layer
+    std::vector<double> at_h(D.apad);
+    std::vector<int32_t> al(D.apad);
+    EKG_CUDA(cudaMemcpyAsync(at_h.data(), D.at.p, D.apad * 8, cudaMemcpyDeviceToHost, s));
+    EKG_CUDA(cudaMemcpyAsync(al.data(), D.a_layer.p, D.apad * 4, cudaMemcpyDeviceToHost, s));
+    EKG_CUDA(cudaStreamSynchronize(s));
+    std::vector<double> lo(nl, INFINITY), hi(nl, -INFINITY);
+    for (int64_t a = 0; a < D.apad; ++a)
+        if (std::isfinite(at_h[a])) {
+            lo[al[a]] = std::min(lo[al[a]], at_h[a]);
+            hi[al[a]] = std::max(hi[al[a]], at_h[a]);
+        }
+    B.centre.assign(nl, 0.0);
+    B.scale.assign(nl, 1.0);
+    for (int i = 0; i < nl; ++i)
+        if (lo[i] <= hi[i]) {
+            B.centre[i] = 0.5 * (lo[i] + hi[i]);
+            B.scale[i] = std::max(0.5 * (hi[i] - lo[i]), 1e-6);
+        }
+    B.d_centre.alloc(nl);
+    B.d_scale.alloc(nl);
+    EKG_CUDA(cudaMemcpyAsync(B.d_centre.p, B.centre.data(), nl * 8, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(B.d_scale.p, B.scale.data(), nl * 8, cudaMemcpyHostToDevice, s));
+    // chunk ranges per layer (chunks of one layer are contiguous)
+    std::vector<int32_t> cl(D.nchunks), c0(nl, 0), c1(nl, 0);
+    EKG_CUDA(cudaMemcpy(cl.data(), D.chunk_layer.p, D.nchunks * 4, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < nl; ++i) {
+        c0[i] = c1[i] = 0;
+        bool seen = false;
+        for (int c = 0; c < D.nchunks; ++c)
+            if (cl[c] == i) {
+                if (!seen) c0[i] = c;
+                seen = true;
+                c1[i] = c + 1;
+            }
+    }
+    B.lc0.alloc(nl);
+    B.lc1.alloc(nl);
+    EKG_CUDA(cudaMemcpyAsync(B.lc0.p, c0.data(), nl * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(B.lc1.p, c1.data(), nl * 4, cudaMemcpyHostToDevice, s));
+    const int rows = L * J;
+    DBuf<float> Wt, lc;
+    DBuf<double> ones, part;
+    Wt.alloc((size_t)rows * D.apad);
+    lc.alloc((size_t)nl * 4);
+    ones.alloc((size_t)nl * D.steps);
+    part.alloc((size_t)D.nchunks * rows * D.steps);
+    std::vector<double> one((size_t)nl * D.steps, 1.0);
+    EKG_CUDA(cudaMemcpyAsync(ones.p, one.data(), one.size() * 8, cudaMemcpyHostToDevice, s));
+    launch_taylor_w(s, D, h->W0.p, J, B.d_centre.p, B.d_scale.p, Wt.p);
+    B.Q1.alloc((size_t)nl * rows * D.steps);
+    B.Q2.alloc((size_t)nl * rows * D.steps);
+    const double L2E = 1.4426950408889634;
+    for (int basis = 0; basis < 2; ++basis) {
+        std::vector<float> c((size_t)nl * 4);
+        for (int i = 0; i < nl; ++i) {
+            c[4 * i + 0] = (float)(key[2 * i] * L2E);
+            c[4 * i + 1] = (float)(key[2 * i + 1] * L2E);
+            c[4 * i + 2] = basis == 0 ? 1.f : 0.f;  // B1 = sigma(k1 tau) exp(-k4 tau)
+            c[4 * i + 3] = basis == 0 ? 0.f : 1.f;  // B2 = sigma(k1 tau)
+        }
+        EKG_CUDA(cudaMemcpyAsync(lc.p, c.data(), c.size() * 4, cudaMemcpyHostToDevice, s));
+        ContractArgs A;
+        A.steps = D.steps;
+        A.rows = rows;
+        A.nl = nl;
+        A.nchunks = D.nchunks;
+        A.n_sims = 1;
+        A.apad = D.apad;
+        A.t_hilo = D.t_hilo.p;
+        A.at_hilo = D.at_hilo.p;
+        A.chunk_a0 = D.chunk_a0.p;
+        A.chunk_a1 = D.chunk_a1.p;
+        A.chunk_layer = D.chunk_layer.p;
+        A.Wp = Wt.p;
+        A.layer_c = lc.p;
+        A.F = ones.p;
+        A.partial = part.p;
+        A.err = h->ev.err.p;
+        EKG_CUDA(cudaMemsetAsync(h->ev.err.p, 0, 4, s));
+        launch_contract_umma_args(s, A);
+        launch_reduce_layers(s, D.steps, rows, nl, B.lc0.p, B.lc1.p, part.p, basis == 0 ? B.Q1.p : B.Q2.p);
+        EKG_CUDA(cudaMemcpyAsync(h->err_host, h->ev.err.p, 4, cudaMemcpyDeviceToHost, s));
+        EKG_CUDA(cudaStreamSynchronize(s));
+        if (*h->err_host) throw Error{EKG_ERR_TIMEOUT, "a bounded device wait ran out (basis build)"};
+    }
+    B.J = J;
+    B.key = key;
+    B.basis_ok = true;
+}
+
+// Decide the pass: the batched (separable) form when the batch shares k1 and k4 per layer, no
+// layer has k0 != 0, exp(k5 at) has a short Taylor expansion and there are at least two sims.
+PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *leads) {
+    PassPlan P;
+    P.n_sims = n_sims;
+    const HeartDev &D = h->dev;
+    const int nl = D.nlayers, L = D.nleads;
+    for (int si = 0; si < n_sims; ++si) {
+        const double *p = leads + (size_t)si * L * 3;
+        for (int l = 0; l < L; ++l)
+            if (p[3 * l] != h->leads0[3 * l] || p[3 * l + 1] != h->leads0[3 * l + 1] || p[3 * l + 2] != h->leads0[3 * l + 2])
+                P.nmove = std::max(P.nmove, l + 1);
+    }
+    if (n_sims < 2 || !h->eng->batched || nl > 255) return P;
+    std::vector<double> key(2 * nl);
+    bool k3_uniform = true;
+    for (int i = 0; i < nl; ++i) {
+        key[2 * i] = layer_k[9 * i + 1];
+        key[2 * i + 1] = layer_k[9 * i + 4];
+    }
+    for (int si = 0; si < n_sims; ++si)
+        for (int i = 0; i < nl; ++i) {
+            const double *k = layer_k + ((size_t)si * nl + i) * 9;
+            if (k[1] != key[2 * i] || k[4] != key[2 * i + 1] || k[0] != 0.0) return P;
+            if (k[3] != layer_k[9 * i + 3]) k3_uniform = false;
+        }
+    ensure_basis(h, key);
+    const BatchState &B = h->bs;
+    double xmax = 0;
+    for (int si = 0; si < n_sims; ++si)
+        for (int i = 0; i < nl; ++i) xmax = std::max(xmax, std::fabs(layer_k[((size_t)si * nl + i) * 9 + 5]) * B.scale[i]);
+    const int J = taylor_terms(xmax, B.J);
+    if (J < 0) return P;
+    P.batch = true;
+    P.J = J;
+    P.two_bases = k3_uniform ? 0 : 1;
+    P.coef.resize((size_t)n_sims * nl * J);
+    P.k3.resize((size_t)n_sims * nl);
+    for (int si = 0; si < n_sims; ++si)
+        for (int i = 0; i < nl; ++i) {
+            const double *k = layer_k + ((size_t)si * nl + i) * 9;
+            const double x = k[5] * B.scale[i];
+            double c = std::exp(k[5] * B.centre[i]);
+            for (int j = 0; j < J; ++j) {
+                P.coef[((size_t)si * nl + i) * J + j] = c;
+                c *= x / (j + 1);
+            }
+            P.k3[(size_t)si * nl + i] = k[3];
+        }
+    const double L2E = 1.4426950408889634;
+    for (int i = 0; i < nl; ++i)
+        P.hc[i] = make_float4((float)(key[2 * i] * L2E), (float)(key[2 * i + 1] * L2E), (float)(1.0 - layer_k[9 * i + 3]),
+                              (float)layer_k[9 * i + 3]);
+    if (P.nmove > 0) {
+        const int N = batch_tile_rows(P.two_bases);
+        P.rows_used = n_sims * P.nmove;
+        P.ntiles = (P.rows_used + N - 1) / N;
+        P.rows = P.ntiles * N;
+        // K chunks: about two CTAs per SM over (t tiles x N tiles x chunks), each inside one layer
+        std::vector<int32_t> ccl(D.nchunks), ca0(D.nchunks), ca1(D.nchunks);
+        EKG_CUDA(cudaMemcpy(ccl.data(), D.chunk_layer.p, D.nchunks * 4, cudaMemcpyDeviceToHost));
+        EKG_CUDA(cudaMemcpy(ca0.data(), D.chunk_a0.p, D.nchunks * 4, cudaMemcpyDeviceToHost));
+        EKG_CUDA(cudaMemcpy(ca1.data(), D.chunk_a1.p, D.nchunks * 4, cudaMemcpyDeviceToHost));
+        std::vector<int> kb(nl, -1), ke(nl, -1);
+        for (int c = 0; c < D.nchunks; ++c) {
+            const int Lc = ccl[c];
+            if (kb[Lc] < 0) kb[Lc] = ca0[c] / 64;
+            ke[Lc] = ca1[c] / 64;
+        }
+        int kt_total = 0;
+        for (int i = 0; i < nl; ++i)
+            if (kb[i] >= 0) kt_total += ke[i] - kb[i];
+        const int ttiles = (D.steps + 127) / 128;
+        const int target = 2 * h->sm_count;
+        const int per = std::max(1, (int)std::ceil((double)target / (ttiles * P.ntiles)));
+        for (int i = 0; i < nl; ++i) {
+            if (kb[i] < 0) continue;
+            const int n = ke[i] - kb[i];
+            const int nc = std::max(1, std::min(n, (int)std::lround((double)per * n / std::max(1, kt_total))));
+            for (int c = 0; c < nc; ++c) {
+                P.ck0.push_back(kb[i] + (int)((int64_t)n * c / nc));
+                P.ck1.push_back(kb[i] + (int)((int64_t)n * (c + 1) / nc));
+                P.cl.push_back(i);
+            }
+        }
+        P.nchunks = (int)P.ck0.size();
+    }
+    return P;
+}
+
+
+
+void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const double *leads) {
     HeartDev &D = h->dev;
     EvalDev &E = h->ev;
     cudaStream_t s = h->stream;
+    const int n_sims = P.n_sims;
     ensure_eval_capacity(h, n_sims);
     const size_t L = D.nleads, S = n_sims;
     EKG_CUDA(cudaMemcpyAsync(E.layer_k.p, layer_k, S * D.nlayers * 9 * 8, cudaMemcpyHostToDevice, s));
-    // number of leading leads that move in any simulation (lead displacement genes come first)
-    int nmove = 0;
-    for (size_t si = 0; si < S; ++si) {
-        const double *p = leads + si * L * 3;
-        for (size_t l = 0; l < L; ++l)
-            if (p[3 * l] != h->leads0[3 * l] || p[3 * l + 1] != h->leads0[3 * l + 1] || p[3 * l + 2] != h->leads0[3 * l + 2])
-                nmove = std::max(nmove, (int)l + 1);
+    h->any_k0 = false;
+    for (size_t i = 0; i < S * D.nlayers; ++i) h->any_k0 = h->any_k0 || layer_k[9 * i] != 0.0;
+    if (P.nmove > 0) EKG_CUDA(cudaMemcpyAsync(E.leads.p, leads, S * L * 3 * 8, cudaMemcpyHostToDevice, s));
+    if (P.batch) {
+        BatchState &B = h->bs;
+        B.coef.alloc(P.coef.size());
+        B.k3.alloc(P.k3.size());
+        B.hconst.alloc(D.nlayers);
+        EKG_CUDA(cudaMemcpyAsync(B.coef.p, P.coef.data(), P.coef.size() * 8, cudaMemcpyHostToDevice, s));
+        EKG_CUDA(cudaMemcpyAsync(B.k3.p, P.k3.data(), P.k3.size() * 8, cudaMemcpyHostToDevice, s));
+        EKG_CUDA(cudaMemcpyAsync(B.hconst.p, P.hc, D.nlayers * sizeof(float4), cudaMemcpyHostToDevice, s));
+        if (P.nmove > 0) {
+            const size_t bt = (size_t)P.rows * D.apad * 4;
+            if (B.Bt.n < bt) B.Bt.alloc(bt);
+            const size_t pb = (size_t)P.nchunks * P.rows * D.steps;
+            if (B.partial.n < pb) B.partial.alloc(pb);
+            B.ck0.alloc(P.nchunks);
+            B.ck1.alloc(P.nchunks);
+            B.cl.alloc(P.nchunks);
+            EKG_CUDA(cudaMemcpyAsync(B.ck0.p, P.ck0.data(), P.nchunks * 4, cudaMemcpyHostToDevice, s));
+            EKG_CUDA(cudaMemcpyAsync(B.ck1.p, P.ck1.data(), P.nchunks * 4, cudaMemcpyHostToDevice, s));
+            EKG_CUDA(cudaMemcpyAsync(B.cl.p, P.cl.data(), P.nchunks * 4, cudaMemcpyHostToDevice, s));
+        }
+    } else {
+        ensure_general_capacity(h, n_sims);
     }
-    if (nmove > 0) EKG_CUDA(cudaMemcpyAsync(E.leads.p, leads, S * L * 3 * 8, cudaMemcpyHostToDevice, s));
-    return nmove;
 }
 
-void compute(ekg_heart *h, int n_sims, int nmove, int n_crit_leads, int mode, PassTiming *tm) {
+void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTiming *tm) {
     HeartDev &D = h->dev;
     EvalDev &E = h->ev;
     cudaStream_t s = h->stream;
+    const int n_sims = P.n_sims, nmove = P.nmove;
     const size_t L = D.nleads, S = n_sims;
     int launches = 0;
     if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[0], s));
-    // lead field: resident rows for leads at their loaded position, recomputed rows for moved ones
-    for (size_t si = 0; si < S; ++si)
-        EKG_CUDA(cudaMemcpyAsync(E.W.p + si * L * D.apad, h->W0.p, L * D.apad * 4, cudaMemcpyDeviceToDevice, s));
-    if (nmove > 0) {
-        launch_lead_field(s, D, E.leads.p, nmove, (int)L, n_sims, E.W.p, (int)L);
-        ++launches;
-    }
-    launch_layer_factors(s, D, E.layer_k.p, n_sims, E.F.p, E.layer_c.p);
-    launch_scale_w(s, D, E.W.p, E.layer_k.p, n_sims, E.Wp.p);
-    launch_k0_term(s, D, E.W.p, E.layer_k.p, n_sims, E.k0w.p);
-    launches += 3;
     EKG_CUDA(cudaMemsetAsync(E.err.p, 0, sizeof(uint32_t), s));
-    if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[1], s));
-    if (h->eng->umma) launch_contract_umma(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p, E.err.p);
-    else launch_contract_cuda(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p);
-    if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[2], s));
-    launch_reduce_ecg(s, D, E.partial.p, E.k0w.p, n_sims, E.ecg.p);
-    launches += 2;
+    launch_layer_factors(s, D, E.layer_k.p, n_sims, E.F.p, E.layer_c.p);
+    ++launches;
+    if (P.batch) {
+        BatchState &B = h->bs;
+        launch_static_combine(s, D, P.J, B.J, nmove, n_sims, E.F.p, B.coef.p, B.k3.p, B.Q1.p, B.Q2.p, E.ecg.p);
+        launches += nmove < (int)L;
+        if (nmove > 0) {
+            if (P.rows_used < P.rows) EKG_CUDA(cudaMemsetAsync(B.Bt.p, 0, (size_t)P.rows * D.apad * 4, s));
+            launch_batch_lead_field(s, D, P.two_bases, E.layer_k.p, E.leads.p, nmove, n_sims, B.Bt.p);
+            ++launches;
+            if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[1], s));
+            BatchArgs A;
+            A.steps = D.steps;
+            A.nl = D.nlayers;
+            A.nkt = (int)(D.apad / 64);
+            A.rows = P.rows;
+            A.nmove = nmove;
+            A.n_sims = n_sims;
+            A.ntiles = P.ntiles;
+            A.nchunks = P.nchunks;
+            A.two_bases = P.two_bases;
+            A.t_hilo = D.t_hilo.p;
+            A.at_hilo = D.at_hilo.p;
+            A.ck0 = B.ck0.p;
+            A.ck1 = B.ck1.p;
+            A.cl = B.cl.p;
+            A.hconst = B.hconst.p;
+            A.k3 = B.k3.p;
+            A.F = E.F.p;
+            A.Bt = B.Bt.p;
+            A.partial = B.partial.p;
+            A.err = E.err.p;
+            launch_batch_gemm(s, A);
+            if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[2], s));
+            launch_reduce_rows(s, D.steps, P.rows_used, P.rows, P.nchunks, nmove, (int)L, B.partial.p, nullptr,
+                               E.ecg.p);
+            launches += 2;
+        } else if (tm && tm->on) {
+            EKG_CUDA(cudaEventRecord(tm->ev[1], s));
+            EKG_CUDA(cudaEventRecord(tm->ev[2], s));
+        }
+    } else {
+        // lead field: resident rows for leads at their loaded position, recomputed rows for moved ones
+        for (size_t si = 0; si < S; ++si)
+            EKG_CUDA(cudaMemcpyAsync(E.W.p + si * L * D.apad, h->W0.p, L * D.apad * 4, cudaMemcpyDeviceToDevice, s));
+        if (nmove > 0) {
+            launch_lead_field(s, D, E.leads.p, nmove, (int)L, n_sims, E.W.p, (int)L);
+            ++launches;
+        }
+        launch_scale_w(s, D, E.W.p, E.layer_k.p, n_sims, E.Wp.p);
+        ++launches;
+        // k0 leaves a constant term only when some layer's k0 differs from zero (AP differences
+        // within a layer cancel it)
+        if (h->any_k0) {
+            launch_k0_term(s, D, E.W.p, E.layer_k.p, n_sims, E.k0w.p);
+            ++launches;
+        } else {
+            EKG_CUDA(cudaMemsetAsync(E.k0w.p, 0, S * L * sizeof(double), s));
+        }
+        if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[1], s));
+        if (h->eng->umma) launch_contract_umma(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p, E.err.p);
+        else launch_contract_cuda(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p);
+        if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[2], s));
+        launch_reduce_ecg(s, D, E.partial.p, E.k0w.p, n_sims, E.ecg.p);
+        launches += 2;
+    }
     if (n_crit_leads > 0) {
         launch_criteria(s, D, E.ecg.p, n_sims, n_crit_leads, n_crit_leads, mode, E.targets.p, E.target_len.p,
                         E.target_off.p, E.crit.p);
@@ -430,8 +706,9 @@ void device_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *
     EvalDev &E = h->ev;
     cudaStream_t s = h->stream;
     EKG_CUDA(cudaSetDevice(h->eng->device));
-    const int nmove = upload_inputs(h, n_sims, layer_k, leads);
-    compute(h, n_sims, nmove, crit_host ? n_crit_leads : 0, mode, nullptr);
+    const PassPlan P = plan_pass(h, n_sims, layer_k, leads);
+    upload_inputs(h, P, layer_k, leads);
+    compute(h, P, crit_host ? n_crit_leads : 0, mode, nullptr);
     const size_t L = D.nleads, S = n_sims;
     EKG_CUDA(cudaMemcpyAsync(h->err_host, E.err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     if (crit_host && n_crit_leads > 0)
@@ -448,10 +725,11 @@ void benchmark(ekg_heart *h, int n_sims, const double *layer_k, const double *le
     std::lock_guard<std::mutex> lk(h->mu);
     EKG_CUDA(cudaSetDevice(h->eng->device));
     cudaStream_t s = h->stream;
-    const int nmove = upload_inputs(h, n_sims, layer_k, leads);
+    const PassPlan P = plan_pass(h, n_sims, layer_k, leads);
+    upload_inputs(h, P, layer_k, leads);
     const int ncl = h->has_eval ? h->es.n_crit_leads : 0;
     const int mode = h->has_eval ? h->es.comparison_mode : 2;
-    for (int i = 0; i < warmup; ++i) compute(h, n_sims, nmove, ncl, mode, nullptr);
+    for (int i = 0; i < warmup; ++i) compute(h, P, ncl, mode, nullptr);
     PassTiming tm;
     tm.on = true;
     for (auto &e : tm.ev) EKG_CUDA(cudaEventCreate(&e));
@@ -462,7 +740,7 @@ void benchmark(ekg_heart *h, int n_sims, const double *layer_k, const double *le
     double contract = 0, prep = 0, tail = 0;
     EKG_CUDA(cudaEventRecord(t0, s));
     for (int i = 0; i < iters; ++i) {
-        compute(h, n_sims, nmove, ncl, mode, &tm);
+        compute(h, P, ncl, mode, &tm);
         EKG_CUDA(cudaEventSynchronize(tm.ev[3]));
         float a = 0, b = 0, c = 0;
         EKG_CUDA(cudaEventElapsedTime(&a, tm.ev[0], tm.ev[1]));
@@ -476,8 +754,8 @@ void benchmark(ekg_heart *h, int n_sims, const double *layer_k, const double *le
     EKG_CUDA(cudaEventSynchronize(t1));
     float total = 0;
     EKG_CUDA(cudaEventElapsedTime(&total, t0, t1));
-    const double vals[6] = {total, contract, prep, tail, (double)g_launch_count, (double)nmove};
-    for (int i = 0; i < n_out && i < 6; ++i) out[i] = vals[i];
+    const double vals[7] = {total, contract, prep, tail, (double)g_launch_count, (double)P.nmove, P.batch ? 1.0 : 0.0};
+    for (int i = 0; i < n_out && i < 7; ++i) out[i] = vals[i];
     for (auto &e : tm.ev) cudaEventDestroy(e);
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
@@ -712,6 +990,7 @@ int ekg_engine_create(int device, ekg_engine **out) {
         e->device = device;
         if (const char *v = std::getenv("EKG_CONTRACT")) e->umma = std::string(v) != "cuda";
         if (const char *v = std::getenv("EKG_CHUNK")) e->chunk_len = std::max(64, std::atoi(v) / 64 * 64);
+        if (const char *v = std::getenv("EKG_BATCHED")) e->batched = std::string(v) != "0";
         EKG_CUDA(cudaSetDevice(device));
         EKG_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
         *out = e.release();

@@ -21,6 +21,7 @@
 #include <cstdio>
 
 #include "ekg_internal.h"
+#include "umma_ptx.h"
 
 namespace ekg {
 
@@ -29,105 +30,8 @@ namespace {
 constexpr int UM_M = 128;       // time steps per tile
 constexpr int UM_KT = 64;       // APs per pipeline stage (4 MMA K steps)
 constexpr int UM_THREADS = 256;
-constexpr uint32_t WAIT_LIMIT = 1u << 22;  // try_wait rounds before giving up (~seconds)
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// bounded wait; returns false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (uint32_t i = 0; i < WAIT_LIMIT; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-__device__ __forceinline__ void fence_barrier_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
-                 : "memory");
-}
-__device__ __forceinline__ void tmem_relinquish() {
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-
-// tcgen05 shared-memory matrix descriptor: start, leading and stride byte offsets (>>4),
-// descriptor version 1, no swizzle, base offset 0.
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
-    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-    d |= (uint64_t)1 << 46;
-    return d;
-}
-// instruction descriptor, kind::f16: FP32 accumulate, BF16 A and B, both K-major, M x N
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-            d_tmem),
-        "l"(a), "l"(b), "r"(idesc), "r"(acc)
-        : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint64_t *bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-                 : "memory");
-}
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
-    uint32_t r[8];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-                 : "r"(taddr)
-                 : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ float ex2_approx(float x) {
-    float y;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-__device__ __forceinline__ float rcp_approx(float x) {
-    float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-__device__ __forceinline__ float h_value(float tau, float4 c) {
-    const float e1 = ex2_approx(-c.x * tau);
-    const float s = rcp_approx(1.0f + e1);
-    const float e4 = ex2_approx(-c.y * tau);
-    const float h = s * fmaf(c.z, e4, c.w);
-    return s == 0.0f ? 0.0f : h;
-}
-// x -> (bf16 hi, bf16 lo) packed pairs for elements (x0, x1)
-__device__ __forceinline__ void split2(float x0, float x1, uint32_t &hi, uint32_t &lo) {
-    __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
-    const float r0 = x0 - __bfloat162float(h.x), r1 = x1 - __bfloat162float(h.y);
-    __nv_bfloat162 l = __floats2bfloat162_rn(r0, r1);
-    hi = *reinterpret_cast<uint32_t *>(&h);
-    lo = *reinterpret_cast<uint32_t *>(&l);
-}
+using namespace ptx;
 
 template <int N>
 struct UmmaSmem {
@@ -297,32 +201,52 @@ __global__ void __launch_bounds__(UM_THREADS, 1) k_contract_umma(
 }
 
 template <int N>
-void launch_n(cudaStream_t st, const HeartDev &h, const float *d_Wp, const float *d_layer_c, const double *d_F,
-              int n_sims, double *d_partial, uint32_t *d_err) {
-    const int nlb = (h.nleads + N - 1) / N;
+void launch_n(cudaStream_t st, const ContractArgs &A) {
+    const int nlb = (A.rows + N - 1) / N;
     const size_t smem = sizeof(UmmaSmem<N>) + 1024;
     static bool attr = false;
     if (!attr) {
         EKG_CUDA(cudaFuncSetAttribute(k_contract_umma<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
-    dim3 grid((unsigned)((h.steps + UM_M - 1) / UM_M), (unsigned)h.nchunks, (unsigned)(n_sims * nlb));
-    k_contract_umma<N><<<grid, UM_THREADS, smem, st>>>(h.steps, h.nleads, h.apad, h.nlayers, h.t_hilo.p, h.at_hilo.p,
-                                                       h.chunk_a0.p, h.chunk_a1.p, h.chunk_layer.p, d_Wp, d_layer_c,
-                                                       d_F, h.nchunks, nlb, d_partial, d_err);
+    dim3 grid((unsigned)((A.steps + UM_M - 1) / UM_M), (unsigned)A.nchunks, (unsigned)(A.n_sims * nlb));
+    k_contract_umma<N><<<grid, UM_THREADS, smem, st>>>(A.steps, A.rows, A.apad, A.nl, A.t_hilo, A.at_hilo, A.chunk_a0,
+                                                       A.chunk_a1, A.chunk_layer, A.Wp, A.layer_c, A.F, A.nchunks, nlb,
+                                                       A.partial, A.err);
     EKG_CUDA(cudaGetLastError());
 }
 
 }  // namespace
 
-// N (padded leads) chosen from the lead count: 16, 32, 64, 128 or 256 per lead block.
+// N (padded rows) chosen from the row count: 16, 32, 64, 128 or 256 per block of rows.
+void launch_contract_umma_args(cudaStream_t s, const ContractArgs &A) {
+    if (A.rows <= 16) launch_n<16>(s, A);
+    else if (A.rows <= 32) launch_n<32>(s, A);
+    else if (A.rows <= 64) launch_n<64>(s, A);
+    else if (A.rows <= 128) launch_n<128>(s, A);
+    else launch_n<256>(s, A);
+}
+
 void launch_contract_umma(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,
                           const double *d_F, int n_sims, double *d_partial, uint32_t *d_err) {
-    if (h.nleads <= 16) launch_n<16>(s, h, d_Wp, d_layer_c, d_F, n_sims, d_partial, d_err);
-    else if (h.nleads <= 32) launch_n<32>(s, h, d_Wp, d_layer_c, d_F, n_sims, d_partial, d_err);
-    else if (h.nleads <= 64) launch_n<64>(s, h, d_Wp, d_layer_c, d_F, n_sims, d_partial, d_err);
-    else if (h.nleads <= 128) launch_n<128>(s, h, d_Wp, d_layer_c, d_F, n_sims, d_partial, d_err);
-    else launch_n<256>(s, h, d_Wp, d_layer_c, d_F, n_sims, d_partial, d_err);
+    ContractArgs A;
+    A.steps = h.steps;
+    A.rows = h.nleads;
+    A.nl = h.nlayers;
+    A.nchunks = h.nchunks;
+    A.n_sims = n_sims;
+    A.apad = h.apad;
+    A.t_hilo = h.t_hilo.p;
+    A.at_hilo = h.at_hilo.p;
+    A.chunk_a0 = h.chunk_a0.p;
+    A.chunk_a1 = h.chunk_a1.p;
+    A.chunk_layer = h.chunk_layer.p;
+    A.Wp = d_Wp;
+    A.layer_c = d_layer_c;
+    A.F = d_F;
+    A.partial = d_partial;
+    A.err = d_err;
+    launch_contract_umma_args(s, A);
 }
 
 }  // namespace ekg

@@ -219,3 +219,43 @@ def test_contract_kernels_agree(tmp_path):
     assert rel_l2(out["umma"], ref) <= ECG_TOL
     assert rel_l2(out["cuda"], ref) <= ECG_TOL
     assert rel_l2(out["umma"], out["cuda"]) <= ECG_TOL
+
+
+def _batch_vs_oracle(engine, spec, steps, genes, layer_k_fn, two_bases=False):
+    from ekgsim_gb300.engine import Heart
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    h = Heart.create(engine, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+    target = synth.analytic_target(spec.n_leads, steps, 3)
+    h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], [t for t in target], mid_position=0.6)
+    crit_b, viol_b, ecg_b = h.eval_batch(genes, want_ecg=True)
+    at, layer = O.activation(grid, tm)
+    worst = 0.0
+    for i, g in enumerate(genes):
+        lk = layer_k_fn(g)
+        moved = O.move_leads(leads, g[12:12 + 2 * spec.n_leads].reshape(-1, 2))
+        ref = O.run(layer, at, lk, moved, "3D4", 0.0, float(steps), 1.0)
+        worst = max(worst, rel_l2(ecg_b[i], ref))
+        crit1, viol1, ecg1, _, _ = h.eval(g, want_ecg=True)
+        assert rel_l2(ecg_b[i], ecg1) <= ECG_TOL
+        assert np.allclose(crit_b[i], crit1, rtol=0, atol=1e-4)
+    return worst
+
+
+def test_batched_form_matches_oracle_64(engine):
+    """Separable batched form (static-lead Taylor basis + moved-lead GEMM) against the oracle."""
+    c = synth.config(0)
+    spec = c["spec"]
+    genes = np.stack([synth.genes_for(spec, r, 0) for r in range(6)])
+    worst = _batch_vs_oracle(engine, spec, 600, genes, lambda g: O.layer_aps(
+        3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], "endo-mid-epi", 0.6, g[:12])[0])
+    assert worst <= ECG_TOL
+
+
+def test_batched_form_twelve_leads_static_and_moved(engine):
+    spec = synth.small_spec(40, n_leads=12)
+    genes = np.stack([synth.genes_for(spec, r, 0) for r in range(5)])
+    worst = _batch_vs_oracle(engine, spec, 400, genes, lambda g: O.layer_aps(
+        3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], "endo-mid-epi", 0.6, g[:12])[0])
+    assert worst <= ECG_TOL
