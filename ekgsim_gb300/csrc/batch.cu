@@ -122,66 +122,90 @@ __global__ void k_static_combine(int steps, int nleads, int nl, int J, int Jb, i
 // ------------------------------------------------------------------ moved-lead operand
 // W'_s[l][a] for the moved leads l < nmove, written as BF16 hi/lo into the tiled B layout:
 // [N tile][K tile][part hi/lo][N*128 bytes], element (row n, k) of a tile at byte
-// ((k/8) * (N/8) + n/8) * 128 + (n%8) * 16 + (k%8) * 2.  One thread per (AP a, simulation s).
+// ((k/8) * (N/8) + n/8) * 128 + (n%8) * 16 + (k%8) * 2.
+// Block = up to 128 simulations (one per thread) x one chunk of 8 consecutive APs, so the voxel
+// data of the chunk is a broadcast load for the warp and each thread writes one 16-byte row
+// segment per part; a warp's 32 simulations x nmove rows are contiguous in the tile.
+// g at p = v + d uses |m - d|^2 = |m|^2 - 2 m.d + |d|^2 with m = r - v, and g.d = (m.d - |d|^2) f,
+// f = |m - d|^-3: one rsqrt and a handful of FMAs per neighbour.
 template <int N>
-__global__ void k_batch_lead_field(int64_t apad, int nkt, const int64_t *__restrict__ a_vox_begin,
-                                   const int32_t *__restrict__ vox_zyx, const uint32_t *__restrict__ nb_in,
-                                   const uint32_t *__restrict__ nb_out, int nnb, const int8_t *__restrict__ difs,
-                                   const double *__restrict__ at, const int32_t *__restrict__ a_layer,
-                                   const double *__restrict__ layer_k, int nl, const double *__restrict__ leads,
-                                   int nleads, int nmove, uint8_t *__restrict__ Bt) {
-    __shared__ int8_t s_dif[26 * 3];
-    if (threadIdx.x < nnb * 3) s_dif[threadIdx.x] = difs[threadIdx.x];
+__global__ void __launch_bounds__(128) k_batch_lead_field(
+    int64_t apad, int nkt, const int64_t *__restrict__ a_vox_begin, const int32_t *__restrict__ vox_zyx,
+    const uint32_t *__restrict__ nb_in, const uint32_t *__restrict__ nb_out, int nnb, const int8_t *__restrict__ difs,
+    const double *__restrict__ at, const int32_t *__restrict__ a_layer, const double *__restrict__ layer_k, int nl,
+    const double *__restrict__ leads, int nleads, int nmove, int n_sims, uint8_t *__restrict__ Bt) {
+    __shared__ float s_d[26 * 4];
+    if (threadIdx.x < nnb) {
+        const float dz = difs[3 * threadIdx.x], dy = difs[3 * threadIdx.x + 1], dx = difs[3 * threadIdx.x + 2];
+        s_d[4 * threadIdx.x] = dz;
+        s_d[4 * threadIdx.x + 1] = dy;
+        s_d[4 * threadIdx.x + 2] = dx;
+        s_d[4 * threadIdx.x + 3] = dz * dz + dy * dy + dx * dx;
+    }
     __syncthreads();
-    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int s = blockIdx.y;
-    if (a >= apad) return;
-    const double aa = at[a];
-    const bool pad = isinf(aa);
-    const float e = pad ? 0.f : expf((float)(layer_k[((size_t)s * nl + a_layer[a]) * 9 + 5] * aa));
-    const int64_t v0 = a_vox_begin[a], v1 = a_vox_begin[a + 1];
-    const int kt = (int)(a / BKT), k = (int)(a % BKT);
+    const int64_t a0 = (int64_t)blockIdx.x * 8;
+    const int s = blockIdx.y * blockDim.x + threadIdx.x;
+    if (s >= n_sims) return;
+    const int kt = (int)(a0 / BKT), kc = (int)((a0 % BKT) / 8);
+    float e[8];
+    int64_t vb[9];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const double aa = at[a0 + j];
+        e[j] = isinf(aa) ? 0.f : expf((float)(layer_k[((size_t)s * nl + a_layer[a0 + j]) * 9 + 5] * aa));
+        vb[j] = a_vox_begin[a0 + j];
+    }
+    vb[8] = a_vox_begin[a0 + 8];
     for (int l = 0; l < nmove; ++l) {
         const double *r = leads + ((size_t)s * nleads + l) * 3;
         const float rz = (float)r[0], ry = (float)r[1], rx = (float)r[2];
         const float rzl = (float)(r[0] - (double)rz), ryl = (float)(r[1] - (double)ry), rxl = (float)(r[2] - (double)rx);
-        double acc = 0.0;
-        for (int64_t v = v0; v < v1; ++v) {
-            const int32_t p = vox_zyx[v];
-            const float pz = (float)((p >> 20) + 1), py = (float)(((p >> 10) & 1023) + 1), px = (float)((p & 1023) + 1);
-            const uint32_t mi = nb_in[v], mo = nb_out[v];
-            float w = 0.f, sz = 0.f, sy = 0.f, sx = 0.f;
-            for (int n = 0; n < nnb; ++n) {
-                const float dz = s_dif[3 * n], dy = s_dif[3 * n + 1], dx = s_dif[3 * n + 2];
-                if (mi & (1u << n)) {
-                    const float mz = (rz - (pz + dz)) + rzl, my = (ry - (py + dy)) + ryl, mx = (rx - (px + dx)) + rxl;
-                    const float ss = fmaf(mz, mz, fmaf(my, my, mx * mx));
-                    const float rs = rsqrtf(ss);
-                    w = fmaf(rs * rs * rs, fmaf(mz, dz, fmaf(my, dy, mx * dx)), w);
+        float wv[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            float acc = 0.f;
+            for (int64_t v = vb[j]; v < vb[j + 1]; ++v) {
+                const int32_t p = vox_zyx[v];
+                const uint32_t mi = nb_in[v], mo = nb_out[v];
+                // m = r - x, x the bordered voxel position (simlib/simulator.cpp:458-463, 531-532)
+                const float mz = (rz - (float)((p >> 20) + 1)) + rzl;
+                const float my = (ry - (float)(((p >> 10) & 1023) + 1)) + ryl;
+                const float mx = (rx - (float)((p & 1023) + 1)) + rxl;
+                const float s0 = fmaf(mz, mz, fmaf(my, my, mx * mx));
+                float w = 0.f, oz = 0.f, oy = 0.f, ox = 0.f;
+                for (int n = 0; n < nnb; ++n) {
+                    const float4 d = reinterpret_cast<const float4 *>(s_d)[n];
+                    if (mi & (1u << n)) {
+                        const float md = fmaf(mz, d.x, fmaf(my, d.y, mx * d.z));
+                        const float sd = fmaf(-2.f, md, s0 + d.w);
+                        const float rs = rsqrtf(sd);
+                        w = fmaf(rs * rs * rs, md - d.w, w);
+                    }
+                    if (mo & (1u << n)) {
+                        oz += d.x;
+                        oy += d.y;
+                        ox += d.z;
+                    }
                 }
-                if (mo & (1u << n)) {
-                    sz += dz;
-                    sy += dy;
-                    sx += dx;
+                if (mo) {
+                    const float rs = rsqrtf(s0);
+                    w = fmaf(-(rs * rs * rs), fmaf(mz, oz, fmaf(my, oy, mx * ox)), w);
                 }
+                acc += w;
             }
-            if (mo) {
-                const float mz = (rz - pz) + rzl, my = (ry - py) + ryl, mx = (rx - px) + rxl;
-                const float ss = fmaf(mz, mz, fmaf(my, my, mx * mx));
-                const float rs = rsqrtf(ss);
-                w = fmaf(-(rs * rs * rs), fmaf(mz, sz, fmaf(my, sy, mx * sx)), w);
-            }
-            acc += (double)w;
+            wv[j] = acc * e[j];
         }
-        const float wv = pad ? 0.f : (float)acc * e;
-        const __nv_bfloat16 hi = __float2bfloat16_rn(wv);
-        const __nv_bfloat16 lo = __float2bfloat16_rn(wv - __bfloat162float(hi));
+        uint4 hv, lv;
+        split2(wv[0], wv[1], hv.x, lv.x);
+        split2(wv[2], wv[3], hv.y, lv.y);
+        split2(wv[4], wv[5], hv.z, lv.z);
+        split2(wv[6], wv[7], hv.w, lv.w);
         const int row = s * nmove + l;
         const int nt = row / N, n = row % N;
         const size_t tile = ((size_t)nt * nkt + kt) * 2;
-        const size_t off = (size_t)((k / 8) * (N / 8) + n / 8) * 128 + (n % 8) * 16 + (k % 8) * 2;
-        *reinterpret_cast<__nv_bfloat16 *>(Bt + tile * (N * 128) + off) = hi;
-        *reinterpret_cast<__nv_bfloat16 *>(Bt + (tile + 1) * (N * 128) + off) = lo;
+        const size_t off = (size_t)(kc * (N / 8) + n / 8) * 128 + (n % 8) * 16;
+        *reinterpret_cast<uint4 *>(Bt + tile * (N * 128) + off) = hv;
+        *reinterpret_cast<uint4 *>(Bt + (tile + 1) * (N * 128) + off) = lv;
     }
 }
 
@@ -197,6 +221,11 @@ struct BatchSmem {
 };
 
 // grid (t tiles, N tiles, K chunks).  Chunk c covers K tiles [ck0[c], ck1[c]) inside layer cl[c].
+// The tensor core's FP32 accumulation loses accuracy over long K (measured: relative ECG error
+// grows with the K length of one accumulation), so the K range is cut into segments of
+// DRAIN tiles (512 APs): segment g accumulates in TMEM set g % 2 while the threads drain set
+// (g - 1) % 2 into FP32 registers (each thread owns one row and half of the columns).
+constexpr int DRAIN = 8;
 template <int NB, int N>
 __global__ void __launch_bounds__(BTHREADS, 1) k_batch_umma(
     int steps, int nl, int nkt, int rows, int nmove, int n_sims, const float2 *__restrict__ t_hilo,
@@ -207,11 +236,14 @@ __global__ void __launch_bounds__(BTHREADS, 1) k_batch_umma(
     extern __shared__ uint8_t smem_raw[];
     BatchSmem<NB, N> &S =
         *reinterpret_cast<BatchSmem<NB, N> *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    constexpr uint32_t TCOLS = NB * N;  // 256
+    constexpr uint32_t SET = NB * N;        // columns of one accumulator set
+    constexpr uint32_t TCOLS = 2 * SET;     // 512
     constexpr uint32_t IDESC = idesc_bf16(BM, N);
     constexpr uint32_t A_LBO = (BM / 8) * 128, A_SBO = 128;
     constexpr uint32_t B_LBO = (N / 8) * 128, B_SBO = 128;
     constexpr uint32_t BPART = N * BKT * 2;
+    constexpr int HALF = N / 2;             // columns per thread per basis
+    constexpr int NACC = NB * HALF;         // 128
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int t0 = blockIdx.x * BM, nt = blockIdx.y, c = blockIdx.z;
@@ -234,9 +266,29 @@ __global__ void __launch_bounds__(BTHREADS, 1) k_batch_umma(
     tc_fence_after();
     const uint32_t tmem = S.tmem_base;
 
+    const int q = warp & 3, ch = warp >> 2;  // TMEM lane quadrant and column half of this warp
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
+    float acc[NACC];
+#pragma unroll
+    for (int i = 0; i < NACC; ++i) acc[i] = 0.f;
+    auto drain = [&](int g) {
+        const uint32_t base = lane_addr + (uint32_t)((g & 1) * SET);
+#pragma unroll
+        for (int bsi = 0; bsi < NB; ++bsi)
+#pragma unroll
+            for (int cb = 0; cb < HALF; cb += 16) {
+                float v[16];
+                tmem_ld16(base + (uint32_t)(bsi * N + ch * HALF + cb), v);
+#pragma unroll
+                for (int jj = 0; jj < 16; ++jj) acc[bsi * HALF + cb + jj] += v[jj];
+            }
+    };
+
     const int row = tid & (BM - 1), half = tid >> 7;
     const float2 th = t_hilo[min(t0 + row, steps - 1)];
     const int nk = kt1 - kt0;
+    const int nseg = (nk + DRAIN - 1) / DRAIN;
+    int drained = 0;
     bool ok = true;
     for (int i = 0; i < nk; ++i) {
         const int b = i & 1;
@@ -246,6 +298,12 @@ __global__ void __launch_bounds__(BTHREADS, 1) k_batch_umma(
             if (__syncthreads_or(!ok)) {
                 ok = false;
                 break;
+            }
+            if ((i - 1) % DRAIN == 0) {  // tile i-2 closed segment (i-2)/DRAIN
+                tc_fence_after();
+                drain((i - 2) / DRAIN);
+                drained = (i - 2) / DRAIN + 1;
+                tc_fence_before();
             }
         }
         if (tid == 0) {
@@ -300,18 +358,20 @@ __global__ void __launch_bounds__(BTHREADS, 1) k_batch_umma(
                 atomicOr(err, KERR_MBAR_TIMEOUT);
             } else {
                 tc_fence_after();
+                const uint32_t set = (uint32_t)(((i / DRAIN) & 1) * SET);
+                const bool first = (i % DRAIN) == 0;
                 const uint32_t bh = smem_u32(S.b[b][0]), bl = smem_u32(S.b[b][1]);
 #pragma unroll
                 for (int j = 0; j < BKT / 16; ++j) {
                     const uint64_t dbh = sdesc(bh + j * 2 * B_LBO, B_LBO, B_SBO);
                     const uint64_t dbl = sdesc(bl + j * 2 * B_LBO, B_LBO, B_SBO);
 #pragma unroll
-                    for (int q = 0; q < NB; ++q) {
-                        const uint32_t ah = smem_u32(S.a[b][q][0]), al = smem_u32(S.a[b][q][1]);
+                    for (int qb = 0; qb < NB; ++qb) {
+                        const uint32_t ah = smem_u32(S.a[b][qb][0]), al = smem_u32(S.a[b][qb][1]);
                         const uint64_t dah = sdesc(ah + j * 2 * A_LBO, A_LBO, A_SBO);
                         const uint64_t dal = sdesc(al + j * 2 * A_LBO, A_LBO, A_SBO);
-                        const uint32_t d = tmem + (uint32_t)(q * N);
-                        mma_bf16(d, dah, dbh, IDESC, (i > 0 || j > 0) ? 1u : 0u);
+                        const uint32_t d = tmem + set + (uint32_t)(qb * N);
+                        mma_bf16(d, dah, dbh, IDESC, (first && j == 0) ? 0u : 1u);
                         mma_bf16(d, dah, dbl, IDESC, 1u);
                         mma_bf16(d, dal, dbh, IDESC, 1u);
                     }
@@ -320,35 +380,30 @@ __global__ void __launch_bounds__(BTHREADS, 1) k_batch_umma(
             mma_commit(&S.done[b]);
         }
     }
-    if (nk > 0) {
+    if (nk > 0 && ok) {
         const int last = (nk - 1) & 1;
         if (!mbar_wait(&S.done[last], (uint32_t)(((nk - 1) >> 1) & 1))) ok = false;
     }
     ok = !__syncthreads_or(!ok);
     tc_fence_after();
     if (ok && nk > 0 && *err == 0) {
-        const int q = warp & 3, ch = warp >> 2;
+        for (int g = drained; g < nseg; ++g) drain(g);
         const int t = t0 + 32 * q + lane;
-        for (int cb = ch * (N / 2); cb < (ch + 1) * (N / 2); cb += 16) {
-            float y1[16], y2[16];
-            tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)cb, y1);
-            if (NB == 2) tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(N + cb), y2);
-            if (t < steps) {
+        if (t < steps) {
 #pragma unroll
-                for (int jj = 0; jj < 16; ++jj) {
-                    const int r = nt * N + cb + jj;
-                    const int s = r / nmove;
-                    if (s >= n_sims) continue;
-                    const double f = F[((size_t)s * nl + L) * steps + t];
-                    double v;
-                    if (NB == 2) {
-                        const double kk = k3[(size_t)s * nl + L];
-                        v = ((1.0 - kk) * (double)y1[jj] + kk * (double)y2[jj]) * f;
-                    } else {
-                        v = (double)y1[jj] * f;
-                    }
-                    partial[((size_t)c * rows + r) * steps + t] = v;
+            for (int jj = 0; jj < HALF; ++jj) {
+                const int r = nt * N + ch * HALF + jj;
+                const int s = r / nmove;
+                if (s >= n_sims) continue;
+                const double f = F[((size_t)s * nl + L) * steps + t];
+                double v;
+                if (NB == 2) {
+                    const double kk = k3[(size_t)s * nl + L];
+                    v = ((1.0 - kk) * (double)acc[jj] + kk * (double)acc[HALF + jj]) * f;
+                } else {
+                    v = (double)acc[jj] * f;
                 }
+                partial[((size_t)c * rows + r) * steps + t] = v;
             }
         }
     } else if (!ok && tid == 0) {
@@ -423,16 +478,17 @@ void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int
 
 void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const double *layer_k,
                              const double *leads, int nmove, int n_sims, uint8_t *Bt) {
-    dim3 grid((unsigned)((h.apad + 127) / 128), (unsigned)n_sims);
+    const int threads = n_sims < 128 ? ((n_sims + 31) / 32) * 32 : 128;
+    dim3 grid((unsigned)(h.apad / 8), (unsigned)((n_sims + threads - 1) / threads));
     const int nkt = (int)(h.apad / BKT);
     if (two_bases)
-        k_batch_lead_field<128><<<grid, 128, 0, s>>>(h.apad, nkt, h.a_vox_begin.p, h.vox_zyx.p, h.vox_nb.p,
-                                                     h.vox_nbo.p, h.nnb, h.difs.p, h.at.p, h.a_layer.p, layer_k,
-                                                     h.nlayers, leads, h.nleads, nmove, Bt);
+        k_batch_lead_field<128><<<grid, threads, 0, s>>>(h.apad, nkt, h.a_vox_begin.p, h.vox_zyx.p, h.vox_nb.p,
+                                                         h.vox_nbo.p, h.nnb, h.difs.p, h.at.p, h.a_layer.p, layer_k,
+                                                         h.nlayers, leads, h.nleads, nmove, n_sims, Bt);
     else
-        k_batch_lead_field<256><<<grid, 128, 0, s>>>(h.apad, nkt, h.a_vox_begin.p, h.vox_zyx.p, h.vox_nb.p,
-                                                     h.vox_nbo.p, h.nnb, h.difs.p, h.at.p, h.a_layer.p, layer_k,
-                                                     h.nlayers, leads, h.nleads, nmove, Bt);
+        k_batch_lead_field<256><<<grid, threads, 0, s>>>(h.apad, nkt, h.a_vox_begin.p, h.vox_zyx.p, h.vox_nb.p,
+                                                         h.vox_nbo.p, h.nnb, h.difs.p, h.at.p, h.a_layer.p, layer_k,
+                                                         h.nlayers, leads, h.nleads, nmove, n_sims, Bt);
     EKG_CUDA(cudaGetLastError());
 }
 

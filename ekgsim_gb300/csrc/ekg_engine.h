@@ -12,6 +12,7 @@ struct ekg_engine {
     int chunk_len = 512;  // APs per K chunk of the contraction (multiple of 64)
     bool umma = true;     // tensor-core contraction (EKG_CONTRACT=cuda selects the CUDA-core kernel)
     bool batched = true;  // separable batched form for multi-simulation passes (EKG_BATCHED=0 disables)
+    int batch_ctas = 0;   // target CTAs of the moved-lead GEMM (0 = two per SM)
 };
 
 namespace ekg {

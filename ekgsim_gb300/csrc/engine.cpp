@@ -561,7 +561,7 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
         for (int i = 0; i < nl; ++i)
             if (kb[i] >= 0) kt_total += ke[i] - kb[i];
         const int ttiles = (D.steps + 127) / 128;
-        const int target = 2 * h->sm_count;
+        const int target = h->eng->batch_ctas > 0 ? h->eng->batch_ctas : 2 * h->sm_count;
         const int per = std::max(1, (int)std::ceil((double)target / (ttiles * P.ntiles)));
         for (int i = 0; i < nl; ++i) {
             if (kb[i] < 0) continue;
@@ -991,6 +991,7 @@ int ekg_engine_create(int device, ekg_engine **out) {
         if (const char *v = std::getenv("EKG_CONTRACT")) e->umma = std::string(v) != "cuda";
         if (const char *v = std::getenv("EKG_CHUNK")) e->chunk_len = std::max(64, std::atoi(v) / 64 * 64);
         if (const char *v = std::getenv("EKG_BATCHED")) e->batched = std::string(v) != "0";
+        if (const char *v = std::getenv("EKG_BATCH_CTAS")) e->batch_ctas = std::atoi(v);
         EKG_CUDA(cudaSetDevice(device));
         EKG_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
         *out = e.release();

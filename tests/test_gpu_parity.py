@@ -156,8 +156,9 @@ def test_batch_matches_single(engine, tmp_path):
     crit_b, viol_b, ecg_b = h.eval_batch(genes, want_ecg=True)
     for i in range(5):
         crit, viol, ecg, _, _ = h.eval(genes[i], want_ecg=True)
-        assert np.allclose(ecg_b[i], ecg, rtol=0, atol=1e-9 * np.abs(ecg).max())
-        assert np.allclose(crit_b[i], crit, rtol=0, atol=1e-9)
+        # the batch runs the separable batched form, the single call the per-simulation form
+        assert rel_l2(ecg_b[i], ecg) <= ECG_TOL
+        assert np.allclose(crit_b[i], crit, rtol=0, atol=1e-4)
         assert viol_b[i] == viol
 
 
