@@ -91,6 +91,8 @@ SIGNATURES = {
     "ekg_server_poll": (ctypes.c_int, [ctypes.c_void_p, c_uint64, c_int32, P(c_double), P(c_double), P(c_double),
                                        P(RequestStats)]),
     "ekg_server_set_free_bytes_provider": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "ekg_activation_noalloc": (ctypes.c_int, [c_int32, c_int32, c_int32, ctypes.c_void_p, c_int32, P(c_double),
+                                              ctypes.c_void_p, P(c_int32)]),
     "ekg_heart_from_ini": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, P(ctypes.c_void_p)]),
     "ekg_move_leads": (ctypes.c_int, [c_int32, P(c_double), P(c_double), P(c_double)]),
     "ekg_layer_aps": (ctypes.c_int, [P(EvalConfig), c_int32, P(c_double), P(c_double), P(c_double)]),

@@ -15,7 +15,9 @@
 // interior voxels are written back, and the neighbour tiles that touch a changed face, edge or
 // corner are flagged.  A compaction kernel turns the flags into the next round's tile list with
 // warp ballots and one atomic per warp.  The host loops until no tile is active.
+#include <cmath>
 #include <cstdio>
+#include <mutex>
 #include <vector>
 
 #include "ekg_internal.h"
@@ -29,7 +31,11 @@ constexpr int HS = TS + 2;       // tile + halo
 constexpr int CA_THREADS = 256;  // 2 voxels per thread
 constexpr int MAX_LOCAL_ITERS = 64;
 
-__global__ void k_ca_round(int nz, int ny, int nx, int ntz, int nty, int ntx, const uint8_t *__restrict__ layers,
+__device__ __forceinline__ uint8_t layer_id(uint8_t v) { return v; }
+__device__ __forceinline__ uint8_t layer_id(int32_t v) { return (uint8_t)(v < 0 ? -v : v); }
+
+template <typename LT>
+__global__ void k_ca_round(int nz, int ny, int nx, int ntz, int nty, int ntx, const LT *__restrict__ layers,
                            const double *__restrict__ lag, int nl1, double *__restrict__ at,
                            const int32_t *__restrict__ active, uint8_t *__restrict__ next_flag) {
     __shared__ double s_at[HS][HS][HS];
@@ -51,7 +57,7 @@ __global__ void k_ca_round(int nz, int ny, int nx, int ntz, int nty, int ntx, co
         uint8_t l = 0;
         if (gx >= 0 && gx < nx && gy >= 0 && gy < ny && gz >= 0 && gz < nz) {
             size_t g = ((size_t)gz * ny + gy) * nx + gx;
-            l = layers[g];
+            l = layer_id(layers[g]);
             if (l) a = at[g];
         }
         s_at[hz][hy][hx] = a;
@@ -207,8 +213,8 @@ CaResult ca_run(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_layers,
             cudaFreeHost(h_count);
             throw Error{EKG_ERR_CA_NOT_CONVERGED, "activation-time relaxation did not converge"};
         }
-        k_ca_round<<<n_active, CA_THREADS, 0, s>>>(nz, ny, nx, ntz, nty, ntx, d_layers, d_lag, nl1, d_at, cur,
-                                                  flag.p);
+        k_ca_round<uint8_t><<<n_active, CA_THREADS, 0, s>>>(nz, ny, nx, ntz, nty, ntx, d_layers, d_lag, nl1, d_at,
+                                                           cur, flag.p);
         EKG_CUDA(cudaGetLastError());
         EKG_CUDA(cudaMemsetAsync(count.p, 0, sizeof(int32_t), s));
         k_ca_compact<<<(ntiles + 255) / 256, 256, 0, s>>>(ntiles, flag.p, nxt, count.p);
@@ -230,4 +236,161 @@ CaResult ca_run(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_layers,
     return res;
 }
 
+
+
+// ------------------------------------------------------------------ no-allocation entry point
+// ekg_activation_noalloc: the same relaxation for callers that cannot allocate device memory
+// (for example code running under a memory pool or allocator that forbids new cudaMalloc calls
+// after start-up, or inside a host loop that must not touch the allocator).  All scratch lives in
+// one file-scope device array, g_noalloc, of fixed size; the caller supplies the layer grid and
+// the output as device buffers it already owns.  Every call shares g_noalloc and leaves its last
+// contents behind, so the counters and flags are cleared at the start of each call; a host mutex
+// serialises callers in this process, and calls whose device work overlaps (for example from
+// another thread that bypasses this entry point's lock) would race on the array.
+namespace {
+constexpr int NOALLOC_MAX_TILES = 65536;  // 8x8x8 tiles, e.g. a 320^3 grid
+constexpr int NOALLOC_MAX_LAYER = 31;     // highest layer id (lag table 32 x 32 x 3)
+struct NoAllocScratch {
+    int32_t list[2][NOALLOC_MAX_TILES];
+    uint8_t flag[NOALLOC_MAX_TILES];
+    int32_t count;
+    int32_t nstart;
+    uint32_t layer_mask;
+    int32_t bad;
+    double lag[(NOALLOC_MAX_LAYER + 1) * (NOALLOC_MAX_LAYER + 1) * 3];
+};
+static __device__ __align__(256) NoAllocScratch g_noalloc;
+
+// per-device address of g_noalloc (host code may not use the symbol itself as an address)
+std::mutex g_noalloc_mu;
+NoAllocScratch *g_noalloc_ptr[64] = {nullptr};
+
+__global__ void k_na_validate(size_t n, const int32_t *__restrict__ layers, NoAllocScratch *sc) {
+    uint32_t mask = 0;
+    int32_t starts = 0, bad = 0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int32_t v = layers[i];
+        const int32_t a = v < 0 ? -v : v;
+        if (a > NOALLOC_MAX_LAYER) bad = 1;
+        else mask |= 1u << a;
+        starts += v < 0;
+    }
+    mask = __reduce_or_sync(0xffffffffu, mask);
+    starts = __reduce_add_sync(0xffffffffu, starts);
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0) {
+        if (mask) atomicOr(&sc->layer_mask, mask);
+        if (starts) atomicAdd(&sc->nstart, starts);
+        if (bad) atomicOr(&sc->bad, 1);
+    }
+}
+
+__global__ void k_na_init(int nz, int ny, int nx, int nty, int ntx, const int32_t *__restrict__ layers,
+                          double *__restrict__ at, uint8_t *__restrict__ flag) {
+    const size_t n = (size_t)nz * ny * nx;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int32_t v = layers[i];
+        double a = 0.0;
+        if (v < 0) {
+            a = 1.0;
+            const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((size_t)nx * ny));
+            flag[((size_t)(z / TS) * nty + (y / TS)) * ntx + (x / TS)] = 1;
+        } else if (v > 0) {
+            a = __longlong_as_double(0x7ff0000000000000LL);
+        }
+        at[i] = a;
+    }
+}
+
+NoAllocScratch *noalloc_scratch() {
+    int dev = 0;
+    EKG_CUDA(cudaGetDevice(&dev));
+    EKG_CHECK(dev >= 0 && dev < 64, EKG_ERR_DEVICE, "device index out of range");
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        EKG_CUDA(cudaGetSymbolAddress(&p, g_noalloc));
+        g_noalloc_ptr[dev] = reinterpret_cast<NoAllocScratch *>(p);
+    }
+    return g_noalloc_ptr[dev];
+}
+}  // namespace
+
 }  // namespace ekg
+
+extern "C" int ekg_activation_noalloc(int32_t nz, int32_t ny, int32_t nx, const int32_t *d_layers, int32_t n_transfer,
+                                      const double *transfer, double *d_at, int32_t *rounds_out) {
+    using namespace ekg;
+    return guard([&] {
+        EKG_CHECK(d_layers && transfer && d_at && n_transfer >= 1, EKG_ERR_BAD_INPUT, "null argument");
+        EKG_CHECK(nz >= 1 && ny >= 1 && nx >= 1, EKG_ERR_BAD_INPUT, "grid extents must be positive");
+        const int ntz = (nz + TS - 1) / TS, nty = (ny + TS - 1) / TS, ntx = (nx + TS - 1) / TS;
+        const int64_t ntiles = (int64_t)ntz * nty * ntx;
+        EKG_CHECK(ntiles <= NOALLOC_MAX_TILES, EKG_ERR_BAD_INPUT,
+                  "grid too large for ekg_activation_noalloc: at most 65536 tiles of 8x8x8 cells");
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        NoAllocScratch *sc = noalloc_scratch();
+        const size_t n = (size_t)nz * ny * nx;
+        cudaStream_t s = 0;
+        // clear what must start at zero: flags, counters, layer mask
+        EKG_CUDA(cudaMemsetAsync(sc->flag, 0, sizeof(sc->flag), s));
+        EKG_CUDA(cudaMemsetAsync(&sc->count, 0, 4 * sizeof(int32_t), s));
+        k_na_validate<<<1024, 256, 0, s>>>(n, d_layers, sc);
+        EKG_CUDA(cudaGetLastError());
+        struct {
+            int32_t count, nstart;
+            uint32_t mask;
+            int32_t bad;
+        } hdr;
+        EKG_CUDA(cudaMemcpy(&hdr, &sc->count, sizeof(hdr), cudaMemcpyDeviceToHost));
+        EKG_CHECK(!hdr.bad, EKG_ERR_BAD_INPUT, "layer ids must be at most 31 for ekg_activation_noalloc");
+        EKG_CHECK(hdr.nstart > 0, EKG_ERR_NO_START, "Could not find starting point for excitation sequence");
+        int nl = 0;
+        for (int a = 1; a <= NOALLOC_MAX_LAYER; ++a)
+            if (hdr.mask & (1u << a)) {
+                nl = a;
+                if (a >= n_transfer)
+                    throw Error{EKG_ERR_TRANSFER, "transfer (conduction) matrix does not define layer " + std::to_string(a)};
+            }
+        const int nl1 = nl + 1;
+        double lag[(NOALLOC_MAX_LAYER + 1) * (NOALLOC_MAX_LAYER + 1) * 3];
+        for (int i = 0; i < nl1 * nl1 * 3; ++i) lag[i] = 0.0;
+        for (int a = 1; a <= nl; ++a)
+            for (int b = 1; b <= nl; ++b) {
+                if (!((hdr.mask >> a) & 1u) || !((hdr.mask >> b) & 1u)) continue;
+                const double t = transfer[(size_t)a * n_transfer + b];
+                EKG_CHECK(t >= 0 && std::isfinite(t), EKG_ERR_BAD_INPUT,
+                          "conduction delays between present layers must be finite and non-negative");
+                for (int k = 1; k <= 3; ++k) {
+                    double l = t;
+                    l *= std::sqrt((double)k);
+                    lag[((size_t)a * nl1 + b) * 3 + (k - 1)] = l;
+                }
+            }
+        EKG_CUDA(cudaMemcpy(sc->lag, lag, (size_t)nl1 * nl1 * 3 * sizeof(double), cudaMemcpyHostToDevice));
+        k_na_init<<<1024, 256, 0, s>>>(nz, ny, nx, nty, ntx, d_layers, d_at, sc->flag);
+        EKG_CUDA(cudaGetLastError());
+        int32_t *cur = sc->list[0], *nxt = sc->list[1];
+        k_ca_compact<<<(unsigned)((ntiles + 255) / 256), 256, 0, s>>>((int)ntiles, sc->flag, cur, &sc->count);
+        EKG_CUDA(cudaGetLastError());
+        int32_t n_active = 0;
+        EKG_CUDA(cudaMemcpy(&n_active, &sc->count, sizeof(int32_t), cudaMemcpyDeviceToHost));
+        const int cap = 16 * (ntz + nty + ntx) + 4 * (int)ntiles + 64;
+        int rounds = 0;
+        while (n_active > 0) {
+            EKG_CHECK(rounds < cap, EKG_ERR_CA_NOT_CONVERGED, "activation-time relaxation did not converge");
+            k_ca_round<int32_t><<<n_active, CA_THREADS, 0, s>>>(nz, ny, nx, ntz, nty, ntx, d_layers, sc->lag, nl1,
+                                                               d_at, cur, sc->flag);
+            EKG_CUDA(cudaGetLastError());
+            EKG_CUDA(cudaMemsetAsync(&sc->count, 0, sizeof(int32_t), s));
+            k_ca_compact<<<(unsigned)((ntiles + 255) / 256), 256, 0, s>>>((int)ntiles, sc->flag, nxt, &sc->count);
+            EKG_CUDA(cudaGetLastError());
+            EKG_CUDA(cudaMemcpy(&n_active, &sc->count, sizeof(int32_t), cudaMemcpyDeviceToHost));
+            std::swap(cur, nxt);
+            ++rounds;
+        }
+        k_ca_finish<<<1024, 256, 0, s>>>(n, d_at);
+        EKG_CUDA(cudaGetLastError());
+        EKG_CUDA(cudaStreamSynchronize(s));
+        if (rounds_out) *rounds_out = rounds;
+    });
+}

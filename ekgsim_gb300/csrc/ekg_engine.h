@@ -27,7 +27,6 @@ struct EvalSettings {
     std::vector<double> disp_min_v, disp_max_v;
     int n_crit_leads = 0, n_criteria = 0, n_genes = 0;
 };
-int guard(const std::function<void()> &f);
 }  // namespace ekg
 
 namespace ekg {

@@ -6,6 +6,7 @@
 
 #include <atomic>
 #include <condition_variable>
+#include <functional>
 #include <deque>
 #include <map>
 #include <memory>
@@ -35,6 +36,9 @@ struct Error {
     do {                                                                                    \
         if (!(cond)) throw ::ekg::Error{(code), (msg)};                                     \
     } while (0)
+
+// Runs f, mapping a thrown Error / std::exception to a status code and the thread's last error.
+int guard(const std::function<void()> &f);
 
 // Kernel error word bits (written by bounded device waits, read by the host after a pass).
 enum : uint32_t { KERR_MBAR_TIMEOUT = 1u, KERR_TMEM = 2u };

@@ -198,6 +198,23 @@ int ekg_server_poll(ekg_server *s, uint64_t request_id, int32_t wait_ms, double 
  * bytes; NULL restores cudaMemGetInfo).  Lets tests refuse admission without filling the GPU. */
 int ekg_server_set_free_bytes_provider(ekg_server *s, uint64_t (*fn)(void *ctx), void *ctx);
 
+/* Activation times without any device allocation, for callers that cannot call cudaMalloc (for
+ * example code running under a framework's memory pool or a real-time loop that forbids new
+ * device allocations after start-up).  No counterpart in the reference, which has no device.
+ *   d_layers: device buffer, nz*ny*nx int32 cells with the ekg_heart_desc.layers convention
+ *             (0 empty, L > 0 layer, -L stimulus voxel of layer L); layer ids at most 31
+ *   transfer: host buffer, n_transfer x n_transfer conduction matrix (ms)
+ *   d_at:     device buffer, nz*ny*nx doubles; receives the activation times (0 = empty or
+ *             unreachable), bit-identical to ekg_heart_activation
+ * Scratch is one fixed device array inside the library (about 600 KB per GPU that loads it, held
+ * until the process exits); grids of more than 65536 tiles of 8x8x8 cells are rejected with
+ * EKG_ERR_BAD_INPUT.  The first call on a device looks the array's device address up, so make the
+ * first call before any stream capture.  Calls run on the legacy default stream and return when
+ * the result is in d_at; calls in one process are serialised, and device work of two calls must
+ * not overlap (they share the array). */
+int ekg_activation_noalloc(int32_t nz, int32_t ny, int32_t nx, const int32_t *d_layers, int32_t n_transfer,
+                           const double *transfer, double *d_at, int32_t *rounds_out);
+
 /* ------------------------------------------------------------------ files */
 /* Build a heart and its eval config from a simulator.ini and the files it names, as the
  * SimImplementation constructor does (sim.cpp:362-431): settings, transfer matrix, measuring
