@@ -510,14 +510,24 @@ void layer_aps_from_genes(const GeneModel &m, int nl, const double *genes, doubl
     static const double kd[9] = {0, 0, 0, 0.001, 0, 0.00005, 0.0005, 0.01, 0.2};
     AP d;
     std::copy(kd, kd + 9, d.k);
+    // The interpolation evaluator (connectors between two border APs) is only needed for layers
+    // between the gene-set APs; it is built when first used and rebuilt only when its border
+    // APs change, which leaves every result as in sim.cpp:751-916.
     Evaluator ev;
+    int ev_border = -1;  // 0: (front, back), 1: (front, mid), 2: (mid, back)
+    auto border = [&](int which, const AP &a, const AP &b) {
+        if (ev_border != which) {
+            ev.set_border(a, b);
+            ev_border = which;
+        }
+    };
     const std::vector<double> &front = m.base.front(), &back = m.base.back();
     if (m.interpolation == 1) {
         aps[0] = fill(front);
         aps[nl - 1] = fill(back);
-        ev.set_border(aps[0], aps[nl - 1]);
         for (int i = 1; i < nl - 1; ++i) {
             const double ratio = i / double(nl - 1);
+            border(0, aps[0], aps[nl - 1]);
             ev.set_ratio(ratio);
             aps[i] = aps[i - 1];
             combine(aps[i], aps[0], aps[nl - 1], ratio);
@@ -528,17 +538,16 @@ void layer_aps_from_genes(const GeneModel &m, int nl, const double *genes, doubl
         aps[0] = fill(front);
         aps[mid] = fill(back);  // the mid AP starts from the last base AP (sim.cpp:855-864)
         aps[nl - 1] = fill(back);
-        ev.set_border(aps[0], aps[nl - 1]);
         for (size_t i = 1; i + 1 < (size_t)nl; ++i) {
             if (i < mid) {
                 const double ratio = i / double(mid);
-                ev.set_border(aps[0], aps[mid]);
+                border(1, aps[0], aps[mid]);
                 ev.set_ratio(ratio);
                 aps[i] = aps[i - 1];
                 combine(aps[i], aps[0], aps[mid], ratio);
             } else if (i > mid) {
                 const double ratio = (i - mid) / double(nl - mid - 1);
-                if (i - mid == 1) ev.set_border(aps[mid], aps[nl - 1]);
+                border(2, aps[mid], aps[nl - 1]);
                 ev.set_ratio(ratio);
                 aps[i] = aps[i - 1];
                 combine(aps[i], aps[mid], aps[nl - 1], ratio);
