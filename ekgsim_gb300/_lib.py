@@ -72,6 +72,7 @@ SIGNATURES = {
     "ekg_heart_create": (ctypes.c_int, [ctypes.c_void_p, P(HeartDesc), P(ctypes.c_void_p)]),
     "ekg_heart_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "ekg_heart_get_info": (ctypes.c_int, [ctypes.c_void_p, P(HeartInfo)]),
+    "ekg_heart_time_axis": (ctypes.c_int, [ctypes.c_void_p, P(c_double), P(c_double), P(c_double)]),
     "ekg_heart_activation": (ctypes.c_int, [ctypes.c_void_p, P(c_double)]),
     "ekg_heart_ap_index": (ctypes.c_int, [ctypes.c_void_p, P(c_int64)]),
     "ekg_simulate": (ctypes.c_int, [ctypes.c_void_p, P(c_double), P(c_double), P(c_double)]),
@@ -94,6 +95,8 @@ SIGNATURES = {
     "ekg_activation_noalloc": (ctypes.c_int, [c_int32, c_int32, c_int32, ctypes.c_void_p, c_int32, P(c_double),
                                               ctypes.c_void_p, P(c_int32)]),
     "ekg_heart_from_ini": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, P(ctypes.c_void_p)]),
+    "ekg_ap_value": (c_double, [P(c_double), c_double, c_double]),
+    "ekg_heart_cell_ap": (ctypes.c_int, [ctypes.c_void_p, c_int64, P(c_int32), P(c_double)]),
     "ekg_move_leads": (ctypes.c_int, [c_int32, P(c_double), P(c_double), P(c_double)]),
     "ekg_layer_aps": (ctypes.c_int, [P(EvalConfig), c_int32, P(c_double), P(c_double), P(c_double)]),
 }

@@ -74,6 +74,7 @@ struct ekg_heart {
     std::vector<double> t;            // time axis
     std::vector<double> leads0;       // loaded lead positions (z,y,x)
     std::vector<double> at_host;      // activation time per cell
+    std::vector<uint8_t> layer_host;  // layer id per cell (stimulus flag stripped)
     std::vector<int64_t> ap_index_ref;
     ekg::HeartDev dev;
     ekg::EvalDev ev;

@@ -154,6 +154,7 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
             }
     }
 
+    h->layer_host.assign(lay.begin(), lay.end());
     // activation times on the device
     EKG_CUDA(cudaSetDevice(h->eng->device));
     if (!h->stream) EKG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
@@ -1051,6 +1052,15 @@ int ekg_heart_get_info(ekg_heart *h, ekg_heart_info *info) {
     });
 }
 
+int ekg_heart_time_axis(ekg_heart *h, double *start, double *length, double *dt) {
+    return guard([&] {
+        EKG_CHECK(h, EKG_ERR_BAD_INPUT, "null heart");
+        if (start) *start = h->start;
+        if (length) *length = h->length;
+        if (dt) *dt = h->dt;
+    });
+}
+
 int ekg_heart_activation(ekg_heart *h, double *at_out) {
     return guard([&] {
         EKG_CHECK(h && at_out, EKG_ERR_BAD_INPUT, "null argument");
@@ -1144,6 +1154,27 @@ int ekg_heart_benchmark(ekg_heart *h, int32_t n_sims, const double *layer_k, con
             leads = lds.data();
         }
         benchmark(h, n_sims, layer_k, leads, warmup, iters, out, n_out);
+    });
+}
+
+double ekg_ap_value(const double *k9, double at, double t) {
+    if (!k9) return NAN;
+    double k[9];
+    std::copy(k9, k9 + 9, k);
+    k[8] -= at;
+    return wohlfart(k, t - at);
+}
+
+int ekg_heart_cell_ap(ekg_heart *h, int64_t index, int32_t *layer_out, double *at_out) {
+    return guard([&] {
+        EKG_CHECK(h && layer_out && at_out, EKG_ERR_BAD_INPUT, "null argument");
+        for (int64_t i = 0; i < h->ncell; ++i)
+            if (h->ap_index_ref[i] == index) {
+                *layer_out = h->layer_host[i];
+                *at_out = h->at_host[i];
+                return;
+            }
+        throw Error{EKG_ERR_NOT_FOUND, "no cell AP with that index"};
     });
 }
 

@@ -95,6 +95,8 @@ typedef struct {
 int ekg_heart_create(ekg_engine *e, const ekg_heart_desc *desc, ekg_heart **out);
 int ekg_heart_destroy(ekg_heart *h);
 int ekg_heart_get_info(ekg_heart *h, ekg_heart_info *info);
+/* Simulation window of the heart: start, length and time step in ms. */
+int ekg_heart_time_axis(ekg_heart *h, double *start, double *length, double *dt);
 /* Activation times [nz][ny][nx] (0 = empty or unreachable), the excitationDelay field of the
  * reference's ShapeElement after calculateExcitationSequence (simlib/matrix.h:82-102). */
 int ekg_heart_activation(ekg_heart *h, double *at_out);
@@ -225,6 +227,14 @@ int ekg_heart_from_ini(ekg_engine *e, const char *ini_path, const char *out_dir,
 /* Lead positions after moving them by per-lead (u, v) displacements (n_leads x 2) in the
  * plane basis of EkgSim::loadMeasuringPoints / moveMeasuringPoints (simlib/sim_lib.h:167-208). */
 int ekg_move_leads(int32_t n_leads, const double *orig_zyx, const double *disp_uv, double *out_zyx);
+
+/* Value at time t of the AP of a cell activated at time `at` (WohlfartPlus with k8 shifted by at,
+ * simlib/simulator.cpp:154-170 and simlib/Wohlfart.h:195-203), FP64 on the host.  Used for the
+ * layer_aps / cell_aps outputs (sim.cpp:939-991). */
+double ekg_ap_value(const double *k9, double at, double t);
+/* Layer (1-based) and activation time of the cell AP with the reference's apIndex `index`
+ * (first appearance in raster order, simlib/simulator.cpp:570-590). */
+int ekg_heart_cell_ap(ekg_heart *h, int64_t index, int32_t *layer_out, double *at_out);
 
 /* Layer APs from the Wohlfart genes (sim.cpp:751-916 with nonlinearFit.h:92-168) under the
  * interpolation settings of `cfg` (targets are not read); also the violation (sim.cpp:582-596).
