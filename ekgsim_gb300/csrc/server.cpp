@@ -128,13 +128,14 @@ void worker_loop(ekg_server *s) {
         std::vector<Result> res(batch.size());
         const auto t_start = Clock::now();
         if (!batch.empty()) {
-            int n_genes = (int)batch[0].genes.size();
             bool same = true;
-            for (const Request &r : batch) same = same && (int)r.genes.size() == n_genes;
+            for (const Request &r : batch) same = same && r.genes.size() == batch[0].genes.size();
             const int nc = h->es.n_criteria;
             const size_t ecg_len = (size_t)h->dev.nleads * h->dev.steps;
+            // one device pass over requests [b0, b1), which all have the same gene count
             auto run = [&](size_t b0, size_t b1) {
                 const int n = (int)(b1 - b0);
+                const int n_genes = (int)batch[b0].genes.size();
                 std::vector<double> g((size_t)n * n_genes), crit((size_t)n * nc), viol(n), ecg((size_t)n * ecg_len);
                 for (int i = 0; i < n; ++i) std::copy(batch[b0 + i].genes.begin(), batch[b0 + i].genes.end(),
                                                       g.begin() + (size_t)i * n_genes);

@@ -91,7 +91,10 @@ def test_cli_matches_reference(name, tmp_path):
 
 def test_cli_errors_print_and_exit_zero(tmp_path):
     c = make_case("tiny24", tmp_path)
-    r = run_cli(str(tmp_path), c["genes"][:7])
+    r = run_cli(str(tmp_path), c["genes"][:7])  # too few genes (sim.cpp:458-459)
+    assert r.returncode == 0
+    assert "runtime error caught: Solution does not contain enough values" in r.stdout
+    r = run_cli(str(tmp_path), list(c["genes"]) + [1.0])  # too many (sim.cpp:835-841)
     assert r.returncode == 0
     assert "runtime error caught: chromosome size does not agree" in r.stdout
     os.remove(os.path.join(str(tmp_path), "leads.txt"))
