@@ -1,11 +1,15 @@
-// ekgsim_extern <dir> -- the evaluation command for AMS-DEMO's ExternalEvaluation.
+// ekgsim_extern [--in NAME] [--out NAME] [dir] -- the evaluation command for AMS-DEMO's
+// ExternalEvaluation.
 //
 // ExternalEvaluation (AMS-DEMO/ExternalEvaluation.h:85-152) writes <dir>/input.txt (a '#' comment
 // line, then one gene per line), runs `<command> <dir>` and reads <dir>/output.txt: the criteria
 // whitespace-separated, '#' lines skipped, and "# violation v" setting the violation; a non-zero
 // exit status makes it throw.  This program reads simulator.ini from the working directory (as
 // ekgSim does), evaluates the genes on the GPU and writes output.txt in that format.  Errors go to
-// stderr with exit status 1.
+// stderr with exit status 1.  ExternalEvaluation appends the directory (process<rank> under MPI,
+// nothing in the sequential build, GeneralOptimizationAlgorithm.cpp:262-281), so it defaults to the
+// working directory; --in / --out take the "input file name" / "output file name" of the
+// [evaluation] section when they are not input.txt / output.txt.
 #include <fstream>
 #include <iomanip>
 #include <iostream>
@@ -16,16 +20,18 @@
 #include "ekgsim.h"
 
 int main(int argc, char **argv) {
-    if (argc < 2) {
-        std::cerr << "usage: ekgsim_extern <dir>\n";
-        return 2;
+    std::string dir = ".", in_name = "input.txt", out_name = "output.txt";
+    for (int i = 1; i < argc; ++i) {
+        const std::string a = argv[i];
+        if (a == "--in" && i + 1 < argc) in_name = argv[++i];
+        else if (a == "--out" && i + 1 < argc) out_name = argv[++i];
+        else if (!a.empty()) dir = a;
     }
-    const std::string dir = argv[1];
     std::vector<double> genes;
     {
-        std::ifstream in((dir + "/input.txt").c_str());
+        std::ifstream in((dir + "/" + in_name).c_str());
         if (!in) {
-            std::cerr << "cannot read " << dir << "/input.txt\n";
+            std::cerr << "cannot read " << dir << "/" << in_name << "\n";
             return 1;
         }
         std::string line;
@@ -50,7 +56,7 @@ int main(int argc, char **argv) {
         std::cerr << "ekgsim_extern: " << ekg_last_error() << "\n";
         return 1;
     }
-    std::ofstream out((dir + "/output.txt").c_str());
+    std::ofstream out((dir + "/" + out_name).c_str());
     out << "# file generated by ekgsim_extern\n";
     out << std::setprecision(17);
     for (int i = 0; i < nc; ++i) out << crit[i] << "\n";
