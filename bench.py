@@ -191,6 +191,58 @@ def cpu_farm(spec, steps, genes, sample_steps: int, threads: int):
     return sims_per_s, dt, sample
 
 
+def served_run(seconds: float = 4.0, rate: float = 500.0, seed: int = 3000):
+    """Served configuration: a Poisson stream of evaluation requests over four resident hearts
+    (48^3, 96^3, 144^3, 192^3 scaled ellipsoids, 3 layers, 12 leads, 600 steps); continuous batching
+    in the engine's request loop.  Returns latency percentiles (submit -> result), throughput and
+    the mean number of requests per device pass."""
+    from ekgsim_gb300 import engine as E
+    from ekgsim_gb300 import synth
+    cfg = synth.config(3)
+    eng = E.Engine(0)
+    hearts, specs = [], []
+    for spec in cfg["hearts"]:
+        grid = synth.ellipsoid_heart(spec)
+        tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+        leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+        h = E.Heart.create(eng, grid, tm, leads, "3D4", 0.0, float(cfg["steps"]), 1.0)
+        h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8],
+                   [t for t in synth.analytic_target(spec.n_leads, cfg["steps"], spec.seed + 999)], mid_position=0.6)
+        hearts.append(h)
+        specs.append(spec)
+    srv = E.Server(eng, max_batch=256, max_wait_us=2000)
+    ids = [srv.add_heart(h) for h in hearts]
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = int(seconds * rate)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
+    which = rng.integers(0, len(hearts), size=n)
+    genes = [synth.genes_for(specs[w], i, 3) for i, w in enumerate(which)]
+    # warm each heart's batched path once
+    for i, hid in enumerate(ids):
+        srv.poll(srv.submit(hid, synth.genes_for(specs[i], 10_000 + i, 3)), hid, wait_ms=120000)
+    submitted = []
+    t0 = time.perf_counter()
+    for i in range(n):
+        now = time.perf_counter() - t0
+        if arrivals[i] > now:
+            time.sleep(arrivals[i] - now)
+        submitted.append((srv.submit(ids[which[i]], genes[i]), ids[which[i]]))
+    lat, batch = [], []
+    for rid, hid in submitted:
+        out = srv.poll(rid, hid, wait_ms=120000)
+        lat.append(out[3]["total_ms"])
+        batch.append(out[3]["batch"])
+    t1 = time.perf_counter()
+    srv.close()
+    for h in hearts:
+        h.close()
+    eng.close()
+    lat = np.array(lat)
+    return {"requests": n, "rate_req_s": rate, "throughput_req_s": n / (t1 - t0),
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_batch": float(np.mean(batch)), "hearts": [s.n for s in specs]}
+
+
 def host_cores() -> int:
     try:
         return len(os.sched_getaffinity(0))
@@ -336,6 +388,8 @@ def run_ours(args):
             ref = O.run(layer, at_ref, lk[i], moved[i], "3D4", 0.0, float(steps), 1.0)
             rels.append(float(np.linalg.norm(ecg[i] - ref) / np.linalg.norm(ref)))
         line["parity"] = {"ecg_rel_l2_max": max(rels), "checked_sims": len(rels), "at_mismatch": mism}
+    if d.rank == 0 and not args.no_served:
+        line["served"] = served_run()
     if d.rank == 0 and d.world == 1 and not args.no_cpu:
         v, dt, sample = cpu_farm(spec, steps, genes, args.cpu_sample_steps, host_cores())
         line["cpu_baseline"] = {"value": v, "unit": "sims/s", "cores": host_cores(), "kind": "port",
@@ -360,6 +414,7 @@ def main():
     ap.add_argument("--ref-sample-steps", type=int, default=6)
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":

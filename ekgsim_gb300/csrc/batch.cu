@@ -128,12 +128,55 @@ __global__ void k_static_combine(int steps, int nleads, int nl, int J, int Jb, i
 // segment per part; a warp's 32 simulations x nmove rows are contiguous in the tile.
 // g at p = v + d uses |m - d|^2 = |m|^2 - 2 m.d + |d|^2 with m = r - v, and g.d = (m.d - |d|^2) f,
 // f = |m - d|^-3: one rsqrt and a handful of FMAs per neighbour.
-template <int N>
+// w(v) for one lead relative position r (both relative to the same centre), general neighbourhood.
+__device__ __forceinline__ float voxel_w_general(float4 pos, float4 out, float rz, float ry, float rx, int nnb,
+                                                 const float *s_d) {
+    const float mz = rz - pos.x, my = ry - pos.y, mx = rx - pos.z;
+    const uint32_t mi = __float_as_uint(pos.w);
+    const float s0 = fmaf(mz, mz, fmaf(my, my, mx * mx));
+    float w = 0.f;
+    for (int n = 0; n < nnb; ++n) {
+        if (!(mi & (1u << n))) continue;
+        const float4 d = reinterpret_cast<const float4 *>(s_d)[n];
+        const float md = fmaf(mz, d.x, fmaf(my, d.y, mx * d.z));
+        const float rs = rsqrtf(fmaf(-2.f, md, s0 + d.w));
+        w = fmaf(rs * rs * rs, md - d.w, w);
+    }
+    if (out.w != 0.f) {
+        const float rs = rsqrtf(s0);
+        w = fmaf(-(rs * rs * rs), fmaf(mz, out.x, fmaf(my, out.y, mx * out.z)), w);
+    }
+    return w;
+}
+
+// Same for the 8 body diagonals ("3D4", creation order (-1,-1,-1) ... (1,1,1)): with p = my + mx and
+// q = my - mx the eight m.d are -mz-p, -mz-q, -mz+q, -mz+p, mz-p, mz-q, mz+q, mz+p; |d|^2 = 3.
+// Missing neighbours are masked by multiplying their term by 0 (branch-free).
+__device__ __forceinline__ float voxel_w_diag(float4 pos, float4 out, float rz, float ry, float rx) {
+    const float mz = rz - pos.x, my = ry - pos.y, mx = rx - pos.z;
+    const uint32_t mi = __float_as_uint(pos.w);
+    const float s0 = fmaf(mz, mz, fmaf(my, my, mx * mx));
+    const float s3 = s0 + 3.f;
+    const float p = my + mx, q = my - mx;
+    const float md[8] = {-mz - p, -mz - q, -mz + q, -mz + p, mz - p, mz - q, mz + q, mz + p};
+    float w = 0.f;
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+        const float rs = rsqrtf(fmaf(-2.f, md[n], s3));
+        const float t = (rs * rs * rs) * (md[n] - 3.f);
+        w += ((mi >> n) & 1u) ? t : 0.f;
+    }
+    const float rs0 = rsqrtf(s0);
+    w = fmaf(-(rs0 * rs0 * rs0) * out.w, fmaf(mz, out.x, fmaf(my, out.y, mx * out.z)), w);
+    return w;
+}
+
+template <int N, bool DIAG>
 __global__ void __launch_bounds__(128) k_batch_lead_field(
-    int64_t apad, int nkt, const int64_t *__restrict__ a_vox_begin, const int32_t *__restrict__ vox_zyx,
-    const uint32_t *__restrict__ nb_in, const uint32_t *__restrict__ nb_out, int nnb, const int8_t *__restrict__ difs,
-    const double *__restrict__ at, const int32_t *__restrict__ a_layer, const double *__restrict__ layer_k, int nl,
-    const double *__restrict__ leads, int nleads, int nmove, int n_sims, uint8_t *__restrict__ Bt) {
+    int64_t apad, int nkt, const int64_t *__restrict__ a_vox_begin, const float4 *__restrict__ vox_pos,
+    const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs, const double *__restrict__ at,
+    const int32_t *__restrict__ a_layer, const double *__restrict__ layer_k, int nl, const double *__restrict__ leads,
+    double cz, double cy, double cx, int nleads, int nmove, int n_sims, uint8_t *__restrict__ Bt) {
     __shared__ float s_d[26 * 4];
     if (threadIdx.x < nnb) {
         const float dz = difs[3 * threadIdx.x], dy = difs[3 * threadIdx.x + 1], dx = difs[3 * threadIdx.x + 2];
@@ -147,54 +190,26 @@ __global__ void __launch_bounds__(128) k_batch_lead_field(
     const int s = blockIdx.y * blockDim.x + threadIdx.x;
     if (s >= n_sims) return;
     const int kt = (int)(a0 / BKT), kc = (int)((a0 % BKT) / 8);
-    float e[8];
-    int64_t vb[9];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        const double aa = at[a0 + j];
-        e[j] = isinf(aa) ? 0.f : expf((float)(layer_k[((size_t)s * nl + a_layer[a0 + j]) * 9 + 5] * aa));
-        vb[j] = a_vox_begin[a0 + j];
-    }
-    vb[8] = a_vox_begin[a0 + 8];
+    const int64_t vstart = a_vox_begin[a0], vend = a_vox_begin[a0 + 8];
     for (int l = 0; l < nmove; ++l) {
+        // lead position relative to the same centre as vox_pos (difference taken in FP64)
         const double *r = leads + ((size_t)s * nleads + l) * 3;
-        const float rz = (float)r[0], ry = (float)r[1], rx = (float)r[2];
-        const float rzl = (float)(r[0] - (double)rz), ryl = (float)(r[1] - (double)ry), rxl = (float)(r[2] - (double)rx);
+        const float rz = (float)(r[0] - cz), ry = (float)(r[1] - cy), rx = (float)(r[2] - cx);
         float wv[8];
+        int64_t v = vstart;
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
+            const int64_t ve = a_vox_begin[a0 + j + 1];
             float acc = 0.f;
-            for (int64_t v = vb[j]; v < vb[j + 1]; ++v) {
-                const int32_t p = vox_zyx[v];
-                const uint32_t mi = nb_in[v], mo = nb_out[v];
-                // m = r - x, x the bordered voxel position (simlib/simulator.cpp:458-463, 531-532)
-                const float mz = (rz - (float)((p >> 20) + 1)) + rzl;
-                const float my = (ry - (float)(((p >> 10) & 1023) + 1)) + ryl;
-                const float mx = (rx - (float)((p & 1023) + 1)) + rxl;
-                const float s0 = fmaf(mz, mz, fmaf(my, my, mx * mx));
-                float w = 0.f, oz = 0.f, oy = 0.f, ox = 0.f;
-                for (int n = 0; n < nnb; ++n) {
-                    const float4 d = reinterpret_cast<const float4 *>(s_d)[n];
-                    if (mi & (1u << n)) {
-                        const float md = fmaf(mz, d.x, fmaf(my, d.y, mx * d.z));
-                        const float sd = fmaf(-2.f, md, s0 + d.w);
-                        const float rs = rsqrtf(sd);
-                        w = fmaf(rs * rs * rs, md - d.w, w);
-                    }
-                    if (mo & (1u << n)) {
-                        oz += d.x;
-                        oy += d.y;
-                        ox += d.z;
-                    }
-                }
-                if (mo) {
-                    const float rs = rsqrtf(s0);
-                    w = fmaf(-(rs * rs * rs), fmaf(mz, oz, fmaf(my, oy, mx * ox)), w);
-                }
-                acc += w;
+            for (; v < ve; ++v) {
+                const float4 pos = vox_pos[v], out = vox_out[v];
+                acc += DIAG ? voxel_w_diag(pos, out, rz, ry, rx) : voxel_w_general(pos, out, rz, ry, rx, nnb, s_d);
             }
-            wv[j] = acc * e[j];
+            const double aa = at[a0 + j];
+            const float e = isinf(aa) ? 0.f : expf((float)(layer_k[((size_t)s * nl + a_layer[a0 + j]) * 9 + 5] * aa));
+            wv[j] = acc * e;
         }
+        (void)vend;
         uint4 hv, lv;
         split2(wv[0], wv[1], hv.x, lv.x);
         split2(wv[2], wv[3], hv.y, lv.y);
@@ -481,14 +496,20 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, c
     const int threads = n_sims < 128 ? ((n_sims + 31) / 32) * 32 : 128;
     dim3 grid((unsigned)(h.apad / 8), (unsigned)((n_sims + threads - 1) / threads));
     const int nkt = (int)(h.apad / BKT);
-    if (two_bases)
-        k_batch_lead_field<128><<<grid, threads, 0, s>>>(h.apad, nkt, h.a_vox_begin.p, h.vox_zyx.p, h.vox_nb.p,
-                                                         h.vox_nbo.p, h.nnb, h.difs.p, h.at.p, h.a_layer.p, layer_k,
-                                                         h.nlayers, leads, h.nleads, nmove, n_sims, Bt);
-    else
-        k_batch_lead_field<256><<<grid, threads, 0, s>>>(h.apad, nkt, h.a_vox_begin.p, h.vox_zyx.p, h.vox_nb.p,
-                                                         h.vox_nbo.p, h.nnb, h.difs.p, h.at.p, h.a_layer.p, layer_k,
-                                                         h.nlayers, leads, h.nleads, nmove, n_sims, Bt);
+    const bool diag = h.nhood == EKG_NHOOD_3D4;
+#define EKG_LF(NN, DG)                                                                                           \
+    k_batch_lead_field<NN, DG><<<grid, threads, 0, s>>>(h.apad, nkt, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, \
+                                                        h.nnb, h.difs.p, h.at.p, h.a_layer.p, layer_k, h.nlayers,  \
+                                                        leads, h.centre[0], h.centre[1], h.centre[2], h.nleads,    \
+                                                        nmove, n_sims, Bt)
+    if (two_bases) {
+        if (diag) EKG_LF(128, true);
+        else EKG_LF(128, false);
+    } else {
+        if (diag) EKG_LF(256, true);
+        else EKG_LF(256, false);
+    }
+#undef EKG_LF
     EKG_CUDA(cudaGetLastError());
 }
 

@@ -99,6 +99,9 @@ struct HeartDev {
     DBuf<int32_t> vox_zyx;  // [nvox] packed z<<20 | y<<10 | x  (each < 1024)
     DBuf<uint32_t> vox_nb;  // [nvox] bits 0..25: in-neighbour mask, (unused high bits)
     DBuf<uint32_t> vox_nbo; // [nvox] out-neighbour mask
+    DBuf<float4> vox_pos;   // [nvox] bordered position relative to `centre` (z,y,x) + in-mask bits in .w
+    DBuf<float4> vox_out;   // [nvox] sum of the out-neighbour offsets (z,y,x), .w = 1 if any
+    double centre[3] = {0, 0, 0};
     // K chunks
     DBuf<int32_t> chunk_a0, chunk_a1, chunk_layer;  // [nchunks]
     // neighbourhood offsets (z,y,x) as int8 triples

@@ -79,6 +79,7 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     D.ny = d->ny;
     D.nx = d->nx;
     D.nleads = d->n_leads;
+    D.nhood = d->nhood;
     D.nnb = neighbourhood(d->nhood, D.nb_dif);
     EKG_CHECK(D.nnb > 0, EKG_ERR_BAD_INPUT, "unknown neighbourhood (only know of these: 2D4, 3D4, 2D8, 3D8 (cube))");
 
@@ -228,6 +229,10 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     std::vector<int32_t> c0, c1, cl;
     std::vector<int32_t> vzyx(nv);
     std::vector<uint32_t> vin(nv), vout(nv);
+    std::vector<float4> vpos_v(nv), vosum(nv);
+    D.centre[0] = 0.5 * d->nz;
+    D.centre[1] = 0.5 * d->ny;
+    D.centre[2] = 0.5 * d->nx;
     int64_t vpos = 0;
     {
         int64_t g = 0;
@@ -268,6 +273,20 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
                         }
                         vin[vpos] = mi;
                         vout[vpos] = mo;
+                        float oz = 0, oy = 0, ox = 0;
+                        for (int q = 0; q < D.nnb; ++q)
+                            if (mo & (1u << q)) {
+                                oz += D.nb_dif[3 * q];
+                                oy += D.nb_dif[3 * q + 1];
+                                ox += D.nb_dif[3 * q + 2];
+                            }
+                        uint32_t mbits = mi;
+                        float mf;
+                        std::memcpy(&mf, &mbits, 4);
+                        // bordered coordinates (+1, simlib/simulator.cpp:458-463) relative to the centre
+                        vpos_v[vpos] = make_float4((float)((z + 1) - D.centre[0]), (float)((y + 1) - D.centre[1]),
+                                                               (float)((x + 1) - D.centre[2]), mf);
+                        vosum[vpos] = make_float4(oz, oy, ox, mo ? 1.f : 0.f);
                         ++vpos;
                     }
                 } else {
@@ -294,6 +313,8 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     D.vox_zyx.alloc(nv);
     D.vox_nb.alloc(nv);
     D.vox_nbo.alloc(nv);
+    D.vox_pos.alloc(nv);
+    D.vox_out.alloc(nv);
     D.chunk_a0.alloc(c0.size());
     D.chunk_a1.alloc(c0.size());
     D.chunk_layer.alloc(c0.size());
@@ -312,6 +333,8 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     EKG_CUDA(cudaMemcpyAsync(D.vox_zyx.p, vzyx.data(), nv * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.vox_nb.p, vin.data(), nv * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.vox_nbo.p, vout.data(), nv * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.vox_pos.p, vpos_v.data(), nv * 16, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.vox_out.p, vosum.data(), nv * 16, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.chunk_a0.p, c0.data(), c0.size() * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.chunk_a1.p, c1.data(), c0.size() * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.chunk_layer.p, cl.data(), c0.size() * 4, cudaMemcpyHostToDevice, s));
