@@ -190,59 +190,93 @@ __global__ void __launch_bounds__(128) k_batch_lead_field(
     const int s = blockIdx.y * blockDim.x + threadIdx.x;
     if (s >= n_sims) return;
     const int kt = (int)(a0 / BKT), kc = (int)((a0 % BKT) / 8);
-    const int64_t vstart = a_vox_begin[a0], vend = a_vox_begin[a0 + 8];
-    for (int l = 0; l < nmove; ++l) {
-        // lead position relative to the same centre as vox_pos (difference taken in FP64)
-        const double *r = leads + ((size_t)s * nleads + l) * 3;
-        const float rz = (float)(r[0] - cz), ry = (float)(r[1] - cy), rx = (float)(r[2] - cx);
-        float wv[8];
-        int64_t v = vstart;
+    float e[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const double aa = at[a0 + j];
+        e[j] = isinf(aa) ? 0.f : expf((float)(layer_k[((size_t)s * nl + a_layer[a0 + j]) * 9 + 5] * aa));
+    }
+    // leads in pairs: the voxel data of the chunk is loaded once per pair
+    for (int l0 = 0; l0 < nmove; l0 += 2) {
+        const bool two = l0 + 1 < nmove;
+        float r0[3], r1[3] = {0.f, 0.f, 0.f};
+        {
+            // lead positions relative to the same centre as vox_pos (difference taken in FP64)
+            const double *r = leads + ((size_t)s * nleads + l0) * 3;
+            r0[0] = (float)(r[0] - cz);
+            r0[1] = (float)(r[1] - cy);
+            r0[2] = (float)(r[2] - cx);
+            if (two) {
+                r1[0] = (float)(r[3] - cz);
+                r1[1] = (float)(r[4] - cy);
+                r1[2] = (float)(r[5] - cx);
+            }
+        }
+        float w0[8], w1[8];
+        int64_t v = a_vox_begin[a0];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int64_t ve = a_vox_begin[a0 + j + 1];
-            float acc = 0.f;
+            float acc0 = 0.f, acc1 = 0.f;
             for (; v < ve; ++v) {
                 const float4 pos = vox_pos[v], out = vox_out[v];
-                acc += DIAG ? voxel_w_diag(pos, out, rz, ry, rx) : voxel_w_general(pos, out, rz, ry, rx, nnb, s_d);
+                if (DIAG) {
+                    acc0 += voxel_w_diag(pos, out, r0[0], r0[1], r0[2]);
+                    if (two) acc1 += voxel_w_diag(pos, out, r1[0], r1[1], r1[2]);
+                } else {
+                    acc0 += voxel_w_general(pos, out, r0[0], r0[1], r0[2], nnb, s_d);
+                    if (two) acc1 += voxel_w_general(pos, out, r1[0], r1[1], r1[2], nnb, s_d);
+                }
             }
-            const double aa = at[a0 + j];
-            const float e = isinf(aa) ? 0.f : expf((float)(layer_k[((size_t)s * nl + a_layer[a0 + j]) * 9 + 5] * aa));
-            wv[j] = acc * e;
+            w0[j] = acc0 * e[j];
+            w1[j] = acc1 * e[j];
         }
-        (void)vend;
-        uint4 hv, lv;
-        split2(wv[0], wv[1], hv.x, lv.x);
-        split2(wv[2], wv[3], hv.y, lv.y);
-        split2(wv[4], wv[5], hv.z, lv.z);
-        split2(wv[6], wv[7], hv.w, lv.w);
-        const int row = s * nmove + l;
-        const int nt = row / N, n = row % N;
-        const size_t tile = ((size_t)nt * nkt + kt) * 2;
-        const size_t off = (size_t)(kc * (N / 8) + n / 8) * 128 + (n % 8) * 16;
-        *reinterpret_cast<uint4 *>(Bt + tile * (N * 128) + off) = hv;
-        *reinterpret_cast<uint4 *>(Bt + (tile + 1) * (N * 128) + off) = lv;
+        for (int q = 0; q < (two ? 2 : 1); ++q) {
+            const float *wv = q ? w1 : w0;
+            uint4 hv, lv;
+            split2(wv[0], wv[1], hv.x, lv.x);
+            split2(wv[2], wv[3], hv.y, lv.y);
+            split2(wv[4], wv[5], hv.z, lv.z);
+            split2(wv[6], wv[7], hv.w, lv.w);
+            const int row = s * nmove + l0 + q;
+            const int nt = row / N, n = row % N;
+            const size_t tile = ((size_t)nt * nkt + kt) * 2;
+            const size_t off = (size_t)(kc * (N / 8) + n / 8) * 128 + (n % 8) * 16;
+            *reinterpret_cast<uint4 *>(Bt + tile * (N * 128) + off) = hv;
+            *reinterpret_cast<uint4 *>(Bt + (tile + 1) * (N * 128) + off) = lv;
+        }
     }
 }
 
 // ------------------------------------------------------------------ batch GEMM
+// Warp-specialised: warps 0-7 produce the A operand (B_b,a(t) in BF16 hi/lo) and drain the
+// accumulators; one lane of warp 8 streams the B operand with 1-D bulk copies; one lane of warp 9
+// issues the MMAs.  Rings: SA stages of A, SB stages of B (32 APs per stage); full/empty mbarrier
+// pairs per stage; two TMEM accumulator sets with full/empty barriers for the segment drains.
+// The tensor core's FP32 accumulation loses accuracy over long K (measured: relative ECG error
+// grows with the K length of one accumulation), so the K range is cut into segments of DRAIN
+// stages (512 APs): segment g accumulates in TMEM set g % 2 and is drained into FP32 registers
+// (each producer thread owns one row and half of the columns) while segment g + 1 accumulates.
+constexpr int WKT = 32;              // APs per stage
+constexpr int SA = 3, SB = 4;        // ring depths
+constexpr int DRAIN = 512 / WKT;     // stages per accumulation segment
+constexpr int WS_THREADS = 320;      // 8 producer warps + bulk-copy warp + MMA warp
+
 template <int NB, int N>
 struct BatchSmem {
-    alignas(1024) uint8_t a[2][NB][2][BM * BKT * 2];  // [stage][basis][hi/lo]
-    alignas(1024) uint8_t b[2][2][N * BKT * 2];       // [stage][hi/lo]
-    float2 at[2][BKT];
-    alignas(8) uint64_t full[2];
-    alignas(8) uint64_t done[2];
+    alignas(1024) uint8_t a[SA][NB][2][BM * WKT * 2];  // [stage][basis][hi/lo]
+    alignas(1024) uint8_t b[SB][2][N * WKT * 2];       // [stage][hi/lo]
+    alignas(8) uint64_t a_full[SA], a_empty[SA], b_full[SB], b_empty[SB], acc_full[2], acc_empty[2];
     uint32_t tmem_base;
 };
 
-// grid (t tiles, N tiles, K chunks).  Chunk c covers K tiles [ck0[c], ck1[c]) inside layer cl[c].
-// The tensor core's FP32 accumulation loses accuracy over long K (measured: relative ECG error
-// grows with the K length of one accumulation), so the K range is cut into segments of
-// DRAIN tiles (512 APs): segment g accumulates in TMEM set g % 2 while the threads drain set
-// (g - 1) % 2 into FP32 registers (each thread owns one row and half of the columns).
-constexpr int DRAIN = 8;
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// grid (t tiles, N tiles, K chunks).  Chunk c covers 64-AP tiles [ck0[c], ck1[c]) inside layer cl[c].
 template <int NB, int N>
-__global__ void __launch_bounds__(BTHREADS, 1) k_batch_umma(
+__global__ void __launch_bounds__(WS_THREADS, 1) k_batch_umma(
     int steps, int nl, int nkt, int rows, int nmove, int n_sims, const float2 *__restrict__ t_hilo,
     const float2 *__restrict__ at_hilo, const int32_t *__restrict__ ck0, const int32_t *__restrict__ ck1,
     const int32_t *__restrict__ cl, const float4 *__restrict__ hconst, const double *__restrict__ k3,
@@ -256,20 +290,30 @@ __global__ void __launch_bounds__(BTHREADS, 1) k_batch_umma(
     constexpr uint32_t IDESC = idesc_bf16(BM, N);
     constexpr uint32_t A_LBO = (BM / 8) * 128, A_SBO = 128;
     constexpr uint32_t B_LBO = (N / 8) * 128, B_SBO = 128;
-    constexpr uint32_t BPART = N * BKT * 2;
-    constexpr int HALF = N / 2;             // columns per thread per basis
+    constexpr uint32_t BTILE = N * BKT * 2;  // one part of a 64-AP tile in global memory
+    constexpr uint32_t BSTAGE = N * WKT * 2; // one part of a 32-AP stage
+    constexpr int HALF = N / 2;
     constexpr int NACC = NB * HALF;         // 128
+    constexpr int NPROD = 256;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int t0 = blockIdx.x * BM, nt = blockIdx.y, c = blockIdx.z;
-    const int kt0 = ck0[c], kt1 = ck1[c], L = cl[c];
-    const float4 hc = hconst[L];  // k1*log2e, k4*log2e, 1-k3, k3 (the last two unused with two bases)
+    const int st0 = 2 * ck0[c], nk = 2 * (ck1[c] - ck0[c]), L = cl[c];
+    const int nseg = (nk + DRAIN - 1) / DRAIN;
 
     if (tid == 0) {
-        mbar_init(&S.full[0], 1);
-        mbar_init(&S.full[1], 1);
-        mbar_init(&S.done[0], 1);
-        mbar_init(&S.done[1], 1);
+        for (int i = 0; i < SA; ++i) {
+            mbar_init(&S.a_full[i], NPROD);
+            mbar_init(&S.a_empty[i], 1);
+        }
+        for (int i = 0; i < SB; ++i) {
+            mbar_init(&S.b_full[i], 1);
+            mbar_init(&S.b_empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&S.acc_full[i], 1);
+            mbar_init(&S.acc_empty[i], NPROD);
+        }
         fence_barrier_init();
     }
     if (warp == 0) {
@@ -280,150 +324,167 @@ __global__ void __launch_bounds__(BTHREADS, 1) k_batch_umma(
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = S.tmem_base;
-
-    const int q = warp & 3, ch = warp >> 2;  // TMEM lane quadrant and column half of this warp
-    const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
-    float acc[NACC];
-#pragma unroll
-    for (int i = 0; i < NACC; ++i) acc[i] = 0.f;
-    auto drain = [&](int g) {
-        const uint32_t base = lane_addr + (uint32_t)((g & 1) * SET);
-#pragma unroll
-        for (int bsi = 0; bsi < NB; ++bsi)
-#pragma unroll
-            for (int cb = 0; cb < HALF; cb += 16) {
-                float v[16];
-                tmem_ld16(base + (uint32_t)(bsi * N + ch * HALF + cb), v);
-#pragma unroll
-                for (int jj = 0; jj < 16; ++jj) acc[bsi * HALF + cb + jj] += v[jj];
-            }
-    };
-
-    const int row = tid & (BM - 1), half = tid >> 7;
-    const float2 th = t_hilo[min(t0 + row, steps - 1)];
-    const int nk = kt1 - kt0;
-    const int nseg = (nk + DRAIN - 1) / DRAIN;
-    int drained = 0;
     bool ok = true;
-    for (int i = 0; i < nk; ++i) {
-        const int b = i & 1;
-        const int kt = kt0 + i;
-        if (i >= 2) {
-            if (!mbar_wait(&S.done[b], (uint32_t)(((i >> 1) + 1) & 1))) ok = false;
-            if (__syncthreads_or(!ok)) {
+
+    if (warp < 8) {
+        // ---------------- producers and drains
+        const float4 hc = hconst[L];
+        const int q = warp & 3, ch = warp >> 2;  // TMEM lane quadrant, column half
+        const int row = tid & (BM - 1), half = tid >> 7;
+        const float2 th = t_hilo[min(t0 + row, steps - 1)];
+        const uint32_t lane_addr = tmem + ((uint32_t)(32 * q) << 16);
+        float acc[NACC];
+#pragma unroll
+        for (int i = 0; i < NACC; ++i) acc[i] = 0.f;
+        int drained = 0;
+        auto drain = [&](int g) {
+            if (!mbar_wait(&S.acc_full[g & 1], (uint32_t)((g >> 1) & 1))) {
+                ok = false;
+                return;
+            }
+            tc_fence_after();
+            const uint32_t base = lane_addr + (uint32_t)((g & 1) * SET);
+#pragma unroll
+            for (int bsi = 0; bsi < NB; ++bsi)
+#pragma unroll
+                for (int cb = 0; cb < HALF; cb += 16) {
+                    float v[16];
+                    tmem_ld16(base + (uint32_t)(bsi * N + ch * HALF + cb), v);
+#pragma unroll
+                    for (int jj = 0; jj < 16; ++jj) acc[bsi * HALF + cb + jj] += v[jj];
+                }
+            tc_fence_before();
+            mbar_arrive(&S.acc_empty[g & 1]);
+        };
+        for (int i = 0; i < nk && ok; ++i) {
+            const int sa = i % SA, u = i / SA;
+            // drain segment g once production is SA stages into segment g + 1
+            if (i >= SA && (i - SA) % DRAIN == 0 && (i - SA) >= DRAIN) {
+                drain(drained);
+                ++drained;
+                if (!ok) break;
+            }
+            if (u > 0 && !mbar_wait(&S.a_empty[sa], (uint32_t)((u - 1) & 1))) {
                 ok = false;
                 break;
             }
-            if ((i - 1) % DRAIN == 0) {  // tile i-2 closed segment (i-2)/DRAIN
-                tc_fence_after();
-                drain((i - 2) / DRAIN);
-                drained = (i - 2) / DRAIN + 1;
-                tc_fence_before();
-            }
-        }
-        if (tid == 0) {
-            const uint8_t *src = Bt + ((size_t)nt * nkt + kt) * 2 * BPART;
-            mbar_expect_tx(&S.full[b], 2 * BPART);
-            bulk_g2s(S.b[b][0], src, BPART, &S.full[b]);
-            bulk_g2s(S.b[b][1], src + BPART, BPART, &S.full[b]);
-        }
-        if (tid < BKT) S.at[b][tid] = at_hilo[(size_t)kt * BKT + tid];
-        __syncthreads();
+            const float2 *atp = at_hilo + (size_t)(st0 + i) * WKT + half * 16;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int kc8 = half * 4 + j;
-            float v1[8], v2[8];
+            for (int j = 0; j < 2; ++j) {
+                const int kc8 = half * 2 + j;
+                float v1[8], v2[8];
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const float2 at = S.at[b][kc8 * 8 + e];
-                const float tau = (th.x - at.x) + (th.y - at.y);
-                const float e1 = ex2a(-hc.x * tau);
-                const float sg = rcpa(1.0f + e1);
-                const float e4 = ex2a(-hc.y * tau);
-                if (NB == 1) {
-                    const float h = sg * fmaf(hc.z, e4, hc.w);
-                    v1[e] = sg == 0.f ? 0.f : h;
-                } else {
-                    const float h = sg * e4;
-                    v1[e] = sg == 0.f ? 0.f : h;
-                    v2[e] = sg;
-                }
-            }
-            const uint32_t off = (uint32_t)((kc8 * (BM / 8) + row / 8) * 128 + (row % 8) * 16);
-            uint4 hv, lv;
-            split2(v1[0], v1[1], hv.x, lv.x);
-            split2(v1[2], v1[3], hv.y, lv.y);
-            split2(v1[4], v1[5], hv.z, lv.z);
-            split2(v1[6], v1[7], hv.w, lv.w);
-            *reinterpret_cast<uint4 *>(S.a[b][0][0] + off) = hv;
-            *reinterpret_cast<uint4 *>(S.a[b][0][1] + off) = lv;
-            if (NB == 2) {
-                split2(v2[0], v2[1], hv.x, lv.x);
-                split2(v2[2], v2[3], hv.y, lv.y);
-                split2(v2[4], v2[5], hv.z, lv.z);
-                split2(v2[6], v2[7], hv.w, lv.w);
-                *reinterpret_cast<uint4 *>(S.a[b][NB - 1][0] + off) = hv;
-                *reinterpret_cast<uint4 *>(S.a[b][NB - 1][1] + off) = lv;
-            }
-        }
-        fence_proxy_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            if (!mbar_wait(&S.full[b], (uint32_t)((i >> 1) & 1))) {
-                atomicOr(err, KERR_MBAR_TIMEOUT);
-            } else {
-                tc_fence_after();
-                const uint32_t set = (uint32_t)(((i / DRAIN) & 1) * SET);
-                const bool first = (i % DRAIN) == 0;
-                const uint32_t bh = smem_u32(S.b[b][0]), bl = smem_u32(S.b[b][1]);
-#pragma unroll
-                for (int j = 0; j < BKT / 16; ++j) {
-                    const uint64_t dbh = sdesc(bh + j * 2 * B_LBO, B_LBO, B_SBO);
-                    const uint64_t dbl = sdesc(bl + j * 2 * B_LBO, B_LBO, B_SBO);
-#pragma unroll
-                    for (int qb = 0; qb < NB; ++qb) {
-                        const uint32_t ah = smem_u32(S.a[b][qb][0]), al = smem_u32(S.a[b][qb][1]);
-                        const uint64_t dah = sdesc(ah + j * 2 * A_LBO, A_LBO, A_SBO);
-                        const uint64_t dal = sdesc(al + j * 2 * A_LBO, A_LBO, A_SBO);
-                        const uint32_t d = tmem + set + (uint32_t)(qb * N);
-                        mma_bf16(d, dah, dbh, IDESC, (first && j == 0) ? 0u : 1u);
-                        mma_bf16(d, dah, dbl, IDESC, 1u);
-                        mma_bf16(d, dal, dbh, IDESC, 1u);
+                for (int e = 0; e < 8; ++e) {
+                    const float2 at = __ldg(atp + j * 8 + e);
+                    const float tau = (th.x - at.x) + (th.y - at.y);
+                    const float e1 = ex2a(-hc.x * tau);
+                    const float sg = rcpa(1.0f + e1);
+                    const float e4 = ex2a(-hc.y * tau);
+                    if (NB == 1) {
+                        const float h = sg * fmaf(hc.z, e4, hc.w);
+                        v1[e] = sg == 0.f ? 0.f : h;
+                    } else {
+                        const float h = sg * e4;
+                        v1[e] = sg == 0.f ? 0.f : h;
+                        v2[e] = sg;
                     }
                 }
-            }
-            mma_commit(&S.done[b]);
-        }
-    }
-    if (nk > 0 && ok) {
-        const int last = (nk - 1) & 1;
-        if (!mbar_wait(&S.done[last], (uint32_t)(((nk - 1) >> 1) & 1))) ok = false;
-    }
-    ok = !__syncthreads_or(!ok);
-    tc_fence_after();
-    if (ok && nk > 0 && *err == 0) {
-        for (int g = drained; g < nseg; ++g) drain(g);
-        const int t = t0 + 32 * q + lane;
-        if (t < steps) {
-#pragma unroll
-            for (int jj = 0; jj < HALF; ++jj) {
-                const int r = nt * N + ch * HALF + jj;
-                const int s = r / nmove;
-                if (s >= n_sims) continue;
-                const double f = F[((size_t)s * nl + L) * steps + t];
-                double v;
+                const uint32_t off = (uint32_t)((kc8 * (BM / 8) + row / 8) * 128 + (row % 8) * 16);
+                uint4 hv, lv;
+                split2(v1[0], v1[1], hv.x, lv.x);
+                split2(v1[2], v1[3], hv.y, lv.y);
+                split2(v1[4], v1[5], hv.z, lv.z);
+                split2(v1[6], v1[7], hv.w, lv.w);
+                *reinterpret_cast<uint4 *>(S.a[sa][0][0] + off) = hv;
+                *reinterpret_cast<uint4 *>(S.a[sa][0][1] + off) = lv;
                 if (NB == 2) {
-                    const double kk = k3[(size_t)s * nl + L];
-                    v = ((1.0 - kk) * (double)acc[jj] + kk * (double)acc[HALF + jj]) * f;
-                } else {
-                    v = (double)acc[jj] * f;
+                    split2(v2[0], v2[1], hv.x, lv.x);
+                    split2(v2[2], v2[3], hv.y, lv.y);
+                    split2(v2[4], v2[5], hv.z, lv.z);
+                    split2(v2[6], v2[7], hv.w, lv.w);
+                    *reinterpret_cast<uint4 *>(S.a[sa][NB - 1][0] + off) = hv;
+                    *reinterpret_cast<uint4 *>(S.a[sa][NB - 1][1] + off) = lv;
                 }
-                partial[((size_t)c * rows + r) * steps + t] = v;
+            }
+            fence_proxy_async_smem();
+            mbar_arrive(&S.a_full[sa]);
+        }
+        while (ok && drained < nseg) {
+            drain(drained);
+            ++drained;
+        }
+        if (ok && nk > 0) {
+            const int t = t0 + 32 * q + lane;
+            if (t < steps) {
+#pragma unroll
+                for (int jj = 0; jj < HALF; ++jj) {
+                    const int r = nt * N + ch * HALF + jj;
+                    const int s = r / nmove;
+                    if (s >= n_sims) continue;
+                    const double f = F[((size_t)s * nl + L) * steps + t];
+                    double v;
+                    if (NB == 2) {
+                        const double kk = k3[(size_t)s * nl + L];
+                        v = ((1.0 - kk) * (double)acc[jj] + kk * (double)acc[HALF + jj]) * f;
+                    } else {
+                        v = (double)acc[jj] * f;
+                    }
+                    partial[((size_t)c * rows + r) * steps + t] = v;
+                }
             }
         }
-    } else if (!ok && tid == 0) {
-        atomicOr(err, KERR_MBAR_TIMEOUT);
+    } else if (warp == 8 && lane == 0) {
+        // ---------------- B operand: 32-AP halves of the tiled 64-AP layout, one bulk copy per part
+        for (int i = 0; i < nk; ++i) {
+            const int sb = i % SB, v = i / SB;
+            if (v > 0 && !mbar_wait(&S.b_empty[sb], (uint32_t)((v - 1) & 1))) {
+                ok = false;
+                break;
+            }
+            const int st = st0 + i;
+            const uint8_t *src = Bt + ((size_t)nt * nkt + st / 2) * 2 * BTILE + (size_t)(st & 1) * BSTAGE;
+            mbar_expect_tx(&S.b_full[sb], 2 * BSTAGE);
+            bulk_g2s(S.b[sb][0], src, BSTAGE, &S.b_full[sb]);
+            bulk_g2s(S.b[sb][1], src + BTILE, BSTAGE, &S.b_full[sb]);
+        }
+    } else if (warp == 9 && lane == 0) {
+        // ---------------- MMA issue
+        for (int i = 0; i < nk; ++i) {
+            const int sa = i % SA, sb = i % SB, g = i / DRAIN;
+            if (!mbar_wait(&S.a_full[sa], (uint32_t)((i / SA) & 1)) ||
+                !mbar_wait(&S.b_full[sb], (uint32_t)((i / SB) & 1))) {
+                ok = false;
+                break;
+            }
+            const bool first = (i % DRAIN) == 0;
+            if (first && g >= 2 && !mbar_wait(&S.acc_empty[g & 1], (uint32_t)(((g - 2) >> 1) & 1))) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t set = (uint32_t)((g & 1) * SET);
+            const uint32_t bh = smem_u32(S.b[sb][0]), bl = smem_u32(S.b[sb][1]);
+#pragma unroll
+            for (int j = 0; j < WKT / 16; ++j) {
+                const uint64_t dbh = sdesc(bh + j * 2 * B_LBO, B_LBO, B_SBO);
+                const uint64_t dbl = sdesc(bl + j * 2 * B_LBO, B_LBO, B_SBO);
+#pragma unroll
+                for (int qb = 0; qb < NB; ++qb) {
+                    const uint32_t ah = smem_u32(S.a[sa][qb][0]), al = smem_u32(S.a[sa][qb][1]);
+                    const uint64_t dah = sdesc(ah + j * 2 * A_LBO, A_LBO, A_SBO);
+                    const uint64_t dal = sdesc(al + j * 2 * A_LBO, A_LBO, A_SBO);
+                    const uint32_t d = tmem + set + (uint32_t)(qb * N);
+                    mma_bf16(d, dah, dbh, IDESC, (first && j == 0) ? 0u : 1u);
+                    mma_bf16(d, dah, dbl, IDESC, 1u);
+                    mma_bf16(d, dal, dbh, IDESC, 1u);
+                }
+            }
+            mma_commit(&S.a_empty[sa]);
+            mma_commit(&S.b_empty[sb]);
+            if ((i % DRAIN) == DRAIN - 1 || i == nk - 1) mma_commit(&S.acc_full[g & 1]);
+        }
     }
+    if (!ok) atomicOr(err, KERR_MBAR_TIMEOUT);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, TCOLS);
@@ -458,9 +519,9 @@ void launch_gemm(cudaStream_t st, const BatchArgs &A) {
         attr = true;
     }
     dim3 grid((unsigned)((A.steps + BM - 1) / BM), (unsigned)A.ntiles, (unsigned)A.nchunks);
-    k_batch_umma<NB, N><<<grid, BTHREADS, smem, st>>>(A.steps, A.nl, A.nkt, A.rows, A.nmove, A.n_sims, A.t_hilo,
-                                                      A.at_hilo, A.ck0, A.ck1, A.cl, A.hconst, A.k3, A.F, A.Bt,
-                                                      A.partial, A.err);
+    k_batch_umma<NB, N><<<grid, WS_THREADS, smem, st>>>(A.steps, A.nl, A.nkt, A.rows, A.nmove, A.n_sims, A.t_hilo,
+                                                        A.at_hilo, A.ck0, A.ck1, A.cl, A.hconst, A.k3, A.F, A.Bt,
+                                                        A.partial, A.err);
     EKG_CUDA(cudaGetLastError());
 }
 
