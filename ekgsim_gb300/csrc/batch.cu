@@ -13,14 +13,24 @@
 //       exp(k5 at_a) = exp(k5 c_L) sum_{j<J} (k5 s_L)^j / j! u_a^j   (truncation bound <= 1e-12),
 //   so per heart the basis Q_{b,L,j}[l,t] = sum_{a in L} W0[l,a] u_a^j B_b,a(t) is contracted once
 //   (tensor cores, ecg path), and each simulation's static-lead ECG is a short FP64 combination.
-// * Moved leads (lead genes): one GEMM per batch on the tensor cores,
-//       Y_b[(s,l), t] = sum_{a in L} W'_s[l,a] B_b,a(t),   W'_s = W_s exp(k5_s at_a),
-//   with M = 128 steps, N = 256 (or 128) rows (simulation, moved lead), K = APs of one layer.
-//   The B operand W' is written per batch in BF16 hi+lo, already tiled in the UMMA canonical
-//   layout, and streamed into shared memory with 1-D bulk copies (TMA engine, mbarrier tx
-//   counts); the A operand B_b,a(t) is evaluated by all 256 threads in FP32 per K stage.  The
-//   epilogue forms ((1-k3) Y1 + k3 Y2) F_L(t) per row in FP64.  With a batch-uniform k3 the two
-//   bases collapse into one (N = 256, three MMAs per K step instead of six).
+// * Moved leads (lead genes): Y_b[(s,l), t] = sum_{a in L} W'_s[l,a] B_b,a(t), W'_s = W_s exp(k5_s at_a).
+//   sigma(k1 tau) is 1 to within 2^-30 for tau > T+ = 30 ln2 / k1, and B_b,a(t) is below 2^-30
+//   for tau < -T- = -30 ln2 / (k1 - k4).  Outside the band |tau| <~ T the bases are exactly
+//       B1 -> exp(-k4 tau),  B2 -> 1   (tau > T+),      B1, B2 -> 0   (tau < -T-),
+//   so for a tile of 128 steps starting at t0 the APs split (they are sorted by at within a
+//   layer) into a steady prefix (at < t0 - T+), a band, and a suffix that does not contribute:
+//       Y_b(t) = band GEMM + [B1: exp(-k4 (t - t0)) U1, B2: U0],
+//       U1 = sum_{steady a} W' exp(-k4 (t0 - at_a)),   U0 = sum_{steady a} W'.
+//   The band GEMM runs on the tensor cores with M = 128 steps, N = 256 (or 128) rows
+//   (simulation, moved lead), K = the band's APs of one layer.  The B operand W' is written per
+//   batch in BF16 hi+lo, already tiled in the UMMA canonical layout, and streamed into shared
+//   memory with 1-D bulk copies (TMA engine, mbarrier tx counts); the A operand B_b,a(t) is
+//   evaluated by 256 producer threads in FP32 per K stage.  The epilogue forms
+//   ((1-k3) Y1 + k3 Y2) F_L(t) per row in FP64.  With a batch-uniform k3 the two bases collapse
+//   into one (N = 256, three MMAs per K step instead of six).  The steady sums U0, U1 come from
+//   per-8-AP partial sums the operand kernel writes in FP32 (k_band_u), and the reduction adds
+//   F_L(t) [(1-k3) exp(-k4 (t - t0)) U1 + k3 U0] per layer.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 
@@ -43,6 +53,12 @@ __device__ __forceinline__ float ex2a(float x) {
 __device__ __forceinline__ float rcpa(float x) {
     float y;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+// 1/sqrt(x) for normal x (squared distances >= 1 here), one MUFU operation
+__device__ __forceinline__ float rsqa(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
 __device__ __forceinline__ void split2(float x0, float x1, uint32_t &hi, uint32_t &lo) {
@@ -73,10 +89,11 @@ __global__ void k_taylor_w(int64_t apad, int nleads, int J, const float *__restr
 }
 
 // Q[L][row][t] = sum over the chunks of layer L of partial[c][row][t] (chunks of a layer are
-// contiguous, [lc0[L], lc1[L])); block per (row, 32 steps), warps split chunks, fixed order.
+// contiguous, [lc0[L], lc1[L])), summed in FP64 and stored in FP32; block per (row, 32 steps),
+// warps split chunks, fixed order.
 __global__ void k_reduce_layers(int steps, int rows, int nl, const int32_t *__restrict__ lc0,
                                 const int32_t *__restrict__ lc1, const double *__restrict__ partial,
-                                double *__restrict__ Q) {
+                                float *__restrict__ Q) {
     __shared__ double red[8][33];
     const int tt = blockIdx.x * 32 + (threadIdx.x & 31);
     const int w = threadIdx.x >> 5;
@@ -90,31 +107,33 @@ __global__ void k_reduce_layers(int steps, int rows, int nl, const int32_t *__re
         if (w == 0 && tt < steps) {
             double r = 0.0;
             for (int i = 0; i < 8; ++i) r += red[i][threadIdx.x];
-            Q[((size_t)L * rows + row) * steps + tt] = r;
+            Q[((size_t)L * rows + row) * steps + tt] = (float)r;
         }
         __syncthreads();
     }
 }
 
-// Static leads: ecg[s][l][t] = sum_L F[s][L][t] sum_j coef[s][L][j] ((1-k3) Q1 + k3 Q2)[L][l*J+j][t]
+// Static leads: ecg[s][l][t] = sum_L F[s][L][t] sum_j coef[s][L][j] ((1-k3) Q1 + k3 Q2)[L][l*J+j][t],
+// the Taylor sum per layer in FP32 (the basis is stored in FP32), the sum over layers in FP64.
 __global__ void k_static_combine(int steps, int nleads, int nl, int J, int Jb, int nmove, int n_sims,
-                                 const double *__restrict__ F, const double *__restrict__ coef,
-                                 const double *__restrict__ k3, const double *__restrict__ Q1,
-                                 const double *__restrict__ Q2, double *__restrict__ ecg) {
+                                 const double *__restrict__ F, const float *__restrict__ coef,
+                                 const double *__restrict__ k3, const float *__restrict__ Q1,
+                                 const float *__restrict__ Q2, double *__restrict__ ecg) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int l = nmove + blockIdx.y, s = blockIdx.z;
     if (t >= steps || l >= nleads) return;
     const int rows = nleads * Jb;  // the basis stores Jb terms per lead
     double acc = 0.0;
     for (int L = 0; L < nl; ++L) {
-        const double kk = k3[(size_t)s * nl + L];
-        const double *c = coef + ((size_t)s * nl + L) * J;
-        double v = 0.0;
+        const float kk = (float)k3[(size_t)s * nl + L];
+        const float *c = coef + ((size_t)s * nl + L) * J;
+        const size_t q0 = ((size_t)L * rows + (size_t)l * Jb) * steps + t;
+        float v1 = 0.f, v2 = 0.f;
         for (int j = 0; j < J; ++j) {
-            const size_t q = ((size_t)L * rows + (size_t)l * Jb + j) * steps + t;
-            v += c[j] * ((1.0 - kk) * Q1[q] + kk * Q2[q]);
+            v1 = fmaf(c[j], Q1[q0 + (size_t)j * steps], v1);
+            v2 = fmaf(c[j], Q2[q0 + (size_t)j * steps], v2);
         }
-        acc += F[((size_t)s * nl + L) * steps + t] * v;
+        acc += F[((size_t)s * nl + L) * steps + t] * (double)fmaf(kk, v2 - v1, v1);
     }
     ecg[((size_t)s * nleads + l) * steps + t] = acc;
 }
@@ -123,129 +142,282 @@ __global__ void k_static_combine(int steps, int nleads, int nl, int J, int Jb, i
 // W'_s[l][a] for the moved leads l < nmove, written as BF16 hi/lo into the tiled B layout:
 // [N tile][K tile][part hi/lo][N*128 bytes], element (row n, k) of a tile at byte
 // ((k/8) * (N/8) + n/8) * 128 + (n%8) * 16 + (k%8) * 2.
-// Block = up to 128 simulations (one per thread) x one chunk of 8 consecutive APs, so the voxel
-// data of the chunk is a broadcast load for the warp and each thread writes one 16-byte row
-// segment per part; a warp's 32 simulations x nmove rows are contiguous in the tile.
-// g at p = v + d uses |m - d|^2 = |m|^2 - 2 m.d + |d|^2 with m = r - v, and g.d = (m.d - |d|^2) f,
-// f = |m - d|^-3: one rsqrt and a handful of FMAs per neighbour.
-// w(v) for one lead relative position r (both relative to the same centre), general neighbourhood.
-__device__ __forceinline__ float voxel_w_general(float4 pos, float4 out, float rz, float ry, float rx, int nnb,
-                                                 const float *s_d) {
-    const float mz = rz - pos.x, my = ry - pos.y, mx = rx - pos.z;
+// Block = up to 128 simulations (one per thread) x one segment of 8-AP chunks; per chunk the voxel
+// data is a broadcast load for the warp (and every branch on it is warp-uniform) and each thread
+// writes one 16-byte row segment per part; a warp's 32 simulations x nmove rows are contiguous
+// in the tile.
+// The field at p = v + d uses |m - d|^2 = |m|^2 - 2 m.d + |d|^2 with m = r - v, and
+// g.d = (m.d - |d|^2) |m - d|^-3: one rsqrt and a few FMAs per neighbour.
+//
+// Interior voxels (every neighbour present, out-neighbour offsets summing to zero):
+// w(v) = sum_n d_n . grad phi(v + d_n)
+// with phi(v) = 1/|r - v| harmonic, so by Taylor expansion in d_n
+//     w = sum_{k odd} (1/k!) sum_n (d_n . grad)^(k+1) phi(v),
+// whose k = 1 term is (sum_n d_x^2) lap phi = 0.  For a neighbour set with the symmetry of the cube
+// the k = 3 and k = 5 terms reduce, with lap phi = 0, to
+//     f4 sum_i d_i^4 phi + f6 sum_i d_i^6 phi,
+//     sum_i d_i^4 phi = rho^5 (105 T4 - 63),   sum_i d_i^6 phi = rho^7 (4050 - 14175 T4 + 10395 T6),
+// rho = 1/|m|, T4 = sum_i (m_i rho)^4, T6 = sum_i (m_i rho)^6 (f4, f6 from the set's 4th and 6th
+// moments, computed on the host; the 8 body diagonals give 168 - 280 T4 and 4320 - 15120 T4 +
+// 11088 T6).  The next term is smaller by about 20/|m|^2; the form is used for |m| >= 20, where it
+// is closer to the exact sum than the FP32 evaluation of the eight cancelling neighbour terms.
+struct InteriorField {
+    float a0 = 0, a1 = 0, b0 = 0, b1 = 0, b2 = 0;  // rho^5 (a1 T4 + a0) + rho^7 (b2 T6 + b1 T4 + b0)
+    uint32_t mask = 0;                              // full neighbour mask (0: never)
+};
+constexpr float INTERIOR_S_MIN = 400.f;  // |m|^2
+
+// every neighbour present and the out-neighbour offsets summing to zero (the out term vanishes)
+__device__ __forceinline__ bool interior_ok(const InteriorField &ic, uint32_t mi, float4 out, float s0) {
+    const uint32_t am = __activemask();
+    return ic.mask != 0u && mi == ic.mask && out.x == 0.f && out.y == 0.f && out.z == 0.f &&
+           __all_sync(am, s0 >= INTERIOR_S_MIN);
+}
+__device__ __forceinline__ float interior_w(const InteriorField &ic, float mz, float my, float mx, float s0) {
+    const float rho = rsqa(s0);
+    const float uz = mz * rho, uy = my * rho, ux = mx * rho;
+    const float z2 = uz * uz, y2 = uy * uy, x2 = ux * ux;
+    const float z4 = z2 * z2, y4 = y2 * y2, x4 = x2 * x2;
+    const float T4 = z4 + y4 + x4;
+    const float T6 = fmaf(z4, z2, fmaf(y4, y2, x4 * x2));
+    const float r2 = rho * rho, r5 = r2 * r2 * rho, r7 = r5 * r2;
+    return fmaf(r5, fmaf(ic.a1, T4, ic.a0), r7 * fmaf(ic.b2, T6, fmaf(ic.b1, T4, ic.b0)));
+}
+
+// w(v) for one lead position r relative to the same centre as the voxel positions, general
+// neighbourhood.
+__device__ __forceinline__ float voxel_w_general(float4 pos, float4 out, float4 r, int nnb, const float *s_d,
+                                                 const InteriorField &ic) {
+    const float mz = r.x - pos.x, my = r.y - pos.y, mx = r.z - pos.z;
     const uint32_t mi = __float_as_uint(pos.w);
     const float s0 = fmaf(mz, mz, fmaf(my, my, mx * mx));
+    if (interior_ok(ic, mi, out, s0)) return interior_w(ic, mz, my, mx, s0);
     float w = 0.f;
     for (int n = 0; n < nnb; ++n) {
         if (!(mi & (1u << n))) continue;
         const float4 d = reinterpret_cast<const float4 *>(s_d)[n];
-        const float md = fmaf(mz, d.x, fmaf(my, d.y, mx * d.z));
-        const float rs = rsqrtf(fmaf(-2.f, md, s0 + d.w));
-        w = fmaf(rs * rs * rs, md - d.w, w);
+        const float y = fmaf(mz, d.x, fmaf(my, d.y, mx * d.z)) - d.w;  // m.d - |d|^2
+        const float rs = rsqa(fmaf(-2.f, y, s0 - d.w));                // |m - d|^2 = |m|^2 - |d|^2 - 2 y
+        w = fmaf(rs * rs * rs, y, w);
     }
     if (out.w != 0.f) {
-        const float rs = rsqrtf(s0);
+        const float rs = rsqa(s0);
         w = fmaf(-(rs * rs * rs), fmaf(mz, out.x, fmaf(my, out.y, mx * out.z)), w);
     }
     return w;
 }
 
-// Same for the 8 body diagonals ("3D4", creation order (-1,-1,-1) ... (1,1,1)): with p = my + mx and
-// q = my - mx the eight m.d are -mz-p, -mz-q, -mz+q, -mz+p, mz-p, mz-q, mz+q, mz+p; |d|^2 = 3.
-// Missing neighbours are masked by multiplying their term by 0 (branch-free).
-__device__ __forceinline__ float voxel_w_diag(float4 pos, float4 out, float rz, float ry, float rx) {
-    const float mz = rz - pos.x, my = ry - pos.y, mx = rx - pos.z;
+// Same for the 8 body diagonals ("3D4", creation order (-1,-1,-1) ... (1,1,1), |d|^2 = 3): with
+// p = my + mx, q = my - mx, zm = -mz - 3, zp = mz - 3 the eight y = m.d - 3 are
+// zm-p, zm-q, zm+q, zm+p, zp-p, zp-q, zp+q, zp+p, and |m - d|^2 = (|m|^2 - 3) - 2 y.  Voxels
+// missing a neighbour are masked, the out-neighbour term is skipped where there is none (all
+// tests on the voxel are uniform over the warp).
+__device__ __forceinline__ float voxel_w_diag(float4 pos, float4 out, float4 r, const InteriorField &ic) {
+    const float mz = r.x - pos.x, my = r.y - pos.y, mx = r.z - pos.z;
     const uint32_t mi = __float_as_uint(pos.w);
     const float s0 = fmaf(mz, mz, fmaf(my, my, mx * mx));
-    const float s3 = s0 + 3.f;
+    if (interior_ok(ic, mi, out, s0)) return interior_w(ic, mz, my, mx, s0);
+    const float b = s0 - 3.f;
     const float p = my + mx, q = my - mx;
-    const float md[8] = {-mz - p, -mz - q, -mz + q, -mz + p, mz - p, mz - q, mz + q, mz + p};
+    const float zm = -mz - 3.f, zp = mz - 3.f;
+    const float y[8] = {zm - p, zm - q, zm + q, zm + p, zp - p, zp - q, zp + q, zp + p};
     float w = 0.f;
 #pragma unroll
     for (int n = 0; n < 8; ++n) {
-        const float rs = rsqrtf(fmaf(-2.f, md[n], s3));
-        const float t = (rs * rs * rs) * (md[n] - 3.f);
-        w += ((mi >> n) & 1u) ? t : 0.f;
+        const float rs = rsqa(fmaf(-2.f, y[n], b));
+        if ((mi >> n) & 1u) w = fmaf(rs * rs * rs, y[n], w);
     }
-    const float rs0 = rsqrtf(s0);
-    w = fmaf(-(rs0 * rs0 * rs0) * out.w, fmaf(mz, out.x, fmaf(my, out.y, mx * out.z)), w);
+    if (out.w != 0.f) {
+        const float rs0 = rsqa(s0);
+        w = fmaf(-(rs0 * rs0 * rs0), fmaf(mz, out.x, fmaf(my, out.y, mx * out.z)), w);
+    }
     return w;
 }
 
-template <int N, bool DIAG>
-__global__ void __launch_bounds__(128) k_batch_lead_field(
-    int64_t apad, int nkt, const int64_t *__restrict__ a_vox_begin, const float4 *__restrict__ vox_pos,
-    const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs, const double *__restrict__ at,
-    const int32_t *__restrict__ a_layer, const double *__restrict__ layer_k, int nl, const double *__restrict__ leads,
-    double cz, double cy, double cx, int nleads, int nmove, int n_sims, uint8_t *__restrict__ Bt) {
-    __shared__ float s_d[26 * 4];
-    if (threadIdx.x < nnb) {
-        const float dz = difs[3 * threadIdx.x], dy = difs[3 * threadIdx.x + 1], dx = difs[3 * threadIdx.x + 2];
-        s_d[4 * threadIdx.x] = dz;
-        s_d[4 * threadIdx.x + 1] = dy;
-        s_d[4 * threadIdx.x + 2] = dx;
-        s_d[4 * threadIdx.x + 3] = dz * dz + dy * dy + dx * dx;
-    }
-    __syncthreads();
-    const int64_t a0 = (int64_t)blockIdx.x * 8;
-    const int s = blockIdx.y * blockDim.x + threadIdx.x;
-    if (s >= n_sims) return;
-    const int kt = (int)(a0 / BKT), kc = (int)((a0 % BKT) / 8);
-    float e[8];
-#pragma unroll
+// W'[a] = exp(k5 at_a) sum_{v in a} w(v) for the 8 APs of chunk a0 and NP lead positions, into
+// s_w[q][j][tid] (shared memory, so the AP loop stays rolled and the code small).
+template <bool DIAG, int NP>
+__device__ __forceinline__ void chunk_w(int64_t a0, const int64_t *__restrict__ a_vox_begin,
+                                        const float2 *__restrict__ at_hilo, const float4 *__restrict__ vox_pos,
+                                        const float4 *__restrict__ vox_out, float4 r0, float4 r1, int nnb,
+                                        const float *s_d, const InteriorField &ic, float k5,
+                                        float (*s_w)[8][128], int tid) {
+    int v = (int)a_vox_begin[a0];
+#pragma unroll 1
     for (int j = 0; j < 8; ++j) {
-        const double aa = at[a0 + j];
-        e[j] = isinf(aa) ? 0.f : expf((float)(layer_k[((size_t)s * nl + a_layer[a0 + j]) * 9 + 5] * aa));
-    }
-    // leads in pairs: the voxel data of the chunk is loaded once per pair
-    for (int l0 = 0; l0 < nmove; l0 += 2) {
-        const bool two = l0 + 1 < nmove;
-        float r0[3], r1[3] = {0.f, 0.f, 0.f};
-        {
-            // lead positions relative to the same centre as vox_pos (difference taken in FP64)
-            const double *r = leads + ((size_t)s * nleads + l0) * 3;
-            r0[0] = (float)(r[0] - cz);
-            r0[1] = (float)(r[1] - cy);
-            r0[2] = (float)(r[2] - cx);
-            if (two) {
-                r1[0] = (float)(r[3] - cz);
-                r1[1] = (float)(r[4] - cy);
-                r1[2] = (float)(r[5] - cx);
-            }
-        }
-        float w0[8], w1[8];
-        int64_t v = a_vox_begin[a0];
+        const int ve = (int)a_vox_begin[a0 + j + 1];
+        float acc[NP];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int64_t ve = a_vox_begin[a0 + j + 1];
-            float acc0 = 0.f, acc1 = 0.f;
-            for (; v < ve; ++v) {
-                const float4 pos = vox_pos[v], out = vox_out[v];
-                if (DIAG) {
-                    acc0 += voxel_w_diag(pos, out, r0[0], r0[1], r0[2]);
-                    if (two) acc1 += voxel_w_diag(pos, out, r1[0], r1[1], r1[2]);
-                } else {
-                    acc0 += voxel_w_general(pos, out, r0[0], r0[1], r0[2], nnb, s_d);
-                    if (two) acc1 += voxel_w_general(pos, out, r1[0], r1[1], r1[2], nnb, s_d);
+        for (int q = 0; q < NP; ++q) acc[q] = 0.f;
+        for (; v < ve; ++v) {
+            const float4 pos = vox_pos[v], out = vox_out[v];
+            acc[0] += DIAG ? voxel_w_diag(pos, out, r0, ic) : voxel_w_general(pos, out, r0, nnb, s_d, ic);
+            if (NP == 2)
+                acc[NP - 1] += DIAG ? voxel_w_diag(pos, out, r1, ic) : voxel_w_general(pos, out, r1, nnb, s_d, ic);
+        }
+        const float2 at = at_hilo[a0 + j];
+        const float e = isinf(at.x) ? 0.f : ex2a(fmaf(k5, at.x, k5 * at.y));
+#pragma unroll
+        for (int q = 0; q < NP; ++q) s_w[q][j][tid] = acc[q] * e;
+    }
+}
+
+// Work items: (64-AP K tile kt, group of blockDim simulations), taken from the counter `work`
+// (zeroed before the launch) by a grid of one wave of resident blocks; every item writes its own
+// outputs, so the results do not depend on the order.  Per item and lead pair the block writes
+// the BF16 hi/lo tile rows and, for the steady part, per entry e of the tile's layer
+//     P1[kt][e][row'] = (sum_c Z0[c], sum_c G_e[c] Z1[c]) over the tile's 8-AP chunks c below the
+//     entry's prefix end,  Z0[c] = sum_{a in c} W'[a],  Z1[c] = sum_{a in c} W'[a] exp(-k4 (at_ref - at_a)),
+// G_e[c] = gtab[goff[L][e] + c - c8s[L]] = exp(-k4 (t0_e - at_ref[c])), at_ref = the chunk's last
+// finite activation time (APs ascend within a layer, so the factors are <= 1), row' = l * S + s;
+// sums in FP32 over at most 8 chunks.  k_band_u adds the K tiles of a layer in a fixed order.
+// lrel: [S][nmove] lead positions relative to the voxel centre (FP32, differences taken in FP64
+// on the host); k5l: [S][nl] k5 * log2(e).
+constexpr int MAXE = 8;
+constexpr int LF_THREADS = 128;
+template <int N, bool DIAG>
+__global__ void __launch_bounds__(LF_THREADS) k_batch_lead_field(
+    int nkt, int nsg, int *__restrict__ work, InteriorField ic, const int64_t *__restrict__ a_vox_begin,
+    const float4 *__restrict__ vox_pos, const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs,
+    const float2 *__restrict__ at_hilo, const int32_t *__restrict__ a_layer, const float *__restrict__ k5l, int nl,
+    const float4 *__restrict__ hconst, const float4 *__restrict__ lrel, int nmove, int n_sims,
+    const int32_t *__restrict__ c8s, const int32_t *__restrict__ nent, const int32_t *__restrict__ esplit8,
+    const int64_t *__restrict__ goff, const float *__restrict__ gtab, int max_ent, uint8_t *__restrict__ Bt,
+    float2 *__restrict__ P1) {
+    __shared__ float s_d[26 * 4];
+    __shared__ float s_w[2][8][LF_THREADS];
+    __shared__ float s_acc[2][MAXE][2][LF_THREADS];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    if (tid < nnb) {
+        const float dz = difs[3 * tid], dy = difs[3 * tid + 1], dx = difs[3 * tid + 2];
+        s_d[4 * tid] = dz;
+        s_d[4 * tid + 1] = dy;
+        s_d[4 * tid + 2] = dx;
+        s_d[4 * tid + 3] = dz * dz + dy * dy + dx * dx;
+    }
+    const int rows_used = n_sims * nmove;
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_item = atomicAdd(work, 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= nkt * nsg) break;
+        const int kt = item / nsg;
+        const int s = (item % nsg) * LF_THREADS + tid;
+        if (s >= n_sims) continue;
+        const int64_t t0a = (int64_t)kt * BKT;
+        const int L = a_layer[t0a];
+        const float k5 = k5l[(size_t)s * nl + L], k4 = hconst[L].y;
+        const int ne = nent[L], cb = c8s[L];
+        for (int l0 = 0; l0 < nmove; l0 += 2) {
+            const int np = l0 + 1 < nmove ? 2 : 1;
+            const float4 r0 = lrel[(size_t)s * nmove + l0];
+            const float4 r1 = np == 2 ? lrel[(size_t)s * nmove + l0 + 1] : r0;
+            for (int e = 0; e < ne; ++e)
+                for (int q = 0; q < 2; ++q) s_acc[q][e][0][tid] = s_acc[q][e][1][tid] = 0.f;
+#pragma unroll 1
+            for (int kc = 0; kc < BKT / 8; ++kc) {
+                const int c8 = kt * (BKT / 8) + kc;
+                const int64_t a0 = (int64_t)c8 * 8;
+                if (np == 2)
+                    chunk_w<DIAG, 2>(a0, a_vox_begin, at_hilo, vox_pos, vox_out, r0, r1, nnb, s_d, ic, k5, s_w, tid);
+                else
+                    chunk_w<DIAG, 1>(a0, a_vox_begin, at_hilo, vox_pos, vox_out, r0, r1, nnb, s_d, ic, k5, s_w, tid);
+                float2 ref = make_float2(0.f, 0.f);
+                for (int j = 7; j >= 0; --j) {
+                    const float2 v = at_hilo[a0 + j];
+                    if (!isinf(v.x)) {
+                        ref = v;
+                        break;
+                    }
+                }
+                float ez[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const float2 v = at_hilo[a0 + j];
+                    ez[j] = isinf(v.x) ? 0.f : ex2a(-k4 * ((ref.x - v.x) + (ref.y - v.y)));
+                }
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    if (q >= np) break;
+                    float wv[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) wv[j] = s_w[q][j][tid];
+                    uint4 hv, lv;
+                    split2(wv[0], wv[1], hv.x, lv.x);
+                    split2(wv[2], wv[3], hv.y, lv.y);
+                    split2(wv[4], wv[5], hv.z, lv.z);
+                    split2(wv[6], wv[7], hv.w, lv.w);
+                    const int row = s * nmove + l0 + q;
+                    const int nt = row / N, n = row % N;
+                    const size_t tile = ((size_t)nt * nkt + kt) * 2;
+                    const size_t off = (size_t)(kc * (N / 8) + n / 8) * 128 + (n % 8) * 16;
+                    *reinterpret_cast<uint4 *>(Bt + tile * (N * 128) + off) = hv;
+                    *reinterpret_cast<uint4 *>(Bt + (tile + 1) * (N * 128) + off) = lv;
+                    float z0 = 0.f, z1 = 0.f;
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        z0 += wv[j];
+                        z1 = fmaf(wv[j], ez[j], z1);
+                    }
+                    for (int ei = 0; ei < ne; ++ei)
+                        if (c8 < esplit8[L * MAXE + ei]) {
+                            s_acc[q][ei][0][tid] += z0;
+                            s_acc[q][ei][1][tid] =
+                                fmaf(gtab[goff[L * MAXE + ei] + (c8 - cb)], z1, s_acc[q][ei][1][tid]);
+                        }
                 }
             }
-            w0[j] = acc0 * e[j];
-            w1[j] = acc1 * e[j];
-        }
-        for (int q = 0; q < (two ? 2 : 1); ++q) {
-            const float *wv = q ? w1 : w0;
-            uint4 hv, lv;
-            split2(wv[0], wv[1], hv.x, lv.x);
-            split2(wv[2], wv[3], hv.y, lv.y);
-            split2(wv[4], wv[5], hv.z, lv.z);
-            split2(wv[6], wv[7], hv.w, lv.w);
-            const int row = s * nmove + l0 + q;
-            const int nt = row / N, n = row % N;
-            const size_t tile = ((size_t)nt * nkt + kt) * 2;
-            const size_t off = (size_t)(kc * (N / 8) + n / 8) * 128 + (n % 8) * 16;
-            *reinterpret_cast<uint4 *>(Bt + tile * (N * 128) + off) = hv;
-            *reinterpret_cast<uint4 *>(Bt + (tile + 1) * (N * 128) + off) = lv;
+            for (int q = 0; q < np; ++q)
+                for (int ei = 0; ei < ne; ++ei)
+                    if (kt * (BKT / 8) < esplit8[L * MAXE + ei])
+                        P1[((size_t)kt * max_ent + ei) * rows_used + (size_t)(l0 + q) * n_sims + s] =
+                            make_float2(s_acc[q][ei][0][tid], s_acc[q][ei][1][tid]);
         }
     }
+}
+
+// Steady sums per (row', layer, entry): U[row'][L][e] = sum over the layer's K tiles [ls0, ls1)
+// below the entry's prefix end of P1[kt][e][row'] (U0, U1), in FP64.  Two passes in a fixed
+// order: k_band_u sums BU_PARTS consecutive parts of the K range per (part, layer) block (threads
+// over rows), k_band_u2 adds the parts.  Up: [parts][rows][nl][max_ent].
+constexpr int BU_PARTS = 64;
+__global__ void __launch_bounds__(256) k_band_u(int rows_used, int nl, int max_ent, const int32_t *__restrict__ nent,
+                                                const int32_t *__restrict__ esplit8, const int32_t *__restrict__ ls0,
+                                                const int32_t *__restrict__ ls1, const float2 *__restrict__ P1,
+                                                double2 *__restrict__ Up) {
+    const int p = blockIdx.x, L = blockIdx.y;
+    const int ne = nent[L], n = ls1[L] - ls0[L];
+    const int g0 = ls0[L] + (int)((int64_t)n * p / BU_PARTS), g1 = ls0[L] + (int)((int64_t)n * (p + 1) / BU_PARTS);
+    for (int rr = threadIdx.x; rr < rows_used; rr += blockDim.x)
+        for (int e = 0; e < ne; ++e) {
+            const int ge = min(g1, (esplit8[L * MAXE + e] + 7) / 8);
+            double a = 0.0, b = 0.0;
+#pragma unroll 4
+            for (int g = g0; g < ge; ++g) {
+                const float2 v = P1[((size_t)g * max_ent + e) * rows_used + rr];
+                a += (double)v.x;
+                b += (double)v.y;
+            }
+            Up[(((size_t)p * rows_used + rr) * nl + L) * max_ent + e] = make_double2(a, b);
+        }
+}
+
+__global__ void k_band_u2(int rows_used, int nl, int max_ent, const int32_t *__restrict__ nent,
+                          const double2 *__restrict__ Up, double2 *__restrict__ U) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= (int64_t)rows_used * nl * max_ent) return;
+    const int e = (int)(i % max_ent), L = (int)((i / max_ent) % nl);
+    if (e >= nent[L]) return;
+    const size_t stride = (size_t)rows_used * nl * max_ent;
+    double a = 0.0, b = 0.0;
+    for (int p = 0; p < BU_PARTS; ++p) {
+        const double2 v = Up[p * stride + i];
+        a += v.x;
+        b += v.y;
+    }
+    U[i] = make_double2(a, b);
 }
 
 // ------------------------------------------------------------------ batch GEMM
@@ -274,14 +446,14 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// grid (t tiles, N tiles, K chunks).  Chunk c covers 64-AP tiles [ck0[c], ck1[c]) inside layer cl[c].
+// grid (work items, N tiles).  Item c = (t tile, first stage, end stage, layer): the band of one
+// 128-step tile inside one layer, in 32-AP stages.  partial: [items][rows][128].
 template <int NB, int N>
 __global__ void __launch_bounds__(WS_THREADS, 1) k_batch_umma(
     int steps, int nl, int nkt, int rows, int nmove, int n_sims, const float2 *__restrict__ t_hilo,
-    const float2 *__restrict__ at_hilo, const int32_t *__restrict__ ck0, const int32_t *__restrict__ ck1,
-    const int32_t *__restrict__ cl, const float4 *__restrict__ hconst, const double *__restrict__ k3,
-    const double *__restrict__ F, const uint8_t *__restrict__ Bt, double *__restrict__ partial,
-    uint32_t *__restrict__ err) {
+    const float2 *__restrict__ at_hilo, const int4 *__restrict__ items, const float4 *__restrict__ hconst,
+    const double *__restrict__ k3, const double *__restrict__ F, const uint8_t *__restrict__ Bt,
+    double *__restrict__ partial, uint32_t *__restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     BatchSmem<NB, N> &S =
         *reinterpret_cast<BatchSmem<NB, N> *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -297,8 +469,9 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_batch_umma(
     constexpr int NPROD = 256;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int t0 = blockIdx.x * BM, nt = blockIdx.y, c = blockIdx.z;
-    const int st0 = 2 * ck0[c], nk = 2 * (ck1[c] - ck0[c]), L = cl[c];
+    const int c = blockIdx.x, nt = blockIdx.y;
+    const int4 item = items[c];
+    const int t0 = item.x * BM, st0 = item.y, nk = item.z - item.y, L = item.w;
     const int nseg = (nk + DRAIN - 1) / DRAIN;
 
     if (tid == 0) {
@@ -429,7 +602,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_batch_umma(
                     } else {
                         v = (double)acc[jj] * f;
                     }
-                    partial[((size_t)c * rows + r) * steps + t] = v;
+                    partial[((size_t)c * rows + r) * BM + (t - t0)] = v;
                 }
             }
         }
@@ -490,22 +663,37 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_batch_umma(
     if (warp == 0) tmem_dealloc(tmem, TCOLS);
 }
 
-// ecg[s][l][t] (l < nmove) = sum_c partial[c][s*nmove + l][t]; block per (row, 32 steps)
-__global__ void k_reduce_rows(int steps, int rows, int nchunks, int nmove, int nleads, const double *__restrict__ partial,
-                              const double *__restrict__ k0w, double *__restrict__ ecg) {
+// ecg[s][l][t] (l < nmove) = sum over the band items c of t's tile of partial[c][row][t - t0]
+//   + sum_L F[s][L][t] ((1 - k3) E[L][t] U1 + k3 U0),  (U0, U1) = U[row'][L][ent[L][j]],
+// E[L][t] = exp(-k4_L (t - t0 of the entry)), row = s * nmove + l, row' = l * S + s, j = t / 128;
+// block per (row, 32 steps), warps split the items, fixed order.
+__global__ void k_reduce_band(int steps, int rows, int nmove, int n_sims, int nleads, int nl, int ntt, int max_ent,
+                              const int32_t *__restrict__ tc0, const int32_t *__restrict__ tc1,
+                              const int32_t *__restrict__ ent, const double *__restrict__ partial,
+                              const double2 *__restrict__ U, const double *__restrict__ E,
+                              const double *__restrict__ F, const double *__restrict__ k3, double *__restrict__ ecg) {
     __shared__ double red[8][33];
     const int tt = blockIdx.x * 32 + (threadIdx.x & 31);
     const int w = threadIdx.x >> 5;
     const int r = blockIdx.y;
     const int s = r / nmove, l = r % nmove;
+    const int j = (blockIdx.x * 32) / BM, tl = tt - j * BM;
     double acc = 0.0;
     if (tt < steps)
-        for (int c = w; c < nchunks; c += 8) acc += partial[((size_t)c * rows + r) * steps + tt];
+        for (int c = tc0[j] + w; c < tc1[j]; c += 8) acc += partial[((size_t)c * rows + r) * BM + tl];
     red[w][threadIdx.x & 31] = acc;
     __syncthreads();
     if (w == 0 && tt < steps) {
-        double v = k0w ? k0w[(size_t)s * nleads + l] : 0.0;
+        double v = 0.0;
         for (int i = 0; i < 8; ++i) v += red[i][threadIdx.x];
+        const size_t rp = (size_t)l * n_sims + s;
+        for (int L = 0; L < nl; ++L) {
+            const int e = ent[L * ntt + j];
+            if (e < 0) continue;
+            const double kk = k3[(size_t)s * nl + L];
+            const double2 u = U[(rp * nl + L) * max_ent + e];
+            v += F[((size_t)s * nl + L) * steps + tt] * ((1.0 - kk) * E[(size_t)L * steps + tt] * u.y + kk * u.x);
+        }
         ecg[((size_t)s * nleads + l) * steps + tt] = v;
     }
 }
@@ -518,10 +706,10 @@ void launch_gemm(cudaStream_t st, const BatchArgs &A) {
         EKG_CUDA(cudaFuncSetAttribute(k_batch_umma<NB, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
-    dim3 grid((unsigned)((A.steps + BM - 1) / BM), (unsigned)A.ntiles, (unsigned)A.nchunks);
+    dim3 grid((unsigned)A.nitems, (unsigned)A.ntiles);
     k_batch_umma<NB, N><<<grid, WS_THREADS, smem, st>>>(A.steps, A.nl, A.nkt, A.rows, A.nmove, A.n_sims, A.t_hilo,
-                                                        A.at_hilo, A.ck0, A.ck1, A.cl, A.hconst, A.k3, A.F, A.Bt,
-                                                        A.partial, A.err);
+                                                        A.at_hilo, A.items, A.hconst, A.k3, A.F, A.Bt, A.partial,
+                                                        A.err);
     EKG_CUDA(cudaGetLastError());
 }
 
@@ -537,14 +725,14 @@ void launch_taylor_w(cudaStream_t s, const HeartDev &h, const float *W0, int J, 
 }
 
 void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int32_t *lc0, const int32_t *lc1,
-                          const double *partial, double *Q) {
+                          const double *partial, float *Q) {
     dim3 grid((unsigned)((steps + 31) / 32), (unsigned)rows);
     k_reduce_layers<<<grid, 256, 0, s>>>(steps, rows, nl, lc0, lc1, partial, Q);
     EKG_CUDA(cudaGetLastError());
 }
 
 void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const double *F,
-                           const double *coef, const double *k3, const double *Q1, const double *Q2, double *ecg) {
+                           const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg) {
     if (nmove >= h.nleads) return;
     dim3 grid((unsigned)((h.steps + 127) / 128), (unsigned)(h.nleads - nmove), (unsigned)n_sims);
     k_static_combine<<<grid, 128, 0, s>>>(h.steps, h.nleads, h.nlayers, J, Jb, nmove, n_sims, F, coef, k3, Q1, Q2,
@@ -552,17 +740,34 @@ void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int
     EKG_CUDA(cudaGetLastError());
 }
 
-void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const double *layer_k,
-                             const double *leads, int nmove, int n_sims, uint8_t *Bt) {
-    const int threads = n_sims < 128 ? ((n_sims + 31) / 32) * 32 : 128;
-    dim3 grid((unsigned)(h.apad / 8), (unsigned)((n_sims + threads - 1) / threads));
+void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const float *k5l,
+                             const float4 *hconst, const float4 *lrel, int nmove, int n_sims, const BandArgs &B,
+                             uint8_t *Bt, int *work, int sm_count) {
+    const int nsg = (n_sims + LF_THREADS - 1) / LF_THREADS;
     const int nkt = (int)(h.apad / BKT);
     const bool diag = h.nhood == EKG_NHOOD_3D4;
-#define EKG_LF(NN, DG)                                                                                           \
-    k_batch_lead_field<NN, DG><<<grid, threads, 0, s>>>(h.apad, nkt, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, \
-                                                        h.nnb, h.difs.p, h.at.p, h.a_layer.p, layer_k, h.nlayers,  \
-                                                        leads, h.centre[0], h.centre[1], h.centre[2], h.nleads,    \
-                                                        nmove, n_sims, Bt)
+    InteriorField ic;
+    if (h.interior_mask) {
+        ic.a0 = h.interior_c[0];
+        ic.a1 = h.interior_c[1];
+        ic.b0 = h.interior_c[2];
+        ic.b1 = h.interior_c[3];
+        ic.b2 = h.interior_c[4];
+        ic.mask = h.interior_mask;
+    }
+    EKG_CUDA(cudaMemsetAsync(work, 0, sizeof(int), s));
+#define EKG_LF(NN, DG)                                                                                            \
+    do {                                                                                                          \
+        static int per_sm = 0;                                                                                    \
+        if (!per_sm)                                                                                              \
+            EKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_lead_field<NN, DG>,           \
+                                                                   LF_THREADS, 0));                               \
+        const int grid = std::max(1, std::min(nkt * nsg, std::max(1, per_sm) * sm_count));                       \
+        k_batch_lead_field<NN, DG><<<grid, LF_THREADS, 0, s>>>(                                                   \
+            nkt, nsg, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p, \
+            k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.c8s, B.nent, B.esplit8, B.goff, B.gtab, B.max_ent, Bt, \
+            B.P1);                                                                                                \
+    } while (0)
     if (two_bases) {
         if (diag) EKG_LF(128, true);
         else EKG_LF(128, false);
@@ -575,14 +780,25 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, c
 }
 
 void launch_batch_gemm(cudaStream_t s, const BatchArgs &A) {
+    if (A.nitems == 0) return;
     if (A.two_bases) launch_gemm<2, 128>(s, A);
     else launch_gemm<1, 256>(s, A);
 }
 
-void launch_reduce_rows(cudaStream_t s, int steps, int rows_used, int rows, int nchunks, int nmove, int nleads,
-                        const double *partial, const double *k0w, double *ecg) {
-    dim3 grid((unsigned)((steps + 31) / 32), (unsigned)rows_used);
-    k_reduce_rows<<<grid, 256, 0, s>>>(steps, rows, nchunks, nmove, nleads, partial, k0w, ecg);
+int band_u_parts() { return BU_PARTS; }
+
+void launch_band_u(cudaStream_t s, const BandArgs &A) {
+    k_band_u<<<dim3(BU_PARTS, (unsigned)A.nl), 256, 0, s>>>(A.rows_used, A.nl, A.max_ent, A.nent, A.esplit8, A.ls0,
+                                                           A.ls1, A.P1, A.Up);
+    const int64_t n = (int64_t)A.rows_used * A.nl * A.max_ent;
+    k_band_u2<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A.rows_used, A.nl, A.max_ent, A.nent, A.Up, A.U);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_reduce_band(cudaStream_t s, const BandArgs &A) {
+    dim3 grid((unsigned)((A.steps + 31) / 32), (unsigned)A.rows_used);
+    k_reduce_band<<<grid, 256, 0, s>>>(A.steps, A.rows, A.nmove, A.n_sims, A.nleads, A.nl, A.ntt, A.max_ent, A.tc0,
+                                       A.tc1, A.ent, A.partial, A.U, A.E, A.F, A.k3, A.ecg);
     EKG_CUDA(cudaGetLastError());
 }
 

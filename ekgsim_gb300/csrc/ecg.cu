@@ -100,22 +100,32 @@ __global__ void k_lead_field(int64_t apad, const int64_t *__restrict__ a_vox_beg
 }
 
 // ------------------------------------------------------------------ per-layer factors
-// One thread per (sim, layer, step).  layer_k: [S][nl][9].
+// F[s][L][t] = k2 exp(-k5 t) R(t), R(t) = 1 - (1 + exp(-k7 (t - k8) + ln(2^(k7/k6) - 1)))^(-k6/k7)
+// (the repolarisation factor of WohlfartPlus, sim.cpp).  Block per (sim, layer): the constant
+// ln(2^(k7/k6) - 1) and the exponent u = -k7 (t - k8) + ln(...) in FP64, the transcendentals in
+// FP32 in a form that keeps relative precision at both ends:
+//     ln(1 + e^u) = log1p(exp(u)) (u + log1p(exp(-u)) for u > 0),  R = -expm1(-(k6/k7) ln(1 + e^u)).
+// layer_k: [S][nl][9].
 __global__ void k_layer_factors(int nl, int steps, const double *__restrict__ t, const double *__restrict__ layer_k,
                                 int n_sims, double *__restrict__ F, float *__restrict__ layer_c) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t total = (int64_t)n_sims * nl * steps;
-    if (i >= total) return;
-    const int step = (int)(i % steps);
-    const int64_t sl = i / steps;  // sim * nl + layer
+    const int64_t sl = blockIdx.x;  // sim * nl + layer
     const double *k = layer_k + sl * 9;
-    const double tt = t[step];
-    const double R = 1 - pow((1 + exp(-k[7] * (tt - k[8]) + log(pow(2.0, (k[7] / k[6])) - 1))), -(k[6] / k[7]));
-    F[i] = k[2] * exp(-k[5] * tt) * R;
-    if (step == 0) {
+    __shared__ double c;
+    if (threadIdx.x == 0) {
+        c = log(pow(2.0, k[7] / k[6]) - 1);
         const double L2E = 1.4426950408889634;
-        float4 c = make_float4((float)(k[1] * L2E), (float)(k[4] * L2E), (float)(1.0 - k[3]), (float)k[3]);
-        reinterpret_cast<float4 *>(layer_c)[sl] = c;
+        reinterpret_cast<float4 *>(layer_c)[sl] =
+            make_float4((float)(k[1] * L2E), (float)(k[4] * L2E), (float)(1.0 - k[3]), (float)k[3]);
+    }
+    __syncthreads();
+    const float r = (float)(k[6] / k[7]);
+    for (int step = threadIdx.x; step < steps; step += blockDim.x) {
+        const double tt = t[step];
+        const float u = (float)fma(-k[7], tt - k[8], c);
+        const float sp = u > 0.f ? u + log1pf(expf(-u)) : log1pf(expf(u));
+        const float R = -expm1f(-r * sp);
+        const float e5 = expf((float)(-k[5] * tt));
+        F[sl * steps + step] = k[2] * (double)e5 * (double)R;
     }
 }
 
@@ -225,128 +235,112 @@ __global__ void __launch_bounds__(256) k_reduce_ecg(int steps, int nleads, int n
 }
 
 // ------------------------------------------------------------------ criteria (FP64)
-// One block (256 threads) per (sim, criterion lead).  Output per (s, i): value and argmax.
-template <int NT>
-__device__ double block_sum(double v, double *red) {
-    red[threadIdx.x] = v;
-    __syncthreads();
-    for (int o = NT / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-        __syncthreads();
-    }
-    const double r = red[0];
-    __syncthreads();
-    return r;
+// Output per (s, i): value and argmax.
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_min(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
 }
 
-__global__ void k_criteria(int steps, int nleads, int ncl, int mode, const double *__restrict__ ecg,
+// One warp per (simulation, criterion lead): lanes stride over the steps, FP64 sums combined by
+// a fixed butterfly.  Writes the criterion value and the argmax (first maximum) of the lead.
+__global__ void k_criteria(int steps, int nleads, int ncl, int n_sims, int mode, const double *__restrict__ ecg,
                            const double *__restrict__ targets, const int64_t *__restrict__ tlen,
                            const double *__restrict__ toff, int crit_stride, double *__restrict__ crit) {
-    constexpr int NT = 256;
-    __shared__ double red[NT];
-    __shared__ double s_min[NT], s_max[NT];
-    __shared__ int s_arg[NT];
-    const int i = blockIdx.x, s = blockIdx.y;
+    const int lane = threadIdx.x & 31;
+    const int pair = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (pair >= ncl * n_sims) return;
+    const int i = pair % ncl, s = pair / ncl;
     const double *a = ecg + ((size_t)s * nleads + i) * steps;
     int64_t off = 0;
     for (int j = 0; j < i; ++j) off += tlen[j];
     const double *b = targets + off;
     const int64_t nb = tlen[i];
     const int64_t len = steps < nb ? steps : nb;
+    const double inv = 1.0 / (double)len;
     double value = 0.0;
     if (mode == 2) {
         double sa = 0, sb = 0;
-        for (int64_t j = threadIdx.x; j < len; j += NT) {
+        for (int64_t j = lane; j < len; j += 32) {
             sa += a[j];
             sb += b[j];
         }
-        const double inv = 1.0 / (double)len;
-        const double ma = block_sum<NT>(sa, red) * inv, mb = block_sum<NT>(sb, red) * inv;
+        const double ma = warp_sum(sa) * inv, mb = warp_sum(sb) * inv;
         double va = 0, vb = 0, cv = 0;
-        for (int64_t j = threadIdx.x; j < len; j += NT) {
+        for (int64_t j = lane; j < len; j += 32) {
             const double x = a[j] - ma, y = b[j] - mb;
             va += x * x;
             vb += y * y;
             cv += x * y;
         }
-        va = block_sum<NT>(va, red) * inv;
-        vb = block_sum<NT>(vb, red) * inv;
-        cv = block_sum<NT>(cv, red) / (double)len;
+        va = warp_sum(va) * inv;
+        vb = warp_sum(vb) * inv;
+        cv = warp_sum(cv) / (double)len;
         value = 1.0 - cv / (sqrt(va) * sqrt(vb));
     } else if (mode == 4) {
         double ab = 0, aa = 0, bb = 0;
-        for (int64_t j = threadIdx.x; j < len; j += NT) {
+        for (int64_t j = lane; j < len; j += 32) {
             ab += a[j] * b[j];
             aa += a[j] * a[j];
             bb += b[j] * b[j];
         }
-        ab = block_sum<NT>(ab, red);
-        aa = block_sum<NT>(aa, red);
-        bb = block_sum<NT>(bb, red);
+        ab = warp_sum(ab);
+        aa = warp_sum(aa);
+        bb = warp_sum(bb);
         value = 1.0 - ab / (sqrt(aa) * sqrt(bb));
     } else if (mode == 1) {
         double q = 0;
-        for (int64_t j = threadIdx.x; j < len; j += NT) {
+        for (int64_t j = lane; j < len; j += 32) {
             const double x = a[j] - b[j];
             q += x * x;
         }
-        value = sqrt(block_sum<NT>(q, red) / (double)len);
+        value = sqrt(warp_sum(q) / (double)len);
     } else {
         // devFromLinear (vectorMath.h:373-404): min/max over the whole simulated lead
         double mn = INFINITY, mx = -INFINITY;
-        for (int64_t j = threadIdx.x; j < steps; j += NT) {
+        for (int64_t j = lane; j < steps; j += 32) {
             mn = fmin(mn, a[j]);
             mx = fmax(mx, a[j]);
         }
-        s_min[threadIdx.x] = mn;
-        s_max[threadIdx.x] = mx;
-        __syncthreads();
-        for (int o = NT / 2; o > 0; o >>= 1) {
-            if (threadIdx.x < o) {
-                s_min[threadIdx.x] = fmin(s_min[threadIdx.x], s_min[threadIdx.x + o]);
-                s_max[threadIdx.x] = fmax(s_max[threadIdx.x], s_max[threadIdx.x + o]);
-            }
-            __syncthreads();
-        }
-        const double amult = 1.0 / (s_max[0] - s_min[0]);
+        const double amult = 1.0 / (warp_max(mx) - warp_min(mn));
         const double bofs = toff[i];
         double sd = 0;
-        for (int64_t j = threadIdx.x; j < len; j += NT) sd += (a[j] * amult + bofs) / (b[j] + bofs);
-        const double inv = 1.0 / (double)len;
-        const double mean = block_sum<NT>(sd, red) * inv;
+        for (int64_t j = lane; j < len; j += 32) sd += (a[j] * amult + bofs) / (b[j] + bofs);
+        const double mean = warp_sum(sd) * inv;
         double var = 0;
-        for (int64_t j = threadIdx.x; j < len; j += NT) {
+        for (int64_t j = lane; j < len; j += 32) {
             const double d = (a[j] * amult + bofs) / (b[j] + bofs) - mean;
             var += d * d;
         }
-        var = block_sum<NT>(var, red) * inv;
+        var = warp_sum(var) * inv;
         value = (var == 0) ? 1.0 / 1e-30 : sqrt(var);
     }
     // argmax of the simulated lead (first maximum), for the peak-position criterion
     double best = -INFINITY;
     int arg = 0x7fffffff;
-    for (int j = threadIdx.x; j < steps; j += NT)
+    for (int j = lane; j < steps; j += 32)
         if (a[j] > best) {
             best = a[j];
             arg = j;
         }
-    s_max[threadIdx.x] = best;
-    s_arg[threadIdx.x] = arg;
-    __syncthreads();
-    for (int o = NT / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) {
-            const double v2 = s_max[threadIdx.x + o];
-            const int a2 = s_arg[threadIdx.x + o];
-            if (v2 > s_max[threadIdx.x] || (v2 == s_max[threadIdx.x] && a2 < s_arg[threadIdx.x])) {
-                s_max[threadIdx.x] = v2;
-                s_arg[threadIdx.x] = a2;
-            }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double v2 = __shfl_xor_sync(0xffffffffu, best, o);
+        const int a2 = __shfl_xor_sync(0xffffffffu, arg, o);
+        if (v2 > best || (v2 == best && a2 < arg)) {
+            best = v2;
+            arg = a2;
         }
-        __syncthreads();
     }
-    if (threadIdx.x == 0) {
+    if (lane == 0) {
         crit[((size_t)s * crit_stride + i) * 2 + 0] = value;
-        crit[((size_t)s * crit_stride + i) * 2 + 1] = (double)s_arg[0];
+        crit[((size_t)s * crit_stride + i) * 2 + 1] = (double)arg;
     }
 }
 
@@ -363,9 +357,8 @@ void launch_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads,
 
 void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_layer_k, int n_sims, double *d_F,
                           float *d_layer_c) {
-    const int64_t total = (int64_t)n_sims * h.nlayers * h.steps;
-    k_layer_factors<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(h.nlayers, h.steps, h.t.p, d_layer_k, n_sims,
-                                                                   d_F, d_layer_c);
+    k_layer_factors<<<(unsigned)((int64_t)n_sims * h.nlayers), 128, 0, s>>>(h.nlayers, h.steps, h.t.p, d_layer_k,
+                                                                            n_sims, d_F, d_layer_c);
     EKG_CUDA(cudaGetLastError());
 }
 
@@ -404,9 +397,9 @@ void launch_criteria(cudaStream_t s, const HeartDev &h, const double *d_ecg, int
                      int n_crit_leads, int mode, const double *d_targets, const int64_t *d_tlen,
                      const double *d_toff, double *d_crit) {
     if (n_crit_leads <= 0) return;
-    dim3 grid((unsigned)n_crit_leads, (unsigned)n_sims);
-    k_criteria<<<grid, 256, 0, s>>>(h.steps, h.nleads, n_crit_leads, mode, d_ecg, d_targets, d_tlen, d_toff,
-                                    ncrit_stride, d_crit);
+    const int64_t pairs = (int64_t)n_crit_leads * n_sims;
+    k_criteria<<<(unsigned)((pairs + 7) / 8), 256, 0, s>>>(h.steps, h.nleads, n_crit_leads, n_sims, mode, d_ecg,
+                                                           d_targets, d_tlen, d_toff, ncrit_stride, d_crit);
     EKG_CUDA(cudaGetLastError());
 }
 

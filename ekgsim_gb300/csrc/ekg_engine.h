@@ -37,22 +37,44 @@ struct BatchState {
     std::vector<double> key;               // k1, k4 per layer the basis was built for
     int J = 0;                             // Taylor terms stored
     std::vector<double> centre, scale;     // per layer
-    DBuf<double> Q1, Q2;                   // [nl][L*J][steps]
+    DBuf<float> Q1, Q2;                    // [nl][L*J][steps]
     DBuf<double> d_centre, d_scale;
     DBuf<int32_t> lc0, lc1;                // chunk range of each layer
+    // band structure of the moved-lead GEMM for the same key, per layer L and 128-step tile j
+    int ntt = 0;                           // tiles
+    int max_ent = 1;                       // steady entries per layer (max)
+    std::vector<int32_t> band_s0, band_s1; // [nl][ntt] band in 32-AP stages [s0, s1)
+    DBuf<int32_t> ls0, ls1;                // [nl] 64-AP K tile range of each layer
+    DBuf<int32_t> c8s, nent, esplit8;      // [nl], [nl], [nl][8]: first chunk, entries, steady prefix ends
+    DBuf<int64_t> goff;                    // [nl][8] offsets into gtab
+    DBuf<float> gtab;                      // exp(-k4 (t0_e - at_ref[c8])) for the steady chunks of entry e
+    DBuf<int32_t> ent;                     // [nl][ntt] entry of each tile (-1: layer without APs)
+    DBuf<double> E;                        // [nl][steps] exp(-k4 (t - t0 of the tile's entry))
+    // per batch
     DBuf<uint8_t> Bt;                      // tiled BF16 hi/lo moved-lead weights
-    DBuf<double> partial;                  // [chunks][rows][steps]
-    DBuf<int32_t> ck0, ck1, cl;            // GEMM K chunks
+    DBuf<float2> P1;                       // [K tiles][max_ent][rows] steady sums per 64-AP tile
+    DBuf<int> work;                        // work counter of the operand kernel
+    DBuf<double2> U, Up;                   // [rows][nl][max_ent] steady sums (U0, U1), per K part
+    DBuf<double> partial;                  // [items][rows][128]
+    DBuf<int4> items;                      // GEMM work items
+    DBuf<int32_t> tc0, tc1;                // item range of each tile
+    DBuf<float> k5l;                       // [S][nl] k5 log2(e)
+    DBuf<float4> lrel;                     // [S][nmove] moved lead positions relative to the voxel centre
     DBuf<float4> hconst;
-    DBuf<double> k3, coef;
+    DBuf<double> k3;
+    DBuf<float> coef;
 };
 // What one device pass does, decided on the host from the batch's layer APs and lead positions.
 struct PassPlan {
     bool batch = false;                    // separable batched form
     int n_sims = 0, nmove = 0, J = 0, two_bases = 0;
-    int rows_used = 0, rows = 0, ntiles = 0, nchunks = 0;
-    std::vector<double> coef, k3;          // [S][nl][J], [S][nl]
-    std::vector<int32_t> ck0, ck1, cl;
+    int rows_used = 0, rows = 0, ntiles = 0, nitems = 0;
+    std::vector<float> coef;               // [S][nl][J]
+    std::vector<double> k3;                // [S][nl]
+    std::vector<int4> items;               // band GEMM work items, grouped by tile
+    std::vector<int32_t> tc0, tc1;         // [ntt] item range of each tile
+    std::vector<float> k5l;                // [S][nl]
+    std::vector<float4> lrel;              // [S][nmove]
     float4 hc[256];
 };
 }  // namespace ekg

@@ -108,6 +108,10 @@ struct HeartDev {
     int nnb = 0;
     int8_t nb_dif[26 * 3];
     DBuf<int8_t> difs;      // [nnb*3] device copy of nb_dif
+    // closed form of the field of a voxel with every neighbour present (moved-lead operand):
+    // rho^5 (c1 T4 + c0) + rho^7 (c4 T6 + c3 T4 + c2); mask 0 when the set lacks cube symmetry
+    float interior_c[5] = {0, 0, 0, 0, 0};
+    uint32_t interior_mask = 0;
     // time axis
     DBuf<double> t;         // [steps]
     DBuf<float2> t_hilo;    // [steps]
@@ -160,27 +164,44 @@ void launch_contract_umma_args(cudaStream_t s, const ContractArgs &a);
 
 // ------------------------------------------------------------------ batched form (batch.cu)
 struct BatchArgs {
-    int steps = 0, nl = 0, nkt = 0, rows = 0, nmove = 0, n_sims = 0, ntiles = 0, nchunks = 0, two_bases = 0;
+    int steps = 0, nl = 0, nkt = 0, rows = 0, nmove = 0, n_sims = 0, ntiles = 0, nitems = 0, two_bases = 0;
     const float2 *t_hilo = nullptr, *at_hilo = nullptr;
-    const int32_t *ck0 = nullptr, *ck1 = nullptr, *cl = nullptr;
+    const int4 *items = nullptr;  // (t tile, first stage, end stage, layer), stages of 32 APs
     const float4 *hconst = nullptr;
     const double *k3 = nullptr, *F = nullptr;
     const uint8_t *Bt = nullptr;
-    double *partial = nullptr;
+    double *partial = nullptr;    // [items][rows][128]
     uint32_t *err = nullptr;
+};
+// Steady part of the moved-lead ECG and the final reduction (batch.cu k_batch_lead_field,
+// k_band_u, k_reduce_band).
+struct BandArgs {
+    int n_sims = 0, nmove = 0, nl = 0, ntt = 0, steps = 0, rows = 0, rows_used = 0, nleads = 0;
+    int max_ent = 1;
+    const int32_t *c8s = nullptr, *nent = nullptr, *esplit8 = nullptr, *ls0 = nullptr, *ls1 = nullptr;
+    const int32_t *ent = nullptr, *tc0 = nullptr, *tc1 = nullptr;
+    const int64_t *goff = nullptr;
+    const float *gtab = nullptr;
+    const double *E = nullptr, *F = nullptr, *k3 = nullptr, *partial = nullptr;
+    float2 *P1 = nullptr;            // [K tiles][max_ent][rows] steady sums per 64-AP tile
+    double2 *Up = nullptr;           // [band_u_parts()][rows][nl][max_ent]
+    double2 *U = nullptr;            // [rows][nl][max_ent]
+    double *ecg = nullptr;
 };
 int batch_tile_rows(int two_bases);
 void launch_taylor_w(cudaStream_t s, const HeartDev &h, const float *W0, int J, const double *centre,
                      const double *scale, float *Wt);
 void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int32_t *lc0, const int32_t *lc1,
-                          const double *partial, double *Q);
+                          const double *partial, float *Q);
 void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const double *F,
-                           const double *coef, const double *k3, const double *Q1, const double *Q2, double *ecg);
-void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const double *layer_k,
-                             const double *leads, int nmove, int n_sims, uint8_t *Bt);
+                           const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg);
+void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const float *k5l,
+                             const float4 *hconst, const float4 *lrel, int nmove, int n_sims, const BandArgs &B,
+                             uint8_t *Bt, int *work, int sm_count);
 void launch_batch_gemm(cudaStream_t s, const BatchArgs &a);
-void launch_reduce_rows(cudaStream_t s, int steps, int rows_used, int rows, int nchunks, int nmove, int nleads,
-                        const double *partial, const double *k0w, double *ecg);
+int band_u_parts();
+void launch_band_u(cudaStream_t s, const BandArgs &a);
+void launch_reduce_band(cudaStream_t s, const BandArgs &a);
 void launch_reduce_ecg(cudaStream_t s, const HeartDev &h, const double *d_partial, const double *d_k0w,
                        int n_sims, double *d_ecg);
 void launch_criteria(cudaStream_t s, const HeartDev &h, const double *d_ecg, int n_sims, int ncrit_stride,

@@ -1,6 +1,7 @@
 // engine.cpp -- C ABI of the engine: engine and heart lifetime, plain and batched evaluation,
 // simulator.ini front end.
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cstdlib>
 #include <cmath>
@@ -56,6 +57,46 @@ int neighbourhood(int code, int8_t *dif) {
     return cnt;
 }
 
+// Coefficients of the closed-form interior field (batch.cu, voxel_w_*): for a neighbour set that
+// is invariant under the 48 signed axis permutations, sum_n (d.grad)^4 phi = c4 sum_i d_i^4 phi and
+// sum_n (d.grad)^6 phi = c6 sum_i d_i^6 phi for harmonic phi, with c4 = a4 - b4/2 and
+// c6 = a6 - b6 + g6/3 from the moments a4 = sum d_x^4, b4 = 6 sum d_x^2 d_y^2, a6 = sum d_x^6,
+// b6 = 15 sum d_x^4 d_y^2, g6 = 90 sum d_x^2 d_y^2 d_z^2.
+void interior_field(HeartDev &D) {
+    D.interior_mask = 0;
+    std::vector<std::array<int, 3>> set;
+    for (int n = 0; n < D.nnb; ++n) set.push_back({D.nb_dif[3 * n], D.nb_dif[3 * n + 1], D.nb_dif[3 * n + 2]});
+    std::sort(set.begin(), set.end());
+    const int perms[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+    for (const auto &pm : perms)
+        for (int sg = 0; sg < 8; ++sg) {
+            std::vector<std::array<int, 3>> t;
+            for (const auto &d : set) {
+                std::array<int, 3> e;
+                for (int i = 0; i < 3; ++i) e[i] = d[pm[i]] * ((sg >> i) & 1 ? -1 : 1);
+                t.push_back(e);
+            }
+            std::sort(t.begin(), t.end());
+            if (t != set) return;
+        }
+    double a4 = 0, b4 = 0, a6 = 0, b6 = 0, g6 = 0;
+    for (const auto &d : set) {
+        const double x = d[0], y = d[1], z = d[2];
+        a4 += x * x * x * x;
+        b4 += 6 * x * x * y * y;
+        a6 += x * x * x * x * x * x;
+        b6 += 15 * x * x * x * x * y * y;
+        g6 += 90 * x * x * y * y * z * z;
+    }
+    const double f4 = (a4 - b4 / 2) / 6, f6 = (a6 - b6 + g6 / 3) / 120;
+    D.interior_c[0] = (float)(-63 * f4);
+    D.interior_c[1] = (float)(105 * f4);
+    D.interior_c[2] = (float)(4050 * f6);
+    D.interior_c[3] = (float)(-14175 * f6);
+    D.interior_c[4] = (float)(10395 * f6);
+    D.interior_mask = D.nnb >= 32 ? 0xFFFFFFFFu : (1u << D.nnb) - 1u;
+}
+
 // ------------------------------------------------------------------ heart setup
 void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     auto t0 = std::chrono::steady_clock::now();
@@ -82,6 +123,7 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     D.nhood = d->nhood;
     D.nnb = neighbourhood(d->nhood, D.nb_dif);
     EKG_CHECK(D.nnb > 0, EKG_ERR_BAD_INPUT, "unknown neighbourhood (only know of these: 2D4, 3D4, 2D8, 3D8 (cube))");
+    interior_field(D);
 
     // time axis: simTime accumulated by += dt from start (simlib/simulator.cpp:496-500, 519)
     const int64_t steps = (int64_t)std::ceil(d->length / d->dt);
@@ -414,6 +456,122 @@ int taylor_terms(double xmax, int jmax) {
     return -1;
 }
 
+// Band structure of the moved-lead GEMM for per-layer (k1, k4) = key (batch.cu explains the
+// split).  Per layer L (APs [a0, a1), finite ones ascending first, padding after) and 128-step tile
+// j starting at t0: the steady prefix of the tile ends at the first AP with at >= t0 - T+ rounded
+// down to a 32-AP stage (the whole layer once every finite AP is steady), the band ends at the first
+// AP with at > t_last + T- rounded up.  Tiles before the first all-steady tile jf share at most
+// MAXE - 1 steady prefixes ("entries"): a tile uses the prefix of the first tile of its group,
+// which is shorter, so its band only grows.  Tiles from jf on use the whole-layer entry.  Rounding
+// and grouping only move APs into the band, where they are exact.
+void build_band(ekg_heart *h, const std::vector<double> &key, const std::vector<double> &at_h,
+                const std::vector<int32_t> &al) {
+    constexpr int MAXE = 8;
+    BatchState &B = h->bs;
+    const HeartDev &D = h->dev;
+    cudaStream_t s = h->stream;
+    const int nl = D.nlayers, steps = D.steps, ntt = (steps + 127) / 128;
+    const double LN2 = 0.69314718055994531;
+    std::vector<int64_t> la0(nl, -1), la1(nl, -1), nfin(nl, 0);
+    for (int64_t a = 0; a < D.apad; ++a) {
+        const int L = al[a];
+        if (la0[L] < 0) la0[L] = a;
+        la1[L] = a + 1;
+        if (std::isfinite(at_h[a])) ++nfin[L];
+    }
+    B.ntt = ntt;
+    B.band_s0.assign((size_t)nl * ntt, 0);
+    B.band_s1.assign((size_t)nl * ntt, 0);
+    std::vector<int32_t> c8s(nl, 0), nent(nl, 0), esplit8((size_t)nl * MAXE, 0), ent((size_t)nl * ntt, -1);
+    std::vector<int32_t> ls0(nl, 0), ls1(nl, 0);
+    std::vector<int64_t> goff((size_t)nl * MAXE, 0);
+    std::vector<float> gtab;
+    std::vector<double> E((size_t)nl * steps, 1.0);
+    int max_ent = 1;
+    for (int L = 0; L < nl; ++L) {
+        if (la0[L] < 0) continue;
+        const double k1 = key[2 * L], k4 = key[2 * L + 1];
+        const int64_t a0 = la0[L], a1 = la1[L], af = a0 + nfin[L];
+        c8s[L] = (int32_t)(a0 / 8);
+        ls0[L] = (int32_t)(a0 / 64);
+        ls1[L] = (int32_t)(a1 / 64);
+        bool ok = k1 > 0 && k4 >= 0 && k1 > 1.05 * k4 && std::isfinite(k1) && std::isfinite(k4);
+        for (int64_t a = a0; ok && a < a1; ++a)
+            ok = a < af ? (std::isfinite(at_h[a]) && (a == a0 || at_h[a] >= at_h[a - 1])) : !std::isfinite(at_h[a]);
+        const double Tp = 30 * LN2 / k1, Tn = 30 * LN2 / (k1 - k4);
+        std::vector<int64_t> sp(ntt, a0), en(ntt, a1);
+        int jf = ntt;
+        for (int j = 0; j < ntt; ++j) {
+            if (ok) {
+                const double t0 = h->t[128 * j], tl = h->t[std::min(128 * j + 127, steps - 1)];
+                const int64_t i = std::lower_bound(at_h.begin() + a0, at_h.begin() + af, t0 - Tp) - at_h.begin();
+                sp[j] = i >= af ? a1 : i / 32 * 32;
+                const int64_t e = std::upper_bound(at_h.begin() + a0, at_h.begin() + af, tl + Tn) - at_h.begin();
+                en[j] = std::min(a1, (e + 31) / 32 * 32);
+            }
+            if (jf == ntt && sp[j] == a1) jf = j;
+        }
+        // entries: groups of gs tiles before jf, then the whole layer
+        const int gs = std::max(1, (jf + MAXE - 2) / (MAXE - 1));
+        const int ngroups = (jf + gs - 1) / gs;
+        std::vector<int64_t> esp;
+        std::vector<double> eref;
+        for (int g = 0; g < ngroups; ++g) {
+            esp.push_back(sp[g * gs]);
+            eref.push_back(h->t[128 * g * gs]);
+        }
+        if (jf < ntt) {
+            esp.push_back(a1);
+            eref.push_back(h->t[128 * jf]);
+        }
+        nent[L] = (int32_t)esp.size();
+        max_ent = std::max(max_ent, nent[L]);
+        for (int j = 0; j < ntt; ++j) {
+            const int e = j < jf ? j / gs : ngroups;
+            ent[(size_t)L * ntt + j] = e;
+            const int64_t split = esp[e];
+            B.band_s0[(size_t)L * ntt + j] = (int32_t)(split / 32);
+            B.band_s1[(size_t)L * ntt + j] = (int32_t)(std::max(split, en[j]) / 32);
+            for (int t = 128 * j; t < std::min(steps, 128 * j + 128); ++t)
+                E[(size_t)L * steps + t] = std::exp(-k4 * (h->t[t] - eref[e]));
+        }
+        for (int e = 0; e < nent[L]; ++e) {
+            esplit8[(size_t)L * MAXE + e] = (int32_t)(esp[e] / 8);
+            goff[(size_t)L * MAXE + e] = (int64_t)gtab.size();
+            for (int64_t c = a0 / 8; c < esp[e] / 8; ++c) {
+                double ref = NAN;
+                for (int64_t a = 8 * c + 7; a >= 8 * c; --a)
+                    if (std::isfinite(at_h[a])) {
+                        ref = at_h[a];
+                        break;
+                    }
+                gtab.push_back(std::isfinite(ref) ? (float)std::exp(-k4 * (eref[e] - ref)) : 0.f);
+            }
+        }
+    }
+    if (gtab.empty()) gtab.push_back(0.f);
+    B.max_ent = max_ent;
+    B.ls0.alloc(nl);
+    B.ls1.alloc(nl);
+    B.c8s.alloc(nl);
+    B.nent.alloc(nl);
+    B.esplit8.alloc((size_t)nl * MAXE);
+    B.goff.alloc((size_t)nl * MAXE);
+    B.gtab.alloc(gtab.size());
+    B.ent.alloc((size_t)nl * ntt);
+    B.E.alloc((size_t)nl * steps);
+    EKG_CUDA(cudaMemcpyAsync(B.ls0.p, ls0.data(), nl * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(B.ls1.p, ls1.data(), nl * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(B.c8s.p, c8s.data(), nl * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(B.nent.p, nent.data(), nl * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(B.esplit8.p, esplit8.data(), esplit8.size() * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(B.goff.p, goff.data(), goff.size() * 8, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(B.gtab.p, gtab.data(), gtab.size() * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(B.ent.p, ent.data(), ent.size() * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(B.E.p, E.data(), E.size() * 8, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaStreamSynchronize(s));
+}
+
 // Build (or reuse) the static-lead Taylor basis for per-layer (k1, k4) = key.
 void ensure_basis(ekg_heart *h, const std::vector<double> &key) {
     BatchState &B = h->bs;
@@ -507,6 +665,7 @@ void ensure_basis(ekg_heart *h, const std::vector<double> &key) {
         EKG_CUDA(cudaStreamSynchronize(s));
         if (*h->err_host) throw Error{EKG_ERR_TIMEOUT, "a bounded device wait ran out (basis build)"};
     }
+    build_band(h, key, at_h, al);
     B.J = J;
     B.key = key;
     B.basis_ok = true;
@@ -556,7 +715,7 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
             const double x = k[5] * B.scale[i];
             double c = std::exp(k[5] * B.centre[i]);
             for (int j = 0; j < J; ++j) {
-                P.coef[((size_t)si * nl + i) * J + j] = c;
+                P.coef[((size_t)si * nl + i) * J + j] = (float)c;
                 c *= x / (j + 1);
             }
             P.k3[(size_t)si * nl + i] = k[3];
@@ -570,34 +729,42 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
         P.rows_used = n_sims * P.nmove;
         P.ntiles = (P.rows_used + N - 1) / N;
         P.rows = P.ntiles * N;
-        // K chunks: about two CTAs per SM over (t tiles x N tiles x chunks), each inside one layer
-        std::vector<int32_t> ccl(D.nchunks), ca0(D.nchunks), ca1(D.nchunks);
-        EKG_CUDA(cudaMemcpy(ccl.data(), D.chunk_layer.p, D.nchunks * 4, cudaMemcpyDeviceToHost));
-        EKG_CUDA(cudaMemcpy(ca0.data(), D.chunk_a0.p, D.nchunks * 4, cudaMemcpyDeviceToHost));
-        EKG_CUDA(cudaMemcpy(ca1.data(), D.chunk_a1.p, D.nchunks * 4, cudaMemcpyDeviceToHost));
-        std::vector<int> kb(nl, -1), ke(nl, -1);
-        for (int c = 0; c < D.nchunks; ++c) {
-            const int Lc = ccl[c];
-            if (kb[Lc] < 0) kb[Lc] = ca0[c] / 64;
-            ke[Lc] = ca1[c] / 64;
+        // band work items: each (tile, layer) band cut into pieces of at most `per` stages, `per`
+        // the smallest that keeps all items x N tiles within one wave of CTAs (one per SM)
+        const int ntt = B.ntt;
+        int64_t total = 0;
+        for (size_t i = 0; i < B.band_s0.size(); ++i) total += B.band_s1[i] - B.band_s0[i];
+        const int target = std::max(1, h->eng->batch_ctas > 0 ? h->eng->batch_ctas : h->sm_count);
+        int64_t per = std::max<int64_t>(1, (total * P.ntiles + target - 1) / target);
+        for (;; ++per) {
+            int64_t cnt = 0;
+            for (size_t i = 0; i < B.band_s0.size(); ++i) cnt += (B.band_s1[i] - B.band_s0[i] + per - 1) / per;
+            if (cnt * P.ntiles <= target || per >= total) break;
         }
-        int kt_total = 0;
-        for (int i = 0; i < nl; ++i)
-            if (kb[i] >= 0) kt_total += ke[i] - kb[i];
-        const int ttiles = (D.steps + 127) / 128;
-        const int target = h->eng->batch_ctas > 0 ? h->eng->batch_ctas : 2 * h->sm_count;
-        const int per = std::max(1, (int)std::ceil((double)target / (ttiles * P.ntiles)));
-        for (int i = 0; i < nl; ++i) {
-            if (kb[i] < 0) continue;
-            const int n = ke[i] - kb[i];
-            const int nc = std::max(1, std::min(n, (int)std::lround((double)per * n / std::max(1, kt_total))));
-            for (int c = 0; c < nc; ++c) {
-                P.ck0.push_back(kb[i] + (int)((int64_t)n * c / nc));
-                P.ck1.push_back(kb[i] + (int)((int64_t)n * (c + 1) / nc));
-                P.cl.push_back(i);
+        P.tc0.assign(ntt, 0);
+        P.tc1.assign(ntt, 0);
+        for (int j = 0; j < ntt; ++j) {
+            P.tc0[j] = (int32_t)P.items.size();
+            for (int i = 0; i < nl; ++i) {
+                const int s0 = B.band_s0[(size_t)i * ntt + j], n = B.band_s1[(size_t)i * ntt + j] - s0;
+                if (n <= 0) continue;
+                const int nc = (int)((n + per - 1) / per);
+                for (int c = 0; c < nc; ++c)
+                    P.items.push_back(make_int4(j, s0 + (int)((int64_t)n * c / nc), s0 + (int)((int64_t)n * (c + 1) / nc), i));
             }
+            P.tc1[j] = (int32_t)P.items.size();
         }
-        P.nchunks = (int)P.ck0.size();
+        P.nitems = (int)P.items.size();
+        // per-simulation k5 and moved lead positions for the operand kernel
+        P.k5l.resize((size_t)n_sims * nl);
+        for (size_t i = 0; i < P.k5l.size(); ++i) P.k5l[i] = (float)(layer_k[9 * i + 5] * L2E);
+        P.lrel.resize((size_t)n_sims * P.nmove);
+        for (int si = 0; si < n_sims; ++si)
+            for (int l = 0; l < P.nmove; ++l) {
+                const double *r = leads + ((size_t)si * L + l) * 3;
+                P.lrel[(size_t)si * P.nmove + l] =
+                    make_float4((float)(r[0] - D.centre[0]), (float)(r[1] - D.centre[1]), (float)(r[2] - D.centre[2]), 0.f);
+            }
     }
     return P;
 }
@@ -620,20 +787,33 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
         B.coef.alloc(P.coef.size());
         B.k3.alloc(P.k3.size());
         B.hconst.alloc(D.nlayers);
-        EKG_CUDA(cudaMemcpyAsync(B.coef.p, P.coef.data(), P.coef.size() * 8, cudaMemcpyHostToDevice, s));
+        EKG_CUDA(cudaMemcpyAsync(B.coef.p, P.coef.data(), P.coef.size() * 4, cudaMemcpyHostToDevice, s));
         EKG_CUDA(cudaMemcpyAsync(B.k3.p, P.k3.data(), P.k3.size() * 8, cudaMemcpyHostToDevice, s));
         EKG_CUDA(cudaMemcpyAsync(B.hconst.p, P.hc, D.nlayers * sizeof(float4), cudaMemcpyHostToDevice, s));
         if (P.nmove > 0) {
             const size_t bt = (size_t)P.rows * D.apad * 4;
             if (B.Bt.n < bt) B.Bt.alloc(bt);
-            const size_t pb = (size_t)P.nchunks * P.rows * D.steps;
+            const size_t pb = (size_t)std::max(1, P.nitems) * P.rows * 128;
             if (B.partial.n < pb) B.partial.alloc(pb);
-            B.ck0.alloc(P.nchunks);
-            B.ck1.alloc(P.nchunks);
-            B.cl.alloc(P.nchunks);
-            EKG_CUDA(cudaMemcpyAsync(B.ck0.p, P.ck0.data(), P.nchunks * 4, cudaMemcpyHostToDevice, s));
-            EKG_CUDA(cudaMemcpyAsync(B.ck1.p, P.ck1.data(), P.nchunks * 4, cudaMemcpyHostToDevice, s));
-            EKG_CUDA(cudaMemcpyAsync(B.cl.p, P.cl.data(), P.nchunks * 4, cudaMemcpyHostToDevice, s));
+            const size_t p1 = (size_t)(D.apad / 64) * B.max_ent * P.rows_used;
+            if (B.P1.n < p1) B.P1.alloc(p1);
+            B.work.alloc(1);
+            const size_t ub = (size_t)P.rows_used * D.nlayers * B.max_ent;
+            if (B.U.n < ub) {
+                B.U.alloc(ub);
+                B.Up.alloc(ub * band_u_parts());
+            }
+            if (B.items.n < (size_t)std::max(1, P.nitems)) B.items.alloc(std::max(1, P.nitems));
+            B.tc0.alloc(B.ntt);
+            B.tc1.alloc(B.ntt);
+            if (B.k5l.n < P.k5l.size()) B.k5l.alloc(P.k5l.size());
+            if (B.lrel.n < P.lrel.size()) B.lrel.alloc(P.lrel.size());
+            if (P.nitems > 0)
+                EKG_CUDA(cudaMemcpyAsync(B.items.p, P.items.data(), P.nitems * sizeof(int4), cudaMemcpyHostToDevice, s));
+            EKG_CUDA(cudaMemcpyAsync(B.tc0.p, P.tc0.data(), B.ntt * 4, cudaMemcpyHostToDevice, s));
+            EKG_CUDA(cudaMemcpyAsync(B.tc1.p, P.tc1.data(), B.ntt * 4, cudaMemcpyHostToDevice, s));
+            EKG_CUDA(cudaMemcpyAsync(B.k5l.p, P.k5l.data(), P.k5l.size() * 4, cudaMemcpyHostToDevice, s));
+            EKG_CUDA(cudaMemcpyAsync(B.lrel.p, P.lrel.data(), P.lrel.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
         }
     } else {
         ensure_general_capacity(h, n_sims);
@@ -657,8 +837,38 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
         launches += nmove < (int)L;
         if (nmove > 0) {
             if (P.rows_used < P.rows) EKG_CUDA(cudaMemsetAsync(B.Bt.p, 0, (size_t)P.rows * D.apad * 4, s));
-            launch_batch_lead_field(s, D, P.two_bases, E.layer_k.p, E.leads.p, nmove, n_sims, B.Bt.p);
-            ++launches;
+            BandArgs U;
+            U.n_sims = n_sims;
+            U.nmove = nmove;
+            U.nl = D.nlayers;
+            U.ntt = B.ntt;
+            U.steps = D.steps;
+            U.rows = P.rows;
+            U.rows_used = P.rows_used;
+            U.nleads = (int)L;
+            U.max_ent = B.max_ent;
+            U.c8s = B.c8s.p;
+            U.nent = B.nent.p;
+            U.esplit8 = B.esplit8.p;
+            U.ls0 = B.ls0.p;
+            U.ls1 = B.ls1.p;
+            U.ent = B.ent.p;
+            U.tc0 = B.tc0.p;
+            U.tc1 = B.tc1.p;
+            U.goff = B.goff.p;
+            U.gtab = B.gtab.p;
+            U.E = B.E.p;
+            U.F = E.F.p;
+            U.k3 = B.k3.p;
+            U.partial = B.partial.p;
+            U.P1 = B.P1.p;
+            U.U = B.U.p;
+            U.Up = B.Up.p;
+            U.ecg = E.ecg.p;
+            launch_batch_lead_field(s, D, P.two_bases, B.k5l.p, B.hconst.p, B.lrel.p, nmove, n_sims, U, B.Bt.p,
+                                    B.work.p, h->sm_count);
+            launch_band_u(s, U);
+            launches += 2;
             if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[1], s));
             BatchArgs A;
             A.steps = D.steps;
@@ -668,13 +878,11 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             A.nmove = nmove;
             A.n_sims = n_sims;
             A.ntiles = P.ntiles;
-            A.nchunks = P.nchunks;
+            A.nitems = P.nitems;
             A.two_bases = P.two_bases;
             A.t_hilo = D.t_hilo.p;
             A.at_hilo = D.at_hilo.p;
-            A.ck0 = B.ck0.p;
-            A.ck1 = B.ck1.p;
-            A.cl = B.cl.p;
+            A.items = B.items.p;
             A.hconst = B.hconst.p;
             A.k3 = B.k3.p;
             A.F = E.F.p;
@@ -682,10 +890,10 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             A.partial = B.partial.p;
             A.err = E.err.p;
             launch_batch_gemm(s, A);
+            launches += P.nitems > 0;
             if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[2], s));
-            launch_reduce_rows(s, D.steps, P.rows_used, P.rows, P.nchunks, nmove, (int)L, B.partial.p, nullptr,
-                               E.ecg.p);
-            launches += 2;
+            launch_reduce_band(s, U);
+            ++launches;
         } else if (tm && tm->on) {
             EKG_CUDA(cudaEventRecord(tm->ev[1], s));
             EKG_CUDA(cudaEventRecord(tm->ev[2], s));
