@@ -44,6 +44,7 @@ using namespace ptx;
 namespace {
 
 constexpr int BM = 128, BKT = 64, BTHREADS = 256;
+constexpr int LF_THREADS = 128;  // threads of the moved-lead operand kernel
 
 __device__ __forceinline__ float ex2a(float x) {
     float y;
@@ -163,35 +164,36 @@ __global__ void k_static_combine(int steps, int nleads, int nl, int J, int Jb, i
 // is closer to the exact sum than the FP32 evaluation of the eight cancelling neighbour terms.
 struct InteriorField {
     float a0 = 0, a1 = 0, b0 = 0, b1 = 0, b2 = 0;  // rho^5 (a1 T4 + a0) + rho^7 (b2 T6 + b1 T4 + b0)
-    uint32_t mask = 0;                              // full neighbour mask (0: never)
 };
-constexpr float INTERIOR_S_MIN = 400.f;  // |m|^2
+// Flag bits above the neighbour mask in vox_pos.w (the mask uses at most 26 bits).
+constexpr uint32_t VOX_INTERIOR = 1u << 31;  // every neighbour present, out-neighbour offsets sum to 0
+constexpr uint32_t VOX_AP_END = 1u << 30;    // last voxel of its AP (voxels are grouped by AP)
 
-// every neighbour present and the out-neighbour offsets summing to zero (the out term vanishes)
-__device__ __forceinline__ bool interior_ok(const InteriorField &ic, uint32_t mi, float4 out, float s0) {
-    const uint32_t am = __activemask();
-    return ic.mask != 0u && mi == ic.mask && out.x == 0.f && out.y == 0.f && out.z == 0.f &&
-           __all_sync(am, s0 >= INTERIOR_S_MIN);
+// closed form of the interior field for m = r - v (used for |m|^2 >= INTERIOR_S_MIN)
+constexpr float INTERIOR_S_MIN = 400.f;
+__device__ __forceinline__ float sq3(float4 pos, float4 r) {
+    const float mz = r.x - pos.x, my = r.y - pos.y, mx = r.z - pos.z;
+    return fmaf(mz, mz, fmaf(my, my, mx * mx));
 }
-__device__ __forceinline__ float interior_w(const InteriorField &ic, float mz, float my, float mx, float s0) {
-    const float rho = rsqa(s0);
-    const float uz = mz * rho, uy = my * rho, ux = mx * rho;
-    const float z2 = uz * uz, y2 = uy * uy, x2 = ux * ux;
+__device__ __forceinline__ float interior_w(const InteriorField &ic, float4 pos, float4 r, float s0) {
+    const float mz = r.x - pos.x, my = r.y - pos.y, mx = r.z - pos.z;
+    const float z2 = mz * mz, y2 = my * my, x2 = mx * mx;
     const float z4 = z2 * z2, y4 = y2 * y2, x4 = x2 * x2;
-    const float T4 = z4 + y4 + x4;
-    const float T6 = fmaf(z4, z2, fmaf(y4, y2, x4 * x2));
-    const float r2 = rho * rho, r5 = r2 * r2 * rho, r7 = r5 * r2;
-    return fmaf(r5, fmaf(ic.a1, T4, ic.a0), r7 * fmaf(ic.b2, T6, fmaf(ic.b1, T4, ic.b0)));
+    const float S4 = z4 + y4 + x4;
+    const float S6 = fmaf(z4, z2, fmaf(y4, y2, x4 * x2));
+    const float rho = rsqa(s0);
+    const float i2 = rho * rho, i4 = i2 * i2;
+    const float T4 = S4 * i4, T6 = S6 * (i4 * i2);
+    const float inner = fmaf(ic.b2, T6, fmaf(ic.b1, T4, ic.b0));
+    return (rho * i4) * fmaf(i2, inner, fmaf(ic.a1, T4, ic.a0));
 }
 
 // w(v) for one lead position r relative to the same centre as the voxel positions, general
-// neighbourhood.
-__device__ __forceinline__ float voxel_w_general(float4 pos, float4 out, float4 r, int nnb, const float *s_d,
-                                                 const InteriorField &ic) {
+// neighbourhood, every term evaluated.
+__device__ __forceinline__ float voxel_w_general(float4 pos, uint32_t mi, float4 out, float4 r, int nnb,
+                                                 const float *s_d) {
     const float mz = r.x - pos.x, my = r.y - pos.y, mx = r.z - pos.z;
-    const uint32_t mi = __float_as_uint(pos.w);
     const float s0 = fmaf(mz, mz, fmaf(my, my, mx * mx));
-    if (interior_ok(ic, mi, out, s0)) return interior_w(ic, mz, my, mx, s0);
     float w = 0.f;
     for (int n = 0; n < nnb; ++n) {
         if (!(mi & (1u << n))) continue;
@@ -209,14 +211,12 @@ __device__ __forceinline__ float voxel_w_general(float4 pos, float4 out, float4 
 
 // Same for the 8 body diagonals ("3D4", creation order (-1,-1,-1) ... (1,1,1), |d|^2 = 3): with
 // p = my + mx, q = my - mx, zm = -mz - 3, zp = mz - 3 the eight y = m.d - 3 are
-// zm-p, zm-q, zm+q, zm+p, zp-p, zp-q, zp+q, zp+p, and |m - d|^2 = (|m|^2 - 3) - 2 y.  Voxels
-// missing a neighbour are masked, the out-neighbour term is skipped where there is none (all
-// tests on the voxel are uniform over the warp).
-__device__ __forceinline__ float voxel_w_diag(float4 pos, float4 out, float4 r, const InteriorField &ic) {
+// zm-p, zm-q, zm+q, zm+p, zp-p, zp-q, zp+q, zp+p, and |m - d|^2 = (|m|^2 - 3) - 2 y.  Missing
+// neighbours are masked, the out-neighbour term is skipped where there is none (every test on
+// the voxel is uniform over the warp).
+__device__ __forceinline__ float voxel_w_diag(float4 pos, uint32_t mi, float4 out, float4 r) {
     const float mz = r.x - pos.x, my = r.y - pos.y, mx = r.z - pos.z;
-    const uint32_t mi = __float_as_uint(pos.w);
     const float s0 = fmaf(mz, mz, fmaf(my, my, mx * mx));
-    if (interior_ok(ic, mi, out, s0)) return interior_w(ic, mz, my, mx, s0);
     const float b = s0 - 3.f;
     const float p = my + mx, q = my - mx;
     const float zm = -mz - 3.f, zp = mz - 3.f;
@@ -234,31 +234,40 @@ __device__ __forceinline__ float voxel_w_diag(float4 pos, float4 out, float4 r, 
     return w;
 }
 
-// W'[a] = exp(k5 at_a) sum_{v in a} w(v) for the 8 APs of chunk a0 and NP lead positions, into
-// s_w[q][j][tid] (shared memory, so the AP loop stays rolled and the code small).
+// sum_{v in a} w(v) for the 8 APs of chunk a0 and NP lead positions, into s_w[q][j][tid]: one flat
+// loop over the chunk's voxels (grouped by AP, the last one of each AP flagged); APs without
+// voxels (padding, at the end of a layer) get 0.  Interior voxels use the closed form where the
+// lane's leads are at least 20 cells away (lanes normally agree), the rest the exact sum.
 template <bool DIAG, int NP>
 __device__ __forceinline__ void chunk_w(int64_t a0, const int64_t *__restrict__ a_vox_begin,
-                                        const float2 *__restrict__ at_hilo, const float4 *__restrict__ vox_pos,
-                                        const float4 *__restrict__ vox_out, float4 r0, float4 r1, int nnb,
-                                        const float *s_d, const InteriorField &ic, float k5,
-                                        float (*s_w)[8][128], int tid) {
-    int v = (int)a_vox_begin[a0];
-#pragma unroll 1
-    for (int j = 0; j < 8; ++j) {
-        const int ve = (int)a_vox_begin[a0 + j + 1];
-        float acc[NP];
-#pragma unroll
-        for (int q = 0; q < NP; ++q) acc[q] = 0.f;
-        for (; v < ve; ++v) {
-            const float4 pos = vox_pos[v], out = vox_out[v];
-            acc[0] += DIAG ? voxel_w_diag(pos, out, r0, ic) : voxel_w_general(pos, out, r0, nnb, s_d, ic);
-            if (NP == 2)
-                acc[NP - 1] += DIAG ? voxel_w_diag(pos, out, r1, ic) : voxel_w_general(pos, out, r1, nnb, s_d, ic);
+                                        const float4 *__restrict__ vox_pos, const float4 *__restrict__ vox_out,
+                                        float4 r0, float4 r1, int nnb, const float *s_d, const InteriorField &ic,
+                                        float (*s_w)[8][LF_THREADS], int tid) {
+    const int vb = (int)a_vox_begin[a0], vend = (int)a_vox_begin[a0 + 8];
+    float acc0 = 0.f, acc1 = 0.f;
+    int j = 0;
+    for (int v = vb; v < vend; ++v) {
+        const float4 pos = vox_pos[v];
+        const uint32_t mi = __float_as_uint(pos.w);
+        const float s0 = sq3(pos, r0), s1 = NP == 2 ? sq3(pos, r1) : s0;
+        if ((mi & VOX_INTERIOR) && s0 >= INTERIOR_S_MIN && s1 >= INTERIOR_S_MIN) {
+            acc0 += interior_w(ic, pos, r0, s0);
+            if (NP == 2) acc1 += interior_w(ic, pos, r1, s1);
+        } else {
+            const float4 out = vox_out[v];
+            acc0 += DIAG ? voxel_w_diag(pos, mi, out, r0) : voxel_w_general(pos, mi, out, r0, nnb, s_d);
+            if (NP == 2) acc1 += DIAG ? voxel_w_diag(pos, mi, out, r1) : voxel_w_general(pos, mi, out, r1, nnb, s_d);
         }
-        const float2 at = at_hilo[a0 + j];
-        const float e = isinf(at.x) ? 0.f : ex2a(fmaf(k5, at.x, k5 * at.y));
-#pragma unroll
-        for (int q = 0; q < NP; ++q) s_w[q][j][tid] = acc[q] * e;
+        if (mi & VOX_AP_END) {
+            s_w[0][j][tid] = acc0;
+            if (NP == 2) s_w[1][j][tid] = acc1;
+            acc0 = acc1 = 0.f;
+            ++j;
+        }
+    }
+    for (; j < 8; ++j) {
+        s_w[0][j][tid] = 0.f;
+        if (NP == 2) s_w[1][j][tid] = 0.f;
     }
 }
 
@@ -274,9 +283,8 @@ __device__ __forceinline__ void chunk_w(int64_t a0, const int64_t *__restrict__ 
 // lrel: [S][nmove] lead positions relative to the voxel centre (FP32, differences taken in FP64
 // on the host); k5l: [S][nl] k5 * log2(e).
 constexpr int MAXE = 8;
-constexpr int LF_THREADS = 128;
 template <int N, bool DIAG>
-__global__ void __launch_bounds__(LF_THREADS) k_batch_lead_field(
+__global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
     int nkt, int nsg, int *__restrict__ work, InteriorField ic, const int64_t *__restrict__ a_vox_begin,
     const float4 *__restrict__ vox_pos, const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs,
     const float2 *__restrict__ at_hilo, const int32_t *__restrict__ a_layer, const float *__restrict__ k5l, int nl,
@@ -320,30 +328,28 @@ __global__ void __launch_bounds__(LF_THREADS) k_batch_lead_field(
             for (int kc = 0; kc < BKT / 8; ++kc) {
                 const int c8 = kt * (BKT / 8) + kc;
                 const int64_t a0 = (int64_t)c8 * 8;
-                if (np == 2)
-                    chunk_w<DIAG, 2>(a0, a_vox_begin, at_hilo, vox_pos, vox_out, r0, r1, nnb, s_d, ic, k5, s_w, tid);
-                else
-                    chunk_w<DIAG, 1>(a0, a_vox_begin, at_hilo, vox_pos, vox_out, r0, r1, nnb, s_d, ic, k5, s_w, tid);
-                float2 ref = make_float2(0.f, 0.f);
-                for (int j = 7; j >= 0; --j) {
-                    const float2 v = at_hilo[a0 + j];
-                    if (!isinf(v.x)) {
-                        ref = v;
-                        break;
-                    }
-                }
-                float ez[8];
+                if (np == 2) chunk_w<DIAG, 2>(a0, a_vox_begin, vox_pos, vox_out, r0, r1, nnb, s_d, ic, s_w, tid);
+                else chunk_w<DIAG, 1>(a0, a_vox_begin, vox_pos, vox_out, r0, r1, nnb, s_d, ic, s_w, tid);
+                float2 at[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) at[j] = at_hilo[a0 + j];
+                float2 ref = at[0];
+#pragma unroll
+                for (int j = 1; j < 8; ++j)
+                    if (!isinf(at[j].x)) ref = at[j];
+                float e[8], ez[8];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
-                    const float2 v = at_hilo[a0 + j];
-                    ez[j] = isinf(v.x) ? 0.f : ex2a(-k4 * ((ref.x - v.x) + (ref.y - v.y)));
+                    const bool pad = isinf(at[j].x);
+                    e[j] = pad ? 0.f : ex2a(fmaf(k5, at[j].x, k5 * at[j].y));
+                    ez[j] = pad ? 0.f : ex2a(-k4 * ((ref.x - at[j].x) + (ref.y - at[j].y)));
                 }
 #pragma unroll
                 for (int q = 0; q < 2; ++q) {
                     if (q >= np) break;
                     float wv[8];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) wv[j] = s_w[q][j][tid];
+                    for (int j = 0; j < 8; ++j) wv[j] = s_w[q][j][tid] * e[j];
                     uint4 hv, lv;
                     split2(wv[0], wv[1], hv.x, lv.x);
                     split2(wv[2], wv[3], hv.y, lv.y);
@@ -747,14 +753,11 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, c
     const int nkt = (int)(h.apad / BKT);
     const bool diag = h.nhood == EKG_NHOOD_3D4;
     InteriorField ic;
-    if (h.interior_mask) {
-        ic.a0 = h.interior_c[0];
-        ic.a1 = h.interior_c[1];
-        ic.b0 = h.interior_c[2];
-        ic.b1 = h.interior_c[3];
-        ic.b2 = h.interior_c[4];
-        ic.mask = h.interior_mask;
-    }
+    ic.a0 = h.interior_c[0];
+    ic.a1 = h.interior_c[1];
+    ic.b0 = h.interior_c[2];
+    ic.b1 = h.interior_c[3];
+    ic.b2 = h.interior_c[4];
     EKG_CUDA(cudaMemsetAsync(work, 0, sizeof(int), s));
 #define EKG_LF(NN, DG)                                                                                            \
     do {                                                                                                          \

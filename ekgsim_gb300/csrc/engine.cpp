@@ -323,6 +323,11 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
                                 ox += D.nb_dif[3 * q + 2];
                             }
                         uint32_t mbits = mi;
+                        // flags for the moved-lead operand kernel (batch.cu): interior voxel (closed-form
+                        // field), last voxel of its AP
+                        if (D.interior_mask && mi == D.interior_mask && oz == 0 && oy == 0 && ox == 0)
+                            mbits |= 1u << 31;
+                        if (i + 1 == gstart[gg + 1]) mbits |= 1u << 30;
                         float mf;
                         std::memcpy(&mf, &mbits, 4);
                         // bordered coordinates (+1, simlib/simulator.cpp:458-463) relative to the centre
