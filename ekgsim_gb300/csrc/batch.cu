@@ -117,7 +117,7 @@ __global__ void k_reduce_layers(int steps, int rows, int nl, const int32_t *__re
 // Static leads: ecg[s][l][t] = sum_L F[s][L][t] sum_j coef[s][L][j] ((1-k3) Q1 + k3 Q2)[L][l*J+j][t],
 // the Taylor sum per layer in FP32 (the basis is stored in FP32), the sum over layers in FP64.
 __global__ void k_static_combine(int steps, int nleads, int nl, int J, int Jb, int nmove, int n_sims,
-                                 const double *__restrict__ F, const float *__restrict__ coef,
+                                 const float *__restrict__ F, const float *__restrict__ coef,
                                  const double *__restrict__ k3, const float *__restrict__ Q1,
                                  const float *__restrict__ Q2, double *__restrict__ ecg) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -134,7 +134,7 @@ __global__ void k_static_combine(int steps, int nleads, int nl, int J, int Jb, i
             v1 = fmaf(c[j], Q1[q0 + (size_t)j * steps], v1);
             v2 = fmaf(c[j], Q2[q0 + (size_t)j * steps], v2);
         }
-        acc += F[((size_t)s * nl + L) * steps + t] * (double)fmaf(kk, v2 - v1, v1);
+        acc += (double)(F[((size_t)s * nl + L) * steps + t] * fmaf(kk, v2 - v1, v1));
     }
     ecg[((size_t)s * nleads + l) * steps + t] = acc;
 }
@@ -385,45 +385,53 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
 }
 
 // Steady sums per (row', layer, entry): U[row'][L][e] = sum over the layer's K tiles [ls0, ls1)
-// below the entry's prefix end of P1[kt][e][row'] (U0, U1), in FP64.  Two passes in a fixed
-// order: k_band_u sums BU_PARTS consecutive parts of the K range per (part, layer) block (threads
-// over rows), k_band_u2 adds the parts.  Up: [parts][rows][nl][max_ent].
-constexpr int BU_PARTS = 64;
+// below the entry's prefix end of P1[kt][e][row'] (U0, U1).  Two passes in a fixed order:
+// k_band_u sums BU_PARTS consecutive parts of the K range in FP32 (a few tiles each) per (part,
+// layer) block, threads over rows; k_band_u2 adds the parts in FP64, eight warps per 32 outputs.
+// Up: [parts][rows][nl][max_ent]; U stored in FP32.
+constexpr int BU_PARTS = 128;
 __global__ void __launch_bounds__(256) k_band_u(int rows_used, int nl, int max_ent, const int32_t *__restrict__ nent,
                                                 const int32_t *__restrict__ esplit8, const int32_t *__restrict__ ls0,
                                                 const int32_t *__restrict__ ls1, const float2 *__restrict__ P1,
-                                                double2 *__restrict__ Up) {
+                                                float2 *__restrict__ Up) {
     const int p = blockIdx.x, L = blockIdx.y;
     const int ne = nent[L], n = ls1[L] - ls0[L];
     const int g0 = ls0[L] + (int)((int64_t)n * p / BU_PARTS), g1 = ls0[L] + (int)((int64_t)n * (p + 1) / BU_PARTS);
     for (int rr = threadIdx.x; rr < rows_used; rr += blockDim.x)
         for (int e = 0; e < ne; ++e) {
             const int ge = min(g1, (esplit8[L * MAXE + e] + 7) / 8);
-            double a = 0.0, b = 0.0;
-#pragma unroll 4
+            float a = 0.f, b = 0.f;
+#pragma unroll 8
             for (int g = g0; g < ge; ++g) {
                 const float2 v = P1[((size_t)g * max_ent + e) * rows_used + rr];
-                a += (double)v.x;
-                b += (double)v.y;
+                a += v.x;
+                b += v.y;
             }
-            Up[(((size_t)p * rows_used + rr) * nl + L) * max_ent + e] = make_double2(a, b);
+            Up[(((size_t)p * rows_used + rr) * nl + L) * max_ent + e] = make_float2(a, b);
         }
 }
 
-__global__ void k_band_u2(int rows_used, int nl, int max_ent, const int32_t *__restrict__ nent,
-                          const double2 *__restrict__ Up, double2 *__restrict__ U) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= (int64_t)rows_used * nl * max_ent) return;
-    const int e = (int)(i % max_ent), L = (int)((i / max_ent) % nl);
-    if (e >= nent[L]) return;
-    const size_t stride = (size_t)rows_used * nl * max_ent;
+__global__ void __launch_bounds__(256) k_band_u2(int64_t n_out, const float2 *__restrict__ Up, float2 *__restrict__ U) {
+    __shared__ double2 red[8][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t i = blockIdx.x * 32 + lane;
     double a = 0.0, b = 0.0;
-    for (int p = 0; p < BU_PARTS; ++p) {
-        const double2 v = Up[p * stride + i];
-        a += v.x;
-        b += v.y;
+    if (i < n_out)
+#pragma unroll 4
+        for (int p = w; p < BU_PARTS; p += 8) {
+            const float2 v = Up[p * n_out + i];
+            a += (double)v.x;
+            b += (double)v.y;
+        }
+    red[w][lane] = make_double2(a, b);
+    __syncthreads();
+    if (w == 0 && i < n_out) {
+        for (int k = 1; k < 8; ++k) {
+            a += red[k][lane].x;
+            b += red[k][lane].y;
+        }
+        U[i] = make_float2((float)a, (float)b);
     }
-    U[i] = make_double2(a, b);
 }
 
 // ------------------------------------------------------------------ batch GEMM
@@ -453,13 +461,13 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 }
 
 // grid (work items, N tiles).  Item c = (t tile, first stage, end stage, layer): the band of one
-// 128-step tile inside one layer, in 32-AP stages.  partial: [items][rows][128].
+// 128-step tile inside one layer, in 32-AP stages.  partial: [items][rows][128] FP32 accumulators
+// (float2 of the two bases with NB = 2).
 template <int NB, int N>
 __global__ void __launch_bounds__(WS_THREADS, 1) k_batch_umma(
     int steps, int nl, int nkt, int rows, int nmove, int n_sims, const float2 *__restrict__ t_hilo,
     const float2 *__restrict__ at_hilo, const int4 *__restrict__ items, const float4 *__restrict__ hconst,
-    const double *__restrict__ k3, const double *__restrict__ F, const uint8_t *__restrict__ Bt,
-    double *__restrict__ partial, uint32_t *__restrict__ err) {
+    const uint8_t *__restrict__ Bt, float *__restrict__ partial, uint32_t *__restrict__ err) {
     extern __shared__ uint8_t smem_raw[];
     BatchSmem<NB, N> &S =
         *reinterpret_cast<BatchSmem<NB, N> *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -593,22 +601,16 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_batch_umma(
             ++drained;
         }
         if (ok && nk > 0) {
+            // raw accumulators (both bases with NB = 2); the reduction applies F_L(t) and k3
             const int t = t0 + 32 * q + lane;
             if (t < steps) {
 #pragma unroll
                 for (int jj = 0; jj < HALF; ++jj) {
                     const int r = nt * N + ch * HALF + jj;
-                    const int s = r / nmove;
-                    if (s >= n_sims) continue;
-                    const double f = F[((size_t)s * nl + L) * steps + t];
-                    double v;
-                    if (NB == 2) {
-                        const double kk = k3[(size_t)s * nl + L];
-                        v = ((1.0 - kk) * (double)acc[jj] + kk * (double)acc[HALF + jj]) * f;
-                    } else {
-                        v = (double)acc[jj] * f;
-                    }
-                    partial[((size_t)c * rows + r) * BM + (t - t0)] = v;
+                    if (r / nmove >= n_sims) continue;
+                    const size_t o = ((size_t)c * rows + r) * BM + (t - t0);
+                    if (NB == 2) reinterpret_cast<float2 *>(partial)[o] = make_float2(acc[jj], acc[HALF + jj]);
+                    else partial[o] = acc[jj];
                 }
             }
         }
@@ -669,39 +671,47 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_batch_umma(
     if (warp == 0) tmem_dealloc(tmem, TCOLS);
 }
 
-// ecg[s][l][t] (l < nmove) = sum over the band items c of t's tile of partial[c][row][t - t0]
-//   + sum_L F[s][L][t] ((1 - k3) E[L][t] U1 + k3 U0),  (U0, U1) = U[row'][L][ent[L][j]],
-// E[L][t] = exp(-k4_L (t - t0 of the entry)), row = s * nmove + l, row' = l * S + s, j = t / 128;
-// block per (row, 32 steps), warps split the items, fixed order.
+// ecg[s][l][t] (l < nmove) = sum_L F[s][L][t] [(1 - k3) (Y1_L + E[L][t] U1) + k3 (Y2_L + U0)]
+// (with one basis the GEMM already mixed k3: Y_L + (1 - k3) E U1 + k3 U0), Y_L = sum over the band
+// items of (t's tile, L) of the raw accumulators, (U0, U1) = U[row'][L][ent[L][j]], row = s * nmove
+// + l, row' = l * S + s, j = t / 128.  Per layer in FP32, over layers in FP64; thread per (row, t).
 __global__ void k_reduce_band(int steps, int rows, int nmove, int n_sims, int nleads, int nl, int ntt, int max_ent,
-                              const int32_t *__restrict__ tc0, const int32_t *__restrict__ tc1,
-                              const int32_t *__restrict__ ent, const double *__restrict__ partial,
-                              const double2 *__restrict__ U, const double *__restrict__ E,
-                              const double *__restrict__ F, const double *__restrict__ k3, double *__restrict__ ecg) {
-    __shared__ double red[8][33];
-    const int tt = blockIdx.x * 32 + (threadIdx.x & 31);
-    const int w = threadIdx.x >> 5;
+                              int nb, const int32_t *__restrict__ ti0, const int32_t *__restrict__ ti1,
+                              const int32_t *__restrict__ ent, const float *__restrict__ partial,
+                              const float2 *__restrict__ U, const float *__restrict__ E, const float *__restrict__ F,
+                              const double *__restrict__ k3, double *__restrict__ ecg) {
+    const int tt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tt >= steps) return;
     const int r = blockIdx.y;
     const int s = r / nmove, l = r % nmove;
-    const int j = (blockIdx.x * 32) / BM, tl = tt - j * BM;
-    double acc = 0.0;
-    if (tt < steps)
-        for (int c = tc0[j] + w; c < tc1[j]; c += 8) acc += partial[((size_t)c * rows + r) * BM + tl];
-    red[w][threadIdx.x & 31] = acc;
-    __syncthreads();
-    if (w == 0 && tt < steps) {
-        double v = 0.0;
-        for (int i = 0; i < 8; ++i) v += red[i][threadIdx.x];
-        const size_t rp = (size_t)l * n_sims + s;
-        for (int L = 0; L < nl; ++L) {
-            const int e = ent[L * ntt + j];
-            if (e < 0) continue;
-            const double kk = k3[(size_t)s * nl + L];
-            const double2 u = U[(rp * nl + L) * max_ent + e];
-            v += F[((size_t)s * nl + L) * steps + tt] * ((1.0 - kk) * E[(size_t)L * steps + tt] * u.y + kk * u.x);
+    const int j = tt / BM, tl = tt - j * BM;
+    const size_t rp = (size_t)l * n_sims + s;
+    double v = 0.0;
+    for (int L = 0; L < nl; ++L) {
+        const float kk = (float)k3[(size_t)s * nl + L];
+        float y1 = 0.f, y2 = 0.f;
+        const int c0 = ti0[j * nl + L], c1 = ti1[j * nl + L];
+        if (nb == 2) {
+            for (int c = c0; c < c1; ++c) {
+                const float2 p = reinterpret_cast<const float2 *>(partial)[((size_t)c * rows + r) * BM + tl];
+                y1 += p.x;
+                y2 += p.y;
+            }
+        } else {
+            for (int c = c0; c < c1; ++c) y1 += partial[((size_t)c * rows + r) * BM + tl];
         }
-        ecg[((size_t)s * nleads + l) * steps + tt] = v;
+        const int e = ent[L * ntt + j];
+        float st1 = 0.f, st0 = 0.f;
+        if (e >= 0) {
+            const float2 u = U[(rp * nl + L) * max_ent + e];
+            st1 = E[(size_t)L * steps + tt] * u.y;
+            st0 = u.x;
+        }
+        const float x = nb == 2 ? fmaf(kk, (y2 + st0) - (y1 + st1), y1 + st1)
+                                : fmaf(kk, st0 - st1, y1 + st1);
+        v += (double)(F[((size_t)s * nl + L) * steps + tt] * x);
     }
+    ecg[((size_t)s * nleads + l) * steps + tt] = v;
 }
 
 template <int NB, int N>
@@ -714,8 +724,7 @@ void launch_gemm(cudaStream_t st, const BatchArgs &A) {
     }
     dim3 grid((unsigned)A.nitems, (unsigned)A.ntiles);
     k_batch_umma<NB, N><<<grid, WS_THREADS, smem, st>>>(A.steps, A.nl, A.nkt, A.rows, A.nmove, A.n_sims, A.t_hilo,
-                                                        A.at_hilo, A.items, A.hconst, A.k3, A.F, A.Bt, A.partial,
-                                                        A.err);
+                                                        A.at_hilo, A.items, A.hconst, A.Bt, A.partial, A.err);
     EKG_CUDA(cudaGetLastError());
 }
 
@@ -737,7 +746,7 @@ void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int
     EKG_CUDA(cudaGetLastError());
 }
 
-void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const double *F,
+void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const float *F,
                            const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg) {
     if (nmove >= h.nleads) return;
     dim3 grid((unsigned)((h.steps + 127) / 128), (unsigned)(h.nleads - nmove), (unsigned)n_sims);
@@ -794,14 +803,14 @@ void launch_band_u(cudaStream_t s, const BandArgs &A) {
     k_band_u<<<dim3(BU_PARTS, (unsigned)A.nl), 256, 0, s>>>(A.rows_used, A.nl, A.max_ent, A.nent, A.esplit8, A.ls0,
                                                            A.ls1, A.P1, A.Up);
     const int64_t n = (int64_t)A.rows_used * A.nl * A.max_ent;
-    k_band_u2<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A.rows_used, A.nl, A.max_ent, A.nent, A.Up, A.U);
+    k_band_u2<<<(unsigned)((n + 31) / 32), 256, 0, s>>>(n, A.Up, A.U);
     EKG_CUDA(cudaGetLastError());
 }
 
 void launch_reduce_band(cudaStream_t s, const BandArgs &A) {
-    dim3 grid((unsigned)((A.steps + 31) / 32), (unsigned)A.rows_used);
-    k_reduce_band<<<grid, 256, 0, s>>>(A.steps, A.rows, A.nmove, A.n_sims, A.nleads, A.nl, A.ntt, A.max_ent, A.tc0,
-                                       A.tc1, A.ent, A.partial, A.U, A.E, A.F, A.k3, A.ecg);
+    dim3 grid((unsigned)((A.steps + 127) / 128), (unsigned)A.rows_used);
+    k_reduce_band<<<grid, 128, 0, s>>>(A.steps, A.rows, A.nmove, A.n_sims, A.nleads, A.nl, A.ntt, A.max_ent, A.nb,
+                                       A.ti0, A.ti1, A.ent, A.partial, A.U, A.E, A.F, A.k3, A.ecg);
     EKG_CUDA(cudaGetLastError());
 }
 

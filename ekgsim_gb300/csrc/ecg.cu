@@ -107,7 +107,8 @@ __global__ void k_lead_field(int64_t apad, const int64_t *__restrict__ a_vox_beg
 //     ln(1 + e^u) = log1p(exp(u)) (u + log1p(exp(-u)) for u > 0),  R = -expm1(-(k6/k7) ln(1 + e^u)).
 // layer_k: [S][nl][9].
 __global__ void k_layer_factors(int nl, int steps, const double *__restrict__ t, const double *__restrict__ layer_k,
-                                int n_sims, double *__restrict__ F, float *__restrict__ layer_c) {
+                                int n_sims, double *__restrict__ F, float *__restrict__ Ff,
+                                float *__restrict__ layer_c) {
     const int64_t sl = blockIdx.x;  // sim * nl + layer
     const double *k = layer_k + sl * 9;
     __shared__ double c;
@@ -125,7 +126,9 @@ __global__ void k_layer_factors(int nl, int steps, const double *__restrict__ t,
         const float sp = u > 0.f ? u + log1pf(expf(-u)) : log1pf(expf(u));
         const float R = -expm1f(-r * sp);
         const float e5 = expf((float)(-k[5] * tt));
-        F[sl * steps + step] = k[2] * (double)e5 * (double)R;
+        const double f = k[2] * (double)e5 * (double)R;
+        F[sl * steps + step] = f;
+        Ff[sl * steps + step] = (float)f;
     }
 }
 
@@ -356,9 +359,9 @@ void launch_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads,
 }
 
 void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_layer_k, int n_sims, double *d_F,
-                          float *d_layer_c) {
+                          float *d_Ff, float *d_layer_c) {
     k_layer_factors<<<(unsigned)((int64_t)n_sims * h.nlayers), 128, 0, s>>>(h.nlayers, h.steps, h.t.p, d_layer_k,
-                                                                            n_sims, d_F, d_layer_c);
+                                                                            n_sims, d_F, d_Ff, d_layer_c);
     EKG_CUDA(cudaGetLastError());
 }
 

@@ -49,15 +49,16 @@ struct BatchState {
     DBuf<int64_t> goff;                    // [nl][8] offsets into gtab
     DBuf<float> gtab;                      // exp(-k4 (t0_e - at_ref[c8])) for the steady chunks of entry e
     DBuf<int32_t> ent;                     // [nl][ntt] entry of each tile (-1: layer without APs)
-    DBuf<double> E;                        // [nl][steps] exp(-k4 (t - t0 of the tile's entry))
+    DBuf<float> E;                         // [nl][steps] exp(-k4 (t - t0 of the tile's entry))
     // per batch
     DBuf<uint8_t> Bt;                      // tiled BF16 hi/lo moved-lead weights
     DBuf<float2> P1;                       // [K tiles][max_ent][rows] steady sums per 64-AP tile
     DBuf<int> work;                        // work counter of the operand kernel
-    DBuf<double2> U, Up;                   // [rows][nl][max_ent] steady sums (U0, U1), per K part
-    DBuf<double> partial;                  // [items][rows][128]
+    DBuf<float2> U, Up;                    // [rows][nl][max_ent] steady sums (U0, U1), per K part
+    DBuf<float> partial;                   // [items][rows][128] raw accumulators (x2 with two bases)
     DBuf<int4> items;                      // GEMM work items
     DBuf<int32_t> tc0, tc1;                // item range of each tile
+    DBuf<int32_t> ti0, ti1;                // [ntt][nl] item range of each (tile, layer)
     DBuf<float> k5l;                       // [S][nl] k5 log2(e)
     DBuf<float4> lrel;                     // [S][nmove] moved lead positions relative to the voxel centre
     DBuf<float4> hconst;
@@ -73,6 +74,7 @@ struct PassPlan {
     std::vector<double> k3;                // [S][nl]
     std::vector<int4> items;               // band GEMM work items, grouped by tile
     std::vector<int32_t> tc0, tc1;         // [ntt] item range of each tile
+    std::vector<int32_t> ti0, ti1;         // [ntt][nl] item range of each (tile, layer)
     std::vector<float> k5l;                // [S][nl]
     std::vector<float4> lrel;              // [S][nmove]
     float4 hc[256];
@@ -82,8 +84,12 @@ struct PassPlan {
 struct ekg_heart {
     ekg_engine *eng = nullptr;
     cudaStream_t stream = nullptr;    // this heart's device passes run here
+    cudaStream_t copy_stream = nullptr;  // early device->host copies overlapping the rest of a pass
+    cudaEvent_t static_done = nullptr;   // static-lead ECG rows complete (batched form)
     uint32_t *err_host = nullptr;     // pinned copy of the kernels' error word
     ~ekg_heart() {
+        if (static_done) cudaEventDestroy(static_done);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         if (stream) cudaStreamDestroy(stream);
         if (err_host) cudaFreeHost(err_host);
     }

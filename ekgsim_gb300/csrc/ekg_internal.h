@@ -124,6 +124,7 @@ struct EvalDev {
     DBuf<double> leads;     // [S][L][3]
     DBuf<float> layer_c;    // [S][nl][4]: k1*log2e, k4*log2e, 1-k3, k3 (FP32 H constants)
     DBuf<double> F;         // [S][nl][steps]
+    DBuf<float> Ff;         // [S][nl][steps] the same in FP32 (batched form)
     DBuf<double> k0w;       // [S][L] constant k0 term
     DBuf<float> W;          // [S][L][apad] lead field for this eval's positions
     DBuf<float> Wp;         // [S][L][apad] W * exp(k5 at)
@@ -139,7 +140,7 @@ struct EvalDev {
 void launch_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads, int nleads_in, int lead_stride,
                        int n_sims, float *d_W, int w_lead_stride);
 void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_layer_k, int n_sims, double *d_F,
-                          float *d_layer_c);
+                          float *d_Ff, float *d_layer_c);
 void launch_scale_w(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
                     float *d_Wp);
 void launch_k0_term(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
@@ -168,24 +169,25 @@ struct BatchArgs {
     const float2 *t_hilo = nullptr, *at_hilo = nullptr;
     const int4 *items = nullptr;  // (t tile, first stage, end stage, layer), stages of 32 APs
     const float4 *hconst = nullptr;
-    const double *k3 = nullptr, *F = nullptr;
     const uint8_t *Bt = nullptr;
-    double *partial = nullptr;    // [items][rows][128]
+    float *partial = nullptr;     // [items][rows][128] raw accumulators (x2 with two bases)
     uint32_t *err = nullptr;
 };
 // Steady part of the moved-lead ECG and the final reduction (batch.cu k_batch_lead_field,
 // k_band_u, k_reduce_band).
 struct BandArgs {
     int n_sims = 0, nmove = 0, nl = 0, ntt = 0, steps = 0, rows = 0, rows_used = 0, nleads = 0;
-    int max_ent = 1;
+    int max_ent = 1, nb = 1;
+    const int32_t *ti0 = nullptr, *ti1 = nullptr;  // [ntt][nl] item range of (tile, layer)
     const int32_t *c8s = nullptr, *nent = nullptr, *esplit8 = nullptr, *ls0 = nullptr, *ls1 = nullptr;
     const int32_t *ent = nullptr, *tc0 = nullptr, *tc1 = nullptr;
     const int64_t *goff = nullptr;
     const float *gtab = nullptr;
-    const double *E = nullptr, *F = nullptr, *k3 = nullptr, *partial = nullptr;
+    const float *E = nullptr, *F = nullptr, *partial = nullptr;
+    const double *k3 = nullptr;
     float2 *P1 = nullptr;            // [K tiles][max_ent][rows] steady sums per 64-AP tile
-    double2 *Up = nullptr;           // [band_u_parts()][rows][nl][max_ent]
-    double2 *U = nullptr;            // [rows][nl][max_ent]
+    float2 *Up = nullptr;            // [band_u_parts()][rows][nl][max_ent]
+    float2 *U = nullptr;             // [rows][nl][max_ent]
     double *ecg = nullptr;
 };
 int batch_tile_rows(int two_bases);
@@ -193,7 +195,7 @@ void launch_taylor_w(cudaStream_t s, const HeartDev &h, const float *W0, int J, 
                      const double *scale, float *Wt);
 void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int32_t *lc0, const int32_t *lc1,
                           const double *partial, float *Q);
-void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const double *F,
+void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const float *F,
                            const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg);
 void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const float *k5l,
                              const float4 *hconst, const float4 *lrel, int nmove, int n_sims, const BandArgs &B,

@@ -426,6 +426,7 @@ void ensure_eval_capacity(ekg_heart *h, int n_sims) {
     E.leads.alloc(S * D.nleads * 3);
     E.layer_c.alloc(S * D.nlayers * 4);
     E.F.alloc(S * D.nlayers * D.steps);
+    E.Ff.alloc(S * D.nlayers * D.steps);
     E.k0w.alloc(S * D.nleads);
     E.ecg.alloc(S * D.nleads * D.steps);
     E.crit.alloc(S * std::max(1, D.nleads) * 2);
@@ -491,7 +492,7 @@ void build_band(ekg_heart *h, const std::vector<double> &key, const std::vector<
     std::vector<int32_t> ls0(nl, 0), ls1(nl, 0);
     std::vector<int64_t> goff((size_t)nl * MAXE, 0);
     std::vector<float> gtab;
-    std::vector<double> E((size_t)nl * steps, 1.0);
+    std::vector<float> E((size_t)nl * steps, 1.f);
     int max_ent = 1;
     for (int L = 0; L < nl; ++L) {
         if (la0[L] < 0) continue;
@@ -538,7 +539,7 @@ void build_band(ekg_heart *h, const std::vector<double> &key, const std::vector<
             B.band_s0[(size_t)L * ntt + j] = (int32_t)(split / 32);
             B.band_s1[(size_t)L * ntt + j] = (int32_t)(std::max(split, en[j]) / 32);
             for (int t = 128 * j; t < std::min(steps, 128 * j + 128); ++t)
-                E[(size_t)L * steps + t] = std::exp(-k4 * (h->t[t] - eref[e]));
+                E[(size_t)L * steps + t] = (float)std::exp(-k4 * (h->t[t] - eref[e]));
         }
         for (int e = 0; e < nent[L]; ++e) {
             esplit8[(size_t)L * MAXE + e] = (int32_t)(esp[e] / 8);
@@ -573,7 +574,7 @@ void build_band(ekg_heart *h, const std::vector<double> &key, const std::vector<
     EKG_CUDA(cudaMemcpyAsync(B.goff.p, goff.data(), goff.size() * 8, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(B.gtab.p, gtab.data(), gtab.size() * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(B.ent.p, ent.data(), ent.size() * 4, cudaMemcpyHostToDevice, s));
-    EKG_CUDA(cudaMemcpyAsync(B.E.p, E.data(), E.size() * 8, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(B.E.p, E.data(), E.size() * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaStreamSynchronize(s));
 }
 
@@ -748,14 +749,18 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
         }
         P.tc0.assign(ntt, 0);
         P.tc1.assign(ntt, 0);
+        P.ti0.assign((size_t)ntt * nl, 0);
+        P.ti1.assign((size_t)ntt * nl, 0);
         for (int j = 0; j < ntt; ++j) {
             P.tc0[j] = (int32_t)P.items.size();
             for (int i = 0; i < nl; ++i) {
                 const int s0 = B.band_s0[(size_t)i * ntt + j], n = B.band_s1[(size_t)i * ntt + j] - s0;
+                P.ti0[(size_t)j * nl + i] = P.ti1[(size_t)j * nl + i] = (int32_t)P.items.size();
                 if (n <= 0) continue;
                 const int nc = (int)((n + per - 1) / per);
                 for (int c = 0; c < nc; ++c)
                     P.items.push_back(make_int4(j, s0 + (int)((int64_t)n * c / nc), s0 + (int)((int64_t)n * (c + 1) / nc), i));
+                P.ti1[(size_t)j * nl + i] = (int32_t)P.items.size();
             }
             P.tc1[j] = (int32_t)P.items.size();
         }
@@ -798,7 +803,7 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
         if (P.nmove > 0) {
             const size_t bt = (size_t)P.rows * D.apad * 4;
             if (B.Bt.n < bt) B.Bt.alloc(bt);
-            const size_t pb = (size_t)std::max(1, P.nitems) * P.rows * 128;
+            const size_t pb = (size_t)std::max(1, P.nitems) * P.rows * 128 * (P.two_bases ? 2 : 1);
             if (B.partial.n < pb) B.partial.alloc(pb);
             const size_t p1 = (size_t)(D.apad / 64) * B.max_ent * P.rows_used;
             if (B.P1.n < p1) B.P1.alloc(p1);
@@ -811,6 +816,10 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
             if (B.items.n < (size_t)std::max(1, P.nitems)) B.items.alloc(std::max(1, P.nitems));
             B.tc0.alloc(B.ntt);
             B.tc1.alloc(B.ntt);
+            B.ti0.alloc((size_t)B.ntt * D.nlayers);
+            B.ti1.alloc((size_t)B.ntt * D.nlayers);
+            EKG_CUDA(cudaMemcpyAsync(B.ti0.p, P.ti0.data(), P.ti0.size() * 4, cudaMemcpyHostToDevice, s));
+            EKG_CUDA(cudaMemcpyAsync(B.ti1.p, P.ti1.data(), P.ti1.size() * 4, cudaMemcpyHostToDevice, s));
             if (B.k5l.n < P.k5l.size()) B.k5l.alloc(P.k5l.size());
             if (B.lrel.n < P.lrel.size()) B.lrel.alloc(P.lrel.size());
             if (P.nitems > 0)
@@ -825,7 +834,7 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
     }
 }
 
-void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTiming *tm) {
+void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTiming *tm, bool mark_static = false) {
     HeartDev &D = h->dev;
     EvalDev &E = h->ev;
     cudaStream_t s = h->stream;
@@ -834,12 +843,13 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
     int launches = 0;
     if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[0], s));
     EKG_CUDA(cudaMemsetAsync(E.err.p, 0, sizeof(uint32_t), s));
-    launch_layer_factors(s, D, E.layer_k.p, n_sims, E.F.p, E.layer_c.p);
+    launch_layer_factors(s, D, E.layer_k.p, n_sims, E.F.p, E.Ff.p, E.layer_c.p);
     ++launches;
     if (P.batch) {
         BatchState &B = h->bs;
-        launch_static_combine(s, D, P.J, B.J, nmove, n_sims, E.F.p, B.coef.p, B.k3.p, B.Q1.p, B.Q2.p, E.ecg.p);
+        launch_static_combine(s, D, P.J, B.J, nmove, n_sims, E.Ff.p, B.coef.p, B.k3.p, B.Q1.p, B.Q2.p, E.ecg.p);
         launches += nmove < (int)L;
+        if (mark_static) EKG_CUDA(cudaEventRecord(h->static_done, s));
         if (nmove > 0) {
             if (P.rows_used < P.rows) EKG_CUDA(cudaMemsetAsync(B.Bt.p, 0, (size_t)P.rows * D.apad * 4, s));
             BandArgs U;
@@ -863,7 +873,10 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             U.goff = B.goff.p;
             U.gtab = B.gtab.p;
             U.E = B.E.p;
-            U.F = E.F.p;
+            U.F = E.Ff.p;
+            U.nb = P.two_bases ? 2 : 1;
+            U.ti0 = B.ti0.p;
+            U.ti1 = B.ti1.p;
             U.k3 = B.k3.p;
             U.partial = B.partial.p;
             U.P1 = B.P1.p;
@@ -889,8 +902,6 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             A.at_hilo = D.at_hilo.p;
             A.items = B.items.p;
             A.hconst = B.hconst.p;
-            A.k3 = B.k3.p;
-            A.F = E.F.p;
             A.Bt = B.Bt.p;
             A.partial = B.partial.p;
             A.err = E.err.p;
@@ -945,13 +956,33 @@ void device_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *
     EKG_CUDA(cudaSetDevice(h->eng->device));
     const PassPlan P = plan_pass(h, n_sims, layer_k, leads);
     upload_inputs(h, P, layer_k, leads);
-    compute(h, P, crit_host ? n_crit_leads : 0, mode, nullptr);
-    const size_t L = D.nleads, S = n_sims;
+    const size_t L = D.nleads, S = n_sims, T = D.steps;
+    // batched form: the static-lead rows of the ECG are final after the first kernel, so their copy
+    // to the host runs on a second stream while the moved-lead part is computed
+    const bool split = ecg_host && P.batch && P.nmove < (int)L;
+    if (split && !h->copy_stream) {
+        EKG_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        EKG_CUDA(cudaEventCreateWithFlags(&h->static_done, cudaEventDisableTiming));
+    }
+    compute(h, P, crit_host ? n_crit_leads : 0, mode, nullptr, split);
+    if (split) {
+        const size_t nm = P.nmove;
+        EKG_CUDA(cudaStreamWaitEvent(h->copy_stream, h->static_done, 0));
+        EKG_CUDA(cudaMemcpy2DAsync(ecg_host + nm * T, L * T * 8, E.ecg.p + nm * T, L * T * 8, (L - nm) * T * 8, S,
+                                   cudaMemcpyDeviceToHost, h->copy_stream));
+    }
     EKG_CUDA(cudaMemcpyAsync(h->err_host, E.err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     if (crit_host && n_crit_leads > 0)
         EKG_CUDA(cudaMemcpyAsync(crit_host, E.crit.p, S * n_crit_leads * 2 * 8, cudaMemcpyDeviceToHost, s));
-    if (ecg_host) EKG_CUDA(cudaMemcpyAsync(ecg_host, E.ecg.p, S * L * D.steps * 8, cudaMemcpyDeviceToHost, s));
+    if (split) {
+        if (P.nmove > 0)
+            EKG_CUDA(cudaMemcpy2DAsync(ecg_host, L * T * 8, E.ecg.p, L * T * 8, (size_t)P.nmove * T * 8, S,
+                                       cudaMemcpyDeviceToHost, s));
+    } else if (ecg_host) {
+        EKG_CUDA(cudaMemcpyAsync(ecg_host, E.ecg.p, S * L * T * 8, cudaMemcpyDeviceToHost, s));
+    }
     EKG_CUDA(cudaStreamSynchronize(s));
+    if (split) EKG_CUDA(cudaStreamSynchronize(h->copy_stream));
     if (*h->err_host) throw Error{EKG_ERR_TIMEOUT, "a bounded device wait ran out (error word " +
                                                        std::to_string(*h->err_host) + ")"};
 }

@@ -164,13 +164,22 @@ class Heart:
             return crit, float(viol[0]), ecg, lk, leads
         return crit, float(viol[0])
 
-    def eval_batch(self, genes: np.ndarray, want_ecg: bool = False):
+    def eval_batch(self, genes: np.ndarray, want_ecg: bool = False, out=None):
+        """Criteria [n, n_criteria], violations [n] (and ECGs [n, n_leads, steps]) for n gene vectors.
+        ``out`` = (crit, viol[, ecg]) reuses caller-owned C-contiguous float64 arrays of those shapes."""
         genes = np.ascontiguousarray(np.atleast_2d(genes), dtype=np.float64)
         n, g = genes.shape
         _, nc = self.eval_shape()
-        crit = np.zeros((n, nc))
-        viol = np.zeros(n)
-        ecg = np.zeros((n, self.n_leads, self.steps)) if want_ecg else None
+        shapes = [(n, nc), (n,)] + ([(n, self.n_leads, self.steps)] if want_ecg else [])
+        if out is not None:
+            if len(out) != len(shapes) or any(
+                    a.shape != sh or a.dtype != np.float64 or not a.flags.c_contiguous for a, sh in zip(out, shapes)):
+                raise ValueError(f"out must be C-contiguous float64 arrays of shapes {shapes}")
+            bufs = list(out)
+        else:
+            bufs = [np.empty(sh) for sh in shapes]
+        crit, viol = bufs[0], bufs[1]
+        ecg = bufs[2] if want_ecg else None
         check(self._lib.ekg_eval_batch(self._h, n, dptr(genes), g, dptr(crit), dptr(viol), dptr(ecg)))
         return (crit, viol, ecg) if want_ecg else (crit, viol)
 
