@@ -112,6 +112,7 @@ struct HeartDev {
     // rho^5 (c1 T4 + c0) + rho^7 (c4 T6 + c3 T4 + c2); mask 0 when the set lacks cube symmetry
     float interior_c[5] = {0, 0, 0, 0, 0};
     uint32_t interior_mask = 0;
+    int64_t n_interior = 0;  // voxels flagged interior
     // time axis
     DBuf<double> t;         // [steps]
     DBuf<float2> t_hilo;    // [steps]

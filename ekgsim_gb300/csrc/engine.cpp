@@ -325,8 +325,10 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
                         uint32_t mbits = mi;
                         // flags for the moved-lead operand kernel (batch.cu): interior voxel (closed-form
                         // field), last voxel of its AP
-                        if (D.interior_mask && mi == D.interior_mask && oz == 0 && oy == 0 && ox == 0)
+                        if (D.interior_mask && mi == D.interior_mask && oz == 0 && oy == 0 && ox == 0) {
                             mbits |= 1u << 31;
+                            ++D.n_interior;
+                        }
                         if (i + 1 == gstart[gg + 1]) mbits |= 1u << 30;
                         float mf;
                         std::memcpy(&mf, &mbits, 4);
@@ -447,7 +449,8 @@ void ensure_general_capacity(ekg_heart *h, int n_sims) {
 // Device pass for n_sims simulations, split into upload / compute / download so the benchmark
 // can time the compute part with its inputs resident.  layer_k [S][nl][9], leads [S][L][3] (host).
 struct PassTiming {
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // start, after lead field, after contraction, end
+    // start, after the lead-field part, after the contraction, end, around the moved-lead operand kernel
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     bool on = false;
 };
 static int g_launch_count = 0;
@@ -883,8 +886,10 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             U.U = B.U.p;
             U.Up = B.Up.p;
             U.ecg = E.ecg.p;
+            if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[4], s));
             launch_batch_lead_field(s, D, P.two_bases, B.k5l.p, B.hconst.p, B.lrel.p, nmove, n_sims, U, B.Bt.p,
                                     B.work.p, h->sm_count);
+            if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[5], s));
             launch_band_u(s, U);
             launches += 2;
             if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[1], s));
@@ -1005,25 +1010,48 @@ void benchmark(ekg_heart *h, int n_sims, const double *layer_k, const double *le
     EKG_CUDA(cudaEventCreate(&t0));
     EKG_CUDA(cudaEventCreate(&t1));
     EKG_CUDA(cudaStreamSynchronize(s));
-    double contract = 0, prep = 0, tail = 0;
+    double contract = 0, prep = 0, tail = 0, operand = 0;
+    const bool op = P.batch && P.nmove > 0;
     EKG_CUDA(cudaEventRecord(t0, s));
     for (int i = 0; i < iters; ++i) {
         compute(h, P, ncl, mode, &tm);
         EKG_CUDA(cudaEventSynchronize(tm.ev[3]));
-        float a = 0, b = 0, c = 0;
+        float a = 0, b = 0, c = 0, d = 0;
         EKG_CUDA(cudaEventElapsedTime(&a, tm.ev[0], tm.ev[1]));
         EKG_CUDA(cudaEventElapsedTime(&b, tm.ev[1], tm.ev[2]));
         EKG_CUDA(cudaEventElapsedTime(&c, tm.ev[2], tm.ev[3]));
+        if (op) EKG_CUDA(cudaEventElapsedTime(&d, tm.ev[4], tm.ev[5]));
         prep += a;
         contract += b;
         tail += c;
+        operand += d;
     }
     EKG_CUDA(cudaEventRecord(t1, s));
     EKG_CUDA(cudaEventSynchronize(t1));
     float total = 0;
     EKG_CUDA(cudaEventElapsedTime(&total, t0, t1));
-    const double vals[7] = {total, contract, prep, tail, (double)g_launch_count, (double)P.nmove, P.batch ? 1.0 : 0.0};
-    for (int i = 0; i < n_out && i < 7; ++i) out[i] = vals[i];
+    // work per pass of the batched form: tensor flops the band GEMM executes (three BF16 products
+    // per K step and basis) and the bytes the moved-lead operand kernel has to move (tile rows in
+    // BF16 hi+lo and steady sums written; voxel geometry, AP ranges and times read once)
+    double gemm_flops = 0, op_bytes = 0;
+    if (op) {
+        const HeartDev &D = h->dev;
+        const BatchState &B = h->bs;
+        const int N = batch_tile_rows(P.two_bases), nb = P.two_bases ? 2 : 1;
+        for (const int4 &it : P.items) gemm_flops += (double)(it.z - it.y) * P.ntiles * 128.0 * N * 32 * 2 * 3 * nb;
+        std::vector<int32_t> nent(D.nlayers), es8((size_t)D.nlayers * 8), ls0(D.nlayers);
+        EKG_CUDA(cudaMemcpy(nent.data(), B.nent.p, D.nlayers * 4, cudaMemcpyDeviceToHost));
+        EKG_CUDA(cudaMemcpy(es8.data(), B.esplit8.p, es8.size() * 4, cudaMemcpyDeviceToHost));
+        EKG_CUDA(cudaMemcpy(ls0.data(), B.ls0.p, D.nlayers * 4, cudaMemcpyDeviceToHost));
+        double p1 = 0;
+        for (int L = 0; L < D.nlayers; ++L)
+            for (int e = 0; e < nent[L]; ++e) p1 += std::max(0, (es8[(size_t)L * 8 + e] + 7) / 8 - ls0[L]);
+        op_bytes = (double)P.rows_used * D.apad * 4 + p1 * P.rows_used * 8 +
+                   (double)D.nvox * 16 + (double)(D.nvox - D.n_interior) * 16 + (double)D.apad * 16;
+    }
+    const double vals[10] = {total, contract, prep, tail, (double)g_launch_count, (double)P.nmove, P.batch ? 1.0 : 0.0,
+                             operand, gemm_flops, op_bytes};
+    for (int i = 0; i < n_out && i < 10; ++i) out[i] = vals[i];
     for (auto &e : tm.ev) cudaEventDestroy(e);
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
