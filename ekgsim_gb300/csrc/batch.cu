@@ -31,6 +31,7 @@
 //   per-8-AP partial sums the operand kernel writes in FP32 (k_band_u), and the reduction adds
 //   F_L(t) [(1-k3) exp(-k4 (t - t0)) U1 + k3 U0] per layer.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 
@@ -130,10 +131,12 @@ __global__ void k_static_combine(int steps, int nleads, int nl, int J, int Jb, i
         const float *c = coef + ((size_t)s * nl + L) * J;
         const size_t q0 = ((size_t)L * rows + (size_t)l * Jb) * steps + t;
         float v1 = 0.f, v2 = 0.f;
-        for (int j = 0; j < J; ++j) {
-            v1 = fmaf(c[j], Q1[q0 + (size_t)j * steps], v1);
-            v2 = fmaf(c[j], Q2[q0 + (size_t)j * steps], v2);
-        }
+#pragma unroll
+        for (int j = 0; j < 10; ++j)  // J <= 10 (the basis order); unrolled so the loads issue together
+            if (j < J) {
+                v1 = fmaf(c[j], Q1[q0 + (size_t)j * steps], v1);
+                v2 = fmaf(c[j], Q2[q0 + (size_t)j * steps], v2);
+            }
         acc += (double)(F[((size_t)s * nl + L) * steps + t] * fmaf(kk, v2 - v1, v1));
     }
     ecg[((size_t)s * nleads + l) * steps + t] = acc;
@@ -384,10 +387,121 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
     }
 }
 
+// Small batches (up to SMALL_SIMS simulations): one thread per (AP, simulation), so the work spreads
+// over the heart instead of over simulations.  A block is two 64-AP tiles of one simulation; eight
+// consecutive lanes are one 8-AP chunk and write its BF16 hi/lo row segment two bytes each.  The
+// chunk's reference time comes from a shuffle over its lanes; the steady sums of a tile are reduced
+// by a shuffle butterfly within each warp (half a tile) and in shared memory across the two halves,
+// in a fixed order.  Same outputs as k_batch_lead_field.
+constexpr int SMALL_SIMS = 16;
+template <int N, bool DIAG>
+__global__ void __launch_bounds__(128) k_batch_lead_field_small(
+    int nkt, InteriorField ic, const int64_t *__restrict__ a_vox_begin, const float4 *__restrict__ vox_pos,
+    const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs, const float2 *__restrict__ at_hilo,
+    const int32_t *__restrict__ a_layer, const float *__restrict__ k5l, int nl, const float4 *__restrict__ hconst,
+    const float4 *__restrict__ lrel, int nmove, int n_sims, const int32_t *__restrict__ c8s,
+    const int32_t *__restrict__ nent, const int32_t *__restrict__ esplit8, const int64_t *__restrict__ goff,
+    const float *__restrict__ gtab, int max_ent, uint8_t *__restrict__ Bt, float2 *__restrict__ P1) {
+    __shared__ float s_d[26 * 4];
+    __shared__ float2 s_red[4][MAXE];  // [warp][entry]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid < nnb) {
+        const float dz = difs[3 * tid], dy = difs[3 * tid + 1], dx = difs[3 * tid + 2];
+        s_d[4 * tid] = dz;
+        s_d[4 * tid + 1] = dy;
+        s_d[4 * tid + 2] = dx;
+        s_d[4 * tid + 3] = dz * dz + dy * dy + dx * dx;
+    }
+    __syncthreads();
+    const int64_t apad = (int64_t)nkt * BKT;
+    const int64_t araw = (int64_t)blockIdx.x * 128 + tid;
+    const bool valid = araw < apad;  // whole 64-AP tiles are in or out (apad and the block are multiples of 64)
+    const int64_t a = valid ? araw : apad - 1;
+    const int s = blockIdx.y;
+    const int rows_used = n_sims * nmove;
+    const int kt = (int)(a / BKT), k = (int)(a % BKT), c8 = (int)(a / 8);
+    const int L = a_layer[a];
+    const float k5 = k5l[(size_t)s * nl + L], k4 = hconst[L].y;
+    const int ne = nent[L], cb = c8s[L];
+    const float2 at = at_hilo[a];
+    const bool pad = isinf(at.x);
+    // the chunk's last finite activation time (ascending, padding last): lane of the largest finite
+    int src = pad ? -1 : (lane & 7);
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) src = max(src, __shfl_xor_sync(0xffffffffu, src, o));
+    const int from = (lane & ~7) + max(src, 0);
+    const float rx = __shfl_sync(0xffffffffu, at.x, from), ry = __shfl_sync(0xffffffffu, at.y, from);
+    const float e = pad ? 0.f : ex2a(fmaf(k5, at.x, k5 * at.y));
+    const float ez = pad ? 0.f : ex2a(-k4 * ((rx - at.x) + (ry - at.y)));
+    const int vb = (int)a_vox_begin[a], ve = (int)a_vox_begin[a + 1];
+    for (int l0 = 0; l0 < nmove; l0 += 2) {
+        const int np = l0 + 1 < nmove ? 2 : 1;
+        const float4 r0 = lrel[(size_t)s * nmove + l0];
+        const float4 r1 = np == 2 ? lrel[(size_t)s * nmove + l0 + 1] : r0;
+        float acc0 = 0.f, acc1 = 0.f;
+        if (valid)
+            for (int v = vb; v < ve; ++v) {
+                const float4 pos = vox_pos[v];
+                const uint32_t mi = __float_as_uint(pos.w);
+                const float s0 = sq3(pos, r0), s1 = sq3(pos, r1);
+                if ((mi & VOX_INTERIOR) && s0 >= INTERIOR_S_MIN && s1 >= INTERIOR_S_MIN) {
+                    acc0 += interior_w(ic, pos, r0, s0);
+                    if (np == 2) acc1 += interior_w(ic, pos, r1, s1);
+                } else {
+                    const float4 out = vox_out[v];
+                    acc0 += DIAG ? voxel_w_diag(pos, mi, out, r0) : voxel_w_general(pos, mi, out, r0, nnb, s_d);
+                    if (np == 2)
+                        acc1 += DIAG ? voxel_w_diag(pos, mi, out, r1) : voxel_w_general(pos, mi, out, r1, nnb, s_d);
+                }
+            }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (q >= np) break;
+            const float w = (q ? acc1 : acc0) * e;
+            const __nv_bfloat16 hb = __float2bfloat16_rn(w);
+            const __nv_bfloat16 lb = __float2bfloat16_rn(w - __bfloat162float(hb));
+            const int row = s * nmove + l0 + q;
+            if (valid) {
+                const int nt = row / N, n = row % N;
+                const size_t tile = ((size_t)nt * nkt + kt) * 2;
+                const size_t off = (size_t)((k / 8) * (N / 8) + n / 8) * 128 + (n % 8) * 16 + (k % 8) * 2;
+                *reinterpret_cast<__nv_bfloat16 *>(Bt + tile * (N * 128) + off) = hb;
+                *reinterpret_cast<__nv_bfloat16 *>(Bt + (tile + 1) * (N * 128) + off) = lb;
+            }
+            for (int ei = 0; ei < max_ent; ++ei) {
+                const bool in = ei < ne && c8 < esplit8[L * MAXE + ei];
+                float x = in ? w : 0.f;
+                float y = in ? gtab[goff[L * MAXE + ei] + (c8 - cb)] * (w * ez) : 0.f;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    x += __shfl_xor_sync(0xffffffffu, x, o);
+                    y += __shfl_xor_sync(0xffffffffu, y, o);
+                }
+                if (lane == 0) s_red[warp][ei] = make_float2(x, y);
+            }
+            __syncthreads();
+            // thread (half-tile pair h, entry ei) combines the two warps of its tile
+            if (tid < 2 * max_ent) {
+                const int h = tid / max_ent, ei = tid % max_ent;
+                const int64_t ta = (int64_t)blockIdx.x * 128 + h * 64;
+                if (ta < apad) {
+                    const int tkt = (int)(ta / BKT), tL = a_layer[ta];
+                    if (ei < nent[tL] && tkt * (BKT / 8) < esplit8[tL * MAXE + ei]) {
+                        const float2 p0 = s_red[2 * h][ei], p1 = s_red[2 * h + 1][ei];
+                        P1[((size_t)tkt * max_ent + ei) * rows_used + (size_t)(l0 + q) * n_sims + s] =
+                            make_float2(p0.x + p1.x, p0.y + p1.y);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
 // Steady sums per (row', layer, entry): U[row'][L][e] = sum over the layer's K tiles [ls0, ls1)
 // below the entry's prefix end of P1[kt][e][row'] (U0, U1).  Two passes in a fixed order:
 // k_band_u sums BU_PARTS consecutive parts of the K range in FP32 (a few tiles each) per (part,
-// layer) block, threads over rows; k_band_u2 adds the parts in FP64, eight warps per 32 outputs.
+// layer) block, threads over rows; k_band_u2 adds the parts in FP64, one warp per output.
 // Up: [parts][rows][nl][max_ent]; U stored in FP32.
 constexpr int BU_PARTS = 128;
 __global__ void __launch_bounds__(256) k_band_u(int rows_used, int nl, int max_ent, const int32_t *__restrict__ nent,
@@ -412,26 +526,20 @@ __global__ void __launch_bounds__(256) k_band_u(int rows_used, int nl, int max_e
 }
 
 __global__ void __launch_bounds__(256) k_band_u2(int64_t n_out, const float2 *__restrict__ Up, float2 *__restrict__ U) {
-    __shared__ double2 red[8][32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t i = blockIdx.x * 32 + lane;
+    const int lane = threadIdx.x & 31;
+    const int64_t i = blockIdx.x * 8 + (threadIdx.x >> 5);  // one warp per output
+    if (i >= n_out) return;
     double a = 0.0, b = 0.0;
-    if (i < n_out)
-#pragma unroll 4
-        for (int p = w; p < BU_PARTS; p += 8) {
-            const float2 v = Up[p * n_out + i];
-            a += (double)v.x;
-            b += (double)v.y;
-        }
-    red[w][lane] = make_double2(a, b);
-    __syncthreads();
-    if (w == 0 && i < n_out) {
-        for (int k = 1; k < 8; ++k) {
-            a += red[k][lane].x;
-            b += red[k][lane].y;
-        }
-        U[i] = make_float2((float)a, (float)b);
+    for (int p = lane; p < BU_PARTS; p += 32) {
+        const float2 v = Up[p * n_out + i];
+        a += (double)v.x;
+        b += (double)v.y;
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) U[i] = make_float2((float)a, (float)b);
 }
 
 // ------------------------------------------------------------------ batch GEMM
@@ -464,7 +572,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 // 128-step tile inside one layer, in 32-AP stages.  partial: [items][rows][128] FP32 accumulators
 // (float2 of the two bases with NB = 2).
 template <int NB, int N>
-__global__ void __launch_bounds__(WS_THREADS, 1) k_batch_umma(
+__global__ void __launch_bounds__(WS_THREADS, (N <= 32 ? 2 : 1)) k_batch_umma(
     int steps, int nl, int nkt, int rows, int nmove, int n_sims, const float2 *__restrict__ t_hilo,
     const float2 *__restrict__ at_hilo, const int4 *__restrict__ items, const float4 *__restrict__ hconst,
     const uint8_t *__restrict__ Bt, float *__restrict__ partial, uint32_t *__restrict__ err) {
@@ -674,7 +782,64 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_batch_umma(
 // ecg[s][l][t] (l < nmove) = sum_L F[s][L][t] [(1 - k3) (Y1_L + E[L][t] U1) + k3 (Y2_L + U0)]
 // (with one basis the GEMM already mixed k3: Y_L + (1 - k3) E U1 + k3 U0), Y_L = sum over the band
 // items of (t's tile, L) of the raw accumulators, (U0, U1) = U[row'][L][ent[L][j]], row = s * nmove
-// + l, row' = l * S + s, j = t / 128.  Per layer in FP32, over layers in FP64; thread per (row, t).
+// + l, row' = l * S + s, j = t / 128.  Block per (row, 32 steps): the 8 warps split each layer's
+// items (FP32, combined in a fixed order), the sum over layers is FP64 (few rows, many items);
+// k_reduce_band: one thread per (row, t) (many rows).
+__global__ void __launch_bounds__(256) k_reduce_band_w(int steps, int rows, int nmove, int n_sims, int nleads, int nl,
+                                                     int ntt, int max_ent, int nb, const int32_t *__restrict__ ti0,
+                                                     const int32_t *__restrict__ ti1, const int32_t *__restrict__ ent,
+                                                     const float *__restrict__ partial, const float2 *__restrict__ U,
+                                                     const float *__restrict__ E, const float *__restrict__ F,
+                                                     const double *__restrict__ k3, double *__restrict__ ecg) {
+    __shared__ float red[8][2][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int tt = blockIdx.x * 32 + lane;
+    const int r = blockIdx.y;
+    const int s = r / nmove, l = r % nmove;
+    const int j = (blockIdx.x * 32) / BM, tl = tt - j * BM;
+    const bool on = tt < steps;
+    const size_t rp = (size_t)l * n_sims + s;
+    double v = 0.0;
+    for (int L = 0; L < nl; ++L) {
+        float y1 = 0.f, y2 = 0.f;
+        const int c1 = ti1[j * nl + L];
+        if (on) {
+            if (nb == 2) {
+                for (int c = ti0[j * nl + L] + w; c < c1; c += 8) {
+                    const float2 p = reinterpret_cast<const float2 *>(partial)[((size_t)c * rows + r) * BM + tl];
+                    y1 += p.x;
+                    y2 += p.y;
+                }
+            } else {
+                for (int c = ti0[j * nl + L] + w; c < c1; c += 8) y1 += partial[((size_t)c * rows + r) * BM + tl];
+            }
+        }
+        red[w][0][lane] = y1;
+        red[w][1][lane] = y2;
+        __syncthreads();
+        if (w == 0 && on) {
+            y1 = y2 = 0.f;
+            for (int i = 0; i < 8; ++i) {
+                y1 += red[i][0][lane];
+                y2 += red[i][1][lane];
+            }
+            const float kk = (float)k3[(size_t)s * nl + L];
+            const int e = ent[L * ntt + j];
+            float st1 = 0.f, st0 = 0.f;
+            if (e >= 0) {
+                const float2 u = U[(rp * nl + L) * max_ent + e];
+                st1 = E[(size_t)L * steps + tt] * u.y;
+                st0 = u.x;
+            }
+            const float x = nb == 2 ? fmaf(kk, (y2 + st0) - (y1 + st1), y1 + st1)
+                                    : fmaf(kk, st0 - st1, y1 + st1);
+            v += (double)(F[((size_t)s * nl + L) * steps + tt] * x);
+        }
+        __syncthreads();
+    }
+    if (w == 0 && on) ecg[((size_t)s * nleads + l) * steps + tt] = v;
+}
+
 __global__ void k_reduce_band(int steps, int rows, int nmove, int n_sims, int nleads, int nl, int ntt, int max_ent,
                               int nb, const int32_t *__restrict__ ti0, const int32_t *__restrict__ ti1,
                               const int32_t *__restrict__ ent, const float *__restrict__ partial,
@@ -730,7 +895,13 @@ void launch_gemm(cudaStream_t st, const BatchArgs &A) {
 
 }  // namespace
 
-int batch_tile_rows(int two_bases) { return two_bases ? 128 : 256; }
+// N of the band GEMM's row tiles: the smallest instance that holds the rows (one simulation's moved
+// leads fit 32), else the largest (256 with one basis, 128 with two).
+int batch_tile_rows(int two_bases, int rows_used) {
+    if (rows_used <= 32) return 32;
+    if (two_bases || rows_used <= 128) return 128;
+    return 256;
+}
 
 void launch_taylor_w(cudaStream_t s, const HeartDev &h, const float *W0, int J, const double *centre,
                      const double *scale, float *Wt) {
@@ -761,6 +932,7 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, c
     const int nsg = (n_sims + LF_THREADS - 1) / LF_THREADS;
     const int nkt = (int)(h.apad / BKT);
     const bool diag = h.nhood == EKG_NHOOD_3D4;
+    const bool small = n_sims <= SMALL_SIMS;
     InteriorField ic;
     ic.a0 = h.interior_c[0];
     ic.a1 = h.interior_c[1];
@@ -770,6 +942,14 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, c
     EKG_CUDA(cudaMemsetAsync(work, 0, sizeof(int), s));
 #define EKG_LF(NN, DG)                                                                                            \
     do {                                                                                                          \
+        if (small) {                                                                                              \
+            dim3 g((unsigned)((nkt * BKT + 127) / 128), (unsigned)n_sims);                                         \
+            k_batch_lead_field_small<NN, DG><<<g, 128, 0, s>>>(                                                   \
+                nkt, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p,    \
+                k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.c8s, B.nent, B.esplit8, B.goff, B.gtab, B.max_ent, \
+                Bt, B.P1);                                                                                        \
+            break;                                                                                                \
+        }                                                                                                         \
         static int per_sm = 0;                                                                                    \
         if (!per_sm)                                                                                              \
             EKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_lead_field<NN, DG>,           \
@@ -780,10 +960,16 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, c
             k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.c8s, B.nent, B.esplit8, B.goff, B.gtab, B.max_ent, Bt, \
             B.P1);                                                                                                \
     } while (0)
-    if (two_bases) {
+    switch (batch_tile_rows(two_bases, n_sims * nmove)) {
+    case 32:
+        if (diag) EKG_LF(32, true);
+        else EKG_LF(32, false);
+        break;
+    case 128:
         if (diag) EKG_LF(128, true);
         else EKG_LF(128, false);
-    } else {
+        break;
+    default:
         if (diag) EKG_LF(256, true);
         else EKG_LF(256, false);
     }
@@ -793,8 +979,15 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, c
 
 void launch_batch_gemm(cudaStream_t s, const BatchArgs &A) {
     if (A.nitems == 0) return;
-    if (A.two_bases) launch_gemm<2, 128>(s, A);
-    else launch_gemm<1, 256>(s, A);
+    const int N = batch_tile_rows(A.two_bases, A.rows_used);
+    if (A.two_bases) {
+        if (N == 32) launch_gemm<2, 32>(s, A);
+        else launch_gemm<2, 128>(s, A);
+    } else {
+        if (N == 32) launch_gemm<1, 32>(s, A);
+        else if (N == 128) launch_gemm<1, 128>(s, A);
+        else launch_gemm<1, 256>(s, A);
+    }
 }
 
 int band_u_parts() { return BU_PARTS; }
@@ -803,14 +996,20 @@ void launch_band_u(cudaStream_t s, const BandArgs &A) {
     k_band_u<<<dim3(BU_PARTS, (unsigned)A.nl), 256, 0, s>>>(A.rows_used, A.nl, A.max_ent, A.nent, A.esplit8, A.ls0,
                                                            A.ls1, A.P1, A.Up);
     const int64_t n = (int64_t)A.rows_used * A.nl * A.max_ent;
-    k_band_u2<<<(unsigned)((n + 31) / 32), 256, 0, s>>>(n, A.Up, A.U);
+    k_band_u2<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(n, A.Up, A.U);
     EKG_CUDA(cudaGetLastError());
 }
 
 void launch_reduce_band(cudaStream_t s, const BandArgs &A) {
-    dim3 grid((unsigned)((A.steps + 127) / 128), (unsigned)A.rows_used);
-    k_reduce_band<<<grid, 128, 0, s>>>(A.steps, A.rows, A.nmove, A.n_sims, A.nleads, A.nl, A.ntt, A.max_ent, A.nb,
-                                       A.ti0, A.ti1, A.ent, A.partial, A.U, A.E, A.F, A.k3, A.ecg);
+    if (A.rows_used < 64) {
+        dim3 grid((unsigned)((A.steps + 31) / 32), (unsigned)A.rows_used);
+        k_reduce_band_w<<<grid, 256, 0, s>>>(A.steps, A.rows, A.nmove, A.n_sims, A.nleads, A.nl, A.ntt, A.max_ent,
+                                             A.nb, A.ti0, A.ti1, A.ent, A.partial, A.U, A.E, A.F, A.k3, A.ecg);
+    } else {
+        dim3 grid((unsigned)((A.steps + 127) / 128), (unsigned)A.rows_used);
+        k_reduce_band<<<grid, 128, 0, s>>>(A.steps, A.rows, A.nmove, A.n_sims, A.nleads, A.nl, A.ntt, A.max_ent,
+                                           A.nb, A.ti0, A.ti1, A.ent, A.partial, A.U, A.E, A.F, A.k3, A.ecg);
+    }
     EKG_CUDA(cudaGetLastError());
 }
 

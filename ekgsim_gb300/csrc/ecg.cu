@@ -106,14 +106,16 @@ __global__ void k_lead_field(int64_t apad, const int64_t *__restrict__ a_vox_beg
 // FP32 in a form that keeps relative precision at both ends:
 //     ln(1 + e^u) = log1p(exp(u)) (u + log1p(exp(-u)) for u > 0),  R = -expm1(-(k6/k7) ln(1 + e^u)).
 // layer_k: [S][nl][9].
+// cpre: the constants ln(2^(k7/k6) - 1) per (sim, layer) when the host computed them (small
+// passes, where the FP64 pow/log would be one block's latency), else NULL.
 __global__ void k_layer_factors(int nl, int steps, const double *__restrict__ t, const double *__restrict__ layer_k,
-                                int n_sims, double *__restrict__ F, float *__restrict__ Ff,
-                                float *__restrict__ layer_c) {
+                                const double *__restrict__ cpre, int n_sims, double *__restrict__ F,
+                                float *__restrict__ Ff, float *__restrict__ layer_c) {
     const int64_t sl = blockIdx.x;  // sim * nl + layer
     const double *k = layer_k + sl * 9;
     __shared__ double c;
     if (threadIdx.x == 0) {
-        c = log(pow(2.0, k[7] / k[6]) - 1);
+        c = cpre ? cpre[sl] : log(pow(2.0, k[7] / k[6]) - 1);
         const double L2E = 1.4426950408889634;
         reinterpret_cast<float4 *>(layer_c)[sl] =
             make_float4((float)(k[1] * L2E), (float)(k[4] * L2E), (float)(1.0 - k[3]), (float)k[3]);
@@ -358,10 +360,10 @@ void launch_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads,
     EKG_CUDA(cudaGetLastError());
 }
 
-void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_layer_k, int n_sims, double *d_F,
-                          float *d_Ff, float *d_layer_c) {
+void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_layer_k, const double *d_cpre,
+                          int n_sims, double *d_F, float *d_Ff, float *d_layer_c) {
     k_layer_factors<<<(unsigned)((int64_t)n_sims * h.nlayers), 128, 0, s>>>(h.nlayers, h.steps, h.t.p, d_layer_k,
-                                                                            n_sims, d_F, d_Ff, d_layer_c);
+                                                                            d_cpre, n_sims, d_F, d_Ff, d_layer_c);
     EKG_CUDA(cudaGetLastError());
 }
 
@@ -400,9 +402,10 @@ void launch_criteria(cudaStream_t s, const HeartDev &h, const double *d_ecg, int
                      int n_crit_leads, int mode, const double *d_targets, const int64_t *d_tlen,
                      const double *d_toff, double *d_crit) {
     if (n_crit_leads <= 0) return;
+    // one warp per block, so the FP64 work of a few simulations spreads over as many SMs as it has warps
     const int64_t pairs = (int64_t)n_crit_leads * n_sims;
-    k_criteria<<<(unsigned)((pairs + 7) / 8), 256, 0, s>>>(h.steps, h.nleads, n_crit_leads, n_sims, mode, d_ecg,
-                                                           d_targets, d_tlen, d_toff, ncrit_stride, d_crit);
+    k_criteria<<<(unsigned)pairs, 32, 0, s>>>(h.steps, h.nleads, n_crit_leads, n_sims, mode, d_ecg, d_targets, d_tlen,
+                                              d_toff, ncrit_stride, d_crit);
     EKG_CUDA(cudaGetLastError());
 }
 

@@ -35,6 +35,7 @@ namespace ekg {
 struct BatchState {
     bool basis_ok = false;
     std::vector<double> key;               // k1, k4 per layer the basis was built for
+    std::vector<double> single_key;        // k1, k4 of the last single-simulation pass
     int J = 0;                             // Taylor terms stored
     std::vector<double> centre, scale;     // per layer
     DBuf<float> Q1, Q2;                    // [nl][L*J][steps]
@@ -114,5 +115,6 @@ struct ekg_heart {
     int sm_count = 152;
     bool has_eval = false;
     bool any_k0 = false;              // some layer AP of the current pass has k0 != 0
+    bool cpre_on = false;             // the current pass's repolarisation constants come from the host
     ekg::SimConfig cfg;
 };

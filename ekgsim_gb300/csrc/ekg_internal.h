@@ -122,6 +122,7 @@ struct HeartDev {
 struct EvalDev {
     int cap_sims = 0;
     DBuf<double> layer_k;   // [S][nl][9]
+    DBuf<double> cpre;      // [S][nl] ln(2^(k7/k6) - 1), host-computed for small passes
     DBuf<double> leads;     // [S][L][3]
     DBuf<float> layer_c;    // [S][nl][4]: k1*log2e, k4*log2e, 1-k3, k3 (FP32 H constants)
     DBuf<double> F;         // [S][nl][steps]
@@ -140,8 +141,8 @@ struct EvalDev {
 
 void launch_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads, int nleads_in, int lead_stride,
                        int n_sims, float *d_W, int w_lead_stride);
-void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_layer_k, int n_sims, double *d_F,
-                          float *d_Ff, float *d_layer_c);
+void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_layer_k, const double *d_cpre,
+                          int n_sims, double *d_F, float *d_Ff, float *d_layer_c);
 void launch_scale_w(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
                     float *d_Wp);
 void launch_k0_term(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
@@ -166,7 +167,8 @@ void launch_contract_umma_args(cudaStream_t s, const ContractArgs &a);
 
 // ------------------------------------------------------------------ batched form (batch.cu)
 struct BatchArgs {
-    int steps = 0, nl = 0, nkt = 0, rows = 0, nmove = 0, n_sims = 0, ntiles = 0, nitems = 0, two_bases = 0;
+    int steps = 0, nl = 0, nkt = 0, rows = 0, rows_used = 0, nmove = 0, n_sims = 0, ntiles = 0, nitems = 0,
+        two_bases = 0;
     const float2 *t_hilo = nullptr, *at_hilo = nullptr;
     const int4 *items = nullptr;  // (t tile, first stage, end stage, layer), stages of 32 APs
     const float4 *hconst = nullptr;
@@ -191,7 +193,7 @@ struct BandArgs {
     float2 *U = nullptr;             // [rows][nl][max_ent]
     double *ecg = nullptr;
 };
-int batch_tile_rows(int two_bases);
+int batch_tile_rows(int two_bases, int rows_used);
 void launch_taylor_w(cudaStream_t s, const HeartDev &h, const float *W0, int J, const double *centre,
                      const double *scale, float *Wt);
 void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int32_t *lc0, const int32_t *lc1,

@@ -1,6 +1,7 @@
 // engine.cpp -- C ABI of the engine: engine and heart lifetime, plain and batched evaluation,
 // simulator.ini front end.
 #include <algorithm>
+#include <climits>
 #include <array>
 #include <chrono>
 #include <cstdlib>
@@ -693,7 +694,7 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
             if (p[3 * l] != h->leads0[3 * l] || p[3 * l + 1] != h->leads0[3 * l + 1] || p[3 * l + 2] != h->leads0[3 * l + 2])
                 P.nmove = std::max(P.nmove, l + 1);
     }
-    if (n_sims < 2 || !h->eng->batched || nl > 255) return P;
+    if (n_sims < 1 || !h->eng->batched || nl > 255) return P;
     std::vector<double> key(2 * nl);
     bool k3_uniform = true;
     for (int i = 0; i < nl; ++i) {
@@ -706,6 +707,16 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
             if (k[1] != key[2 * i] || k[4] != key[2 * i + 1] || k[0] != 0.0) return P;
             if (k[3] != layer_k[9 * i + 3]) k3_uniform = false;
         }
+    // A single simulation takes the batched form once its (k1, k4) is settled: when the basis for it
+    // exists, or when the previous single call had the same values (callers that vary k1, k4 from
+    // call to call keep the per-simulation form instead of rebuilding the basis each time).
+    if (n_sims == 1) {
+        BatchState &Bm = h->bs;
+        const bool have = Bm.basis_ok && Bm.key == key;
+        const bool repeat = Bm.single_key == key;
+        Bm.single_key = key;
+        if (!have && !repeat) return P;
+    }
     ensure_basis(h, key);
     const BatchState &B = h->bs;
     double xmax = 0;
@@ -734,8 +745,8 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
         P.hc[i] = make_float4((float)(key[2 * i] * L2E), (float)(key[2 * i + 1] * L2E), (float)(1.0 - layer_k[9 * i + 3]),
                               (float)layer_k[9 * i + 3]);
     if (P.nmove > 0) {
-        const int N = batch_tile_rows(P.two_bases);
         P.rows_used = n_sims * P.nmove;
+        const int N = batch_tile_rows(P.two_bases, P.rows_used);
         P.ntiles = (P.rows_used + N - 1) / N;
         P.rows = P.ntiles * N;
         // band work items: each (tile, layer) band cut into pieces of at most `per` stages, `per`
@@ -743,7 +754,7 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
         const int ntt = B.ntt;
         int64_t total = 0;
         for (size_t i = 0; i < B.band_s0.size(); ++i) total += B.band_s1[i] - B.band_s0[i];
-        const int target = std::max(1, h->eng->batch_ctas > 0 ? h->eng->batch_ctas : h->sm_count);
+        const int target = std::max(1, h->eng->batch_ctas > 0 ? h->eng->batch_ctas : h->sm_count * (N <= 32 ? 2 : 1));
         int64_t per = std::max<int64_t>(1, (total * P.ntiles + target - 1) / target);
         for (;; ++per) {
             int64_t cnt = 0;
@@ -792,6 +803,16 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
     ensure_eval_capacity(h, n_sims);
     const size_t L = D.nleads, S = n_sims;
     EKG_CUDA(cudaMemcpyAsync(E.layer_k.p, layer_k, S * D.nlayers * 9 * 8, cudaMemcpyHostToDevice, s));
+    // small passes: the repolarisation constant ln(2^(k7/k6) - 1) per (sim, layer) on the host
+    h->cpre_on = S <= 16;
+    if (h->cpre_on) {
+        double c[16 * 256];
+        const size_t n = S * D.nlayers;
+        for (size_t i = 0; i < n && i < 16 * 256; ++i) c[i] = std::log(std::pow(2.0, layer_k[9 * i + 7] / layer_k[9 * i + 6]) - 1);
+        E.cpre.alloc(16 * 256);
+        // (a copy from pageable memory is staged before the call returns, so the stack buffer may go)
+        EKG_CUDA(cudaMemcpyAsync(E.cpre.p, c, std::min<size_t>(n, 16 * 256) * 8, cudaMemcpyHostToDevice, s));
+    }
     h->any_k0 = false;
     for (size_t i = 0; i < S * D.nlayers; ++i) h->any_k0 = h->any_k0 || layer_k[9 * i] != 0.0;
     if (P.nmove > 0) EKG_CUDA(cudaMemcpyAsync(E.leads.p, leads, S * L * 3 * 8, cudaMemcpyHostToDevice, s));
@@ -846,7 +867,7 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
     int launches = 0;
     if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[0], s));
     EKG_CUDA(cudaMemsetAsync(E.err.p, 0, sizeof(uint32_t), s));
-    launch_layer_factors(s, D, E.layer_k.p, n_sims, E.F.p, E.Ff.p, E.layer_c.p);
+    launch_layer_factors(s, D, E.layer_k.p, h->cpre_on ? E.cpre.p : nullptr, n_sims, E.F.p, E.Ff.p, E.layer_c.p);
     ++launches;
     if (P.batch) {
         BatchState &B = h->bs;
@@ -898,6 +919,7 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             A.nl = D.nlayers;
             A.nkt = (int)(D.apad / 64);
             A.rows = P.rows;
+            A.rows_used = P.rows_used;
             A.nmove = nmove;
             A.n_sims = n_sims;
             A.ntiles = P.ntiles;
@@ -1037,7 +1059,7 @@ void benchmark(ekg_heart *h, int n_sims, const double *layer_k, const double *le
     if (op) {
         const HeartDev &D = h->dev;
         const BatchState &B = h->bs;
-        const int N = batch_tile_rows(P.two_bases), nb = P.two_bases ? 2 : 1;
+        const int N = batch_tile_rows(P.two_bases, P.rows_used), nb = P.two_bases ? 2 : 1;
         for (const int4 &it : P.items) gemm_flops += (double)(it.z - it.y) * P.ntiles * 128.0 * N * 32 * 2 * 3 * nb;
         std::vector<int32_t> nent(D.nlayers), es8((size_t)D.nlayers * 8), ls0(D.nlayers);
         EKG_CUDA(cudaMemcpy(nent.data(), B.nent.p, D.nlayers * 4, cudaMemcpyDeviceToHost));

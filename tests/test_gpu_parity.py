@@ -260,3 +260,56 @@ def test_batched_form_twelve_leads_static_and_moved(engine):
     worst = _batch_vs_oracle(engine, spec, 400, genes, lambda g: O.layer_aps(
         3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], "endo-mid-epi", 0.6, g[:12])[0])
     assert worst <= ECG_TOL
+
+
+def test_batched_two_bases_free_k3(engine):
+    """k3 free per simulation: the batched form keeps both bases (N = 128 / 32 tiles, six MMAs per K
+    step) and still matches the oracle."""
+    from ekgsim_gb300.engine import Heart
+    spec = synth.config(0)["spec"]
+    steps = 500
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    h = Heart.create(engine, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+    free = [3, 5, 6, 7, 8]
+    target = synth.analytic_target(spec.n_leads, steps, 4)
+    h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, free, [t for t in target], mid_position=0.6)
+    ng, _ = h.eval_shape()
+    lo, hi = h.gene_bounds()
+    rng = np.random.Generator(np.random.PCG64(11))
+    genes = lo + (hi - lo) * rng.random((20, ng))
+    # lead displacements as in the README-bounded vectors (the AP genes above are free within bounds)
+    genes[:, 15:] = np.stack([synth.genes_for(spec, r, 0)[12:] for r in range(20)])
+    _, _, ecg_b = h.eval_batch(genes, want_ecg=True)
+    at, layer = O.activation(grid, tm)
+    for i in (0, 7, 19):
+        g = genes[i]
+        lk = O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, free, "endo-mid-epi", 0.6,
+                         g[:15])[0]
+        moved = O.move_leads(leads, g[15:15 + 2 * spec.n_leads].reshape(-1, 2))
+        ref = O.run(layer, at, lk, moved, "3D4", 0.0, float(steps), 1.0)
+        assert rel_l2(ecg_b[i], ref) <= ECG_TOL
+
+
+def test_single_simulation_batched_form(engine):
+    """Repeated single evaluations with the same k1, k4 switch to the batched form (static-lead basis +
+    32-row band GEMM); the first call uses the per-simulation form.  Both match the oracle."""
+    from ekgsim_gb300.engine import Heart
+    spec = synth.small_spec(40, n_leads=4, seed=21)
+    steps = 400
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(3, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    h = Heart.create(engine, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+    target = synth.analytic_target(spec.n_leads, steps, 5)
+    h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], [t for t in target], mid_position=0.6)
+    at, layer = O.activation(grid, tm)
+    for r in range(3):
+        g = synth.genes_for(spec, 50 + r, 0)
+        crit, viol, ecg, _, _ = h.eval(g, want_ecg=True)
+        lk = O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], "endo-mid-epi",
+                         0.6, g[:12])[0]
+        moved = O.move_leads(leads, g[12:12 + 2 * spec.n_leads].reshape(-1, 2))
+        ref = O.run(layer, at, lk, moved, "3D4", 0.0, float(steps), 1.0)
+        assert rel_l2(ecg, ref) <= ECG_TOL
