@@ -126,6 +126,9 @@ def make_heart_spec(name: str):
     if name == "batched":
         c = synth.config(2)
         return c["spec"], c["steps"], c["batch"], 2, c["name"]
+    if name == "bsm":
+        c = synth.config(4)
+        return c["spec"], c["steps"], c["batch"], 4, c["name"]
     c = synth.config(1)
     return c["spec"], c["steps"], 64, 1, c["name"]
 
@@ -193,11 +196,12 @@ def cpu_farm(spec, steps, genes, sample_steps: int, threads: int):
     return sims_per_s, dt, sample
 
 
-def served_run(seconds: float = 4.0, rate: float = 500.0, seed: int = 3000):
+def served_run(seconds: float = 4.0, rate: float = 500.0, seed: int = 3000, max_wait_us: int = 0):
     """Served configuration: a Poisson stream of evaluation requests over four resident hearts
     (48^3, 96^3, 144^3, 192^3 scaled ellipsoids, 3 layers, 12 leads, 600 steps); continuous batching
-    in the engine's request loop.  Returns latency percentiles (submit -> result), throughput and
-    the mean number of requests per device pass."""
+    in the engine's request loop.  With max_wait_us = 0 a pass starts as soon as its heart is idle
+    and requests that arrive during a pass form the next one.  Returns latency percentiles (submit ->
+    result), throughput and the mean number of requests per device pass."""
     from ekgsim_gb300 import engine as E
     from ekgsim_gb300 import synth
     cfg = synth.config(3)
@@ -212,7 +216,7 @@ def served_run(seconds: float = 4.0, rate: float = 500.0, seed: int = 3000):
                    [t for t in synth.analytic_target(spec.n_leads, cfg["steps"], spec.seed + 999)], mid_position=0.6)
         hearts.append(h)
         specs.append(spec)
-    srv = E.Server(eng, max_batch=256, max_wait_us=2000)
+    srv = E.Server(eng, max_batch=256, max_wait_us=max_wait_us)
     ids = [srv.add_heart(h) for h in hearts]
     rng = np.random.Generator(np.random.PCG64(seed))
     n = int(seconds * rate)
@@ -242,7 +246,7 @@ def served_run(seconds: float = 4.0, rate: float = 500.0, seed: int = 3000):
     lat = np.array(lat)
     return {"requests": n, "rate_req_s": rate, "throughput_req_s": n / (t1 - t0),
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "mean_batch": float(np.mean(batch)), "hearts": [s.n for s in specs]}
+            "mean_batch": float(np.mean(batch)), "max_wait_us": max_wait_us, "hearts": [s.n for s in specs]}
 
 
 def host_cores() -> int:
@@ -297,7 +301,7 @@ def run_ours(args):
     info = heart.info
     # per-simulation layer APs and moved leads (host, as the evaluation does)
     cfg = heart._cfg
-    lk = np.stack([E.layer_aps(cfg, 3, g[:12])[0] for g in genes])
+    lk = np.stack([E.layer_aps(cfg, info.n_layers, g[:12])[0] for g in genes])
     moved = np.stack([E.move_leads(leads_zyx, g[12:].reshape(-1, 2)) for g in genes])
 
     # device-only throughput (inputs resident)
@@ -399,7 +403,7 @@ def run_ours(args):
             rels.append(float(np.linalg.norm(ecg[i] - ref) / np.linalg.norm(ref)))
         line["parity"] = {"ecg_rel_l2_max": max(rels), "checked_sims": len(rels), "at_mismatch": mism}
     if d.rank == 0 and not args.no_served:
-        line["served"] = served_run()
+        line["served"] = served_run(max_wait_us=args.served_wait_us)
     if d.rank == 0 and d.world == 1 and not args.no_cpu:
         v, dt, sample = cpu_farm(spec, steps, genes, args.cpu_sample_steps, host_cores())
         line["cpu_baseline"] = {"value": v, "unit": "sims/s", "cores": host_cores(), "kind": "port",
@@ -417,7 +421,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["batched", "single"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "single", "bsm"])
+    ap.add_argument("--served-wait-us", type=int, default=0,
+                    help="served form: longest a request waits for others to join its pass while its heart is idle")
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--plain-calls", type=int, default=50)
     ap.add_argument("--cpu-sample-steps", type=int, default=16)

@@ -1083,7 +1083,8 @@ void benchmark(ekg_heart *h, int n_sims, const double *layer_k, const double *le
 
 // Per-simulation host part of SimImplementation::eval (sim.cpp:443-492): genes -> layer APs and
 // lead positions.
-void prepare_sim(ekg_heart *h, const double *genes, int n_genes, double *layer_k, double *leads, double *violation) {
+void prepare_sim(ekg_heart *h, const double *genes, int n_genes, double *layer_k, double *leads, double *violation,
+                 std::vector<LayerFit> &fits) {
     const EvalSettings &es = h->es;
     EKG_CHECK(h->has_eval, EKG_ERR_BAD_INPUT, "evaluation settings not set for this heart");
     const int nw = es.gm.n_free() * (es.gm.interpolation == 2 ? 3 : 2);
@@ -1108,7 +1109,104 @@ void prepare_sim(ekg_heart *h, const double *genes, int n_genes, double *layer_k
     } else {
         std::copy(h->leads0.begin(), h->leads0.end(), leads);
     }
-    layer_aps_from_genes(es.gm, h->dev.nlayers, genes, layer_k, violation);
+    layer_aps_setup(es.gm, h->dev.nlayers, genes, layer_k, violation, fits);
+}
+
+// Host worker threads for the FP64 layer-AP fits of a pass (independent per simulation and layer,
+// see host_model.h): run(n, f) calls f(begin, end) on contiguous parts of [0, n), one per thread,
+// the caller taking the first; one pass at a time.
+class HostPool {
+  public:
+    static HostPool &get() {
+        static HostPool p;
+        return p;
+    }
+    void run(size_t n, const std::function<void(size_t, size_t)> &f) {
+        std::lock_guard<std::mutex> one(run_mu_);
+        const size_t parts = std::min(n, workers_.size() + 1);
+        if (parts <= 1) {
+            f(0, n);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            job_ = &f;
+            n_ = n;
+            parts_ = parts;
+            remaining_ = (int)parts - 1;
+            failed_ = false;
+            ++gen_;
+        }
+        cv_.notify_all();
+        bool mine_failed = false;
+        try {
+            f(0, n / parts);
+        } catch (...) {
+            mine_failed = true;
+        }
+        std::unique_lock<std::mutex> lk(mu_);
+        done_cv_.wait(lk, [&] { return remaining_ == 0; });
+        job_ = nullptr;
+        if (mine_failed || failed_) throw Error{EKG_ERR_OUT_OF_MEMORY, "host worker failed (allocation)"};
+    }
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : workers_) t.join();
+    }
+
+  private:
+    HostPool() {
+        const unsigned hc = std::thread::hardware_concurrency();
+        const size_t nw = hc > 1 ? std::min<unsigned>(hc, 32) - 1 : 0;
+        for (size_t w = 0; w < nw; ++w) workers_.emplace_back([this, w] { loop(w + 1); });
+    }
+    void loop(size_t part) {
+        int seen = 0;
+        for (;;) {
+            const std::function<void(size_t, size_t)> *f;
+            size_t n, parts;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+                f = job_;
+                n = n_;
+                parts = parts_;
+            }
+            bool bad = false;
+            if (part < parts) {
+                try {
+                    (*f)(n * part / parts, n * (part + 1) / parts);
+                } catch (...) {
+                    bad = true;
+                }
+                std::lock_guard<std::mutex> lk(mu_);
+                failed_ = failed_ || bad;
+                if (--remaining_ == 0) done_cv_.notify_all();
+            }
+        }
+    }
+    std::vector<std::thread> workers_;
+    std::mutex run_mu_, mu_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(size_t, size_t)> *job_ = nullptr;
+    size_t n_ = 0, parts_ = 0;
+    int gen_ = 0, remaining_ = 0;
+    bool stop_ = false, failed_ = false;
+};
+
+// The fits of a pass, in parallel when there is more than one.
+void run_fits(std::vector<LayerFitJob> &jobs) {
+    if (jobs.size() <= 1) {
+        layer_aps_run_fits(jobs.data(), jobs.size());
+        return;
+    }
+    HostPool::get().run(jobs.size(), [&](size_t b, size_t e) { layer_aps_run_fits(jobs.data() + b, e - b); });
 }
 
 // SimImplementation::calculateFitness (sim.cpp:600-702) from the device's per-lead comparison
@@ -1220,11 +1318,16 @@ void eval_many(ekg_heart *h, int n_sims, const double *genes, int n_genes, doubl
     std::vector<char> done(n_sims, 1);
     std::vector<double> acrit(n_sims, 2.0);
     std::vector<std::vector<double>> approx(n_sims);
+    std::vector<LayerFitJob> jobs;
+    std::vector<LayerFit> fits;
     for (int s = 0; s < n_sims; ++s) {
+        fits.clear();
         prepare_sim(h, genes + (size_t)s * n_genes, n_genes, &lk_all[(size_t)s * nl * 9], &leads_all[(size_t)s * L * 3],
-                    &viol[s]);
-        done[s] = approx_gate(h, &lk_all[(size_t)s * nl * 9], acrit[s], approx[s]);
+                    &viol[s], fits);
+        for (const LayerFit &f : fits) jobs.push_back(LayerFitJob{f, &lk_all[(size_t)s * nl * 9]});
     }
+    run_fits(jobs);
+    for (int s = 0; s < n_sims; ++s) done[s] = approx_gate(h, &lk_all[(size_t)s * nl * 9], acrit[s], approx[s]);
     const int ncl = h->es.n_crit_leads;
     std::vector<double> crit2((size_t)n_sims * std::max(1, ncl) * 2);
     device_pass(h, n_sims, lk_all.data(), leads_all.data(), ecg, crit2.data(), ncl, h->es.comparison_mode);
@@ -1514,7 +1617,11 @@ int ekg_layer_aps(const ekg_eval_config *c, int32_t n_layers, const double *gene
         gm.k_min.assign(c->k_min, c->k_min + 9);
         gm.k_max.assign(c->k_max, c->k_max + 9);
         gm.free_mask = c->free_k_mask & 0x1ffu;
-        layer_aps_from_genes(gm, n_layers, genes, layer_k_out, violation_out);
+        std::vector<LayerFit> fits;
+        layer_aps_setup(gm, n_layers, genes, layer_k_out, violation_out, fits);
+        std::vector<LayerFitJob> jobs;
+        for (const LayerFit &f : fits) jobs.push_back(LayerFitJob{f, layer_k_out});
+        run_fits(jobs);
     });
 }
 

@@ -491,72 +491,73 @@ void combine(AP &dst, const AP &s1, const AP &s2, double ratio) {
 }
 }  // namespace
 
-void layer_aps_from_genes(const GeneModel &m, int nl, const double *genes, double *out_k, double *violation) {
-    std::vector<AP> aps((size_t)nl);
-    for (AP &a : aps) std::fill(a.k, a.k + 9, 0.0);
+void layer_aps_setup(const GeneModel &m, int nl, const double *genes, double *out_k, double *violation,
+                     std::vector<LayerFit> &fits) {
+    std::fill(out_k, out_k + 9 * (size_t)nl, 0.0);
     int gi = 0;
     double viol = 0.0;
-    auto fill = [&](const std::vector<double> &base) {
-        AP t;
-        std::copy(base.begin(), base.begin() + 9, t.k);
+    auto fill = [&](const std::vector<double> &base, int row) {
+        double *k = out_k + 9 * (size_t)row;
+        std::copy(base.begin(), base.begin() + 9, k);
         for (int i = 0; i < 9; ++i)
             if (m.free_mask & (1u << i)) {
-                t.k[i] = genes[gi++];
-                if (t.k[i] < m.k_min[i]) viol += m.k_min[i] - t.k[i];
-                else if (t.k[i] > m.k_max[i]) viol += t.k[i] - m.k_max[i];
+                k[i] = genes[gi++];
+                if (k[i] < m.k_min[i]) viol += m.k_min[i] - k[i];
+                else if (k[i] > m.k_max[i]) viol += k[i] - m.k_max[i];
             }
-        return t;
     };
+    if (m.interpolation == 1) {
+        fill(m.base.front(), 0);
+        fill(m.base.back(), nl - 1);
+        for (int i = 1; i < nl - 1; ++i) fits.push_back(LayerFit{i, 0, nl - 1, i / double(nl - 1)});
+    } else {
+        const int mid = (int)std::floor(m.mid_position * (nl - 1) + 0.5);
+        fill(m.base.front(), 0);
+        fill(m.base.back(), mid);  // the mid AP starts from the last base AP (sim.cpp:855-864)
+        fill(m.base.back(), nl - 1);
+        for (int i = 1; i + 1 < nl; ++i) {
+            if (i < mid) fits.push_back(LayerFit{i, 0, mid, i / double(mid)});
+            else if (i > mid) fits.push_back(LayerFit{i, mid, nl - 1, (i - mid) / double(nl - mid - 1)});
+        }
+    }
+    *violation = viol;
+}
+
+void layer_aps_run_fits(const LayerFitJob *jobs, size_t n) {
     static const double kd[9] = {0, 0, 0, 0.001, 0, 0.00005, 0.0005, 0.01, 0.2};
     AP d;
     std::copy(kd, kd + 9, d.k);
-    // The interpolation evaluator (connectors between two border APs) is only needed for layers
-    // between the gene-set APs; it is built when first used and rebuilt only when its border
-    // APs change, which leaves every result as in sim.cpp:751-916.
+    // the interpolation evaluator (connectors between the two border APs) is rebuilt only when the
+    // border APs change from one fit to the next
     Evaluator ev;
-    int ev_border = -1;  // 0: (front, back), 1: (front, mid), 2: (mid, back)
-    auto border = [&](int which, const AP &a, const AP &b) {
-        if (ev_border != which) {
+    double key[18];
+    bool have = false;
+    for (size_t j = 0; j < n; ++j) {
+        const LayerFit &f = jobs[j].fit;
+        double *k = jobs[j].out_k;
+        AP a, b;
+        std::copy(k + 9 * (size_t)f.a, k + 9 * (size_t)f.a + 9, a.k);
+        std::copy(k + 9 * (size_t)f.b, k + 9 * (size_t)f.b + 9, b.k);
+        if (!have || std::memcmp(key, a.k, 72) != 0 || std::memcmp(key + 9, b.k, 72) != 0) {
             ev.set_border(a, b);
-            ev_border = which;
+            std::copy(a.k, a.k + 9, key);
+            std::copy(b.k, b.k + 9, key + 9);
+            have = true;
         }
-    };
-    const std::vector<double> &front = m.base.front(), &back = m.base.back();
-    if (m.interpolation == 1) {
-        aps[0] = fill(front);
-        aps[nl - 1] = fill(back);
-        for (int i = 1; i < nl - 1; ++i) {
-            const double ratio = i / double(nl - 1);
-            border(0, aps[0], aps[nl - 1]);
-            ev.set_ratio(ratio);
-            aps[i] = aps[i - 1];
-            combine(aps[i], aps[0], aps[nl - 1], ratio);
-            steepest(ev, aps[i], d, 0.5, 1e-3, 100);
-        }
-    } else {
-        const size_t mid = (size_t)std::floor(m.mid_position * (nl - 1) + 0.5);
-        aps[0] = fill(front);
-        aps[mid] = fill(back);  // the mid AP starts from the last base AP (sim.cpp:855-864)
-        aps[nl - 1] = fill(back);
-        for (size_t i = 1; i + 1 < (size_t)nl; ++i) {
-            if (i < mid) {
-                const double ratio = i / double(mid);
-                border(1, aps[0], aps[mid]);
-                ev.set_ratio(ratio);
-                aps[i] = aps[i - 1];
-                combine(aps[i], aps[0], aps[mid], ratio);
-            } else if (i > mid) {
-                const double ratio = (i - mid) / double(nl - mid - 1);
-                border(2, aps[mid], aps[nl - 1]);
-                ev.set_ratio(ratio);
-                aps[i] = aps[i - 1];
-                combine(aps[i], aps[mid], aps[nl - 1], ratio);
-            }
-            if (i != mid) steepest(ev, aps[i], d, 0.5, 1e-3, 100);
-        }
+        ev.set_ratio(f.ratio);
+        AP x;
+        combine(x, a, b, f.ratio);
+        steepest(ev, x, d, 0.5, 1e-3, 100);
+        std::copy(x.k, x.k + 9, k + 9 * (size_t)f.layer);
     }
-    for (int i = 0; i < nl; ++i) std::copy(aps[i].k, aps[i].k + 9, out_k + 9 * i);
-    *violation = viol;
+}
+
+void layer_aps_from_genes(const GeneModel &m, int nl, const double *genes, double *out_k, double *violation) {
+    std::vector<LayerFit> fits;
+    layer_aps_setup(m, nl, genes, out_k, violation, fits);
+    std::vector<LayerFitJob> jobs;
+    for (const LayerFit &f : fits) jobs.push_back(LayerFitJob{f, out_k});
+    layer_aps_run_fits(jobs.data(), jobs.size());
 }
 
 void move_leads(int n, const double *orig, const double *disp, double *out) {

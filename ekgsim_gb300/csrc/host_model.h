@@ -86,6 +86,23 @@ struct GeneModel {
 // simUsingBorderAps / simUsingBorderAndMidAps (sim.cpp:751-916): layer APs [nl][9] and the
 // violation of the gene-set APs (sim.cpp:582-596).
 void layer_aps_from_genes(const GeneModel &m, int n_layers, const double *genes, double *out_k, double *violation);
+// The same in two phases, so that the fits of many layers and simulations can run in parallel:
+// layer_aps_setup writes the gene-set APs (rows of out_k) and the violation and lists the fits of the
+// interpolated layers; each fit (steepest descent from the interpolated start, nonlinearFit.h:92-168)
+// reads its two border rows and writes its own row, independently of the other fits (the start
+// of layer i is fully overwritten by the interpolation, sim.cpp:800-830), so any order or split gives
+// the same doubles.
+struct LayerFit {
+    int layer, a, b;  // fitted row, border rows
+    double ratio;
+};
+struct LayerFitJob {
+    LayerFit fit;
+    double *out_k;    // the simulation's [nl][9]
+};
+void layer_aps_setup(const GeneModel &m, int n_layers, const double *genes, double *out_k, double *violation,
+                     std::vector<LayerFit> &fits);
+void layer_aps_run_fits(const LayerFitJob *jobs, size_t n);
 // EkgSim::loadMeasuringPoints basis + moveMeasuringPoints (simlib/sim_lib.h:167-208).
 void move_leads(int n, const double *orig_zyx, const double *disp_uv, double *out_zyx);
 

@@ -313,3 +313,30 @@ def test_single_simulation_batched_form(engine):
         moved = O.move_leads(leads, g[12:12 + 2 * spec.n_leads].reshape(-1, 2))
         ref = O.run(layer, at, lk, moved, "3D4", 0.0, float(steps), 1.0)
         assert rel_l2(ecg, ref) <= ECG_TOL
+
+
+def test_bsm_256_64lead_batched(engine):
+    """The large body-surface-map configuration at full size: 256^3 ellipsoid, 10 layers with seeded
+    delays, 64 electrodes on an ellipsoidal torso, 800 steps, a batch of 64 vectors.  Activation times
+    bit-exact; one simulation of the batch against the FP64 oracle."""
+    from ekgsim_gb300.engine import Heart
+    c = synth.config(4)
+    spec, steps, batch = c["spec"], c["steps"], c["batch"]
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    h = Heart.create(engine, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+    at, layer = O.activation(grid, tm)
+    assert np.array_equal(h.activation().view(np.int64), at.view(np.int64))
+    target = synth.analytic_target(spec.n_leads, steps, 6)
+    h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], [t for t in target], mid_position=0.6)
+    genes = np.stack([synth.genes_for(spec, r, 4) for r in range(batch)])
+    crit, viol, ecg = h.eval_batch(genes, want_ecg=True)
+    assert np.isfinite(crit).all() and np.isfinite(ecg).all()
+    g = genes[5]
+    lk = O.layer_aps(spec.n_layers, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8],
+                     "endo-mid-epi", 0.6, g[:12])[0]
+    moved = O.move_leads(leads, g[12:12 + 2 * spec.n_leads].reshape(-1, 2))
+    ref = O.run(layer, at, lk, moved, "3D4", 0.0, float(steps), 1.0)
+    assert rel_l2(ecg[5], ref) <= ECG_TOL
+    h.close()
