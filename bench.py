@@ -293,6 +293,10 @@ def run_ours(args):
         batch = args.batch
     grid, tm, leads_zyx, genes, target = build_inputs(spec, steps, batch, cfg_index)
     eng = E.Engine(d.local)
+    # a small heart first, so that the measured heart's set-up does not include module loading
+    ws = synth.small_spec(16)
+    E.Heart.create(eng, synth.ellipsoid_heart(ws), synth.transfer_matrix(3, ws.delays), np.array([[40.0, 40.0, 40.0]]),
+                   "3D4", 0.0, 10.0, 1.0).close()
     t0 = time.perf_counter()
     heart = E.Heart.create(eng, grid, tm, leads_zyx, "3D4", 0.0, float(steps), 1.0)
     setup_s = time.perf_counter() - t0
@@ -388,6 +392,17 @@ def run_ours(args):
         "device_ms": {"prep": bm["prep_ms"] / args.steps, "operand": bm["operand_ms"] / args.steps,
                       "contract": bm["contract_ms"] / args.steps, "tail": bm["tail_ms"] / args.steps},
         "roofline": roof,
+        # the activation-time relaxation (once per heart): N^3 x 1 B layers in + N^3 x 8 B times out
+        "ca": {"kernel": "k_ca_round", "rounds": int(info.ca_rounds), "ms": info.ca_ms,
+               "algorithmic_bytes": 9 * int(info.n_cells),
+               "achieved_gbs": 9 * info.n_cells / (info.ca_ms / 1000.0) / 1e9 if info.ca_ms > 0 else None,
+               "frac": 9 * info.n_cells / (info.ca_ms / 1000.0) / 1e9 / hbm if info.ca_ms > 0 else None},
+        # the dense lead contraction's algorithmic flops (2 x L x 3V x T per simulation) over the
+        # whole device step; the engine does not perform that contraction (W-form over de-duplicated
+        # APs, static-lead basis, band split), so this rate can exceed the tensor peak
+        "contraction_equivalent": {"flops_per_sim": 2.0 * info.n_leads * 3 * info.n_voxels * steps,
+                                   "tflops": 2.0 * info.n_leads * 3 * info.n_voxels * steps * batch * args.steps
+                                   / (bm["total_ms"] / 1000.0) / 1e12},
         "gpu_launches": int(bm["launches"]) * args.steps,
         "clocks": clk,
     }
