@@ -44,7 +44,7 @@ using namespace ptx;
 
 namespace {
 
-constexpr int BM = 128, BKT = 64, BTHREADS = 256;
+constexpr int BM = 128, BKT = 64;
 constexpr int LF_THREADS = 128;  // threads of the moved-lead operand kernel
 
 __device__ __forceinline__ float ex2a(float x) {

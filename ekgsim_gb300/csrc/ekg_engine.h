@@ -58,7 +58,6 @@ struct BatchState {
     DBuf<float2> U, Up;                    // [rows][nl][max_ent] steady sums (U0, U1), per K part
     DBuf<float> partial;                   // [items][rows][128] raw accumulators (x2 with two bases)
     DBuf<int4> items;                      // GEMM work items
-    DBuf<int32_t> tc0, tc1;                // item range of each tile
     DBuf<int32_t> ti0, ti1;                // [ntt][nl] item range of each (tile, layer)
     DBuf<float> k5l;                       // [S][nl] k5 log2(e)
     DBuf<float4> lrel;                     // [S][nmove] moved lead positions relative to the voxel centre
@@ -74,7 +73,6 @@ struct PassPlan {
     std::vector<float> coef;               // [S][nl][J]
     std::vector<double> k3;                // [S][nl]
     std::vector<int4> items;               // band GEMM work items, grouped by tile
-    std::vector<int32_t> tc0, tc1;         // [ntt] item range of each tile
     std::vector<int32_t> ti0, ti1;         // [ntt][nl] item range of each (tile, layer)
     std::vector<float> k5l;                // [S][nl]
     std::vector<float4> lrel;              // [S][nmove]

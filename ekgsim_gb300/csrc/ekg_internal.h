@@ -183,7 +183,7 @@ struct BandArgs {
     int max_ent = 1, nb = 1;
     const int32_t *ti0 = nullptr, *ti1 = nullptr;  // [ntt][nl] item range of (tile, layer)
     const int32_t *c8s = nullptr, *nent = nullptr, *esplit8 = nullptr, *ls0 = nullptr, *ls1 = nullptr;
-    const int32_t *ent = nullptr, *tc0 = nullptr, *tc1 = nullptr;
+    const int32_t *ent = nullptr;
     const int64_t *goff = nullptr;
     const float *gtab = nullptr;
     const float *E = nullptr, *F = nullptr, *partial = nullptr;

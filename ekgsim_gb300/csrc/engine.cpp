@@ -761,12 +761,9 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
             for (size_t i = 0; i < B.band_s0.size(); ++i) cnt += (B.band_s1[i] - B.band_s0[i] + per - 1) / per;
             if (cnt * P.ntiles <= target || per >= total) break;
         }
-        P.tc0.assign(ntt, 0);
-        P.tc1.assign(ntt, 0);
         P.ti0.assign((size_t)ntt * nl, 0);
         P.ti1.assign((size_t)ntt * nl, 0);
         for (int j = 0; j < ntt; ++j) {
-            P.tc0[j] = (int32_t)P.items.size();
             for (int i = 0; i < nl; ++i) {
                 const int s0 = B.band_s0[(size_t)i * ntt + j], n = B.band_s1[(size_t)i * ntt + j] - s0;
                 P.ti0[(size_t)j * nl + i] = P.ti1[(size_t)j * nl + i] = (int32_t)P.items.size();
@@ -776,7 +773,6 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
                     P.items.push_back(make_int4(j, s0 + (int)((int64_t)n * c / nc), s0 + (int)((int64_t)n * (c + 1) / nc), i));
                 P.ti1[(size_t)j * nl + i] = (int32_t)P.items.size();
             }
-            P.tc1[j] = (int32_t)P.items.size();
         }
         P.nitems = (int)P.items.size();
         // per-simulation k5 and moved lead positions for the operand kernel
@@ -838,8 +834,6 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
                 B.Up.alloc(ub * band_u_parts());
             }
             if (B.items.n < (size_t)std::max(1, P.nitems)) B.items.alloc(std::max(1, P.nitems));
-            B.tc0.alloc(B.ntt);
-            B.tc1.alloc(B.ntt);
             B.ti0.alloc((size_t)B.ntt * D.nlayers);
             B.ti1.alloc((size_t)B.ntt * D.nlayers);
             EKG_CUDA(cudaMemcpyAsync(B.ti0.p, P.ti0.data(), P.ti0.size() * 4, cudaMemcpyHostToDevice, s));
@@ -848,8 +842,6 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
             if (B.lrel.n < P.lrel.size()) B.lrel.alloc(P.lrel.size());
             if (P.nitems > 0)
                 EKG_CUDA(cudaMemcpyAsync(B.items.p, P.items.data(), P.nitems * sizeof(int4), cudaMemcpyHostToDevice, s));
-            EKG_CUDA(cudaMemcpyAsync(B.tc0.p, P.tc0.data(), B.ntt * 4, cudaMemcpyHostToDevice, s));
-            EKG_CUDA(cudaMemcpyAsync(B.tc1.p, P.tc1.data(), B.ntt * 4, cudaMemcpyHostToDevice, s));
             EKG_CUDA(cudaMemcpyAsync(B.k5l.p, P.k5l.data(), P.k5l.size() * 4, cudaMemcpyHostToDevice, s));
             EKG_CUDA(cudaMemcpyAsync(B.lrel.p, P.lrel.data(), P.lrel.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
         }
@@ -892,8 +884,6 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             U.ls0 = B.ls0.p;
             U.ls1 = B.ls1.p;
             U.ent = B.ent.p;
-            U.tc0 = B.tc0.p;
-            U.tc1 = B.tc1.p;
             U.goff = B.goff.p;
             U.gtab = B.gtab.p;
             U.E = B.E.p;
