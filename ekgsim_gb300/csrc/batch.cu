@@ -172,7 +172,8 @@ struct InteriorField {
 constexpr uint32_t VOX_INTERIOR = 1u << 31;  // every neighbour present, out-neighbour offsets sum to 0
 constexpr uint32_t VOX_AP_END = 1u << 30;    // last voxel of its AP (voxels are grouped by AP)
 
-// closed form of the interior field for m = r - v (used for |m|^2 >= INTERIOR_S_MIN)
+// closed form of the interior field for m = r - v, used where |m|^2 >= INTERIOR_S_MIN for every lead
+// of the lane (a lead displaced towards the heart takes the exact sum for the voxels near it)
 constexpr float INTERIOR_S_MIN = 400.f;
 __device__ __forceinline__ float sq3(float4 pos, float4 r) {
     const float mz = r.x - pos.x, my = r.y - pos.y, mx = r.z - pos.z;
