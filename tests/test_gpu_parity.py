@@ -340,3 +340,41 @@ def test_bsm_256_64lead_batched(engine):
     ref = O.run(layer, at, lk, moved, "3D4", 0.0, float(steps), 1.0)
     assert rel_l2(ecg[5], ref) <= ECG_TOL
     h.close()
+
+
+def _batched_general(engine, spec, nhood, start, length, dt, n, seed=9):
+    """Batched evaluation (eval_batch) with any neighbourhood and time axis against the oracle."""
+    from ekgsim_gb300.engine import Heart
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    h = Heart.create(engine, grid, tm, leads, nhood, start, length, dt)
+    steps = h.steps
+    target = synth.analytic_target(spec.n_leads, steps, seed)
+    h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], [t for t in target], mid_position=0.6)
+    genes = np.stack([synth.genes_for(spec, 60 + r, 0) for r in range(n)])
+    _, _, ecg_b = h.eval_batch(genes, want_ecg=True)
+    at, layer = O.activation(grid, tm)
+    worst = 0.0
+    for i in (0, n - 1):
+        g = genes[i]
+        lk = O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], "endo-mid-epi",
+                         0.6, g[:12])[0]
+        moved = O.move_leads(leads, g[12:12 + 2 * spec.n_leads].reshape(-1, 2))
+        ref = O.run(layer, at, lk, moved, nhood, start, length, dt)
+        worst = max(worst, rel_l2(ecg_b[i], ref))
+    h.close()
+    return worst
+
+
+@pytest.mark.parametrize("nhood", ["cube", "2D8", "2D4"])
+def test_batched_form_neighbourhoods(engine, nhood):
+    """Batched form with the general-neighbourhood operand kernel (the 26-neighbour cube also takes
+    the closed-form interior field; the 2-D sets have no cube symmetry and keep the exact sum)."""
+    assert _batched_general(engine, synth.small_spec(24, n_leads=3), nhood, 0.0, 250.0, 1.0, 5) <= ECG_TOL
+
+
+def test_batched_form_fine_time_axis(engine):
+    """dt = 1/32 ms over 100 ms (3200 steps): tiles of 4 ms, bands spanning several tiles and more
+    tiles before the first all-steady one than steady-prefix entries, so tiles share entries."""
+    assert _batched_general(engine, synth.small_spec(32, n_leads=2), "3D4", 2.0, 100.0, 0.03125, 4) <= ECG_TOL
