@@ -99,6 +99,119 @@ void interior_field(HeartDev &D) {
 }
 
 // ------------------------------------------------------------------ heart setup
+// Host worker threads (heart set-up, the FP64 layer-AP fits of a pass): run(n, f) calls f(begin, end)
+// on contiguous parts of [0, n), one per thread, the caller taking the first; one job at a time.
+class HostPool {
+  public:
+    static HostPool &get() {
+        static HostPool p;
+        return p;
+    }
+    void run(size_t n, const std::function<void(size_t, size_t)> &f) {
+        std::lock_guard<std::mutex> one(run_mu_);
+        const size_t parts = std::min(n, workers_.size() + 1);
+        if (parts <= 1) {
+            f(0, n);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            job_ = &f;
+            n_ = n;
+            parts_ = parts;
+            remaining_ = (int)parts - 1;
+            failed_ = false;
+            ++gen_;
+        }
+        cv_.notify_all();
+        bool mine_failed = false;
+        try {
+            f(0, n / parts);
+        } catch (...) {
+            mine_failed = true;
+        }
+        std::unique_lock<std::mutex> lk(mu_);
+        done_cv_.wait(lk, [&] { return remaining_ == 0; });
+        job_ = nullptr;
+        if (mine_failed || failed_) throw Error{EKG_ERR_OUT_OF_MEMORY, "host worker failed (allocation)"};
+    }
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : workers_) t.join();
+    }
+
+  private:
+    HostPool() {
+        const unsigned hc = std::thread::hardware_concurrency();
+        const size_t nw = hc > 1 ? std::min<unsigned>(hc, 32) - 1 : 0;
+        for (size_t w = 0; w < nw; ++w) workers_.emplace_back([this, w] { loop(w + 1); });
+    }
+    void loop(size_t part) {
+        int seen = 0;
+        for (;;) {
+            const std::function<void(size_t, size_t)> *f;
+            size_t n, parts;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+                f = job_;
+                n = n_;
+                parts = parts_;
+            }
+            bool bad = false;
+            if (part < parts) {
+                try {
+                    (*f)(n * part / parts, n * (part + 1) / parts);
+                } catch (...) {
+                    bad = true;
+                }
+                std::lock_guard<std::mutex> lk(mu_);
+                failed_ = failed_ || bad;
+                if (--remaining_ == 0) done_cv_.notify_all();
+            }
+        }
+    }
+    std::vector<std::thread> workers_;
+    std::mutex run_mu_, mu_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(size_t, size_t)> *job_ = nullptr;
+    size_t n_ = 0, parts_ = 0;
+    int gen_ = 0, remaining_ = 0;
+    bool stop_ = false, failed_ = false;
+};
+
+// Sorts v in parallel: parts sorted on the pool, then merged pairwise (the result is the one
+// std::sort gives, the keys being distinct).
+template <class T>
+void parallel_sort(std::vector<T> &v) {
+    const size_t n = v.size();
+    const size_t parts = std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), n / 65536));
+    if (parts <= 1) {
+        std::sort(v.begin(), v.end());
+        return;
+    }
+    std::vector<size_t> cut(parts + 1);
+    for (size_t i = 0; i <= parts; ++i) cut[i] = n * i / parts;
+    HostPool::get().run(parts, [&](size_t b, size_t e) {
+        for (size_t i = b; i < e; ++i) std::sort(v.begin() + cut[i], v.begin() + cut[i + 1]);
+    });
+    for (size_t w = 1; w < parts; w *= 2) {
+        const size_t pairs = (parts + 2 * w - 1) / (2 * w);
+        HostPool::get().run(pairs, [&](size_t b, size_t e) {
+            for (size_t q = b; q < e; ++q) {
+                const size_t lo = 2 * w * q, mid = std::min(parts, lo + w), hi = std::min(parts, lo + 2 * w);
+                if (mid < hi) std::inplace_merge(v.begin() + cut[lo], v.begin() + cut[mid], v.begin() + cut[hi]);
+            }
+        });
+    }
+}
+
 void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     auto t0 = std::chrono::steady_clock::now();
     EKG_CHECK(d && d->layers && d->transfer && d->leads_zyx, EKG_ERR_BAD_INPUT, "null heart description field");
@@ -224,44 +337,52 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
         EKG_CUDA(cudaStreamSynchronize(s));
     }
 
-    // de-duplicate (layer, at) pairs: sorted by (layer, at); the reference numbers them by first
-    // appearance in raster order (simlib/simulator.cpp:570-590), kept for ekg_heart_ap_index
-    std::vector<int64_t> vox;
-    vox.reserve(n / 4);
+    // de-duplicate (layer, at) pairs: voxels sorted by (layer, at, cell index) -- as 16-byte keys
+    // (layer, at bits (non-negative doubles order as their bit patterns), cell) sorted on the host
+    // pool -- then equal (layer, at) runs are the APs.  The reference numbers APs by first
+    // appearance in raster order (simlib/simulator.cpp:570-590); that numbering is derived on demand.
+    struct VKey {
+        uint64_t hi, lo;  // (layer << 56 | cell), at bits  -- compared as (layer, at, cell)
+        bool operator<(const VKey &o) const {
+            const uint64_t la = hi >> 56, lb = o.hi >> 56;
+            if (la != lb) return la < lb;
+            if (lo != o.lo) return lo < o.lo;
+            return hi < o.hi;
+        }
+    };
+    EKG_CHECK(n < ((int64_t)1 << 56), EKG_ERR_BAD_INPUT, "grid too large");
+    std::vector<VKey> keys;
+    keys.reserve(n / 4);
     for (int64_t i = 0; i < n; ++i)
-        if (lay[i]) vox.push_back(i);
-    const int64_t nv = (int64_t)vox.size();
+        if (lay[i]) {
+            uint64_t b;
+            std::memcpy(&b, &h->at_host[i], 8);
+            keys.push_back(VKey{((uint64_t)lay[i] << 56) | (uint64_t)i, b});
+        }
+    parallel_sort(keys);
+    const int64_t nv = (int64_t)keys.size();
     h->nvox = nv;
     D.nvox = nv;
-    std::vector<int64_t> ord(vox);
-    std::sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) {
-        if (lay[a] != lay[b]) return lay[a] < lay[b];
-        if (h->at_host[a] != h->at_host[b]) return h->at_host[a] < h->at_host[b];
-        return a < b;
-    });
-    // groups
+    std::vector<int64_t> ord(nv);
+    for (int64_t i = 0; i < nv; ++i) ord[i] = (int64_t)(keys[i].hi & (((uint64_t)1 << 56) - 1));
+    // groups (APs): runs of equal (layer, at); the last voxel of each is flagged for the operand kernel
     std::vector<int64_t> gstart;  // index into ord
-    for (int64_t i = 0; i < nv; ++i)
-        if (i == 0 || lay[ord[i]] != lay[ord[i - 1]] || h->at_host[ord[i]] != h->at_host[ord[i - 1]]) gstart.push_back(i);
+    std::vector<uint8_t> gend(nv, 0);
+    for (int64_t i = 0; i < nv; ++i) {
+        if (i == 0 || (keys[i].hi >> 56) != (keys[i - 1].hi >> 56) || keys[i].lo != keys[i - 1].lo) {
+            gstart.push_back(i);
+            if (i > 0) gend[i - 1] = 1;
+        }
+    }
+    if (nv > 0) gend[nv - 1] = 1;
+    std::vector<VKey>().swap(keys);
     const int64_t na = (int64_t)gstart.size();
     h->naps = na;
     D.naps = na;
     gstart.push_back(nv);
-    // reference numbering
-    {
-        std::vector<int64_t> g_of_cell(n, -1);
-        for (int64_t g = 0; g < na; ++g)
-            for (int64_t i = gstart[g]; i < gstart[g + 1]; ++i) g_of_cell[ord[i]] = g;
-        std::vector<int64_t> g2ref(na, -1);
-        int64_t next = 0;
-        h->ap_index_ref.assign(n, -1);
-        for (int64_t i = 0; i < n; ++i) {
-            const int64_t g = g_of_cell[i];
-            if (g < 0) continue;
-            if (g2ref[g] < 0) g2ref[g] = next++;
-            h->ap_index_ref[i] = g2ref[g];
-        }
-    }
+    h->vox_cell = ord;
+    h->vox_group_start = gstart;
+    h->ap_index_ref.clear();
     // padded per-layer K layout, tiles of KT APs, chunks of up to chunk_len APs inside one layer
     const int KT = 64;
     const int chunk_len = h->eng->chunk_len;
@@ -270,13 +391,9 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     std::vector<int32_t> a_layer;
     std::vector<int64_t> a_vb;
     std::vector<int32_t> c0, c1, cl;
-    std::vector<int32_t> vzyx(nv);
-    std::vector<uint32_t> vin(nv), vout(nv);
-    std::vector<float4> vpos_v(nv), vosum(nv);
     D.centre[0] = 0.5 * d->nz;
     D.centre[1] = 0.5 * d->ny;
     D.centre[2] = 0.5 * d->nx;
-    int64_t vpos = 0;
     {
         int64_t g = 0;
         for (int L = 1; L <= nl; ++L) {
@@ -288,57 +405,12 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
             const int64_t padded = (cnt + KT - 1) / KT * KT;
             for (int64_t j = 0; j < padded; ++j) {
                 a_layer.push_back(L - 1);
-                a_vb.push_back(vpos);
+                a_vb.push_back(j < cnt ? gstart[gb + j] : gstart[g]);
                 if (j < cnt) {
-                    const int64_t gg = gb + j;
-                    const double at = h->at_host[ord[gstart[gg]]];
+                    const double at = h->at_host[ord[gstart[gb + j]]];
                     a_at.push_back(at);
                     const float hi = (float)at;
                     a_hilo.push_back(make_float2(hi, (float)(at - (double)hi)));
-                    for (int64_t i = gstart[gg]; i < gstart[gg + 1]; ++i) {
-                        const int64_t c = ord[i];
-                        const int z = (int)(c / ((int64_t)d->ny * d->nx)), y = (int)((c / d->nx) % d->ny),
-                                  x = (int)(c % d->nx);
-                        vzyx[vpos] = (z << 20) | (y << 10) | x;
-                        uint32_t mi = 0, mo = 0;
-                        for (int q = 0; q < D.nnb; ++q) {
-                            const int dz = D.nb_dif[3 * q], dy = D.nb_dif[3 * q + 1], dx = D.nb_dif[3 * q + 2];
-                            int z2 = z + dz, y2 = y + dy, x2 = x + dx;
-                            if (z2 >= 0 && z2 < d->nz && y2 >= 0 && y2 < d->ny && x2 >= 0 && x2 < d->nx &&
-                                lay[((int64_t)z2 * d->ny + y2) * d->nx + x2])
-                                mi |= 1u << q;
-                            z2 = z - dz;
-                            y2 = y - dy;
-                            x2 = x - dx;
-                            if (z2 >= 0 && z2 < d->nz && y2 >= 0 && y2 < d->ny && x2 >= 0 && x2 < d->nx &&
-                                lay[((int64_t)z2 * d->ny + y2) * d->nx + x2])
-                                mo |= 1u << q;
-                        }
-                        vin[vpos] = mi;
-                        vout[vpos] = mo;
-                        float oz = 0, oy = 0, ox = 0;
-                        for (int q = 0; q < D.nnb; ++q)
-                            if (mo & (1u << q)) {
-                                oz += D.nb_dif[3 * q];
-                                oy += D.nb_dif[3 * q + 1];
-                                ox += D.nb_dif[3 * q + 2];
-                            }
-                        uint32_t mbits = mi;
-                        // flags for the moved-lead operand kernel (batch.cu): interior voxel (closed-form
-                        // field), last voxel of its AP
-                        if (D.interior_mask && mi == D.interior_mask && oz == 0 && oy == 0 && ox == 0) {
-                            mbits |= 1u << 31;
-                            ++D.n_interior;
-                        }
-                        if (i + 1 == gstart[gg + 1]) mbits |= 1u << 30;
-                        float mf;
-                        std::memcpy(&mf, &mbits, 4);
-                        // bordered coordinates (+1, simlib/simulator.cpp:458-463) relative to the centre
-                        vpos_v[vpos] = make_float4((float)((z + 1) - D.centre[0]), (float)((y + 1) - D.centre[1]),
-                                                               (float)((x + 1) - D.centre[2]), mf);
-                        vosum[vpos] = make_float4(oz, oy, ox, mo ? 1.f : 0.f);
-                        ++vpos;
-                    }
                 } else {
                     a_at.push_back(INFINITY);
                     a_hilo.push_back(make_float2(INFINITY, 0.f));
@@ -350,8 +422,65 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
                 cl.push_back(L - 1);
             }
         }
-        a_vb.push_back(vpos);
+        a_vb.push_back(nv);
     }
+    // per voxel (in AP order): packed position, neighbour masks, bordered position relative to the
+    // centre with the mask and flags, out-offset sum -- independent per voxel, on the host pool
+    std::vector<int32_t> vzyx(nv);
+    std::vector<uint32_t> vin(nv), vout(nv);
+    std::vector<float4> vpos_v(nv), vosum(nv);
+    std::vector<int64_t> interior_parts(64, 0);
+    const size_t vparts = (size_t)std::min<int64_t>(64, std::max<int64_t>(1, nv / 4096));
+    HostPool::get().run(vparts, [&](size_t pb, size_t pe) {
+        for (size_t part = pb; part < pe; ++part) {
+            int64_t cnt_int = 0;
+            for (int64_t i = nv * (int64_t)part / (int64_t)vparts; i < nv * (int64_t)(part + 1) / (int64_t)vparts; ++i) {
+                const int64_t c = ord[i];
+                const int z = (int)(c / ((int64_t)d->ny * d->nx)), y = (int)((c / d->nx) % d->ny), x = (int)(c % d->nx);
+                vzyx[i] = (z << 20) | (y << 10) | x;
+                uint32_t mi = 0, mo = 0;
+                for (int q = 0; q < D.nnb; ++q) {
+                    const int dz = D.nb_dif[3 * q], dy = D.nb_dif[3 * q + 1], dx = D.nb_dif[3 * q + 2];
+                    int z2 = z + dz, y2 = y + dy, x2 = x + dx;
+                    if (z2 >= 0 && z2 < d->nz && y2 >= 0 && y2 < d->ny && x2 >= 0 && x2 < d->nx &&
+                        lay[((int64_t)z2 * d->ny + y2) * d->nx + x2])
+                        mi |= 1u << q;
+                    z2 = z - dz;
+                    y2 = y - dy;
+                    x2 = x - dx;
+                    if (z2 >= 0 && z2 < d->nz && y2 >= 0 && y2 < d->ny && x2 >= 0 && x2 < d->nx &&
+                        lay[((int64_t)z2 * d->ny + y2) * d->nx + x2])
+                        mo |= 1u << q;
+                }
+                vin[i] = mi;
+                vout[i] = mo;
+                float oz = 0, oy = 0, ox = 0;
+                for (int q = 0; q < D.nnb; ++q)
+                    if (mo & (1u << q)) {
+                        oz += D.nb_dif[3 * q];
+                        oy += D.nb_dif[3 * q + 1];
+                        ox += D.nb_dif[3 * q + 2];
+                    }
+                uint32_t mbits = mi;
+                // flags for the moved-lead operand kernel (batch.cu): interior voxel (closed-form field),
+                // last voxel of its AP
+                if (D.interior_mask && mi == D.interior_mask && oz == 0 && oy == 0 && ox == 0) {
+                    mbits |= 1u << 31;
+                    ++cnt_int;
+                }
+                if (gend[i]) mbits |= 1u << 30;
+                float mf;
+                std::memcpy(&mf, &mbits, 4);
+                // bordered coordinates (+1, simlib/simulator.cpp:458-463) relative to the centre
+                vpos_v[i] = make_float4((float)((z + 1) - D.centre[0]), (float)((y + 1) - D.centre[1]),
+                                        (float)((x + 1) - D.centre[2]), mf);
+                vosum[i] = make_float4(oz, oy, ox, mo ? 1.f : 0.f);
+            }
+            interior_parts[part] = cnt_int;
+        }
+    });
+    D.n_interior = 0;
+    for (int64_t c : interior_parts) D.n_interior += c;
     const int64_t apad = (int64_t)a_at.size();
     EKG_CHECK(apad < (int64_t)1 << 31, EKG_ERR_BAD_INPUT, "too many distinct activation times");
     D.apad = apad;
@@ -1102,94 +1231,6 @@ void prepare_sim(ekg_heart *h, const double *genes, int n_genes, double *layer_k
     layer_aps_setup(es.gm, h->dev.nlayers, genes, layer_k, violation, fits);
 }
 
-// Host worker threads for the FP64 layer-AP fits of a pass (independent per simulation and layer,
-// see host_model.h): run(n, f) calls f(begin, end) on contiguous parts of [0, n), one per thread,
-// the caller taking the first; one pass at a time.
-class HostPool {
-  public:
-    static HostPool &get() {
-        static HostPool p;
-        return p;
-    }
-    void run(size_t n, const std::function<void(size_t, size_t)> &f) {
-        std::lock_guard<std::mutex> one(run_mu_);
-        const size_t parts = std::min(n, workers_.size() + 1);
-        if (parts <= 1) {
-            f(0, n);
-            return;
-        }
-        {
-            std::lock_guard<std::mutex> lk(mu_);
-            job_ = &f;
-            n_ = n;
-            parts_ = parts;
-            remaining_ = (int)parts - 1;
-            failed_ = false;
-            ++gen_;
-        }
-        cv_.notify_all();
-        bool mine_failed = false;
-        try {
-            f(0, n / parts);
-        } catch (...) {
-            mine_failed = true;
-        }
-        std::unique_lock<std::mutex> lk(mu_);
-        done_cv_.wait(lk, [&] { return remaining_ == 0; });
-        job_ = nullptr;
-        if (mine_failed || failed_) throw Error{EKG_ERR_OUT_OF_MEMORY, "host worker failed (allocation)"};
-    }
-    ~HostPool() {
-        {
-            std::lock_guard<std::mutex> lk(mu_);
-            stop_ = true;
-        }
-        cv_.notify_all();
-        for (auto &t : workers_) t.join();
-    }
-
-  private:
-    HostPool() {
-        const unsigned hc = std::thread::hardware_concurrency();
-        const size_t nw = hc > 1 ? std::min<unsigned>(hc, 32) - 1 : 0;
-        for (size_t w = 0; w < nw; ++w) workers_.emplace_back([this, w] { loop(w + 1); });
-    }
-    void loop(size_t part) {
-        int seen = 0;
-        for (;;) {
-            const std::function<void(size_t, size_t)> *f;
-            size_t n, parts;
-            {
-                std::unique_lock<std::mutex> lk(mu_);
-                cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
-                if (stop_) return;
-                seen = gen_;
-                f = job_;
-                n = n_;
-                parts = parts_;
-            }
-            bool bad = false;
-            if (part < parts) {
-                try {
-                    (*f)(n * part / parts, n * (part + 1) / parts);
-                } catch (...) {
-                    bad = true;
-                }
-                std::lock_guard<std::mutex> lk(mu_);
-                failed_ = failed_ || bad;
-                if (--remaining_ == 0) done_cv_.notify_all();
-            }
-        }
-    }
-    std::vector<std::thread> workers_;
-    std::mutex run_mu_, mu_;
-    std::condition_variable cv_, done_cv_;
-    const std::function<void(size_t, size_t)> *job_ = nullptr;
-    size_t n_ = 0, parts_ = 0;
-    int gen_ = 0, remaining_ = 0;
-    bool stop_ = false, failed_ = false;
-};
-
 // The fits of a pass, in parallel when there is more than one.
 void run_fits(std::vector<LayerFitJob> &jobs) {
     if (jobs.size() <= 1) {
@@ -1478,9 +1519,30 @@ int ekg_heart_activation(ekg_heart *h, double *at_out) {
     });
 }
 
+// The reference's AP numbering (first appearance in raster order, simlib/simulator.cpp:570-590),
+// derived from the AP groups when first asked for.
+void ensure_ap_ref(ekg_heart *h) {
+    if (!h->ap_index_ref.empty() || h->ncell == 0) return;
+    const int64_t n = h->ncell, na = h->naps;
+    std::vector<int64_t> g_of_cell(n, -1);
+    for (int64_t g = 0; g < na; ++g)
+        for (int64_t i = h->vox_group_start[g]; i < h->vox_group_start[g + 1]; ++i) g_of_cell[h->vox_cell[i]] = g;
+    std::vector<int64_t> g2ref(na, -1);
+    int64_t next = 0;
+    h->ap_index_ref.assign(n, -1);
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t g = g_of_cell[i];
+        if (g < 0) continue;
+        if (g2ref[g] < 0) g2ref[g] = next++;
+        h->ap_index_ref[i] = g2ref[g];
+    }
+}
+
 int ekg_heart_ap_index(ekg_heart *h, int64_t *out) {
     return guard([&] {
         EKG_CHECK(h && out, EKG_ERR_BAD_INPUT, "null argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        ensure_ap_ref(h);
         std::copy(h->ap_index_ref.begin(), h->ap_index_ref.end(), out);
     });
 }
@@ -1578,6 +1640,8 @@ double ekg_ap_value(const double *k9, double at, double t) {
 int ekg_heart_cell_ap(ekg_heart *h, int64_t index, int32_t *layer_out, double *at_out) {
     return guard([&] {
         EKG_CHECK(h && layer_out && at_out, EKG_ERR_BAD_INPUT, "null argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        ensure_ap_ref(h);
         for (int64_t i = 0; i < h->ncell; ++i)
             if (h->ap_index_ref[i] == index) {
                 *layer_out = h->layer_host[i];
