@@ -12,7 +12,8 @@ struct ekg_engine {
     int chunk_len = 512;  // APs per K chunk of the contraction (multiple of 64)
     bool umma = true;     // tensor-core contraction (EKG_CONTRACT=cuda selects the CUDA-core kernel)
     bool batched = true;  // separable batched form for multi-simulation passes (EKG_BATCHED=0 disables)
-    int batch_ctas = 0;   // target CTAs of the moved-lead GEMM (0 = two per SM)
+    int batch_ctas = 0;   // target CTAs of the moved-lead GEMM (0 = one wave)
+    bool graphs = true;   // replay repeated passes as CUDA graphs (EKG_GRAPHS=0 disables)
 };
 
 namespace ekg {
@@ -86,7 +87,18 @@ struct ekg_heart {
     cudaStream_t copy_stream = nullptr;  // early device->host copies overlapping the rest of a pass
     cudaEvent_t static_done = nullptr;   // static-lead ECG rows complete (batched form)
     uint32_t *err_host = nullptr;     // pinned copy of the kernels' error word
+    // device passes captured as CUDA graphs, keyed by everything their launches depend on
+    struct PassGraph {
+        std::vector<uint64_t> sig;
+        cudaGraphExec_t exec = nullptr;
+        uint64_t used = 0;
+        bool seen_once = false;  // the first pass with a signature runs directly
+    };
+    PassGraph graphs[4];
+    uint64_t graph_clock = 0;
     ~ekg_heart() {
+        for (PassGraph &g : graphs)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
         if (static_done) cudaEventDestroy(static_done);
         if (copy_stream) cudaStreamDestroy(copy_stream);
         if (stream) cudaStreamDestroy(stream);

@@ -994,7 +994,15 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
         BatchState &B = h->bs;
         launch_static_combine(s, D, P.J, B.J, nmove, n_sims, E.Ff.p, B.coef.p, B.k3.p, B.Q1.p, B.Q2.p, E.ecg.p);
         launches += nmove < (int)L;
-        if (mark_static) EKG_CUDA(cudaEventRecord(h->static_done, s));
+        if (mark_static) {
+            // inside a graph capture the record must be an external event node (the copy stream waits
+            // on it outside the graph)
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            EKG_CUDA(cudaStreamIsCapturing(s, &cs));
+            EKG_CUDA(cudaEventRecordWithFlags(h->static_done, s,
+                                              cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal
+                                                                                  : cudaEventRecordDefault));
+        }
         if (nmove > 0) {
             if (P.rows_used < P.rows) EKG_CUDA(cudaMemsetAsync(B.Bt.p, 0, (size_t)P.rows * D.apad * 4, s));
             BandArgs U;
@@ -1094,6 +1102,78 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
     g_launch_count = launches;
 }
 
+// Everything the launches of compute() depend on: the pass shape and every device pointer it passes.
+std::vector<uint64_t> pass_signature(const ekg_heart *h, const PassPlan &P, int ncl, int mode, bool mark_static) {
+    const EvalDev &E = h->ev;
+    const BatchState &B = h->bs;
+    auto u = [](const void *p) { return (uint64_t)(uintptr_t)p; };
+    std::vector<uint64_t> v = {(uint64_t)P.batch, (uint64_t)P.n_sims, (uint64_t)P.nmove, (uint64_t)P.J,
+                               (uint64_t)P.two_bases, (uint64_t)P.rows, (uint64_t)P.rows_used, (uint64_t)P.ntiles,
+                               (uint64_t)P.nitems, (uint64_t)ncl, (uint64_t)mode, (uint64_t)mark_static,
+                               (uint64_t)h->cpre_on, (uint64_t)h->any_k0, (uint64_t)h->eng->umma, (uint64_t)B.J,
+                               (uint64_t)B.max_ent, (uint64_t)B.ntt};
+    for (const void *p : {(const void *)E.layer_k.p, (const void *)E.cpre.p, (const void *)E.F.p, (const void *)E.Ff.p,
+                          (const void *)E.layer_c.p, (const void *)E.ecg.p, (const void *)E.crit.p, (const void *)E.err.p,
+                          (const void *)E.targets.p, (const void *)E.target_len.p, (const void *)E.target_off.p,
+                          (const void *)E.W.p, (const void *)E.Wp.p, (const void *)E.partial.p, (const void *)E.k0w.p,
+                          (const void *)E.leads.p, (const void *)B.coef.p, (const void *)B.k3.p, (const void *)B.Q1.p,
+                          (const void *)B.Q2.p, (const void *)B.Bt.p, (const void *)B.P1.p, (const void *)B.U.p,
+                          (const void *)B.Up.p, (const void *)B.partial.p, (const void *)B.items.p, (const void *)B.ti0.p,
+                          (const void *)B.ti1.p, (const void *)B.k5l.p, (const void *)B.lrel.p, (const void *)B.hconst.p,
+                          (const void *)B.c8s.p, (const void *)B.nent.p, (const void *)B.esplit8.p, (const void *)B.ls0.p,
+                          (const void *)B.ls1.p, (const void *)B.ent.p, (const void *)B.goff.p, (const void *)B.gtab.p,
+                          (const void *)B.E.p, (const void *)B.work.p, (const void *)h->W0.p})
+        v.push_back(u(p));
+    return v;
+}
+
+// compute() as a CUDA graph: the first pass with a signature runs directly (it also performs the
+// launchers' one-time set-up), the second is captured (thread-local capture on the heart's stream)
+// and instantiated, later ones replay it.  Up to four graphs per heart, least recently used out.
+void run_pass(ekg_heart *h, const PassPlan &P, int ncl, int mode, bool mark_static) {
+    if (!h->eng->graphs) {
+        compute(h, P, ncl, mode, nullptr, mark_static);
+        return;
+    }
+    const std::vector<uint64_t> sig = pass_signature(h, P, ncl, mode, mark_static);
+    ekg_heart::PassGraph *g = nullptr, *victim = &h->graphs[0];
+    for (auto &c : h->graphs) {
+        if (!c.sig.empty() && c.sig == sig) g = &c;
+        if (c.used < victim->used) victim = &c;
+    }
+    cudaStream_t s = h->stream;
+    if (g && g->exec) {
+        g->used = ++h->graph_clock;
+        EKG_CUDA(cudaGraphLaunch(g->exec, s));
+        return;
+    }
+    if (!g) {
+        if (victim->exec) cudaGraphExecDestroy(victim->exec);
+        *victim = ekg_heart::PassGraph();
+        victim->sig = sig;
+        victim->used = ++h->graph_clock;
+        compute(h, P, ncl, mode, nullptr, mark_static);
+        return;
+    }
+    cudaGraph_t graph = nullptr;
+    EKG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+        compute(h, P, ncl, mode, nullptr, mark_static);
+    } catch (...) {
+        cudaStreamEndCapture(s, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        throw;
+    }
+    EKG_CUDA(cudaStreamEndCapture(s, &graph));
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    EKG_CUDA(e);
+    g->exec = exec;
+    g->used = ++h->graph_clock;
+    EKG_CUDA(cudaGraphLaunch(exec, s));
+}
+
 void device_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *leads, double *ecg_host,
                  double *crit_host, int n_crit_leads, int mode) {
     HeartDev &D = h->dev;
@@ -1110,7 +1190,7 @@ void device_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *
         EKG_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
         EKG_CUDA(cudaEventCreateWithFlags(&h->static_done, cudaEventDisableTiming));
     }
-    compute(h, P, crit_host ? n_crit_leads : 0, mode, nullptr, split);
+    run_pass(h, P, crit_host ? n_crit_leads : 0, mode, split);
     if (split) {
         const size_t nm = P.nmove;
         EKG_CUDA(cudaStreamWaitEvent(h->copy_stream, h->static_done, 0));
@@ -1444,6 +1524,7 @@ int ekg_engine_create(int device, ekg_engine **out) {
         if (const char *v = std::getenv("EKG_CHUNK")) e->chunk_len = std::max(64, std::atoi(v) / 64 * 64);
         if (const char *v = std::getenv("EKG_BATCHED")) e->batched = std::string(v) != "0";
         if (const char *v = std::getenv("EKG_BATCH_CTAS")) e->batch_ctas = std::atoi(v);
+        if (const char *v = std::getenv("EKG_GRAPHS")) e->graphs = std::string(v) != "0";
         EKG_CUDA(cudaSetDevice(device));
         EKG_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
         *out = e.release();

@@ -378,3 +378,35 @@ def test_batched_form_fine_time_axis(engine):
     """dt = 1/32 ms over 100 ms (3200 steps): tiles of 4 ms, bands spanning several tiles and more
     tiles before the first all-steady one than steady-prefix entries, so tiles share entries."""
     assert _batched_general(engine, synth.small_spec(32, n_leads=2), "3D4", 2.0, 100.0, 0.03125, 4) <= ECG_TOL
+
+
+def test_graph_replay_is_bit_identical():
+    """Repeated passes replay a captured CUDA graph (from the third pass with the same shape); the
+    results are bitwise those of direct launches (EKG_GRAPHS=0), single and batched."""
+    from ekgsim_gb300.engine import Engine, Heart
+    spec = synth.small_spec(32, n_leads=3, seed=13)
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(3, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    target = synth.analytic_target(spec.n_leads, 300, 8)
+    genes = np.stack([synth.genes_for(spec, r, 0) for r in range(6)])
+    out = {}
+    for flag in ("1", "0"):
+        os.environ["EKG_GRAPHS"] = flag
+        try:
+            e = Engine(0)
+            h = Heart.create(e, grid, tm, leads, "3D4", 0.0, 300.0, 1.0)
+            h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], [t for t in target],
+                       mid_position=0.6)
+            res = []
+            for _ in range(4):
+                res.append(h.eval_batch(genes, want_ecg=True))
+                res.append(h.eval(genes[2], want_ecg=True)[:3])
+            out[flag] = res
+            h.close()
+            e.close()
+        finally:
+            os.environ.pop("EKG_GRAPHS", None)
+    for a, b in zip(out["1"], out["0"]):
+        for x, y in zip(a, b):
+            assert np.array_equal(np.asarray(x), np.asarray(y))
