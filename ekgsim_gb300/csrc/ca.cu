@@ -10,11 +10,15 @@
 // __dmul_rn / __dadd_rn so the compiler cannot fuse them into an FMA.
 //
 // Layout: the grid is cut into 8x8x8 tiles.  A round processes the active tiles, one CTA each:
-// the tile and a one-voxel halo are staged in shared memory (FP64 times + uint8 layers), the
-// tile relaxes locally until a block-wide vote (__syncthreads_or) finds no change, the changed
-// interior voxels are written back, and the neighbour tiles that touch a changed face, edge or
-// corner are flagged.  A compaction kernel turns the flags into the next round's tile list with
-// warp ballots and one atomic per warp.  The host loops until no tile is active.
+// the tile and a one-voxel halo are staged in shared memory (the FP64 times as their bit patterns,
+// which order like the values for non-negative doubles, + uint8 layers).  The tile relaxes
+// locally: a first sweep pulls every voxel's candidates from its 26 neighbours, later sweeps only
+// push from the voxels that improved in the sweep before (64-bit atomicMin on the bit patterns),
+// until a block-wide vote (__syncthreads_or) finds no change.  A candidate is skipped without the
+// FP64 add when the offering voxel is not earlier than the receiving one (lags are positive).  The
+// changed interior voxels are written back and the neighbour tiles that touch a changed face,
+// edge or corner are flagged.  A compaction kernel turns the flags into the next round's tile list
+// with warp ballots and one atomic per warp.  The host loops until no tile is active.
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -38,8 +42,9 @@ template <typename LT>
 __global__ void k_ca_round(int nz, int ny, int nx, int ntz, int nty, int ntx, const LT *__restrict__ layers,
                            const double *__restrict__ lag, int nl1, double *__restrict__ at,
                            const int32_t *__restrict__ active, uint8_t *__restrict__ next_flag) {
-    __shared__ double s_at[HS][HS][HS];
+    __shared__ unsigned long long s_b[HS][HS][HS];  // activation-time bits
     __shared__ uint8_t s_l[HS][HS][HS];
+    __shared__ uint8_t s_ch[2][HS][HS][HS];         // improved in the last sweep (tile interior)
     __shared__ uint32_t s_mark;  // 27-bit mask of neighbour tiles to flag (bit = (dz+1)*9+(dy+1)*3+(dx+1))
 
     const int tile = active[blockIdx.x];
@@ -50,43 +55,80 @@ __global__ void k_ca_round(int nz, int ny, int nx, int ntz, int nty, int ntx, co
     if (tid == 0) s_mark = 0;
 
     // stage tile + halo
+    const unsigned long long INF_BITS = 0x7ff0000000000000ULL;
     for (int i = tid; i < HS * HS * HS; i += CA_THREADS) {
         int hx = i % HS, hy = (i / HS) % HS, hz = i / (HS * HS);
         int gx = tx0 + hx - 1, gy = ty0 + hy - 1, gz = tz0 + hz - 1;
-        double a = __longlong_as_double(0x7ff0000000000000LL);  // +inf
+        unsigned long long b = INF_BITS;
         uint8_t l = 0;
         if (gx >= 0 && gx < nx && gy >= 0 && gy < ny && gz >= 0 && gz < nz) {
             size_t g = ((size_t)gz * ny + gy) * nx + gx;
             l = layer_id(layers[g]);
-            if (l) a = at[g];
+            if (l) b = (unsigned long long)__double_as_longlong(at[g]);
         }
-        s_at[hz][hy][hx] = a;
+        s_b[hz][hy][hx] = b;
         s_l[hz][hy][hx] = l;
+        s_ch[0][hz][hy][hx] = 0;
+        s_ch[1][hz][hy][hx] = 0;
     }
     __syncthreads();
 
     const int lx = (tid & 7) + 1, ly = ((tid >> 3) & 7) + 1, lz0 = (tid >> 6) + 1;
-    double orig[2];
+    unsigned long long orig[2];
     uint8_t myl[2];
     bool inside[2];
 #pragma unroll
     for (int r = 0; r < 2; ++r) {
         int lz = lz0 + 4 * r;
-        orig[r] = s_at[lz][ly][lx];
+        orig[r] = s_b[lz][ly][lx];
         myl[r] = s_l[lz][ly][lx];
         inside[r] = (tx0 + lx - 1 < nx) && (ty0 + ly - 1 < ny) && (tz0 + lz - 1 < nz);
     }
 
-    int iters = 0;
-    bool again = true;
+    // sweep 0: pull from the 26 neighbours (the halo may carry new times from other tiles)
+    bool changed = false;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        if (!inside[r] || myl[r] == 0) continue;
+        const int lz = lz0 + 4 * r;
+        unsigned long long best = s_b[lz][ly][lx];
+        const double *lagd = lag + (size_t)myl[r] * 3;  // lag[src][dst=myl][k]
+#pragma unroll
+        for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+            for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+                for (int dx = -1; dx <= 1; ++dx) {
+                    if (dz == 0 && dy == 0 && dx == 0) continue;
+                    const uint8_t lu = s_l[lz + dz][ly + dy][lx + dx];
+                    if (lu == 0) continue;
+                    const unsigned long long bu = s_b[lz + dz][ly + dy][lx + dx];
+                    if (bu >= best) continue;
+                    const int k = (dz != 0) + (dy != 0) + (dx != 0);
+                    const double c = __dadd_rn(__longlong_as_double((long long)bu),
+                                               __ldg(lagd + (size_t)lu * nl1 * 3 + (k - 1)));
+                    const unsigned long long cb = (unsigned long long)__double_as_longlong(c);
+                    if (cb < best) best = cb;
+                }
+        if (best < s_b[lz][ly][lx]) {
+            s_b[lz][ly][lx] = best;
+            s_ch[0][lz][ly][lx] = 1;
+            changed = true;
+        }
+    }
+    int iters = 1, cur = 0;
+    bool again = __syncthreads_or(changed);
+    // later sweeps: the voxels that improved push to their interior neighbours
     while (again && iters < MAX_LOCAL_ITERS) {
-        bool changed = false;
+        changed = false;
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
-            if (!inside[r] || myl[r] == 0) continue;
             const int lz = lz0 + 4 * r;
-            double best = s_at[lz][ly][lx];
-            const double *lagd = lag + (size_t)myl[r] * 3;  // lag[src][dst=myl][k]
+            if (!inside[r] || myl[r] == 0 || !s_ch[cur][lz][ly][lx]) continue;
+            s_ch[cur][lz][ly][lx] = 0;
+            const unsigned long long bu = s_b[lz][ly][lx];
+            const double au = __longlong_as_double((long long)bu);
+            const double *lags = lag + (size_t)myl[r] * nl1 * 3;  // lag[src=myl][dst][k]
 #pragma unroll
             for (int dz = -1; dz <= 1; ++dz)
 #pragma unroll
@@ -94,18 +136,22 @@ __global__ void k_ca_round(int nz, int ny, int nx, int ntz, int nty, int ntx, co
 #pragma unroll
                     for (int dx = -1; dx <= 1; ++dx) {
                         if (dz == 0 && dy == 0 && dx == 0) continue;
-                        const uint8_t lu = s_l[lz + dz][ly + dy][lx + dx];
-                        if (lu == 0) continue;
-                        const double au = s_at[lz + dz][ly + dy][lx + dx];
+                        const int wz = lz + dz, wy = ly + dy, wx = lx + dx;
+                        if (wz < 1 || wz > TS || wy < 1 || wy > TS || wx < 1 || wx > TS) continue;
+                        const uint8_t lw = s_l[wz][wy][wx];
+                        if (lw == 0) continue;
+                        const unsigned long long bw = s_b[wz][wy][wx];
+                        if (bu >= bw) continue;
                         const int k = (dz != 0) + (dy != 0) + (dx != 0);
-                        const double c = __dadd_rn(au, __ldg(lagd + (size_t)lu * nl1 * 3 + (k - 1)));
-                        if (c < best) best = c;
+                        const unsigned long long cb = (unsigned long long)__double_as_longlong(
+                            __dadd_rn(au, __ldg(lags + (size_t)lw * 3 + (k - 1))));
+                        if (cb < bw && cb < atomicMin(&s_b[wz][wy][wx], cb)) {
+                            s_ch[cur ^ 1][wz][wy][wx] = 1;
+                            changed = true;
+                        }
                     }
-            if (best < s_at[lz][ly][lx]) {
-                s_at[lz][ly][lx] = best;
-                changed = true;
-            }
         }
+        cur ^= 1;
         again = __syncthreads_or(changed);
         ++iters;
     }
@@ -116,10 +162,10 @@ __global__ void k_ca_round(int nz, int ny, int nx, int ntz, int nty, int ntx, co
     for (int r = 0; r < 2; ++r) {
         const int lz = lz0 + 4 * r;
         if (!inside[r] || myl[r] == 0) continue;
-        const double v = s_at[lz][ly][lx];
+        const unsigned long long v = s_b[lz][ly][lx];
         if (v < orig[r]) {
             size_t g = ((size_t)(tz0 + lz - 1) * ny + (ty0 + ly - 1)) * nx + (tx0 + lx - 1);
-            at[g] = v;
+            at[g] = __longlong_as_double((long long)v);
             const int fz = (lz == 1) ? -1 : (lz == TS ? 1 : 0);
             const int fy = (ly == 1) ? -1 : (ly == TS ? 1 : 0);
             const int fx = (lx == 1) ? -1 : (lx == TS ? 1 : 0);
