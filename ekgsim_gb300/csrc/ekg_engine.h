@@ -58,13 +58,6 @@ struct BatchState {
     DBuf<int> work;                        // work counter of the operand kernel
     DBuf<float2> U, Up;                    // [rows][nl][max_ent] steady sums (U0, U1), per K part
     DBuf<float> partial;                   // [items][rows][128] raw accumulators (x2 with two bases)
-    DBuf<int4> items;                      // GEMM work items
-    DBuf<int32_t> ti0, ti1;                // [ntt][nl] item range of each (tile, layer)
-    DBuf<float> k5l;                       // [S][nl] k5 log2(e)
-    DBuf<float4> lrel;                     // [S][nmove] moved lead positions relative to the voxel centre
-    DBuf<float4> hconst;
-    DBuf<double> k3;
-    DBuf<float> coef;
 };
 // What one device pass does, decided on the host from the batch's layer APs and lead positions.
 struct PassPlan {
@@ -96,9 +89,22 @@ struct ekg_heart {
     };
     PassGraph graphs[4];
     uint64_t graph_clock = 0;
+    // the small per-pass inputs, packed into one pinned host buffer and copied with one transfer into
+    // one device buffer (both grow only, so the device addresses the graphs hold stay valid)
+    uint8_t *stage_host = nullptr;
+    ekg::DBuf<uint8_t> stage_dev;
+    size_t stage_cap = 0;
+    struct PassInputs {
+        const double *layer_k = nullptr, *cpre = nullptr, *leads = nullptr, *k3 = nullptr;
+        const float *coef = nullptr, *k5l = nullptr;
+        const float4 *hconst = nullptr, *lrel = nullptr;
+        const int4 *items = nullptr;
+        const int32_t *ti0 = nullptr, *ti1 = nullptr;
+    } in;
     ~ekg_heart() {
         for (PassGraph &g : graphs)
             if (g.exec) cudaGraphExecDestroy(g.exec);
+        if (stage_host) cudaFreeHost(stage_host);
         if (static_done) cudaEventDestroy(static_done);
         if (copy_stream) cudaStreamDestroy(copy_stream);
         if (stream) cudaStreamDestroy(stream);

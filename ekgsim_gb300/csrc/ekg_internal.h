@@ -121,9 +121,6 @@ struct HeartDev {
 // Per-evaluation scratch (sized for n_sims simulations).
 struct EvalDev {
     int cap_sims = 0;
-    DBuf<double> layer_k;   // [S][nl][9]
-    DBuf<double> cpre;      // [S][nl] ln(2^(k7/k6) - 1), host-computed for small passes
-    DBuf<double> leads;     // [S][L][3]
     DBuf<float> layer_c;    // [S][nl][4]: k1*log2e, k4*log2e, 1-k3, k3 (FP32 H constants)
     DBuf<double> F;         // [S][nl][steps]
     DBuf<float> Ff;         // [S][nl][steps] the same in FP32 (batched form)

@@ -535,7 +535,7 @@ int64_t heart_device_bytes(const ekg_heart *h) {
                 D.vox_nb.bytes() + D.vox_nbo.bytes() + D.chunk_a0.bytes() * 3 + D.t.bytes() + D.t_hilo.bytes() +
                 h->W0.bytes() + h->at_cells.bytes();
     const EvalDev &E = h->ev;
-    b += E.layer_k.bytes() + E.leads.bytes() + E.layer_c.bytes() + E.F.bytes() + E.k0w.bytes() + E.W.bytes() +
+    b += (int64_t)h->stage_dev.bytes() + E.layer_c.bytes() + E.F.bytes() + E.k0w.bytes() + E.W.bytes() +
          E.Wp.bytes() + E.partial.bytes() + E.ecg.bytes() + E.crit.bytes() + E.targets.bytes();
     return b;
 }
@@ -554,8 +554,6 @@ void ensure_eval_capacity(ekg_heart *h, int n_sims) {
     const HeartDev &D = h->dev;
     if (E.cap_sims >= n_sims) return;
     const size_t S = (size_t)n_sims;
-    E.layer_k.alloc(S * D.nlayers * 9);
-    E.leads.alloc(S * D.nleads * 3);
     E.layer_c.alloc(S * D.nlayers * 4);
     E.F.alloc(S * D.nlayers * D.steps);
     E.Ff.alloc(S * D.nlayers * D.steps);
@@ -922,33 +920,78 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
 
 void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const double *leads) {
     HeartDev &D = h->dev;
-    EvalDev &E = h->ev;
     cudaStream_t s = h->stream;
     const int n_sims = P.n_sims;
     ensure_eval_capacity(h, n_sims);
-    const size_t L = D.nleads, S = n_sims;
-    EKG_CUDA(cudaMemcpyAsync(E.layer_k.p, layer_k, S * D.nlayers * 9 * 8, cudaMemcpyHostToDevice, s));
+    const size_t L = D.nleads, S = n_sims, nl = D.nlayers;
+    h->any_k0 = false;
+    for (size_t i = 0; i < S * nl; ++i) h->any_k0 = h->any_k0 || layer_k[9 * i] != 0.0;
     // small passes: the repolarisation constant ln(2^(k7/k6) - 1) per (sim, layer) on the host
     h->cpre_on = S <= 16;
+    std::vector<double> cpre;
     if (h->cpre_on) {
-        double c[16 * 256];
-        const size_t n = S * D.nlayers;
-        for (size_t i = 0; i < n && i < 16 * 256; ++i) c[i] = std::log(std::pow(2.0, layer_k[9 * i + 7] / layer_k[9 * i + 6]) - 1);
-        E.cpre.alloc(16 * 256);
-        // (a copy from pageable memory is staged before the call returns, so the stack buffer may go)
-        EKG_CUDA(cudaMemcpyAsync(E.cpre.p, c, std::min<size_t>(n, 16 * 256) * 8, cudaMemcpyHostToDevice, s));
+        cpre.resize(S * nl);
+        for (size_t i = 0; i < S * nl; ++i) cpre[i] = std::log(std::pow(2.0, layer_k[9 * i + 7] / layer_k[9 * i + 6]) - 1);
     }
-    h->any_k0 = false;
-    for (size_t i = 0; i < S * D.nlayers; ++i) h->any_k0 = h->any_k0 || layer_k[9 * i] != 0.0;
-    if (P.nmove > 0) EKG_CUDA(cudaMemcpyAsync(E.leads.p, leads, S * L * 3 * 8, cudaMemcpyHostToDevice, s));
+    // layout of the staging buffer (16-byte aligned slots)
+    struct Slot {
+        const void *src;
+        size_t bytes, off;
+    };
+    std::vector<Slot> slots;
+    size_t off = 0;
+    auto add = [&](const void *src, size_t bytes) {
+        const size_t o = off;
+        if (bytes) slots.push_back(Slot{src, bytes, o});
+        off = (off + bytes + 15) / 16 * 16;
+        return o;
+    };
+    const size_t o_lk = add(layer_k, S * nl * 9 * 8);
+    const size_t o_cp = add(cpre.data(), cpre.size() * 8);
+    const size_t o_ld = add(leads, P.nmove > 0 ? S * L * 3 * 8 : 0);
+    size_t o_coef = 0, o_k3 = 0, o_hc = 0, o_ti0 = 0, o_ti1 = 0, o_it = 0, o_k5 = 0, o_lr = 0;
     if (P.batch) {
+        o_coef = add(P.coef.data(), P.coef.size() * 4);
+        o_k3 = add(P.k3.data(), P.k3.size() * 8);
+        o_hc = add(P.hc, nl * sizeof(float4));
+        if (P.nmove > 0) {
+            o_ti0 = add(P.ti0.data(), P.ti0.size() * 4);
+            o_ti1 = add(P.ti1.data(), P.ti1.size() * 4);
+            o_it = add(P.items.data(), P.items.size() * sizeof(int4));
+            o_k5 = add(P.k5l.data(), P.k5l.size() * 4);
+            o_lr = add(P.lrel.data(), P.lrel.size() * sizeof(float4));
+        }
+    }
+    if (off > h->stage_cap) {
+        const size_t cap = std::max(off, 2 * h->stage_cap);
+        EKG_CUDA(cudaStreamSynchronize(s));  // the old buffers may still be read
+        if (h->stage_host) cudaFreeHost(h->stage_host);
+        h->stage_host = nullptr;
+        h->stage_cap = 0;
+        EKG_CUDA(cudaMallocHost(&h->stage_host, cap));
+        h->stage_dev.alloc(cap);
+        h->stage_cap = cap;
+    }
+    for (const Slot &sl : slots) std::memcpy(h->stage_host + sl.off, sl.src, sl.bytes);
+    if (off) EKG_CUDA(cudaMemcpyAsync(h->stage_dev.p, h->stage_host, off, cudaMemcpyHostToDevice, s));
+    const uint8_t *dv = h->stage_dev.p;
+    ekg_heart::PassInputs &in = h->in;
+    in = ekg_heart::PassInputs();
+    in.layer_k = reinterpret_cast<const double *>(dv + o_lk);
+    in.cpre = h->cpre_on ? reinterpret_cast<const double *>(dv + o_cp) : nullptr;
+    in.leads = P.nmove > 0 ? reinterpret_cast<const double *>(dv + o_ld) : nullptr;
+    if (P.batch) {
+        in.coef = reinterpret_cast<const float *>(dv + o_coef);
+        in.k3 = reinterpret_cast<const double *>(dv + o_k3);
+        in.hconst = reinterpret_cast<const float4 *>(dv + o_hc);
+        if (P.nmove > 0) {
+            in.ti0 = reinterpret_cast<const int32_t *>(dv + o_ti0);
+            in.ti1 = reinterpret_cast<const int32_t *>(dv + o_ti1);
+            in.items = reinterpret_cast<const int4 *>(dv + o_it);
+            in.k5l = reinterpret_cast<const float *>(dv + o_k5);
+            in.lrel = reinterpret_cast<const float4 *>(dv + o_lr);
+        }
         BatchState &B = h->bs;
-        B.coef.alloc(P.coef.size());
-        B.k3.alloc(P.k3.size());
-        B.hconst.alloc(D.nlayers);
-        EKG_CUDA(cudaMemcpyAsync(B.coef.p, P.coef.data(), P.coef.size() * 4, cudaMemcpyHostToDevice, s));
-        EKG_CUDA(cudaMemcpyAsync(B.k3.p, P.k3.data(), P.k3.size() * 8, cudaMemcpyHostToDevice, s));
-        EKG_CUDA(cudaMemcpyAsync(B.hconst.p, P.hc, D.nlayers * sizeof(float4), cudaMemcpyHostToDevice, s));
         if (P.nmove > 0) {
             const size_t bt = (size_t)P.rows * D.apad * 4;
             if (B.Bt.n < bt) B.Bt.alloc(bt);
@@ -956,23 +999,12 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
             if (B.partial.n < pb) B.partial.alloc(pb);
             const size_t p1 = (size_t)(D.apad / 64) * B.max_ent * P.rows_used;
             if (B.P1.n < p1) B.P1.alloc(p1);
-            B.work.alloc(1);
+            if (!B.work.p) B.work.alloc(1);
             const size_t ub = (size_t)P.rows_used * D.nlayers * B.max_ent;
             if (B.U.n < ub) {
                 B.U.alloc(ub);
                 B.Up.alloc(ub * band_u_parts());
             }
-            if (B.items.n < (size_t)std::max(1, P.nitems)) B.items.alloc(std::max(1, P.nitems));
-            B.ti0.alloc((size_t)B.ntt * D.nlayers);
-            B.ti1.alloc((size_t)B.ntt * D.nlayers);
-            EKG_CUDA(cudaMemcpyAsync(B.ti0.p, P.ti0.data(), P.ti0.size() * 4, cudaMemcpyHostToDevice, s));
-            EKG_CUDA(cudaMemcpyAsync(B.ti1.p, P.ti1.data(), P.ti1.size() * 4, cudaMemcpyHostToDevice, s));
-            if (B.k5l.n < P.k5l.size()) B.k5l.alloc(P.k5l.size());
-            if (B.lrel.n < P.lrel.size()) B.lrel.alloc(P.lrel.size());
-            if (P.nitems > 0)
-                EKG_CUDA(cudaMemcpyAsync(B.items.p, P.items.data(), P.nitems * sizeof(int4), cudaMemcpyHostToDevice, s));
-            EKG_CUDA(cudaMemcpyAsync(B.k5l.p, P.k5l.data(), P.k5l.size() * 4, cudaMemcpyHostToDevice, s));
-            EKG_CUDA(cudaMemcpyAsync(B.lrel.p, P.lrel.data(), P.lrel.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
         }
     } else {
         ensure_general_capacity(h, n_sims);
@@ -988,11 +1020,12 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
     int launches = 0;
     if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[0], s));
     EKG_CUDA(cudaMemsetAsync(E.err.p, 0, sizeof(uint32_t), s));
-    launch_layer_factors(s, D, E.layer_k.p, h->cpre_on ? E.cpre.p : nullptr, n_sims, E.F.p, E.Ff.p, E.layer_c.p);
+    const ekg_heart::PassInputs &in = h->in;
+    launch_layer_factors(s, D, in.layer_k, in.cpre, n_sims, E.F.p, E.Ff.p, E.layer_c.p);
     ++launches;
     if (P.batch) {
         BatchState &B = h->bs;
-        launch_static_combine(s, D, P.J, B.J, nmove, n_sims, E.Ff.p, B.coef.p, B.k3.p, B.Q1.p, B.Q2.p, E.ecg.p);
+        launch_static_combine(s, D, P.J, B.J, nmove, n_sims, E.Ff.p, in.coef, in.k3, B.Q1.p, B.Q2.p, E.ecg.p);
         launches += nmove < (int)L;
         if (mark_static) {
             // inside a graph capture the record must be an external event node (the copy stream waits
@@ -1026,16 +1059,16 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             U.E = B.E.p;
             U.F = E.Ff.p;
             U.nb = P.two_bases ? 2 : 1;
-            U.ti0 = B.ti0.p;
-            U.ti1 = B.ti1.p;
-            U.k3 = B.k3.p;
+            U.ti0 = in.ti0;
+            U.ti1 = in.ti1;
+            U.k3 = in.k3;
             U.partial = B.partial.p;
             U.P1 = B.P1.p;
             U.U = B.U.p;
             U.Up = B.Up.p;
             U.ecg = E.ecg.p;
             if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[4], s));
-            launch_batch_lead_field(s, D, P.two_bases, B.k5l.p, B.hconst.p, B.lrel.p, nmove, n_sims, U, B.Bt.p,
+            launch_batch_lead_field(s, D, P.two_bases, in.k5l, in.hconst, in.lrel, nmove, n_sims, U, B.Bt.p,
                                     B.work.p, h->sm_count);
             if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[5], s));
             launch_band_u(s, U);
@@ -1054,8 +1087,8 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             A.two_bases = P.two_bases;
             A.t_hilo = D.t_hilo.p;
             A.at_hilo = D.at_hilo.p;
-            A.items = B.items.p;
-            A.hconst = B.hconst.p;
+            A.items = in.items;
+            A.hconst = in.hconst;
             A.Bt = B.Bt.p;
             A.partial = B.partial.p;
             A.err = E.err.p;
@@ -1073,15 +1106,15 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
         for (size_t si = 0; si < S; ++si)
             EKG_CUDA(cudaMemcpyAsync(E.W.p + si * L * D.apad, h->W0.p, L * D.apad * 4, cudaMemcpyDeviceToDevice, s));
         if (nmove > 0) {
-            launch_lead_field(s, D, E.leads.p, nmove, (int)L, n_sims, E.W.p, (int)L);
+            launch_lead_field(s, D, in.leads, nmove, (int)L, n_sims, E.W.p, (int)L);
             ++launches;
         }
-        launch_scale_w(s, D, E.W.p, E.layer_k.p, n_sims, E.Wp.p);
+        launch_scale_w(s, D, E.W.p, in.layer_k, n_sims, E.Wp.p);
         ++launches;
         // k0 leaves a constant term only when some layer's k0 differs from zero (AP differences
         // within a layer cancel it)
         if (h->any_k0) {
-            launch_k0_term(s, D, E.W.p, E.layer_k.p, n_sims, E.k0w.p);
+            launch_k0_term(s, D, E.W.p, in.layer_k, n_sims, E.k0w.p);
             ++launches;
         } else {
             EKG_CUDA(cudaMemsetAsync(E.k0w.p, 0, S * L * sizeof(double), s));
@@ -1112,14 +1145,17 @@ std::vector<uint64_t> pass_signature(const ekg_heart *h, const PassPlan &P, int 
                                (uint64_t)P.nitems, (uint64_t)ncl, (uint64_t)mode, (uint64_t)mark_static,
                                (uint64_t)h->cpre_on, (uint64_t)h->any_k0, (uint64_t)h->eng->umma, (uint64_t)B.J,
                                (uint64_t)B.max_ent, (uint64_t)B.ntt};
-    for (const void *p : {(const void *)E.layer_k.p, (const void *)E.cpre.p, (const void *)E.F.p, (const void *)E.Ff.p,
+    const ekg_heart::PassInputs &in = h->in;
+    for (const void *p : {(const void *)in.layer_k, (const void *)in.cpre, (const void *)in.leads, (const void *)in.k3,
+                          (const void *)in.coef, (const void *)in.k5l, (const void *)in.hconst, (const void *)in.lrel,
+                          (const void *)in.items, (const void *)in.ti0, (const void *)in.ti1,
+                          (const void *)E.F.p, (const void *)E.Ff.p,
                           (const void *)E.layer_c.p, (const void *)E.ecg.p, (const void *)E.crit.p, (const void *)E.err.p,
                           (const void *)E.targets.p, (const void *)E.target_len.p, (const void *)E.target_off.p,
                           (const void *)E.W.p, (const void *)E.Wp.p, (const void *)E.partial.p, (const void *)E.k0w.p,
-                          (const void *)E.leads.p, (const void *)B.coef.p, (const void *)B.k3.p, (const void *)B.Q1.p,
+                          (const void *)B.Q1.p,
                           (const void *)B.Q2.p, (const void *)B.Bt.p, (const void *)B.P1.p, (const void *)B.U.p,
-                          (const void *)B.Up.p, (const void *)B.partial.p, (const void *)B.items.p, (const void *)B.ti0.p,
-                          (const void *)B.ti1.p, (const void *)B.k5l.p, (const void *)B.lrel.p, (const void *)B.hconst.p,
+                          (const void *)B.Up.p, (const void *)B.partial.p,
                           (const void *)B.c8s.p, (const void *)B.nent.p, (const void *)B.esplit8.p, (const void *)B.ls0.p,
                           (const void *)B.ls1.p, (const void *)B.ent.p, (const void *)B.goff.p, (const void *)B.gtab.p,
                           (const void *)B.E.p, (const void *)B.work.p, (const void *)h->W0.p})
