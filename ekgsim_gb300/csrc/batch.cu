@@ -116,16 +116,18 @@ __global__ void k_reduce_layers(int steps, int rows, int nl, const int32_t *__re
 }
 
 // Static leads: ecg[s][l][t] = sum_L F[s][L][t] sum_j coef[s][L][j] ((1-k3) Q1 + k3 Q2)[L][l*J+j][t],
-// the Taylor sum per layer in FP32 (the basis is stored in FP32), the sum over layers in FP64.
+// the Taylor sum per layer in FP32 (the basis is stored in FP32), the sum over layers in
+// float-float; written as FP64 and as float-float.
 __global__ void k_static_combine(int steps, int nleads, int nl, int J, int Jb, int nmove, int n_sims,
                                  const float *__restrict__ F, const float *__restrict__ coef,
                                  const double *__restrict__ k3, const float *__restrict__ Q1,
-                                 const float *__restrict__ Q2, double *__restrict__ ecg) {
+                                 const float *__restrict__ Q2, double *__restrict__ ecg,
+                                 float2 *__restrict__ ecg_ff) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int l = nmove + blockIdx.y, s = blockIdx.z;
     if (t >= steps || l >= nleads) return;
     const int rows = nleads * Jb;  // the basis stores Jb terms per lead
-    double acc = 0.0;
+    float2 acc = make_float2(0.f, 0.f);
     for (int L = 0; L < nl; ++L) {
         const float kk = (float)k3[(size_t)s * nl + L];
         const float *c = coef + ((size_t)s * nl + L) * J;
@@ -137,9 +139,11 @@ __global__ void k_static_combine(int steps, int nleads, int nl, int J, int Jb, i
                 v1 = fmaf(c[j], Q1[q0 + (size_t)j * steps], v1);
                 v2 = fmaf(c[j], Q2[q0 + (size_t)j * steps], v2);
             }
-        acc += (double)(F[((size_t)s * nl + L) * steps + t] * fmaf(kk, v2 - v1, v1));
+        acc = ff_add_f(acc, F[((size_t)s * nl + L) * steps + t] * fmaf(kk, v2 - v1, v1));
     }
-    ecg[((size_t)s * nleads + l) * steps + t] = acc;
+    const size_t o = ((size_t)s * nleads + l) * steps + t;
+    ecg[o] = ff_to_double(acc);
+    ecg_ff[o] = acc;
 }
 
 // ------------------------------------------------------------------ moved-lead operand
@@ -784,14 +788,15 @@ __global__ void __launch_bounds__(WS_THREADS, (N <= 32 ? 2 : 1)) k_batch_umma(
 // (with one basis the GEMM already mixed k3: Y_L + (1 - k3) E U1 + k3 U0), Y_L = sum over the band
 // items of (t's tile, L) of the raw accumulators, (U0, U1) = U[row'][L][ent[L][j]], row = s * nmove
 // + l, row' = l * S + s, j = t / 128.  Block per (row, 32 steps): the 8 warps split each layer's
-// items (FP32, combined in a fixed order), the sum over layers is FP64 (few rows, many items);
-// k_reduce_band: one thread per (row, t) (many rows).
+// items (FP32, combined in a fixed order), the sum over layers is float-float, written as FP64 and
+// float-float (few rows, many items); k_reduce_band: one thread per (row, t) (many rows).
 __global__ void __launch_bounds__(256) k_reduce_band_w(int steps, int rows, int nmove, int n_sims, int nleads, int nl,
                                                      int ntt, int max_ent, int nb, const int32_t *__restrict__ ti0,
                                                      const int32_t *__restrict__ ti1, const int32_t *__restrict__ ent,
                                                      const float *__restrict__ partial, const float2 *__restrict__ U,
                                                      const float *__restrict__ E, const float *__restrict__ F,
-                                                     const double *__restrict__ k3, double *__restrict__ ecg) {
+                                                     const double *__restrict__ k3, double *__restrict__ ecg,
+                                                       float2 *__restrict__ ecg_ff) {
     __shared__ float red[8][2][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int tt = blockIdx.x * 32 + lane;
@@ -800,7 +805,7 @@ __global__ void __launch_bounds__(256) k_reduce_band_w(int steps, int rows, int 
     const int j = (blockIdx.x * 32) / BM, tl = tt - j * BM;
     const bool on = tt < steps;
     const size_t rp = (size_t)l * n_sims + s;
-    double v = 0.0;
+    float2 v = make_float2(0.f, 0.f);
     for (int L = 0; L < nl; ++L) {
         float y1 = 0.f, y2 = 0.f;
         const int c1 = ti1[j * nl + L];
@@ -834,25 +839,30 @@ __global__ void __launch_bounds__(256) k_reduce_band_w(int steps, int rows, int 
             }
             const float x = nb == 2 ? fmaf(kk, (y2 + st0) - (y1 + st1), y1 + st1)
                                     : fmaf(kk, st0 - st1, y1 + st1);
-            v += (double)(F[((size_t)s * nl + L) * steps + tt] * x);
+            v = ff_add_f(v, F[((size_t)s * nl + L) * steps + tt] * x);
         }
         __syncthreads();
     }
-    if (w == 0 && on) ecg[((size_t)s * nleads + l) * steps + tt] = v;
+    if (w == 0 && on) {
+        const size_t o = ((size_t)s * nleads + l) * steps + tt;
+        ecg[o] = ff_to_double(v);
+        ecg_ff[o] = v;
+    }
 }
 
 __global__ void k_reduce_band(int steps, int rows, int nmove, int n_sims, int nleads, int nl, int ntt, int max_ent,
                               int nb, const int32_t *__restrict__ ti0, const int32_t *__restrict__ ti1,
                               const int32_t *__restrict__ ent, const float *__restrict__ partial,
                               const float2 *__restrict__ U, const float *__restrict__ E, const float *__restrict__ F,
-                              const double *__restrict__ k3, double *__restrict__ ecg) {
+                              const double *__restrict__ k3, double *__restrict__ ecg,
+                              float2 *__restrict__ ecg_ff) {
     const int tt = blockIdx.x * blockDim.x + threadIdx.x;
     if (tt >= steps) return;
     const int r = blockIdx.y;
     const int s = r / nmove, l = r % nmove;
     const int j = tt / BM, tl = tt - j * BM;
     const size_t rp = (size_t)l * n_sims + s;
-    double v = 0.0;
+    float2 v = make_float2(0.f, 0.f);
     for (int L = 0; L < nl; ++L) {
         const float kk = (float)k3[(size_t)s * nl + L];
         float y1 = 0.f, y2 = 0.f;
@@ -875,9 +885,11 @@ __global__ void k_reduce_band(int steps, int rows, int nmove, int n_sims, int nl
         }
         const float x = nb == 2 ? fmaf(kk, (y2 + st0) - (y1 + st1), y1 + st1)
                                 : fmaf(kk, st0 - st1, y1 + st1);
-        v += (double)(F[((size_t)s * nl + L) * steps + tt] * x);
+        v = ff_add_f(v, F[((size_t)s * nl + L) * steps + tt] * x);
     }
-    ecg[((size_t)s * nleads + l) * steps + tt] = v;
+    const size_t o = ((size_t)s * nleads + l) * steps + tt;
+    ecg[o] = ff_to_double(v);
+    ecg_ff[o] = v;
 }
 
 template <int NB, int N>
@@ -919,11 +931,12 @@ void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int
 }
 
 void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const float *F,
-                           const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg) {
+                           const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg,
+                           float2 *ecg_ff) {
     if (nmove >= h.nleads) return;
     dim3 grid((unsigned)((h.steps + 127) / 128), (unsigned)(h.nleads - nmove), (unsigned)n_sims);
     k_static_combine<<<grid, 128, 0, s>>>(h.steps, h.nleads, h.nlayers, J, Jb, nmove, n_sims, F, coef, k3, Q1, Q2,
-                                          ecg);
+                                          ecg, ecg_ff);
     EKG_CUDA(cudaGetLastError());
 }
 
@@ -1005,11 +1018,13 @@ void launch_reduce_band(cudaStream_t s, const BandArgs &A) {
     if (A.rows_used < 64) {
         dim3 grid((unsigned)((A.steps + 31) / 32), (unsigned)A.rows_used);
         k_reduce_band_w<<<grid, 256, 0, s>>>(A.steps, A.rows, A.nmove, A.n_sims, A.nleads, A.nl, A.ntt, A.max_ent,
-                                             A.nb, A.ti0, A.ti1, A.ent, A.partial, A.U, A.E, A.F, A.k3, A.ecg);
+                                             A.nb, A.ti0, A.ti1, A.ent, A.partial, A.U, A.E, A.F, A.k3, A.ecg,
+                                             A.ecg_ff);
     } else {
         dim3 grid((unsigned)((A.steps + 127) / 128), (unsigned)A.rows_used);
         k_reduce_band<<<grid, 128, 0, s>>>(A.steps, A.rows, A.nmove, A.n_sims, A.nleads, A.nl, A.ntt, A.max_ent,
-                                           A.nb, A.ti0, A.ti1, A.ent, A.partial, A.U, A.E, A.F, A.k3, A.ecg);
+                                           A.nb, A.ti0, A.ti1, A.ent, A.partial, A.U, A.E, A.F, A.k3, A.ecg,
+                                           A.ecg_ff);
     }
     EKG_CUDA(cudaGetLastError());
 }

@@ -219,10 +219,11 @@ __global__ void __launch_bounds__(CC_T) k_contract_cuda(int steps, int nleads, i
 
 // ecg[s][l][t] = k0w[s][l] + sum_c partial[s][c][l][t]: one block per (s, l, 32 steps); warp w
 // sums chunks c = w, w+8, ... for 32 consecutive steps (coalesced), then the 8 warp sums are added
-// in warp order, so the result does not depend on scheduling.
+// in warp order, so the result does not depend on scheduling.  Also writes the float-float copy.
 __global__ void __launch_bounds__(256) k_reduce_ecg(int steps, int nleads, int nchunks,
                                                     const double *__restrict__ partial,
-                                                    const double *__restrict__ k0w, double *__restrict__ ecg) {
+                                                    const double *__restrict__ k0w, double *__restrict__ ecg,
+                                                    float2 *__restrict__ ecg_ff) {
     __shared__ double red[8][33];
     const int tt = blockIdx.x * 32 + (threadIdx.x & 31);
     const int w = threadIdx.x >> 5;
@@ -235,11 +236,13 @@ __global__ void __launch_bounds__(256) k_reduce_ecg(int steps, int nleads, int n
     if (w == 0 && tt < steps) {
         double r = k0w[(size_t)s * nleads + l];
         for (int i = 0; i < 8; ++i) r += red[i][threadIdx.x];
-        ecg[((size_t)s * nleads + l) * steps + tt] = r;
+        const size_t o = ((size_t)s * nleads + l) * steps + tt;
+        ecg[o] = r;
+        ecg_ff[o] = ff_from_double(r);
     }
 }
 
-// ------------------------------------------------------------------ criteria (FP64)
+// ------------------------------------------------------------------ criteria
 // Output per (s, i): value and argmax.
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -253,62 +256,79 @@ __device__ __forceinline__ double warp_max(double v) {
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
+// float-float butterfly sum; lane 0's result is broadcast so every lane holds the same value
+__device__ __forceinline__ double warp_sum_ff(float2 v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const float2 w = make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
+        v = ff_add(v, w);
+    }
+    v.x = __shfl_sync(0xffffffffu, v.x, 0);
+    v.y = __shfl_sync(0xffffffffu, v.y, 0);
+    return ff_to_double(v);
+}
+__device__ __forceinline__ bool ff_greater(float2 a, float2 b) { return a.x > b.x || (a.x == b.x && a.y > b.y); }
 
-// One warp per (simulation, criterion lead): lanes stride over the steps, FP64 sums combined by
-// a fixed butterfly.  Writes the criterion value and the argmax (first maximum) of the lead.
+// One warp per (simulation, criterion lead): lanes stride over the steps, sums combined by a fixed
+// butterfly.  Pearson, vector correlation and RMS accumulate in float-float (about 48 significant
+// bits) on the FP32 pipe, reading the float-float copies of the ECG and targets; the few closing
+// operations (means, square roots, quotients) are FP64.  devFromLinear stays FP64 throughout.
+// Writes the criterion value and the argmax (first maximum) of the lead.
 __global__ void k_criteria(int steps, int nleads, int ncl, int n_sims, int mode, const double *__restrict__ ecg,
-                           const double *__restrict__ targets, const int64_t *__restrict__ tlen,
+                           const float2 *__restrict__ ecg_ff, const double *__restrict__ targets,
+                           const float2 *__restrict__ targets_ff, const int64_t *__restrict__ tlen,
                            const double *__restrict__ toff, int crit_stride, double *__restrict__ crit) {
     const int lane = threadIdx.x & 31;
     const int pair = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (pair >= ncl * n_sims) return;
     const int i = pair % ncl, s = pair / ncl;
-    const double *a = ecg + ((size_t)s * nleads + i) * steps;
+    const size_t row = ((size_t)s * nleads + i) * steps;
+    const float2 *af = ecg_ff + row;
     int64_t off = 0;
     for (int j = 0; j < i; ++j) off += tlen[j];
-    const double *b = targets + off;
+    const float2 *bf = targets_ff + off;
     const int64_t nb = tlen[i];
     const int64_t len = steps < nb ? steps : nb;
     const double inv = 1.0 / (double)len;
     double value = 0.0;
     if (mode == 2) {
-        double sa = 0, sb = 0;
+        float2 sa = make_float2(0.f, 0.f), sb = sa;
         for (int64_t j = lane; j < len; j += 32) {
-            sa += a[j];
-            sb += b[j];
+            sa = ff_add(sa, af[j]);
+            sb = ff_add(sb, bf[j]);
         }
-        const double ma = warp_sum(sa) * inv, mb = warp_sum(sb) * inv;
-        double va = 0, vb = 0, cv = 0;
+        const float2 ma = ff_neg(ff_from_double(warp_sum_ff(sa) * inv));
+        const float2 mb = ff_neg(ff_from_double(warp_sum_ff(sb) * inv));
+        float2 va = make_float2(0.f, 0.f), vb = va, cv = va;
         for (int64_t j = lane; j < len; j += 32) {
-            const double x = a[j] - ma, y = b[j] - mb;
-            va += x * x;
-            vb += y * y;
-            cv += x * y;
+            const float2 x = ff_add(af[j], ma), y = ff_add(bf[j], mb);
+            va = ff_add(va, ff_mul(x, x));
+            vb = ff_add(vb, ff_mul(y, y));
+            cv = ff_add(cv, ff_mul(x, y));
         }
-        va = warp_sum(va) * inv;
-        vb = warp_sum(vb) * inv;
-        cv = warp_sum(cv) / (double)len;
-        value = 1.0 - cv / (sqrt(va) * sqrt(vb));
+        const double dva = warp_sum_ff(va) * inv, dvb = warp_sum_ff(vb) * inv;
+        const double dcv = warp_sum_ff(cv) / (double)len;
+        value = 1.0 - dcv / (sqrt(dva) * sqrt(dvb));
     } else if (mode == 4) {
-        double ab = 0, aa = 0, bb = 0;
+        float2 ab = make_float2(0.f, 0.f), aa = ab, bb = ab;
         for (int64_t j = lane; j < len; j += 32) {
-            ab += a[j] * b[j];
-            aa += a[j] * a[j];
-            bb += b[j] * b[j];
+            const float2 x = af[j], y = bf[j];
+            ab = ff_add(ab, ff_mul(x, y));
+            aa = ff_add(aa, ff_mul(x, x));
+            bb = ff_add(bb, ff_mul(y, y));
         }
-        ab = warp_sum(ab);
-        aa = warp_sum(aa);
-        bb = warp_sum(bb);
-        value = 1.0 - ab / (sqrt(aa) * sqrt(bb));
+        const double dab = warp_sum_ff(ab), daa = warp_sum_ff(aa), dbb = warp_sum_ff(bb);
+        value = 1.0 - dab / (sqrt(daa) * sqrt(dbb));
     } else if (mode == 1) {
-        double q = 0;
+        float2 q = make_float2(0.f, 0.f);
         for (int64_t j = lane; j < len; j += 32) {
-            const double x = a[j] - b[j];
-            q += x * x;
+            const float2 x = ff_add(af[j], ff_neg(bf[j]));
+            q = ff_add(q, ff_mul(x, x));
         }
-        value = sqrt(warp_sum(q) / (double)len);
+        value = sqrt(warp_sum_ff(q) / (double)len);
     } else {
         // devFromLinear (vectorMath.h:373-404): min/max over the whole simulated lead
+        const double *a = ecg + row;
+        const double *b = targets + off;
         double mn = INFINITY, mx = -INFINITY;
         for (int64_t j = lane; j < steps; j += 32) {
             mn = fmin(mn, a[j]);
@@ -327,18 +347,21 @@ __global__ void k_criteria(int steps, int nleads, int ncl, int n_sims, int mode,
         var = warp_sum(var) * inv;
         value = (var == 0) ? 1.0 / 1e-30 : sqrt(var);
     }
-    // argmax of the simulated lead (first maximum), for the peak-position criterion
-    double best = -INFINITY;
+    // argmax of the simulated lead (first maximum), for the peak-position criterion; float-float
+    // values are normalised, so comparing (hi, lo) in order compares the values
+    float2 best = make_float2(-INFINITY, 0.f);
     int arg = 0x7fffffff;
-    for (int j = lane; j < steps; j += 32)
-        if (a[j] > best) {
-            best = a[j];
+    for (int j = lane; j < steps; j += 32) {
+        const float2 v = af[j];
+        if (ff_greater(v, best)) {
+            best = v;
             arg = j;
         }
+    }
     for (int o = 16; o > 0; o >>= 1) {
-        const double v2 = __shfl_xor_sync(0xffffffffu, best, o);
+        const float2 v2 = make_float2(__shfl_xor_sync(0xffffffffu, best.x, o), __shfl_xor_sync(0xffffffffu, best.y, o));
         const int a2 = __shfl_xor_sync(0xffffffffu, arg, o);
-        if (v2 > best || (v2 == best && a2 < arg)) {
+        if (ff_greater(v2, best) || (v2.x == best.x && v2.y == best.y && a2 < arg)) {
             best = v2;
             arg = a2;
         }
@@ -392,20 +415,20 @@ void launch_contract_cuda(cudaStream_t s, const HeartDev &h, const float *d_Wp, 
 }
 
 void launch_reduce_ecg(cudaStream_t s, const HeartDev &h, const double *d_partial, const double *d_k0w,
-                       int n_sims, double *d_ecg) {
+                       int n_sims, double *d_ecg, float2 *d_ecg_ff) {
     dim3 grid((unsigned)((h.steps + 31) / 32), (unsigned)h.nleads, (unsigned)n_sims);
-    k_reduce_ecg<<<grid, 256, 0, s>>>(h.steps, h.nleads, h.nchunks, d_partial, d_k0w, d_ecg);
+    k_reduce_ecg<<<grid, 256, 0, s>>>(h.steps, h.nleads, h.nchunks, d_partial, d_k0w, d_ecg, d_ecg_ff);
     EKG_CUDA(cudaGetLastError());
 }
 
-void launch_criteria(cudaStream_t s, const HeartDev &h, const double *d_ecg, int n_sims, int ncrit_stride,
-                     int n_crit_leads, int mode, const double *d_targets, const int64_t *d_tlen,
-                     const double *d_toff, double *d_crit) {
+void launch_criteria(cudaStream_t s, const HeartDev &h, const double *d_ecg, const float2 *d_ecg_ff, int n_sims,
+                     int ncrit_stride, int n_crit_leads, int mode, const double *d_targets, const float2 *d_targets_ff,
+                     const int64_t *d_tlen, const double *d_toff, double *d_crit) {
     if (n_crit_leads <= 0) return;
     // one warp per block, so the FP64 work of a few simulations spreads over as many SMs as it has warps
     const int64_t pairs = (int64_t)n_crit_leads * n_sims;
-    k_criteria<<<(unsigned)pairs, 32, 0, s>>>(h.steps, h.nleads, n_crit_leads, n_sims, mode, d_ecg, d_targets, d_tlen,
-                                              d_toff, ncrit_stride, d_crit);
+    k_criteria<<<(unsigned)pairs, 32, 0, s>>>(h.steps, h.nleads, n_crit_leads, n_sims, mode, d_ecg, d_ecg_ff,
+                                              d_targets, d_targets_ff, d_tlen, d_toff, ncrit_stride, d_crit);
     EKG_CUDA(cudaGetLastError());
 }
 

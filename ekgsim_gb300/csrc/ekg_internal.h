@@ -43,6 +43,41 @@ int guard(const std::function<void()> &f);
 // Kernel error word bits (written by bounded device waits, read by the host after a pass).
 enum : uint32_t { KERR_MBAR_TIMEOUT = 1u, KERR_TMEM = 2u };
 
+// Float-float ("double-single") arithmetic with error-free transformations (Knuth's two-sum, an
+// FMA two-product): about 48 significant bits on the FP32 pipe, for sums where GB300's FP64 rate
+// would dominate.  The hi part is the float nearest the value, lo the remainder.  The _rn
+// intrinsics keep the compiler from contracting a product into the error-free steps.
+#ifdef __CUDACC__
+__device__ __forceinline__ float2 ff_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+__device__ __forceinline__ float2 ff_norm(float h, float e) {
+    const float s = __fadd_rn(h, e);
+    return make_float2(s, __fsub_rn(e, __fsub_rn(s, h)));
+}
+__device__ __forceinline__ float2 ff_add(float2 x, float2 y) {
+    const float2 s = ff_two_sum(x.x, y.x);
+    return ff_norm(s.x, __fadd_rn(__fadd_rn(s.y, x.y), y.y));
+}
+__device__ __forceinline__ float2 ff_add_f(float2 x, float b) {
+    const float2 s = ff_two_sum(x.x, b);
+    return ff_norm(s.x, __fadd_rn(s.y, x.y));
+}
+__device__ __forceinline__ float2 ff_mul(float2 x, float2 y) {
+    const float p = __fmul_rn(x.x, y.x);
+    const float e = fmaf(x.x, y.y, fmaf(x.y, y.x, fmaf(x.x, y.x, -p)));
+    return ff_norm(p, e);
+}
+__device__ __forceinline__ float2 ff_neg(float2 x) { return make_float2(-x.x, -x.y); }
+__device__ __forceinline__ double ff_to_double(float2 x) { return (double)x.x + (double)x.y; }
+__device__ __forceinline__ float2 ff_from_double(double v) {
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+#endif
+
 // device buffer owning helper
 template <class T>
 struct DBuf {
@@ -129,8 +164,10 @@ struct EvalDev {
     DBuf<float> Wp;         // [S][L][apad] W * exp(k5 at)
     DBuf<double> partial;   // [S][nchunks][L][steps]
     DBuf<double> ecg;       // [S][L][steps]
+    DBuf<float2> ecg_ff;    // [S][L][steps] the same as float-float (hi, lo), read by the criteria
     DBuf<double> crit;      // [S][ncrit]
     DBuf<double> targets;   // concatenated targets
+    DBuf<float2> targets_ff;  // the same as float-float
     DBuf<int64_t> target_len;
     DBuf<double> target_off;
     DBuf<uint32_t> err;     // [1]
@@ -189,6 +226,7 @@ struct BandArgs {
     float2 *Up = nullptr;            // [band_u_parts()][rows][nl][max_ent]
     float2 *U = nullptr;             // [rows][nl][max_ent]
     double *ecg = nullptr;
+    float2 *ecg_ff = nullptr;
 };
 int batch_tile_rows(int two_bases, int rows_used);
 void launch_taylor_w(cudaStream_t s, const HeartDev &h, const float *W0, int J, const double *centre,
@@ -196,7 +234,8 @@ void launch_taylor_w(cudaStream_t s, const HeartDev &h, const float *W0, int J, 
 void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int32_t *lc0, const int32_t *lc1,
                           const double *partial, float *Q);
 void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const float *F,
-                           const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg);
+                           const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg,
+                           float2 *ecg_ff);
 void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const float *k5l,
                              const float4 *hconst, const float4 *lrel, int nmove, int n_sims, const BandArgs &B,
                              uint8_t *Bt, int *work, int sm_count);
@@ -205,9 +244,9 @@ int band_u_parts();
 void launch_band_u(cudaStream_t s, const BandArgs &a);
 void launch_reduce_band(cudaStream_t s, const BandArgs &a);
 void launch_reduce_ecg(cudaStream_t s, const HeartDev &h, const double *d_partial, const double *d_k0w,
-                       int n_sims, double *d_ecg);
-void launch_criteria(cudaStream_t s, const HeartDev &h, const double *d_ecg, int n_sims, int ncrit_stride,
-                     int n_crit_leads, int mode, const double *d_targets, const int64_t *d_tlen,
-                     const double *d_toff, double *d_crit);
+                       int n_sims, double *d_ecg, float2 *d_ecg_ff);
+void launch_criteria(cudaStream_t s, const HeartDev &h, const double *d_ecg, const float2 *d_ecg_ff, int n_sims,
+                     int ncrit_stride, int n_crit_leads, int mode, const double *d_targets, const float2 *d_targets_ff,
+                     const int64_t *d_tlen, const double *d_toff, double *d_crit);
 
 }  // namespace ekg

@@ -536,7 +536,8 @@ int64_t heart_device_bytes(const ekg_heart *h) {
                 h->W0.bytes() + h->at_cells.bytes();
     const EvalDev &E = h->ev;
     b += (int64_t)h->stage_dev.bytes() + E.layer_c.bytes() + E.F.bytes() + E.k0w.bytes() + E.W.bytes() +
-         E.Wp.bytes() + E.partial.bytes() + E.ecg.bytes() + E.crit.bytes() + E.targets.bytes();
+         E.Wp.bytes() + E.partial.bytes() + E.ecg.bytes() + E.ecg_ff.bytes() + E.crit.bytes() + E.targets.bytes() +
+         E.targets_ff.bytes();
     return b;
 }
 
@@ -545,7 +546,7 @@ int64_t eval_bytes_per_sim(const ekg_heart *h) {
     const HeartDev &D = h->dev;
     const int64_t L = D.nleads, nl = D.nlayers;
     return nl * 9 * 8 + L * 3 * 8 + nl * 4 * 4 + nl * D.steps * 8 + L * 8 + 2 * L * D.apad * 4 +
-           (int64_t)D.nchunks * L * D.steps * 8 + L * D.steps * 8 + std::max<int64_t>(1, L) * 2 * 8;
+           (int64_t)D.nchunks * L * D.steps * 8 + 2 * L * D.steps * 8 + std::max<int64_t>(1, L) * 2 * 8;
 }
 int64_t eval_bytes_held(const ekg_heart *h) { return (int64_t)h->ev.cap_sims * eval_bytes_per_sim(h); }
 
@@ -559,6 +560,7 @@ void ensure_eval_capacity(ekg_heart *h, int n_sims) {
     E.Ff.alloc(S * D.nlayers * D.steps);
     E.k0w.alloc(S * D.nleads);
     E.ecg.alloc(S * D.nleads * D.steps);
+    E.ecg_ff.alloc(S * D.nleads * D.steps);
     E.crit.alloc(S * std::max(1, D.nleads) * 2);
     E.err.alloc(1);
     E.cap_sims = n_sims;
@@ -1025,7 +1027,8 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
     ++launches;
     if (P.batch) {
         BatchState &B = h->bs;
-        launch_static_combine(s, D, P.J, B.J, nmove, n_sims, E.Ff.p, in.coef, in.k3, B.Q1.p, B.Q2.p, E.ecg.p);
+        launch_static_combine(s, D, P.J, B.J, nmove, n_sims, E.Ff.p, in.coef, in.k3, B.Q1.p, B.Q2.p, E.ecg.p,
+                              E.ecg_ff.p);
         launches += nmove < (int)L;
         if (mark_static) {
             // inside a graph capture the record must be an external event node (the copy stream waits
@@ -1067,6 +1070,7 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             U.U = B.U.p;
             U.Up = B.Up.p;
             U.ecg = E.ecg.p;
+            U.ecg_ff = E.ecg_ff.p;
             if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[4], s));
             launch_batch_lead_field(s, D, P.two_bases, in.k5l, in.hconst, in.lrel, nmove, n_sims, U, B.Bt.p,
                                     B.work.p, h->sm_count);
@@ -1123,12 +1127,12 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
         if (h->eng->umma) launch_contract_umma(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p, E.err.p);
         else launch_contract_cuda(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p);
         if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[2], s));
-        launch_reduce_ecg(s, D, E.partial.p, E.k0w.p, n_sims, E.ecg.p);
+        launch_reduce_ecg(s, D, E.partial.p, E.k0w.p, n_sims, E.ecg.p, E.ecg_ff.p);
         launches += 2;
     }
     if (n_crit_leads > 0) {
-        launch_criteria(s, D, E.ecg.p, n_sims, n_crit_leads, n_crit_leads, mode, E.targets.p, E.target_len.p,
-                        E.target_off.p, E.crit.p);
+        launch_criteria(s, D, E.ecg.p, E.ecg_ff.p, n_sims, n_crit_leads, n_crit_leads, mode, E.targets.p,
+                        E.targets_ff.p, E.target_len.p, E.target_off.p, E.crit.p);
         ++launches;
     }
     if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[3], s));
@@ -1151,7 +1155,7 @@ std::vector<uint64_t> pass_signature(const ekg_heart *h, const PassPlan &P, int 
                           (const void *)in.items, (const void *)in.ti0, (const void *)in.ti1,
                           (const void *)E.F.p, (const void *)E.Ff.p,
                           (const void *)E.layer_c.p, (const void *)E.ecg.p, (const void *)E.crit.p, (const void *)E.err.p,
-                          (const void *)E.targets.p, (const void *)E.target_len.p, (const void *)E.target_off.p,
+                          (const void *)E.ecg_ff.p, (const void *)E.targets_ff.p, (const void *)E.targets.p, (const void *)E.target_len.p, (const void *)E.target_off.p,
                           (const void *)E.W.p, (const void *)E.Wp.p, (const void *)E.partial.p, (const void *)E.k0w.p,
                           (const void *)B.Q1.p,
                           (const void *)B.Q2.p, (const void *)B.Bt.p, (const void *)B.P1.p, (const void *)B.U.p,
@@ -1530,10 +1534,20 @@ void set_eval(ekg_heart *h, const ekg_eval_config *c) {
     // device copies of the targets
     EvalDev &E = h->ev;
     E.targets.alloc(off);
+    E.targets_ff.alloc(off);
     E.target_len.alloc(c->n_targets);
     E.target_off.alloc(c->n_targets);
     EKG_CUDA(cudaSetDevice(h->eng->device));
     EKG_CUDA(cudaMemcpy(E.targets.p, c->targets, off * 8, cudaMemcpyHostToDevice));
+    {
+        // float-float split of the targets for the criteria: hi the nearest float, lo the remainder
+        std::vector<float2> ff(off);
+        for (size_t i = 0; i < off; ++i) {
+            const float hi = (float)c->targets[i];
+            ff[i] = make_float2(hi, (float)(c->targets[i] - (double)hi));
+        }
+        EKG_CUDA(cudaMemcpy(E.targets_ff.p, ff.data(), off * sizeof(float2), cudaMemcpyHostToDevice));
+    }
     EKG_CUDA(cudaMemcpy(E.target_len.p, c->target_len, c->n_targets * 8, cudaMemcpyHostToDevice));
     EKG_CUDA(cudaMemcpy(E.target_off.p, es.target_offsets.data(), c->n_targets * 8, cudaMemcpyHostToDevice));
     h->es = es;
