@@ -117,33 +117,61 @@ __global__ void k_reduce_layers(int steps, int rows, int nl, const int32_t *__re
 
 // Static leads: ecg[s][l][t] = sum_L F[s][L][t] sum_j coef[s][L][j] ((1-k3) Q1 + k3 Q2)[L][l*J+j][t],
 // the Taylor sum per layer in FP32 (the basis is stored in FP32), the sum over layers in
-// float-float; written as FP64 and as float-float.
-__global__ void k_static_combine(int steps, int nleads, int nl, int J, int Jb, int nmove, int n_sims,
-                                 const float *__restrict__ F, const float *__restrict__ coef,
-                                 const double *__restrict__ k3, const float *__restrict__ Q1,
-                                 const float *__restrict__ Q2, double *__restrict__ ecg,
-                                 float2 *__restrict__ ecg_ff) {
+// float-float; written as FP64 and as float-float.  Block = 128 steps of one static lead for
+// SC_SIMS simulations: a thread loads the basis rows of its step once per layer and applies them
+// to every simulation of the group (coefficients broadcast from shared memory).
+constexpr int SC_SIMS = 16;
+__global__ void __launch_bounds__(128) k_static_combine(int steps, int nleads, int nl, int J, int Jb, int nmove,
+                                                        int n_sims, const float *__restrict__ F,
+                                                        const float *__restrict__ coef, const double *__restrict__ k3,
+                                                        const float *__restrict__ Q1, const float *__restrict__ Q2,
+                                                        double *__restrict__ ecg, float2 *__restrict__ ecg_ff) {
+    __shared__ float s_c[SC_SIMS][11];  // [simulation][j < J: coefficient, 10: k3] of the current layer
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int l = nmove + blockIdx.y, s = blockIdx.z;
-    if (t >= steps || l >= nleads) return;
+    const int l = nmove + blockIdx.y, s0 = blockIdx.z * SC_SIMS;
+    const int ns = min(SC_SIMS, n_sims - s0);
+    const bool on = t < steps;
+    const int tc = on ? t : steps - 1;
     const int rows = nleads * Jb;  // the basis stores Jb terms per lead
-    float2 acc = make_float2(0.f, 0.f);
-    for (int L = 0; L < nl; ++L) {
-        const float kk = (float)k3[(size_t)s * nl + L];
-        const float *c = coef + ((size_t)s * nl + L) * J;
-        const size_t q0 = ((size_t)L * rows + (size_t)l * Jb) * steps + t;
-        float v1 = 0.f, v2 = 0.f;
+    float2 acc[SC_SIMS];
 #pragma unroll
-        for (int j = 0; j < 10; ++j)  // J <= 10 (the basis order); unrolled so the loads issue together
-            if (j < J) {
-                v1 = fmaf(c[j], Q1[q0 + (size_t)j * steps], v1);
-                v2 = fmaf(c[j], Q2[q0 + (size_t)j * steps], v2);
+    for (int i = 0; i < SC_SIMS; ++i) acc[i] = make_float2(0.f, 0.f);
+    for (int L = 0; L < nl; ++L) {
+        __syncthreads();
+        for (int k = threadIdx.x; k < ns * 11; k += blockDim.x) {
+            const int i = k / 11, j = k % 11;
+            const size_t sl = (size_t)(s0 + i) * nl + L;
+            s_c[i][j] = j < J ? coef[sl * J + j] : (j == 10 ? (float)k3[sl] : 0.f);
+        }
+        __syncthreads();
+        const size_t q0 = ((size_t)L * rows + (size_t)l * Jb) * steps + tc;
+        float q1[10], q2[10];
+#pragma unroll
+        for (int j = 0; j < 10; ++j) {  // J <= 10 (the basis order)
+            q1[j] = j < J ? Q1[q0 + (size_t)j * steps] : 0.f;
+            q2[j] = j < J ? Q2[q0 + (size_t)j * steps] : 0.f;
+        }
+#pragma unroll
+        for (int i = 0; i < SC_SIMS; ++i)
+            if (i < ns) {
+                float v1 = 0.f, v2 = 0.f;
+#pragma unroll
+                for (int j = 0; j < 10; ++j)
+                    if (j < J) {
+                        v1 = fmaf(s_c[i][j], q1[j], v1);
+                        v2 = fmaf(s_c[i][j], q2[j], v2);
+                    }
+                acc[i] = ff_add_f(acc[i], F[((size_t)(s0 + i) * nl + L) * steps + tc] * fmaf(s_c[i][10], v2 - v1, v1));
             }
-        acc = ff_add_f(acc, F[((size_t)s * nl + L) * steps + t] * fmaf(kk, v2 - v1, v1));
     }
-    const size_t o = ((size_t)s * nleads + l) * steps + t;
-    ecg[o] = ff_to_double(acc);
-    ecg_ff[o] = acc;
+    if (!on) return;
+#pragma unroll
+    for (int i = 0; i < SC_SIMS; ++i)
+        if (i < ns) {
+            const size_t o = ((size_t)(s0 + i) * nleads + l) * steps + t;
+            ecg[o] = ff_to_double(acc[i]);
+            ecg_ff[o] = acc[i];
+        }
 }
 
 // ------------------------------------------------------------------ moved-lead operand
@@ -559,12 +587,14 @@ __global__ void __launch_bounds__(256) k_band_u2(int64_t n_out, const float2 *__
 constexpr int WKT = 32;              // APs per stage
 constexpr int SA = 3, SB = 4;        // ring depths
 constexpr int DRAIN = 512 / WKT;     // stages per accumulation segment
+static_assert(SA <= SB, "producers read a stage's activation times from its B slot");
 constexpr int WS_THREADS = 320;      // 8 producer warps + bulk-copy warp + MMA warp
 
 template <int NB, int N>
 struct BatchSmem {
     alignas(1024) uint8_t a[SA][NB][2][BM * WKT * 2];  // [stage][basis][hi/lo]
     alignas(1024) uint8_t b[SB][2][N * WKT * 2];       // [stage][hi/lo]
+    alignas(16) float2 at[SB][WKT];                     // activation times of the stage's APs
     alignas(8) uint64_t a_full[SA], a_empty[SA], b_full[SB], b_empty[SB], acc_full[2], acc_empty[2];
     uint32_t tmem_base;
 };
@@ -668,14 +698,22 @@ __global__ void __launch_bounds__(WS_THREADS, (N <= 32 ? 2 : 1)) k_batch_umma(
                 ok = false;
                 break;
             }
-            const float2 *atp = at_hilo + (size_t)(st0 + i) * WKT + half * 16;
+            // the stage's activation times arrive with its B operand (the B slot is recycled only
+            // after the MMAs of this stage, which wait for this production, and SA <= SB keeps
+            // the wait within the slot's current phase)
+            const int sb = i % SB;
+            if (!mbar_wait(&S.b_full[sb], (uint32_t)((i / SB) & 1))) {
+                ok = false;
+                break;
+            }
+            const float2 *atp = S.at[sb] + half * 16;
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
                 const int kc8 = half * 2 + j;
                 float v1[8], v2[8];
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
-                    const float2 at = __ldg(atp + j * 8 + e);
+                    const float2 at = atp[j * 8 + e];
                     const float tau = (th.x - at.x) + (th.y - at.y);
                     const float e1 = ex2a(-hc.x * tau);
                     const float sg = rcpa(1.0f + e1);
@@ -737,9 +775,10 @@ __global__ void __launch_bounds__(WS_THREADS, (N <= 32 ? 2 : 1)) k_batch_umma(
             }
             const int st = st0 + i;
             const uint8_t *src = Bt + ((size_t)nt * nkt + st / 2) * 2 * BTILE + (size_t)(st & 1) * BSTAGE;
-            mbar_expect_tx(&S.b_full[sb], 2 * BSTAGE);
+            mbar_expect_tx(&S.b_full[sb], 2 * BSTAGE + WKT * (uint32_t)sizeof(float2));
             bulk_g2s(S.b[sb][0], src, BSTAGE, &S.b_full[sb]);
             bulk_g2s(S.b[sb][1], src + BTILE, BSTAGE, &S.b_full[sb]);
+            bulk_g2s(S.at[sb], at_hilo + (size_t)st * WKT, WKT * (uint32_t)sizeof(float2), &S.b_full[sb]);
         }
     } else if (warp == 9 && lane == 0) {
         // ---------------- MMA issue
@@ -934,7 +973,7 @@ void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int
                            const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg,
                            float2 *ecg_ff) {
     if (nmove >= h.nleads) return;
-    dim3 grid((unsigned)((h.steps + 127) / 128), (unsigned)(h.nleads - nmove), (unsigned)n_sims);
+    dim3 grid((unsigned)((h.steps + 127) / 128), (unsigned)(h.nleads - nmove), (unsigned)((n_sims + SC_SIMS - 1) / SC_SIMS));
     k_static_combine<<<grid, 128, 0, s>>>(h.steps, h.nleads, h.nlayers, J, Jb, nmove, n_sims, F, coef, k3, Q1, Q2,
                                           ecg, ecg_ff);
     EKG_CUDA(cudaGetLastError());
