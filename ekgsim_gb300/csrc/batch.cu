@@ -197,8 +197,14 @@ __global__ void __launch_bounds__(128) k_static_combine(int steps, int nleads, i
 // moments, computed on the host; the 8 body diagonals give 168 - 280 T4 and 4320 - 15120 T4 +
 // 11088 T6).  The next term is smaller by about 20/|m|^2; the form is used for |m| >= 20, where it
 // is closer to the exact sum than the FP32 evaluation of the eight cancelling neighbour terms.
+// Evaluated through the symmetric functions of the squares a, b, c of m's components:
+// s = a + b + c, P = ab + bc + ca, Q = abc, so that T4 = 1 - 2 P/s^2 and T6 = 1 - 3 P/s^2 + 3 Q/s^3;
+// with u = 1/s = rho^2 the field is
+//     w = rho u^2 [(A0 + u B0) + u^2 (P (A1 + u B1) + u^2 B2 Q)],
+// A0 = a0 + a1, A1 = -2 a1, B0 = b0 + b1 + b2, B1 = -3 b2 - 2 b1, B2 = 3 b2 for the coefficients
+// of rho^5 (a1 T4 + a0) + rho^7 (b2 T6 + b1 T4 + b0) (about 20 FP32 operations and one rsqrt).
 struct InteriorField {
-    float a0 = 0, a1 = 0, b0 = 0, b1 = 0, b2 = 0;  // rho^5 (a1 T4 + a0) + rho^7 (b2 T6 + b1 T4 + b0)
+    float A0 = 0, A1 = 0, B0 = 0, B1 = 0, B2 = 0;
 };
 // Flag bits above the neighbour mask in vox_pos.w (the mask uses at most 26 bits).
 constexpr uint32_t VOX_INTERIOR = 1u << 31;  // every neighbour present, out-neighbour offsets sum to 0
@@ -207,21 +213,27 @@ constexpr uint32_t VOX_AP_END = 1u << 30;    // last voxel of its AP (voxels are
 // closed form of the interior field for m = r - v, used where |m|^2 >= INTERIOR_S_MIN for every lead
 // of the lane (a lead displaced towards the heart takes the exact sum for the voxels near it)
 constexpr float INTERIOR_S_MIN = 400.f;
-__device__ __forceinline__ float sq3(float4 pos, float4 r) {
+struct MSquares {
+    float a, b, c, h, s;  // squares of m's components, h = a + b, s = h + c = |m|^2
+};
+__device__ __forceinline__ MSquares msq(float4 pos, float4 r) {
     const float mz = r.x - pos.x, my = r.y - pos.y, mx = r.z - pos.z;
-    return fmaf(mz, mz, fmaf(my, my, mx * mx));
+    MSquares q;
+    q.a = mz * mz;
+    q.b = my * my;
+    q.c = mx * mx;
+    q.h = q.a + q.b;
+    q.s = q.h + q.c;
+    return q;
 }
-__device__ __forceinline__ float interior_w(const InteriorField &ic, float4 pos, float4 r, float s0) {
-    const float mz = r.x - pos.x, my = r.y - pos.y, mx = r.z - pos.z;
-    const float z2 = mz * mz, y2 = my * my, x2 = mx * mx;
-    const float z4 = z2 * z2, y4 = y2 * y2, x4 = x2 * x2;
-    const float S4 = z4 + y4 + x4;
-    const float S6 = fmaf(z4, z2, fmaf(y4, y2, x4 * x2));
-    const float rho = rsqa(s0);
-    const float i2 = rho * rho, i4 = i2 * i2;
-    const float T4 = S4 * i4, T6 = S6 * (i4 * i2);
-    const float inner = fmaf(ic.b2, T6, fmaf(ic.b1, T4, ic.b0));
-    return (rho * i4) * fmaf(i2, inner, fmaf(ic.a1, T4, ic.a0));
+__device__ __forceinline__ float interior_w(const InteriorField &ic, const MSquares &q) {
+    const float rho = rsqa(q.s);
+    const float u = rho * rho, u2 = u * u;
+    const float ab = q.a * q.b;
+    const float P = fmaf(q.c, q.h, ab), Q = ab * q.c;
+    const float c1 = fmaf(u, ic.B0, ic.A0), c2 = fmaf(u, ic.B1, ic.A1);
+    const float inner = fmaf(P, c2, Q * (ic.B2 * u2));
+    return (rho * u2) * fmaf(u2, inner, c1);
 }
 
 // w(v) for one lead position r relative to the same centre as the voxel positions, general
@@ -285,10 +297,10 @@ __device__ __forceinline__ void chunk_w(int64_t a0, const int64_t *__restrict__ 
     for (int v = vb; v < vend; ++v) {
         const float4 pos = vox_pos[v];
         const uint32_t mi = __float_as_uint(pos.w);
-        const float s0 = sq3(pos, r0), s1 = NP == 2 ? sq3(pos, r1) : s0;
-        if ((mi & VOX_INTERIOR) && s0 >= INTERIOR_S_MIN && s1 >= INTERIOR_S_MIN) {
-            acc0 += interior_w(ic, pos, r0, s0);
-            if (NP == 2) acc1 += interior_w(ic, pos, r1, s1);
+        const MSquares q0 = msq(pos, r0), q1 = NP == 2 ? msq(pos, r1) : q0;
+        if ((mi & VOX_INTERIOR) && q0.s >= INTERIOR_S_MIN && q1.s >= INTERIOR_S_MIN) {
+            acc0 += interior_w(ic, q0);
+            if (NP == 2) acc1 += interior_w(ic, q1);
         } else {
             const float4 out = vox_out[v];
             acc0 += DIAG ? voxel_w_diag(pos, mi, out, r0) : voxel_w_general(pos, mi, out, r0, nnb, s_d);
@@ -476,10 +488,10 @@ __global__ void __launch_bounds__(128) k_batch_lead_field_small(
             for (int v = vb; v < ve; ++v) {
                 const float4 pos = vox_pos[v];
                 const uint32_t mi = __float_as_uint(pos.w);
-                const float s0 = sq3(pos, r0), s1 = sq3(pos, r1);
-                if ((mi & VOX_INTERIOR) && s0 >= INTERIOR_S_MIN && s1 >= INTERIOR_S_MIN) {
-                    acc0 += interior_w(ic, pos, r0, s0);
-                    if (np == 2) acc1 += interior_w(ic, pos, r1, s1);
+                const MSquares q0 = msq(pos, r0), q1 = msq(pos, r1);
+                if ((mi & VOX_INTERIOR) && q0.s >= INTERIOR_S_MIN && q1.s >= INTERIOR_S_MIN) {
+                    acc0 += interior_w(ic, q0);
+                    if (np == 2) acc1 += interior_w(ic, q1);
                 } else {
                     const float4 out = vox_out[v];
                     acc0 += DIAG ? voxel_w_diag(pos, mi, out, r0) : voxel_w_general(pos, mi, out, r0, nnb, s_d);
@@ -987,11 +999,11 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, c
     const bool diag = h.nhood == EKG_NHOOD_3D4;
     const bool small = n_sims <= SMALL_SIMS;
     InteriorField ic;
-    ic.a0 = h.interior_c[0];
-    ic.a1 = h.interior_c[1];
-    ic.b0 = h.interior_c[2];
-    ic.b1 = h.interior_c[3];
-    ic.b2 = h.interior_c[4];
+    ic.A0 = h.interior_c[0];
+    ic.A1 = h.interior_c[1];
+    ic.B0 = h.interior_c[2];
+    ic.B1 = h.interior_c[3];
+    ic.B2 = h.interior_c[4];
     EKG_CUDA(cudaMemsetAsync(work, 0, sizeof(int), s));
 #define EKG_LF(NN, DG)                                                                                            \
     do {                                                                                                          \

@@ -144,7 +144,8 @@ struct HeartDev {
     int8_t nb_dif[26 * 3];
     DBuf<int8_t> difs;      // [nnb*3] device copy of nb_dif
     // closed form of the field of a voxel with every neighbour present (moved-lead operand):
-    // rho^5 (c1 T4 + c0) + rho^7 (c4 T6 + c3 T4 + c2); mask 0 when the set lacks cube symmetry
+    // coefficients A0, A1, B0, B1, B2 of rho u^2 [(A0 + u B0) + u^2 (P (A1 + u B1) + u^2 B2 Q)];
+    // mask 0 when the set lacks cube symmetry
     float interior_c[5] = {0, 0, 0, 0, 0};
     uint32_t interior_mask = 0;
     int64_t n_interior = 0;  // voxels flagged interior

@@ -90,11 +90,14 @@ void interior_field(HeartDev &D) {
         g6 += 90 * x * x * y * y * z * z;
     }
     const double f4 = (a4 - b4 / 2) / 6, f6 = (a6 - b6 + g6 / 3) / 120;
-    D.interior_c[0] = (float)(-63 * f4);
-    D.interior_c[1] = (float)(105 * f4);
-    D.interior_c[2] = (float)(4050 * f6);
-    D.interior_c[3] = (float)(-14175 * f6);
-    D.interior_c[4] = (float)(10395 * f6);
+    // rho^5 (a1 T4 + a0) + rho^7 (b2 T6 + b1 T4 + b0) with a0 = -63 f4, a1 = 105 f4, b0 = 4050 f6,
+    // b1 = -14175 f6, b2 = 10395 f6, stored as the coefficients of the symmetric-function form
+    // A0 = a0 + a1, A1 = -2 a1, B0 = b0 + b1 + b2, B1 = -3 b2 - 2 b1, B2 = 3 b2
+    D.interior_c[0] = (float)(42 * f4);
+    D.interior_c[1] = (float)(-210 * f4);
+    D.interior_c[2] = (float)(270 * f6);
+    D.interior_c[3] = (float)(-2835 * f6);
+    D.interior_c[4] = (float)(31185 * f6);
     D.interior_mask = D.nnb >= 32 ? 0xFFFFFFFFu : (1u << D.nnb) - 1u;
 }
 
