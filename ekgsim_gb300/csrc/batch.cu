@@ -209,6 +209,7 @@ struct InteriorField {
 // Flag bits above the neighbour mask in vox_pos.w (the mask uses at most 26 bits).
 constexpr uint32_t VOX_INTERIOR = 1u << 31;  // every neighbour present, out-neighbour offsets sum to 0
 constexpr uint32_t VOX_AP_END = 1u << 30;    // last voxel of its AP (voxels are grouped by AP)
+constexpr uint32_t VOX_FEW = 1u << 29;       // not interior, few neighbours absent (closed form minus them)
 
 // closed form of the interior field for m = r - v, used where |m|^2 >= INTERIOR_S_MIN for every lead
 // of the lane (a lead displaced towards the heart takes the exact sum for the voxels near it)
@@ -226,8 +227,7 @@ __device__ __forceinline__ MSquares msq(float4 pos, float4 r) {
     q.s = q.h + q.c;
     return q;
 }
-__device__ __forceinline__ float interior_w(const InteriorField &ic, const MSquares &q) {
-    const float rho = rsqa(q.s);
+__device__ __forceinline__ float interior_w(const InteriorField &ic, const MSquares &q, float rho) {
     const float u = rho * rho, u2 = u * u;
     const float ab = q.a * q.b;
     const float P = fmaf(q.c, q.h, ab), Q = ab * q.c;
@@ -282,25 +282,62 @@ __device__ __forceinline__ float voxel_w_diag(float4 pos, uint32_t mi, float4 ou
     return w;
 }
 
+// A voxel flagged VOX_FEW with the lane's leads at least 20 cells away: the field of the full set
+// (closed form) minus the terms of the absent neighbours `miss`, minus the out-neighbour term,
+//     w = W_full(m) - sum_{n in miss} y_n |m - d_n|^-3 - |m|^-3 m.out,
+// one rsqrt per absent neighbour instead of one per present one.  The loop over the absent
+// neighbours is uniform over the warp (one voxel per warp), shared by the NP leads.
+template <int NP>
+__device__ __forceinline__ void few_w(const InteriorField &ic, const MSquares &q0, const MSquares &q1, float4 pos,
+                                      float4 r0, float4 r1, uint32_t miss, float4 out, const float *s_d, float &acc0,
+                                      float &acc1) {
+    const float mz0 = r0.x - pos.x, my0 = r0.y - pos.y, mx0 = r0.z - pos.z;
+    const float mz1 = r1.x - pos.x, my1 = r1.y - pos.y, mx1 = r1.z - pos.z;
+    const float rho0 = rsqa(q0.s), rho1 = NP == 2 ? rsqa(q1.s) : rho0;
+    float w0 = interior_w(ic, q0, rho0), w1 = NP == 2 ? interior_w(ic, q1, rho1) : 0.f;
+    for (; miss; miss &= miss - 1) {
+        const float4 d = reinterpret_cast<const float4 *>(s_d)[__ffs(miss) - 1];
+        const float y0 = fmaf(mz0, d.x, fmaf(my0, d.y, mx0 * d.z)) - d.w;
+        const float rs0 = rsqa(fmaf(-2.f, y0, q0.s - d.w));
+        w0 = fmaf(-(rs0 * rs0 * rs0), y0, w0);
+        if (NP == 2) {
+            const float y1 = fmaf(mz1, d.x, fmaf(my1, d.y, mx1 * d.z)) - d.w;
+            const float rs1 = rsqa(fmaf(-2.f, y1, q1.s - d.w));
+            w1 = fmaf(-(rs1 * rs1 * rs1), y1, w1);
+        }
+    }
+    if (out.w != 0.f) {
+        w0 = fmaf(-(rho0 * rho0 * rho0), fmaf(mz0, out.x, fmaf(my0, out.y, mx0 * out.z)), w0);
+        if (NP == 2) w1 = fmaf(-(rho1 * rho1 * rho1), fmaf(mz1, out.x, fmaf(my1, out.y, mx1 * out.z)), w1);
+    }
+    acc0 += w0;
+    if (NP == 2) acc1 += w1;
+}
+
 // sum_{v in a} w(v) for the 8 APs of chunk a0 and NP lead positions, into s_w[q][j][tid]: one flat
 // loop over the chunk's voxels (grouped by AP, the last one of each AP flagged); APs without
 // voxels (padding, at the end of a layer) get 0.  Interior voxels use the closed form where the
-// lane's leads are at least 20 cells away (lanes normally agree), the rest the exact sum.
+// lane's leads are at least 20 cells away (lanes normally agree), boundary voxels with few absent
+// neighbours the closed form minus those, the rest the exact sum.
 template <bool DIAG, int NP>
 __device__ __forceinline__ void chunk_w(int64_t a0, const int64_t *__restrict__ a_vox_begin,
                                         const float4 *__restrict__ vox_pos, const float4 *__restrict__ vox_out,
                                         float4 r0, float4 r1, int nnb, const float *s_d, const InteriorField &ic,
                                         float (*s_w)[8][LF_THREADS], int tid) {
     const int vb = (int)a_vox_begin[a0], vend = (int)a_vox_begin[a0 + 8];
+    const uint32_t full = (1u << nnb) - 1u;
     float acc0 = 0.f, acc1 = 0.f;
     int j = 0;
     for (int v = vb; v < vend; ++v) {
         const float4 pos = vox_pos[v];
         const uint32_t mi = __float_as_uint(pos.w);
         const MSquares q0 = msq(pos, r0), q1 = NP == 2 ? msq(pos, r1) : q0;
-        if ((mi & VOX_INTERIOR) && q0.s >= INTERIOR_S_MIN && q1.s >= INTERIOR_S_MIN) {
-            acc0 += interior_w(ic, q0);
-            if (NP == 2) acc1 += interior_w(ic, q1);
+        const bool far = q0.s >= INTERIOR_S_MIN && q1.s >= INTERIOR_S_MIN;
+        if ((mi & VOX_INTERIOR) && far) {
+            acc0 += interior_w(ic, q0, rsqa(q0.s));
+            if (NP == 2) acc1 += interior_w(ic, q1, rsqa(q1.s));
+        } else if ((mi & VOX_FEW) && far) {
+            few_w<NP>(ic, q0, q1, pos, r0, r1, full & ~mi, vox_out[v], s_d, acc0, acc1);
         } else {
             const float4 out = vox_out[v];
             acc0 += DIAG ? voxel_w_diag(pos, mi, out, r0) : voxel_w_general(pos, mi, out, r0, nnb, s_d);
@@ -490,8 +527,8 @@ __global__ void __launch_bounds__(128) k_batch_lead_field_small(
                 const uint32_t mi = __float_as_uint(pos.w);
                 const MSquares q0 = msq(pos, r0), q1 = msq(pos, r1);
                 if ((mi & VOX_INTERIOR) && q0.s >= INTERIOR_S_MIN && q1.s >= INTERIOR_S_MIN) {
-                    acc0 += interior_w(ic, q0);
-                    if (np == 2) acc1 += interior_w(ic, q1);
+                    acc0 += interior_w(ic, q0, rsqa(q0.s));
+                    if (np == 2) acc1 += interior_w(ic, q1, rsqa(q1.s));
                 } else {
                     const float4 out = vox_out[v];
                     acc0 += DIAG ? voxel_w_diag(pos, mi, out, r0) : voxel_w_general(pos, mi, out, r0, nnb, s_d);

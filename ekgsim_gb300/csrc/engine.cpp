@@ -433,6 +433,9 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     std::vector<uint32_t> vin(nv), vout(nv);
     std::vector<float4> vpos_v(nv), vosum(nv);
     std::vector<int64_t> interior_parts(64, 0);
+    // absent neighbours up to which the closed form minus their terms is cheaper than the sum over
+    // the present ones (the 8 body diagonals have a cheaper direct sum)
+    const int few_max = D.nhood == EKG_NHOOD_3D4 ? 2 : D.nnb / 2;
     const size_t vparts = (size_t)std::min<int64_t>(64, std::max<int64_t>(1, nv / 4096));
     HostPool::get().run(vparts, [&](size_t pb, size_t pe) {
         for (size_t part = pb; part < pe; ++part) {
@@ -466,10 +469,12 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
                     }
                 uint32_t mbits = mi;
                 // flags for the moved-lead operand kernel (batch.cu): interior voxel (closed-form field),
-                // last voxel of its AP
+                // boundary voxel with few absent neighbours, last voxel of its AP
                 if (D.interior_mask && mi == D.interior_mask && oz == 0 && oy == 0 && ox == 0) {
                     mbits |= 1u << 31;
                     ++cnt_int;
+                } else if (D.interior_mask && __builtin_popcount(D.interior_mask & ~mi) <= few_max) {
+                    mbits |= 1u << 29;  // few absent neighbours: closed form minus their terms
                 }
                 if (gend[i]) mbits |= 1u << 30;
                 float mf;
