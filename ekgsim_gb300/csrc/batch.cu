@@ -286,35 +286,38 @@ __device__ __forceinline__ float voxel_w_diag(float4 pos, uint32_t mi, float4 ou
 // (closed form) minus the terms of the absent neighbours `miss`, minus the out-neighbour term,
 //     w = W_full(m) - sum_{n in miss} y_n |m - d_n|^-3 - |m|^-3 m.out,
 // one rsqrt per absent neighbour instead of one per present one.  The loop over the absent
-// neighbours is uniform over the warp (one voxel per warp), shared by the NP leads.
+// neighbours is uniform over the warp (one voxel per warp), shared by the NP lead positions.
 template <int NP>
-__device__ __forceinline__ void few_w(const InteriorField &ic, const MSquares &q0, const MSquares &q1, float4 pos,
-                                      float4 r0, float4 r1, uint32_t miss, float4 out, const float *s_d, float &acc0,
-                                      float &acc1) {
-    const float mz0 = r0.x - pos.x, my0 = r0.y - pos.y, mx0 = r0.z - pos.z;
-    const float mz1 = r1.x - pos.x, my1 = r1.y - pos.y, mx1 = r1.z - pos.z;
-    const float rho0 = rsqa(q0.s), rho1 = NP == 2 ? rsqa(q1.s) : rho0;
-    float w0 = interior_w(ic, q0, rho0), w1 = NP == 2 ? interior_w(ic, q1, rho1) : 0.f;
+__device__ __forceinline__ void few_w(const InteriorField &ic, const MSquares (&q)[NP], float4 pos,
+                                      const float4 (&r)[NP], uint32_t miss, float4 out, const float *s_d,
+                                      float (&acc)[NP]) {
+    float mz[NP], my[NP], mx[NP], rho[NP], w[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        mz[k] = r[k].x - pos.x;
+        my[k] = r[k].y - pos.y;
+        mx[k] = r[k].z - pos.z;
+        rho[k] = rsqa(q[k].s);
+        w[k] = interior_w(ic, q[k], rho[k]);
+    }
     for (; miss; miss &= miss - 1) {
         const float4 d = reinterpret_cast<const float4 *>(s_d)[__ffs(miss) - 1];
-        const float y0 = fmaf(mz0, d.x, fmaf(my0, d.y, mx0 * d.z)) - d.w;
-        const float rs0 = rsqa(fmaf(-2.f, y0, q0.s - d.w));
-        w0 = fmaf(-(rs0 * rs0 * rs0), y0, w0);
-        if (NP == 2) {
-            const float y1 = fmaf(mz1, d.x, fmaf(my1, d.y, mx1 * d.z)) - d.w;
-            const float rs1 = rsqa(fmaf(-2.f, y1, q1.s - d.w));
-            w1 = fmaf(-(rs1 * rs1 * rs1), y1, w1);
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+            const float y = fmaf(mz[k], d.x, fmaf(my[k], d.y, mx[k] * d.z)) - d.w;
+            const float rs = rsqa(fmaf(-2.f, y, q[k].s - d.w));
+            w[k] = fmaf(-(rs * rs * rs), y, w[k]);
         }
     }
-    if (out.w != 0.f) {
-        w0 = fmaf(-(rho0 * rho0 * rho0), fmaf(mz0, out.x, fmaf(my0, out.y, mx0 * out.z)), w0);
-        if (NP == 2) w1 = fmaf(-(rho1 * rho1 * rho1), fmaf(mz1, out.x, fmaf(my1, out.y, mx1 * out.z)), w1);
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        if (out.w != 0.f)
+            w[k] = fmaf(-(rho[k] * rho[k] * rho[k]), fmaf(mz[k], out.x, fmaf(my[k], out.y, mx[k] * out.z)), w[k]);
+        acc[k] += w[k];
     }
-    acc0 += w0;
-    if (NP == 2) acc1 += w1;
 }
 
-// sum_{v in a} w(v) for the 8 APs of chunk a0 and NP lead positions, into s_w[q][j][tid]: one flat
+// sum_{v in a} w(v) for the 8 APs of chunk a0 and NP lead positions, into s_w[k][j][tid]: one flat
 // loop over the chunk's voxels (grouped by AP, the last one of each AP flagged); APs without
 // voxels (padding, at the end of a layer) get 0.  Interior voxels use the closed form where the
 // lane's leads are at least 20 cells away (lanes normally agree), boundary voxels with few absent
@@ -322,64 +325,78 @@ __device__ __forceinline__ void few_w(const InteriorField &ic, const MSquares &q
 template <bool DIAG, int NP>
 __device__ __forceinline__ void chunk_w(int64_t a0, const int64_t *__restrict__ a_vox_begin,
                                         const float4 *__restrict__ vox_pos, const float4 *__restrict__ vox_out,
-                                        float4 r0, float4 r1, int nnb, const float *s_d, const InteriorField &ic,
+                                        const float4 (&r)[NP], int nnb, const float *s_d, const InteriorField &ic,
                                         float (*s_w)[8][LF_THREADS], int tid) {
     const int vb = (int)a_vox_begin[a0], vend = (int)a_vox_begin[a0 + 8];
     const uint32_t full = (1u << nnb) - 1u;
-    float acc0 = 0.f, acc1 = 0.f;
+    float acc[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) acc[k] = 0.f;
     int j = 0;
     for (int v = vb; v < vend; ++v) {
         const float4 pos = vox_pos[v];
         const uint32_t mi = __float_as_uint(pos.w);
-        const MSquares q0 = msq(pos, r0), q1 = NP == 2 ? msq(pos, r1) : q0;
-        const bool far = q0.s >= INTERIOR_S_MIN && q1.s >= INTERIOR_S_MIN;
+        MSquares q[NP];
+        bool far = true;
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+            q[k] = msq(pos, r[k]);
+            far = far && q[k].s >= INTERIOR_S_MIN;
+        }
         if ((mi & VOX_INTERIOR) && far) {
-            acc0 += interior_w(ic, q0, rsqa(q0.s));
-            if (NP == 2) acc1 += interior_w(ic, q1, rsqa(q1.s));
+#pragma unroll
+            for (int k = 0; k < NP; ++k) acc[k] += interior_w(ic, q[k], rsqa(q[k].s));
         } else if ((mi & VOX_FEW) && far) {
-            few_w<NP>(ic, q0, q1, pos, r0, r1, full & ~mi, vox_out[v], s_d, acc0, acc1);
+            few_w<NP>(ic, q, pos, r, full & ~mi, vox_out[v], s_d, acc);
         } else {
             const float4 out = vox_out[v];
-            acc0 += DIAG ? voxel_w_diag(pos, mi, out, r0) : voxel_w_general(pos, mi, out, r0, nnb, s_d);
-            if (NP == 2) acc1 += DIAG ? voxel_w_diag(pos, mi, out, r1) : voxel_w_general(pos, mi, out, r1, nnb, s_d);
+#pragma unroll
+            for (int k = 0; k < NP; ++k)
+                acc[k] += DIAG ? voxel_w_diag(pos, mi, out, r[k]) : voxel_w_general(pos, mi, out, r[k], nnb, s_d);
         }
         if (mi & VOX_AP_END) {
-            s_w[0][j][tid] = acc0;
-            if (NP == 2) s_w[1][j][tid] = acc1;
-            acc0 = acc1 = 0.f;
+#pragma unroll
+            for (int k = 0; k < NP; ++k) {
+                s_w[k][j][tid] = acc[k];
+                acc[k] = 0.f;
+            }
             ++j;
         }
     }
-    for (; j < 8; ++j) {
-        s_w[0][j][tid] = 0.f;
-        if (NP == 2) s_w[1][j][tid] = 0.f;
-    }
+    for (; j < 8; ++j)
+#pragma unroll
+        for (int k = 0; k < NP; ++k) s_w[k][j][tid] = 0.f;
 }
 
-// Work items: (64-AP K tile kt, group of blockDim simulations), taken from the counter `work`
+// Work items: (32-AP stage st, group of LF_THREADS * LF_ROWS rows), taken from the counter `work`
 // (zeroed before the launch) by a grid of one wave of resident blocks; every item writes its own
-// outputs, so the results do not depend on the order.  Per item and lead pair the block writes
-// the BF16 hi/lo tile rows and, for the steady part, per entry e of the tile's layer
-//     P1[kt][e][row'] = (sum_c Z0[c], sum_c G_e[c] Z1[c]) over the tile's 8-AP chunks c below the
-//     entry's prefix end,  Z0[c] = sum_{a in c} W'[a],  Z1[c] = sum_{a in c} W'[a] exp(-k4 (at_ref - at_a)),
-// G_e[c] = gtab[goff[L][e] + c - c8s[L]] = exp(-k4 (t0_e - at_ref[c])), at_ref = the chunk's last
-// finite activation time (APs ascend within a layer, so the factors are <= 1), row' = l * S + s;
-// sums in FP32 over at most 8 chunks.  k_band_u adds the K tiles of a layer in a fixed order.
+// outputs, so the results do not depend on the order.  A thread owns LF_ROWS consecutive rows
+// (row = s * nmove + l) and evaluates their lead positions together, so the voxel loads and tests
+// are shared by LF_ROWS field evaluations.  Per item and row the thread writes the BF16 hi/lo tile
+// row segments and, for the steady part, per entry e of the stage's layer whose steady prefix
+// contains the stage,
+//     P1[st][e][row'] = (sum_a W'[a], G_e[st] sum_a W'[a] exp(-k4 (T_st - at_a))) over the stage's APs,
+// G_e[st] = gtab[goff[L][e] + st - ls0[L]] = exp(-k4 (t0_e - T_st)), T_st = tref[st] = the stage's last
+// finite activation time (APs ascend within a layer, so every factor is <= 1), row' = l * S + s.
+// k_band_u adds the stages of a layer in a fixed order.
 // lrel: [S][nmove] lead positions relative to the voxel centre (FP32, differences taken in FP64
 // on the host); k5l: [S][nl] k5 * log2(e).
 constexpr int MAXE = 8;
+constexpr int BST = 32;     // APs per stage
+constexpr int LF_ROWS = 4;  // rows per thread
 template <int N, bool DIAG>
 __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
-    int nkt, int nsg, int *__restrict__ work, InteriorField ic, const int64_t *__restrict__ a_vox_begin,
+    int nst, int ngr, int *__restrict__ work, InteriorField ic, const int64_t *__restrict__ a_vox_begin,
     const float4 *__restrict__ vox_pos, const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs,
     const float2 *__restrict__ at_hilo, const int32_t *__restrict__ a_layer, const float *__restrict__ k5l, int nl,
     const float4 *__restrict__ hconst, const float4 *__restrict__ lrel, int nmove, int n_sims,
-    const int32_t *__restrict__ c8s, const int32_t *__restrict__ nent, const int32_t *__restrict__ esplit8,
-    const int64_t *__restrict__ goff, const float *__restrict__ gtab, int max_ent, uint8_t *__restrict__ Bt,
-    float2 *__restrict__ P1) {
+    const float2 *__restrict__ tref, const int32_t *__restrict__ ls0, const int32_t *__restrict__ nent,
+    const int32_t *__restrict__ esplit, const int64_t *__restrict__ goff, const float *__restrict__ gtab, int max_ent,
+    uint8_t *__restrict__ Bt, float2 *__restrict__ P1) {
     __shared__ float s_d[26 * 4];
-    __shared__ float s_w[2][8][LF_THREADS];
-    __shared__ float s_acc[2][MAXE][2][LF_THREADS];
+    __shared__ float s_w[LF_ROWS][8][LF_THREADS];
+    __shared__ float2 s_at[BST];  // the stage's activation times
+    __shared__ float s_ez[BST];   // exp(-k4 (T_st - at)), 0 for padding
     __shared__ int s_item;
     const int tid = threadIdx.x;
     if (tid < nnb) {
@@ -390,103 +407,100 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
         s_d[4 * tid + 3] = dz * dz + dy * dy + dx * dx;
     }
     const int rows_used = n_sims * nmove;
+    const int nkt = nst / 2;
     for (;;) {
         __syncthreads();
         if (tid == 0) s_item = atomicAdd(work, 1);
         __syncthreads();
         const int item = s_item;
-        if (item >= nkt * nsg) break;
-        const int kt = item / nsg;
-        const int s = (item % nsg) * LF_THREADS + tid;
-        if (s >= n_sims) continue;
-        const int64_t t0a = (int64_t)kt * BKT;
-        const int L = a_layer[t0a];
-        const float k5 = k5l[(size_t)s * nl + L], k4 = hconst[L].y;
-        const int ne = nent[L], cb = c8s[L];
-        for (int l0 = 0; l0 < nmove; l0 += 2) {
-            const int np = l0 + 1 < nmove ? 2 : 1;
-            const float4 r0 = lrel[(size_t)s * nmove + l0];
-            const float4 r1 = np == 2 ? lrel[(size_t)s * nmove + l0 + 1] : r0;
-            for (int e = 0; e < ne; ++e)
-                for (int q = 0; q < 2; ++q) s_acc[q][e][0][tid] = s_acc[q][e][1][tid] = 0.f;
+        if (item >= nst * ngr) break;
+        const int st = item / ngr;
+        const int L = a_layer[(int64_t)st * BST];
+        if (tid < BST) {
+            const float2 at = at_hilo[(int64_t)st * BST + tid], T = tref[st];
+            s_at[tid] = at;
+            s_ez[tid] = isinf(at.x) ? 0.f : ex2a(-hconst[L].y * ((T.x - at.x) + (T.y - at.y)));
+        }
+        __syncthreads();
+        const int rb = (item % ngr) * (LF_THREADS * LF_ROWS) + tid * LF_ROWS;
+        if (rb >= rows_used) continue;
+        const int nr = min(LF_ROWS, rows_used - rb);  // rows of this thread; the rest repeat its last row
+        float4 r[LF_ROWS];
+        float k5[LF_ROWS], S0[LF_ROWS], S1[LF_ROWS];
+#pragma unroll
+        for (int q = 0; q < LF_ROWS; ++q) {
+            const int row = rb + min(q, nr - 1);
+            r[q] = lrel[row];
+            k5[q] = k5l[(size_t)(row / nmove) * nl + L];
+            S0[q] = S1[q] = 0.f;
+        }
+        const int kt = st >> 1;
 #pragma unroll 1
-            for (int kc = 0; kc < BKT / 8; ++kc) {
-                const int c8 = kt * (BKT / 8) + kc;
-                const int64_t a0 = (int64_t)c8 * 8;
-                if (np == 2) chunk_w<DIAG, 2>(a0, a_vox_begin, vox_pos, vox_out, r0, r1, nnb, s_d, ic, s_w, tid);
-                else chunk_w<DIAG, 1>(a0, a_vox_begin, vox_pos, vox_out, r0, r1, nnb, s_d, ic, s_w, tid);
-                float2 at[8];
+        for (int kc = 0; kc < BST / 8; ++kc) {
+            const int64_t a0 = (int64_t)st * BST + kc * 8;
+            chunk_w<DIAG, LF_ROWS>(a0, a_vox_begin, vox_pos, vox_out, r, nnb, s_d, ic, s_w, tid);
+            const int col = (st & 1) * (BST / 8) + kc;  // 8-AP column within the 64-AP tile
 #pragma unroll
-                for (int j = 0; j < 8; ++j) at[j] = at_hilo[a0 + j];
-                float2 ref = at[0];
-#pragma unroll
-                for (int j = 1; j < 8; ++j)
-                    if (!isinf(at[j].x)) ref = at[j];
-                float e[8], ez[8];
+            for (int q = 0; q < LF_ROWS; ++q) {
+                if (q >= nr) break;
+                float wv[8];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
-                    const bool pad = isinf(at[j].x);
-                    e[j] = pad ? 0.f : ex2a(fmaf(k5, at[j].x, k5 * at[j].y));
-                    ez[j] = pad ? 0.f : ex2a(-k4 * ((ref.x - at[j].x) + (ref.y - at[j].y)));
+                    const float2 at = s_at[kc * 8 + j];
+                    wv[j] = isinf(at.x) ? 0.f : s_w[q][j][tid] * ex2a(fmaf(k5[q], at.x, k5[q] * at.y));
                 }
+                uint4 hv, lv;
+                split2(wv[0], wv[1], hv.x, lv.x);
+                split2(wv[2], wv[3], hv.y, lv.y);
+                split2(wv[4], wv[5], hv.z, lv.z);
+                split2(wv[6], wv[7], hv.w, lv.w);
+                const int row = rb + q;
+                const int nt = row / N, n = row % N;
+                const size_t tile = ((size_t)nt * nkt + kt) * 2;
+                const size_t off = (size_t)(col * (N / 8) + n / 8) * 128 + (n % 8) * 16;
+                *reinterpret_cast<uint4 *>(Bt + tile * (N * 128) + off) = hv;
+                *reinterpret_cast<uint4 *>(Bt + (tile + 1) * (N * 128) + off) = lv;
+                float z0 = 0.f, z1 = 0.f;
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    if (q >= np) break;
-                    float wv[8];
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) wv[j] = s_w[q][j][tid] * e[j];
-                    uint4 hv, lv;
-                    split2(wv[0], wv[1], hv.x, lv.x);
-                    split2(wv[2], wv[3], hv.y, lv.y);
-                    split2(wv[4], wv[5], hv.z, lv.z);
-                    split2(wv[6], wv[7], hv.w, lv.w);
-                    const int row = s * nmove + l0 + q;
-                    const int nt = row / N, n = row % N;
-                    const size_t tile = ((size_t)nt * nkt + kt) * 2;
-                    const size_t off = (size_t)(kc * (N / 8) + n / 8) * 128 + (n % 8) * 16;
-                    *reinterpret_cast<uint4 *>(Bt + tile * (N * 128) + off) = hv;
-                    *reinterpret_cast<uint4 *>(Bt + (tile + 1) * (N * 128) + off) = lv;
-                    float z0 = 0.f, z1 = 0.f;
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        z0 += wv[j];
-                        z1 = fmaf(wv[j], ez[j], z1);
-                    }
-                    for (int ei = 0; ei < ne; ++ei)
-                        if (c8 < esplit8[L * MAXE + ei]) {
-                            s_acc[q][ei][0][tid] += z0;
-                            s_acc[q][ei][1][tid] =
-                                fmaf(gtab[goff[L * MAXE + ei] + (c8 - cb)], z1, s_acc[q][ei][1][tid]);
-                        }
+                for (int j = 0; j < 8; ++j) {
+                    z0 += wv[j];
+                    z1 = fmaf(wv[j], s_ez[kc * 8 + j], z1);
                 }
+                S0[q] += z0;
+                S1[q] += z1;
             }
-            for (int q = 0; q < np; ++q)
-                for (int ei = 0; ei < ne; ++ei)
-                    if (kt * (BKT / 8) < esplit8[L * MAXE + ei])
-                        P1[((size_t)kt * max_ent + ei) * rows_used + (size_t)(l0 + q) * n_sims + s] =
-                            make_float2(s_acc[q][ei][0][tid], s_acc[q][ei][1][tid]);
+        }
+        const int ne = nent[L];
+        for (int e = 0; e < ne; ++e) {
+            if (st >= esplit[L * MAXE + e]) continue;
+            const float g = gtab[goff[L * MAXE + e] + (st - ls0[L])];
+#pragma unroll
+            for (int q = 0; q < LF_ROWS; ++q) {
+                if (q >= nr) break;
+                const int row = rb + q, s = row / nmove, l = row % nmove;
+                P1[((size_t)st * max_ent + e) * rows_used + (size_t)l * n_sims + s] = make_float2(S0[q], g * S1[q]);
+            }
         }
     }
 }
 
 // Small batches (up to SMALL_SIMS simulations): one thread per (AP, simulation), so the work spreads
-// over the heart instead of over simulations.  A block is two 64-AP tiles of one simulation; eight
-// consecutive lanes are one 8-AP chunk and write its BF16 hi/lo row segment two bytes each.  The
-// chunk's reference time comes from a shuffle over its lanes; the steady sums of a tile are reduced
-// by a shuffle butterfly within each warp (half a tile) and in shared memory across the two halves,
-// in a fixed order.  Same outputs as k_batch_lead_field.
+// over the heart instead of over simulations.  A block is four 32-AP stages of one simulation, one
+// per warp; eight consecutive lanes are one 8-AP chunk and write its BF16 hi/lo row segment two
+// bytes each.  The steady sums of a stage are reduced by a shuffle butterfly within its warp.
+// Same outputs as k_batch_lead_field.
 constexpr int SMALL_SIMS = 16;
 template <int N, bool DIAG>
 __global__ void __launch_bounds__(128) k_batch_lead_field_small(
-    int nkt, InteriorField ic, const int64_t *__restrict__ a_vox_begin, const float4 *__restrict__ vox_pos,
+    int nst, InteriorField ic, const int64_t *__restrict__ a_vox_begin, const float4 *__restrict__ vox_pos,
     const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs, const float2 *__restrict__ at_hilo,
     const int32_t *__restrict__ a_layer, const float *__restrict__ k5l, int nl, const float4 *__restrict__ hconst,
-    const float4 *__restrict__ lrel, int nmove, int n_sims, const int32_t *__restrict__ c8s,
-    const int32_t *__restrict__ nent, const int32_t *__restrict__ esplit8, const int64_t *__restrict__ goff,
-    const float *__restrict__ gtab, int max_ent, uint8_t *__restrict__ Bt, float2 *__restrict__ P1) {
+    const float4 *__restrict__ lrel, int nmove, int n_sims, const float2 *__restrict__ tref,
+    const int32_t *__restrict__ ls0, const int32_t *__restrict__ nent, const int32_t *__restrict__ esplit,
+    const int64_t *__restrict__ goff, const float *__restrict__ gtab, int max_ent, uint8_t *__restrict__ Bt,
+    float2 *__restrict__ P1) {
     __shared__ float s_d[26 * 4];
-    __shared__ float2 s_red[4][MAXE];  // [warp][entry]
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x, lane = tid & 31;
     if (tid < nnb) {
         const float dz = difs[3 * tid], dy = difs[3 * tid + 1], dx = difs[3 * tid + 2];
         s_d[4 * tid] = dz;
@@ -495,26 +509,21 @@ __global__ void __launch_bounds__(128) k_batch_lead_field_small(
         s_d[4 * tid + 3] = dz * dz + dy * dy + dx * dx;
     }
     __syncthreads();
-    const int64_t apad = (int64_t)nkt * BKT;
+    const int64_t apad = (int64_t)nst * BST;
     const int64_t araw = (int64_t)blockIdx.x * 128 + tid;
-    const bool valid = araw < apad;  // whole 64-AP tiles are in or out (apad and the block are multiples of 64)
+    const bool valid = araw < apad;  // whole stages are in or out (apad is a multiple of 64)
     const int64_t a = valid ? araw : apad - 1;
     const int s = blockIdx.y;
     const int rows_used = n_sims * nmove;
-    const int kt = (int)(a / BKT), k = (int)(a % BKT), c8 = (int)(a / 8);
+    const int nkt = nst / 2;
+    const int kt = (int)(a / BKT), k = (int)(a % BKT), st = (int)(a / BST);
     const int L = a_layer[a];
     const float k5 = k5l[(size_t)s * nl + L], k4 = hconst[L].y;
-    const int ne = nent[L], cb = c8s[L];
-    const float2 at = at_hilo[a];
+    const int ne = nent[L];
+    const float2 at = at_hilo[a], T = tref[st];
     const bool pad = isinf(at.x);
-    // the chunk's last finite activation time (ascending, padding last): lane of the largest finite
-    int src = pad ? -1 : (lane & 7);
-#pragma unroll
-    for (int o = 1; o < 8; o <<= 1) src = max(src, __shfl_xor_sync(0xffffffffu, src, o));
-    const int from = (lane & ~7) + max(src, 0);
-    const float rx = __shfl_sync(0xffffffffu, at.x, from), ry = __shfl_sync(0xffffffffu, at.y, from);
     const float e = pad ? 0.f : ex2a(fmaf(k5, at.x, k5 * at.y));
-    const float ez = pad ? 0.f : ex2a(-k4 * ((rx - at.x) + (ry - at.y)));
+    const float ez = pad ? 0.f : ex2a(-k4 * ((T.x - at.x) + (T.y - at.y)));
     const int vb = (int)a_vox_begin[a], ve = (int)a_vox_begin[a + 1];
     for (int l0 = 0; l0 < nmove; l0 += 2) {
         const int np = l0 + 1 < nmove ? 2 : 1;
@@ -550,44 +559,31 @@ __global__ void __launch_bounds__(128) k_batch_lead_field_small(
                 *reinterpret_cast<__nv_bfloat16 *>(Bt + tile * (N * 128) + off) = hb;
                 *reinterpret_cast<__nv_bfloat16 *>(Bt + (tile + 1) * (N * 128) + off) = lb;
             }
-            for (int ei = 0; ei < max_ent; ++ei) {
-                const bool in = ei < ne && c8 < esplit8[L * MAXE + ei];
-                float x = in ? w : 0.f;
-                float y = in ? gtab[goff[L * MAXE + ei] + (c8 - cb)] * (w * ez) : 0.f;
+            // the warp is one stage of one layer: every test below is uniform over it
+            for (int ei = 0; ei < ne; ++ei) {
+                if (!valid || st >= esplit[L * MAXE + ei]) continue;
+                float x = w, y = w * ez;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     x += __shfl_xor_sync(0xffffffffu, x, o);
                     y += __shfl_xor_sync(0xffffffffu, y, o);
                 }
-                if (lane == 0) s_red[warp][ei] = make_float2(x, y);
+                if (lane == 0)
+                    P1[((size_t)st * max_ent + ei) * rows_used + (size_t)(l0 + q) * n_sims + s] =
+                        make_float2(x, gtab[goff[L * MAXE + ei] + (st - ls0[L])] * y);
             }
-            __syncthreads();
-            // thread (half-tile pair h, entry ei) combines the two warps of its tile
-            if (tid < 2 * max_ent) {
-                const int h = tid / max_ent, ei = tid % max_ent;
-                const int64_t ta = (int64_t)blockIdx.x * 128 + h * 64;
-                if (ta < apad) {
-                    const int tkt = (int)(ta / BKT), tL = a_layer[ta];
-                    if (ei < nent[tL] && tkt * (BKT / 8) < esplit8[tL * MAXE + ei]) {
-                        const float2 p0 = s_red[2 * h][ei], p1 = s_red[2 * h + 1][ei];
-                        P1[((size_t)tkt * max_ent + ei) * rows_used + (size_t)(l0 + q) * n_sims + s] =
-                            make_float2(p0.x + p1.x, p0.y + p1.y);
-                    }
-                }
-            }
-            __syncthreads();
         }
     }
 }
 
-// Steady sums per (row', layer, entry): U[row'][L][e] = sum over the layer's K tiles [ls0, ls1)
-// below the entry's prefix end of P1[kt][e][row'] (U0, U1).  Two passes in a fixed order:
-// k_band_u sums BU_PARTS consecutive parts of the K range in FP32 (a few tiles each) per (part,
-// layer) block, threads over rows; k_band_u2 adds the parts in FP64, one warp per output.
+// Steady sums per (row', layer, entry): U[row'][L][e] = sum over the layer's stages [ls0, ls1)
+// below the entry's prefix end of P1[st][e][row'] (U0, U1).  Two passes in a fixed order:
+// k_band_u sums BU_PARTS consecutive parts of the stage range in FP32 (a few stages each) per
+// (part, layer) block, threads over rows; k_band_u2 adds the parts in FP64, one warp per output.
 // Up: [parts][rows][nl][max_ent]; U stored in FP32.
 constexpr int BU_PARTS = 128;
 __global__ void __launch_bounds__(256) k_band_u(int rows_used, int nl, int max_ent, const int32_t *__restrict__ nent,
-                                                const int32_t *__restrict__ esplit8, const int32_t *__restrict__ ls0,
+                                                const int32_t *__restrict__ esplit, const int32_t *__restrict__ ls0,
                                                 const int32_t *__restrict__ ls1, const float2 *__restrict__ P1,
                                                 float2 *__restrict__ Up) {
     const int p = blockIdx.x, L = blockIdx.y;
@@ -595,7 +591,7 @@ __global__ void __launch_bounds__(256) k_band_u(int rows_used, int nl, int max_e
     const int g0 = ls0[L] + (int)((int64_t)n * p / BU_PARTS), g1 = ls0[L] + (int)((int64_t)n * (p + 1) / BU_PARTS);
     for (int rr = threadIdx.x; rr < rows_used; rr += blockDim.x)
         for (int e = 0; e < ne; ++e) {
-            const int ge = min(g1, (esplit8[L * MAXE + e] + 7) / 8);
+            const int ge = min(g1, esplit[L * MAXE + e]);
             float a = 0.f, b = 0.f;
 #pragma unroll 8
             for (int g = g0; g < ge; ++g) {
@@ -1031,8 +1027,9 @@ void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int
 void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const float *k5l,
                              const float4 *hconst, const float4 *lrel, int nmove, int n_sims, const BandArgs &B,
                              uint8_t *Bt, int *work, int sm_count) {
-    const int nsg = (n_sims + LF_THREADS - 1) / LF_THREADS;
-    const int nkt = (int)(h.apad / BKT);
+    const int rows_used = n_sims * nmove;
+    const int ngr = (rows_used + LF_THREADS * LF_ROWS - 1) / (LF_THREADS * LF_ROWS);
+    const int nst = (int)(h.apad / BST);
     const bool diag = h.nhood == EKG_NHOOD_3D4;
     const bool small = n_sims <= SMALL_SIMS;
     InteriorField ic;
@@ -1045,22 +1042,22 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, c
 #define EKG_LF(NN, DG)                                                                                            \
     do {                                                                                                          \
         if (small) {                                                                                              \
-            dim3 g((unsigned)((nkt * BKT + 127) / 128), (unsigned)n_sims);                                         \
+            dim3 g((unsigned)((nst * BST + 127) / 128), (unsigned)n_sims);                                         \
             k_batch_lead_field_small<NN, DG><<<g, 128, 0, s>>>(                                                   \
-                nkt, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p,    \
-                k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.c8s, B.nent, B.esplit8, B.goff, B.gtab, B.max_ent, \
-                Bt, B.P1);                                                                                        \
+                nst, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p,    \
+                k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.ls0, B.nent, B.esplit, B.goff, B.gtab,     \
+                B.max_ent, Bt, B.P1);                                                                             \
             break;                                                                                                \
         }                                                                                                         \
         static int per_sm = 0;                                                                                    \
         if (!per_sm)                                                                                              \
             EKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_lead_field<NN, DG>,           \
                                                                    LF_THREADS, 0));                               \
-        const int grid = std::max(1, std::min(nkt * nsg, std::max(1, per_sm) * sm_count));                       \
+        const int grid = std::max(1, std::min(nst * ngr, std::max(1, per_sm) * sm_count));                       \
         k_batch_lead_field<NN, DG><<<grid, LF_THREADS, 0, s>>>(                                                   \
-            nkt, nsg, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p, \
-            k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.c8s, B.nent, B.esplit8, B.goff, B.gtab, B.max_ent, Bt, \
-            B.P1);                                                                                                \
+            nst, ngr, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p, \
+            k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.ls0, B.nent, B.esplit, B.goff, B.gtab,         \
+            B.max_ent, Bt, B.P1);                                                                                 \
     } while (0)
     switch (batch_tile_rows(two_bases, n_sims * nmove)) {
     case 32:
@@ -1095,7 +1092,7 @@ void launch_batch_gemm(cudaStream_t s, const BatchArgs &A) {
 int band_u_parts() { return BU_PARTS; }
 
 void launch_band_u(cudaStream_t s, const BandArgs &A) {
-    k_band_u<<<dim3(BU_PARTS, (unsigned)A.nl), 256, 0, s>>>(A.rows_used, A.nl, A.max_ent, A.nent, A.esplit8, A.ls0,
+    k_band_u<<<dim3(BU_PARTS, (unsigned)A.nl), 256, 0, s>>>(A.rows_used, A.nl, A.max_ent, A.nent, A.esplit, A.ls0,
                                                            A.ls1, A.P1, A.Up);
     const int64_t n = (int64_t)A.rows_used * A.nl * A.max_ent;
     k_band_u2<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(n, A.Up, A.U);

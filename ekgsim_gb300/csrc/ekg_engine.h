@@ -46,15 +46,16 @@ struct BatchState {
     int ntt = 0;                           // tiles
     int max_ent = 1;                       // steady entries per layer (max)
     std::vector<int32_t> band_s0, band_s1; // [nl][ntt] band in 32-AP stages [s0, s1)
-    DBuf<int32_t> ls0, ls1;                // [nl] 64-AP K tile range of each layer
-    DBuf<int32_t> c8s, nent, esplit8;      // [nl], [nl], [nl][8]: first chunk, entries, steady prefix ends
+    DBuf<int32_t> ls0, ls1;                // [nl] 32-AP stage range of each layer
+    DBuf<int32_t> nent, esplit;            // [nl], [nl][8]: entries, steady prefix ends (stages)
+    DBuf<float2> tref;                     // [stages] last finite activation time of the stage (hi, lo)
     DBuf<int64_t> goff;                    // [nl][8] offsets into gtab
-    DBuf<float> gtab;                      // exp(-k4 (t0_e - at_ref[c8])) for the steady chunks of entry e
+    DBuf<float> gtab;                      // exp(-k4 (t0_e - tref[st])) for the steady stages of entry e
     DBuf<int32_t> ent;                     // [nl][ntt] entry of each tile (-1: layer without APs)
     DBuf<float> E;                         // [nl][steps] exp(-k4 (t - t0 of the tile's entry))
     // per batch
     DBuf<uint8_t> Bt;                      // tiled BF16 hi/lo moved-lead weights
-    DBuf<float2> P1;                       // [K tiles][max_ent][rows] steady sums per 64-AP tile
+    DBuf<float2> P1;                       // [stages][max_ent][rows] steady sums per 32-AP stage
     DBuf<int> work;                        // work counter of the operand kernel
     DBuf<float2> U, Up;                    // [rows][nl][max_ent] steady sums (U0, U1), per K part
     DBuf<float> partial;                   // [items][rows][128] raw accumulators (x2 with two bases)

@@ -217,13 +217,14 @@ struct BandArgs {
     int n_sims = 0, nmove = 0, nl = 0, ntt = 0, steps = 0, rows = 0, rows_used = 0, nleads = 0;
     int max_ent = 1, nb = 1;
     const int32_t *ti0 = nullptr, *ti1 = nullptr;  // [ntt][nl] item range of (tile, layer)
-    const int32_t *c8s = nullptr, *nent = nullptr, *esplit8 = nullptr, *ls0 = nullptr, *ls1 = nullptr;
+    const float2 *tref = nullptr;                   // [stages] last finite activation time of each 32-AP stage
+    const int32_t *nent = nullptr, *esplit = nullptr, *ls0 = nullptr, *ls1 = nullptr;  // stage units
     const int32_t *ent = nullptr;
     const int64_t *goff = nullptr;
     const float *gtab = nullptr;
     const float *E = nullptr, *F = nullptr, *partial = nullptr;
     const double *k3 = nullptr;
-    float2 *P1 = nullptr;            // [K tiles][max_ent][rows] steady sums per 64-AP tile
+    float2 *P1 = nullptr;            // [stages][max_ent][rows] steady sums per 32-AP stage
     float2 *Up = nullptr;            // [band_u_parts()][rows][nl][max_ent]
     float2 *U = nullptr;             // [rows][nl][max_ent]
     double *ecg = nullptr;

@@ -629,8 +629,20 @@ void build_band(ekg_heart *h, const std::vector<double> &key, const std::vector<
     B.ntt = ntt;
     B.band_s0.assign((size_t)nl * ntt, 0);
     B.band_s1.assign((size_t)nl * ntt, 0);
-    std::vector<int32_t> c8s(nl, 0), nent(nl, 0), esplit8((size_t)nl * MAXE, 0), ent((size_t)nl * ntt, -1);
+    std::vector<int32_t> nent(nl, 0), esplit((size_t)nl * MAXE, 0), ent((size_t)nl * ntt, -1);
     std::vector<int32_t> ls0(nl, 0), ls1(nl, 0);
+    // per 32-AP stage its last finite activation time (hi, lo as the device's at_hilo), 0 if none
+    const int64_t nst = D.apad / 32;
+    std::vector<double> tr(nst, NAN);
+    std::vector<float2> tref(nst, make_float2(0.f, 0.f));
+    for (int64_t st = 0; st < nst; ++st)
+        for (int64_t a = 32 * st + 31; a >= 32 * st; --a)
+            if (std::isfinite(at_h[a])) {
+                tr[st] = at_h[a];
+                const float hi = (float)at_h[a];
+                tref[st] = make_float2(hi, (float)(at_h[a] - (double)hi));
+                break;
+            }
     std::vector<int64_t> goff((size_t)nl * MAXE, 0);
     std::vector<float> gtab;
     std::vector<float> E((size_t)nl * steps, 1.f);
@@ -639,9 +651,8 @@ void build_band(ekg_heart *h, const std::vector<double> &key, const std::vector<
         if (la0[L] < 0) continue;
         const double k1 = key[2 * L], k4 = key[2 * L + 1];
         const int64_t a0 = la0[L], a1 = la1[L], af = a0 + nfin[L];
-        c8s[L] = (int32_t)(a0 / 8);
-        ls0[L] = (int32_t)(a0 / 64);
-        ls1[L] = (int32_t)(a1 / 64);
+        ls0[L] = (int32_t)(a0 / 32);
+        ls1[L] = (int32_t)(a1 / 32);
         bool ok = k1 > 0 && k4 >= 0 && k1 > 1.05 * k4 && std::isfinite(k1) && std::isfinite(k4);
         for (int64_t a = a0; ok && a < a1; ++a)
             ok = a < af ? (std::isfinite(at_h[a]) && (a == a0 || at_h[a] >= at_h[a - 1])) : !std::isfinite(at_h[a]);
@@ -683,35 +694,29 @@ void build_band(ekg_heart *h, const std::vector<double> &key, const std::vector<
                 E[(size_t)L * steps + t] = (float)std::exp(-k4 * (h->t[t] - eref[e]));
         }
         for (int e = 0; e < nent[L]; ++e) {
-            esplit8[(size_t)L * MAXE + e] = (int32_t)(esp[e] / 8);
+            // prefix ends are multiples of 32 APs from a layer start padded to 64: whole stages
+            esplit[(size_t)L * MAXE + e] = (int32_t)(esp[e] / 32);
             goff[(size_t)L * MAXE + e] = (int64_t)gtab.size();
-            for (int64_t c = a0 / 8; c < esp[e] / 8; ++c) {
-                double ref = NAN;
-                for (int64_t a = 8 * c + 7; a >= 8 * c; --a)
-                    if (std::isfinite(at_h[a])) {
-                        ref = at_h[a];
-                        break;
-                    }
-                gtab.push_back(std::isfinite(ref) ? (float)std::exp(-k4 * (eref[e] - ref)) : 0.f);
-            }
+            for (int64_t st = a0 / 32; st < esp[e] / 32; ++st)
+                gtab.push_back(std::isfinite(tr[st]) ? (float)std::exp(-k4 * (eref[e] - tr[st])) : 0.f);
         }
     }
     if (gtab.empty()) gtab.push_back(0.f);
     B.max_ent = max_ent;
     B.ls0.alloc(nl);
     B.ls1.alloc(nl);
-    B.c8s.alloc(nl);
+    B.tref.alloc(nst);
     B.nent.alloc(nl);
-    B.esplit8.alloc((size_t)nl * MAXE);
+    B.esplit.alloc((size_t)nl * MAXE);
     B.goff.alloc((size_t)nl * MAXE);
     B.gtab.alloc(gtab.size());
     B.ent.alloc((size_t)nl * ntt);
     B.E.alloc((size_t)nl * steps);
     EKG_CUDA(cudaMemcpyAsync(B.ls0.p, ls0.data(), nl * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(B.ls1.p, ls1.data(), nl * 4, cudaMemcpyHostToDevice, s));
-    EKG_CUDA(cudaMemcpyAsync(B.c8s.p, c8s.data(), nl * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(B.tref.p, tref.data(), nst * sizeof(float2), cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(B.nent.p, nent.data(), nl * 4, cudaMemcpyHostToDevice, s));
-    EKG_CUDA(cudaMemcpyAsync(B.esplit8.p, esplit8.data(), esplit8.size() * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(B.esplit.p, esplit.data(), esplit.size() * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(B.goff.p, goff.data(), goff.size() * 8, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(B.gtab.p, gtab.data(), gtab.size() * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(B.ent.p, ent.data(), ent.size() * 4, cudaMemcpyHostToDevice, s));
@@ -1007,7 +1012,7 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
             if (B.Bt.n < bt) B.Bt.alloc(bt);
             const size_t pb = (size_t)std::max(1, P.nitems) * P.rows * 128 * (P.two_bases ? 2 : 1);
             if (B.partial.n < pb) B.partial.alloc(pb);
-            const size_t p1 = (size_t)(D.apad / 64) * B.max_ent * P.rows_used;
+            const size_t p1 = (size_t)(D.apad / 32) * B.max_ent * P.rows_used;
             if (B.P1.n < p1) B.P1.alloc(p1);
             if (!B.work.p) B.work.alloc(1);
             const size_t ub = (size_t)P.rows_used * D.nlayers * B.max_ent;
@@ -1059,9 +1064,9 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             U.rows_used = P.rows_used;
             U.nleads = (int)L;
             U.max_ent = B.max_ent;
-            U.c8s = B.c8s.p;
+            U.tref = B.tref.p;
             U.nent = B.nent.p;
-            U.esplit8 = B.esplit8.p;
+            U.esplit = B.esplit.p;
             U.ls0 = B.ls0.p;
             U.ls1 = B.ls1.p;
             U.ent = B.ent.p;
@@ -1168,7 +1173,7 @@ std::vector<uint64_t> pass_signature(const ekg_heart *h, const PassPlan &P, int 
                           (const void *)B.Q1.p,
                           (const void *)B.Q2.p, (const void *)B.Bt.p, (const void *)B.P1.p, (const void *)B.U.p,
                           (const void *)B.Up.p, (const void *)B.partial.p,
-                          (const void *)B.c8s.p, (const void *)B.nent.p, (const void *)B.esplit8.p, (const void *)B.ls0.p,
+                          (const void *)B.tref.p, (const void *)B.nent.p, (const void *)B.esplit.p, (const void *)B.ls0.p,
                           (const void *)B.ls1.p, (const void *)B.ent.p, (const void *)B.goff.p, (const void *)B.gtab.p,
                           (const void *)B.E.p, (const void *)B.work.p, (const void *)h->W0.p})
         v.push_back(u(p));
@@ -1308,13 +1313,13 @@ void benchmark(ekg_heart *h, int n_sims, const double *layer_k, const double *le
         const BatchState &B = h->bs;
         const int N = batch_tile_rows(P.two_bases, P.rows_used), nb = P.two_bases ? 2 : 1;
         for (const int4 &it : P.items) gemm_flops += (double)(it.z - it.y) * P.ntiles * 128.0 * N * 32 * 2 * 3 * nb;
-        std::vector<int32_t> nent(D.nlayers), es8((size_t)D.nlayers * 8), ls0(D.nlayers);
+        std::vector<int32_t> nent(D.nlayers), esp((size_t)D.nlayers * 8), ls0(D.nlayers);
         EKG_CUDA(cudaMemcpy(nent.data(), B.nent.p, D.nlayers * 4, cudaMemcpyDeviceToHost));
-        EKG_CUDA(cudaMemcpy(es8.data(), B.esplit8.p, es8.size() * 4, cudaMemcpyDeviceToHost));
+        EKG_CUDA(cudaMemcpy(esp.data(), B.esplit.p, esp.size() * 4, cudaMemcpyDeviceToHost));
         EKG_CUDA(cudaMemcpy(ls0.data(), B.ls0.p, D.nlayers * 4, cudaMemcpyDeviceToHost));
-        double p1 = 0;
+        double p1 = 0;  // steady sums written (stages x entries)
         for (int L = 0; L < D.nlayers; ++L)
-            for (int e = 0; e < nent[L]; ++e) p1 += std::max(0, (es8[(size_t)L * 8 + e] + 7) / 8 - ls0[L]);
+            for (int e = 0; e < nent[L]; ++e) p1 += std::max(0, esp[(size_t)L * 8 + e] - ls0[L]);
         op_bytes = (double)P.rows_used * D.apad * 4 + p1 * P.rows_used * 8 +
                    (double)D.nvox * 16 + (double)(D.nvox - D.n_interior) * 16 + (double)D.apad * 16;
     }
