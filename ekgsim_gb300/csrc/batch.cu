@@ -317,17 +317,17 @@ __device__ __forceinline__ void few_w(const InteriorField &ic, const MSquares (&
     }
 }
 
-// sum_{v in a} w(v) for the 8 APs of chunk a0 and NP lead positions, into s_w[k][j][tid]: one flat
-// loop over the chunk's voxels (grouped by AP, the last one of each AP flagged); APs without
+// sum_{v in a} w(v) for the 8 APs of a chunk (voxels [vb, vend)) and NP lead positions, into
+// s_w[k][j][tid]: one flat loop over the chunk's voxels (grouped by AP, the last one of each AP
+// flagged); APs without
 // voxels (padding, at the end of a layer) get 0.  Interior voxels use the closed form where the
 // lane's leads are at least 20 cells away (lanes normally agree), boundary voxels with few absent
 // neighbours the closed form minus those, the rest the exact sum.
 template <bool DIAG, int NP>
-__device__ __forceinline__ void chunk_w(int64_t a0, const int64_t *__restrict__ a_vox_begin,
-                                        const float4 *__restrict__ vox_pos, const float4 *__restrict__ vox_out,
-                                        const float4 (&r)[NP], int nnb, const float *s_d, const InteriorField &ic,
-                                        float (*s_w)[8][LF_THREADS], int tid) {
-    const int vb = (int)a_vox_begin[a0], vend = (int)a_vox_begin[a0 + 8];
+__device__ __forceinline__ void chunk_w(int vb, int vend, const float4 *__restrict__ vox_pos,
+                                        const float4 *__restrict__ vox_out, const float4 (&r)[NP], int nnb,
+                                        const float *s_d, const InteriorField &ic, float (*s_w)[8][LF_THREADS],
+                                        int tid) {
     const uint32_t full = (1u << nnb) - 1u;
     float acc[NP];
 #pragma unroll
@@ -373,30 +373,32 @@ __device__ __forceinline__ void chunk_w(int64_t a0, const int64_t *__restrict__ 
 // outputs, so the results do not depend on the order.  A thread owns LF_ROWS consecutive rows
 // (row = s * nmove + l) and evaluates their lead positions together, so the voxel loads and tests
 // are shared by LF_ROWS field evaluations.  Per item and row the thread writes the BF16 hi/lo tile
-// row segments and, for the steady part, per entry e of the stage's layer whose steady prefix
-// contains the stage,
-//     P1[st][e][row'] = (sum_a W'[a], G_e[st] sum_a W'[a] exp(-k4 (T_st - at_a))) over the stage's APs,
-// G_e[st] = gtab[goff[L][e] + st - ls0[L]] = exp(-k4 (t0_e - T_st)), T_st = tref[st] = the stage's last
-// finite activation time (APs ascend within a layer, so every factor is <= 1), row' = l * S + s.
-// k_band_u adds the stages of a layer in a fixed order.
+// row segments and, for the steady part, the stage's sums
+//     P1[st][row'] = (sum_a W'[a], sum_a W'[a] exp(-k4 (T_st - at_a))) over the stage's APs,
+// T_st = tref[st] = the stage's last finite activation time (APs ascend within a layer, so every
+// factor is <= 1), row' = l * S + s.  k_band_u scales the second sum by each entry's
+// G_e[st] = exp(-k4 (t0_e - T_st)) and adds the stages of a layer in a fixed order.
 // lrel: [S][nmove] lead positions relative to the voxel centre (FP32, differences taken in FP64
 // on the host); k5l: [S][nl] k5 * log2(e).
 constexpr int MAXE = 8;
 constexpr int BST = 32;     // APs per stage
 constexpr int LF_ROWS = 4;  // rows per thread
+static_assert(LF_THREADS >= BST + BST / 8 + 1, "the stage tables are loaded one entry per thread");
 template <int N, bool DIAG>
 __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
     int nst, int ngr, int *__restrict__ work, InteriorField ic, const int64_t *__restrict__ a_vox_begin,
     const float4 *__restrict__ vox_pos, const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs,
     const float2 *__restrict__ at_hilo, const int32_t *__restrict__ a_layer, const float *__restrict__ k5l, int nl,
     const float4 *__restrict__ hconst, const float4 *__restrict__ lrel, int nmove, int n_sims,
-    const float2 *__restrict__ tref, const int32_t *__restrict__ ls0, const int32_t *__restrict__ nent,
-    const int32_t *__restrict__ esplit, const int64_t *__restrict__ goff, const float *__restrict__ gtab, int max_ent,
+    const float2 *__restrict__ tref, const int32_t *__restrict__ nent, const int32_t *__restrict__ esplit,
     uint8_t *__restrict__ Bt, float2 *__restrict__ P1) {
     __shared__ float s_d[26 * 4];
     __shared__ float s_w[LF_ROWS][8][LF_THREADS];
     __shared__ float2 s_at[BST];  // the stage's activation times
     __shared__ float s_ez[BST];   // exp(-k4 (T_st - at)), 0 for padding
+    __shared__ int s_vb[BST / 8 + 1];  // first voxel of each chunk of the stage, and the end
+    __shared__ float s_k5[LF_ROWS][LF_THREADS];       // k5 log2(e) of each row's simulation
+    __shared__ float2 s_sum[LF_ROWS][LF_THREADS];     // the stage's steady sums of each row
     __shared__ int s_item;
     const int tid = threadIdx.x;
     if (tid < nnb) {
@@ -420,34 +422,40 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
             const float2 at = at_hilo[(int64_t)st * BST + tid], T = tref[st];
             s_at[tid] = at;
             s_ez[tid] = isinf(at.x) ? 0.f : ex2a(-hconst[L].y * ((T.x - at.x) + (T.y - at.y)));
+        } else if (tid < BST + BST / 8 + 1) {
+            s_vb[tid - BST] = (int)a_vox_begin[(int64_t)st * BST + (tid - BST) * 8];
         }
         __syncthreads();
         const int rb = (item % ngr) * (LF_THREADS * LF_ROWS) + tid * LF_ROWS;
         if (rb >= rows_used) continue;
         const int nr = min(LF_ROWS, rows_used - rb);  // rows of this thread; the rest repeat its last row
-        float4 r[LF_ROWS];
-        float k5[LF_ROWS], S0[LF_ROWS], S1[LF_ROWS];
+        // per-row state lives in shared memory; the lead positions are (re)loaded for each chunk's
+        // voxel loop, so that registers are not held across the chunk's output stage
 #pragma unroll
         for (int q = 0; q < LF_ROWS; ++q) {
             const int row = rb + min(q, nr - 1);
-            r[q] = lrel[row];
-            k5[q] = k5l[(size_t)(row / nmove) * nl + L];
-            S0[q] = S1[q] = 0.f;
+            s_k5[q][tid] = k5l[(size_t)(row / nmove) * nl + L];
+            s_sum[q][tid] = make_float2(0.f, 0.f);
         }
         const int kt = st >> 1;
 #pragma unroll 1
         for (int kc = 0; kc < BST / 8; ++kc) {
-            const int64_t a0 = (int64_t)st * BST + kc * 8;
-            chunk_w<DIAG, LF_ROWS>(a0, a_vox_begin, vox_pos, vox_out, r, nnb, s_d, ic, s_w, tid);
+            {
+                float4 r[LF_ROWS];
+#pragma unroll
+                for (int q = 0; q < LF_ROWS; ++q) r[q] = lrel[rb + min(q, nr - 1)];
+                chunk_w<DIAG, LF_ROWS>(s_vb[kc], s_vb[kc + 1], vox_pos, vox_out, r, nnb, s_d, ic, s_w, tid);
+            }
             const int col = (st & 1) * (BST / 8) + kc;  // 8-AP column within the 64-AP tile
 #pragma unroll
             for (int q = 0; q < LF_ROWS; ++q) {
                 if (q >= nr) break;
                 float wv[8];
+                const float k5 = s_k5[q][tid];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const float2 at = s_at[kc * 8 + j];
-                    wv[j] = isinf(at.x) ? 0.f : s_w[q][j][tid] * ex2a(fmaf(k5[q], at.x, k5[q] * at.y));
+                    wv[j] = isinf(at.x) ? 0.f : s_w[q][j][tid] * ex2a(fmaf(k5, at.x, k5 * at.y));
                 }
                 uint4 hv, lv;
                 split2(wv[0], wv[1], hv.x, lv.x);
@@ -466,21 +474,18 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
                     z0 += wv[j];
                     z1 = fmaf(wv[j], s_ez[kc * 8 + j], z1);
                 }
-                S0[q] += z0;
-                S1[q] += z1;
+                const float2 sm = s_sum[q][tid];
+                s_sum[q][tid] = make_float2(sm.x + z0, sm.y + z1);
             }
         }
         const int ne = nent[L];
-        for (int e = 0; e < ne; ++e) {
-            if (st >= esplit[L * MAXE + e]) continue;
-            const float g = gtab[goff[L * MAXE + e] + (st - ls0[L])];
+        if (ne > 0 && st < esplit[L * MAXE + ne - 1])  // the last entry's steady prefix is the longest
 #pragma unroll
             for (int q = 0; q < LF_ROWS; ++q) {
                 if (q >= nr) break;
                 const int row = rb + q, s = row / nmove, l = row % nmove;
-                P1[((size_t)st * max_ent + e) * rows_used + (size_t)l * n_sims + s] = make_float2(S0[q], g * S1[q]);
+                P1[(size_t)st * rows_used + (size_t)l * n_sims + s] = s_sum[q][tid];
             }
-        }
     }
 }
 
@@ -496,8 +501,7 @@ __global__ void __launch_bounds__(128) k_batch_lead_field_small(
     const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs, const float2 *__restrict__ at_hilo,
     const int32_t *__restrict__ a_layer, const float *__restrict__ k5l, int nl, const float4 *__restrict__ hconst,
     const float4 *__restrict__ lrel, int nmove, int n_sims, const float2 *__restrict__ tref,
-    const int32_t *__restrict__ ls0, const int32_t *__restrict__ nent, const int32_t *__restrict__ esplit,
-    const int64_t *__restrict__ goff, const float *__restrict__ gtab, int max_ent, uint8_t *__restrict__ Bt,
+    const int32_t *__restrict__ nent, const int32_t *__restrict__ esplit, uint8_t *__restrict__ Bt,
     float2 *__restrict__ P1) {
     __shared__ float s_d[26 * 4];
     const int tid = threadIdx.x, lane = tid & 31;
@@ -560,47 +564,58 @@ __global__ void __launch_bounds__(128) k_batch_lead_field_small(
                 *reinterpret_cast<__nv_bfloat16 *>(Bt + (tile + 1) * (N * 128) + off) = lb;
             }
             // the warp is one stage of one layer: every test below is uniform over it
-            for (int ei = 0; ei < ne; ++ei) {
-                if (!valid || st >= esplit[L * MAXE + ei]) continue;
+            if (valid && ne > 0 && st < esplit[L * MAXE + ne - 1]) {
                 float x = w, y = w * ez;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     x += __shfl_xor_sync(0xffffffffu, x, o);
                     y += __shfl_xor_sync(0xffffffffu, y, o);
                 }
-                if (lane == 0)
-                    P1[((size_t)st * max_ent + ei) * rows_used + (size_t)(l0 + q) * n_sims + s] =
-                        make_float2(x, gtab[goff[L * MAXE + ei] + (st - ls0[L])] * y);
+                if (lane == 0) P1[(size_t)st * rows_used + (size_t)(l0 + q) * n_sims + s] = make_float2(x, y);
             }
         }
     }
 }
 
 // Steady sums per (row', layer, entry): U[row'][L][e] = sum over the layer's stages [ls0, ls1)
-// below the entry's prefix end of P1[st][e][row'] (U0, U1).  Two passes in a fixed order:
-// k_band_u sums BU_PARTS consecutive parts of the stage range in FP32 (a few stages each) per
-// (part, layer) block, threads over rows; k_band_u2 adds the parts in FP64, one warp per output.
-// Up: [parts][rows][nl][max_ent]; U stored in FP32.
+// below the entry's prefix end of (P1[st][row'].x, G_e[st] P1[st][row'].y) (U0, U1),
+// G_e[st] = gtab[goff[L][e] + st - ls0[L]].  Two passes in a fixed order: k_band_u sums BU_PARTS
+// consecutive parts of the stage range in FP32 (a few stages each) per (part, layer) block,
+// threads over rows, all entries from one read of P1; k_band_u2 adds the parts in FP64, one warp
+// per output.  Up: [parts][rows][nl][max_ent]; U stored in FP32.  The prefix ends ascend with e.
 constexpr int BU_PARTS = 128;
 __global__ void __launch_bounds__(256) k_band_u(int rows_used, int nl, int max_ent, const int32_t *__restrict__ nent,
                                                 const int32_t *__restrict__ esplit, const int32_t *__restrict__ ls0,
-                                                const int32_t *__restrict__ ls1, const float2 *__restrict__ P1,
+                                                const int32_t *__restrict__ ls1, const int64_t *__restrict__ goff,
+                                                const float *__restrict__ gtab, const float2 *__restrict__ P1,
                                                 float2 *__restrict__ Up) {
     const int p = blockIdx.x, L = blockIdx.y;
     const int ne = nent[L], n = ls1[L] - ls0[L];
     const int g0 = ls0[L] + (int)((int64_t)n * p / BU_PARTS), g1 = ls0[L] + (int)((int64_t)n * (p + 1) / BU_PARTS);
-    for (int rr = threadIdx.x; rr < rows_used; rr += blockDim.x)
-        for (int e = 0; e < ne; ++e) {
-            const int ge = min(g1, esplit[L * MAXE + e]);
-            float a = 0.f, b = 0.f;
-#pragma unroll 8
-            for (int g = g0; g < ge; ++g) {
-                const float2 v = P1[((size_t)g * max_ent + e) * rows_used + rr];
-                a += v.x;
-                b += v.y;
-            }
-            Up[(((size_t)p * rows_used + rr) * nl + L) * max_ent + e] = make_float2(a, b);
+    int ge[MAXE];
+    int64_t go[MAXE];  // gtab index of stage g of entry e: go[e] + g
+#pragma unroll
+    for (int e = 0; e < MAXE; ++e) {
+        ge[e] = e < ne ? min(g1, esplit[L * MAXE + e]) : g0;
+        go[e] = e < ne ? goff[L * MAXE + e] - ls0[L] : 0;
+    }
+    const int gend = ne > 0 ? ge[ne - 1] : g0;
+    for (int rr = threadIdx.x; rr < rows_used; rr += blockDim.x) {
+        float a[MAXE], b[MAXE];
+#pragma unroll
+        for (int e = 0; e < MAXE; ++e) a[e] = b[e] = 0.f;
+        for (int g = g0; g < gend; ++g) {
+            const float2 v = P1[(size_t)g * rows_used + rr];
+#pragma unroll
+            for (int e = 0; e < MAXE; ++e)
+                if (g < ge[e]) {
+                    a[e] += v.x;
+                    b[e] = fmaf(gtab[go[e] + g], v.y, b[e]);
+                }
         }
+        for (int e = 0; e < ne; ++e)
+            Up[(((size_t)p * rows_used + rr) * nl + L) * max_ent + e] = make_float2(a[e], b[e]);
+    }
 }
 
 __global__ void __launch_bounds__(256) k_band_u2(int64_t n_out, const float2 *__restrict__ Up, float2 *__restrict__ U) {
@@ -1045,8 +1060,7 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, c
             dim3 g((unsigned)((nst * BST + 127) / 128), (unsigned)n_sims);                                         \
             k_batch_lead_field_small<NN, DG><<<g, 128, 0, s>>>(                                                   \
                 nst, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p,    \
-                k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.ls0, B.nent, B.esplit, B.goff, B.gtab,     \
-                B.max_ent, Bt, B.P1);                                                                             \
+                k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, Bt, B.P1);                 \
             break;                                                                                                \
         }                                                                                                         \
         static int per_sm = 0;                                                                                    \
@@ -1056,8 +1070,7 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, c
         const int grid = std::max(1, std::min(nst * ngr, std::max(1, per_sm) * sm_count));                       \
         k_batch_lead_field<NN, DG><<<grid, LF_THREADS, 0, s>>>(                                                   \
             nst, ngr, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p, \
-            k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.ls0, B.nent, B.esplit, B.goff, B.gtab,         \
-            B.max_ent, Bt, B.P1);                                                                                 \
+            k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, Bt, B.P1);                     \
     } while (0)
     switch (batch_tile_rows(two_bases, n_sims * nmove)) {
     case 32:
@@ -1093,7 +1106,7 @@ int band_u_parts() { return BU_PARTS; }
 
 void launch_band_u(cudaStream_t s, const BandArgs &A) {
     k_band_u<<<dim3(BU_PARTS, (unsigned)A.nl), 256, 0, s>>>(A.rows_used, A.nl, A.max_ent, A.nent, A.esplit, A.ls0,
-                                                           A.ls1, A.P1, A.Up);
+                                                           A.ls1, A.goff, A.gtab, A.P1, A.Up);
     const int64_t n = (int64_t)A.rows_used * A.nl * A.max_ent;
     k_band_u2<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(n, A.Up, A.U);
     EKG_CUDA(cudaGetLastError());

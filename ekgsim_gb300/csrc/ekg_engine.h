@@ -55,7 +55,7 @@ struct BatchState {
     DBuf<float> E;                         // [nl][steps] exp(-k4 (t - t0 of the tile's entry))
     // per batch
     DBuf<uint8_t> Bt;                      // tiled BF16 hi/lo moved-lead weights
-    DBuf<float2> P1;                       // [stages][max_ent][rows] steady sums per 32-AP stage
+    DBuf<float2> P1;                       // [stages][rows] steady sums per 32-AP stage
     DBuf<int> work;                        // work counter of the operand kernel
     DBuf<float2> U, Up;                    // [rows][nl][max_ent] steady sums (U0, U1), per K part
     DBuf<float> partial;                   // [items][rows][128] raw accumulators (x2 with two bases)
@@ -80,6 +80,10 @@ struct ekg_heart {
     cudaStream_t stream = nullptr;    // this heart's device passes run here
     cudaStream_t copy_stream = nullptr;  // early device->host copies overlapping the rest of a pass
     cudaEvent_t static_done = nullptr;   // static-lead ECG rows complete (batched form)
+    // the batched form's static-lead combine and steady-sum reduction run on a second stream beside
+    // the moved-lead operand kernel and GEMM (fork and join by events; captured into the graphs)
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_op = nullptr, ev_join = nullptr;
     uint32_t *err_host = nullptr;     // pinned copy of the kernels' error word
     // device passes captured as CUDA graphs, keyed by everything their launches depend on
     struct PassGraph {
@@ -107,6 +111,9 @@ struct ekg_heart {
             if (g.exec) cudaGraphExecDestroy(g.exec);
         if (stage_host) cudaFreeHost(stage_host);
         if (static_done) cudaEventDestroy(static_done);
+        for (cudaEvent_t e : {ev_fork, ev_op, ev_join})
+            if (e) cudaEventDestroy(e);
+        if (aux_stream) cudaStreamDestroy(aux_stream);
         if (copy_stream) cudaStreamDestroy(copy_stream);
         if (stream) cudaStreamDestroy(stream);
         if (err_host) cudaFreeHost(err_host);

@@ -224,7 +224,7 @@ struct BandArgs {
     const float *gtab = nullptr;
     const float *E = nullptr, *F = nullptr, *partial = nullptr;
     const double *k3 = nullptr;
-    float2 *P1 = nullptr;            // [stages][max_ent][rows] steady sums per 32-AP stage
+    float2 *P1 = nullptr;            // [stages][rows] steady sums per 32-AP stage
     float2 *Up = nullptr;            // [band_u_parts()][rows][nl][max_ent]
     float2 *U = nullptr;             // [rows][nl][max_ent]
     double *ecg = nullptr;

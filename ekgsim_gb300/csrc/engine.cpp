@@ -318,6 +318,11 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     // activation times on the device
     EKG_CUDA(cudaSetDevice(h->eng->device));
     if (!h->stream) EKG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    if (!h->aux_stream) {
+        EKG_CUDA(cudaStreamCreateWithFlags(&h->aux_stream, cudaStreamNonBlocking));
+        for (cudaEvent_t *e : {&h->ev_fork, &h->ev_op, &h->ev_join})
+            EKG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
     if (!h->err_host) EKG_CUDA(cudaMallocHost(&h->err_host, sizeof(uint32_t)));
     EKG_CUDA(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->eng->device));
     h->ev.err.alloc(1);
@@ -1012,7 +1017,7 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
             if (B.Bt.n < bt) B.Bt.alloc(bt);
             const size_t pb = (size_t)std::max(1, P.nitems) * P.rows * 128 * (P.two_bases ? 2 : 1);
             if (B.partial.n < pb) B.partial.alloc(pb);
-            const size_t p1 = (size_t)(D.apad / 32) * B.max_ent * P.rows_used;
+            const size_t p1 = (size_t)(D.apad / 32) * P.rows_used;
             if (B.P1.n < p1) B.P1.alloc(p1);
             if (!B.work.p) B.work.alloc(1);
             const size_t ub = (size_t)P.rows_used * D.nlayers * B.max_ent;
@@ -1040,7 +1045,15 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
     ++launches;
     if (P.batch) {
         BatchState &B = h->bs;
-        launch_static_combine(s, D, P.J, B.J, nmove, n_sims, E.Ff.p, in.coef, in.k3, B.Q1.p, B.Q2.p, E.ecg.p,
+        // with both static and moved leads the static combine and later the steady-sum reduction run
+        // on the auxiliary stream, joined before the band reduction
+        const bool fork = nmove > 0 && nmove < (int)L;
+        cudaStream_t sx = fork ? h->aux_stream : s;
+        if (fork) {
+            EKG_CUDA(cudaEventRecord(h->ev_fork, s));
+            EKG_CUDA(cudaStreamWaitEvent(sx, h->ev_fork, 0));
+        }
+        launch_static_combine(sx, D, P.J, B.J, nmove, n_sims, E.Ff.p, in.coef, in.k3, B.Q1.p, B.Q2.p, E.ecg.p,
                               E.ecg_ff.p);
         launches += nmove < (int)L;
         if (mark_static) {
@@ -1048,7 +1061,7 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             // on it outside the graph)
             cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
             EKG_CUDA(cudaStreamIsCapturing(s, &cs));
-            EKG_CUDA(cudaEventRecordWithFlags(h->static_done, s,
+            EKG_CUDA(cudaEventRecordWithFlags(h->static_done, sx,
                                               cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal
                                                                                   : cudaEventRecordDefault));
         }
@@ -1088,7 +1101,12 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             launch_batch_lead_field(s, D, P.two_bases, in.k5l, in.hconst, in.lrel, nmove, n_sims, U, B.Bt.p,
                                     B.work.p, h->sm_count);
             if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[5], s));
-            launch_band_u(s, U);
+            if (fork) {
+                EKG_CUDA(cudaEventRecord(h->ev_op, s));
+                EKG_CUDA(cudaStreamWaitEvent(sx, h->ev_op, 0));
+            }
+            launch_band_u(sx, U);
+            if (fork) EKG_CUDA(cudaEventRecord(h->ev_join, sx));
             launches += 2;
             if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[1], s));
             BatchArgs A;
@@ -1112,6 +1130,7 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             launch_batch_gemm(s, A);
             launches += P.nitems > 0;
             if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[2], s));
+            if (fork) EKG_CUDA(cudaStreamWaitEvent(s, h->ev_join, 0));
             launch_reduce_band(s, U);
             ++launches;
         } else if (tm && tm->on) {
@@ -1317,9 +1336,9 @@ void benchmark(ekg_heart *h, int n_sims, const double *layer_k, const double *le
         EKG_CUDA(cudaMemcpy(nent.data(), B.nent.p, D.nlayers * 4, cudaMemcpyDeviceToHost));
         EKG_CUDA(cudaMemcpy(esp.data(), B.esplit.p, esp.size() * 4, cudaMemcpyDeviceToHost));
         EKG_CUDA(cudaMemcpy(ls0.data(), B.ls0.p, D.nlayers * 4, cudaMemcpyDeviceToHost));
-        double p1 = 0;  // steady sums written (stages x entries)
+        double p1 = 0;  // stages whose steady sums are written (inside the longest prefix of their layer)
         for (int L = 0; L < D.nlayers; ++L)
-            for (int e = 0; e < nent[L]; ++e) p1 += std::max(0, esp[(size_t)L * 8 + e] - ls0[L]);
+            if (nent[L] > 0) p1 += std::max(0, esp[(size_t)L * 8 + nent[L] - 1] - ls0[L]);
         op_bytes = (double)P.rows_used * D.apad * 4 + p1 * P.rows_used * 8 +
                    (double)D.nvox * 16 + (double)(D.nvox - D.n_interior) * 16 + (double)D.apad * 16;
     }
