@@ -65,7 +65,6 @@ struct PassPlan {
     bool batch = false;                    // separable batched form
     int n_sims = 0, nmove = 0, J = 0, two_bases = 0;
     int rows_used = 0, rows = 0, ntiles = 0, nitems = 0;
-    std::vector<float> coef;               // [S][nl][J]
     std::vector<double> k3;                // [S][nl]
     std::vector<int4> items;               // band GEMM work items, grouped by tile
     std::vector<int32_t> ti0, ti1;         // [ntt][nl] item range of each (tile, layer)
@@ -101,7 +100,7 @@ struct ekg_heart {
     size_t stage_cap = 0;
     struct PassInputs {
         const double *layer_k = nullptr, *cpre = nullptr, *leads = nullptr, *k3 = nullptr;
-        const float *coef = nullptr, *k5l = nullptr;
+        const float *k5l = nullptr;
         const float4 *hconst = nullptr, *lrel = nullptr;
         const int4 *items = nullptr;
         const int32_t *ti0 = nullptr, *ti1 = nullptr;
@@ -126,6 +125,7 @@ struct ekg_heart {
     double ca_ms = 0, setup_ms = 0;
     std::vector<double> t;            // time axis
     std::vector<double> leads0;       // loaded lead positions (z,y,x)
+    std::vector<double> lead_uv;      // their displacement frames [n][u, v]
     std::vector<double> at_host;      // activation time per cell
     std::vector<uint8_t> layer_host;  // layer id per cell (stimulus flag stripped)
     std::vector<int64_t> ap_index_ref;    // reference AP numbering per cell (built on demand)

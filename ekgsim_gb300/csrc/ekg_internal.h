@@ -236,7 +236,8 @@ void launch_taylor_w(cudaStream_t s, const HeartDev &h, const float *W0, int J, 
 void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int32_t *lc0, const int32_t *lc1,
                           const double *partial, float *Q);
 void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const float *F,
-                           const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg,
+                           const double *layer_k, const double *centre, const double *scale, const double *k3,
+                           const float *Q1, const float *Q2, double *ecg,
                            float2 *ecg_ff);
 void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const float *k5l,
                              const float4 *hconst, const float4 *lrel, int nmove, int n_sims, const BandArgs &B,

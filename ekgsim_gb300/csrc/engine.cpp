@@ -232,6 +232,8 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     h->dt = d->dt;
     h->nhood = d->nhood;
     h->leads0.assign(d->leads_zyx, d->leads_zyx + 3 * d->n_leads);
+    h->lead_uv.resize(6 * (size_t)d->n_leads);
+    lead_frames(d->n_leads, h->leads0.data(), h->lead_uv.data());
     HeartDev &D = h->dev;
     D.nz = d->nz;
     D.ny = d->ny;
@@ -874,19 +876,8 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
     P.batch = true;
     P.J = J;
     P.two_bases = k3_uniform ? 0 : 1;
-    P.coef.resize((size_t)n_sims * nl * J);
     P.k3.resize((size_t)n_sims * nl);
-    for (int si = 0; si < n_sims; ++si)
-        for (int i = 0; i < nl; ++i) {
-            const double *k = layer_k + ((size_t)si * nl + i) * 9;
-            const double x = k[5] * B.scale[i];
-            double c = std::exp(k[5] * B.centre[i]);
-            for (int j = 0; j < J; ++j) {
-                P.coef[((size_t)si * nl + i) * J + j] = (float)c;
-                c *= x / (j + 1);
-            }
-            P.k3[(size_t)si * nl + i] = k[3];
-        }
+    for (size_t i = 0; i < P.k3.size(); ++i) P.k3[i] = layer_k[9 * i + 3];
     const double L2E = 1.4426950408889634;
     for (int i = 0; i < nl; ++i)
         P.hc[i] = make_float4((float)(key[2 * i] * L2E), (float)(key[2 * i + 1] * L2E), (float)(1.0 - layer_k[9 * i + 3]),
@@ -969,9 +960,8 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
     const size_t o_lk = add(layer_k, S * nl * 9 * 8);
     const size_t o_cp = add(cpre.data(), cpre.size() * 8);
     const size_t o_ld = add(leads, P.nmove > 0 ? S * L * 3 * 8 : 0);
-    size_t o_coef = 0, o_k3 = 0, o_hc = 0, o_ti0 = 0, o_ti1 = 0, o_it = 0, o_k5 = 0, o_lr = 0;
+    size_t o_k3 = 0, o_hc = 0, o_ti0 = 0, o_ti1 = 0, o_it = 0, o_k5 = 0, o_lr = 0;
     if (P.batch) {
-        o_coef = add(P.coef.data(), P.coef.size() * 4);
         o_k3 = add(P.k3.data(), P.k3.size() * 8);
         o_hc = add(P.hc, nl * sizeof(float4));
         if (P.nmove > 0) {
@@ -1001,7 +991,6 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
     in.cpre = h->cpre_on ? reinterpret_cast<const double *>(dv + o_cp) : nullptr;
     in.leads = P.nmove > 0 ? reinterpret_cast<const double *>(dv + o_ld) : nullptr;
     if (P.batch) {
-        in.coef = reinterpret_cast<const float *>(dv + o_coef);
         in.k3 = reinterpret_cast<const double *>(dv + o_k3);
         in.hconst = reinterpret_cast<const float4 *>(dv + o_hc);
         if (P.nmove > 0) {
@@ -1053,7 +1042,8 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             EKG_CUDA(cudaEventRecord(h->ev_fork, s));
             EKG_CUDA(cudaStreamWaitEvent(sx, h->ev_fork, 0));
         }
-        launch_static_combine(sx, D, P.J, B.J, nmove, n_sims, E.Ff.p, in.coef, in.k3, B.Q1.p, B.Q2.p, E.ecg.p,
+        launch_static_combine(sx, D, P.J, B.J, nmove, n_sims, E.Ff.p, in.layer_k, B.d_centre.p, B.d_scale.p, in.k3,
+                              B.Q1.p, B.Q2.p, E.ecg.p,
                               E.ecg_ff.p);
         launches += nmove < (int)L;
         if (mark_static) {
@@ -1183,7 +1173,7 @@ std::vector<uint64_t> pass_signature(const ekg_heart *h, const PassPlan &P, int 
                                (uint64_t)B.max_ent, (uint64_t)B.ntt};
     const ekg_heart::PassInputs &in = h->in;
     for (const void *p : {(const void *)in.layer_k, (const void *)in.cpre, (const void *)in.leads, (const void *)in.k3,
-                          (const void *)in.coef, (const void *)in.k5l, (const void *)in.hconst, (const void *)in.lrel,
+                          (const void *)B.d_centre.p, (const void *)B.d_scale.p, (const void *)in.k5l, (const void *)in.hconst, (const void *)in.lrel,
                           (const void *)in.items, (const void *)in.ti0, (const void *)in.ti1,
                           (const void *)E.F.p, (const void *)E.Ff.p,
                           (const void *)E.layer_c.p, (const void *)E.ecg.p, (const void *)E.crit.p, (const void *)E.err.p,
@@ -1371,12 +1361,8 @@ void prepare_sim(ekg_heart *h, const double *genes, int n_genes, double *layer_k
     for (int i = 0; i < n_genes; ++i)
         EKG_CHECK(std::isfinite(genes[i]), EKG_ERR_BAD_INPUT, "gene values must be finite");
     if (es.optimize_points) {
-        std::vector<double> disp(2 * h->dev.nleads);
-        for (int i = 0; i < h->dev.nleads; ++i) {
-            disp[2 * i] = genes[nw + 2 * i];
-            disp[2 * i + 1] = genes[nw + 2 * i + 1];
-        }
-        move_leads(h->dev.nleads, h->leads0.data(), disp.data(), leads);
+        // the displacement genes are (u, v) pairs per lead, the layout move_leads takes
+        move_leads_framed(h->dev.nleads, h->leads0.data(), h->lead_uv.data(), genes + nw, leads);
     } else {
         std::copy(h->leads0.begin(), h->leads0.end(), leads);
     }

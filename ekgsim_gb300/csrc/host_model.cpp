@@ -560,7 +560,7 @@ void layer_aps_from_genes(const GeneModel &m, int nl, const double *genes, doubl
     layer_aps_run_fits(jobs.data(), jobs.size());
 }
 
-void move_leads(int n, const double *orig, const double *disp, double *out) {
+void lead_frames(int n, const double *orig, double *uv) {
     for (int i = 0; i < n; ++i) {
         const double *p = orig + 3 * i;
         const double x[3] = {0, 0, 1};
@@ -583,9 +583,23 @@ void move_leads(int n, const double *orig, const double *disp, double *out) {
                 w[2] *= 0.0;
             }
         }
+        std::copy(u, u + 3, uv + 6 * i);
+        std::copy(v, v + 3, uv + 6 * i + 3);
+    }
+}
+
+void move_leads_framed(int n, const double *orig, const double *uv, const double *disp, double *out) {
+    for (int i = 0; i < n; ++i) {
+        const double *p = orig + 3 * i, *u = uv + 6 * i, *v = uv + 6 * i + 3;
         const double du = disp ? disp[2 * i] : 0.0, dv = disp ? disp[2 * i + 1] : 0.0;
         for (int c = 0; c < 3; ++c) out[3 * i + c] = (p[c] + du * u[c]) + dv * v[c];
     }
+}
+
+void move_leads(int n, const double *orig, const double *disp, double *out) {
+    std::vector<double> uv(6 * (size_t)std::max(0, n));
+    lead_frames(n, orig, uv.data());
+    move_leads_framed(n, orig, uv.data(), disp, out);
 }
 
 }  // namespace ekg

@@ -105,5 +105,9 @@ void layer_aps_setup(const GeneModel &m, int n_layers, const double *genes, doub
 void layer_aps_run_fits(const LayerFitJob *jobs, size_t n);
 // EkgSim::loadMeasuringPoints basis + moveMeasuringPoints (simlib/sim_lib.h:167-208).
 void move_leads(int n, const double *orig_zyx, const double *disp_uv, double *out_zyx);
+// the same in two parts: the per-lead displacement frames (u, v unit vectors, [n][6]), which depend
+// only on the loaded positions, and the move itself (same arithmetic, same results)
+void lead_frames(int n, const double *orig_zyx, double *uv);
+void move_leads_framed(int n, const double *orig_zyx, const double *uv, const double *disp_uv, double *out_zyx);
 
 }  // namespace ekg
