@@ -117,17 +117,15 @@ __global__ void k_reduce_layers(int steps, int rows, int nl, const int32_t *__re
 
 // Static leads: ecg[s][l][t] = sum_L F[s][L][t] sum_j coef[s][L][j] ((1-k3) Q1 + k3 Q2)[L][l*J+j][t],
 // coef[s][L][j] = exp(k5 c_L) (k5 s_L)^j / j! (k5 of the simulation's layer AP, c_L and s_L the
-// centre and half-range of the layer's activation times), the Taylor sum per layer in FP32 (the
-// basis is stored in FP32), the sum over layers in float-float; written as FP64 and as
-// float-float.  Block = 128 steps of one static lead for SC_SIMS simulations: a thread loads the
-// basis rows of its step once per layer and applies them to every simulation of the group
-// (coefficients computed in FP64 and broadcast from shared memory).
+// centre and half-range of the layer's activation times; from k_layer_factors), the Taylor sum
+// per layer in FP32 (the basis is stored in FP32), the sum over layers in float-float; written as
+// FP64 and as float-float.  Block = 128 steps of one static lead for SC_SIMS simulations: a
+// thread loads the basis rows of its step once per layer and applies them to every simulation of
+// the group (coefficients broadcast from shared memory).
 constexpr int SC_SIMS = 16;
 __global__ void __launch_bounds__(128) k_static_combine(int steps, int nleads, int nl, int J, int Jb, int nmove,
                                                         int n_sims, const float *__restrict__ F,
-                                                        const double *__restrict__ layer_k,
-                                                        const double *__restrict__ centre,
-                                                        const double *__restrict__ scale, const double *__restrict__ k3,
+                                                        const float *__restrict__ coef, const double *__restrict__ k3,
                                                         const float *__restrict__ Q1, const float *__restrict__ Q2,
                                                         double *__restrict__ ecg, float2 *__restrict__ ecg_ff) {
     __shared__ float s_c[SC_SIMS][11];  // [simulation][j < J: coefficient, 10: k3] of the current layer
@@ -142,15 +140,10 @@ __global__ void __launch_bounds__(128) k_static_combine(int steps, int nleads, i
     for (int i = 0; i < SC_SIMS; ++i) acc[i] = make_float2(0.f, 0.f);
     for (int L = 0; L < nl; ++L) {
         __syncthreads();
-        for (int i = threadIdx.x; i < ns; i += blockDim.x) {
+        for (int k = threadIdx.x; k < ns * 11; k += blockDim.x) {
+            const int i = k / 11, j = k % 11;
             const size_t sl = (size_t)(s0 + i) * nl + L;
-            const double k5 = layer_k[sl * 9 + 5], x = k5 * scale[L];
-            double c = exp(k5 * centre[L]);
-            for (int j = 0; j < 10; ++j) {
-                s_c[i][j] = j < J ? (float)c : 0.f;
-                c *= x / (j + 1);
-            }
-            s_c[i][10] = (float)k3[sl];
+            s_c[i][j] = j < J ? coef[sl * J + j] : (j == 10 ? (float)k3[sl] : 0.f);
         }
         __syncthreads();
         const size_t q0 = ((size_t)L * rows + (size_t)l * Jb) * steps + tc;
@@ -1039,13 +1032,11 @@ void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int
 }
 
 void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const float *F,
-                           const double *layer_k, const double *centre, const double *scale, const double *k3,
-                           const float *Q1, const float *Q2, double *ecg,
+                           const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg,
                            float2 *ecg_ff) {
     if (nmove >= h.nleads) return;
     dim3 grid((unsigned)((h.steps + 127) / 128), (unsigned)(h.nleads - nmove), (unsigned)((n_sims + SC_SIMS - 1) / SC_SIMS));
-    k_static_combine<<<grid, 128, 0, s>>>(h.steps, h.nleads, h.nlayers, J, Jb, nmove, n_sims, F, layer_k, centre,
-                                          scale, k3, Q1, Q2,
+    k_static_combine<<<grid, 128, 0, s>>>(h.steps, h.nleads, h.nlayers, J, Jb, nmove, n_sims, F, coef, k3, Q1, Q2,
                                           ecg, ecg_ff);
     EKG_CUDA(cudaGetLastError());
 }

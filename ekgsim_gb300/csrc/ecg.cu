@@ -110,7 +110,8 @@ __global__ void k_lead_field(int64_t apad, const int64_t *__restrict__ a_vox_beg
 // passes, where the FP64 pow/log would be one block's latency), else NULL.
 __global__ void k_layer_factors(int nl, int steps, const double *__restrict__ t, const double *__restrict__ layer_k,
                                 const double *__restrict__ cpre, int n_sims, double *__restrict__ F,
-                                float *__restrict__ Ff, float *__restrict__ layer_c) {
+                                float *__restrict__ Ff, float *__restrict__ layer_c, const double *__restrict__ centre,
+                                const double *__restrict__ scale, int J, float *__restrict__ coef) {
     const int64_t sl = blockIdx.x;  // sim * nl + layer
     const double *k = layer_k + sl * 9;
     __shared__ double c;
@@ -119,6 +120,15 @@ __global__ void k_layer_factors(int nl, int steps, const double *__restrict__ t,
         const double L2E = 1.4426950408889634;
         reinterpret_cast<float4 *>(layer_c)[sl] =
             make_float4((float)(k[1] * L2E), (float)(k[4] * L2E), (float)(1.0 - k[3]), (float)k[3]);
+    } else if (threadIdx.x == 32 && coef) {
+        // Taylor coefficients of the static-lead basis: coef[sl][j] = exp(k5 c_L) (k5 s_L)^j / j!
+        const int L = (int)(sl % nl);
+        const double x = k[5] * scale[L];
+        double e = exp(k[5] * centre[L]);
+        for (int j = 0; j < J; ++j) {
+            coef[sl * J + j] = (float)e;
+            e *= x / (j + 1);
+        }
     }
     __syncthreads();
     const float r = (float)(k[6] / k[7]);
@@ -384,9 +394,10 @@ void launch_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads,
 }
 
 void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_layer_k, const double *d_cpre,
-                          int n_sims, double *d_F, float *d_Ff, float *d_layer_c) {
-    k_layer_factors<<<(unsigned)((int64_t)n_sims * h.nlayers), 128, 0, s>>>(h.nlayers, h.steps, h.t.p, d_layer_k,
-                                                                            d_cpre, n_sims, d_F, d_Ff, d_layer_c);
+                          int n_sims, double *d_F, float *d_Ff, float *d_layer_c, const double *d_centre,
+                          const double *d_scale, int J, float *d_coef) {
+    k_layer_factors<<<(unsigned)((int64_t)n_sims * h.nlayers), 128, 0, s>>>(
+        h.nlayers, h.steps, h.t.p, d_layer_k, d_cpre, n_sims, d_F, d_Ff, d_layer_c, d_centre, d_scale, J, d_coef);
     EKG_CUDA(cudaGetLastError());
 }
 

@@ -164,6 +164,7 @@ struct EvalDev {
     DBuf<float> W;          // [S][L][apad] lead field for this eval's positions
     DBuf<float> Wp;         // [S][L][apad] W * exp(k5 at)
     DBuf<double> partial;   // [S][nchunks][L][steps]
+    DBuf<float> coef;       // [S][nl][J] static-lead Taylor coefficients (batched form)
     DBuf<double> ecg;       // [S][L][steps]
     DBuf<float2> ecg_ff;    // [S][L][steps] the same as float-float (hi, lo), read by the criteria
     DBuf<double> crit;      // [S][ncrit]
@@ -177,7 +178,8 @@ struct EvalDev {
 void launch_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads, int nleads_in, int lead_stride,
                        int n_sims, float *d_W, int w_lead_stride);
 void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_layer_k, const double *d_cpre,
-                          int n_sims, double *d_F, float *d_Ff, float *d_layer_c);
+                          int n_sims, double *d_F, float *d_Ff, float *d_layer_c, const double *d_centre = nullptr,
+                          const double *d_scale = nullptr, int J = 0, float *d_coef = nullptr);
 void launch_scale_w(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
                     float *d_Wp);
 void launch_k0_term(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
@@ -236,8 +238,7 @@ void launch_taylor_w(cudaStream_t s, const HeartDev &h, const float *W0, int J, 
 void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int32_t *lc0, const int32_t *lc1,
                           const double *partial, float *Q);
 void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const float *F,
-                           const double *layer_k, const double *centre, const double *scale, const double *k3,
-                           const float *Q1, const float *Q2, double *ecg,
+                           const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg,
                            float2 *ecg_ff);
 void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const float *k5l,
                              const float4 *hconst, const float4 *lrel, int nmove, int n_sims, const BandArgs &B,

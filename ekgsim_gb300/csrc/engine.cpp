@@ -551,7 +551,7 @@ int64_t heart_device_bytes(const ekg_heart *h) {
                 h->W0.bytes() + h->at_cells.bytes();
     const EvalDev &E = h->ev;
     b += (int64_t)h->stage_dev.bytes() + E.layer_c.bytes() + E.F.bytes() + E.k0w.bytes() + E.W.bytes() +
-         E.Wp.bytes() + E.partial.bytes() + E.ecg.bytes() + E.ecg_ff.bytes() + E.crit.bytes() + E.targets.bytes() +
+         E.Wp.bytes() + E.partial.bytes() + E.ecg.bytes() + E.ecg_ff.bytes() + E.coef.bytes() + E.crit.bytes() + E.targets.bytes() +
          E.targets_ff.bytes();
     return b;
 }
@@ -1001,6 +1001,8 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
             in.lrel = reinterpret_cast<const float4 *>(dv + o_lr);
         }
         BatchState &B = h->bs;
+        const size_t nc = (size_t)n_sims * D.nlayers * std::max(1, P.J);
+        if (h->ev.coef.n < nc) h->ev.coef.alloc(nc);
         if (P.nmove > 0) {
             const size_t bt = (size_t)P.rows * D.apad * 4;
             if (B.Bt.n < bt) B.Bt.alloc(bt);
@@ -1030,31 +1032,36 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
     if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[0], s));
     EKG_CUDA(cudaMemsetAsync(E.err.p, 0, sizeof(uint32_t), s));
     const ekg_heart::PassInputs &in = h->in;
-    launch_layer_factors(s, D, in.layer_k, in.cpre, n_sims, E.F.p, E.Ff.p, E.layer_c.p);
+    launch_layer_factors(s, D, in.layer_k, in.cpre, n_sims, E.F.p, E.Ff.p, E.layer_c.p,
+                         P.batch ? h->bs.d_centre.p : nullptr, P.batch ? h->bs.d_scale.p : nullptr, P.J,
+                         P.batch ? E.coef.p : nullptr);
     ++launches;
     if (P.batch) {
         BatchState &B = h->bs;
-        // with both static and moved leads the static combine and later the steady-sum reduction run
-        // on the auxiliary stream, joined before the band reduction
+        // with both static and moved leads, the static combine (beside the moved-lead operand kernel)
+        // and the steady-sum reduction (beside the band GEMM) run on the auxiliary stream, joined
+        // before the band reduction
         const bool fork = nmove > 0 && nmove < (int)L;
         cudaStream_t sx = fork ? h->aux_stream : s;
         if (fork) {
             EKG_CUDA(cudaEventRecord(h->ev_fork, s));
             EKG_CUDA(cudaStreamWaitEvent(sx, h->ev_fork, 0));
         }
-        launch_static_combine(sx, D, P.J, B.J, nmove, n_sims, E.Ff.p, in.layer_k, B.d_centre.p, B.d_scale.p, in.k3,
-                              B.Q1.p, B.Q2.p, E.ecg.p,
-                              E.ecg_ff.p);
-        launches += nmove < (int)L;
-        if (mark_static) {
-            // inside a graph capture the record must be an external event node (the copy stream waits
-            // on it outside the graph)
-            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-            EKG_CUDA(cudaStreamIsCapturing(s, &cs));
-            EKG_CUDA(cudaEventRecordWithFlags(h->static_done, sx,
-                                              cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal
-                                                                                  : cudaEventRecordDefault));
-        }
+        auto static_part = [&]() {
+            launch_static_combine(sx, D, P.J, B.J, nmove, n_sims, E.Ff.p, E.coef.p, in.k3, B.Q1.p, B.Q2.p, E.ecg.p,
+                                  E.ecg_ff.p);
+            launches += nmove < (int)L;
+            if (mark_static) {
+                // inside a graph capture the record must be an external event node (the copy stream
+                // waits on it outside the graph)
+                cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+                EKG_CUDA(cudaStreamIsCapturing(s, &cs));
+                EKG_CUDA(cudaEventRecordWithFlags(h->static_done, sx,
+                                                  cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal
+                                                                                      : cudaEventRecordDefault));
+            }
+        };
+        static_part();
         if (nmove > 0) {
             if (P.rows_used < P.rows) EKG_CUDA(cudaMemsetAsync(B.Bt.p, 0, (size_t)P.rows * D.apad * 4, s));
             BandArgs U;
@@ -1173,7 +1180,8 @@ std::vector<uint64_t> pass_signature(const ekg_heart *h, const PassPlan &P, int 
                                (uint64_t)B.max_ent, (uint64_t)B.ntt};
     const ekg_heart::PassInputs &in = h->in;
     for (const void *p : {(const void *)in.layer_k, (const void *)in.cpre, (const void *)in.leads, (const void *)in.k3,
-                          (const void *)B.d_centre.p, (const void *)B.d_scale.p, (const void *)in.k5l, (const void *)in.hconst, (const void *)in.lrel,
+                          (const void *)B.d_centre.p, (const void *)B.d_scale.p, (const void *)E.coef.p,
+                          (const void *)in.k5l, (const void *)in.hconst, (const void *)in.lrel,
                           (const void *)in.items, (const void *)in.ti0, (const void *)in.ti1,
                           (const void *)E.F.p, (const void *)E.Ff.p,
                           (const void *)E.layer_c.p, (const void *)E.ecg.p, (const void *)E.crit.p, (const void *)E.err.p,
