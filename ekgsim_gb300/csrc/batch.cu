@@ -582,42 +582,44 @@ __global__ void __launch_bounds__(128) k_batch_lead_field_small(
 // Steady sums per (row', layer, entry): U[row'][L][e] = sum over the layer's stages [ls0, ls1)
 // below the entry's prefix end of (P1[st][row'].x, G_e[st] P1[st][row'].y) (U0, U1),
 // G_e[st] = gtab[goff[L][e] + st - ls0[L]].  Two passes in a fixed order: k_band_u sums BU_PARTS
-// consecutive parts of the stage range in FP32 (a few stages each) per (part, layer) block,
-// threads over rows, all entries from one read of P1; k_band_u2 adds the parts in FP64, one warp
-// per output.  Up: [parts][rows][nl][max_ent]; U stored in FP32.  The prefix ends ascend with e.
+// consecutive parts of the stage range in FP32 (a few stages each), block per (part, 128 rows,
+// layer), thread per row, all entries from one read of P1 (small blocks that fit beside the band
+// GEMM's CTAs, which they run next to); k_band_u2 adds the parts in FP64, one warp per output.
+// Up: [parts][rows][nl][max_ent]; U stored in FP32.  The prefix ends ascend with e.
 constexpr int BU_PARTS = 128;
-__global__ void __launch_bounds__(256) k_band_u(int rows_used, int nl, int max_ent, const int32_t *__restrict__ nent,
-                                                const int32_t *__restrict__ esplit, const int32_t *__restrict__ ls0,
-                                                const int32_t *__restrict__ ls1, const int64_t *__restrict__ goff,
-                                                const float *__restrict__ gtab, const float2 *__restrict__ P1,
-                                                float2 *__restrict__ Up) {
-    const int p = blockIdx.x, L = blockIdx.y;
+__global__ void __launch_bounds__(128, 8) k_band_u(int rows_used, int nl, int max_ent,
+                                                   const int32_t *__restrict__ nent, const int32_t *__restrict__ esplit,
+                                                   const int32_t *__restrict__ ls0, const int32_t *__restrict__ ls1,
+                                                   const int64_t *__restrict__ goff, const float *__restrict__ gtab,
+                                                   const float2 *__restrict__ P1, float2 *__restrict__ Up) {
+    const int p = blockIdx.x, L = blockIdx.z;
+    const int rr = blockIdx.y * blockDim.x + threadIdx.x;
+    if (rr >= rows_used) return;
     const int ne = nent[L], n = ls1[L] - ls0[L];
     const int g0 = ls0[L] + (int)((int64_t)n * p / BU_PARTS), g1 = ls0[L] + (int)((int64_t)n * (p + 1) / BU_PARTS);
     int ge[MAXE];
-    int64_t go[MAXE];  // gtab index of stage g of entry e: go[e] + g
+    const float *gt[MAXE];  // entry e's factor of stage g: gt[e][g - g0]
 #pragma unroll
     for (int e = 0; e < MAXE; ++e) {
         ge[e] = e < ne ? min(g1, esplit[L * MAXE + e]) : g0;
-        go[e] = e < ne ? goff[L * MAXE + e] - ls0[L] : 0;
+        gt[e] = gtab + (e < ne ? goff[L * MAXE + e] + (g0 - ls0[L]) : 0);
     }
     const int gend = ne > 0 ? ge[ne - 1] : g0;
-    for (int rr = threadIdx.x; rr < rows_used; rr += blockDim.x) {
-        float a[MAXE], b[MAXE];
+    float a[MAXE], b[MAXE];
 #pragma unroll
-        for (int e = 0; e < MAXE; ++e) a[e] = b[e] = 0.f;
-        for (int g = g0; g < gend; ++g) {
-            const float2 v = P1[(size_t)g * rows_used + rr];
+    for (int e = 0; e < MAXE; ++e) a[e] = b[e] = 0.f;
+    for (int g = g0; g < gend; ++g) {
+        const float2 v = P1[(size_t)g * rows_used + rr];
 #pragma unroll
-            for (int e = 0; e < MAXE; ++e)
-                if (g < ge[e]) {
-                    a[e] += v.x;
-                    b[e] = fmaf(gtab[go[e] + g], v.y, b[e]);
-                }
-        }
-        for (int e = 0; e < ne; ++e)
-            Up[(((size_t)p * rows_used + rr) * nl + L) * max_ent + e] = make_float2(a[e], b[e]);
+        for (int e = 0; e < MAXE; ++e)
+            if (g < ge[e]) {
+                a[e] += v.x;
+                b[e] = fmaf(gt[e][g - g0], v.y, b[e]);
+            }
     }
+#pragma unroll
+    for (int e = 0; e < MAXE; ++e)
+        if (e < ne) Up[(((size_t)p * rows_used + rr) * nl + L) * max_ent + e] = make_float2(a[e], b[e]);
 }
 
 __global__ void __launch_bounds__(256) k_band_u2(int64_t n_out, const float2 *__restrict__ Up, float2 *__restrict__ U) {
@@ -1107,8 +1109,8 @@ void launch_batch_gemm(cudaStream_t s, const BatchArgs &A) {
 int band_u_parts() { return BU_PARTS; }
 
 void launch_band_u(cudaStream_t s, const BandArgs &A) {
-    k_band_u<<<dim3(BU_PARTS, (unsigned)A.nl), 256, 0, s>>>(A.rows_used, A.nl, A.max_ent, A.nent, A.esplit, A.ls0,
-                                                           A.ls1, A.goff, A.gtab, A.P1, A.Up);
+    k_band_u<<<dim3(BU_PARTS, (unsigned)((A.rows_used + 127) / 128), (unsigned)A.nl), 128, 0, s>>>(
+        A.rows_used, A.nl, A.max_ent, A.nent, A.esplit, A.ls0, A.ls1, A.goff, A.gtab, A.P1, A.Up);
     const int64_t n = (int64_t)A.rows_used * A.nl * A.max_ent;
     k_band_u2<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(n, A.Up, A.U);
     EKG_CUDA(cudaGetLastError());
