@@ -358,8 +358,9 @@ def run_ours(args):
                 "traffic": tr * batch if tr is not None else None, "peak_source": src,
                 "kernel": "k_batch_lead_field", "launch_ms": op_s * 1000.0,
                 "algorithmic_bytes": bm["operand_bytes"],
-                "note": "FP32 + SFU issue-bound field evaluation (one rsqrt per interior voxel and lead, nine per "
-                        "boundary voxel); the HBM figure is the kernel's byte floor"}
+                "note": "FP32 + SFU issue-bound field evaluation (one rsqrt per interior voxel and lead, one more "
+                        "per absent neighbour of a boundary voxel with few absent, nine for the other boundary "
+                        "voxels); the HBM figure is the kernel's byte floor"}
         gemm_s = bm["contract_ms"] / 1000.0 / args.steps
         roof["gemm"] = {"kernel": "k_batch_umma", "bound": "tensor", "launch_ms": gemm_s * 1000.0,
                         "executed_tflops": bm["gemm_flops"] / gemm_s / 1e12 if gemm_s > 0 else None,
