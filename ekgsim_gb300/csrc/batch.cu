@@ -319,17 +319,16 @@ __device__ __forceinline__ void few_w(const InteriorField &ic, const MSquares (&
     }
 }
 
-// sum_{v in a} w(v) for the 8 APs of a chunk (voxels [vb, vend)) and NP lead positions, into
-// s_w[k][j][tid]: one flat loop over the chunk's voxels (grouped by AP, the last one of each AP
-// flagged); APs without
+// sum_{v in a} w(v) for the 8 APs of a chunk (voxel records [vb, vend) of vox_pos / vox_out, in
+// shared or global memory) and NP lead positions, into s_w[k][j][tid]: one flat loop over the
+// chunk's voxels (grouped by AP, the last one of each AP flagged); APs without
 // voxels (padding, at the end of a layer) get 0.  Interior voxels use the closed form where the
 // lane's leads are at least 20 cells away (lanes normally agree), boundary voxels with few absent
 // neighbours the closed form minus those, the rest the exact sum.
 template <bool DIAG, int NP>
-__device__ __forceinline__ void chunk_w(int vb, int vend, const float4 *__restrict__ vox_pos,
-                                        const float4 *__restrict__ vox_out, const float4 (&r)[NP], int nnb,
-                                        const float *s_d, const InteriorField &ic, float (*s_w)[8][LF_THREADS],
-                                        int tid) {
+__device__ __forceinline__ void chunk_w(int vb, int vend, const float4 *vox_pos, const float4 *vox_out,
+                                        const float4 (&r)[NP], int nnb, const float *s_d, const InteriorField &ic,
+                                        float (*s_w)[8][LF_THREADS], int tid) {
     const uint32_t full = (1u << nnb) - 1u;
     float acc[NP];
 #pragma unroll
@@ -385,6 +384,7 @@ __device__ __forceinline__ void chunk_w(int vb, int vend, const float4 *__restri
 constexpr int MAXE = 8;
 constexpr int BST = 32;     // APs per stage
 constexpr int LF_ROWS = 4;  // rows per thread
+constexpr int LF_VCAP = 256;  // voxel records of a stage staged in shared memory
 static_assert(LF_THREADS >= BST + BST / 8 + 1, "the stage tables are loaded one entry per thread");
 template <int N, bool DIAG>
 __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
@@ -399,8 +399,7 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
     __shared__ float2 s_at[BST];  // the stage's activation times
     __shared__ float s_ez[BST];   // exp(-k4 (T_st - at)), 0 for padding
     __shared__ int s_vb[BST / 8 + 1];  // first voxel of each chunk of the stage, and the end
-    __shared__ float s_k5[LF_ROWS][LF_THREADS];       // k5 log2(e) of each row's simulation
-    __shared__ float2 s_sum[LF_ROWS][LF_THREADS];     // the stage's steady sums of each row
+    __shared__ float4 s_vpos[LF_VCAP], s_vout[LF_VCAP];  // the stage's voxel records, when they fit
     __shared__ int s_item;
     const int tid = threadIdx.x;
     if (tid < nnb) {
@@ -420,24 +419,33 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
         if (item >= nst * ngr) break;
         const int st = item / ngr;
         const int L = a_layer[(int64_t)st * BST];
+        // the stage's voxel records are copied to shared memory once per item (a stage of up to
+        // LF_VCAP voxels; larger ones read global memory), so the voxel loop waits on no global load
+        const int v0 = (int)a_vox_begin[(int64_t)st * BST], nv = (int)a_vox_begin[(int64_t)(st + 1) * BST] - v0;
+        const bool staged = nv <= LF_VCAP;
+        if (staged)
+            for (int i = tid; i < nv; i += LF_THREADS) {
+                s_vpos[i] = vox_pos[v0 + i];
+                s_vout[i] = vox_out[v0 + i];
+            }
         if (tid < BST) {
             const float2 at = at_hilo[(int64_t)st * BST + tid], T = tref[st];
             s_at[tid] = at;
             s_ez[tid] = isinf(at.x) ? 0.f : ex2a(-hconst[L].y * ((T.x - at.x) + (T.y - at.y)));
         } else if (tid < BST + BST / 8 + 1) {
-            s_vb[tid - BST] = (int)a_vox_begin[(int64_t)st * BST + (tid - BST) * 8];
+            s_vb[tid - BST] = (int)a_vox_begin[(int64_t)st * BST + (tid - BST) * 8] - (staged ? v0 : 0);
         }
         __syncthreads();
+        const float4 *vp = staged ? s_vpos : vox_pos, *vo = staged ? s_vout : vox_out;
         const int rb = (item % ngr) * (LF_THREADS * LF_ROWS) + tid * LF_ROWS;
         if (rb >= rows_used) continue;
         const int nr = min(LF_ROWS, rows_used - rb);  // rows of this thread; the rest repeat its last row
-        // per-row state lives in shared memory; the lead positions are (re)loaded for each chunk's
-        // voxel loop, so that registers are not held across the chunk's output stage
+        float k5[LF_ROWS], S0[LF_ROWS], S1[LF_ROWS];
 #pragma unroll
         for (int q = 0; q < LF_ROWS; ++q) {
             const int row = rb + min(q, nr - 1);
-            s_k5[q][tid] = k5l[(size_t)(row / nmove) * nl + L];
-            s_sum[q][tid] = make_float2(0.f, 0.f);
+            k5[q] = k5l[(size_t)(row / nmove) * nl + L];
+            S0[q] = S1[q] = 0.f;
         }
         const int kt = st >> 1;
 #pragma unroll 1
@@ -446,18 +454,17 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
                 float4 r[LF_ROWS];
 #pragma unroll
                 for (int q = 0; q < LF_ROWS; ++q) r[q] = lrel[rb + min(q, nr - 1)];
-                chunk_w<DIAG, LF_ROWS>(s_vb[kc], s_vb[kc + 1], vox_pos, vox_out, r, nnb, s_d, ic, s_w, tid);
+                chunk_w<DIAG, LF_ROWS>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
             }
             const int col = (st & 1) * (BST / 8) + kc;  // 8-AP column within the 64-AP tile
 #pragma unroll
             for (int q = 0; q < LF_ROWS; ++q) {
                 if (q >= nr) break;
                 float wv[8];
-                const float k5 = s_k5[q][tid];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const float2 at = s_at[kc * 8 + j];
-                    wv[j] = isinf(at.x) ? 0.f : s_w[q][j][tid] * ex2a(fmaf(k5, at.x, k5 * at.y));
+                    wv[j] = isinf(at.x) ? 0.f : s_w[q][j][tid] * ex2a(fmaf(k5[q], at.x, k5[q] * at.y));
                 }
                 uint4 hv, lv;
                 split2(wv[0], wv[1], hv.x, lv.x);
@@ -476,8 +483,8 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
                     z0 += wv[j];
                     z1 = fmaf(wv[j], s_ez[kc * 8 + j], z1);
                 }
-                const float2 sm = s_sum[q][tid];
-                s_sum[q][tid] = make_float2(sm.x + z0, sm.y + z1);
+                S0[q] += z0;
+                S1[q] += z1;
             }
         }
         const int ne = nent[L];
@@ -486,7 +493,7 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
             for (int q = 0; q < LF_ROWS; ++q) {
                 if (q >= nr) break;
                 const int row = rb + q, s = row / nmove, l = row % nmove;
-                P1[(size_t)st * rows_used + (size_t)l * n_sims + s] = s_sum[q][tid];
+                P1[(size_t)st * rows_used + (size_t)l * n_sims + s] = make_float2(S0[q], S1[q]);
             }
     }
 }
