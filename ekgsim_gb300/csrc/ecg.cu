@@ -266,31 +266,68 @@ __device__ __forceinline__ double warp_max(double v) {
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
-// float-float butterfly sum; lane 0's result is broadcast so every lane holds the same value
-__device__ __forceinline__ double warp_sum_ff(float2 v) {
+// Block-wide reductions for the criteria (NT threads): a warp butterfly, then lane 0 of each warp
+// in warp order, so every thread gets the same value in a fixed order.  `red` is shared scratch of
+// NT / 32 entries.
+template <int NT>
+__device__ __forceinline__ double block_sum_ff(float2 v, float2 *red) {
+    constexpr int CR_WARPS = NT / 32;
     for (int o = 16; o > 0; o >>= 1) {
         const float2 w = make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
         v = ff_add(v, w);
     }
-    v.x = __shfl_sync(0xffffffffu, v.x, 0);
-    v.y = __shfl_sync(0xffffffffu, v.y, 0);
-    return ff_to_double(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    float2 t = red[0];
+    for (int k = 1; k < CR_WARPS; ++k) t = ff_add(t, red[k]);
+    return ff_to_double(t);
+}
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double *red) {
+    constexpr int CR_WARPS = NT / 32;
+    v = warp_sum(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = red[0];
+    for (int k = 1; k < CR_WARPS; ++k) t += red[k];
+    return t;
+}
+template <int NT>
+__device__ __forceinline__ double block_minmax(double v, bool is_max, double *red) {
+    constexpr int CR_WARPS = NT / 32;
+    v = is_max ? warp_max(v) : warp_min(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = red[0];
+    for (int k = 1; k < CR_WARPS; ++k) t = is_max ? fmax(t, red[k]) : fmin(t, red[k]);
+    return t;
 }
 __device__ __forceinline__ bool ff_greater(float2 a, float2 b) { return a.x > b.x || (a.x == b.x && a.y > b.y); }
 
-// One warp per (simulation, criterion lead): lanes stride over the steps, sums combined by a fixed
-// butterfly.  Pearson, vector correlation and RMS accumulate in float-float (about 48 significant
-// bits) on the FP32 pipe, reading the float-float copies of the ECG and targets; the few closing
-// operations (means, square roots, quotients) are FP64.  devFromLinear stays FP64 throughout.
-// Writes the criterion value and the argmax (first maximum) of the lead.
-__global__ void k_criteria(int steps, int nleads, int ncl, int n_sims, int mode, const double *__restrict__ ecg,
-                           const float2 *__restrict__ ecg_ff, const double *__restrict__ targets,
-                           const float2 *__restrict__ targets_ff, const int64_t *__restrict__ tlen,
-                           const double *__restrict__ toff, int crit_stride, double *__restrict__ crit) {
-    const int lane = threadIdx.x & 31;
-    const int pair = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (pair >= ncl * n_sims) return;
-    const int i = pair % ncl, s = pair / ncl;
+// One block of NT threads per (simulation, criterion lead): threads stride over the steps, sums
+// combined in a fixed order (one warp per pair when there are many pairs, four for few).  Pearson, vector correlation and RMS accumulate in float-float (about
+// 48 significant bits) on the FP32 pipe, reading the float-float copies of the ECG and targets;
+// the few closing operations (means, square roots, quotients) are FP64.  devFromLinear stays FP64
+// throughout.  Writes the criterion value and the argmax (first maximum) of the lead.
+template <int NT>
+__global__ void __launch_bounds__(NT) k_criteria(int steps, int nleads, int i0, int i1, int n_sims, int mode,
+                                                         const double *__restrict__ ecg,
+                                                         const float2 *__restrict__ ecg_ff,
+                                                         const double *__restrict__ targets,
+                                                         const float2 *__restrict__ targets_ff,
+                                                         const int64_t *__restrict__ tlen,
+                                                         const double *__restrict__ toff, int crit_stride,
+                                                         double *__restrict__ crit) {
+    constexpr int CR_THREADS = NT, CR_WARPS = NT / 32;
+    __shared__ float2 redf[CR_WARPS];
+    __shared__ double redd[CR_WARPS];
+    __shared__ int redi[CR_WARPS];
+    const int tid = threadIdx.x;
+    const int ni = i1 - i0;  // criterion leads [i0, i1) of this launch
+    const int i = i0 + (int)(blockIdx.x % ni), s = (int)(blockIdx.x / ni);
     const size_t row = ((size_t)s * nleads + i) * steps;
     const float2 *af = ecg_ff + row;
     int64_t off = 0;
@@ -302,66 +339,68 @@ __global__ void k_criteria(int steps, int nleads, int ncl, int n_sims, int mode,
     double value = 0.0;
     if (mode == 2) {
         float2 sa = make_float2(0.f, 0.f), sb = sa;
-        for (int64_t j = lane; j < len; j += 32) {
+        for (int64_t j = tid; j < len; j += CR_THREADS) {
             sa = ff_add(sa, af[j]);
             sb = ff_add(sb, bf[j]);
         }
-        const float2 ma = ff_neg(ff_from_double(warp_sum_ff(sa) * inv));
-        const float2 mb = ff_neg(ff_from_double(warp_sum_ff(sb) * inv));
+        const float2 ma = ff_neg(ff_from_double(block_sum_ff<NT>(sa, redf) * inv));
+        const float2 mb = ff_neg(ff_from_double(block_sum_ff<NT>(sb, redf) * inv));
         float2 va = make_float2(0.f, 0.f), vb = va, cv = va;
-        for (int64_t j = lane; j < len; j += 32) {
+        for (int64_t j = tid; j < len; j += CR_THREADS) {
             const float2 x = ff_add(af[j], ma), y = ff_add(bf[j], mb);
             va = ff_add(va, ff_mul(x, x));
             vb = ff_add(vb, ff_mul(y, y));
             cv = ff_add(cv, ff_mul(x, y));
         }
-        const double dva = warp_sum_ff(va) * inv, dvb = warp_sum_ff(vb) * inv;
-        const double dcv = warp_sum_ff(cv) / (double)len;
+        const double dva = block_sum_ff<NT>(va, redf) * inv, dvb = block_sum_ff<NT>(vb, redf) * inv;
+        const double dcv = block_sum_ff<NT>(cv, redf) / (double)len;
         value = 1.0 - dcv / (sqrt(dva) * sqrt(dvb));
     } else if (mode == 4) {
         float2 ab = make_float2(0.f, 0.f), aa = ab, bb = ab;
-        for (int64_t j = lane; j < len; j += 32) {
+        for (int64_t j = tid; j < len; j += CR_THREADS) {
             const float2 x = af[j], y = bf[j];
             ab = ff_add(ab, ff_mul(x, y));
             aa = ff_add(aa, ff_mul(x, x));
             bb = ff_add(bb, ff_mul(y, y));
         }
-        const double dab = warp_sum_ff(ab), daa = warp_sum_ff(aa), dbb = warp_sum_ff(bb);
+        const double dab = block_sum_ff<NT>(ab, redf), daa = block_sum_ff<NT>(aa, redf), dbb = block_sum_ff<NT>(bb, redf);
         value = 1.0 - dab / (sqrt(daa) * sqrt(dbb));
     } else if (mode == 1) {
         float2 q = make_float2(0.f, 0.f);
-        for (int64_t j = lane; j < len; j += 32) {
+        for (int64_t j = tid; j < len; j += CR_THREADS) {
             const float2 x = ff_add(af[j], ff_neg(bf[j]));
             q = ff_add(q, ff_mul(x, x));
         }
-        value = sqrt(warp_sum_ff(q) / (double)len);
+        value = sqrt(block_sum_ff<NT>(q, redf) / (double)len);
     } else {
         // devFromLinear (vectorMath.h:373-404): min/max over the whole simulated lead
         const double *a = ecg + row;
         const double *b = targets + off;
         double mn = INFINITY, mx = -INFINITY;
-        for (int64_t j = lane; j < steps; j += 32) {
+        for (int64_t j = tid; j < steps; j += CR_THREADS) {
             mn = fmin(mn, a[j]);
             mx = fmax(mx, a[j]);
         }
-        const double amult = 1.0 / (warp_max(mx) - warp_min(mn));
+        const double amax = block_minmax<NT>(mx, true, redd);
+        const double amin = block_minmax<NT>(mn, false, redd);
+        const double amult = 1.0 / (amax - amin);
         const double bofs = toff[i];
         double sd = 0;
-        for (int64_t j = lane; j < len; j += 32) sd += (a[j] * amult + bofs) / (b[j] + bofs);
-        const double mean = warp_sum(sd) * inv;
+        for (int64_t j = tid; j < len; j += CR_THREADS) sd += (a[j] * amult + bofs) / (b[j] + bofs);
+        const double mean = block_sum<NT>(sd, redd) * inv;
         double var = 0;
-        for (int64_t j = lane; j < len; j += 32) {
+        for (int64_t j = tid; j < len; j += CR_THREADS) {
             const double d = (a[j] * amult + bofs) / (b[j] + bofs) - mean;
             var += d * d;
         }
-        var = warp_sum(var) * inv;
+        var = block_sum<NT>(var, redd) * inv;
         value = (var == 0) ? 1.0 / 1e-30 : sqrt(var);
     }
     // argmax of the simulated lead (first maximum), for the peak-position criterion; float-float
     // values are normalised, so comparing (hi, lo) in order compares the values
     float2 best = make_float2(-INFINITY, 0.f);
     int arg = 0x7fffffff;
-    for (int j = lane; j < steps; j += 32) {
+    for (int j = tid; j < steps; j += CR_THREADS) {
         const float2 v = af[j];
         if (ff_greater(v, best)) {
             best = v;
@@ -376,7 +415,18 @@ __global__ void k_criteria(int steps, int nleads, int ncl, int n_sims, int mode,
             arg = a2;
         }
     }
-    if (lane == 0) {
+    __syncthreads();
+    if ((tid & 31) == 0) {
+        redf[tid >> 5] = best;
+        redi[tid >> 5] = arg;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int k = 1; k < CR_WARPS; ++k)
+            if (ff_greater(redf[k], best) || (redf[k].x == best.x && redf[k].y == best.y && redi[k] < arg)) {
+                best = redf[k];
+                arg = redi[k];
+            }
         crit[((size_t)s * crit_stride + i) * 2 + 0] = value;
         crit[((size_t)s * crit_stride + i) * 2 + 1] = (double)arg;
     }
@@ -433,13 +483,17 @@ void launch_reduce_ecg(cudaStream_t s, const HeartDev &h, const double *d_partia
 }
 
 void launch_criteria(cudaStream_t s, const HeartDev &h, const double *d_ecg, const float2 *d_ecg_ff, int n_sims,
-                     int ncrit_stride, int n_crit_leads, int mode, const double *d_targets, const float2 *d_targets_ff,
+                     int ncrit_stride, int i0, int i1, int mode, const double *d_targets, const float2 *d_targets_ff,
                      const int64_t *d_tlen, const double *d_toff, double *d_crit) {
-    if (n_crit_leads <= 0) return;
-    // one warp per block, so the FP64 work of a few simulations spreads over as many SMs as it has warps
-    const int64_t pairs = (int64_t)n_crit_leads * n_sims;
-    k_criteria<<<(unsigned)pairs, 32, 0, s>>>(h.steps, h.nleads, n_crit_leads, n_sims, mode, d_ecg, d_ecg_ff,
-                                              d_targets, d_targets_ff, d_tlen, d_toff, ncrit_stride, d_crit);
+    if (i1 <= i0) return;
+    // one block per (simulation, lead): a warp when the pairs fill the GPU, four warps when few
+    const int64_t pairs = (int64_t)(i1 - i0) * n_sims;
+    if (pairs >= 1024)
+        k_criteria<32><<<(unsigned)pairs, 32, 0, s>>>(h.steps, h.nleads, i0, i1, n_sims, mode, d_ecg, d_ecg_ff,
+                                                      d_targets, d_targets_ff, d_tlen, d_toff, ncrit_stride, d_crit);
+    else
+        k_criteria<128><<<(unsigned)pairs, 128, 0, s>>>(h.steps, h.nleads, i0, i1, n_sims, mode, d_ecg, d_ecg_ff,
+                                                        d_targets, d_targets_ff, d_tlen, d_toff, ncrit_stride, d_crit);
     EKG_CUDA(cudaGetLastError());
 }
 

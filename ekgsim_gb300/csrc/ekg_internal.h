@@ -249,8 +249,9 @@ void launch_band_u(cudaStream_t s, const BandArgs &a);
 void launch_reduce_band(cudaStream_t s, const BandArgs &a);
 void launch_reduce_ecg(cudaStream_t s, const HeartDev &h, const double *d_partial, const double *d_k0w,
                        int n_sims, double *d_ecg, float2 *d_ecg_ff);
+// criteria of the criterion leads [i0, i1) of every simulation
 void launch_criteria(cudaStream_t s, const HeartDev &h, const double *d_ecg, const float2 *d_ecg_ff, int n_sims,
-                     int ncrit_stride, int n_crit_leads, int mode, const double *d_targets, const float2 *d_targets_ff,
+                     int ncrit_stride, int i0, int i1, int mode, const double *d_targets, const float2 *d_targets_ff,
                      const int64_t *d_tlen, const double *d_toff, double *d_crit);
 
 }  // namespace ekg

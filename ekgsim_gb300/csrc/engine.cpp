@@ -1036,17 +1036,18 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
                          P.batch ? h->bs.d_centre.p : nullptr, P.batch ? h->bs.d_scale.p : nullptr, P.J,
                          P.batch ? E.coef.p : nullptr);
     ++launches;
+    // batched form with both static and moved leads: the static combine (beside the moved-lead
+    // operand kernel) and the steady-sum reduction (beside the band GEMM) run on the auxiliary
+    // stream, joined before the band reduction (measured: other placements of the small kernels,
+    // such as the criteria of the static leads beside the GEMM, lengthen the pass)
+    const bool fork = P.batch && nmove > 0 && nmove < (int)L;
+    cudaStream_t sx = fork ? h->aux_stream : s;
+    if (fork) {
+        EKG_CUDA(cudaEventRecord(h->ev_fork, s));
+        EKG_CUDA(cudaStreamWaitEvent(sx, h->ev_fork, 0));
+    }
     if (P.batch) {
         BatchState &B = h->bs;
-        // with both static and moved leads, the static combine (beside the moved-lead operand kernel)
-        // and the steady-sum reduction (beside the band GEMM) run on the auxiliary stream, joined
-        // before the band reduction
-        const bool fork = nmove > 0 && nmove < (int)L;
-        cudaStream_t sx = fork ? h->aux_stream : s;
-        if (fork) {
-            EKG_CUDA(cudaEventRecord(h->ev_fork, s));
-            EKG_CUDA(cudaStreamWaitEvent(sx, h->ev_fork, 0));
-        }
         auto static_part = [&]() {
             launch_static_combine(sx, D, P.J, B.J, nmove, n_sims, E.Ff.p, E.coef.p, in.k3, B.Q1.p, B.Q2.p, E.ecg.p,
                                   E.ecg_ff.p);
@@ -1160,7 +1161,7 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
         launches += 2;
     }
     if (n_crit_leads > 0) {
-        launch_criteria(s, D, E.ecg.p, E.ecg_ff.p, n_sims, n_crit_leads, n_crit_leads, mode, E.targets.p,
+        launch_criteria(s, D, E.ecg.p, E.ecg_ff.p, n_sims, n_crit_leads, 0, n_crit_leads, mode, E.targets.p,
                         E.targets_ff.p, E.target_len.p, E.target_off.p, E.crit.p);
         ++launches;
     }
