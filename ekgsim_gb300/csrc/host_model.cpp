@@ -361,13 +361,27 @@ void load_targets(const SimConfig &c, const std::string &path, const std::string
 }
 
 // ------------------------------------------------------------------ Wohlfart AP and genes
-double wohlfart(const double *k, double t) {
-    return (1.0 / (1.0 + std::exp(-k[1] * t))) * (k[2] * ((1.0 - k[3]) * std::exp(-k[4] * t) + k[3])) *
-               (std::exp(-k[5] * t) *
-                (1 - std::pow((1 + std::exp(-k[7] * (t - k[8]) + std::log(std::pow(2, (k[7] / k[6])) - 1))),
-                              -(k[6] / k[7])))) +
-           k[0];
+// The formula as three factors, evaluated in the reference's operation order:
+//   value = A * B * C + k0,  A = 1 / (1 + e^{-k1 t}),  B = k2 ((1 - k3) e^{-k4 t} + k3),
+//   C = e^{-k5 t} R,  R = 1 - (1 + e^{-k7 (t - k8) + lc})^{ex},  lc = log(2^{k7/k6} - 1),  ex = -(k6/k7).
+// lc and ex depend on the coefficients only, so callers that evaluate one AP at many times compute
+// them once; a change of one coefficient re-evaluates only the factors it enters (same results).
+namespace {
+struct RepolConst {
+    double lc, ex;
+};
+inline RepolConst repol_const(const double *k) { return {std::log(std::pow(2, (k[7] / k[6])) - 1), -(k[6] / k[7])}; }
+inline double fac_a(const double *k, double t) { return 1.0 / (1.0 + std::exp(-k[1] * t)); }
+inline double fac_b(const double *k, double e4) { return k[2] * ((1.0 - k[3]) * e4 + k[3]); }
+inline double fac_r(const double *k, const RepolConst &rc, double t) {
+    return 1 - std::pow((1 + std::exp(-k[7] * (t - k[8]) + rc.lc)), rc.ex);
 }
+inline double wohlfart_rc(const double *k, const RepolConst &rc, double t) {
+    return fac_a(k, t) * fac_b(k, std::exp(-k[4] * t)) * (std::exp(-k[5] * t) * fac_r(k, rc, t)) + k[0];
+}
+}  // namespace
+
+double wohlfart(const double *k, double t) { return wohlfart_rc(k, repol_const(k), t); }
 
 int GeneModel::n_free() const { return __builtin_popcount(free_mask & 0x1ffu); }
 
@@ -380,7 +394,8 @@ struct AP {
 // WohlfartPlus::apd90 (simlib/Wohlfart.h:206-223)
 double apd90(const double *k) {
     double d[1000];
-    for (int i = 0; i < 1000; ++i) d[i] = wohlfart(k, (double)i);
+    const RepolConst rc = repol_const(k);
+    for (int i = 0; i < 1000; ++i) d[i] = wohlfart_rc(k, rc, (double)i);
     const double target = k[0] + k[2] * 0.1;
     double time = -1.0;
     for (int i = 1; i < 1000; ++i)
@@ -403,9 +418,10 @@ struct Evaluator {
         const size_t numPoints = 15, startX = 10;
         const double apd1 = apd90(a1.k), apd2 = apd90(a2.k);
         double y1[701], y2[701];
+        const RepolConst rc1 = repol_const(a1.k), rc2 = repol_const(a2.k);
         for (size_t i = 0; i < 700; ++i) {
-            y1[i] = a1((double)i);
-            y2[i] = a2((double)i);
+            y1[i] = wohlfart_rc(a1.k, rc1, (double)i - a1.at);
+            y2[i] = wohlfart_rc(a2.k, rc2, (double)i - a2.at);
         }
         y1[700] = y1[699];  // the reference reads one past its 700-sample buffer here; hold the last value
         y2[700] = y2[699];
@@ -434,6 +450,7 @@ struct Evaluator {
             lc.n = y2[std::min<size_t>(i2, 700)] - lc.k * (double)i2;
             conns.push_back(lc);
         }
+        static_assert(numPoints <= kMaxPts, "the fit's factor cache holds every point");
     }
     void set_ratio(double r) {
         pts.clear();
@@ -451,19 +468,58 @@ struct Evaluator {
         }
         return sum;
     }
+    // The same sum with the factors of every point kept (A, e^{-k4 t}, e^{-k5 t}, R), and the sum
+    // for `ap` that differs from the kept AP in coefficient i only, re-evaluating only the factors
+    // that coefficient enters.  Both give the doubles operator() gives.
+    static constexpr size_t kMaxPts = 16;  // set_border makes 15 points
+    struct Factors {
+        double a[kMaxPts], e4[kMaxPts], e5[kMaxPts], r[kMaxPts];
+    };
+    double full(const AP &ap, Factors &c) const {
+        const RepolConst rc = repol_const(ap.k);
+        double sum = 0;
+        for (size_t i = 0, p = 0; i < pts.size(); i += 2, ++p) {
+            const double t = pts[i] - ap.at;
+            c.a[p] = fac_a(ap.k, t);
+            c.e4[p] = std::exp(-ap.k[4] * t);
+            c.e5[p] = std::exp(-ap.k[5] * t);
+            c.r[p] = fac_r(ap.k, rc, t);
+            const double q = (c.a[p] * fac_b(ap.k, c.e4[p]) * (c.e5[p] * c.r[p]) + ap.k[0]) - pts[i + 1];
+            sum += q * q;
+        }
+        return sum;
+    }
+    double changed(const AP &ap, int i_changed, const Factors &c) const {
+        const bool ka = i_changed == 1, k4 = i_changed == 4, k5 = i_changed == 5;
+        const bool kr = i_changed == 6 || i_changed == 7 || i_changed == 8;
+        const RepolConst rc = kr ? repol_const(ap.k) : RepolConst{0, 0};
+        double sum = 0;
+        for (size_t i = 0, p = 0; i < pts.size(); i += 2, ++p) {
+            const double t = pts[i] - ap.at;
+            const double a = ka ? fac_a(ap.k, t) : c.a[p];
+            const double e4 = k4 ? std::exp(-ap.k[4] * t) : c.e4[p];
+            const double e5 = k5 ? std::exp(-ap.k[5] * t) : c.e5[p];
+            const double r = kr ? fac_r(ap.k, rc, t) : c.r[p];
+            const double q = (a * fac_b(ap.k, e4) * (e5 * r) + ap.k[0]) - pts[i + 1];
+            sum += q * q;
+        }
+        return sum;
+    }
 };
 // steepestDescend (nonlinearFit.h:92-168) over the 9 k values
+// (the probes of the gradient change one coefficient each, so they re-evaluate only its factors)
 void steepest(const Evaluator &f, AP &x0, const AP &d, double stepSize, double epsilon, int iterations) {
     AP grad = x0, oldGrad = x0, move = d;
     for (int i = 0; i < 9; ++i) oldGrad.k[i] = 0;
-    double y0 = f(x0);
+    Evaluator::Factors c0, c1;
+    double y0 = f.full(x0, c0);
     for (; iterations > 0 && y0 > epsilon; --iterations) {
         bool stepChange = false;
         for (int i = 0; i < 9; ++i) {
             AP x1 = x0;
             if (d.k[i] != 0) {
                 x1.k[i] += d.k[i] * .001;
-                grad.k[i] = (f(x1) - y0) / (d.k[i] * .001);
+                grad.k[i] = (f.changed(x1, i, c0) - y0) / (d.k[i] * .001);
                 if (grad.k[i] * oldGrad.k[i] < 0) {
                     move.k[i] *= 0.5;
                     stepChange = true;
@@ -477,10 +533,11 @@ void steepest(const Evaluator &f, AP &x0, const AP &d, double stepSize, double e
         oldGrad = grad;
         AP x1 = x0;
         for (int i = 0; i < 9; ++i) x1.k[i] -= stepSize * ((grad.k[i] > 0) ? move.k[i] : -move.k[i]);
-        const double y1 = f(x1);
+        const double y1 = f.full(x1, c1);
         if (y1 < y0) {
             y0 = y1;
             x0 = x1;
+            c0 = c1;
         } else if (!stepChange) {
             stepSize *= 0.5;
         }
