@@ -391,19 +391,22 @@ struct AP {
     double at = 0;
     double operator()(double t) const { return wohlfart(k, t - at); }
 };
-// WohlfartPlus::apd90 (simlib/Wohlfart.h:206-223)
+// WohlfartPlus::apd90 (simlib/Wohlfart.h:206-223): the last downward crossing of k0 + k2/10 among
+// the samples at 0 .. 999 ms, found by scanning from the end (the samples after it are the only
+// ones that decide that it is the last)
 double apd90(const double *k) {
-    double d[1000];
     const RepolConst rc = repol_const(k);
-    for (int i = 0; i < 1000; ++i) d[i] = wohlfart_rc(k, rc, (double)i);
     const double target = k[0] + k[2] * 0.1;
-    double time = -1.0;
-    for (int i = 1; i < 1000; ++i)
-        if (d[i - 1] > target && d[i] <= target) {
-            const double a = i - 1, wa = d[i - 1] - target, b = i, wb = target - d[i];
-            time = (a * wa + b * wb) / (wa + wb);
+    double next = wohlfart_rc(k, rc, 999.0);
+    for (int i = 999; i >= 1; --i) {
+        const double prev = wohlfart_rc(k, rc, (double)(i - 1));
+        if (prev > target && next <= target) {
+            const double a = i - 1, wa = prev - target, b = i, wb = target - next;
+            return (a * wa + b * wb) / (wa + wb);
         }
-    return time;
+        next = prev;
+    }
+    return -1.0;
 }
 // WohlfartInterpolationEvaluator (sim.cpp:91-313): connectors between two border APs, points
 // on them at a ratio, and the sum of squared distances of an AP from those points.
@@ -468,9 +471,10 @@ struct Evaluator {
         }
         return sum;
     }
-    // The same sum with the factors of every point kept (A, e^{-k4 t}, e^{-k5 t}, R), and the sum
-    // for `ap` that differs from the kept AP in coefficient i only, re-evaluating only the factors
-    // that coefficient enters.  Both give the doubles operator() gives.
+    // The same sum with the factors of every point kept (A, e^{-k4 t}, e^{-k5 t}, R): `full` computes
+    // them all, `from` re-evaluates only the factors whose coefficients differ from those of the AP
+    // `ref` the kept factors `c` belong to (and keeps the new ones in `out` when given).  Both give
+    // the doubles operator() gives.
     static constexpr size_t kMaxPts = 16;  // set_border makes 15 points
     struct Factors {
         double a[kMaxPts], e4[kMaxPts], e5[kMaxPts], r[kMaxPts];
@@ -489,9 +493,10 @@ struct Evaluator {
         }
         return sum;
     }
-    double changed(const AP &ap, int i_changed, const Factors &c) const {
-        const bool ka = i_changed == 1, k4 = i_changed == 4, k5 = i_changed == 5;
-        const bool kr = i_changed == 6 || i_changed == 7 || i_changed == 8;
+    double from(const AP &ap, const AP &ref, const Factors &c, Factors *out) const {
+        const bool ka = ap.k[1] != ref.k[1] || ap.at != ref.at, k4 = ap.k[4] != ref.k[4] || ap.at != ref.at;
+        const bool k5 = ap.k[5] != ref.k[5] || ap.at != ref.at;
+        const bool kr = ap.k[6] != ref.k[6] || ap.k[7] != ref.k[7] || ap.k[8] != ref.k[8] || ap.at != ref.at;
         const RepolConst rc = kr ? repol_const(ap.k) : RepolConst{0, 0};
         double sum = 0;
         for (size_t i = 0, p = 0; i < pts.size(); i += 2, ++p) {
@@ -500,6 +505,12 @@ struct Evaluator {
             const double e4 = k4 ? std::exp(-ap.k[4] * t) : c.e4[p];
             const double e5 = k5 ? std::exp(-ap.k[5] * t) : c.e5[p];
             const double r = kr ? fac_r(ap.k, rc, t) : c.r[p];
+            if (out) {
+                out->a[p] = a;
+                out->e4[p] = e4;
+                out->e5[p] = e5;
+                out->r[p] = r;
+            }
             const double q = (a * fac_b(ap.k, e4) * (e5 * r) + ap.k[0]) - pts[i + 1];
             sum += q * q;
         }
@@ -507,7 +518,8 @@ struct Evaluator {
     }
 };
 // steepestDescend (nonlinearFit.h:92-168) over the 9 k values
-// (the probes of the gradient change one coefficient each, so they re-evaluate only its factors)
+// (the gradient probes and the step change some coefficients only, so they re-evaluate only the
+// factors those enter)
 void steepest(const Evaluator &f, AP &x0, const AP &d, double stepSize, double epsilon, int iterations) {
     AP grad = x0, oldGrad = x0, move = d;
     for (int i = 0; i < 9; ++i) oldGrad.k[i] = 0;
@@ -519,7 +531,7 @@ void steepest(const Evaluator &f, AP &x0, const AP &d, double stepSize, double e
             AP x1 = x0;
             if (d.k[i] != 0) {
                 x1.k[i] += d.k[i] * .001;
-                grad.k[i] = (f.changed(x1, i, c0) - y0) / (d.k[i] * .001);
+                grad.k[i] = (f.from(x1, x0, c0, nullptr) - y0) / (d.k[i] * .001);
                 if (grad.k[i] * oldGrad.k[i] < 0) {
                     move.k[i] *= 0.5;
                     stepChange = true;
@@ -533,7 +545,7 @@ void steepest(const Evaluator &f, AP &x0, const AP &d, double stepSize, double e
         oldGrad = grad;
         AP x1 = x0;
         for (int i = 0; i < 9; ++i) x1.k[i] -= stepSize * ((grad.k[i] > 0) ? move.k[i] : -move.k[i]);
-        const double y1 = f.full(x1, c1);
+        const double y1 = f.from(x1, x0, c0, &c1);
         if (y1 < y0) {
             y0 = y1;
             x0 = x1;
