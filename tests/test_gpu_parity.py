@@ -410,3 +410,29 @@ def test_graph_replay_is_bit_identical():
     for a, b in zip(out["1"], out["0"]):
         for x, y in zip(a, b):
             assert np.array_equal(np.asarray(x), np.asarray(y))
+
+
+@pytest.mark.parametrize("mode", [1, 2, 3, 4])
+def test_criteria_modes_match_fp64_compare(engine, mode):
+    """Every comparison mode (1 RMS, 2 Pearson, 3 devFromLinear, 4 vector correlation) gives the
+    FP64 comparison of the engine's own ECG with the target (the oracle's compare, vectorMath.h),
+    for a batch of 256 (one warp per simulation and lead) and a single evaluation (four warps);
+    the target is shorter than the simulation, so the compared length is the target's."""
+    from ekgsim_gb300.engine import Heart
+    spec = synth.small_spec(40, n_leads=4, seed=5)
+    steps = 300
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    h = Heart.create(engine, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+    target = synth.analytic_target(spec.n_leads, steps - 20, 9)
+    offs = [0.5, 1.0, 0.25, 2.0]
+    h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], [t for t in target],
+               target_offsets=offs, mid_position=0.6, comparison_mode=mode)
+    genes = np.stack([synth.genes_for(spec, r, 0) for r in range(256)])
+    crit_b, _, ecg_b = h.eval_batch(genes, want_ecg=True)
+    crit_1, _, ecg_1, _, _ = h.eval(genes[3], want_ecg=True)
+    for crit, ecg in [(crit_b[0], ecg_b[0]), (crit_b[100], ecg_b[100]), (crit_b[255], ecg_b[255]), (crit_1, ecg_1)]:
+        for l in range(spec.n_leads):
+            ref = O.clamp(O.compare(mode, ecg[l], target[l], offs[l]))
+            assert crit[l] == pytest.approx(ref, rel=1e-9, abs=1e-12), (mode, l)
