@@ -137,12 +137,16 @@ class Heart:
     def set_eval(self, base_aps, k_min, k_max, free_k, targets, target_offsets=None, **kw):
         """Evaluation settings (ekg_heart_set_eval); keyword arguments as ``eval_config``."""
         self._cfg = eval_config(base_aps, k_min, k_max, free_k, targets, target_offsets, **kw)
+        self._eval_shape = None
         check(self._lib.ekg_heart_set_eval(self._h, ctypes.byref(self._cfg)))
 
     def eval_shape(self):
-        g, c = ctypes.c_int32(), ctypes.c_int32()
-        check(self._lib.ekg_eval_shape(self._h, ctypes.byref(g), ctypes.byref(c)))
-        return g.value, c.value
+        """(genes, criteria) per evaluation; kept until the evaluation settings change."""
+        if getattr(self, "_eval_shape", None) is None:
+            g, c = ctypes.c_int32(), ctypes.c_int32()
+            check(self._lib.ekg_eval_shape(self._h, ctypes.byref(g), ctypes.byref(c)))
+            self._eval_shape = (g.value, c.value)
+        return self._eval_shape
 
     def gene_bounds(self):
         g, _ = self.eval_shape()
@@ -181,7 +185,8 @@ class Heart:
             bufs = [np.empty(sh) for sh in shapes]
         crit, viol = bufs[0], bufs[1]
         ecg = bufs[2] if want_ecg else None
-        check(self._lib.ekg_eval_batch(self._h, n, dptr(genes), g, dptr(crit), dptr(viol), dptr(ecg)))
+        check(self._lib.ekg_eval_batch(self._h, n, genes.ctypes.data, g, crit.ctypes.data, viol.ctypes.data,
+                                       ecg.ctypes.data if ecg is not None else None))
         return (crit, viol, ecg) if want_ecg else (crit, viol)
 
     def close(self):
