@@ -79,6 +79,7 @@ struct ekg_heart {
     cudaStream_t stream = nullptr;    // this heart's device passes run here
     cudaStream_t copy_stream = nullptr;  // early device->host copies overlapping the rest of a pass
     cudaEvent_t static_done = nullptr;   // static-lead ECG rows complete (batched form)
+    cudaEvent_t moved_done = nullptr;    // moved-lead ECG rows complete (batched form)
     // the batched form's static-lead combine and steady-sum reduction run on a second stream beside
     // the moved-lead operand kernel and GEMM (fork and join by events; captured into the graphs)
     cudaStream_t aux_stream = nullptr;
@@ -110,6 +111,7 @@ struct ekg_heart {
             if (g.exec) cudaGraphExecDestroy(g.exec);
         if (stage_host) cudaFreeHost(stage_host);
         if (static_done) cudaEventDestroy(static_done);
+        if (moved_done) cudaEventDestroy(moved_done);
         for (cudaEvent_t e : {ev_fork, ev_op, ev_join})
             if (e) cudaEventDestroy(e);
         if (aux_stream) cudaStreamDestroy(aux_stream);

@@ -1131,6 +1131,14 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             if (fork) EKG_CUDA(cudaStreamWaitEvent(s, h->ev_join, 0));
             launch_reduce_band(s, U);
             ++launches;
+            if (mark_static) {
+                // the moved-lead rows are final too: their copy to the host overlaps the criteria
+                cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+                EKG_CUDA(cudaStreamIsCapturing(s, &cs));
+                EKG_CUDA(cudaEventRecordWithFlags(h->moved_done, s,
+                                                  cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal
+                                                                                      : cudaEventRecordDefault));
+            }
         } else if (tm && tm->on) {
             EKG_CUDA(cudaEventRecord(tm->ev[1], s));
             EKG_CUDA(cudaEventRecord(tm->ev[2], s));
@@ -1260,6 +1268,7 @@ void device_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *
     if (split && !h->copy_stream) {
         EKG_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
         EKG_CUDA(cudaEventCreateWithFlags(&h->static_done, cudaEventDisableTiming));
+        EKG_CUDA(cudaEventCreateWithFlags(&h->moved_done, cudaEventDisableTiming));
     }
     run_pass(h, P, crit_host ? n_crit_leads : 0, mode, split);
     if (split) {
@@ -1272,9 +1281,11 @@ void device_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *
     if (crit_host && n_crit_leads > 0)
         EKG_CUDA(cudaMemcpyAsync(crit_host, E.crit.p, S * n_crit_leads * 2 * 8, cudaMemcpyDeviceToHost, s));
     if (split) {
-        if (P.nmove > 0)
+        if (P.nmove > 0) {
+            EKG_CUDA(cudaStreamWaitEvent(h->copy_stream, h->moved_done, 0));
             EKG_CUDA(cudaMemcpy2DAsync(ecg_host, L * T * 8, E.ecg.p, L * T * 8, (size_t)P.nmove * T * 8, S,
-                                       cudaMemcpyDeviceToHost, s));
+                                       cudaMemcpyDeviceToHost, h->copy_stream));
+        }
     } else if (ecg_host) {
         EKG_CUDA(cudaMemcpyAsync(ecg_host, E.ecg.p, S * L * T * 8, cudaMemcpyDeviceToHost, s));
     }
