@@ -27,7 +27,7 @@ NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler"
            "-Xcompiler", "-ffp-contract=off",
            "-diag-suppress", "177,550", "-I", os.path.join(ROOT, "include")]
 
-SOURCES = ["ca.cu", "ecg.cu", "umma.cu", "batch.cu", "engine.cpp", "host_model.cpp", "server.cpp"]
+SOURCES = ["ca.cu", "ecg.cu", "umma.cu", "batch.cu", "setup.cu", "engine.cpp", "host_model.cpp", "server.cpp"]
 PROGRAMS = {"ekgSim": ["cli_main.cpp"], "ekgsim_extern": ["extern_main.cpp"]}
 
 

@@ -128,11 +128,11 @@ struct ekg_heart {
     std::vector<double> t;            // time axis
     std::vector<double> leads0;       // loaded lead positions (z,y,x)
     std::vector<double> lead_uv;      // their displacement frames [n][u, v]
-    std::vector<double> at_host;      // activation time per cell
+    std::vector<double> at_host;      // activation time per cell (copied from the device on first use)
     std::vector<uint8_t> layer_host;  // layer id per cell (stimulus flag stripped)
     std::vector<int64_t> ap_index_ref;    // reference AP numbering per cell (built on demand)
-    std::vector<int64_t> vox_cell;        // cell of each voxel, voxels in AP order
-    std::vector<int64_t> vox_group_start; // [naps + 1] first voxel of each AP
+    std::vector<int32_t> vox_cell;        // cell of each voxel, voxels in AP order
+    std::vector<int32_t> vox_group_start; // [naps + 1] first voxel of each AP
     ekg::HeartDev dev;
     ekg::EvalDev ev;
     ekg::DBuf<double> at_cells;       // device activation times per cell

@@ -87,6 +87,20 @@ struct DBuf {
     DBuf(const DBuf &) = delete;
     DBuf &operator=(const DBuf &) = delete;
     ~DBuf() { release(); }
+    DBuf(DBuf &&o) noexcept : p(o.p), n(o.n) {
+        o.p = nullptr;
+        o.n = 0;
+    }
+    DBuf &operator=(DBuf &&o) noexcept {
+        if (this != &o) {
+            release();
+            p = o.p;
+            n = o.n;
+            o.p = nullptr;
+            o.n = 0;
+        }
+        return *this;
+    }
     void release() {
         if (p) cudaFree(p);
         p = nullptr;
@@ -153,6 +167,28 @@ struct HeartDev {
     DBuf<double> t;         // [steps]
     DBuf<float2> t_hilo;    // [steps]
 };
+
+// De-duplication of a heart's voxels into APs on the device (setup.cu): the voxels sorted by
+// (layer, activation time, cell), the first voxel of every AP, and per present layer (in order)
+// its first AP, AP count and base in the padded (multiple of 64) per-layer K layout.
+struct DedupResult {
+    int64_t nvox = 0, naps = 0, apad = 0;
+    std::vector<int> pl_layer, pfirst, pcount;  // per present layer: id (1-based), first AP, APs
+    std::vector<int64_t> pbase;                  // per present layer: first padded AP slot
+    DBuf<int> cell;                              // [nvox] cell of each sorted voxel
+    DBuf<int> gstart;                            // [naps (+1)] first sorted voxel of each AP
+    DBuf<uint64_t> key;                          // [nvox] activation-time bits of each sorted voxel
+    DBuf<uint8_t> vl;                            // [nvox] layer of each sorted voxel
+};
+void setup_voxels_device(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_lay, const double *d_at_cells,
+                         int nl, DedupResult &r);
+// at / at_hilo / a_layer [apad], a_vb [apad + 1]
+void setup_ap_arrays_device(cudaStream_t s, const DedupResult &r, const double *d_at_cells, double *at,
+                            float2 *at_hilo, int32_t *a_layer, int64_t *a_vb);
+// per-voxel records of the dipole kernels; returns the number of voxels flagged interior
+int64_t setup_voxel_records_device(cudaStream_t s, const DedupResult &r, int nz, int ny, int nx, const uint8_t *d_lay,
+                                   const HeartDev &D, int few_max, int32_t *vzyx, uint32_t *vin, uint32_t *vout,
+                                   float4 *vpos, float4 *vosum);
 
 // Per-evaluation scratch (sized for n_sims simulations).
 struct EvalDev {

@@ -263,20 +263,43 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
         }
     }
 
-    // layers, stimulus, validation
+    // layers, stimulus, validation: in parts on the host pool (per part its largest layer, present
+    // layers, first out-of-range cell and stimulus cells in order)
     std::vector<uint8_t> lay(n), st(n);
+    const size_t vparts = (size_t)std::min<int64_t>(64, std::max<int64_t>(1, n / 65536));
+    struct Part {
+        int nl = 0;
+        int64_t bad = -1;
+        std::vector<int64_t> starts;
+        char present[256] = {0};
+    };
+    std::vector<Part> parts(vparts);
+    HostPool::get().run(vparts, [&](size_t pb, size_t pe) {
+        for (size_t q = pb; q < pe; ++q) {
+            Part &P = parts[q];
+            for (int64_t i = n * (int64_t)q / (int64_t)vparts; i < n * (int64_t)(q + 1) / (int64_t)vparts; ++i) {
+                const int32_t v = d->layers[i];
+                const int32_t a = v < 0 ? -v : v;
+                if (a > 254) {
+                    if (P.bad < 0) P.bad = i;
+                    continue;
+                }
+                lay[i] = (uint8_t)a;
+                st[i] = v < 0;
+                if (v < 0) P.starts.push_back(i);
+                P.nl = std::max(P.nl, a);
+                P.present[a] = 1;
+            }
+        }
+    });
     int nl = 0;
     int64_t nstart = 0;
     std::vector<char> present(256, 0);
-    for (int64_t i = 0; i < n; ++i) {
-        int32_t v = d->layers[i];
-        int32_t a = v < 0 ? -v : v;
-        EKG_CHECK(a <= 254, EKG_ERR_BAD_INPUT, "layer ids must be at most 254");
-        lay[i] = (uint8_t)a;
-        st[i] = v < 0;
-        nstart += v < 0;
-        nl = std::max(nl, a);
-        present[a] = 1;
+    for (const Part &P : parts) {
+        EKG_CHECK(P.bad < 0, EKG_ERR_BAD_INPUT, "layer ids must be at most 254");
+        nl = std::max(nl, P.nl);
+        nstart += (int64_t)P.starts.size();
+        for (int a = 0; a < 256; ++a) present[a] = present[a] || P.present[a];
     }
     EKG_CHECK(nstart > 0, EKG_ERR_NO_START, "Could not find starting point for excitation sequence");
     EKG_CHECK(nl >= 1, EKG_ERR_BAD_INPUT, "model has no non-empty voxel");
@@ -305,8 +328,8 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     {
         const int ntx = (d->nx + 7) / 8, nty = (d->ny + 7) / 8;
         std::vector<char> seen((size_t)ntx * nty * ((d->nz + 7) / 8), 0);
-        for (int64_t i = 0; i < n; ++i)
-            if (st[i]) {
+        for (const Part &P : parts)
+            for (const int64_t i : P.starts) {
                 const int64_t z = i / ((int64_t)d->ny * d->nx), y = (i / d->nx) % d->ny, x = i % d->nx;
                 const int64_t tile = ((z / 8) * nty + (y / 8)) * ntx + (x / 8);
                 if (!seen[tile]) {
@@ -329,176 +352,52 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     EKG_CUDA(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->eng->device));
     h->ev.err.alloc(1);
     cudaStream_t s = h->stream;
+    // activation times (the layer grid stays on the device for the de-duplication)
+    DBuf<uint8_t> dl;
+    dl.alloc(n);
+    EKG_CUDA(cudaMemcpyAsync(dl.p, lay.data(), n, cudaMemcpyHostToDevice, s));
     {
-        DBuf<uint8_t> dl, ds;
+        DBuf<uint8_t> ds;
         DBuf<double> dlag;
-        dl.alloc(n);
         ds.alloc(n);
         dlag.alloc(lag.size());
         h->at_cells.alloc(n);
-        EKG_CUDA(cudaMemcpyAsync(dl.p, lay.data(), n, cudaMemcpyHostToDevice, s));
         EKG_CUDA(cudaMemcpyAsync(ds.p, st.data(), n, cudaMemcpyHostToDevice, s));
         EKG_CUDA(cudaMemcpyAsync(dlag.p, lag.data(), lag.size() * 8, cudaMemcpyHostToDevice, s));
         CaResult r = ca_run(s, d->nz, d->ny, d->nx, dl.p, ds.p, start_tiles, nl1, dlag.p, h->at_cells.p, nullptr);
         h->ca_rounds = r.rounds;
         h->ca_ms = r.ms;
-        h->at_host.resize(n);
-        EKG_CUDA(cudaMemcpyAsync(h->at_host.data(), h->at_cells.p, n * 8, cudaMemcpyDeviceToHost, s));
         EKG_CUDA(cudaStreamSynchronize(s));
     }
+    h->at_host.clear();  // copied to the host on first use (ensure_at_host)
 
-    // de-duplicate (layer, at) pairs: voxels sorted by (layer, at, cell index) -- as 16-byte keys
-    // (layer, at bits (non-negative doubles order as their bit patterns), cell) sorted on the host
-    // pool -- then equal (layer, at) runs are the APs.  The reference numbers APs by first
-    // appearance in raster order (simlib/simulator.cpp:570-590); that numbering is derived on demand.
-    struct VKey {
-        uint64_t hi, lo;  // (layer << 56 | cell), at bits  -- compared as (layer, at, cell)
-        bool operator<(const VKey &o) const {
-            const uint64_t la = hi >> 56, lb = o.hi >> 56;
-            if (la != lb) return la < lb;
-            if (lo != o.lo) return lo < o.lo;
-            return hi < o.hi;
-        }
-    };
-    EKG_CHECK(n < ((int64_t)1 << 56), EKG_ERR_BAD_INPUT, "grid too large");
-    std::vector<VKey> keys;
-    keys.reserve(n / 4);
-    for (int64_t i = 0; i < n; ++i)
-        if (lay[i]) {
-            uint64_t b;
-            std::memcpy(&b, &h->at_host[i], 8);
-            keys.push_back(VKey{((uint64_t)lay[i] << 56) | (uint64_t)i, b});
-        }
-    parallel_sort(keys);
-    const int64_t nv = (int64_t)keys.size();
+    // de-duplicate (layer, at) pairs on the device (setup.cu): voxels sorted by (layer, at bits,
+    // cell), equal (layer, at) runs are the APs.  The reference numbers APs by first appearance in
+    // raster order (simlib/simulator.cpp:570-590); that numbering is derived on demand.
+    EKG_CHECK(n < ((int64_t)1 << 31), EKG_ERR_BAD_INPUT, "grid too large");
+    DedupResult dd;
+    setup_voxels_device(s, d->nz, d->ny, d->nx, dl.p, h->at_cells.p, nl, dd);
+    const int64_t nv = dd.nvox, na = dd.naps, apad = dd.apad;
     h->nvox = nv;
     D.nvox = nv;
-    std::vector<int64_t> ord(nv);
-    for (int64_t i = 0; i < nv; ++i) ord[i] = (int64_t)(keys[i].hi & (((uint64_t)1 << 56) - 1));
-    // groups (APs): runs of equal (layer, at); the last voxel of each is flagged for the operand kernel
-    std::vector<int64_t> gstart;  // index into ord
-    std::vector<uint8_t> gend(nv, 0);
-    for (int64_t i = 0; i < nv; ++i) {
-        if (i == 0 || (keys[i].hi >> 56) != (keys[i - 1].hi >> 56) || keys[i].lo != keys[i - 1].lo) {
-            gstart.push_back(i);
-            if (i > 0) gend[i - 1] = 1;
-        }
-    }
-    if (nv > 0) gend[nv - 1] = 1;
-    std::vector<VKey>().swap(keys);
-    const int64_t na = (int64_t)gstart.size();
     h->naps = na;
     D.naps = na;
-    gstart.push_back(nv);
-    h->vox_cell = ord;
-    h->vox_group_start = gstart;
-    h->ap_index_ref.clear();
-    // padded per-layer K layout, tiles of KT APs, chunks of up to chunk_len APs inside one layer
-    const int KT = 64;
-    const int chunk_len = h->eng->chunk_len;
-    std::vector<double> a_at;
-    std::vector<float2> a_hilo;
-    std::vector<int32_t> a_layer;
-    std::vector<int64_t> a_vb;
-    std::vector<int32_t> c0, c1, cl;
+    EKG_CHECK(apad < (int64_t)1 << 31, EKG_ERR_BAD_INPUT, "too many distinct activation times");
+    D.apad = apad;
     D.centre[0] = 0.5 * d->nz;
     D.centre[1] = 0.5 * d->ny;
     D.centre[2] = 0.5 * d->nx;
-    {
-        int64_t g = 0;
-        for (int L = 1; L <= nl; ++L) {
-            const int64_t gb = g;
-            while (g < na && lay[ord[gstart[g]]] == L) ++g;
-            const int64_t cnt = g - gb;
-            if (cnt == 0) continue;
-            const int64_t base = (int64_t)a_at.size();
-            const int64_t padded = (cnt + KT - 1) / KT * KT;
-            for (int64_t j = 0; j < padded; ++j) {
-                a_layer.push_back(L - 1);
-                a_vb.push_back(j < cnt ? gstart[gb + j] : gstart[g]);
-                if (j < cnt) {
-                    const double at = h->at_host[ord[gstart[gb + j]]];
-                    a_at.push_back(at);
-                    const float hi = (float)at;
-                    a_hilo.push_back(make_float2(hi, (float)(at - (double)hi)));
-                } else {
-                    a_at.push_back(INFINITY);
-                    a_hilo.push_back(make_float2(INFINITY, 0.f));
-                }
-            }
-            for (int64_t j = 0; j < padded; j += chunk_len) {
-                c0.push_back((int32_t)(base + j));
-                c1.push_back((int32_t)(base + std::min<int64_t>(padded, j + chunk_len)));
-                cl.push_back(L - 1);
-            }
+    // chunks of up to chunk_len APs inside one layer's padded range
+    const int chunk_len = h->eng->chunk_len;
+    std::vector<int32_t> c0, c1, cl;
+    for (size_t k = 0; k < dd.pl_layer.size(); ++k) {
+        const int64_t base = dd.pbase[k], padded = (dd.pcount[k] + 63) / 64 * 64;
+        for (int64_t j = 0; j < padded; j += chunk_len) {
+            c0.push_back((int32_t)(base + j));
+            c1.push_back((int32_t)(base + std::min<int64_t>(padded, j + chunk_len)));
+            cl.push_back(dd.pl_layer[k] - 1);
         }
-        a_vb.push_back(nv);
     }
-    // per voxel (in AP order): packed position, neighbour masks, bordered position relative to the
-    // centre with the mask and flags, out-offset sum -- independent per voxel, on the host pool
-    std::vector<int32_t> vzyx(nv);
-    std::vector<uint32_t> vin(nv), vout(nv);
-    std::vector<float4> vpos_v(nv), vosum(nv);
-    std::vector<int64_t> interior_parts(64, 0);
-    // absent neighbours up to which the closed form minus their terms is cheaper than the sum over
-    // the present ones (the 8 body diagonals have a cheaper direct sum)
-    const int few_max = D.nhood == EKG_NHOOD_3D4 ? 2 : D.nnb / 2;
-    const size_t vparts = (size_t)std::min<int64_t>(64, std::max<int64_t>(1, nv / 4096));
-    HostPool::get().run(vparts, [&](size_t pb, size_t pe) {
-        for (size_t part = pb; part < pe; ++part) {
-            int64_t cnt_int = 0;
-            for (int64_t i = nv * (int64_t)part / (int64_t)vparts; i < nv * (int64_t)(part + 1) / (int64_t)vparts; ++i) {
-                const int64_t c = ord[i];
-                const int z = (int)(c / ((int64_t)d->ny * d->nx)), y = (int)((c / d->nx) % d->ny), x = (int)(c % d->nx);
-                vzyx[i] = (z << 20) | (y << 10) | x;
-                uint32_t mi = 0, mo = 0;
-                for (int q = 0; q < D.nnb; ++q) {
-                    const int dz = D.nb_dif[3 * q], dy = D.nb_dif[3 * q + 1], dx = D.nb_dif[3 * q + 2];
-                    int z2 = z + dz, y2 = y + dy, x2 = x + dx;
-                    if (z2 >= 0 && z2 < d->nz && y2 >= 0 && y2 < d->ny && x2 >= 0 && x2 < d->nx &&
-                        lay[((int64_t)z2 * d->ny + y2) * d->nx + x2])
-                        mi |= 1u << q;
-                    z2 = z - dz;
-                    y2 = y - dy;
-                    x2 = x - dx;
-                    if (z2 >= 0 && z2 < d->nz && y2 >= 0 && y2 < d->ny && x2 >= 0 && x2 < d->nx &&
-                        lay[((int64_t)z2 * d->ny + y2) * d->nx + x2])
-                        mo |= 1u << q;
-                }
-                vin[i] = mi;
-                vout[i] = mo;
-                float oz = 0, oy = 0, ox = 0;
-                for (int q = 0; q < D.nnb; ++q)
-                    if (mo & (1u << q)) {
-                        oz += D.nb_dif[3 * q];
-                        oy += D.nb_dif[3 * q + 1];
-                        ox += D.nb_dif[3 * q + 2];
-                    }
-                uint32_t mbits = mi;
-                // flags for the moved-lead operand kernel (batch.cu): interior voxel (closed-form field),
-                // boundary voxel with few absent neighbours, last voxel of its AP
-                if (D.interior_mask && mi == D.interior_mask && oz == 0 && oy == 0 && ox == 0) {
-                    mbits |= 1u << 31;
-                    ++cnt_int;
-                } else if (D.interior_mask && __builtin_popcount(D.interior_mask & ~mi) <= few_max) {
-                    mbits |= 1u << 29;  // few absent neighbours: closed form minus their terms
-                }
-                if (gend[i]) mbits |= 1u << 30;
-                float mf;
-                std::memcpy(&mf, &mbits, 4);
-                // bordered coordinates (+1, simlib/simulator.cpp:458-463) relative to the centre
-                vpos_v[i] = make_float4((float)((z + 1) - D.centre[0]), (float)((y + 1) - D.centre[1]),
-                                        (float)((x + 1) - D.centre[2]), mf);
-                vosum[i] = make_float4(oz, oy, ox, mo ? 1.f : 0.f);
-            }
-            interior_parts[part] = cnt_int;
-        }
-    });
-    D.n_interior = 0;
-    for (int64_t c : interior_parts) D.n_interior += c;
-    const int64_t apad = (int64_t)a_at.size();
-    EKG_CHECK(apad < (int64_t)1 << 31, EKG_ERR_BAD_INPUT, "too many distinct activation times");
-    D.apad = apad;
     D.nchunks = (int)c0.size();
     D.at.alloc(apad);
     D.at_hilo.alloc(apad);
@@ -515,26 +414,31 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     D.difs.alloc(3 * D.nnb);
     D.t.alloc(steps);
     D.t_hilo.alloc(steps);
+    setup_ap_arrays_device(s, dd, h->at_cells.p, D.at.p, D.at_hilo.p, D.a_layer.p, D.a_vox_begin.p);
+    // absent neighbours up to which the closed form minus their terms is cheaper than the sum over
+    // the present ones (the 8 body diagonals have a cheaper direct sum)
+    const int few_max = D.nhood == EKG_NHOOD_3D4 ? 2 : D.nnb / 2;
+    D.n_interior = setup_voxel_records_device(s, dd, d->nz, d->ny, d->nx, dl.p, D, few_max, D.vox_zyx.p, D.vox_nb.p,
+                                              D.vox_nbo.p, D.vox_pos.p, D.vox_out.p);
+    // host copies of the sorted voxel cells and AP starts, for the reference's AP numbering
+    h->vox_cell.resize(nv);
+    h->vox_group_start.resize(na + 1);
+    EKG_CUDA(cudaMemcpyAsync(h->vox_cell.data(), dd.cell.p, nv * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    EKG_CUDA(cudaMemcpyAsync(h->vox_group_start.data(), dd.gstart.p, na * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    h->ap_index_ref.clear();
     std::vector<float2> th(steps);
     for (int64_t i = 0; i < steps; ++i) {
         const float hi = (float)h->t[i];
         th[i] = make_float2(hi, (float)(h->t[i] - (double)hi));
     }
-    EKG_CUDA(cudaMemcpyAsync(D.at.p, a_at.data(), apad * 8, cudaMemcpyHostToDevice, s));
-    EKG_CUDA(cudaMemcpyAsync(D.at_hilo.p, a_hilo.data(), apad * 8, cudaMemcpyHostToDevice, s));
-    EKG_CUDA(cudaMemcpyAsync(D.a_layer.p, a_layer.data(), apad * 4, cudaMemcpyHostToDevice, s));
-    EKG_CUDA(cudaMemcpyAsync(D.a_vox_begin.p, a_vb.data(), (apad + 1) * 8, cudaMemcpyHostToDevice, s));
-    EKG_CUDA(cudaMemcpyAsync(D.vox_zyx.p, vzyx.data(), nv * 4, cudaMemcpyHostToDevice, s));
-    EKG_CUDA(cudaMemcpyAsync(D.vox_nb.p, vin.data(), nv * 4, cudaMemcpyHostToDevice, s));
-    EKG_CUDA(cudaMemcpyAsync(D.vox_nbo.p, vout.data(), nv * 4, cudaMemcpyHostToDevice, s));
-    EKG_CUDA(cudaMemcpyAsync(D.vox_pos.p, vpos_v.data(), nv * 16, cudaMemcpyHostToDevice, s));
-    EKG_CUDA(cudaMemcpyAsync(D.vox_out.p, vosum.data(), nv * 16, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.chunk_a0.p, c0.data(), c0.size() * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.chunk_a1.p, c1.data(), c0.size() * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.chunk_layer.p, cl.data(), c0.size() * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.difs.p, D.nb_dif, 3 * D.nnb, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.t.p, h->t.data(), steps * 8, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.t_hilo.p, th.data(), steps * 8, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaStreamSynchronize(s));
+    h->vox_group_start[na] = (int32_t)nv;
     // resident lead field for the loaded lead positions
     h->leads0_dev.alloc(3 * D.nleads);
     EKG_CUDA(cudaMemcpyAsync(h->leads0_dev.p, h->leads0.data(), h->leads0.size() * 8, cudaMemcpyHostToDevice, s));
@@ -1681,9 +1585,20 @@ int ekg_heart_time_axis(ekg_heart *h, double *start, double *length, double *dt)
     });
 }
 
+// the activation times per cell on the host, copied from the device when first asked for
+void ensure_at_host(ekg_heart *h) {
+    if ((int64_t)h->at_host.size() == h->ncell) return;
+    h->at_host.resize(h->ncell);
+    EKG_CUDA(cudaSetDevice(h->eng->device));
+    EKG_CUDA(cudaMemcpyAsync(h->at_host.data(), h->at_cells.p, h->ncell * 8, cudaMemcpyDeviceToHost, h->stream));
+    EKG_CUDA(cudaStreamSynchronize(h->stream));
+}
+
 int ekg_heart_activation(ekg_heart *h, double *at_out) {
     return guard([&] {
         EKG_CHECK(h && at_out, EKG_ERR_BAD_INPUT, "null argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        ensure_at_host(h);
         std::copy(h->at_host.begin(), h->at_host.end(), at_out);
     });
 }
@@ -1811,6 +1726,7 @@ int ekg_heart_cell_ap(ekg_heart *h, int64_t index, int32_t *layer_out, double *a
         EKG_CHECK(h && layer_out && at_out, EKG_ERR_BAD_INPUT, "null argument");
         std::lock_guard<std::mutex> lk(h->mu);
         ensure_ap_ref(h);
+        ensure_at_host(h);
         for (int64_t i = 0; i < h->ncell; ++i)
             if (h->ap_index_ref[i] == index) {
                 *layer_out = h->layer_host[i];
