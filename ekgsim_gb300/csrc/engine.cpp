@@ -936,20 +936,21 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
     if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[0], s));
     EKG_CUDA(cudaMemsetAsync(E.err.p, 0, sizeof(uint32_t), s));
     const ekg_heart::PassInputs &in = h->in;
-    launch_layer_factors(s, D, in.layer_k, in.cpre, n_sims, E.F.p, E.Ff.p, E.layer_c.p,
-                         P.batch ? h->bs.d_centre.p : nullptr, P.batch ? h->bs.d_scale.p : nullptr, P.J,
-                         P.batch ? E.coef.p : nullptr);
-    ++launches;
-    // batched form with both static and moved leads: the static combine (beside the moved-lead
-    // operand kernel) and the steady-sum reduction (beside the band GEMM) run on the auxiliary
-    // stream, joined before the band reduction (measured: other placements of the small kernels,
-    // such as the criteria of the static leads beside the GEMM, lengthen the pass)
+    // batched form with both static and moved leads: the layer factors and the static combine
+    // (beside the moved-lead operand kernel, which needs neither) and the steady-sum reduction
+    // (beside the band GEMM) run on the auxiliary stream, joined before the band reduction
+    // (measured: other placements of the small kernels, such as the criteria of the static leads
+    // beside the GEMM, lengthen the pass)
     const bool fork = P.batch && nmove > 0 && nmove < (int)L;
     cudaStream_t sx = fork ? h->aux_stream : s;
     if (fork) {
         EKG_CUDA(cudaEventRecord(h->ev_fork, s));
         EKG_CUDA(cudaStreamWaitEvent(sx, h->ev_fork, 0));
     }
+    launch_layer_factors(sx, D, in.layer_k, in.cpre, n_sims, E.F.p, E.Ff.p, E.layer_c.p,
+                         P.batch ? h->bs.d_centre.p : nullptr, P.batch ? h->bs.d_scale.p : nullptr, P.J,
+                         P.batch ? E.coef.p : nullptr);
+    ++launches;
     if (P.batch) {
         BatchState &B = h->bs;
         auto static_part = [&]() {
