@@ -115,8 +115,9 @@ int ekg_simulate(ekg_heart *h, const double *layer_k, const double *leads_zyx, d
 /* Device timing of the simulation itself, inputs resident in device memory: uploads layer_k
  * (n_sims x n_layers x 9) and leads (n_sims x n_leads x 3, NULL = loaded positions) once, runs
  * `warmup` untimed and `iters` timed device passes, and writes up to n_out values:
- * [0] total ms of the timed passes (CUDA events on the heart's stream), [1] ms in the lead
- * contraction kernel, [2] ms in lead field / AP factors, [3] ms in reduction + criteria,
+ * [0] total ms of the timed passes (back to back, as replayed evaluation passes; CUDA events on
+ * the heart's stream), then over `iters` more passes with events between their parts: [1] ms in
+ * the lead contraction kernel, [2] ms in lead field / AP factors, [3] ms in reduction + criteria,
  * [4] kernel launches per pass, [5] leads whose lead field is recomputed per pass,
  * [6] 1 when the pass used the separable batched form, 0 for the per-simulation form,
  * batched form with moved leads only (else 0): [7] ms in the moved-lead operand kernel,
