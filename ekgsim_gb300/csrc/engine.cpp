@@ -189,32 +189,6 @@ class HostPool {
     bool stop_ = false, failed_ = false;
 };
 
-// Sorts v in parallel: parts sorted on the pool, then merged pairwise (the result is the one
-// std::sort gives, the keys being distinct).
-template <class T>
-void parallel_sort(std::vector<T> &v) {
-    const size_t n = v.size();
-    const size_t parts = std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), n / 65536));
-    if (parts <= 1) {
-        std::sort(v.begin(), v.end());
-        return;
-    }
-    std::vector<size_t> cut(parts + 1);
-    for (size_t i = 0; i <= parts; ++i) cut[i] = n * i / parts;
-    HostPool::get().run(parts, [&](size_t b, size_t e) {
-        for (size_t i = b; i < e; ++i) std::sort(v.begin() + cut[i], v.begin() + cut[i + 1]);
-    });
-    for (size_t w = 1; w < parts; w *= 2) {
-        const size_t pairs = (parts + 2 * w - 1) / (2 * w);
-        HostPool::get().run(pairs, [&](size_t b, size_t e) {
-            for (size_t q = b; q < e; ++q) {
-                const size_t lo = 2 * w * q, mid = std::min(parts, lo + w), hi = std::min(parts, lo + 2 * w);
-                if (mid < hi) std::inplace_merge(v.begin() + cut[lo], v.begin() + cut[mid], v.begin() + cut[hi]);
-            }
-        });
-    }
-}
-
 void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     auto t0 = std::chrono::steady_clock::now();
     EKG_CHECK(d && d->layers && d->transfer && d->leads_zyx, EKG_ERR_BAD_INPUT, "null heart description field");
