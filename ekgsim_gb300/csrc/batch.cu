@@ -370,7 +370,8 @@ __device__ __forceinline__ void chunk_w(int vb, int vend, const float4 *vox_pos,
 }
 
 // Work items: (32-AP stage st, group of LF_THREADS * LF_ROWS rows), taken from the counter `work`
-// (zeroed before the launch) by a grid of one wave of resident blocks; every item writes its own
+// (zeroed before the launch) by a grid of one wave of resident blocks, stages in `stage_order`
+// (descending voxel count, so that the last items are short); every item writes its own
 // outputs, so the results do not depend on the order.  A thread owns LF_ROWS consecutive rows
 // (row = s * nmove + l) and evaluates their lead positions together, so the voxel loads and tests
 // are shared by LF_ROWS field evaluations.  Per item and row the thread writes the BF16 hi/lo tile
@@ -393,7 +394,7 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
     const float2 *__restrict__ at_hilo, const int32_t *__restrict__ a_layer, const float *__restrict__ k5l, int nl,
     const float4 *__restrict__ hconst, const float4 *__restrict__ lrel, int nmove, int n_sims,
     const float2 *__restrict__ tref, const int32_t *__restrict__ nent, const int32_t *__restrict__ esplit,
-    uint8_t *__restrict__ Bt, float2 *__restrict__ P1) {
+    const int32_t *__restrict__ stage_order, uint8_t *__restrict__ Bt, float2 *__restrict__ P1) {
     __shared__ float s_d[26 * 4];
     __shared__ float s_w[LF_ROWS][8][LF_THREADS];
     __shared__ float2 s_at[BST];  // the stage's activation times
@@ -417,7 +418,7 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
         __syncthreads();
         const int item = s_item;
         if (item >= nst * ngr) break;
-        const int st = item / ngr;
+        const int st = stage_order[item / ngr];  // stages with the most voxels first
         const int L = a_layer[(int64_t)st * BST];
         // the stage's voxel records are copied to shared memory once per item (a stage of up to
         // LF_VCAP voxels; larger ones read global memory), so the voxel loop waits on no global load
@@ -1081,7 +1082,7 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, c
         const int grid = std::max(1, std::min(nst * ngr, std::max(1, per_sm) * sm_count));                       \
         k_batch_lead_field<NN, DG><<<grid, LF_THREADS, 0, s>>>(                                                   \
             nst, ngr, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p, \
-            k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, Bt, B.P1);                     \
+            k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, B.stage_order, Bt, B.P1);      \
     } while (0)
     switch (batch_tile_rows(two_bases, n_sims * nmove)) {
     case 32:

@@ -49,6 +49,7 @@ struct BatchState {
     DBuf<int32_t> ls0, ls1;                // [nl] 32-AP stage range of each layer
     DBuf<int32_t> nent, esplit;            // [nl], [nl][8]: entries, steady prefix ends (stages)
     DBuf<float2> tref;                     // [stages] last finite activation time of the stage (hi, lo)
+    DBuf<int32_t> stage_order;             // [stages] by descending voxel count (operand kernel's item order)
     DBuf<int64_t> goff;                    // [nl][8] offsets into gtab
     DBuf<float> gtab;                      // exp(-k4 (t0_e - tref[st])) for the steady stages of entry e
     DBuf<int32_t> ent;                     // [nl][ntt] entry of each tile (-1: layer without APs)

@@ -256,6 +256,7 @@ struct BandArgs {
     int max_ent = 1, nb = 1;
     const int32_t *ti0 = nullptr, *ti1 = nullptr;  // [ntt][nl] item range of (tile, layer)
     const float2 *tref = nullptr;                   // [stages] last finite activation time of each 32-AP stage
+    const int32_t *stage_order = nullptr;           // [stages] by descending voxel count
     const int32_t *nent = nullptr, *esplit = nullptr, *ls0 = nullptr, *ls1 = nullptr;  // stage units
     const int32_t *ent = nullptr;
     const int64_t *goff = nullptr;

@@ -591,6 +591,18 @@ void build_band(ekg_heart *h, const std::vector<double> &key, const std::vector<
     B.ls0.alloc(nl);
     B.ls1.alloc(nl);
     B.tref.alloc(nst);
+    {
+        // operand kernel items: stages with the most voxels first (longest-first), ties by index
+        std::vector<int64_t> vb(D.apad + 1);
+        EKG_CUDA(cudaMemcpy(vb.data(), D.a_vox_begin.p, vb.size() * 8, cudaMemcpyDeviceToHost));
+        std::vector<int32_t> order(nst);
+        for (int64_t st = 0; st < nst; ++st) order[st] = (int32_t)st;
+        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+            return vb[32 * (a + 1)] - vb[32 * a] > vb[32 * (b + 1)] - vb[32 * b];
+        });
+        B.stage_order.alloc(nst);
+        EKG_CUDA(cudaMemcpy(B.stage_order.p, order.data(), nst * 4, cudaMemcpyHostToDevice));
+    }
     B.nent.alloc(nl);
     B.esplit.alloc((size_t)nl * MAXE);
     B.goff.alloc((size_t)nl * MAXE);
@@ -955,6 +967,7 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             U.nleads = (int)L;
             U.max_ent = B.max_ent;
             U.tref = B.tref.p;
+            U.stage_order = B.stage_order.p;
             U.nent = B.nent.p;
             U.esplit = B.esplit.p;
             U.ls0 = B.ls0.p;
@@ -1078,7 +1091,7 @@ std::vector<uint64_t> pass_signature(const ekg_heart *h, const PassPlan &P, int 
                           (const void *)B.Q1.p,
                           (const void *)B.Q2.p, (const void *)B.Bt.p, (const void *)B.P1.p, (const void *)B.U.p,
                           (const void *)B.Up.p, (const void *)B.partial.p,
-                          (const void *)B.tref.p, (const void *)B.nent.p, (const void *)B.esplit.p, (const void *)B.ls0.p,
+                          (const void *)B.tref.p, (const void *)B.stage_order.p, (const void *)B.nent.p, (const void *)B.esplit.p, (const void *)B.ls0.p,
                           (const void *)B.ls1.p, (const void *)B.ent.p, (const void *)B.goff.p, (const void *)B.gtab.p,
                           (const void *)B.E.p, (const void *)B.work.p, (const void *)h->W0.p})
         v.push_back(u(p));
