@@ -436,3 +436,35 @@ def test_criteria_modes_match_fp64_compare(engine, mode):
         for l in range(spec.n_leads):
             ref = O.clamp(O.compare(mode, ecg[l], target[l], offs[l]))
             assert crit[l] == pytest.approx(ref, rel=1e-9, abs=1e-12), (mode, l)
+
+
+def test_batched_form_plane_fronts_large_aps(engine):
+    """A slab stimulated on a whole plane activates plane by plane, so every AP holds a full plane
+    of voxels and a 32-AP stage holds thousands: the operand kernel reads those stages' voxel
+    records from global memory instead of its shared-memory copy.  Batched ECGs (more than 16
+    simulations, the persistent operand kernel) match the oracle."""
+    from ekgsim_gb300.engine import Heart
+    n, steps, nl = 24, 300, 3
+    grid = np.zeros((n, n, n), dtype=np.int16)
+    for z in range(4, 22):
+        grid[z, 3:21, 3:21] = 1 + min(2, (z - 4) // 6)
+    grid[4, 3:21, 3:21] = -1
+    tm = synth.transfer_matrix(nl, [1, 2, 2])
+    rng = np.random.Generator(np.random.PCG64(17))
+    v = rng.normal(size=(4, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    leads = (n / 2.0 + 40.0 * v)[:, ::-1].copy()
+    h = Heart.create(engine, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+    target = synth.analytic_target(4, steps, 5)
+    h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], [t for t in target], mid_position=0.6)
+    spec = synth.small_spec(40, n_leads=4, seed=5)
+    genes = np.stack([synth.genes_for(spec, r, 0) for r in range(20)])
+    _, _, ecg_b = h.eval_batch(genes, want_ecg=True)
+    at, layer = O.activation(grid, tm)
+    for i in (0, 9, 19):
+        g = genes[i]
+        lk = O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], "endo-mid-epi",
+                         0.6, g[:12])[0]
+        moved = O.move_leads(leads, g[12:12 + 8].reshape(-1, 2))
+        ref = O.run(layer, at, lk, moved, "3D4", 0.0, float(steps), 1.0)
+        assert rel_l2(ecg_b[i], ref) <= ECG_TOL
