@@ -900,7 +900,8 @@ __global__ void __launch_bounds__(WS_THREADS, (N <= 32 ? 2 : 1)) k_batch_umma(
 // items of (t's tile, L) of the raw accumulators, (U0, U1) = U[row'][L][ent[L][j]], row = s * nmove
 // + l, row' = l * S + s, j = t / 128.  Block per (row, 32 steps): the 8 warps split each layer's
 // items (FP32, combined in a fixed order), the sum over layers is float-float, written as FP64 and
-// float-float (few rows, many items); k_reduce_band: one thread per (row, t) (many rows).
+// float-float (few rows, many items); k_reduce_band: one thread per (row, RB_T consecutive steps),
+// vector loads of the partials (many rows).
 __global__ void __launch_bounds__(256) k_reduce_band_w(int steps, int rows, int nmove, int n_sims, int nleads, int nl,
                                                      int ntt, int max_ent, int nb, const int32_t *__restrict__ ti0,
                                                      const int32_t *__restrict__ ti1, const int32_t *__restrict__ ent,
@@ -961,46 +962,70 @@ __global__ void __launch_bounds__(256) k_reduce_band_w(int steps, int rows, int 
     }
 }
 
+constexpr int RB_T = 4;  // consecutive steps per thread of k_reduce_band
 __global__ void k_reduce_band(int steps, int rows, int nmove, int n_sims, int nleads, int nl, int ntt, int max_ent,
                               int nb, const int32_t *__restrict__ ti0, const int32_t *__restrict__ ti1,
                               const int32_t *__restrict__ ent, const float *__restrict__ partial,
                               const float2 *__restrict__ U, const float *__restrict__ E, const float *__restrict__ F,
                               const double *__restrict__ k3, double *__restrict__ ecg,
                               float2 *__restrict__ ecg_ff) {
-    const int tt = blockIdx.x * blockDim.x + threadIdx.x;
-    if (tt >= steps) return;
+    const int t0 = (blockIdx.x * blockDim.x + threadIdx.x) * RB_T;  // RB_T steps inside one 128-step tile
+    if (t0 >= steps) return;
     const int r = blockIdx.y;
     const int s = r / nmove, l = r % nmove;
-    const int j = tt / BM, tl = tt - j * BM;
+    const int j = t0 / BM, tl = t0 - j * BM;
     const size_t rp = (size_t)l * n_sims + s;
-    float2 v = make_float2(0.f, 0.f);
+    float2 v[RB_T];
+#pragma unroll
+    for (int k = 0; k < RB_T; ++k) v[k] = make_float2(0.f, 0.f);
     for (int L = 0; L < nl; ++L) {
         const float kk = (float)k3[(size_t)s * nl + L];
-        float y1 = 0.f, y2 = 0.f;
+        float y1[RB_T], y2[RB_T];
+#pragma unroll
+        for (int k = 0; k < RB_T; ++k) y1[k] = y2[k] = 0.f;
         const int c0 = ti0[j * nl + L], c1 = ti1[j * nl + L];
         if (nb == 2) {
             for (int c = c0; c < c1; ++c) {
-                const float2 p = reinterpret_cast<const float2 *>(partial)[((size_t)c * rows + r) * BM + tl];
-                y1 += p.x;
-                y2 += p.y;
+                const float4 *p = reinterpret_cast<const float4 *>(partial + (((size_t)c * rows + r) * BM + tl) * 2);
+                const float4 a = p[0], b = p[1];
+                y1[0] += a.x;
+                y2[0] += a.y;
+                y1[1] += a.z;
+                y2[1] += a.w;
+                y1[2] += b.x;
+                y2[2] += b.y;
+                y1[3] += b.z;
+                y2[3] += b.w;
             }
         } else {
-            for (int c = c0; c < c1; ++c) y1 += partial[((size_t)c * rows + r) * BM + tl];
+            for (int c = c0; c < c1; ++c) {
+                const float4 a = *reinterpret_cast<const float4 *>(partial + ((size_t)c * rows + r) * BM + tl);
+                y1[0] += a.x;
+                y1[1] += a.y;
+                y1[2] += a.z;
+                y1[3] += a.w;
+            }
         }
         const int e = ent[L * ntt + j];
-        float st1 = 0.f, st0 = 0.f;
-        if (e >= 0) {
-            const float2 u = U[(rp * nl + L) * max_ent + e];
-            st1 = E[(size_t)L * steps + tt] * u.y;
-            st0 = u.x;
+        const float2 u = e >= 0 ? U[(rp * nl + L) * max_ent + e] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < RB_T; ++k) {
+            const int tt = t0 + k;
+            if (tt >= steps) break;
+            const float st1 = e >= 0 ? E[(size_t)L * steps + tt] * u.y : 0.f, st0 = u.x;
+            const float x = nb == 2 ? fmaf(kk, (y2[k] + st0) - (y1[k] + st1), y1[k] + st1)
+                                    : fmaf(kk, st0 - st1, y1[k] + st1);
+            v[k] = ff_add_f(v[k], F[((size_t)s * nl + L) * steps + tt] * x);
         }
-        const float x = nb == 2 ? fmaf(kk, (y2 + st0) - (y1 + st1), y1 + st1)
-                                : fmaf(kk, st0 - st1, y1 + st1);
-        v = ff_add_f(v, F[((size_t)s * nl + L) * steps + tt] * x);
     }
-    const size_t o = ((size_t)s * nleads + l) * steps + tt;
-    ecg[o] = ff_to_double(v);
-    ecg_ff[o] = v;
+#pragma unroll
+    for (int k = 0; k < RB_T; ++k) {
+        const int tt = t0 + k;
+        if (tt >= steps) break;
+        const size_t o = ((size_t)s * nleads + l) * steps + tt;
+        ecg[o] = ff_to_double(v[k]);
+        ecg_ff[o] = v[k];
+    }
 }
 
 template <int NB, int N>
@@ -1131,7 +1156,7 @@ void launch_reduce_band(cudaStream_t s, const BandArgs &A) {
                                              A.nb, A.ti0, A.ti1, A.ent, A.partial, A.U, A.E, A.F, A.k3, A.ecg,
                                              A.ecg_ff);
     } else {
-        dim3 grid((unsigned)((A.steps + 127) / 128), (unsigned)A.rows_used);
+        dim3 grid((unsigned)((A.steps + 128 * RB_T - 1) / (128 * RB_T)), (unsigned)A.rows_used);
         k_reduce_band<<<grid, 128, 0, s>>>(A.steps, A.rows, A.nmove, A.n_sims, A.nleads, A.nl, A.ntt, A.max_ent,
                                            A.nb, A.ti0, A.ti1, A.ent, A.partial, A.U, A.E, A.F, A.k3, A.ecg,
                                            A.ecg_ff);
