@@ -1,7 +1,6 @@
 // engine.cpp -- C ABI of the engine: engine and heart lifetime, plain and batched evaluation,
 // simulator.ini front end.
 #include <algorithm>
-#include <atomic>
 #include <climits>
 #include <array>
 #include <chrono>
@@ -1288,23 +1287,12 @@ void prepare_sim(ekg_heart *h, const double *genes, int n_genes, double *layer_k
 }
 
 // The fits of a pass, in parallel when there is more than one.
-// Fits take different numbers of descent steps, so the workers take runs of jobs from a shared
-// counter (a run of consecutive jobs mostly shares one simulation's border APs, whose connectors
-// the fit code keeps); each job writes only its own layer, so the order does not matter.
 void run_fits(std::vector<LayerFitJob> &jobs) {
     if (jobs.size() <= 1) {
         layer_aps_run_fits(jobs.data(), jobs.size());
         return;
     }
-    constexpr size_t kRun = 4;
-    const size_t runs = (jobs.size() + kRun - 1) / kRun;
-    std::atomic<size_t> next{0};
-    HostPool::get().run(std::min<size_t>(runs, 64), [&](size_t, size_t) {
-        for (size_t r; (r = next.fetch_add(1)) < runs;) {
-            const size_t b = r * kRun, e = std::min(jobs.size(), b + kRun);
-            layer_aps_run_fits(jobs.data() + b, e - b);
-        }
-    });
+    HostPool::get().run(jobs.size(), [&](size_t b, size_t e) { layer_aps_run_fits(jobs.data() + b, e - b); });
 }
 
 // SimImplementation::calculateFitness (sim.cpp:600-702) from the device's per-lead comparison
