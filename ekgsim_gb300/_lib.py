@@ -87,6 +87,11 @@ SIGNATURES = {
     # pointer objects cost more than the call itself
     "ekg_eval_batch": (ctypes.c_int, [ctypes.c_void_p, c_int32, ctypes.c_void_p, c_int32, ctypes.c_void_p,
                                       ctypes.c_void_p, ctypes.c_void_p]),
+    "ekg_eval_batch_submit": (ctypes.c_int, [ctypes.c_void_p, c_int32, ctypes.c_void_p, c_int32, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_void_p, P(ctypes.c_int64)]),
+    "ekg_eval_batch_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),
+    "ekg_host_register": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),
+    "ekg_host_unregister": (ctypes.c_int, [ctypes.c_void_p]),
     "ekg_server_create": (ctypes.c_int, [ctypes.c_void_p, P(ServerOpts), P(ctypes.c_void_p)]),
     "ekg_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "ekg_server_add_heart": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, P(c_int32)]),

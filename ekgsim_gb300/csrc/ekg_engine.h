@@ -96,21 +96,55 @@ struct ekg_heart {
     PassGraph graphs[4];
     uint64_t graph_clock = 0;
     // the small per-pass inputs, packed into one pinned host buffer and copied with one transfer into
-    // one device buffer (both grow only, so the device addresses the graphs hold stay valid)
-    uint8_t *stage_host = nullptr;
-    ekg::DBuf<uint8_t> stage_dev;
-    size_t stage_cap = 0;
+    // one device buffer (both grow only, so the device addresses the graphs hold stay valid); two
+    // of them, so that a pass can be prepared while the one before runs
     struct PassInputs {
         const double *layer_k = nullptr, *cpre = nullptr, *leads = nullptr, *k3 = nullptr;
         const float *k5l = nullptr;
         const float4 *hconst = nullptr, *lrel = nullptr;
         const int4 *items = nullptr;
         const int32_t *ti0 = nullptr, *ti1 = nullptr;
-    } in;
+    };
+    struct Staging {
+        uint8_t *host = nullptr;
+        ekg::DBuf<uint8_t> dev;
+        size_t cap = 0;
+        PassInputs in;
+    };
+    Staging stg[2];
+    int cur = 0;  // staging buffer (and pending slot) of the next pass
+    const PassInputs &in() const { return stg[cur].in; }
+    // batched evaluations in flight (submitted, results not yet handed over), one per staging buffer
+    struct Pending {
+        bool busy = false;
+        int64_t ticket = 0;
+        cudaEvent_t done = nullptr;        // the pass and its copies to the host are complete
+        uint32_t *err = nullptr;           // pinned error word of the pass
+        double *crit2 = nullptr;           // pinned per-lead criterion values and peaks
+        size_t crit2_cap = 0;
+        int n_sims = 0;
+        std::vector<double> lk_all, leads_all, viol, acrit;
+        std::vector<char> done_flags;
+        std::vector<std::vector<double>> approx;
+        double *criteria = nullptr, *violation = nullptr;  // the caller's outputs
+    };
+    Pending pend[2];
+    int64_t next_ticket = 0;
+    cudaEvent_t copies_done = nullptr;  // the last pass's copies to the host are complete
+    cudaEvent_t pass_end = nullptr;     // the last pass's work on the heart's stream is complete
+    bool copies_pending = false;
     ~ekg_heart() {
         for (PassGraph &g : graphs)
             if (g.exec) cudaGraphExecDestroy(g.exec);
-        if (stage_host) cudaFreeHost(stage_host);
+        for (Staging &g : stg)
+            if (g.host) cudaFreeHost(g.host);
+        for (Pending &p : pend) {
+            if (p.done) cudaEventDestroy(p.done);
+            if (p.err) cudaFreeHost(p.err);
+            if (p.crit2) cudaFreeHost(p.crit2);
+        }
+        if (copies_done) cudaEventDestroy(copies_done);
+        if (pass_end) cudaEventDestroy(pass_end);
         if (static_done) cudaEventDestroy(static_done);
         if (moved_done) cudaEventDestroy(moved_done);
         for (cudaEvent_t e : {ev_fork, ev_op, ev_join})

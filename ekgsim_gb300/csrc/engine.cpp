@@ -428,7 +428,7 @@ int64_t heart_device_bytes(const ekg_heart *h) {
                 D.vox_nb.bytes() + D.vox_nbo.bytes() + D.chunk_a0.bytes() * 3 + D.t.bytes() + D.t_hilo.bytes() +
                 h->W0.bytes() + h->at_cells.bytes();
     const EvalDev &E = h->ev;
-    b += (int64_t)h->stage_dev.bytes() + E.layer_c.bytes() + E.F.bytes() + E.k0w.bytes() + E.W.bytes() +
+    b += (int64_t)h->stg[0].dev.bytes() + (int64_t)h->stg[1].dev.bytes() + E.layer_c.bytes() + E.F.bytes() + E.k0w.bytes() + E.W.bytes() +
          E.Wp.bytes() + E.partial.bytes() + E.ecg.bytes() + E.ecg_ff.bytes() + E.coef.bytes() + E.crit.bytes() + E.targets.bytes() +
          E.targets_ff.bytes();
     return b;
@@ -862,20 +862,21 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
             o_lr = add(P.lrel.data(), P.lrel.size() * sizeof(float4));
         }
     }
-    if (off > h->stage_cap) {
-        const size_t cap = std::max(off, 2 * h->stage_cap);
+    ekg_heart::Staging &sg = h->stg[h->cur];
+    if (off > sg.cap) {
+        const size_t cap = std::max(off, 2 * sg.cap);
         EKG_CUDA(cudaStreamSynchronize(s));  // the old buffers may still be read
-        if (h->stage_host) cudaFreeHost(h->stage_host);
-        h->stage_host = nullptr;
-        h->stage_cap = 0;
-        EKG_CUDA(cudaMallocHost(&h->stage_host, cap));
-        h->stage_dev.alloc(cap);
-        h->stage_cap = cap;
+        if (sg.host) cudaFreeHost(sg.host);
+        sg.host = nullptr;
+        sg.cap = 0;
+        EKG_CUDA(cudaMallocHost(&sg.host, cap));
+        sg.dev.alloc(cap);
+        sg.cap = cap;
     }
-    for (const Slot &sl : slots) std::memcpy(h->stage_host + sl.off, sl.src, sl.bytes);
-    if (off) EKG_CUDA(cudaMemcpyAsync(h->stage_dev.p, h->stage_host, off, cudaMemcpyHostToDevice, s));
-    const uint8_t *dv = h->stage_dev.p;
-    ekg_heart::PassInputs &in = h->in;
+    for (const Slot &sl : slots) std::memcpy(sg.host + sl.off, sl.src, sl.bytes);
+    if (off) EKG_CUDA(cudaMemcpyAsync(sg.dev.p, sg.host, off, cudaMemcpyHostToDevice, s));
+    const uint8_t *dv = sg.dev.p;
+    ekg_heart::PassInputs &in = sg.in;
     in = ekg_heart::PassInputs();
     in.layer_k = reinterpret_cast<const double *>(dv + o_lk);
     in.cpre = h->cpre_on ? reinterpret_cast<const double *>(dv + o_cp) : nullptr;
@@ -921,7 +922,7 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
     int launches = 0;
     if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[0], s));
     EKG_CUDA(cudaMemsetAsync(E.err.p, 0, sizeof(uint32_t), s));
-    const ekg_heart::PassInputs &in = h->in;
+    const ekg_heart::PassInputs &in = h->in();
     // batched form with both static and moved leads: the layer factors and the static combine
     // (beside the moved-lead operand kernel, which needs neither) and the steady-sum reduction
     // (beside the band GEMM) run on the auxiliary stream, joined before the band reduction
@@ -1079,7 +1080,7 @@ std::vector<uint64_t> pass_signature(const ekg_heart *h, const PassPlan &P, int 
                                (uint64_t)P.nitems, (uint64_t)ncl, (uint64_t)mode, (uint64_t)mark_static,
                                (uint64_t)h->cpre_on, (uint64_t)h->any_k0, (uint64_t)h->eng->umma, (uint64_t)B.J,
                                (uint64_t)B.max_ent, (uint64_t)B.ntt};
-    const ekg_heart::PassInputs &in = h->in;
+    const ekg_heart::PassInputs &in = h->in();
     for (const void *p : {(const void *)in.layer_k, (const void *)in.cpre, (const void *)in.leads, (const void *)in.k3,
                           (const void *)B.d_centre.p, (const void *)B.d_scale.p, (const void *)E.coef.p,
                           (const void *)in.k5l, (const void *)in.hconst, (const void *)in.lrel,
@@ -1145,33 +1146,54 @@ void run_pass(ekg_heart *h, const PassPlan &P, int ncl, int mode, bool mark_stat
     EKG_CUDA(cudaGraphLaunch(exec, s));
 }
 
-void device_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *leads, double *ecg_host,
-                 double *crit_host, int n_crit_leads, int mode) {
+void assemble_criteria(const ekg_heart *h, const double *layer_k, const double *crit2, bool done,
+                       double approx_crit, const std::vector<double> &approx, double *out);
+
+// Queues one device pass from the current staging buffer (h->cur): plan, upload, the pass (a graph
+// replay) and the copies of its outputs (ECG to ecg_host; criterion values and the error word to
+// the pending slot's pinned buffers).  pend[h->cur].done marks the pass and its copies complete.
+// The pass's kernels wait for the previous pass's copies to the host (they overwrite its outputs).
+void launch_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *leads, double *ecg_host,
+                 int n_crit_leads, int mode) {
     HeartDev &D = h->dev;
     EvalDev &E = h->ev;
     cudaStream_t s = h->stream;
+    ekg_heart::Pending &pd = h->pend[h->cur];
     EKG_CUDA(cudaSetDevice(h->eng->device));
+    if (!h->copy_stream) {
+        EKG_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        for (cudaEvent_t *e : {&h->static_done, &h->moved_done, &h->copies_done, &h->pass_end})
+            EKG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+    if (!pd.done) {
+        EKG_CUDA(cudaEventCreateWithFlags(&pd.done, cudaEventDisableTiming));
+        EKG_CUDA(cudaMallocHost(&pd.err, sizeof(uint32_t)));
+    }
+    const size_t need = (size_t)n_sims * std::max(1, n_crit_leads) * 2;
+    if (pd.crit2_cap < need) {
+        if (pd.crit2) cudaFreeHost(pd.crit2);
+        pd.crit2 = nullptr;
+        pd.crit2_cap = 0;
+        EKG_CUDA(cudaMallocHost(&pd.crit2, need * sizeof(double)));
+        pd.crit2_cap = need;
+    }
     const PassPlan P = plan_pass(h, n_sims, layer_k, leads);
     upload_inputs(h, P, layer_k, leads);
+    if (h->copies_pending) EKG_CUDA(cudaStreamWaitEvent(s, h->copies_done, 0));
     const size_t L = D.nleads, S = n_sims, T = D.steps;
-    // batched form: the static-lead rows of the ECG are final after the first kernel, so their copy
-    // to the host runs on a second stream while the moved-lead part is computed
+    // batched form: the static-lead rows of the ECG are final early, so their copy to the host runs
+    // on the copy stream while the moved-lead part is computed
     const bool split = ecg_host && P.batch && P.nmove < (int)L;
-    if (split && !h->copy_stream) {
-        EKG_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
-        EKG_CUDA(cudaEventCreateWithFlags(&h->static_done, cudaEventDisableTiming));
-        EKG_CUDA(cudaEventCreateWithFlags(&h->moved_done, cudaEventDisableTiming));
-    }
-    run_pass(h, P, crit_host ? n_crit_leads : 0, mode, split);
+    run_pass(h, P, n_crit_leads, mode, split);
     if (split) {
         const size_t nm = P.nmove;
         EKG_CUDA(cudaStreamWaitEvent(h->copy_stream, h->static_done, 0));
         EKG_CUDA(cudaMemcpy2DAsync(ecg_host + nm * T, L * T * 8, E.ecg.p + nm * T, L * T * 8, (L - nm) * T * 8, S,
                                    cudaMemcpyDeviceToHost, h->copy_stream));
     }
-    EKG_CUDA(cudaMemcpyAsync(h->err_host, E.err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    if (crit_host && n_crit_leads > 0)
-        EKG_CUDA(cudaMemcpyAsync(crit_host, E.crit.p, S * n_crit_leads * 2 * 8, cudaMemcpyDeviceToHost, s));
+    EKG_CUDA(cudaMemcpyAsync(pd.err, E.err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    if (n_crit_leads > 0)
+        EKG_CUDA(cudaMemcpyAsync(pd.crit2, E.crit.p, S * n_crit_leads * 2 * 8, cudaMemcpyDeviceToHost, s));
     if (split) {
         if (P.nmove > 0) {
             EKG_CUDA(cudaStreamWaitEvent(h->copy_stream, h->moved_done, 0));
@@ -1181,16 +1203,51 @@ void device_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *
     } else if (ecg_host) {
         EKG_CUDA(cudaMemcpyAsync(ecg_host, E.ecg.p, S * L * T * 8, cudaMemcpyDeviceToHost, s));
     }
-    EKG_CUDA(cudaStreamSynchronize(s));
-    if (split) EKG_CUDA(cudaStreamSynchronize(h->copy_stream));
-    if (*h->err_host) throw Error{EKG_ERR_TIMEOUT, "a bounded device wait ran out (error word " +
-                                                       std::to_string(*h->err_host) + ")"};
+    // done = the heart's stream and the copy stream both past this pass
+    EKG_CUDA(cudaEventRecord(h->pass_end, s));
+    EKG_CUDA(cudaStreamWaitEvent(h->copy_stream, h->pass_end, 0));
+    EKG_CUDA(cudaEventRecord(h->copies_done, h->copy_stream));
+    EKG_CUDA(cudaEventRecord(pd.done, h->copy_stream));
+    h->copies_pending = true;
+}
+
+// Hands over a pending batched evaluation: waits for its pass, checks the device error word and
+// writes the criteria and violations to the caller's buffers.
+void complete_pending(ekg_heart *h, int slot) {
+    ekg_heart::Pending &pd = h->pend[slot];
+    if (!pd.busy) return;
+    pd.busy = false;
+    EKG_CUDA(cudaEventSynchronize(pd.done));
+    if (*pd.err) throw Error{EKG_ERR_TIMEOUT, "a bounded device wait ran out (error word " + std::to_string(*pd.err) + ")"};
+    if (!pd.criteria) return;
+    const int nl = h->dev.nlayers, ncl = h->es.n_crit_leads;
+    for (int s = 0; s < pd.n_sims; ++s) {
+        assemble_criteria(h, &pd.lk_all[(size_t)s * nl * 9], &pd.crit2[(size_t)s * ncl * 2], pd.done_flags[s] != 0,
+                          pd.acrit[s], pd.approx[s], pd.criteria + (size_t)s * h->es.n_criteria);
+        pd.violation[s] = pd.viol[s];
+    }
+}
+void drain_pending(ekg_heart *h) {
+    for (int i = 0; i < 2; ++i) complete_pending(h, (h->cur + i) % 2);  // oldest first
+}
+
+// One device pass, synchronous (the drop-in simulate call): waits for the evaluations in flight first.
+void device_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *leads, double *ecg_host) {
+    drain_pending(h);
+    const int slot = h->cur;
+    launch_pass(h, n_sims, layer_k, leads, ecg_host, 0, 2);
+    ekg_heart::Pending &pd = h->pend[slot];
+    pd.busy = true;
+    pd.criteria = nullptr;
+    h->cur ^= 1;
+    complete_pending(h, slot);
 }
 
 // Device-only timing of `iters` passes with inputs resident (after `warmup` untimed passes).
 void benchmark(ekg_heart *h, int n_sims, const double *layer_k, const double *leads, int warmup, int iters,
                double *out, int n_out) {
     std::lock_guard<std::mutex> lk(h->mu);
+    drain_pending(h);
     EKG_CUDA(cudaSetDevice(h->eng->device));
     cudaStream_t s = h->stream;
     const PassPlan P = plan_pass(h, n_sims, layer_k, leads);
@@ -1396,34 +1453,56 @@ bool approx_gate(const ekg_heart *h, const double *layer_k, double &approx_crit,
     return !(approx_crit > es.fast_limit);
 }
 
-void eval_many(ekg_heart *h, int n_sims, const double *genes, int n_genes, double *criteria, double *violation,
-               double *ecg, double *layer_k_out, double *leads_out) {
+// SimImplementation::eval for a batch, asynchronously: the host part (genes -> layer APs and lead
+// positions, fits, the fast-approximation gate) and the pass are queued into the current staging
+// buffer; the criteria reach the caller's buffers when the evaluation is handed over
+// (eval_wait, or when its staging buffer is needed again two submissions later).
+int64_t eval_submit(ekg_heart *h, int n_sims, const double *genes, int n_genes, double *criteria, double *violation,
+                    double *ecg, double *layer_k_out, double *leads_out) {
     std::lock_guard<std::mutex> lk(h->mu);
+    const int slot = h->cur;
+    complete_pending(h, slot);  // the staging buffer's previous evaluation
+    ekg_heart::Pending &pd = h->pend[slot];
     const int nl = h->dev.nlayers, L = h->dev.nleads;
-    std::vector<double> lk_all((size_t)n_sims * nl * 9), leads_all((size_t)n_sims * L * 3), viol(n_sims);
-    std::vector<char> done(n_sims, 1);
-    std::vector<double> acrit(n_sims, 2.0);
-    std::vector<std::vector<double>> approx(n_sims);
+    pd.lk_all.assign((size_t)n_sims * nl * 9, 0.0);
+    pd.leads_all.assign((size_t)n_sims * L * 3, 0.0);
+    pd.viol.assign(n_sims, 0.0);
+    pd.done_flags.assign(n_sims, 1);
+    pd.acrit.assign(n_sims, 2.0);
+    pd.approx.assign(n_sims, {});
     std::vector<LayerFitJob> jobs;
     std::vector<LayerFit> fits;
     for (int s = 0; s < n_sims; ++s) {
         fits.clear();
-        prepare_sim(h, genes + (size_t)s * n_genes, n_genes, &lk_all[(size_t)s * nl * 9], &leads_all[(size_t)s * L * 3],
-                    &viol[s], fits);
-        for (const LayerFit &f : fits) jobs.push_back(LayerFitJob{f, &lk_all[(size_t)s * nl * 9]});
+        prepare_sim(h, genes + (size_t)s * n_genes, n_genes, &pd.lk_all[(size_t)s * nl * 9],
+                    &pd.leads_all[(size_t)s * L * 3], &pd.viol[s], fits);
+        for (const LayerFit &f : fits) jobs.push_back(LayerFitJob{f, &pd.lk_all[(size_t)s * nl * 9]});
     }
     run_fits(jobs);
-    for (int s = 0; s < n_sims; ++s) done[s] = approx_gate(h, &lk_all[(size_t)s * nl * 9], acrit[s], approx[s]);
-    const int ncl = h->es.n_crit_leads;
-    std::vector<double> crit2((size_t)n_sims * std::max(1, ncl) * 2);
-    device_pass(h, n_sims, lk_all.data(), leads_all.data(), ecg, crit2.data(), ncl, h->es.comparison_mode);
-    for (int s = 0; s < n_sims; ++s) {
-        assemble_criteria(h, &lk_all[(size_t)s * nl * 9], &crit2[(size_t)s * ncl * 2], done[s], acrit[s], approx[s],
-                          criteria + (size_t)s * h->es.n_criteria);
-        violation[s] = viol[s];
-    }
-    if (layer_k_out) std::copy(lk_all.begin(), lk_all.end(), layer_k_out);
-    if (leads_out) std::copy(leads_all.begin(), leads_all.end(), leads_out);
+    for (int s = 0; s < n_sims; ++s)
+        pd.done_flags[s] = approx_gate(h, &pd.lk_all[(size_t)s * nl * 9], pd.acrit[s], pd.approx[s]) ? 1 : 0;
+    if (layer_k_out) std::copy(pd.lk_all.begin(), pd.lk_all.end(), layer_k_out);
+    if (leads_out) std::copy(pd.leads_all.begin(), pd.leads_all.end(), leads_out);
+    launch_pass(h, n_sims, pd.lk_all.data(), pd.leads_all.data(), ecg, h->es.n_crit_leads, h->es.comparison_mode);
+    pd.busy = true;
+    pd.ticket = ++h->next_ticket;
+    pd.n_sims = n_sims;
+    pd.criteria = criteria;
+    pd.violation = violation;
+    h->cur ^= 1;
+    return pd.ticket;
+}
+
+void eval_wait(ekg_heart *h, int64_t ticket) {
+    std::lock_guard<std::mutex> lk(h->mu);
+    EKG_CHECK(ticket >= 1 && ticket <= h->next_ticket, EKG_ERR_NOT_FOUND, "unknown evaluation ticket");
+    for (int i = 0; i < 2; ++i)
+        if (h->pend[i].busy && h->pend[i].ticket == ticket) complete_pending(h, i);
+}
+
+void eval_many(ekg_heart *h, int n_sims, const double *genes, int n_genes, double *criteria, double *violation,
+               double *ecg, double *layer_k_out, double *leads_out) {
+    eval_wait(h, eval_submit(h, n_sims, genes, n_genes, criteria, violation, ecg, layer_k_out, leads_out));
 }
 
 void set_eval(ekg_heart *h, const ekg_eval_config *c) {
@@ -1466,6 +1545,7 @@ void set_eval(ekg_heart *h, const ekg_eval_config *c) {
     if (c->disp_min && c->n_disp_min > 0) es.disp_min_v.assign(c->disp_min, c->disp_min + c->n_disp_min);
     if (c->disp_max && c->n_disp_max > 0) es.disp_max_v.assign(c->disp_max, c->disp_max + c->n_disp_max);
     std::lock_guard<std::mutex> lk(h->mu);
+    drain_pending(h);  // evaluations in flight are handed over with the settings they ran with
     // device copies of the targets
     EvalDev &E = h->ev;
     E.targets.alloc(off);
@@ -1630,7 +1710,7 @@ int ekg_simulate(ekg_heart *h, const double *layer_k, const double *leads_zyx, d
         for (int i = 0; i < 9 * h->dev.nlayers; ++i)
             EKG_CHECK(std::isfinite(layer_k[i]), EKG_ERR_BAD_INPUT, "AP coefficients must be finite");
         std::lock_guard<std::mutex> lk(h->mu);
-        device_pass(h, 1, layer_k, leads_zyx ? leads_zyx : h->leads0.data(), ecg_out, nullptr, 0, 2);
+        device_pass(h, 1, layer_k, leads_zyx ? leads_zyx : h->leads0.data(), ecg_out);
     });
 }
 
@@ -1690,6 +1770,36 @@ int ekg_eval_batch(ekg_heart *h, int32_t n_sims, const double *genes, int32_t n_
     return guard([&] {
         EKG_CHECK(h && genes && criteria_out && violation_out && n_sims >= 1, EKG_ERR_BAD_INPUT, "bad argument");
         eval_many(h, n_sims, genes, n_genes, criteria_out, violation_out, ecg_out, nullptr, nullptr);
+    });
+}
+
+int ekg_eval_batch_submit(ekg_heart *h, int32_t n_sims, const double *genes, int32_t n_genes, double *criteria_out,
+                          double *violation_out, double *ecg_out, int64_t *ticket_out) {
+    return guard([&] {
+        EKG_CHECK(h && genes && criteria_out && violation_out && ticket_out && n_sims >= 1, EKG_ERR_BAD_INPUT,
+                  "bad argument");
+        *ticket_out = eval_submit(h, n_sims, genes, n_genes, criteria_out, violation_out, ecg_out, nullptr, nullptr);
+    });
+}
+
+int ekg_eval_batch_wait(ekg_heart *h, int64_t ticket) {
+    return guard([&] {
+        EKG_CHECK(h, EKG_ERR_BAD_INPUT, "null heart");
+        eval_wait(h, ticket);
+    });
+}
+
+int ekg_host_register(void *ptr, int64_t bytes) {
+    return guard([&] {
+        EKG_CHECK(ptr && bytes > 0, EKG_ERR_BAD_INPUT, "bad argument");
+        EKG_CUDA(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault));
+    });
+}
+
+int ekg_host_unregister(void *ptr) {
+    return guard([&] {
+        EKG_CHECK(ptr, EKG_ERR_BAD_INPUT, "bad argument");
+        EKG_CUDA(cudaHostUnregister(ptr));
     });
 }
 

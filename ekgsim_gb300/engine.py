@@ -169,9 +169,7 @@ class Heart:
             return crit, float(viol[0]), ecg, lk, leads
         return crit, float(viol[0])
 
-    def eval_batch(self, genes: np.ndarray, want_ecg: bool = False, out=None):
-        """Criteria [n, n_criteria], violations [n] (and ECGs [n, n_leads, steps]) for n gene vectors.
-        ``out`` = (crit, viol[, ecg]) reuses caller-owned C-contiguous float64 arrays of those shapes."""
+    def _batch_args(self, genes, want_ecg, out):
         genes = np.ascontiguousarray(np.atleast_2d(genes), dtype=np.float64)
         n, g = genes.shape
         _, nc = self.eval_shape()
@@ -183,11 +181,31 @@ class Heart:
             bufs = list(out)
         else:
             bufs = [np.empty(sh) for sh in shapes]
+        return genes, n, g, bufs
+
+    def eval_batch(self, genes: np.ndarray, want_ecg: bool = False, out=None):
+        """Criteria [n, n_criteria], violations [n] (and ECGs [n, n_leads, steps]) for n gene vectors.
+        ``out`` = (crit, viol[, ecg]) reuses caller-owned C-contiguous float64 arrays of those shapes."""
+        genes, n, g, bufs = self._batch_args(genes, want_ecg, out)
         crit, viol = bufs[0], bufs[1]
         ecg = bufs[2] if want_ecg else None
         check(self._lib.ekg_eval_batch(self._h, n, genes.ctypes.data, g, crit.ctypes.data, viol.ctypes.data,
                                        ecg.ctypes.data if ecg is not None else None))
         return (crit, viol, ecg) if want_ecg else (crit, viol)
+
+    def eval_batch_submit(self, genes: np.ndarray, out, want_ecg: bool = False) -> int:
+        """Queues a batched evaluation into caller-owned ``out`` = (crit, viol[, ecg]) and returns its
+        ticket; the arrays are complete after ``eval_batch_wait(ticket)`` (ekg_eval_batch_submit)."""
+        genes, n, g, bufs = self._batch_args(genes, want_ecg, out)
+        crit, viol = bufs[0], bufs[1]
+        ecg = bufs[2] if want_ecg else None
+        t = ctypes.c_int64()
+        check(self._lib.ekg_eval_batch_submit(self._h, n, genes.ctypes.data, g, crit.ctypes.data, viol.ctypes.data,
+                                              ecg.ctypes.data if ecg is not None else None, ctypes.byref(t)))
+        return t.value
+
+    def eval_batch_wait(self, ticket: int):
+        check(self._lib.ekg_eval_batch_wait(self._h, ticket))
 
     def close(self):
         if self._h:
@@ -295,3 +313,12 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def host_register(a: np.ndarray):
+    """Page-locks a numpy array's memory (ekg_host_register) so device copies into it run asynchronously."""
+    check(L.load().ekg_host_register(a.ctypes.data, a.nbytes))
+
+
+def host_unregister(a: np.ndarray):
+    check(L.load().ekg_host_unregister(a.ctypes.data))

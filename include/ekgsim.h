@@ -174,6 +174,22 @@ int ekg_eval(ekg_heart *h, const double *genes, int32_t n_genes, double *criteri
 int ekg_eval_batch(ekg_heart *h, int32_t n_sims, const double *genes, int32_t n_genes,
                    double *criteria_out, double *violation_out, double *ecg_out);
 
+/* The same, queued: returns once the host part of the evaluation is done (genes may be reused)
+ * and its device pass is queued; *ticket_out identifies it.  The outputs are complete after
+ * ekg_eval_batch_wait(ticket).  Two evaluations per heart can be in flight, so a caller can
+ * prepare the next batch while the device runs the current one (the reference's master process
+ * hands out the next generation's jobs the same way, AMS-DEMO/ParallelFramework.h:226-520); a
+ * third submission first completes the oldest.  Copies into pageable output memory block the
+ * calling thread; ekg_host_register the output buffers to let the copies run asynchronously. */
+int ekg_eval_batch_submit(ekg_heart *h, int32_t n_sims, const double *genes, int32_t n_genes,
+                          double *criteria_out, double *violation_out, double *ecg_out, int64_t *ticket_out);
+int ekg_eval_batch_wait(ekg_heart *h, int64_t ticket);
+
+/* Page-locks (and releases) caller memory so that device copies into it run asynchronously
+ * (cudaHostRegister).  The memory must stay allocated while it is registered. */
+int ekg_host_register(void *ptr, int64_t bytes);
+int ekg_host_unregister(void *ptr);
+
 /* ------------------------------------------------------------------ served form */
 typedef struct {
     int32_t max_batch;           /* most requests packed into one device pass (default 256) */

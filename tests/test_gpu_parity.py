@@ -468,3 +468,37 @@ def test_batched_form_plane_fronts_large_aps(engine):
         moved = O.move_leads(leads, g[12:12 + 8].reshape(-1, 2))
         ref = O.run(layer, at, lk, moved, "3D4", 0.0, float(steps), 1.0)
         assert rel_l2(ecg_b[i], ref) <= ECG_TOL
+
+
+def test_queued_batches_match_synchronous(engine):
+    """Queued batched evaluations (two in flight, a third submission completing the oldest) give the
+    same criteria, violations and ECGs as synchronous calls, bit for bit."""
+    from ekgsim_gb300 import engine as E
+    spec = synth.small_spec(40, n_leads=4, seed=8)
+    steps = 300
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    h = E.Heart.create(engine, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+    target = synth.analytic_target(spec.n_leads, steps, 2)
+    h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], [t for t in target], mid_position=0.6)
+    batches = [np.stack([synth.genes_for(spec, 40 * b + r, 0) for r in range(20 + 3 * b)]) for b in range(3)]
+    ref = [h.eval_batch(g, want_ecg=True) for g in batches]
+    outs = [(np.empty_like(r[0]), np.empty_like(r[1]), np.empty_like(r[2])) for r in ref]
+    for o in outs:
+        for a in o:
+            E.host_register(a)
+    try:
+        t0 = h.eval_batch_submit(batches[0], outs[0], want_ecg=True)
+        t1 = h.eval_batch_submit(batches[1], outs[1], want_ecg=True)
+        t2 = h.eval_batch_submit(batches[2], outs[2], want_ecg=True)  # completes the first
+        h.eval_batch_wait(t2)
+        h.eval_batch_wait(t0)
+        h.eval_batch_wait(t1)
+        for o, r in zip(outs, ref):
+            for a, b in zip(o, r):
+                assert np.array_equal(a, b)
+    finally:
+        for o in outs:
+            for a in o:
+                E.host_unregister(a)
