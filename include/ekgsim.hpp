@@ -76,6 +76,16 @@ public:
         for (int32_t i = 0; i < n; ++i)
             std::copy(c.begin() + (size_t)i * criteria_, c.begin() + (size_t)(i + 1) * criteria_, results[i].begin());
     }
+    // a generation queued while the previous one runs (ekg_eval_batch_submit / _wait): the
+    // outputs must stay allocated until waitBatch returns
+    int64_t submitBatch(const std::vector<double> &genes_flat, int32_t n, double *criteria, double *violations,
+                        double *ecg = nullptr) const {
+        if ((int64_t)genes_flat.size() != (int64_t)n * genes_) throw std::runtime_error("Solution does not contain enough values");
+        int64_t t = 0;
+        check(ekg_eval_batch_submit(h_, n, genes_flat.data(), genes_, criteria, violations, ecg, &t));
+        return t;
+    }
+    void waitBatch(int64_t ticket) const { check(ekg_eval_batch_wait(h_, ticket)); }
     // getGeneParams (sim.cpp:523-580)
     void getGeneParams(size_t &numGenes, size_t &numCriteria, std::vector<double> &gMin, std::vector<double> &gMax) const {
         numGenes = genes_;
