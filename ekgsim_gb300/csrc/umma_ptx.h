@@ -98,6 +98,16 @@ __device__ __forceinline__ float h_value(float tau, float4 c) {
     const float h = s * fmaf(c.z, e4, c.w);
     return s == 0.0f ? 0.0f : h;
 }
+// The same value with the sigmoid's two SFU operations skipped where they cannot change the
+// result.  For k1 tau log2(e) >= 26 the term 2^(-k1 tau log2 e) is below half an ulp of 1, so
+// 1 + e1 rounds to 1 and the sigmoid is 1; for k1 tau log2(e) <= -130, e1 overflows to +inf and
+// h_value returns 0.  Most (AP, step) pairs of a simulation lie far before or after the upstroke.
+__device__ __forceinline__ float h_value_fast(float tau, float4 c) {
+    const float x = c.x * tau;
+    if (x >= 26.f) return fmaf(c.z, ex2_approx(-c.y * tau), c.w);
+    if (x <= -130.f) return 0.f;
+    return h_value(tau, c);
+}
 // x -> (bf16 hi, bf16 lo) packed pairs for elements (x0, x1)
 __device__ __forceinline__ void split2(float x0, float x1, uint32_t &hi, uint32_t &lo) {
     __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
