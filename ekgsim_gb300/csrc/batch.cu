@@ -1076,6 +1076,96 @@ void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int
     EKG_CUDA(cudaGetLastError());
 }
 
+// Lead field of the per-simulation form: one thread per (AP, simulation).  The moved leads (rows
+// [0, nmove)) are evaluated in pairs that share the voxel loads, with the same field evaluation as
+// the batched form's operand kernel (closed form for interior voxels and for boundary voxels with
+// few absent neighbours where the leads are at least 20 cells away, exact sums otherwise); their
+// W is written for the k0 term and W' = W exp(k5_L at_a) for the contraction.  Leads at their
+// loaded position take the resident field W0, scaled the same way.  Lead positions are FP64
+// [S][lead_stride][3] (z, y, x), made relative to the voxel centre in FP64 before the FP32 cast.
+template <bool DIAG>
+__global__ void __launch_bounds__(128) k_sim_lead_field(
+    int64_t apad, InteriorField ic, const int64_t *__restrict__ a_vox_begin, const float4 *__restrict__ vox_pos,
+    const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs, const double *__restrict__ at,
+    const int32_t *__restrict__ a_layer, const double *__restrict__ layer_k, int nl, const double *__restrict__ leads,
+    int lead_stride, double cz, double cy, double cx, int nmove, int nleads, const float *__restrict__ W0,
+    float *__restrict__ W, float *__restrict__ Wp) {
+    __shared__ float s_d[26 * 4];
+    const int tid = threadIdx.x;
+    if (tid < nnb) {
+        const float dz = difs[3 * tid], dy = difs[3 * tid + 1], dx = difs[3 * tid + 2];
+        s_d[4 * tid] = dz;
+        s_d[4 * tid + 1] = dy;
+        s_d[4 * tid + 2] = dx;
+        s_d[4 * tid + 3] = dz * dz + dy * dy + dx * dx;
+    }
+    __syncthreads();
+    const int64_t a = (int64_t)blockIdx.x * 128 + tid;
+    const int s = blockIdx.y;
+    if (a >= apad) return;
+    const double aa = at[a];
+    const float f = isinf(aa) ? 0.f : expf((float)(layer_k[((size_t)s * nl + a_layer[a]) * 9 + 5] * aa));
+    const int vb = (int)a_vox_begin[a], ve = (int)a_vox_begin[a + 1];
+    const uint32_t full = (1u << nnb) - 1u;
+    for (int l0 = 0; l0 < nmove; l0 += 2) {
+        const int np = l0 + 1 < nmove ? 2 : 1;
+        float4 r[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const double *p = leads + ((size_t)s * lead_stride + l0 + min(q, np - 1)) * 3;
+            r[q] = make_float4((float)(p[0] - cz), (float)(p[1] - cy), (float)(p[2] - cx), 0.f);
+        }
+        float acc[2] = {0.f, 0.f};
+        for (int v = vb; v < ve; ++v) {
+            const float4 pos = vox_pos[v];
+            const uint32_t mi = __float_as_uint(pos.w);
+            MSquares q[2];
+            q[0] = msq(pos, r[0]);
+            q[1] = msq(pos, r[1]);
+            const bool far = q[0].s >= INTERIOR_S_MIN && q[1].s >= INTERIOR_S_MIN;
+            if ((mi & VOX_INTERIOR) && far) {
+                acc[0] += interior_w(ic, q[0], rsqa(q[0].s));
+                acc[1] += interior_w(ic, q[1], rsqa(q[1].s));
+            } else if ((mi & VOX_FEW) && far) {
+                few_w<2>(ic, q, pos, r, full & ~mi, vox_out[v], s_d, acc);
+            } else {
+                const float4 out = vox_out[v];
+#pragma unroll
+                for (int k = 0; k < 2; ++k)
+                    acc[k] += DIAG ? voxel_w_diag(pos, mi, out, r[k]) : voxel_w_general(pos, mi, out, r[k], nnb, s_d);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (q >= np) break;
+            const size_t o = ((size_t)s * nleads + l0 + q) * apad + a;
+            W[o] = acc[q];
+            Wp[o] = acc[q] * f;
+        }
+    }
+    for (int l = nmove; l < nleads; ++l) Wp[((size_t)s * nleads + l) * apad + a] = W0[(size_t)l * apad + a] * f;
+}
+
+void launch_sim_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads, int nmove, int lead_stride,
+                           int n_sims, const double *d_layer_k, const float *W0, float *W, float *Wp) {
+    InteriorField ic;
+    ic.A0 = h.interior_c[0];
+    ic.A1 = h.interior_c[1];
+    ic.B0 = h.interior_c[2];
+    ic.B1 = h.interior_c[3];
+    ic.B2 = h.interior_c[4];
+    const dim3 g((unsigned)((h.apad + 127) / 128), (unsigned)n_sims);
+    if (h.nhood == EKG_NHOOD_3D4)
+        k_sim_lead_field<true><<<g, 128, 0, s>>>(h.apad, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p,
+                                                 h.at.p, h.a_layer.p, d_layer_k, h.nlayers, d_leads, lead_stride,
+                                                 h.centre[0], h.centre[1], h.centre[2], nmove, h.nleads, W0, W, Wp);
+    else
+        k_sim_lead_field<false><<<g, 128, 0, s>>>(h.apad, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p,
+                                                  h.at.p, h.a_layer.p, d_layer_k, h.nlayers, d_leads, lead_stride,
+                                                  h.centre[0], h.centre[1], h.centre[2], nmove, h.nleads, W0, W, Wp);
+    EKG_CUDA(cudaGetLastError());
+}
+
 void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const float *k5l,
                              const float4 *hconst, const float4 *lrel, int nmove, int n_sims, const BandArgs &B,
                              uint8_t *Bt, int *work, int sm_count) {

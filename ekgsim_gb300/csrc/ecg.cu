@@ -144,22 +144,6 @@ __global__ void k_layer_factors(int nl, int steps, const double *__restrict__ t,
     }
 }
 
-// W' = W * exp(k5_L(a) at_a); one thread per (a, sim), looping leads.
-__global__ void k_scale_w(int64_t apad, int nleads, const float *__restrict__ W, const double *__restrict__ at,
-                          const int32_t *__restrict__ a_layer, const double *__restrict__ layer_k, int nl,
-                          int n_sims, float *__restrict__ Wp) {
-    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int s = blockIdx.y;
-    if (a >= apad) return;
-    const double aa = at[a];
-    float f = 0.f;
-    if (!isinf(aa)) f = expf((float)(layer_k[((size_t)s * nl + a_layer[a]) * 9 + 5] * aa));
-    for (int l = 0; l < nleads; ++l) {
-        const size_t o = ((size_t)s * nleads + l) * apad + a;
-        Wp[o] = W[o] * f;
-    }
-}
-
 // k0 term: k0w[s][l] = sum_L k0_L sum_{a in L} W[s][l][a]; one block per (l, s).
 __global__ void k_k0_term(int64_t apad, int nleads, const float *__restrict__ W, const int32_t *__restrict__ a_layer,
                           const double *__restrict__ layer_k, int nl, double *__restrict__ k0w) {
@@ -448,13 +432,6 @@ void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_lay
                           const double *d_scale, int J, float *d_coef) {
     k_layer_factors<<<(unsigned)((int64_t)n_sims * h.nlayers), 128, 0, s>>>(
         h.nlayers, h.steps, h.t.p, d_layer_k, d_cpre, n_sims, d_F, d_Ff, d_layer_c, d_centre, d_scale, J, d_coef);
-    EKG_CUDA(cudaGetLastError());
-}
-
-void launch_scale_w(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
-                    float *d_Wp) {
-    dim3 grid((unsigned)((h.apad + 255) / 256), (unsigned)n_sims);
-    k_scale_w<<<grid, 256, 0, s>>>(h.apad, h.nleads, d_W, h.at.p, h.a_layer.p, d_layer_k, h.nlayers, n_sims, d_Wp);
     EKG_CUDA(cudaGetLastError());
 }
 

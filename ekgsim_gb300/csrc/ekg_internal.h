@@ -216,8 +216,9 @@ void launch_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads,
 void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_layer_k, const double *d_cpre,
                           int n_sims, double *d_F, float *d_Ff, float *d_layer_c, const double *d_centre = nullptr,
                           const double *d_scale = nullptr, int J = 0, float *d_coef = nullptr);
-void launch_scale_w(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
-                    float *d_Wp);
+// per-simulation form: W (moved rows) and W' = W exp(k5 at) (every row) from the lead positions (batch.cu)
+void launch_sim_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads, int nmove, int lead_stride,
+                           int n_sims, const double *d_layer_k, const float *W0, float *W, float *Wp);
 void launch_k0_term(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
                     double *d_k0w);
 void launch_contract_cuda(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,

@@ -1037,14 +1037,12 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             EKG_CUDA(cudaEventRecord(tm->ev[2], s));
         }
     } else {
-        // lead field: resident rows for leads at their loaded position, recomputed rows for moved ones
-        for (size_t si = 0; si < S; ++si)
-            EKG_CUDA(cudaMemcpyAsync(E.W.p + si * L * D.apad, h->W0.p, L * D.apad * 4, cudaMemcpyDeviceToDevice, s));
-        if (nmove > 0) {
-            launch_lead_field(s, D, in.leads, nmove, (int)L, n_sims, E.W.p, (int)L);
-            ++launches;
-        }
-        launch_scale_w(s, D, E.W.p, in.layer_k, n_sims, E.Wp.p);
+        // lead field: recomputed rows for moved leads, the resident rows for leads at their loaded
+        // position (W, unscaled, is needed in full only for the k0 term)
+        if (h->any_k0)
+            for (size_t si = 0; si < S; ++si)
+                EKG_CUDA(cudaMemcpyAsync(E.W.p + si * L * D.apad, h->W0.p, L * D.apad * 4, cudaMemcpyDeviceToDevice, s));
+        launch_sim_lead_field(s, D, in.leads, nmove, (int)L, n_sims, in.layer_k, h->W0.p, E.W.p, E.Wp.p);
         ++launches;
         // k0 leaves a constant term only when some layer's k0 differs from zero (AP differences
         // within a layer cancel it)
