@@ -211,6 +211,175 @@ __global__ void __launch_bounds__(CC_T) k_contract_cuda(int steps, int nleads, i
     }
 }
 
+// ------------------------------------------------------------------ contraction, band form
+// Block per (simulation, K chunk, 16 leads).  With amin, amax the chunk's earliest and latest
+// finite activation times and x = k1 log2(e) tau, the steps of the chunk fall into three runs:
+//   zero    every AP has k1 (amin - t) log2 e >= 30.5 and (k1 - k4)(amin - t) log2 e >= 30.5:
+//           H < 2^-30 of its amplitude (the batched form's truncation), P = 0;
+//   steady  k1 (t - amax) log2 e >= 26.5 for every AP: the sigmoid is 1 in FP32 and
+//           P[t,l] = (1 - k3) 2^(-k4' (t - amax)) S0[l] + k3 S1[l],
+//           S0[l] = sum_a W'[l,a] 2^(-k4' (amax - at_a)), S1[l] = sum_a W'[l,a]  (k4' = k4 log2 e);
+//   band    the steps in between (the chunk's upstrokes, some 10 to 30 steps of 1 ms):
+//           P[t,l] = sum_a W'[l,a] H_a(t) evaluated directly in FP32, 32 steps x 8 AP slices.
+// APs with an infinite activation time (unreached cells, padding) contribute nothing.  Writes
+// partial[s][c][l][t] = P[t,l] F_L(t) in FP64 for every step, like the other contractions.
+constexpr int CB_THREADS = 256, CB_LB = 16, CB_CAP = CONTRACT_BAND_CAP, CB_ROWS = 32, CB_SLICES = CB_THREADS / CB_ROWS;
+constexpr size_t CB_SMEM = (size_t)CB_CAP * CB_LB * 4 + (size_t)CB_CAP * 8 + (size_t)CB_SLICES * CB_ROWS * (CB_LB + 1) * 4;
+__global__ void __launch_bounds__(CB_THREADS) k_contract_band(int steps, int nleads, int64_t apad, int nl,
+                                                             const float2 *__restrict__ t_hilo,
+                                                             const float2 *__restrict__ at_hilo,
+                                                             const int32_t *__restrict__ chunk_a0,
+                                                             const int32_t *__restrict__ chunk_a1,
+                                                             const int32_t *__restrict__ chunk_layer,
+                                                             const float *__restrict__ Wp,
+                                                             const float *__restrict__ layer_c,
+                                                             const double *__restrict__ F, int nchunks, int nlb,
+                                                             double *__restrict__ partial) {
+    extern __shared__ __align__(16) uint8_t cb_smem[];
+    float(*s_w)[CB_LB] = reinterpret_cast<float(*)[CB_LB]>(cb_smem);  // W'[a][l] of the chunk
+    float2 *s_at = reinterpret_cast<float2 *>(cb_smem + (size_t)CB_CAP * CB_LB * 4);
+    float(*s_red)[CB_ROWS][CB_LB + 1] = reinterpret_cast<float(*)[CB_ROWS][CB_LB + 1]>(s_at + CB_CAP);
+    __shared__ float s_ext[2][CB_THREADS / 32];
+    __shared__ float s_part[2][CB_THREADS / 32][CB_LB];
+    __shared__ float s_sum[2][CB_LB];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int c = blockIdx.x;
+    const int s = blockIdx.y / nlb, lb = blockIdx.y % nlb;
+    const int a0 = chunk_a0[c], na = chunk_a1[c] - a0, L = chunk_layer[c];
+    const int l0 = lb * CB_LB, nlh = min(CB_LB, nleads - l0);
+    const float4 kc = reinterpret_cast<const float4 *>(layer_c)[(size_t)s * nl + L];
+    double *out = partial + ((size_t)s * nchunks + c) * nleads * (size_t)steps + (size_t)l0 * steps;
+    const double *Fl = F + ((size_t)s * nl + L) * steps;
+
+    // the chunk: activation times, W' transposed to [a][l], the extreme finite activation times
+    float amin = INFINITY, amax = -INFINITY;
+    for (int i = tid; i < na; i += CB_THREADS) {
+        const float2 at = at_hilo[a0 + i];
+        s_at[i] = at;
+        if (isfinite(at.x)) {
+            amin = fminf(amin, at.x);
+            amax = fmaxf(amax, at.x);
+        }
+        float w[CB_LB];
+#pragma unroll
+        for (int l = 0; l < CB_LB; ++l) w[l] = l < nlh ? Wp[((size_t)s * nleads + l0 + l) * apad + a0 + i] : 0.f;
+#pragma unroll
+        for (int l = 0; l < CB_LB; l += 4)
+            *reinterpret_cast<float4 *>(&s_w[i][l]) = make_float4(w[l], w[l + 1], w[l + 2], w[l + 3]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        amin = fminf(amin, __shfl_xor_sync(0xffffffffu, amin, o));
+        amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    }
+    if (lane == 0) {
+        s_ext[0][warp] = amin;
+        s_ext[1][warp] = amax;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int w = 0; w < CB_THREADS / 32; ++w) {
+        amin = fminf(amin, s_ext[0][w]);
+        amax = fmaxf(amax, s_ext[1][w]);
+    }
+    const bool any_finite = amin <= amax;
+    const bool classify = any_finite && kc.x > 0.f && kc.y >= 0.f;
+    int nzero = 0, nsteady = 0;
+    for (int tb = 0; tb < steps; tb += CB_THREADS) {
+        const int t = tb + tid;
+        bool z = false, st = false;
+        if (t < steps && classify) {
+            const float tt = t_hilo[t].x;
+            z = kc.x * (amin - tt) >= 30.5f && (kc.x - kc.y) * (amin - tt) >= 30.5f;
+            st = kc.x * (tt - amax) >= 26.5f;
+        }
+        nzero += __syncthreads_count(z);
+        nsteady += __syncthreads_count(st);
+    }
+    if (!any_finite) nzero = steps;
+    const int tb0 = nzero, tb1 = steps - nsteady;  // band steps [tb0, tb1)
+
+    for (int i = tid; i < nzero * nlh; i += CB_THREADS) out[(size_t)(i / nzero) * steps + i % nzero] = 0.0;
+
+    if (nsteady > 0) {
+        // S0, S1 per lead: each thread its APs, then a shuffle and a shared-memory reduction
+        float u0[CB_LB], u1[CB_LB];
+#pragma unroll
+        for (int l = 0; l < CB_LB; ++l) u0[l] = u1[l] = 0.f;
+        for (int i = tid; i < na; i += CB_THREADS) {
+            const float2 at = s_at[i];
+            if (!isfinite(at.x)) continue;
+            const float g = ex2_approx(-kc.y * ((amax - at.x) - at.y));
+#pragma unroll
+            for (int l = 0; l < CB_LB; ++l) {
+                const float w = s_w[i][l];
+                u0[l] = fmaf(w, g, u0[l]);
+                u1[l] += w;
+            }
+        }
+#pragma unroll
+        for (int l = 0; l < CB_LB; ++l) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                u0[l] += __shfl_xor_sync(0xffffffffu, u0[l], o);
+                u1[l] += __shfl_xor_sync(0xffffffffu, u1[l], o);
+            }
+        }
+        if (lane == 0)
+#pragma unroll
+            for (int l = 0; l < CB_LB; ++l) {
+                s_part[0][warp][l] = u0[l];
+                s_part[1][warp][l] = u1[l];
+            }
+        __syncthreads();
+        if (tid < 2 * CB_LB) {
+            const int k = tid / CB_LB, l = tid % CB_LB;
+            float v = 0.f;
+            for (int w = 0; w < CB_THREADS / 32; ++w) v += s_part[k][w][l];
+            s_sum[k][l] = v;
+        }
+        __syncthreads();
+        for (int i = tid; i < nsteady * nlh; i += CB_THREADS) {
+            const int l = i / nsteady, t = tb1 + i % nsteady;
+            const float2 th = t_hilo[t];
+            const float e = kc.z * ex2_approx(-kc.y * ((th.x - amax) + th.y));
+            out[(size_t)l * steps + t] = (double)fmaf(e, s_sum[0][l], kc.w * s_sum[1][l]) * Fl[t];
+        }
+    }
+
+    // band: CB_ROWS steps per pass, warp = slice of the chunk's APs, lane = step
+    const int sa0 = na * warp / CB_SLICES, sa1 = na * (warp + 1) / CB_SLICES;
+    for (int tb = tb0; tb < tb1; tb += CB_ROWS) {
+        const float2 th = t_hilo[min(tb + lane, steps - 1)];
+        float acc[CB_LB];
+#pragma unroll
+        for (int l = 0; l < CB_LB; ++l) acc[l] = 0.f;
+        for (int i = sa0; i < sa1; ++i) {
+            const float2 at = s_at[i];
+            const float h = h_value(((th.x - at.x) + (th.y - at.y)), kc);
+#pragma unroll
+            for (int l = 0; l < CB_LB; l += 4) {
+                const float4 w = *reinterpret_cast<const float4 *>(&s_w[i][l]);
+                acc[l] = fmaf(w.x, h, acc[l]);
+                acc[l + 1] = fmaf(w.y, h, acc[l + 1]);
+                acc[l + 2] = fmaf(w.z, h, acc[l + 2]);
+                acc[l + 3] = fmaf(w.w, h, acc[l + 3]);
+            }
+        }
+#pragma unroll
+        for (int l = 0; l < CB_LB; ++l) s_red[warp][lane][l] = acc[l];
+        __syncthreads();
+        for (int i = tid; i < CB_ROWS * CB_LB; i += CB_THREADS) {
+            const int l = i / CB_ROWS, r = i % CB_ROWS, t = tb + r;
+            float v = 0.f;
+#pragma unroll
+            for (int w = 0; w < CB_SLICES; ++w) v += s_red[w][r][l];
+            if (t < tb1 && l < nlh) out[(size_t)l * steps + t] = (double)v * Fl[t];
+        }
+        __syncthreads();
+    }
+}
+
 // ecg[s][l][t] = k0w[s][l] + sum_c partial[s][c][l][t]: one block per (s, l, 32 steps); warp w
 // sums chunks c = w, w+8, ... for 32 consecutive steps (coalesced), then the 8 warp sums are added
 // in warp order, so the result does not depend on scheduling.  Also writes the float-float copy.
@@ -449,6 +618,21 @@ void launch_contract_cuda(cudaStream_t s, const HeartDev &h, const float *d_Wp, 
     k_contract_cuda<<<grid, CC_T, 0, s>>>(h.steps, h.nleads, h.apad, h.nlayers, h.t_hilo.p, h.at_hilo.p,
                                           h.chunk_a0.p, h.chunk_a1.p, h.chunk_layer.p, d_Wp, d_layer_c, d_F,
                                           h.nchunks, nlb, d_partial);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_contract_band(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,
+                          const double *d_F, int n_sims, double *d_partial) {
+    static bool attr = false;
+    if (!attr) {
+        EKG_CUDA(cudaFuncSetAttribute(k_contract_band, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CB_SMEM));
+        attr = true;
+    }
+    const int nlb = (h.nleads + CB_LB - 1) / CB_LB;
+    dim3 grid((unsigned)h.nchunks, (unsigned)(n_sims * nlb));
+    k_contract_band<<<grid, CB_THREADS, CB_SMEM, s>>>(h.steps, h.nleads, h.apad, h.nlayers, h.t_hilo.p, h.at_hilo.p,
+                                                      h.chunk_a0.p, h.chunk_a1.p, h.chunk_layer.p, d_Wp, d_layer_c,
+                                                      d_F, h.nchunks, nlb, d_partial);
     EKG_CUDA(cudaGetLastError());
 }
 

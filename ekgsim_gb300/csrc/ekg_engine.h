@@ -6,11 +6,15 @@
 #include "ekg_internal.h"
 #include "host_model.h"
 
+enum { EKG_CONTRACT_BAND = 0, EKG_CONTRACT_DENSE_UMMA = 1, EKG_CONTRACT_DENSE_CUDA = 2 };
+
 struct ekg_engine {
     int device = 0;
     cudaStream_t stream = nullptr;
     int chunk_len = 512;  // APs per K chunk of the contraction (multiple of 64)
-    bool umma = true;     // tensor-core contraction (EKG_CONTRACT=cuda selects the CUDA-core kernel)
+    // per-simulation contraction: band form (default), dense on the tensor cores (EKG_CONTRACT=umma)
+    // or dense on the CUDA cores (EKG_CONTRACT=cuda)
+    int contract = 0;
     bool batched = true;  // separable batched form for multi-simulation passes (EKG_BATCHED=0 disables)
     int batch_ctas = 0;   // target CTAs of the moved-lead GEMM (0 = one wave)
     bool graphs = true;   // replay repeated passes as CUDA graphs (EKG_GRAPHS=0 disables)

@@ -139,6 +139,7 @@ struct HeartDev {
     int64_t nvox = 0, naps = 0, apad = 0;  // apad: A rounded to a multiple of 64 per layer (K tiles)
     int nlayers = 0, nleads = 0, steps = 0, nhood = 0;
     int nchunks = 0;                        // K chunks (each inside one layer)
+    int chunk_max = 0;                      // APs of the longest chunk
     // per-AP (ordered by (layer, at), padded per layer to a multiple of 64)
     DBuf<float2> at_hilo;   // [apad] activation time split hi+lo (pad: +inf -> H = 0)
     DBuf<double> at;        // [apad]
@@ -222,6 +223,10 @@ void launch_sim_lead_field(cudaStream_t s, const HeartDev &h, const double *d_le
 void launch_k0_term(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
                     double *d_k0w);
 void launch_contract_cuda(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,
+                          const double *d_F, int n_sims, double *d_partial);
+// band form (zero / steady / band steps per chunk) for chunks of up to CONTRACT_BAND_CAP APs
+constexpr int CONTRACT_BAND_CAP = 512;
+void launch_contract_band(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,
                           const double *d_F, int n_sims, double *d_partial);
 void launch_contract_umma(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,
                           const double *d_F, int n_sims, double *d_partial, uint32_t *d_err);

@@ -373,6 +373,8 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
         }
     }
     D.nchunks = (int)c0.size();
+    D.chunk_max = 0;
+    for (size_t k = 0; k < c0.size(); ++k) D.chunk_max = std::max(D.chunk_max, c1[k] - c0[k]);
     D.at.alloc(apad);
     D.at_hilo.alloc(apad);
     D.a_layer.alloc(apad);
@@ -1053,8 +1055,12 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             EKG_CUDA(cudaMemsetAsync(E.k0w.p, 0, S * L * sizeof(double), s));
         }
         if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[1], s));
-        if (h->eng->umma) launch_contract_umma(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p, E.err.p);
-        else launch_contract_cuda(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p);
+        if (h->eng->contract == EKG_CONTRACT_BAND && D.chunk_max <= CONTRACT_BAND_CAP)
+            launch_contract_band(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p);
+        else if (h->eng->contract != EKG_CONTRACT_DENSE_CUDA)
+            launch_contract_umma(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p, E.err.p);
+        else
+            launch_contract_cuda(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p);
         if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[2], s));
         launch_reduce_ecg(s, D, E.partial.p, E.k0w.p, n_sims, E.ecg.p, E.ecg_ff.p);
         launches += 2;
@@ -1076,7 +1082,7 @@ std::vector<uint64_t> pass_signature(const ekg_heart *h, const PassPlan &P, int 
     std::vector<uint64_t> v = {(uint64_t)P.batch, (uint64_t)P.n_sims, (uint64_t)P.nmove, (uint64_t)P.J,
                                (uint64_t)P.two_bases, (uint64_t)P.rows, (uint64_t)P.rows_used, (uint64_t)P.ntiles,
                                (uint64_t)P.nitems, (uint64_t)ncl, (uint64_t)mode, (uint64_t)mark_static,
-                               (uint64_t)h->cpre_on, (uint64_t)h->any_k0, (uint64_t)h->eng->umma, (uint64_t)B.J,
+                               (uint64_t)h->cpre_on, (uint64_t)h->any_k0, (uint64_t)h->eng->contract, (uint64_t)B.J,
                                (uint64_t)B.max_ent, (uint64_t)B.ntt};
     const ekg_heart::PassInputs &in = h->in();
     for (const void *p : {(const void *)in.layer_k, (const void *)in.cpre, (const void *)in.leads, (const void *)in.k3,
@@ -1583,7 +1589,10 @@ int ekg_engine_create(int device, ekg_engine **out) {
         EKG_CHECK(device >= 0 && device < n, EKG_ERR_BAD_INPUT, "no such CUDA device");
         std::unique_ptr<ekg_engine> e(new ekg_engine());
         e->device = device;
-        if (const char *v = std::getenv("EKG_CONTRACT")) e->umma = std::string(v) != "cuda";
+        if (const char *v = std::getenv("EKG_CONTRACT"))
+            e->contract = std::string(v) == "cuda" ? EKG_CONTRACT_DENSE_CUDA
+                          : std::string(v) == "umma" ? EKG_CONTRACT_DENSE_UMMA
+                                                     : EKG_CONTRACT_BAND;
         if (const char *v = std::getenv("EKG_CHUNK")) e->chunk_len = std::max(64, std::atoi(v) / 64 * 64);
         if (const char *v = std::getenv("EKG_BATCHED")) e->batched = std::string(v) != "0";
         if (const char *v = std::getenv("EKG_BATCH_CTAS")) e->batch_ctas = std::atoi(v);

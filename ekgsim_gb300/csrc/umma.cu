@@ -193,11 +193,50 @@ __global__ void __launch_bounds__(UM_THREADS, 1) k_contract_umma(
     // producer roles: row (time step) and half of the 64-wide K stage
     const int row = tid & (UM_M - 1), half = tid >> 7;
     const int nkt = (a1 - a0) / UM_KT;
+    // B operand W'[l][a] (N rows l, 64 a's; thread -> (row n, 8-wide K chunk)) and the stage's
+    // activation times: loaded into registers one stage ahead, so that the global loads of stage
+    // k+1 are in flight while the producers evaluate stage k
+    constexpr int BPT = (N * (UM_KT / 8) + UM_THREADS - 1) / UM_THREADS;
+    float4 pw[BPT][2];
+    float2 pat = make_float2(0.f, 0.f);
+    auto load_stage = [&](int abase) {
+        if (tid < UM_KT) pat = at_hilo[abase + tid];
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) {
+            const int i = tid + k * UM_THREADS;
+            const int n = i % N, kcn = i / N, l = l0 + n;
+            if (i < N * (UM_KT / 8) && l < nleads) {
+                const float4 *src = reinterpret_cast<const float4 *>(Wp + ((size_t)s * nleads + l) * apad + abase + kcn * 8);
+                pw[k][0] = __ldg(src);
+                pw[k][1] = __ldg(src + 1);
+            } else {
+                pw[k][0] = pw[k][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        }
+    };
+    auto store_stage = [&](int b) {
+        if (tid < UM_KT) S.at[b][tid] = pat;
+#pragma unroll
+        for (int k = 0; k < BPT; ++k) {
+            const int i = tid + k * UM_THREADS;
+            if (i >= N * (UM_KT / 8)) break;
+            const int n = i % N, kcn = i / N;
+            uint4 hv, lv;
+            split2(pw[k][0].x, pw[k][0].y, hv.x, lv.x);
+            split2(pw[k][0].z, pw[k][0].w, hv.y, lv.y);
+            split2(pw[k][1].x, pw[k][1].y, hv.z, lv.z);
+            split2(pw[k][1].z, pw[k][1].w, hv.w, lv.w);
+            const uint32_t off = (uint32_t)((kcn * (N / 8) + n / 8) * 128 + (n % 8) * 16);
+            *reinterpret_cast<uint4 *>(S.b_hi[b] + off) = hv;
+            *reinterpret_cast<uint4 *>(S.b_lo[b] + off) = lv;
+        }
+    };
     bool ok = true;
     int g = 0;  // operand stages issued so far, over all band tiles of the block
     for (int j = jb0; j < jb1 && ok && nkt > 0; ++j) {
         const int t0 = j * UM_M;
         const float2 th = t_hilo[min(t0 + row, steps - 1)];
+        load_stage(a0);
         for (int kt = 0; kt < nkt; ++kt, ++g) {
             const int b = g & 1;
             if (g >= 2) {
@@ -208,31 +247,8 @@ __global__ void __launch_bounds__(UM_THREADS, 1) k_contract_umma(
                     break;
                 }
             }
-            const int abase = a0 + kt * UM_KT;
-            if (tid < UM_KT) S.at[b][tid] = at_hilo[abase + tid];
-            // B operand: W'[l][a] rows l (N), 64 a's; thread -> (row n, 8-wide K chunk)
-            for (int i = tid; i < N * (UM_KT / 8); i += UM_THREADS) {
-                const int n = i % N, kcn = i / N;
-                const int l = l0 + n;
-                float w[8];
-                if (l < nleads) {
-                    const float4 *src = reinterpret_cast<const float4 *>(Wp + ((size_t)s * nleads + l) * apad + abase + kcn * 8);
-                    const float4 p0 = __ldg(src), p1 = __ldg(src + 1);
-                    w[0] = p0.x; w[1] = p0.y; w[2] = p0.z; w[3] = p0.w;
-                    w[4] = p1.x; w[5] = p1.y; w[6] = p1.z; w[7] = p1.w;
-                } else {
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) w[q] = 0.f;
-                }
-                uint4 hv, lv;
-                split2(w[0], w[1], hv.x, lv.x);
-                split2(w[2], w[3], hv.y, lv.y);
-                split2(w[4], w[5], hv.z, lv.z);
-                split2(w[6], w[7], hv.w, lv.w);
-                const uint32_t off = (uint32_t)((kcn * (N / 8) + n / 8) * 128 + (n % 8) * 16);
-                *reinterpret_cast<uint4 *>(S.b_hi[b] + off) = hv;
-                *reinterpret_cast<uint4 *>(S.b_lo[b] + off) = lv;
-            }
+            store_stage(b);
+            if (kt + 1 < nkt) load_stage(a0 + (kt + 1) * UM_KT);
             __syncthreads();  // S.at visible
             // A operand: H_a(t) for this thread's row and 32 K columns
 #pragma unroll

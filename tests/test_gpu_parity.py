@@ -197,7 +197,8 @@ def test_bad_inputs(engine, tmp_path):
 
 
 def test_contract_kernels_agree(tmp_path):
-    """The tensor-core and CUDA-core contractions give the same ECG within the split tolerance."""
+    """The band-form, tensor-core and dense CUDA-core contractions give the same ECG within the
+    tolerance, and each matches the FP64 oracle."""
     from ekgsim_gb300.engine import Engine, Heart
     spec = synth.config(0)["spec"]
     grid = synth.ellipsoid_heart(spec)
@@ -205,7 +206,7 @@ def test_contract_kernels_agree(tmp_path):
     leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
     lk = layer_k_for(spec, 3)
     out = {}
-    for impl in ("umma", "cuda"):
+    for impl in ("band", "umma", "cuda"):
         os.environ["EKG_CONTRACT"] = impl
         try:
             e = Engine(0)
@@ -217,9 +218,10 @@ def test_contract_kernels_agree(tmp_path):
             os.environ.pop("EKG_CONTRACT", None)
     at, layer = O.activation(grid, tm)
     ref = O.run(layer, at, lk, leads, "3D4", 0.0, 600.0, 1.0)
-    assert rel_l2(out["umma"], ref) <= ECG_TOL
-    assert rel_l2(out["cuda"], ref) <= ECG_TOL
+    for impl in ("band", "umma", "cuda"):
+        assert rel_l2(out[impl], ref) <= ECG_TOL, impl
     assert rel_l2(out["umma"], out["cuda"]) <= ECG_TOL
+    assert rel_l2(out["band"], out["cuda"]) <= ECG_TOL
 
 
 def _batch_vs_oracle(engine, spec, steps, genes, layer_k_fn, two_bases=False):
