@@ -12,7 +12,8 @@ Workload (default): the batched configuration -- one resident 160^3 ellipsoid he
   roofline   the dominant kernel, timed alone with CUDA events: in the batched form the moved-lead
              operand kernel against the measured HBM copy bandwidth (its byte floor; the kernel is
              FP32-issue-bound), with the band GEMM's executed tensor rate beside it; in the
-             per-simulation form the lead contraction against the measured bf16 peak
+             per-simulation form the band-form contraction against the measured HBM copy
+             bandwidth (the bytes it moves), or a dense contraction against the bf16 peak
   cpu_baseline  the reference's CPU algorithm (FP64 port with the reference's cost structure,
              bit-identical results) run as one independent simulation per host core, on a bounded
              sample of the same heart (the first few time steps; cost is linear in steps)
@@ -389,6 +390,17 @@ def run_ours(args):
                         "executed_tflops": bm["gemm_flops"] / gemm_s / 1e12 if gemm_s > 0 else None,
                         "peak": bf16, "frac": bm["gemm_flops"] / gemm_s / 1e12 / bf16 if gemm_s > 0 else None,
                         "note": "band GEMM, three BF16 products per K step (hi/lo split), FP32 accumulation"}
+    elif bm["band_bytes"] > 0:
+        # per-simulation form, band-form contraction on the CUDA cores: bound by the bytes it moves
+        # (W' read, per-chunk FP64 partial sums written)
+        contract_s = bm["contract_ms"] / 1000.0 / args.steps
+        kernel = "k_contract_band"
+        achieved = bm["band_bytes"] / contract_s / 1e9
+        tr = profiled_traffic(kernel, wname)
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": tr * batch if tr is not None else None, "peak_source": src, "kernel": kernel,
+                "launch_ms": contract_s * 1000.0, "algorithmic_bytes": bm["band_bytes"],
+                "note": "zero / steady / band steps per chunk; the band is evaluated directly in FP32"}
     else:
         contract_s = bm["contract_ms"] / 1000.0 / args.steps  # one launch per step
         kernel = "k_contract_umma"

@@ -1310,9 +1310,16 @@ void benchmark(ekg_heart *h, int n_sims, const double *layer_k, const double *le
         op_bytes = (double)P.rows_used * D.apad * 4 + p1 * P.rows_used * 8 +
                    (double)D.nvox * 16 + (double)(D.nvox - D.n_interior) * 16 + (double)D.apad * 16;
     }
-    const double vals[10] = {total, contract, prep, tail, (double)g_launch_count, (double)P.nmove, P.batch ? 1.0 : 0.0,
-                             operand, gemm_flops, op_bytes};
-    for (int i = 0; i < n_out && i < 10; ++i) out[i] = vals[i];
+    double band_bytes = 0;
+    if (!P.batch && h->eng->contract == EKG_CONTRACT_BAND && h->dev.chunk_max <= CONTRACT_BAND_CAP) {
+        const HeartDev &D = h->dev;
+        const int nlb = (D.nleads + 15) / 16;
+        band_bytes = (double)n_sims * ((double)D.nleads * D.apad * 4 + (double)D.nchunks * D.nleads * D.steps * 8 +
+                                       (double)nlb * D.apad * 8);
+    }
+    const double vals[11] = {total, contract, prep, tail, (double)g_launch_count, (double)P.nmove, P.batch ? 1.0 : 0.0,
+                             operand, gemm_flops, op_bytes, band_bytes};
+    for (int i = 0; i < n_out && i < 11; ++i) out[i] = vals[i];
     for (auto &e : tm.ev) cudaEventDestroy(e);
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);

@@ -127,11 +127,11 @@ class Heart:
         lk = np.ascontiguousarray(layer_k, dtype=np.float64)
         n = lk.shape[0] if lk.ndim == 3 else 1
         lp = None if leads_zyx is None else np.ascontiguousarray(leads_zyx, dtype=np.float64)
-        out = np.zeros(10)
-        check(self._lib.ekg_heart_benchmark(self._h, n, dptr(lk), dptr(lp), warmup, iters, dptr(out), 10))
+        out = np.zeros(11)
+        check(self._lib.ekg_heart_benchmark(self._h, n, dptr(lk), dptr(lp), warmup, iters, dptr(out), 11))
         return dict(total_ms=out[0], contract_ms=out[1], prep_ms=out[2], tail_ms=out[3], launches=int(out[4]),
                     moved_leads=int(out[5]), batched=bool(out[6]), operand_ms=out[7], gemm_flops=out[8],
-                    operand_bytes=out[9], iters=iters, n_sims=n)
+                    operand_bytes=out[9], band_bytes=out[10], iters=iters, n_sims=n)
 
     # ------------------------------------------------------------------ evaluation
     def set_eval(self, base_aps, k_min, k_max, free_k, targets, target_offsets=None, **kw):

@@ -121,7 +121,9 @@ int ekg_simulate(ekg_heart *h, const double *layer_k, const double *leads_zyx, d
  * [4] kernel launches per pass, [5] leads whose lead field is recomputed per pass,
  * [6] 1 when the pass used the separable batched form, 0 for the per-simulation form,
  * batched form with moved leads only (else 0): [7] ms in the moved-lead operand kernel,
- * [8] tensor flops the band GEMM executes per pass, [9] bytes the operand kernel moves per pass.
+ * [8] tensor flops the band GEMM executes per pass, [9] bytes the operand kernel moves per pass;
+ * per-simulation form with the band-form contraction (else 0): [10] bytes that contraction has to
+ * move per pass (W' read, per-chunk FP64 partial sums written, activation times read).
  * No counterpart in the reference (it has no device); used by the benchmark. */
 int ekg_heart_benchmark(ekg_heart *h, int32_t n_sims, const double *layer_k, const double *leads, int32_t warmup,
                         int32_t iters, double *out, int32_t n_out);
