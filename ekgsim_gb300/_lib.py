@@ -83,6 +83,7 @@ SIGNATURES = {
     "ekg_eval_gene_bounds": (ctypes.c_int, [ctypes.c_void_p, P(c_double), P(c_double)]),
     "ekg_eval": (ctypes.c_int, [ctypes.c_void_p, P(c_double), c_int32, P(c_double), P(c_double), P(c_double),
                                 P(c_double), P(c_double)]),
+    "ekg_eval_simulated": (ctypes.c_int, [ctypes.c_void_p, P(c_int32)]),
     # raw addresses (array.ctypes.data): the batched call is on the per-step path, where ctypes
     # pointer objects cost more than the call itself
     "ekg_eval_batch": (ctypes.c_int, [ctypes.c_void_p, c_int32, ctypes.c_void_p, c_int32, ctypes.c_void_p,

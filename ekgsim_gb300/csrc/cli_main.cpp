@@ -187,6 +187,8 @@ int run(int argc, char **argv) {
     check(ekg_eval(heart, genes.data(), (int32_t)genes.size(), crit.data(), &viol, ecg.data(), lk.data(),
                    leads.data()));
     const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    int32_t simulated = 1;
+    check(ekg_eval_simulated(heart, &simulated));
     // writeOutputs (sim.cpp:977-991)
     {
         std::vector<std::string> names;
@@ -220,7 +222,9 @@ int run(int argc, char **argv) {
             std::ostringstream nm;  // x,y,z of the (moved) lead, default precision
             nm << leads[3 * l + 2] << "," << leads[3 * l + 1] << "," << leads[3 * l + 0];
             names.push_back(nm.str());
-            data.emplace_back(ecg.begin() + (size_t)l * info.steps, ecg.begin() + (size_t)(l + 1) * info.steps);
+            // a simulation the fast-approximation gate skipped has no measurement rows
+            if (simulated) data.emplace_back(ecg.begin() + (size_t)l * info.steps, ecg.begin() + (size_t)(l + 1) * info.steps);
+            else data.emplace_back();
         }
         double start = 0, length = 0, dt = 1;
         check(ekg_heart_time_axis(heart, &start, &length, &dt));

@@ -1150,8 +1150,8 @@ void run_pass(ekg_heart *h, const PassPlan &P, int ncl, int mode, bool mark_stat
     EKG_CUDA(cudaGraphLaunch(exec, s));
 }
 
-void assemble_criteria(const ekg_heart *h, const double *layer_k, const double *crit2, bool done,
-                       double approx_crit, const std::vector<double> &approx, double *out);
+void assemble_criteria(const ekg_heart *h, const double *crit2, bool done, double approx_crit,
+                       const std::vector<double> &approx, double endo_epi, double *out);
 
 // Queues one device pass from the current staging buffer (h->cur): plan, upload, the pass (a graph
 // replay) and the copies of its outputs (ECG to ecg_host; criterion values and the error word to
@@ -1226,10 +1226,11 @@ void complete_pending(ekg_heart *h, int slot) {
     if (!pd.criteria) return;
     const int nl = h->dev.nlayers, ncl = h->es.n_crit_leads;
     for (int s = 0; s < pd.n_sims; ++s) {
-        assemble_criteria(h, &pd.lk_all[(size_t)s * nl * 9], &pd.crit2[(size_t)s * ncl * 2], pd.done_flags[s] != 0,
-                          pd.acrit[s], pd.approx[s], pd.criteria + (size_t)s * h->es.n_criteria);
+        assemble_criteria(h, &pd.crit2[(size_t)s * ncl * 2], pd.done_flags[s] != 0, pd.acrit[s], pd.approx[s],
+                          pd.endo_epi[s], pd.criteria + (size_t)s * h->es.n_criteria);
         pd.violation[s] = pd.viol[s];
     }
+    if (pd.n_sims > 0) h->last_simulated = pd.done_flags[0] != 0;
 }
 void drain_pending(ekg_heart *h) {
     for (int i = 0; i < 2; ++i) complete_pending(h, (h->cur + i) % 2);  // oldest first
@@ -1365,8 +1366,8 @@ void run_fits(std::vector<LayerFitJob> &jobs) {
 
 // SimImplementation::calculateFitness (sim.cpp:600-702) from the device's per-lead comparison
 // values and peak positions, plus the host-side fast approximation and endo-epi terms.
-void assemble_criteria(const ekg_heart *h, const double *layer_k, const double *crit2, bool done,
-                       double approx_crit, const std::vector<double> &approx, double *out) {
+void assemble_criteria(const ekg_heart *h, const double *crit2, bool done, double approx_crit,
+                       const std::vector<double> &approx, double endo_epi, double *out) {
     const EvalSettings &es = h->es;
     EKG_CHECK(es.criteria_mode == 1, EKG_ERR_BAD_INPUT, "selected criteria mode is either not implemented yet or invalid");
     const int nm = es.n_crit_leads;
@@ -1391,15 +1392,19 @@ void assemble_criteria(const ekg_heart *h, const double *layer_k, const double *
         out[ci] = value;
         if (out[ci] < 0 || !std::isfinite(out[ci]) || !std::isnormal(out[ci])) out[ci] = 2e10;
     }
-    if (es.endo_epi_delay >= 0) {
-        const int nl = h->dev.nlayers;
-        double sd = 0.0;
-        for (double t = 1.0; t < 700.0; t += 1.0) {
-            const double dd = wohlfart(layer_k, t + es.endo_epi_delay) - wohlfart(layer_k + 9 * (nl - 1), t);
-            sd += dd * dd;
-        }
-        out[nc - 1] = sd;
+    if (es.endo_epi_delay >= 0) out[nc - 1] = endo_epi;
+}
+
+// the endo-epi criterion (sim.cpp:686-697): squared difference of the first layer's AP, delayed,
+// and the last layer's over 1 .. 699 ms
+double endo_epi_term(const ekg_heart *h, const double *layer_k) {
+    const WohlfartAP endo(layer_k), epi(layer_k + 9 * (h->dev.nlayers - 1));
+    double sd = 0.0;
+    for (double t = 1.0; t < 700.0; t += 1.0) {
+        const double dd = endo(t + h->es.endo_epi_delay) - epi(t);
+        sd += dd * dd;
     }
+    return sd;
 }
 
 // host comparison for the fast approximation (same formulas as the device criteria)
@@ -1455,10 +1460,11 @@ bool approx_gate(const ekg_heart *h, const double *layer_k, double &approx_crit,
     if (!(es.fast_is_crit || es.fast_limit < 2)) return true;
     const int nl = h->dev.nlayers;
     const size_t n = (size_t)(h->length / h->dt);
+    const WohlfartAP endo(layer_k), epi(layer_k + 9 * (nl - 1));
     approx.resize(n);
     for (size_t i = 0; i < n; ++i) {
         const double t = h->start + i * h->dt;
-        approx[i] = wohlfart(layer_k, t + es.fast_delay) - wohlfart(layer_k + 9 * (nl - 1), t);
+        approx[i] = endo(t + es.fast_delay) - epi(t);
     }
     approx_crit = compare_host(es.comparison_mode, approx, es.targets[0], es.target_offsets[0]);
     return !(approx_crit > es.fast_limit);
@@ -1490,8 +1496,19 @@ int64_t eval_submit(ekg_heart *h, int n_sims, const double *genes, int n_genes, 
         for (const LayerFit &f : fits) jobs.push_back(LayerFitJob{f, &pd.lk_all[(size_t)s * nl * 9]});
     }
     run_fits(jobs);
-    for (int s = 0; s < n_sims; ++s)
-        pd.done_flags[s] = approx_gate(h, &pd.lk_all[(size_t)s * nl * 9], pd.acrit[s], pd.approx[s]) ? 1 : 0;
+    // the fast-approximation gate and the endo-epi criterion: a few thousand FP64 AP values per
+    // simulation when enabled, spread over the host pool for larger batches
+    const bool gate = h->es.fast_is_crit || h->es.fast_limit < 2, endo = h->es.endo_epi_delay >= 0;
+    pd.endo_epi.assign(n_sims, 0.0);
+    auto extras = [&](size_t b, size_t e) {
+        for (size_t s = b; s < e; ++s) {
+            const double *lk = &pd.lk_all[s * nl * 9];
+            pd.done_flags[s] = approx_gate(h, lk, pd.acrit[s], pd.approx[s]) ? 1 : 0;
+            if (endo) pd.endo_epi[s] = endo_epi_term(h, lk);
+        }
+    };
+    if ((gate || endo) && n_sims >= 8) HostPool::get().run((size_t)n_sims, extras);
+    else extras(0, (size_t)n_sims);
     if (layer_k_out) std::copy(pd.lk_all.begin(), pd.lk_all.end(), layer_k_out);
     if (leads_out) std::copy(pd.leads_all.begin(), pd.leads_all.end(), leads_out);
     launch_pass(h, n_sims, pd.lk_all.data(), pd.leads_all.data(), ecg, h->es.n_crit_leads, h->es.comparison_mode);
@@ -1776,6 +1793,14 @@ int ekg_eval(ekg_heart *h, const double *genes, int32_t n_genes, double *criteri
     return guard([&] {
         EKG_CHECK(h && genes && criteria_out && violation_out, EKG_ERR_BAD_INPUT, "null argument");
         eval_many(h, 1, genes, n_genes, criteria_out, violation_out, ecg_out, layer_k_out, leads_out);
+    });
+}
+
+int ekg_eval_simulated(ekg_heart *h, int32_t *simulated_out) {
+    return guard([&] {
+        EKG_CHECK(h && simulated_out, EKG_ERR_BAD_INPUT, "null argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        *simulated_out = h->last_simulated ? 1 : 0;
     });
 }
 

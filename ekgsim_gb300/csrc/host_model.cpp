@@ -383,6 +383,13 @@ inline double wohlfart_rc(const double *k, const RepolConst &rc, double t) {
 
 double wohlfart(const double *k, double t) { return wohlfart_rc(k, repol_const(k), t); }
 
+WohlfartAP::WohlfartAP(const double *k) : k_(k) {
+    const RepolConst rc = repol_const(k);
+    lc_ = rc.lc;
+    ex_ = rc.ex;
+}
+double WohlfartAP::operator()(double t) const { return wohlfart_rc(k_, RepolConst{lc_, ex_}, t); }
+
 int GeneModel::n_free() const { return __builtin_popcount(free_mask & 0x1ffu); }
 
 namespace {

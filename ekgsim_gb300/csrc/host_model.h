@@ -74,6 +74,17 @@ void write_columns(const std::string &path, const std::vector<std::string> &name
 
 // ------------------------------------------------------------------ APs and genes
 double wohlfart(const double *k, double t);  // WohlfartPlus::operator[] (simlib/Wohlfart.h:195-203)
+// One AP evaluated at many times: the coefficient-only repolarisation constants are computed once;
+// every value equals wohlfart(k, t) bit for bit.
+class WohlfartAP {
+  public:
+    explicit WohlfartAP(const double *k);
+    double operator()(double t) const;
+
+  private:
+    const double *k_;
+    double lc_, ex_;
+};
 
 struct GeneModel {
     int interpolation = 2;  // 1 endo-epi, 2 endo-mid-epi

@@ -210,7 +210,8 @@ def ini_text(shape="model.matrix", transfer="conduction.matrix", points="leads.t
              targets="target.column", start=0, length=600, dt=1, nhood="3D4",
              base_aps=(BASE_AP, BASE_AP, BASE_AP), k_min=K_MIN, k_max=K_MAX,
              free_k=(5, 6, 7, 8), optimize_points=1, comparison=2, mid=0.6,
-             interpolation="endo-mid-epi", fast_limit=2, extra_opt: str = "") -> str:
+             interpolation="endo-mid-epi", fast_limit=2, fast_is_crit=0, fast_delay=10.0, peak=0,
+             endo_epi=-0.5, extra_opt: str = "") -> str:
     def vec(v):
         return ", ".join(repr(float(x)) for x in v)
     lines = [
@@ -247,13 +248,13 @@ def ini_text(shape="model.matrix", transfer="conduction.matrix", points="leads.t
         "mode = 1",
         f"targets filename = {targets}",
         f"comparison mode = {comparison}",
-        "endo-epi minimization criterion epi delay = -0.5",
-        "peak position is criterion = 0",
+        f"endo-epi minimization criterion epi delay = {endo_epi}",
+        f"peak position is criterion = {peak}",
         f"optimize measuring points = {optimize_points}",
         "population size = 100",
         "number of generations = 100",
-        "fast approximation is criterion = 0",
-        "fast approximation epi delay = 10.0",
+        f"fast approximation is criterion = {fast_is_crit}",
+        f"fast approximation epi delay = {fast_delay}",
         f"fast approximation limit = {fast_limit}",
     ]
     if extra_opt:

@@ -168,6 +168,10 @@ int ekg_eval_gene_bounds(ekg_heart *h, double *gene_min, double *gene_max);
  * layer_k_out (n_layers x 9) and leads_out (n_leads x 3, z,y,x) may be NULL. */
 int ekg_eval(ekg_heart *h, const double *genes, int32_t n_genes, double *criteria_out,
              double *violation_out, double *ecg_out, double *layer_k_out, double *leads_out);
+/* 1 when the last ekg_eval on this heart ran the simulation, 0 when the fast-approximation gate
+ * skipped it (SimImplementation::simulationDone, sim.cpp:712-748): its criteria then come from the
+ * approximation and the reference writes no ECG rows (ecg_out still receives the simulated ECG). */
+int ekg_eval_simulated(ekg_heart *h, int32_t *simulated_out);
 
 /* Batched evaluation of n_sims gene vectors on one resident heart (the reference's MPI farm of
  * independent evaluations, AMS-DEMO/ParallelFramework.h:226-520, folded into one device pass).

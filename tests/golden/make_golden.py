@@ -14,10 +14,15 @@ directory; the reference's test model is used for the last case):
               steepest-descent fit runs for 8 layers), 2 leads, 300 steps: criteria, violation,
               result.column and layer_aps.column (ekgSim_ref -out result -out layer_aps)
   endoepi5    32^3 ellipsoid, 5 layers, endo-epi interpolation, 2 leads, 200 steps: as layers10
+  extras24    as tiny24 with the optional criteria on: peak position, the fast approximation as a
+              criterion (epi delay 10 ms) and the endo-epi criterion (epi delay 2 ms)
+  gate24      as tiny24 with fast approximation limit 0.05, so that the approximation gate skips
+              the simulation and the criteria come from the approximation
   model24     the reference's own testRun model (93 x 124 x 124, 24 layers) with the README
               v>=0.1.4 example vector: criteria, violation, result.column (about 3 minutes)
 
-Usage: python tests/golden/make_golden.py [--reference DIR] [--skip-model24]
+Usage: python tests/golden/make_golden.py [--reference DIR] [--skip-model24] [--only NAME,...]
+(--only regenerates the named cases and keeps the others in golden.json)
 """
 from __future__ import annotations
 
@@ -95,14 +100,21 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--skip-model24", action="store_true")
+    ap.add_argument("--only", default="")
     args = ap.parse_args()
+    only = set(x for x in args.only.split(",") if x)
     subprocess.check_call(["sh", os.path.join(ROOT, "oracle", "build_ref.sh"), args.reference])
     ekgsim = os.path.join(ROOT, "oracle", "_ref", "ekgSim_ref")
     ref_dump = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
     meta = {"generator": "tests/golden/make_golden.py", "cases": {}}
+    if only:
+        with open(os.path.join(HERE, "golden.json")) as f:
+            meta = json.load(f)
     tmp = tempfile.mkdtemp(prefix="ekg_golden_")
 
     def synth_case(name, spec, steps, nlayers, genes, dump, outs=("result",), raw_at=False, **ini):
+        if only and name not in only:
+            return
         wd = os.path.join(tmp, name)
         synth.make_workload(wd, spec, steps, **ini)
         crit, viol = run_cli(ekgsim, wd, genes, outs)
@@ -136,8 +148,11 @@ def main():
     g5 = np.concatenate([g5[:8], g5[12:16]])  # endo-epi: two gene sets + 2 x 2 lead moves
     synth_case("endoepi5", s5, 200, 5, g5, dump=False, outs=("result", "layer_aps"),
                interpolation="endo-epi", base_aps=(synth.BASE_AP, synth.BASE_AP))
+    synth_case("extras24", s24, 200, 3, synth.genes_for(s24, 1, 0), dump=False, mid=0.6, peak=1, fast_is_crit=1,
+               endo_epi=2.0)
+    synth_case("gate24", s24, 200, 3, synth.genes_for(s24, 2, 0), dump=False, mid=0.6, fast_limit=0.05)
 
-    if not args.skip_model24:
+    if not args.skip_model24 and (not only or "model24" in only):
         wd = os.path.join(tmp, "model24")
         shutil.copytree(os.path.join(args.reference, "testRun"), wd)
         for f in os.listdir(wd):

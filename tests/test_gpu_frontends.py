@@ -62,7 +62,7 @@ def run_cli(wd, genes, outs=("result",)):
     return subprocess.run(args, cwd=wd, capture_output=True, text=True, timeout=300)
 
 
-@pytest.mark.parametrize("name", ["tiny24", "c64", "layers10", "endoepi5"])
+@pytest.mark.parametrize("name", ["tiny24", "c64", "layers10", "endoepi5", "extras24", "gate24"])
 def test_cli_matches_reference(name, tmp_path):
     c = make_case(name, tmp_path)
     outs = ("result", "layer_aps") if name in ("layers10", "endoepi5") else ("result",)
@@ -78,6 +78,9 @@ def test_cli_matches_reference(name, tmp_path):
     g = np.load(os.path.join(GOLD, f"{name}.npz"))
     head, res = read_column(os.path.join(str(tmp_path), "result.column"))
     assert head[0].startswith("#Comment: input=<") and head[-1].startswith("#Time[ms]\t")
+    if g["result"].size == 0:  # the fast-approximation gate skipped the simulation: headers only
+        assert res.size == 0
+        return
     assert res.shape == g["result"].shape
     assert np.allclose(res[:, 0], g["result"][:, 0])
     assert rel_l2(res[:, 1:], g["result"][:, 1:]) <= TOL

@@ -224,6 +224,50 @@ def test_contract_kernels_agree(tmp_path):
     assert rel_l2(out["band"], out["cuda"]) <= ECG_TOL
 
 
+@pytest.mark.parametrize("case", ["fine_dt", "k4_zero", "k4_negative", "sharp_k1", "slow_k1", "two_blobs"])
+def test_per_simulation_zero_steady_band_cases(case):
+    """The per-simulation contractions split each chunk's steps into zero, steady and band runs:
+    a fine time axis (bands of 100+ steps, several passes), k4 = 0 and k4 < 0 (no zero run),
+    sharp and slow upstrokes, and a heart with a second, unstimulated blob (activation time 0)."""
+    from ekgsim_gb300.engine import Engine, Heart
+    spec = synth.small_spec(24, n_leads=3)
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    steps, dt = 300, 1.0
+    lk = layer_k_for(spec, 1)
+    if case == "fine_dt":
+        steps, dt = 600, 0.1
+    elif case == "k4_zero":
+        lk[:, 4] = 0.0
+    elif case == "k4_negative":
+        lk[:, 4] = -0.02
+    elif case == "sharp_k1":
+        lk[:, 1] = 20.0
+    elif case == "slow_k1":
+        lk[:, 1] = 0.3
+    elif case == "two_blobs":
+        rng = np.random.Generator(np.random.PCG64(5))
+        grid = np.zeros((20, 22, 18), dtype=np.int32)
+        grid[2:9, 3:12, 2:10] = rng.integers(1, 4, size=(7, 9, 8))
+        grid[12:18, 10:20, 8:16] = rng.integers(1, 4, size=(6, 10, 8))
+        grid[3, 4, 3] = -abs(grid[3, 4, 3])
+        leads = np.array([[60.0, 11.0, 9.0], [10.0, 60.0, 9.0], [-40.0, 5.0, 30.0]])
+    at, layer = O.activation(grid, tm)
+    ref = O.run(layer, at, lk, leads, "3D4", 0.0, steps * dt, dt)
+    for impl in ("band", "umma"):
+        os.environ["EKG_CONTRACT"] = impl
+        try:
+            e = Engine(0)
+            h = Heart.create(e, grid, tm, leads, "3D4", 0.0, steps * dt, dt)
+            ecg = h.simulate(lk)
+            h.close()
+            e.close()
+        finally:
+            os.environ.pop("EKG_CONTRACT", None)
+        assert rel_l2(ecg, ref) <= ECG_TOL, impl
+
+
 def _batch_vs_oracle(engine, spec, steps, genes, layer_k_fn, two_bases=False):
     from ekgsim_gb300.engine import Heart
     grid = synth.ellipsoid_heart(spec)
