@@ -61,6 +61,23 @@ def test_criteria_and_printed_ecg(name, tmp_path):
     assert printed_close(ecg.T, res[:, 1:])
 
 
+@pytest.mark.parametrize("name", [c for c in ("extras24", "gate24") if c in META["cases"]])
+def test_optional_criteria_and_approximation_gate(name, tmp_path):
+    """extras24: peak position, fast approximation and endo-epi criteria together (the reference
+    writes the approximation at index n_leads, where the peak pairs then overwrite it); gate24: the
+    approximation gate skips the simulation, the criteria come from the approximation and the
+    reference writes no ECG rows."""
+    c, s = make_case(name, tmp_path)
+    g = np.load(os.path.join(GOLD, f"{name}.npz"))
+    crit, viol, ecg, lk, leads = O.evaluate(s, np.array(c["genes"]))
+    assert crit.shape == (len(c["criteria"]),)
+    assert printed_close(crit, np.array(c["criteria"]))
+    if name == "gate24":
+        assert g["result"].size == 0
+    else:
+        assert printed_close(ecg.T, g["result"][:, 1:])
+
+
 @pytest.mark.parametrize("name", [c for c in ("layers10", "endoepi5") if c in META["cases"]])
 def test_layer_aps_from_genes(name, tmp_path):
     """Gene -> layer AP construction incl. the steepest-descent interpolation (sim.cpp:751-916),
