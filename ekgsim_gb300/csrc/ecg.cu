@@ -220,12 +220,12 @@ __global__ void __launch_bounds__(CC_T) k_contract_cuda(int steps, int nleads, i
 //           P[t,l] = (1 - k3) 2^(-k4' (t - amax)) S0[l] + k3 S1[l],
 //           S0[l] = sum_a W'[l,a] 2^(-k4' (amax - at_a)), S1[l] = sum_a W'[l,a]  (k4' = k4 log2 e);
 //   band    the steps in between (the chunk's upstrokes, some 10 to 30 steps of 1 ms):
-//           P[t,l] = sum_a W'[l,a] H_a(t) evaluated directly in FP32, 32 steps x 8 AP slices.
+//           P[t,l] = sum_a W'[l,a] H_a(t) evaluated directly in FP32, 32 (or 16) steps per pass.
 // APs with an infinite activation time (unreached cells, padding) contribute nothing.  Writes
 // partial[s][c][l][t] = P[t,l] F_L(t) in FP64 for every step, like the other contractions.
-constexpr int CB_THREADS = 256, CB_LB = 16, CB_CAP = CONTRACT_BAND_CAP, CB_ROWS = 32, CB_SLICES = CB_THREADS / CB_ROWS;
-constexpr size_t CB_SMEM = (size_t)CB_CAP * CB_LB * 4 + (size_t)CB_CAP * 8 + (size_t)CB_SLICES * CB_ROWS * (CB_LB + 1) * 4;
-__global__ void __launch_bounds__(CB_THREADS) k_contract_band(int steps, int nleads, int64_t apad, int nl,
+constexpr int CB_THREADS = 256, CB_LB = 16, CB_CAP = CONTRACT_BAND_CAP;
+constexpr size_t CB_SMEM = (size_t)CB_CAP * CB_LB * 4 + (size_t)CB_CAP * 8 + (size_t)CB_THREADS * (CB_LB + 1) * 4;
+__global__ void __launch_bounds__(CB_THREADS, 4) k_contract_band(int steps, int nleads, int64_t apad, int nl,
                                                              const float2 *__restrict__ t_hilo,
                                                              const float2 *__restrict__ at_hilo,
                                                              const int32_t *__restrict__ chunk_a0,
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(CB_THREADS) k_contract_band(int steps, int nle
     extern __shared__ __align__(16) uint8_t cb_smem[];
     float(*s_w)[CB_LB] = reinterpret_cast<float(*)[CB_LB]>(cb_smem);  // W'[a][l] of the chunk
     float2 *s_at = reinterpret_cast<float2 *>(cb_smem + (size_t)CB_CAP * CB_LB * 4);
-    float(*s_red)[CB_ROWS][CB_LB + 1] = reinterpret_cast<float(*)[CB_ROWS][CB_LB + 1]>(s_at + CB_CAP);
+    float(*s_red)[CB_LB + 1] = reinterpret_cast<float(*)[CB_LB + 1]>(s_at + CB_CAP);  // [slice * rows + step]
     __shared__ float s_ext[2][CB_THREADS / 32];
     __shared__ float s_part[2][CB_THREADS / 32][CB_LB];
     __shared__ float s_sum[2][CB_LB];
@@ -299,38 +299,43 @@ __global__ void __launch_bounds__(CB_THREADS) k_contract_band(int steps, int nle
     if (!any_finite) nzero = steps;
     const int tb0 = nzero, tb1 = steps - nsteady;  // band steps [tb0, tb1)
 
-    for (int i = tid; i < nzero * nlh; i += CB_THREADS) out[(size_t)(i / nzero) * steps + i % nzero] = 0.0;
+    for (int t = tid; t < nzero; t += CB_THREADS)
+        for (int l = 0; l < nlh; ++l) out[(size_t)l * steps + t] = 0.0;
 
     if (nsteady > 0) {
-        // S0, S1 per lead: each thread its APs, then a shuffle and a shared-memory reduction
-        float u0[CB_LB], u1[CB_LB];
+        // S0, S1 per lead: each thread its APs, then a shuffle and a shared-memory reduction (eight
+        // leads at a time, which keeps the accumulators in registers)
+#pragma unroll 1
+        for (int lh = 0; lh < CB_LB; lh += 8) {
+            float u0[8], u1[8];
 #pragma unroll
-        for (int l = 0; l < CB_LB; ++l) u0[l] = u1[l] = 0.f;
-        for (int i = tid; i < na; i += CB_THREADS) {
-            const float2 at = s_at[i];
-            if (!isfinite(at.x)) continue;
-            const float g = ex2_approx(-kc.y * ((amax - at.x) - at.y));
+            for (int l = 0; l < 8; ++l) u0[l] = u1[l] = 0.f;
+            for (int i = tid; i < na; i += CB_THREADS) {
+                const float2 at = s_at[i];
+                if (!isfinite(at.x)) continue;
+                const float g = ex2_approx(-kc.y * ((amax - at.x) - at.y));
 #pragma unroll
-            for (int l = 0; l < CB_LB; ++l) {
-                const float w = s_w[i][l];
-                u0[l] = fmaf(w, g, u0[l]);
-                u1[l] += w;
+                for (int l = 0; l < 8; ++l) {
+                    const float w = s_w[i][lh + l];
+                    u0[l] = fmaf(w, g, u0[l]);
+                    u1[l] += w;
+                }
             }
+#pragma unroll
+            for (int l = 0; l < 8; ++l) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    u0[l] += __shfl_xor_sync(0xffffffffu, u0[l], o);
+                    u1[l] += __shfl_xor_sync(0xffffffffu, u1[l], o);
+                }
+            }
+            if (lane == 0)
+#pragma unroll
+                for (int l = 0; l < 8; ++l) {
+                    s_part[0][warp][lh + l] = u0[l];
+                    s_part[1][warp][lh + l] = u1[l];
+                }
         }
-#pragma unroll
-        for (int l = 0; l < CB_LB; ++l) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                u0[l] += __shfl_xor_sync(0xffffffffu, u0[l], o);
-                u1[l] += __shfl_xor_sync(0xffffffffu, u1[l], o);
-            }
-        }
-        if (lane == 0)
-#pragma unroll
-            for (int l = 0; l < CB_LB; ++l) {
-                s_part[0][warp][l] = u0[l];
-                s_part[1][warp][l] = u1[l];
-            }
         __syncthreads();
         if (tid < 2 * CB_LB) {
             const int k = tid / CB_LB, l = tid % CB_LB;
@@ -339,22 +344,28 @@ __global__ void __launch_bounds__(CB_THREADS) k_contract_band(int steps, int nle
             s_sum[k][l] = v;
         }
         __syncthreads();
-        for (int i = tid; i < nsteady * nlh; i += CB_THREADS) {
-            const int l = i / nsteady, t = tb1 + i % nsteady;
+        // thread per step: the step's factor once, then every lead (coalesced over the steps)
+        for (int t = tb1 + tid; t < steps; t += CB_THREADS) {
             const float2 th = t_hilo[t];
             const float e = kc.z * ex2_approx(-kc.y * ((th.x - amax) + th.y));
-            out[(size_t)l * steps + t] = (double)fmaf(e, s_sum[0][l], kc.w * s_sum[1][l]) * Fl[t];
+            const double f = Fl[t];
+            for (int l = 0; l < nlh; ++l)
+                out[(size_t)l * steps + t] = (double)fmaf(e, s_sum[0][l], kc.w * s_sum[1][l]) * f;
         }
     }
 
-    // band: CB_ROWS steps per pass, warp = slice of the chunk's APs, lane = step
-    const int sa0 = na * warp / CB_SLICES, sa1 = na * (warp + 1) / CB_SLICES;
-    for (int tb = tb0; tb < tb1; tb += CB_ROWS) {
-        const float2 th = t_hilo[min(tb + lane, steps - 1)];
+    // band: passes of 32 steps (16 when at most 16 remain), lane = step.  The chunk's APs are dealt
+    // round-robin to 256 / rows slices (slice j takes APs j, j + nsl, ...): in 32-step passes a
+    // warp is one slice (broadcast reads of s_w), in 16-step passes its two slices read
+    // neighbouring rows (no bank conflict).
+    for (int tb = tb0; tb < tb1;) {
+        const int rows = tb1 - tb <= 16 ? 16 : 32;
+        const int nsl = CB_THREADS / rows, r = lane & (rows - 1), sl = warp * (32 / rows) + lane / rows;
+        const float2 th = t_hilo[min(tb + r, steps - 1)];
         float acc[CB_LB];
 #pragma unroll
         for (int l = 0; l < CB_LB; ++l) acc[l] = 0.f;
-        for (int i = sa0; i < sa1; ++i) {
+        for (int i = sl; i < na; i += nsl) {
             const float2 at = s_at[i];
             const float h = h_value(((th.x - at.x) + (th.y - at.y)), kc);
 #pragma unroll
@@ -367,16 +378,16 @@ __global__ void __launch_bounds__(CB_THREADS) k_contract_band(int steps, int nle
             }
         }
 #pragma unroll
-        for (int l = 0; l < CB_LB; ++l) s_red[warp][lane][l] = acc[l];
+        for (int l = 0; l < CB_LB; ++l) s_red[sl * rows + r][l] = acc[l];
         __syncthreads();
-        for (int i = tid; i < CB_ROWS * CB_LB; i += CB_THREADS) {
-            const int l = i / CB_ROWS, r = i % CB_ROWS, t = tb + r;
+        for (int i = tid; i < rows * CB_LB; i += CB_THREADS) {
+            const int l = i / rows, rr = i % rows, t = tb + rr;
             float v = 0.f;
-#pragma unroll
-            for (int w = 0; w < CB_SLICES; ++w) v += s_red[w][r][l];
+            for (int w = 0; w < nsl; ++w) v += s_red[w * rows + rr][l];
             if (t < tb1 && l < nlh) out[(size_t)l * steps + t] = (double)v * Fl[t];
         }
         __syncthreads();
+        tb += rows;
     }
 }
 
