@@ -403,7 +403,9 @@ __global__ void __launch_bounds__(256) k_reduce_ecg(int steps, int nleads, int n
     const int w = threadIdx.x >> 5;
     const int l = blockIdx.y, s = blockIdx.z;
     double acc = 0.0;
+    // the additions stay in chunk order; unrolling lets four loads be in flight at once
     if (tt < steps)
+#pragma unroll 4
         for (int c = w; c < nchunks; c += 8) acc += partial[(((size_t)s * nchunks + c) * nleads + l) * steps + tt];
     red[w][threadIdx.x & 31] = acc;
     __syncthreads();
