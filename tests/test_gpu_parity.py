@@ -268,6 +268,49 @@ def test_per_simulation_zero_steady_band_cases(case):
         assert rel_l2(ecg, ref) <= ECG_TOL, impl
 
 
+def test_per_simulation_twenty_leads_three_moved(engine):
+    """Per-simulation form with two 16-lead blocks (the second partial) and an odd number of
+    moved leads (the field kernel evaluates moved leads in pairs)."""
+    spec = synth.small_spec(24, n_leads=20)
+    h, grid, tm, leads = make_heart(engine, spec, steps=250)
+    at, layer = O.activation(grid, tm)
+    lk = layer_k_for(spec, 2)
+    disp = np.zeros((20, 2))
+    disp[:3] = [[3.0, -2.0], [-1.5, 4.0], [2.5, 2.5]]
+    moved = O.move_leads(leads, disp)
+    assert np.array_equal(moved[3:], leads[3:]) and not np.array_equal(moved[:3], leads[:3])
+    ecg = h.simulate(lk, moved)
+    ref = O.run(layer, at, lk, moved, "3D4", 0.0, 250.0, 1.0)
+    assert ecg.shape == (20, 250)
+    assert rel_l2(ecg, ref) <= ECG_TOL
+
+
+def test_batch_fast_approximation_and_endo_epi_match_single(engine):
+    """The fast-approximation criterion and the endo-epi criterion of a batch (computed on the host
+    pool) equal those of single evaluations bit for bit; with a limit that gates every simulation,
+    all criteria come from the approximation."""
+    from ekgsim_gb300.engine import Heart
+    spec = synth.small_spec(24, n_leads=2)
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    h = Heart.create(engine, grid, tm, leads, "3D4", 0.0, 200.0, 1.0)
+    target = [t for t in synth.analytic_target(2, 200, 5)]
+    genes = np.stack([synth.genes_for(spec, r, 0) for r in range(12)])
+    for limit in (2.0, 0.05):
+        h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], target, mid_position=0.6,
+                   fast_is_criterion=True, fast_delay=10.0, fast_limit=limit, endo_epi_delay=2.0)
+        assert h.eval_shape()[1] == 4  # two leads, the approximation, endo-epi
+        crit_b, viol_b = h.eval_batch(genes)
+        for i in range(len(genes)):
+            crit1, viol1 = h.eval(genes[i])[:2]
+            assert crit_b[i][2] == crit1[2] and crit_b[i][3] == crit1[3]
+            assert np.allclose(crit_b[i], crit1, rtol=0, atol=1e-4)
+            assert viol_b[i] == viol1
+            if limit < 2.0 and crit1[2] > limit:  # gated: every lead's criterion is the approximation's
+                assert crit_b[i][0] == crit1[2] and crit_b[i][1] == crit1[2]
+
+
 def _batch_vs_oracle(engine, spec, steps, genes, layer_k_fn, two_bases=False):
     from ekgsim_gb300.engine import Heart
     grid = synth.ellipsoid_heart(spec)
