@@ -62,7 +62,8 @@ def run_cli(wd, genes, outs=("result",)):
     return subprocess.run(args, cwd=wd, capture_output=True, text=True, timeout=300)
 
 
-@pytest.mark.parametrize("name", ["tiny24", "c64", "layers10", "endoepi5", "extras24", "gate24"])
+@pytest.mark.parametrize("name", ["tiny24", "c64", "layers10", "endoepi5", "extras24", "gate24", "rms24", "devlin24",
+                                  "vcorr24"])
 def test_cli_matches_reference(name, tmp_path):
     c = make_case(name, tmp_path)
     outs = ("result", "layer_aps") if name in ("layers10", "endoepi5") else ("result",)
