@@ -20,6 +20,8 @@ directory; the reference's test model is used for the last case):
               the simulation and the criteria come from the approximation
   rms24, devlin24, vcorr24
               as tiny24 with comparison modes 1 (rms), 3 (devFromLinear) and 4 (vector correlation)
+  cube24, n2d4_24
+              as tiny24 with the dipole neighbourhoods "cube" (26 neighbours) and "2D4"
   model24     the reference's own testRun model (93 x 124 x 124, 24 layers) with the README
               v>=0.1.4 example vector: criteria, violation, result.column (about 3 minutes)
 
@@ -155,6 +157,8 @@ def main():
     synth_case("gate24", s24, 200, 3, synth.genes_for(s24, 2, 0), dump=False, mid=0.6, fast_limit=0.05)
     for i, (name, mode) in enumerate((("rms24", 1), ("devlin24", 3), ("vcorr24", 4))):
         synth_case(name, s24, 200, 3, synth.genes_for(s24, 3 + i, 0), dump=False, mid=0.6, comparison=mode)
+    synth_case("cube24", s24, 200, 3, synth.genes_for(s24, 6, 0), dump=False, mid=0.6, nhood="cube")
+    synth_case("n2d4_24", s24, 200, 3, synth.genes_for(s24, 7, 0), dump=False, mid=0.6, nhood="2D4")
 
     if not args.skip_model24 and (not only or "model24" in only):
         wd = os.path.join(tmp, "model24")
