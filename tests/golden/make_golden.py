@@ -22,6 +22,9 @@ directory; the reference's test model is used for the last case):
               as tiny24 with comparison modes 1 (rms), 3 (devFromLinear) and 4 (vector correlation)
   cube24, n2d4_24
               as tiny24 with the dipole neighbourhoods "cube" (26 neighbours) and "2D4"
+  start24     as tiny24 with the simulation starting at 40 ms (the targets are resampled from there)
+  k0_24       as tiny24 with resting potentials k0 = -86, -80, -90 in the three base APs (a constant
+              term across layers)
   model24     the reference's own testRun model (93 x 124 x 124, 24 layers) with the README
               v>=0.1.4 example vector: criteria, violation, result.column (about 3 minutes)
 
@@ -127,6 +130,8 @@ def main():
                          "n_stim": spec.n_stim, "seed": spec.seed},
                 "steps": steps, "ini": {k: v for k, v in ini.items() if k != "base_aps"},
                 "genes": [float(g) for g in genes], "criteria": crit, "violation": viol}
+        if "base_aps" in ini and name not in ("endoepi5",):
+            case["base_aps"] = [[float(v) for v in b] for b in ini["base_aps"]]
         arrays = {"result": read_column_text(os.path.join(wd, "result.column"))}
         if "layer_aps" in outs:
             arrays["layer_aps"] = read_column_text(os.path.join(wd, "layer_aps.column"))
@@ -159,6 +164,9 @@ def main():
         synth_case(name, s24, 200, 3, synth.genes_for(s24, 3 + i, 0), dump=False, mid=0.6, comparison=mode)
     synth_case("cube24", s24, 200, 3, synth.genes_for(s24, 6, 0), dump=False, mid=0.6, nhood="cube")
     synth_case("n2d4_24", s24, 200, 3, synth.genes_for(s24, 7, 0), dump=False, mid=0.6, nhood="2D4")
+    synth_case("start24", s24, 200, 3, synth.genes_for(s24, 8, 0), dump=False, mid=0.6, start=40)
+    k0_base = tuple([k0] + list(synth.BASE_AP[1:]) for k0 in (-86.0, -80.0, -90.0))
+    synth_case("k0_24", s24, 200, 3, synth.genes_for(s24, 9, 0), dump=False, mid=0.6, base_aps=k0_base)
 
     if not args.skip_model24 and (not only or "model24" in only):
         wd = os.path.join(tmp, "model24")

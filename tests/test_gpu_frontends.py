@@ -41,6 +41,8 @@ def make_case(name, tmp_path):
     ini = dict(c["ini"])
     if ini.get("interpolation") == "endo-epi":
         ini["base_aps"] = (synth.BASE_AP, synth.BASE_AP)
+    if "base_aps" in c:
+        ini["base_aps"] = tuple(tuple(b) for b in c["base_aps"])
     synth.make_workload(str(tmp_path), spec, c["steps"], **ini)
     return c
 
@@ -63,7 +65,7 @@ def run_cli(wd, genes, outs=("result",)):
 
 
 @pytest.mark.parametrize("name", ["tiny24", "c64", "layers10", "endoepi5", "extras24", "gate24", "rms24", "devlin24",
-                                  "vcorr24", "cube24", "n2d4_24"])
+                                  "vcorr24", "cube24", "n2d4_24", "start24", "k0_24"])
 def test_cli_matches_reference(name, tmp_path):
     c = make_case(name, tmp_path)
     outs = ("result", "layer_aps") if name in ("layers10", "endoepi5") else ("result",)

@@ -18,7 +18,7 @@ from oracle import oracle as O
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 META = json.load(open(os.path.join(GOLD, "golden.json")))
 SYNTH_CASES = [c for c in ("tiny24", "c64", "layers10", "endoepi5", "rms24", "devlin24", "vcorr24", "cube24",
-                           "n2d4_24") if c in META["cases"]]
+                           "n2d4_24", "start24", "k0_24") if c in META["cases"]]
 PRINT_RTOL = 1e-5  # %e with 6 significant digits
 
 
@@ -30,6 +30,8 @@ def make_case(name, tmp_path):
     ini = dict(c["ini"])
     if ini.get("interpolation") == "endo-epi":
         ini["base_aps"] = (synth.BASE_AP, synth.BASE_AP)
+    if "base_aps" in c:
+        ini["base_aps"] = tuple(tuple(b) for b in c["base_aps"])
     synth.make_workload(str(tmp_path), spec, c["steps"], **ini)
     return c, O.load_setup(str(tmp_path))
 
