@@ -190,3 +190,29 @@ def test_replica_timing_max_over_two_gloo_ranks():
         p.join(120)
     out = sorted(q.get(timeout=10) for _ in range(2))
     assert out == [(0, 3.0), (1, 3.0)]
+
+
+def test_band_form_run_bounds():
+    """The per-simulation band-form contraction replaces H_a(t) = sigma(k1 tau)((1-k3) e^{-k4 tau} + k3)
+    by 0 where k1' (amin - t) >= 30.5 and (k1' - k4')(amin - t) >= 30.5, and by its sigma = 1 form
+    where k1' (t - amax) >= 26.5 (k' = k log2 e).  In FP64 over the gene ranges, the dropped part
+    stays below 2^-30 of the AP's amplitude before the upstroke, and FP32 rounds the sigmoid to
+    exactly 1 after it."""
+    l2e = 1.4426950408889634
+    rng = np.random.Generator(np.random.PCG64(3))
+    k1 = rng.uniform(0.3, 20.0, 2000)
+    k4 = rng.uniform(0.0, 0.2, 2000) * np.minimum(1.0, k1 / 0.4)
+    k3 = rng.uniform(0.0, 1.0, 2000)
+    c1, c4 = k1 * l2e, k4 * l2e
+    ok = c1 > c4
+    # the first tau before the upstroke that the zero run covers, and a long way past it
+    tz = -np.maximum(30.5 / c1, 30.5 / np.where(ok, c1 - c4, np.inf))
+    for f in (1.0, 1.5, 4.0):
+        tau = tz * f
+        h = (1.0 - k3) * np.exp(-k4 * tau) + k3
+        sig = 1.0 / (1.0 + np.exp(-k1 * tau))
+        assert np.all((sig * h)[ok] <= 2.0 ** -30 * (1.0 + 1e-9))
+    # the first tau after the upstroke of the steady run: 1 + 2^-x rounds to 1 in FP32
+    ts = 26.5 / c1
+    e1 = np.exp2(-(c1 * ts)).astype(np.float32)
+    assert np.all(np.float32(1.0) + e1 == np.float32(1.0))
