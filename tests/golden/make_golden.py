@@ -25,6 +25,8 @@ directory; the reference's test model is used for the last case):
   start24     as tiny24 with the simulation starting at 40 ms (the targets are resampled from there)
   k0_24       as tiny24 with resting potentials k0 = -86, -80, -90 in the three base APs (a constant
               term across layers)
+  fixed24     as tiny24 with "optimize measuring points = 0" (12 genes, leads at their loaded positions)
+  n2d8_24     as tiny24 with the dipole neighbourhood "2D8"
   model24     the reference's own testRun model (93 x 124 x 124, 24 layers) with the README
               v>=0.1.4 example vector: criteria, violation, result.column (about 3 minutes)
 
@@ -167,6 +169,8 @@ def main():
     synth_case("start24", s24, 200, 3, synth.genes_for(s24, 8, 0), dump=False, mid=0.6, start=40)
     k0_base = tuple([k0] + list(synth.BASE_AP[1:]) for k0 in (-86.0, -80.0, -90.0))
     synth_case("k0_24", s24, 200, 3, synth.genes_for(s24, 9, 0), dump=False, mid=0.6, base_aps=k0_base)
+    synth_case("fixed24", s24, 200, 3, synth.genes_for(s24, 10, 0)[:12], dump=False, mid=0.6, optimize_points=0)
+    synth_case("n2d8_24", s24, 200, 3, synth.genes_for(s24, 11, 0), dump=False, mid=0.6, nhood="2D8")
 
     if not args.skip_model24 and (not only or "model24" in only):
         wd = os.path.join(tmp, "model24")

@@ -65,7 +65,7 @@ def run_cli(wd, genes, outs=("result",)):
 
 
 @pytest.mark.parametrize("name", ["tiny24", "c64", "layers10", "endoepi5", "extras24", "gate24", "rms24", "devlin24",
-                                  "vcorr24", "cube24", "n2d4_24", "start24", "k0_24"])
+                                  "vcorr24", "cube24", "n2d4_24", "start24", "k0_24", "fixed24", "n2d8_24"])
 def test_cli_matches_reference(name, tmp_path):
     c = make_case(name, tmp_path)
     outs = ("result", "layer_aps") if name in ("layers10", "endoepi5") else ("result",)

@@ -18,7 +18,7 @@ from oracle import oracle as O
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 META = json.load(open(os.path.join(GOLD, "golden.json")))
 SYNTH_CASES = [c for c in ("tiny24", "c64", "layers10", "endoepi5", "rms24", "devlin24", "vcorr24", "cube24",
-                           "n2d4_24", "start24", "k0_24") if c in META["cases"]]
+                           "n2d4_24", "start24", "k0_24", "fixed24", "n2d8_24") if c in META["cases"]]
 PRINT_RTOL = 1e-5  # %e with 6 significant digits
 
 
