@@ -86,6 +86,13 @@ public:
         return t;
     }
     void waitBatch(int64_t ticket) const { check(ekg_eval_batch_wait(h_, ticket)); }
+    // whether the last operator() ran its simulation (false when the fast-approximation gate skipped
+    // it: SimImplementation::simulationDone, sim.cpp:712-748)
+    bool simulationDone() const {
+        int32_t v = 1;
+        check(ekg_eval_simulated(h_, &v));
+        return v != 0;
+    }
     // getGeneParams (sim.cpp:523-580)
     void getGeneParams(size_t &numGenes, size_t &numCriteria, std::vector<double> &gMin, std::vector<double> &gMax) const {
         numGenes = genes_;
