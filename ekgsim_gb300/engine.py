@@ -169,6 +169,13 @@ class Heart:
             return crit, float(viol[0]), ecg, lk, leads
         return crit, float(viol[0])
 
+    def simulation_done(self) -> bool:
+        """Whether the last eval() ran its simulation (False when the fast-approximation gate
+        skipped it; ekg_eval_simulated)."""
+        v = ctypes.c_int32(1)
+        check(self._lib.ekg_eval_simulated(self._h, ctypes.byref(v)))
+        return bool(v.value)
+
     def _batch_args(self, genes, want_ecg, out):
         genes = np.ascontiguousarray(np.atleast_2d(genes), dtype=np.float64)
         n, g = genes.shape

@@ -85,6 +85,10 @@ class OptimizationFunction:
         crit, viol = self.heart.eval(np.asarray(solution, dtype=np.float64))
         return list(crit), viol
 
+    def simulation_done(self) -> bool:
+        """SimImplementation::simulationDone (sim.cpp:712-748) for the last call."""
+        return self.heart.simulation_done()
+
     def evaluate_batch(self, solutions: np.ndarray):
         crit, viol = self.heart.eval_batch(np.asarray(solutions, dtype=np.float64))
         return crit, viol

@@ -304,6 +304,7 @@ def test_batch_fast_approximation_and_endo_epi_match_single(engine):
         crit_b, viol_b = h.eval_batch(genes)
         for i in range(len(genes)):
             crit1, viol1 = h.eval(genes[i])[:2]
+            assert h.simulation_done() == (not crit1[2] > limit)
             assert crit_b[i][2] == crit1[2] and crit_b[i][3] == crit1[3]
             assert np.allclose(crit_b[i], crit1, rtol=0, atol=1e-4)
             assert viol_b[i] == viol1
