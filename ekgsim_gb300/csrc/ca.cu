@@ -316,9 +316,10 @@ __global__ void k_na_validate(size_t n, const int32_t *__restrict__ layers, NoAl
     int32_t starts = 0, bad = 0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const int32_t v = layers[i];
-        const int32_t a = v < 0 ? -v : v;
+        // widened before the negation: INT32_MIN is out of range, not a negative shift
+        const int64_t a = v < 0 ? -(int64_t)v : (int64_t)v;
         if (a > NOALLOC_MAX_LAYER) bad = 1;
-        else mask |= 1u << a;
+        else mask |= 1u << (uint32_t)a;
         starts += v < 0;
     }
     mask = __reduce_or_sync(0xffffffffu, mask);

@@ -127,6 +127,7 @@ struct ekg_heart {
         double *crit2 = nullptr;           // pinned per-lead criterion values and peaks
         size_t crit2_cap = 0;
         int n_sims = 0;
+        bool single = false;               // an ekg_eval call (sets simulationDone when handed over)
         std::vector<double> lk_all, leads_all, viol, acrit, endo_epi;
         std::vector<char> done_flags;
         std::vector<std::vector<double>> approx;
@@ -137,7 +138,7 @@ struct ekg_heart {
     cudaEvent_t copies_done = nullptr;  // the last pass's copies to the host are complete
     cudaEvent_t pass_end = nullptr;     // the last pass's work on the heart's stream is complete
     bool copies_pending = false;
-    // whether the simulation of the first evaluation last handed over ran (false when the
+    // whether the simulation of the last single evaluation (ekg_eval) ran (false when the
     // fast-approximation gate skipped it: SimImplementation::simulationDone, sim.cpp:743-748)
     bool last_simulated = true;
     ~ekg_heart() {

@@ -253,7 +253,8 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
             Part &P = parts[q];
             for (int64_t i = n * (int64_t)q / (int64_t)vparts; i < n * (int64_t)(q + 1) / (int64_t)vparts; ++i) {
                 const int32_t v = d->layers[i];
-                const int32_t a = v < 0 ? -v : v;
+                // widened before the negation, so that INT32_MIN is rejected rather than overflowing
+                const int64_t a = v < 0 ? -(int64_t)v : (int64_t)v;
                 if (a > 254) {
                     if (P.bad < 0) P.bad = i;
                     continue;
@@ -261,7 +262,7 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
                 lay[i] = (uint8_t)a;
                 st[i] = v < 0;
                 if (v < 0) P.starts.push_back(i);
-                P.nl = std::max(P.nl, a);
+                P.nl = std::max(P.nl, (int)a);
                 P.present[a] = 1;
             }
         }
@@ -1230,7 +1231,9 @@ void complete_pending(ekg_heart *h, int slot) {
                           pd.endo_epi[s], pd.criteria + (size_t)s * h->es.n_criteria);
         pd.violation[s] = pd.viol[s];
     }
-    if (pd.n_sims > 0) h->last_simulated = pd.done_flags[0] != 0;
+    // simulationDone() describes the last single evaluation (sim.cpp:742-745 sets it inside the
+    // call); batched evaluations leave it alone
+    if (pd.single && pd.n_sims == 1) h->last_simulated = pd.done_flags[0] != 0;
 }
 void drain_pending(ekg_heart *h) {
     for (int i = 0; i < 2; ++i) complete_pending(h, (h->cur + i) % 2);  // oldest first
@@ -1475,7 +1478,7 @@ bool approx_gate(const ekg_heart *h, const double *layer_k, double &approx_crit,
 // buffer; the criteria reach the caller's buffers when the evaluation is handed over
 // (eval_wait, or when its staging buffer is needed again two submissions later).
 int64_t eval_submit(ekg_heart *h, int n_sims, const double *genes, int n_genes, double *criteria, double *violation,
-                    double *ecg, double *layer_k_out, double *leads_out) {
+                    double *ecg, double *layer_k_out, double *leads_out, bool single) {
     std::lock_guard<std::mutex> lk(h->mu);
     const int slot = h->cur;
     complete_pending(h, slot);  // the staging buffer's previous evaluation
@@ -1515,6 +1518,7 @@ int64_t eval_submit(ekg_heart *h, int n_sims, const double *genes, int n_genes, 
     pd.busy = true;
     pd.ticket = ++h->next_ticket;
     pd.n_sims = n_sims;
+    pd.single = single;
     pd.criteria = criteria;
     pd.violation = violation;
     h->cur ^= 1;
@@ -1529,8 +1533,8 @@ void eval_wait(ekg_heart *h, int64_t ticket) {
 }
 
 void eval_many(ekg_heart *h, int n_sims, const double *genes, int n_genes, double *criteria, double *violation,
-               double *ecg, double *layer_k_out, double *leads_out) {
-    eval_wait(h, eval_submit(h, n_sims, genes, n_genes, criteria, violation, ecg, layer_k_out, leads_out));
+               double *ecg, double *layer_k_out, double *leads_out, bool single) {
+    eval_wait(h, eval_submit(h, n_sims, genes, n_genes, criteria, violation, ecg, layer_k_out, leads_out, single));
 }
 
 void set_eval(ekg_heart *h, const ekg_eval_config *c) {
@@ -1792,7 +1796,7 @@ int ekg_eval(ekg_heart *h, const double *genes, int32_t n_genes, double *criteri
              double *ecg_out, double *layer_k_out, double *leads_out) {
     return guard([&] {
         EKG_CHECK(h && genes && criteria_out && violation_out, EKG_ERR_BAD_INPUT, "null argument");
-        eval_many(h, 1, genes, n_genes, criteria_out, violation_out, ecg_out, layer_k_out, leads_out);
+        eval_many(h, 1, genes, n_genes, criteria_out, violation_out, ecg_out, layer_k_out, leads_out, true);
     });
 }
 
@@ -1808,7 +1812,7 @@ int ekg_eval_batch(ekg_heart *h, int32_t n_sims, const double *genes, int32_t n_
                    double *violation_out, double *ecg_out) {
     return guard([&] {
         EKG_CHECK(h && genes && criteria_out && violation_out && n_sims >= 1, EKG_ERR_BAD_INPUT, "bad argument");
-        eval_many(h, n_sims, genes, n_genes, criteria_out, violation_out, ecg_out, nullptr, nullptr);
+        eval_many(h, n_sims, genes, n_genes, criteria_out, violation_out, ecg_out, nullptr, nullptr, false);
     });
 }
 
@@ -1817,7 +1821,8 @@ int ekg_eval_batch_submit(ekg_heart *h, int32_t n_sims, const double *genes, int
     return guard([&] {
         EKG_CHECK(h && genes && criteria_out && violation_out && ticket_out && n_sims >= 1, EKG_ERR_BAD_INPUT,
                   "bad argument");
-        *ticket_out = eval_submit(h, n_sims, genes, n_genes, criteria_out, violation_out, ecg_out, nullptr, nullptr);
+        *ticket_out =
+            eval_submit(h, n_sims, genes, n_genes, criteria_out, violation_out, ecg_out, nullptr, nullptr, false);
     });
 }
 

@@ -15,7 +15,7 @@
 
 namespace ekg {
 void eval_many(ekg_heart *h, int n_sims, const double *genes, int n_genes, double *criteria, double *violation,
-               double *ecg, double *layer_k_out, double *leads_out);
+               double *ecg, double *layer_k_out, double *leads_out, bool single);
 int64_t eval_bytes_per_sim(const ekg_heart *h);
 int64_t eval_bytes_held(const ekg_heart *h);
 }  // namespace ekg
@@ -140,7 +140,7 @@ void worker_loop(ekg_server *s) {
                 for (int i = 0; i < n; ++i) std::copy(batch[b0 + i].genes.begin(), batch[b0 + i].genes.end(),
                                                       g.begin() + (size_t)i * n_genes);
                 int rc = guard([&] { eval_many(h, n, g.data(), n_genes, crit.data(), viol.data(), ecg.data(),
-                                               nullptr, nullptr); });
+                                               nullptr, nullptr, false); });
                 std::string msg = rc ? std::string(ekg_last_error()) : std::string();
                 for (int i = 0; i < n; ++i) {
                     Result &r = res[b0 + i];

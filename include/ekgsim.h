@@ -235,10 +235,12 @@ int ekg_server_set_free_bytes_provider(ekg_server *s, uint64_t (*fn)(void *ctx),
  *             unreachable), bit-identical to ekg_heart_activation
  * Scratch is one fixed device array inside the library (about 600 KB per GPU that loads it, held
  * until the process exits); grids of more than 65536 tiles of 8x8x8 cells are rejected with
- * EKG_ERR_BAD_INPUT.  The first call on a device looks the array's device address up, so make the
- * first call before any stream capture.  Calls run on the legacy default stream and return when
- * the result is in d_at; calls in one process are serialised, and device work of two calls must
- * not overlap (they share the array). */
+ * EKG_ERR_BAD_INPUT.  The first call on a device looks the array's device address up.  Every call
+ * makes synchronous copies and waits for its kernels on the legacy default stream, so it must not
+ * be called while any stream capture is in progress in the process.  The calls do not wait for
+ * work on other streams: finish (or synchronise) every write to d_layers and every use of d_at
+ * before the call.  A call returns when the result is in d_at; calls in one process are
+ * serialised, and device work of two calls must not overlap (they share the array). */
 int ekg_activation_noalloc(int32_t nz, int32_t ny, int32_t nx, const int32_t *d_layers, int32_t n_transfer,
                            const double *transfer, double *d_at, int32_t *rounds_out);
 

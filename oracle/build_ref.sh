@@ -8,8 +8,10 @@
 #   ekgSim_ref : the unmodified ekgSim CLI (main.cpp, sim.cpp, simlib, copyOfLibs)
 #   ref_dump   : oracle/ref_dump.cpp linked with simlib, writes raw FP64 results
 set -e
-REF=${1:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+# the reference sources: the first argument, else $EKGSIM_REFERENCE, else a checkout named
+# "reference" beside this repository
+REF=${1:-${EKGSIM_REFERENCE:-$(dirname "$(dirname "$HERE")")/reference}}
 OUT="$HERE/_ref"
 mkdir -p "$OUT"
 FLAGS="-O2 -std=c++11 -DNDEBUG -DNO_MPI -ffp-contract=off -w -I$REF -I$REF/copyOfLibs -I$REF/simlib"

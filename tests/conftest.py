@@ -1,7 +1,6 @@
 import os
 import sys
 
-import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -14,16 +13,6 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "slow: long CPU test")
 
 
-def has_gpu() -> bool:
-    try:
-        import ctypes
-        lib = ctypes.CDLL("libcudart.so") if False else None  # noqa: F841
-        import torch  # noqa: F401
-        return torch.cuda.is_available()
-    except Exception:
-        return False
-
-
 @pytest.fixture(scope="session")
 def engine():
     from ekgsim_gb300.engine import Engine
@@ -31,8 +20,8 @@ def engine():
     yield e
 
 
-REF_ROOT = "/root/reference"
-
-
-def reference_available() -> bool:
-    return os.path.isdir(REF_ROOT)
+def reference_dir():
+    """Sources of the reference simulator, when present: $EKGSIM_REFERENCE, else a checkout named
+    ``reference`` beside this repository; None when neither exists (as on the GPU machines)."""
+    from oracle.refpath import reference_dir as rd
+    return rd()

@@ -1,6 +1,7 @@
 """Generate the golden fixtures in tests/golden/ by running the reference itself.
 
-Needs the reference sources (default /root/reference) to build oracle/_ref/ekgSim_ref (the
+Needs the reference sources ($EKGSIM_REFERENCE, else a checkout named ``reference`` beside this
+repository) to build oracle/_ref/ekgSim_ref (the
 unmodified ekgSim command line) and oracle/_ref/ref_dump (a driver over the reference's own
 simulator library that writes raw FP64 activation times and ECGs); see oracle/build_ref.sh.
 
@@ -107,11 +108,16 @@ def run_dump(ref_dump, wd, genes, nlayers):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=None)
     ap.add_argument("--skip-model24", action="store_true")
     ap.add_argument("--only", default="")
     args = ap.parse_args()
     only = set(x for x in args.only.split(",") if x)
+    if args.reference is None:
+        from oracle.refpath import reference_dir
+        args.reference = reference_dir()
+    if args.reference is None:
+        raise SystemExit("reference sources not found: pass --reference or set EKGSIM_REFERENCE")
     subprocess.check_call(["sh", os.path.join(ROOT, "oracle", "build_ref.sh"), args.reference])
     ekgsim = os.path.join(ROOT, "oracle", "_ref", "ekgSim_ref")
     ref_dump = os.path.join(ROOT, "oracle", "_ref", "ref_dump")

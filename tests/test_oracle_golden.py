@@ -14,6 +14,7 @@ import pytest
 
 from ekgsim_gb300 import synth
 from oracle import oracle as O
+from oracle.refpath import reference_dir
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 META = json.load(open(os.path.join(GOLD, "golden.json")))
@@ -95,14 +96,14 @@ def test_layer_aps_from_genes(name, tmp_path):
         assert printed_close(got, curves[:, 1 + i], atol=1e-9), i
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/testRun") or "model24" not in META["cases"],
+@pytest.mark.skipif(reference_dir() is None or "model24" not in META["cases"],
                     reason="the reference's test model is not present")
 def test_reference_test_model_24_layers(tmp_path):
     """The reference's own test model (93 x 124 x 124, 24 layers, 555,868 voxels) with the README
     example vector: criteria, violation and the full printed ECG."""
     import shutil
     wd = str(tmp_path / "testRun")
-    shutil.copytree("/root/reference/testRun", wd)
+    shutil.copytree(os.path.join(reference_dir(), "testRun"), wd)
     for f in os.listdir(wd):
         os.chmod(os.path.join(wd, f), 0o644)
     c = META["cases"]["model24"]
