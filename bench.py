@@ -198,16 +198,12 @@ def cpu_farm(spec, steps, genes, sample_steps: int, threads: int):
     return sims_per_s, dt, sample
 
 
-def served_run(seconds: float = 4.0, rate: float = 500.0, seed: int = 3000, max_wait_us: int = 0):
-    """Served configuration: a Poisson stream of evaluation requests over four resident hearts
-    (48^3, 96^3, 144^3, 192^3 scaled ellipsoids, 3 layers, 12 leads, 600 steps); continuous batching
-    in the engine's request loop.  With max_wait_us = 0 a pass starts as soon as its heart is idle
-    and requests that arrive during a pass form the next one.  Returns latency percentiles (submit ->
-    result), throughput and the mean number of requests per device pass."""
+def served_hearts(eng):
+    """The four resident hearts of the served configuration (48^3, 96^3, 144^3, 192^3 scaled
+    ellipsoids, 3 layers, 12 leads, 600 steps), evaluation settings set."""
     from ekgsim_gb300 import engine as E
     from ekgsim_gb300 import synth
     cfg = synth.config(3)
-    eng = E.Engine(0)
     hearts, specs = [], []
     for spec in cfg["hearts"]:
         grid = synth.ellipsoid_heart(spec)
@@ -218,37 +214,111 @@ def served_run(seconds: float = 4.0, rate: float = 500.0, seed: int = 3000, max_
                    [t for t in synth.analytic_target(spec.n_leads, cfg["steps"], spec.seed + 999)], mid_position=0.6)
         hearts.append(h)
         specs.append(spec)
-    srv = E.Server(eng, max_batch=256, max_wait_us=max_wait_us)
-    ids = [srv.add_heart(h) for h in hearts]
+    return hearts, specs
+
+
+def served_stream(srv, ids, specs, rate: float, n: int, seed: int, n_crit: int):
+    """One Poisson stream of n requests at `rate` per second over the hearts (uniformly), submitted
+    through ekg_server_submit_many as they fall due (the loop wakes every ~50 us) and handed over
+    with ekg_server_poll_many.  Latency is the engine's submit -> result time per request."""
+    from ekgsim_gb300 import synth
     rng = np.random.Generator(np.random.PCG64(seed))
-    n = int(seconds * rate)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
-    which = rng.integers(0, len(hearts), size=n)
-    genes = [synth.genes_for(specs[w], i, 3) for i, w in enumerate(which)]
-    # warm each heart's batched path once
-    for i, hid in enumerate(ids):
-        srv.poll(srv.submit(hid, synth.genes_for(specs[i], 10_000 + i, 3)), hid, wait_ms=120000)
-    submitted = []
+    which = rng.integers(0, len(ids), size=n).astype(np.int32)
+    # 16 README-bounded genes per request, zeros for the displacements of leads 2..11
+    genes = np.zeros((n, 12 + 2 * specs[0].n_leads))
+    genes[:, :16] = synth.GENE_MIN + (synth.GENE_MAX - synth.GENE_MIN) * rng.random((n, 16))
+    hid = np.array([ids[w] for w in which], dtype=np.int32)
+    rids = np.zeros(n, dtype=np.uint64)
+    sub_t = np.zeros(n)
     t0 = time.perf_counter()
-    for i in range(n):
+    i = 0
+    while i < n:
         now = time.perf_counter() - t0
-        if arrivals[i] > now:
-            time.sleep(arrivals[i] - now)
-        submitted.append((srv.submit(ids[which[i]], genes[i]), ids[which[i]]))
-    lat, batch = [], []
-    for rid, hid in submitted:
-        out = srv.poll(rid, hid, wait_ms=120000)
-        lat.append(out[3]["total_ms"])
-        batch.append(out[3]["batch"])
-    t1 = time.perf_counter()
+        j = int(np.searchsorted(arrivals, now, side="right"))
+        if j > i:
+            rids[i:j] = srv.submit_many(hid[i:j], genes[i:j])
+            sub_t[i:j] = now
+            i = j
+        else:
+            time.sleep(min(5e-5, max(0.0, arrivals[i] - now)))
+    status, crit, viol, total, batch = srv.poll_many(rids, n_crit, wait_ms=600000)
+    assert (status == 0).all(), "served requests failed"
+    done_t = sub_t + total / 1000.0
+    span = float(done_t.max() - min(arrivals[0], sub_t[0]))
+    return {"rate_req_s": rate, "requests": n, "throughput_req_s": n / span,
+            "p50_ms": float(np.percentile(total, 50)), "p99_ms": float(np.percentile(total, 99)),
+            "mean_batch": float(np.mean(batch))}
+
+
+def served_run(rates=(500.0, 5e3, 5e4, 2e5, 1e6), seconds: float = 1.0, max_requests: int = 200_000,
+               seed: int = 3000, max_wait_us: int = 0):
+    """Served configuration: Poisson streams of evaluation requests over four resident hearts,
+    continuous batching in the engine's request loop (each heart's next pass is prepared and queued
+    while its current one runs; with max_wait_us = 0 a pass starts as soon as its heart has nothing on
+    the device).  One stream per offered rate; the highest rate saturates the engine, so its
+    throughput is the served form's capacity."""
+    from ekgsim_gb300 import engine as E
+    from ekgsim_gb300 import synth
+    eng = E.Engine(0)
+    hearts, specs = served_hearts(eng)
+    srv = E.Server(eng, max_batch=256, max_wait_us=max_wait_us, keep_ecg=False)
+    ids = [srv.add_heart(h) for h in hearts]
+    _, nc = hearts[0].eval_shape()
+    # warm each heart's batched path (graph capture, buffers) with a few full passes
+    for k in range(3):
+        hid = np.repeat(np.array(ids, dtype=np.int32), 256)
+        g = np.stack([synth.genes_for(specs[i // 256], 20_000 + k * 1024 + i, 3) for i in range(hid.size)])
+        st = srv.poll_many(srv.submit_many(hid, g), nc, wait_ms=600000)[0]
+        assert (st == 0).all()
+    sweep = []
+    for r_i, rate in enumerate(rates):
+        n = int(min(max_requests, max(200, rate * seconds)))
+        sweep.append(served_stream(srv, ids, specs, rate, n, seed + r_i, nc))
     srv.close()
     for h in hearts:
         h.close()
     eng.close()
-    lat = np.array(lat)
-    return {"requests": n, "rate_req_s": rate, "throughput_req_s": n / (t1 - t0),
-            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "mean_batch": float(np.mean(batch)), "max_wait_us": max_wait_us, "hearts": [s.n for s in specs]}
+    sat = max(sweep, key=lambda d: d["throughput_req_s"])
+    return {"hearts": [s.n for s in specs], "max_batch": 256, "max_wait_us": max_wait_us,
+            "form": "per-heart dispatchers, two passes in flight per heart, criteria only (no ECG copies)",
+            "sweep": sweep, "saturated": sat}
+
+
+def parity_check(E, eng, grid, tm, leads_zyx, spec, steps, genes, target, ecg, heart, lk, moved, n_oracle):
+    """Parity of the timed batch's results, by a stated policy:
+    - every result against the engine's per-simulation form (a second heart on an engine with the
+      batched form off: band-form FP32 contraction, a different algorithm from the batched form's
+      static-lead basis and tensor-core band GEMM), ECG rel-L2 per result;
+    - n_oracle results spread over the batch (first, last, middle, seeded random others) against
+      the FP64 oracle (the reference's algorithm, pinned bit for bit to the compiled reference);
+    - activation times of the heart against the oracle's, bitwise."""
+    from oracle import oracle as O
+    batch = len(genes)
+    at_ref, layer = O.activation(grid, tm)
+    at_gpu = heart.activation()
+    mism = int(np.count_nonzero(at_gpu.view(np.int64) != at_ref.view(np.int64)))
+    pick = sorted(set([0, batch - 1, batch // 2] + [int(x) for x in np.random.Generator(
+        np.random.PCG64(7)).choice(batch, size=min(batch, max(0, n_oracle - 3)), replace=False)]))[:max(1, n_oracle)]
+    rels = []
+    for i in pick:
+        ref = O.run(layer, at_ref, lk[i], moved[i], "3D4", 0.0, float(steps), 1.0)
+        rels.append(float(np.linalg.norm(ecg[i] - ref) / np.linalg.norm(ref)))
+    os.environ["EKG_BATCHED"] = "0"
+    try:
+        eng2 = E.Engine(0)
+    finally:
+        os.environ.pop("EKG_BATCHED", None)
+    h2 = E.Heart.create(eng2, grid, tm, leads_zyx, "3D4", 0.0, float(steps), 1.0)
+    h2.set_eval(*heart.eval_args[0], **heart.eval_args[1])
+    _, _, ecg2 = h2.eval_batch(genes, want_ecg=True)
+    cross = [float(np.linalg.norm(ecg[i] - ecg2[i]) / np.linalg.norm(ecg2[i])) for i in range(batch)]
+    h2.close()
+    eng2.close()
+    return {"policy": "every result vs the per-simulation form; a spread sample vs the FP64 oracle; activation "
+                      "times bitwise", "ecg_rel_l2_max": max(rels), "checked_sims": len(rels), "oracle_sims": pick,
+            "cross_form_rel_l2_max": max(cross), "cross_checked": batch, "at_mismatch": mism,
+            "tolerance": 1e-4}
 
 
 def host_cores() -> int:
@@ -258,29 +328,70 @@ def host_cores() -> int:
         return os.cpu_count() or 1
 
 
+def workload_config(spec, steps, batch, wname, n_voxels, n_aps, world):
+    """The `config` object both arms print, so that their lines describe the same workload."""
+    return {"workload": wname, "grid": spec.n, "voxels": int(n_voxels), "aps": int(n_aps), "leads": spec.n_leads,
+            "steps": steps, "batch": batch, "layers": spec.n_layers,
+            "l2": "inputs larger than L2 (per-step lead fields and partials exceed 129 MB)",
+            "parallelism": f"replicas{world}"}
+
+
 def run_reference(args):
+    """The reference's CPU algorithm (the oracle's port with the reference's own cost structure:
+    every cell and neighbour AP evaluated per step, simlib/simulator.cpp:452-550) as a farm of P
+    concurrent single-threaded simulations, P = host cores, as the reference's MPI farm runs
+    independent evaluations.  The K timed steps are consecutive slices of the time axis of the
+    same P simulations, so together they run P complete simulations of every time step: nothing is
+    extrapolated.  The W warm-up steps each run one time step of every simulation first."""
     d = Dist()
     if d.rank != 0:
         d.close()
         return
-    spec, steps, batch, cfg_index, wname = make_heart_spec(args.workload)
+    from concurrent.futures import ThreadPoolExecutor
     from ekgsim_gb300 import synth
-    genes = np.stack([synth.genes_for(spec, r, cfg_index) for r in range(max(1, host_cores()))])
+    from oracle import oracle as O
+    spec, steps, batch, cfg_index, wname = make_heart_spec(args.workload)
     cores = host_cores()
-    sample_steps = max(1, int(args.ref_sample_steps))
-    vals = []
-    for i in range(args.warmup + args.steps):
-        v, dt, sample = cpu_farm(spec, steps, genes, sample_steps, cores)
-        if i >= args.warmup:
-            vals.append(v)
-    value = float(np.mean(vals))
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    rng = np.random.Generator(np.random.PCG64(spec.seed))
+    leads_zyx = synth.leads(spec, rng)[:, ::-1].copy()
+    at, layer = O.activation(grid, tm)
+    n_vox = int(np.count_nonzero(layer))
+    n_aps = int(O.ap_indices(layer, at)[0].max() + 1)
+    jobs = []
+    for i in range(cores):
+        g = synth.genes_for(spec, i, cfg_index)
+        lk, _, _ = O.layer_aps(spec.n_layers, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX,
+                               [5, 6, 7, 8], "endo-mid-epi", 0.6, g[:12])
+        jobs.append((lk, O.move_leads(leads_zyx, g[12:12 + 2 * spec.n_leads].reshape(-1, 2))))
+
+    def farm(k0, k1):
+        with ThreadPoolExecutor(max_workers=cores) as ex:
+            list(ex.map(lambda j: O.run_naive_range(layer, at, j[0], j[1], "3D4", 0.0, float(steps), 1.0, k0, k1),
+                        jobs))
+
+    for w in range(args.warmup):
+        farm(w % steps, w % steps + 1)
+    bounds = [round(steps * i / args.steps) for i in range(args.steps + 1)]
+    step_s = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        farm(bounds[i], bounds[i + 1])
+        step_s.append(time.perf_counter() - t0)
+    total = sum(step_s)
+    value = cores / total
+    sample = (f"{cores} concurrent single-thread simulations of the {spec.n}^3 heart (the reference's per-voxel "
+              f"cost structure), all {steps} time steps: the {args.steps} timed steps are consecutive slices of "
+              f"the time axis of the same simulations ({total:.1f} s wall in all); nothing is extrapolated")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "sims/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * cores / value if value else None,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": wname, "grid": spec.n, "leads": spec.n_leads, "steps": steps},
+        "config": workload_config(spec, steps, batch, wname, n_vox, n_aps, args.gpus),
         "cpu_baseline": {"value": value, "unit": "sims/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "sims/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "step_s": {"min": min(step_s), "max": max(step_s)},
     }
     print(json.dumps(line), flush=True)
     d.close()
@@ -417,10 +528,8 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "sims/s", "n_gpus": d.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": bm["total_ms"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16x3", "data": "synthetic",
-        "config": {"workload": wname, "grid": spec.n, "voxels": int(info.n_voxels), "aps": int(info.n_aps),
-                   "leads": info.n_leads, "steps": steps, "batch": batch, "layers": info.n_layers,
-                   "l2": "inputs larger than L2 (per-step lead fields and partials exceed 129 MB)",
-                   "parallelism": f"replicas{d.world}", "heart_setup_s": setup_s, "ca_rounds": info.ca_rounds},
+        "config": workload_config(spec, steps, batch, wname, info.n_voxels, info.n_aps, d.world),
+        "heart": {"setup_s": setup_s, "ca_rounds": int(info.ca_rounds)},
         "e2e": {"value": e2e, "unit": "sims/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "form": "queued batched calls, two in flight", "sync_value": e2e_sync},
         "plain": plain,
@@ -444,18 +553,11 @@ def run_ours(args):
         "clocks": clk,
     }
     if d.rank == 0 and not args.no_check:
-        # parity of a sample of results against the FP64 oracle, and activation-time mismatch
-        from oracle import oracle as O
-        at_ref, layer = O.activation(grid, tm)
-        at_gpu = heart.activation()
-        mism = int(np.count_nonzero(at_gpu.view(np.int64) != at_ref.view(np.int64)))
-        rels = []
-        for i in range(min(2, batch)):
-            ref = O.run(layer, at_ref, lk[i], moved[i], "3D4", 0.0, float(steps), 1.0)
-            rels.append(float(np.linalg.norm(ecg[i] - ref) / np.linalg.norm(ref)))
-        line["parity"] = {"ecg_rel_l2_max": max(rels), "checked_sims": len(rels), "at_mismatch": mism}
+        line["parity"] = parity_check(E, eng, grid, tm, leads_zyx, spec, steps, genes, target, ecg, heart, lk, moved,
+                                      args.parity_sims)
     if d.rank == 0 and not args.no_served:
         line["served"] = served_run(max_wait_us=args.served_wait_us)
+        line["served_over_plain"] = line["served"]["saturated"]["throughput_req_s"] / plain["sims_per_s"]
     if d.rank == 0 and d.world == 1 and not args.no_cpu:
         v, dt, sample = cpu_farm(spec, steps, genes, args.cpu_sample_steps, host_cores())
         line["cpu_baseline"] = {"value": v, "unit": "sims/s", "cores": host_cores(), "kind": "port",
@@ -479,7 +581,7 @@ def main():
     ap.add_argument("--batch", type=int, default=0)
     ap.add_argument("--plain-calls", type=int, default=50)
     ap.add_argument("--cpu-sample-steps", type=int, default=16)
-    ap.add_argument("--ref-sample-steps", type=int, default=6)
+    ap.add_argument("--parity-sims", type=int, default=8, help="results checked against the FP64 oracle")
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-served", action="store_true")

@@ -35,7 +35,7 @@ class HeartDesc(ctypes.Structure):
     _fields_ = [("nz", c_int32), ("ny", c_int32), ("nx", c_int32), ("layers", P(c_int32)),
                 ("n_transfer", c_int32), ("transfer", P(c_double)), ("n_leads", c_int32),
                 ("leads_zyx", P(c_double)), ("nhood", c_int32), ("start", c_double), ("length", c_double),
-                ("dt", c_double)]
+                ("dt", c_double), ("activation_in", P(c_double))]
 
 
 class HeartInfo(ctypes.Structure):
@@ -56,7 +56,8 @@ class EvalConfig(ctypes.Structure):
 
 
 class ServerOpts(ctypes.Structure):
-    _fields_ = [("max_batch", c_int32), ("max_wait_us", c_int32), ("hbm_reserve_bytes", c_uint64)]
+    _fields_ = [("max_batch", c_int32), ("max_wait_us", c_int32), ("hbm_reserve_bytes", c_uint64),
+                ("no_ecg", c_int32)]
 
 
 class RequestStats(ctypes.Structure):
@@ -99,6 +100,10 @@ SIGNATURES = {
     "ekg_server_submit": (ctypes.c_int, [ctypes.c_void_p, c_int32, P(c_double), c_int32, P(c_uint64)]),
     "ekg_server_poll": (ctypes.c_int, [ctypes.c_void_p, c_uint64, c_int32, P(c_double), P(c_double), P(c_double),
                                        P(RequestStats)]),
+    "ekg_server_submit_many": (ctypes.c_int, [ctypes.c_void_p, c_int32, P(c_int32), P(c_double), c_int32,
+                                              P(c_uint64)]),
+    "ekg_server_poll_many": (ctypes.c_int, [ctypes.c_void_p, c_int32, P(c_uint64), c_int32, c_int32, P(c_double),
+                                            P(c_double), P(c_int32), P(RequestStats)]),
     "ekg_server_set_free_bytes_provider": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "ekg_activation_noalloc": (ctypes.c_int, [c_int32, c_int32, c_int32, ctypes.c_void_p, c_int32, P(c_double),
                                               ctypes.c_void_p, P(c_int32)]),

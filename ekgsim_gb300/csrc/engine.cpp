@@ -276,29 +276,41 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
         nstart += (int64_t)P.starts.size();
         for (int a = 0; a < 256; ++a) present[a] = present[a] || P.present[a];
     }
-    EKG_CHECK(nstart > 0, EKG_ERR_NO_START, "Could not find starting point for excitation sequence");
+    // a loaded sequence replaces the automaton (simlib/sim_lib.h:224-231): the stimulus and the
+    // conduction matrix are not used then
+    const bool loaded = d->activation_in != nullptr;
+    EKG_CHECK(loaded || nstart > 0, EKG_ERR_NO_START, "Could not find starting point for excitation sequence");
     EKG_CHECK(nl >= 1, EKG_ERR_BAD_INPUT, "model has no non-empty voxel");
     D.nlayers = nl;
     const int nt = d->n_transfer;
-    for (int a = 1; a <= nl; ++a)
-        if (present[a] && a >= nt)
-            throw Error{EKG_ERR_TRANSFER, "transfer (conduction) matrix does not define layer " + std::to_string(a)};
-    for (int s = 1; s <= nl; ++s)
-        for (int t = 1; t <= nl; ++t)
-            if (present[s] && present[t]) {
-                const double v = d->transfer[(size_t)s * nt + t];
-                EKG_CHECK(v >= 0 && std::isfinite(v), EKG_ERR_BAD_INPUT,
-                          "conduction delays between present layers must be finite and non-negative");
-            }
     const int nl1 = nl + 1;
     std::vector<double> lag((size_t)nl1 * nl1 * 3, 0.0);
-    for (int s = 1; s <= nl; ++s)
-        for (int t = 1; t <= nl; ++t)
-            for (int k = 1; k <= 3; ++k) {
-                double l = d->transfer[(size_t)s * nt + t];
-                l *= std::sqrt((double)k);  // simlib/simulator.cpp:239-240
-                lag[((size_t)s * nl1 + t) * 3 + (k - 1)] = l;
+    if (loaded) {
+        for (int64_t i = 0; i < n; ++i)
+            if (lay[i]) {
+                const double v = d->activation_in[i];
+                EKG_CHECK(std::isfinite(v) && v >= 0, EKG_ERR_BAD_INPUT,
+                          "loaded activation times of non-empty cells must be finite and non-negative");
             }
+    } else {
+        for (int a = 1; a <= nl; ++a)
+            if (present[a] && a >= nt)
+                throw Error{EKG_ERR_TRANSFER, "transfer (conduction) matrix does not define layer " + std::to_string(a)};
+        for (int s = 1; s <= nl; ++s)
+            for (int t = 1; t <= nl; ++t)
+                if (present[s] && present[t]) {
+                    const double v = d->transfer[(size_t)s * nt + t];
+                    EKG_CHECK(v >= 0 && std::isfinite(v), EKG_ERR_BAD_INPUT,
+                              "conduction delays between present layers must be finite and non-negative");
+                }
+        for (int s = 1; s <= nl; ++s)
+            for (int t = 1; t <= nl; ++t)
+                for (int k = 1; k <= 3; ++k) {
+                    double l = d->transfer[(size_t)s * nt + t];
+                    l *= std::sqrt((double)k);  // simlib/simulator.cpp:239-240
+                    lag[((size_t)s * nl1 + t) * 3 + (k - 1)] = l;
+                }
+    }
     std::vector<int32_t> start_tiles;
     {
         const int ntx = (d->nx + 7) / 8, nty = (d->ny + 7) / 8;
@@ -331,7 +343,17 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     DBuf<uint8_t> dl;
     dl.alloc(n);
     EKG_CUDA(cudaMemcpyAsync(dl.p, lay.data(), n, cudaMemcpyHostToDevice, s));
-    {
+    if (loaded) {
+        // -0.0 keys like +0.0 in the reference's std::map (simlib/simulator.cpp:570-590)
+        std::vector<double> at_in(d->activation_in, d->activation_in + n);
+        for (double &v : at_in)
+            if (v == 0.0) v = 0.0;
+        h->at_cells.alloc(n);
+        EKG_CUDA(cudaMemcpyAsync(h->at_cells.p, at_in.data(), n * 8, cudaMemcpyHostToDevice, s));
+        h->ca_rounds = 0;
+        h->ca_ms = 0;
+        EKG_CUDA(cudaStreamSynchronize(s));
+    } else {
         DBuf<uint8_t> ds;
         DBuf<double> dlag;
         ds.alloc(n);
@@ -1926,8 +1948,9 @@ int ekg_heart_from_ini(ekg_engine *e, const char *ini_path, const char *out_dir,
         int nz, ny, nx;
         std::vector<int32_t> lay;
         read_shape(c.shape, nz, ny, nx, lay);
-        EKG_CHECK(c.excitation_in.empty(), EKG_ERR_BAD_INPUT,
-                  "loading a precomputed excitation sequence is not supported; remove [model] excitation sequence");
+        // a precomputed sequence instead of the automaton (simlib/sim_lib.h:224-231)
+        std::vector<double> at_in;
+        if (!c.excitation_in.empty()) read_excitation(c.excitation_in, nz, ny, nx, at_in);
         const int nh = nhood_code(c.nhood);
         if (nh < 0) throw Error{EKG_ERR_BAD_INPUT, "\n   unknown neighbourhood (only know of these: 2D4, 3D4, 2D8, 3D8 (cube))"};
         ekg_heart_desc d{};
@@ -1943,9 +1966,15 @@ int ekg_heart_from_ini(ekg_engine *e, const char *ini_path, const char *out_dir,
         d.start = c.start;
         d.length = c.length;
         d.dt = c.dt;
+        d.activation_in = at_in.empty() ? nullptr : at_in.data();
         std::unique_ptr<ekg_heart> h(new ekg_heart());
         h->eng = e;
         heart_setup(h.get(), &d);
+        if (!c.excitation_out.empty()) {
+            // the reference exports right after computing or loading (simlib/simulator.cpp:284-285, :364-366)
+            ensure_at_host(h.get());
+            write_excitation(c.excitation_out, nz, ny, nx, h->at_host.data());
+        }
         if (c.interpolation != "endo-epi" && c.interpolation != "endo-mid-epi")
             throw Error{EKG_ERR_BAD_INPUT, "unknown interpolation type [" + c.interpolation + "]"};
         std::vector<std::vector<double>> targets;

@@ -152,7 +152,69 @@ SimConfig load_config(const std::string &path) {
     c.points = resolve(d, c.points);
     c.transfer = resolve(d, c.transfer);
     c.targets_file = resolve(d, c.targets_file);
+    if (!c.excitation_in.empty()) c.excitation_in = resolve(d, c.excitation_in);
+    if (!c.excitation_out.empty()) c.excitation_out = resolve(d, c.excitation_out);
     return c;
+}
+
+// ------------------------------------------------------------------ excitation sequence files
+static bool has_matrix_ext(const std::string &path) {
+    const size_t dot = path.find_last_of('.');
+    return dot != std::string::npos && path.substr(dot) == ".matrix";
+}
+
+void read_excitation(const std::string &path, int nz, int ny, int nx, std::vector<double> &at) {
+    if (!has_matrix_ext(path)) throw std::runtime_error("can only import from .matrix for the time being");
+    std::ifstream in(path);
+    if (!in.is_open()) throw std::runtime_error("could not open file " + path + " to load excitation sequence");
+    in.ignore(100000000, '\n');  // comment line
+    std::string dim;
+    in >> dim;
+    if (!(dim.size() >= 2 && (dim[1] == 'D' || dim[1] == 'd') && dim[0] > '0' && dim[0] <= '3'))
+        throw std::runtime_error("error while loading matrix, could not read dimensionality");
+    long size[3] = {1, 1, 1};  // [0] z, [1] y, [2] x; the header lists x first
+    int w = 2;
+    in >> size[w];
+    for (int k = dim[0] - '0' - 1; k > 0; --k) {
+        in.ignore(100, 'x');
+        --w;
+        in >> size[w];
+    }
+    std::string rest, sep_name;
+    std::getline(in, rest, '\n');
+    std::istringstream(rest) >> sep_name;
+    const char sep = sep_name == "tab" ? '\t' : (sep_name == "comma" || sep_name == "," ? ',' : (sep_name == "space" ? ' ' : 0));
+    if (in.fail()) throw std::runtime_error("reading file " + path + " failed (while reading size)");
+    if (size[0] != nz || size[1] != ny || size[2] != nx)
+        throw std::runtime_error("failed to read excitation sequence due to its incompatible size");
+    // one time per cell, z slowest; a failed extraction leaves 0 (the cells start at 0)
+    at.assign((size_t)nz * ny * nx, 0.0);
+    for (size_t i = 0; i < at.size() && in; ++i) {
+        double v = 0.0;
+        if (!(in >> v)) break;
+        at[i] = v;
+        if (sep == ',') in.ignore(1);
+    }
+}
+
+void write_excitation(const std::string &path, int nz, int ny, int nx, const double *at) {
+    if (!has_matrix_ext(path)) throw std::runtime_error("can only export to .matrix for the time being");
+    std::FILE *f = std::fopen(path.c_str(), "w");
+    if (!f) throw std::runtime_error("could not open file " + path + " to export the excitation sequence");
+    std::fputs("Excitation file (next line specifies matrix type (2D) size (X x Y x Z) and elemet separator type "
+               "(tab) after that comes data (x are rows, y are lines, z are blocks - separated with empty line)\n",
+               f);
+    if (nz > 1) std::fprintf(f, "3D %d x %d x %d tab\n", nx, ny, nz);
+    else std::fprintf(f, "2D %d x %d tab\n", nx, ny);
+    for (int z = 0; z < nz; ++z) {
+        for (int y = 0; y < ny; ++y) {
+            const double *row = at + ((size_t)z * ny + y) * nx;
+            for (int x = 0; x < nx; ++x) std::fprintf(f, x ? "\t%.3f" : "%.3f", row[x]);
+            std::fputc('\n', f);
+        }
+        std::fputc('\n', f);
+    }
+    if (std::fclose(f) != 0) throw std::runtime_error("could not write " + path);
 }
 
 // ------------------------------------------------------------------ .matrix

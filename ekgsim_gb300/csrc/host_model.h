@@ -59,6 +59,12 @@ void read_shape(const std::string &path, int &nz, int &ny, int &nx, std::vector<
 void read_transfer(const std::string &path, int &n, std::vector<double> &t);
 // Simulation::loadMeasuringPoints (simlib/simulator.cpp:369-397): returns (z,y,x) triples.
 void read_points(const std::string &path, std::vector<double> &zyx);
+// Simulation::loadExcitationSequence for .matrix files (simlib/simulator.cpp:288-367): one time per
+// cell [z][y][x] after a comment line and the "<d>D X x Y x Z <sep>" header; the size must be the
+// shape's.
+void read_excitation(const std::string &path, int nz, int ny, int nx, std::vector<double> &at);
+// exportShape with excit = true (simlib/simulator.cpp:71-106): times printed with 3 decimals.
+void write_excitation(const std::string &path, int nz, int ny, int nx, const double *at);
 // ColumnFile::load (simlib/columnFile.h:115-165).
 void read_columns(const std::string &path, std::vector<std::vector<double>> &cols);
 // SimImplementation::loadTargets (sim.cpp:999-1042); writes target_chk.column into out_dir

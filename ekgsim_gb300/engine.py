@@ -56,15 +56,21 @@ class Heart:
 
     @classmethod
     def create(cls, engine: Engine, layers: np.ndarray, transfer: np.ndarray, leads_zyx: np.ndarray,
-               nhood: str = "3D4", start: float = 0.0, length: float = 600.0, dt: float = 1.0) -> "Heart":
+               nhood: str = "3D4", start: float = 0.0, length: float = 600.0, dt: float = 1.0,
+               activation: Optional[np.ndarray] = None) -> "Heart":
+        """Upload a heart.  `activation` (same shape as `layers`) replaces the computed activation
+        times, as a loaded excitation sequence does in the reference."""
         layers = np.ascontiguousarray(layers, dtype=np.int32)
         if layers.ndim == 2:
             layers = layers[None]
         transfer = np.ascontiguousarray(transfer, dtype=np.float64)
         leads_zyx = np.ascontiguousarray(np.atleast_2d(leads_zyx), dtype=np.float64)
+        at_in = None
+        if activation is not None:
+            at_in = np.ascontiguousarray(activation, dtype=np.float64).reshape(layers.shape)
         d = L.HeartDesc(layers.shape[0], layers.shape[1], layers.shape[2], i32ptr(layers), transfer.shape[0],
                         dptr(transfer), leads_zyx.shape[0], dptr(leads_zyx), L.NHOOD[nhood], float(start),
-                        float(length), float(dt))
+                        float(length), float(dt), dptr(at_in) if at_in is not None else None)
         h = ctypes.c_void_p()
         check(engine._lib.ekg_heart_create(engine.handle, ctypes.byref(d), ctypes.byref(h)))
         heart = cls(engine, h)
@@ -137,6 +143,7 @@ class Heart:
     def set_eval(self, base_aps, k_min, k_max, free_k, targets, target_offsets=None, **kw):
         """Evaluation settings (ekg_heart_set_eval); keyword arguments as ``eval_config``."""
         self._cfg = eval_config(base_aps, k_min, k_max, free_k, targets, target_offsets, **kw)
+        self.eval_args = ((base_aps, k_min, k_max, free_k, targets, target_offsets), dict(kw))
         self._eval_shape = None
         check(self._lib.ekg_heart_set_eval(self._h, ctypes.byref(self._cfg)))
 
@@ -274,10 +281,11 @@ def move_leads(orig_zyx: np.ndarray, disp_uv: Optional[np.ndarray]) -> np.ndarra
 class Server:
     """Served form: request loop with continuous batching over resident hearts."""
 
-    def __init__(self, engine: Engine, max_batch: int = 256, max_wait_us: int = 200, hbm_reserve_bytes: int = 2 << 30):
+    def __init__(self, engine: Engine, max_batch: int = 256, max_wait_us: int = 200, hbm_reserve_bytes: int = 2 << 30,
+                 keep_ecg: bool = True):
         self.engine = engine
         self._lib = engine._lib
-        o = L.ServerOpts(max_batch, max_wait_us, hbm_reserve_bytes)
+        o = L.ServerOpts(max_batch, max_wait_us, hbm_reserve_bytes, 0 if keep_ecg else 1)
         h = ctypes.c_void_p()
         check(self._lib.ekg_server_create(engine.handle, ctypes.byref(o), ctypes.byref(h)))
         self._h = h
@@ -309,6 +317,33 @@ class Server:
             return None
         check(rc)
         return crit, float(viol[0]), ecg, dict(queue_ms=st.queue_ms, total_ms=st.total_ms, batch=st.batch_size)
+
+    def submit_many(self, heart_ids, genes) -> np.ndarray:
+        """Submit len(heart_ids) requests (genes: one row per request); returns their ids."""
+        hid = np.ascontiguousarray(heart_ids, dtype=np.int32)
+        g = np.ascontiguousarray(np.atleast_2d(genes), dtype=np.float64)
+        ids = np.zeros(hid.size, dtype=np.uint64)
+        check(self._lib.ekg_server_submit_many(self._h, hid.size, hid.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                               dptr(g), g.shape[1], ids.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))))
+        return ids
+
+    def poll_many(self, ids, n_criteria: int, wait_ms: int = 0):
+        """Hand over finished requests: (status [n], criteria [n, n_criteria], violation [n],
+        total_ms [n], batch [n]); status -10 marks a request that is not finished yet."""
+        ids = np.ascontiguousarray(ids, dtype=np.uint64)
+        n = ids.size
+        crit = np.zeros((n, n_criteria))
+        viol = np.zeros(n)
+        status = np.zeros(n, dtype=np.int32)
+        stats = (L.RequestStats * max(1, n))()
+        rc = self._lib.ekg_server_poll_many(self._h, n, ids.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), wait_ms,
+                                            n_criteria, dptr(crit), dptr(viol),
+                                            status.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), stats)
+        if rc not in (0, -10):
+            check(rc)
+        total = np.array([stats[i].total_ms for i in range(n)])
+        batch = np.array([stats[i].batch_size for i in range(n)])
+        return status, crit, viol, total, batch
 
     def close(self):
         if self._h:

@@ -211,7 +211,10 @@ def ini_text(shape="model.matrix", transfer="conduction.matrix", points="leads.t
              base_aps=(BASE_AP, BASE_AP, BASE_AP), k_min=K_MIN, k_max=K_MAX,
              free_k=(5, 6, 7, 8), optimize_points=1, comparison=2, mid=0.6,
              interpolation="endo-mid-epi", fast_limit=2, fast_is_crit=0, fast_delay=10.0, peak=0,
-             endo_epi=-0.5, extra_opt: str = "") -> str:
+             endo_epi=-0.5, extra_opt: str = "", excitation_in: str = "", excitation_out: str = "") -> str:
+    """simulator.ini text.  excitation_in / excitation_out set the "excitation sequence" keys of
+    [model] (load a precomputed sequence instead of computing it) and [output files] (write the
+    sequence, simlib/simulator.h:107-145)."""
     def vec(v):
         return ", ".join(repr(float(x)) for x in v)
     lines = [
@@ -219,9 +222,17 @@ def ini_text(shape="model.matrix", transfer="conduction.matrix", points="leads.t
         f"shape = {shape}",
         f"transfer = {transfer}",
         f"points = {points}",
+    ]
+    if excitation_in:
+        lines.append(f"excitation sequence = {excitation_in}")
+    lines += [
         "",
         "[output files]",
         "results filename = result.column",
+    ]
+    if excitation_out:
+        lines.append(f"excitation sequence = {excitation_out}")
+    lines += [
         "",
         "[simulation]",
         f"start = {start}",

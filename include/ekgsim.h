@@ -72,6 +72,11 @@ typedef struct {
     double start;              /* [simulation] start (ms) */
     double length;             /* [simulation] length (ms) */
     double dt;                 /* [simulation] time step (ms) */
+    const double *activation_in; /* NULL: compute the activation times; else [nz][ny][nx] times (ms,
+                                  * finite and >= 0 in non-empty cells) used instead, as the
+                                  * reference does with "[model] excitation sequence"
+                                  * (Simulation::loadExcitationSequence, simlib/simulator.cpp:288-367;
+                                  * no stimulus voxel or conduction matrix is needed then) */
 } ekg_heart_desc;
 
 typedef struct {
@@ -199,8 +204,11 @@ int ekg_host_unregister(void *ptr);
 /* ------------------------------------------------------------------ served form */
 typedef struct {
     int32_t max_batch;           /* most requests packed into one device pass (default 256) */
-    int32_t max_wait_us;         /* longest a request waits for others to join (default 200) */
+    int32_t max_wait_us;         /* longest a request waits for others to join while nothing of its
+                                  * heart is on the device (default 200) */
     uint64_t hbm_reserve_bytes;  /* free memory kept back from admission (default 2 GiB) */
+    int32_t no_ecg;              /* 1: results carry criteria and violation only (no ECG copies to
+                                  * the host); polling for an ECG is then an error.  0 (default) keeps them */
 } ekg_server_opts;
 
 typedef struct {
@@ -210,7 +218,13 @@ typedef struct {
 } ekg_request_stats;
 
 /* Request loop with continuous batching over resident hearts; replaces the MPI master/worker
- * job queue of AMS-DEMO (AMS-DEMO/ParallelFramework.h:109-520) on one GPU. */
+ * job queue of AMS-DEMO (AMS-DEMO/ParallelFramework.h:109-520) on one GPU.  Every heart has its
+ * own queue and dispatcher: while one pass of a heart runs on the device the next one is prepared
+ * and queued behind it, so requests that arrive during a pass join the next; hearts overlap on the
+ * device.  A request with the wrong gene count or non-finite genes fails alone (EKG_ERR_BAD_INPUT,
+ * the reference's messages of sim.cpp:458-459 and :835-841); a pass that does not fit the free
+ * device memory minus the reserve is halved until it does (EKG_ERR_OUT_OF_MEMORY when not even one
+ * simulation fits). */
 int ekg_server_create(ekg_engine *e, const ekg_server_opts *opts, ekg_server **out);
 int ekg_server_destroy(ekg_server *s);
 /* Register a heart (with its eval config set); returns its id. */
@@ -220,6 +234,19 @@ int ekg_server_submit(ekg_server *s, int32_t heart_id, const double *genes, int3
 /* Wait up to wait_ms (0 = poll) for a result; EKG_ERR_BUSY if not ready.  ecg_out may be NULL. */
 int ekg_server_poll(ekg_server *s, uint64_t request_id, int32_t wait_ms, double *criteria_out,
                     double *violation_out, double *ecg_out, ekg_request_stats *stats);
+/* Many requests in one call (as the reference's master hands out a generation of jobs,
+ * AMS-DEMO/ParallelNumericOptimizer.h:509-599): heart_ids and request_ids have n entries, genes is
+ * n x n_genes. */
+int ekg_server_submit_many(ekg_server *s, int32_t n, const int32_t *heart_ids, const double *genes,
+                           int32_t n_genes, uint64_t *request_ids);
+/* Wait up to wait_ms until all n requests are finished, then hand over the finished ones: per
+ * request status_out[i] (EKG_OK, its error code, or EKG_ERR_BUSY when not finished), its criteria at
+ * criteria_out + i * crit_stride (at most crit_stride values), violation_out[i] and stats_out[i]
+ * (criteria_out, violation_out and stats_out may be NULL).  Returns EKG_ERR_BUSY when some request
+ * is not finished, else EKG_OK (each request's own outcome is in status_out). */
+int ekg_server_poll_many(ekg_server *s, int32_t n, const uint64_t *request_ids, int32_t wait_ms,
+                         int32_t crit_stride, double *criteria_out, double *violation_out,
+                         int32_t *status_out, ekg_request_stats *stats_out);
 
 /* Test hook: replace the free-device-memory query the admission check uses (fn returns free
  * bytes; NULL restores cudaMemGetInfo).  Lets tests refuse admission without filling the GPU. */
@@ -248,7 +275,10 @@ int ekg_activation_noalloc(int32_t nz, int32_t ny, int32_t nx, const int32_t *d_
 /* Build a heart and its eval config from a simulator.ini and the files it names, as the
  * SimImplementation constructor does (sim.cpp:362-431): settings, transfer matrix, measuring
  * points, shape, excitation sequence, targets (target_chk.column is written to `out_dir`
- * when it is not NULL, as sim.cpp:1031-1039 does). */
+ * when it is not NULL, as sim.cpp:1031-1039 does).  "[model] excitation sequence" loads the
+ * activation times from that .matrix file instead of computing them, and "[output files]
+ * excitation sequence" writes them (3 decimals) to that file, as simlib/sim_lib.h:224-231 with
+ * simlib/simulator.cpp:71-106 and :288-367 do. */
 int ekg_heart_from_ini(ekg_engine *e, const char *ini_path, const char *out_dir, ekg_heart **out);
 
 /* Lead positions after moving them by per-lead (u, v) displacements (n_leads x 2) in the

@@ -623,12 +623,18 @@ double ekgo_clamp(double c) {
  * build (setApIndices, :561-621).  Used only to time the CPU baseline; results are bit-identical
  * to ekgo_run.  `steps_limit` > 0 runs only the first steps_limit steps (a bounded sample).
  */
-int ekgo_run_naive(int nz, int ny, int nx, const int32_t *layer, const double *at, int nlayers,
-                   const double *layer_k, int nlead, const double *lead_zyx, int nhood_code, double start,
-                   double length, double dt, int steps_limit, double *ecg) {
+/* Steps [k0, k1) of the reference's voxel-major loop (ecg is nlead x (k1 - k0)): the time of step k
+ * is start advanced by += dt k times, as simTime is in simlib/simulator.cpp:496-500, 519, so any
+ * split of the time axis into ranges gives the same values as one pass over all of it. */
+int ekgo_run_naive_range(int nz, int ny, int nx, const int32_t *layer, const double *at, int nlayers,
+                         const double *layer_k, int nlead, const double *lead_zyx, int nhood_code, double start,
+                         double length, double dt, int64_t k0, int64_t k1, double *ecg) {
     int64_t n = (int64_t)nz * ny * nx;
-    int64_t steps = (int64_t)ceil(length / dt);
-    if (steps_limit > 0 && steps_limit < steps) steps = steps_limit;
+    int64_t total = (int64_t)ceil(length / dt);
+    if (k1 > total) k1 = total;
+    if (k0 < 0 || k0 > k1) return EKGO_ERR_ARG;
+    int64_t steps = k1 - k0;
+    for (int64_t k = 0; k < k0; ++k) start += dt;
     int64_t *api = (int64_t *)malloc((size_t)n * sizeof(int64_t));
     int32_t *apl = (int32_t *)malloc((size_t)n * sizeof(int32_t));
     double *apat = (double *)malloc((size_t)n * sizeof(double));
@@ -678,4 +684,14 @@ int ekgo_run_naive(int nz, int ny, int nx, const int32_t *layer, const double *a
     }
     free(dip); free(cell); free(aps); free(apat); free(apl); free(api);
     return EKGO_OK;
+}
+
+/* The whole time axis, or its first steps_limit steps. */
+int ekgo_run_naive(int nz, int ny, int nx, const int32_t *layer, const double *at, int nlayers,
+                   const double *layer_k, int nlead, const double *lead_zyx, int nhood_code, double start,
+                   double length, double dt, int steps_limit, double *ecg) {
+    int64_t steps = (int64_t)ceil(length / dt);
+    if (steps_limit > 0 && steps_limit < steps) steps = steps_limit;
+    return ekgo_run_naive_range(nz, ny, nx, layer, at, nlayers, layer_k, nlead, lead_zyx, nhood_code, start, length,
+                                dt, 0, steps, ecg);
 }

@@ -52,6 +52,8 @@ def lib():
                                                     ctypes.c_int, d, d, d, P(d), ctypes.c_int]
         L.ekgo_run_naive.argtypes = [ctypes.c_int] * 3 + [P(i32), P(d), ctypes.c_int, P(d), ctypes.c_int, P(d),
                                                           ctypes.c_int, d, d, d, ctypes.c_int, P(d)]
+        L.ekgo_run_naive_range.argtypes = [ctypes.c_int] * 3 + [P(i32), P(d), ctypes.c_int, P(d), ctypes.c_int,
+                                                                P(d), ctypes.c_int, d, d, d, i64, i64, P(d)]
         L.ekgo_ap_indices.argtypes = [i64, P(i32), P(d), P(i64), P(i32), P(d)]
         L.ekgo_ap_indices.restype = i64
         L.ekgo_layer_aps.argtypes = [ctypes.c_int, ctypes.c_int, P(d), P(d), P(d), ctypes.c_uint,
@@ -137,6 +139,26 @@ def run_naive(layer, at, layer_k, leads_zyx, nhood="3D4", start=0.0, length=600.
                          _p(layer_k, ctypes.c_double), leads_zyx.shape[0], _p(leads_zyx, ctypes.c_double),
                          NHOOD[nhood], float(start), float(length), float(dt), int(steps_limit),
                          _p(ecg, ctypes.c_double))
+    return ecg
+
+
+def run_naive_range(layer, at, layer_k, leads_zyx, nhood="3D4", start=0.0, length=600.0, dt=1.0, k0=0, k1=None):
+    """Steps [k0, k1) of the ECG with the reference's per-voxel cost structure (single thread); the
+    values equal the same columns of run_naive over the whole axis."""
+    layer = np.ascontiguousarray(layer, dtype=np.int32)
+    at = np.ascontiguousarray(at, dtype=np.float64)
+    layer_k = np.ascontiguousarray(layer_k, dtype=np.float64)
+    leads_zyx = np.ascontiguousarray(np.atleast_2d(leads_zyx), dtype=np.float64)
+    steps = int(math.ceil(length / dt))
+    k1 = steps if k1 is None else min(int(k1), steps)
+    ecg = np.zeros((leads_zyx.shape[0], max(0, k1 - int(k0))), dtype=np.float64)
+    nz, ny, nx = layer.shape
+    rc = lib().ekgo_run_naive_range(nz, ny, nx, _p(layer, ctypes.c_int32), _p(at, ctypes.c_double), layer_k.shape[0],
+                                    _p(layer_k, ctypes.c_double), leads_zyx.shape[0], _p(leads_zyx, ctypes.c_double),
+                                    NHOOD[nhood], float(start), float(length), float(dt), int(k0), int(k1),
+                                    _p(ecg, ctypes.c_double))
+    if rc != 0:
+        raise RuntimeError(f"oracle run error {rc}")
     return ecg
 
 
@@ -297,6 +319,51 @@ def resample(src: np.ndarray, factor: float, start_offset: int) -> np.ndarray:
     return dest
 
 
+def export_excitation(at: np.ndarray) -> str:
+    """Text of an exported excitation sequence: exportShape with excit = true
+    (simlib/simulator.cpp:71-106): a comment line, the "3D X x Y x Z tab" (or "2D X x Y tab")
+    header, then per z block one line per y row of tab-separated times printed with three
+    decimals, and an empty line after each block."""
+    nz, ny, nx = at.shape
+    out = ["Excitation file (next line specifies matrix type (2D) size (X x Y x Z) and elemet separator type "
+           "(tab) after that comes data (x are rows, y are lines, z are blocks - separated with empty line)\n"]
+    out.append(f"3D {nx} x {ny} x {nz} tab\n" if nz > 1 else f"2D {nx} x {ny} tab\n")
+    for z in range(nz):
+        for y in range(ny):
+            out.append("\t".join("%.3f" % v for v in at[z, y]) + "\n")
+        out.append("\n")
+    return "".join(out)
+
+
+def read_excitation(path: str, shape) -> np.ndarray:
+    """Simulation::loadExcitationSequence (simlib/simulator.cpp:288-367) for a .matrix file: skip
+    the comment line, read the "<d>D X x Y [x Z] <sep>" header, check the size against the shape,
+    then read one time per cell in z, y, x order (stream extraction, a comma separator skipped)."""
+    if not path.endswith(".matrix"):
+        raise RuntimeError("can only import from .matrix for the time being")
+    try:
+        text = open(path).read()
+    except OSError:
+        raise RuntimeError(f"could not open file {path} to load excitation sequence")
+    body = text.split("\n", 1)[1] if "\n" in text else ""
+    toks = body.split(None, 1)
+    dim = toks[0] if toks else ""
+    if len(dim) < 2 or dim[1] not in "dD" or not ("0" < dim[0] <= "3"):
+        raise RuntimeError("error while loading matrix, could not read dimensionality")
+    rest = toks[1] if len(toks) > 1 else ""
+    header, data = (rest.split("\n", 1) + [""])[:2]
+    sizes = [int(v) for v in header.replace("x", " ").split()[:int(dim[0])]]
+    size = [1, 1, 1]
+    for i, v in enumerate(sizes):  # X first, then Y, then Z
+        size[2 - i] = v
+    if tuple(size) != tuple(shape):
+        raise RuntimeError("failed to read excitation sequence due to its incompatible size")
+    vals = np.array([float(v) for v in data.replace(",", " ").split()[: shape[0] * shape[1] * shape[2]]])
+    if vals.size < shape[0] * shape[1] * shape[2]:
+        vals = np.concatenate([vals, np.zeros(shape[0] * shape[1] * shape[2] - vals.size)])
+    return vals.reshape(shape)
+
+
 @dataclass
 class Setup:
     """Everything SimImplementation's constructor loads (sim.cpp:362-431)."""
@@ -381,7 +448,13 @@ def load_setup(workdir: str, ini_name: str = "simulator.ini") -> Setup:
               fast_is_crit=int(float(opt.get("fast approximation is criterion", 0))) > 0,
               fast_delay=float(opt.get("fast approximation epi delay", 0)),
               fast_limit=float(opt.get("fast approximation limit", 2)))
-    s.at, s.layer = activation(s.raw, s.tm)
+    ex_in = m.get("excitation sequence", "")
+    if ex_in:
+        # simlib/sim_lib.h:224-231: a precomputed sequence replaces the cellular automaton
+        s.layer = np.abs(s.raw).astype(np.int32)
+        s.at = read_excitation(os.path.join(workdir, ex_in), s.raw.shape)
+    else:
+        s.at, s.layer = activation(s.raw, s.tm)
     s.n_layers = int(s.layer.max())
     return s
 

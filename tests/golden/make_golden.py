@@ -28,6 +28,11 @@ directory; the reference's test model is used for the last case):
               term across layers)
   fixed24     as tiny24 with "optimize measuring points = 0" (12 genes, leads at their loaded positions)
   n2d8_24     as tiny24 with the dipole neighbourhood "2D8"
+  cells24     as tiny24 with "-out cell_aps 0 3 17 250 100000" (cell APs by the reference's apIndex;
+              the last index is out of range and skipped): cell_aps.column values and header lines
+  exout24     as tiny24 with "[output files] excitation sequence": the exported sequence text
+  exin24      as tiny24 loading a sequence from "[model] excitation sequence" (one the reference
+              exported for the same shape with delays {2, 1, 3}) and exporting it again
   model24     the reference's own testRun model (93 x 124 x 124, 24 layers) with the README
               v>=0.1.4 example vector: criteria, violation, result.column (about 3 minutes)
 
@@ -79,6 +84,10 @@ def read_column_text(path):
     return np.array(rows)
 
 
+def file_head(path):
+    return [line.rstrip("\n") for line in open(path) if line.startswith("#")]
+
+
 def layer_k_hex(path, lk):
     with open(path, "w") as f:
         for row in lk:
@@ -127,22 +136,35 @@ def main():
             meta = json.load(f)
     tmp = tempfile.mkdtemp(prefix="ekg_golden_")
 
-    def synth_case(name, spec, steps, nlayers, genes, dump, outs=("result",), raw_at=False, **ini):
+    def synth_case(name, spec, steps, nlayers, genes, dump, outs=("result",), raw_at=False, pre_files=None, **ini):
         if only and name not in only:
             return
         wd = os.path.join(tmp, name)
         synth.make_workload(wd, spec, steps, **ini)
+        for fname, text in (pre_files or {}).items():
+            with open(os.path.join(wd, fname), "w") as f:
+                f.write(text)
         crit, viol = run_cli(ekgsim, wd, genes, outs)
         case = {"spec": {"n": spec.n, "semi_axes": list(spec.semi_axes), "wall": spec.wall, "n_layers": nlayers,
                          "delays": list(spec.delays), "n_leads": spec.n_leads, "lead_radius": spec.lead_radius,
                          "n_stim": spec.n_stim, "seed": spec.seed},
                 "steps": steps, "ini": {k: v for k, v in ini.items() if k != "base_aps"},
-                "genes": [float(g) for g in genes], "criteria": crit, "violation": viol}
+                "genes": [float(g) for g in genes], "criteria": crit, "violation": viol, "outs": list(outs)}
+        if pre_files:
+            case["files"] = sorted(pre_files)
         if "base_aps" in ini and name not in ("endoepi5",):
             case["base_aps"] = [[float(v) for v in b] for b in ini["base_aps"]]
         arrays = {"result": read_column_text(os.path.join(wd, "result.column"))}
         if "layer_aps" in outs:
             arrays["layer_aps"] = read_column_text(os.path.join(wd, "layer_aps.column"))
+        if any(o.startswith("cell_aps") for o in outs):
+            arrays["cell_aps"] = read_column_text(os.path.join(wd, "cell_aps.column"))
+            arrays["cell_aps_head"] = np.array(file_head(os.path.join(wd, "cell_aps.column")))
+        if ini.get("excitation_out"):
+            arrays["excitation_out"] = np.array(open(os.path.join(wd, ini["excitation_out"])).read())
+        if pre_files:
+            for fname, text in pre_files.items():
+                arrays["file_" + fname.replace(".", "_")] = np.array(text)
         if dump:
             at, ecg, lk = run_dump(ref_dump, wd, genes, nlayers)
             case["at_sha256"] = hashlib.sha256(at.tobytes()).hexdigest()
@@ -177,6 +199,22 @@ def main():
     synth_case("k0_24", s24, 200, 3, synth.genes_for(s24, 9, 0), dump=False, mid=0.6, base_aps=k0_base)
     synth_case("fixed24", s24, 200, 3, synth.genes_for(s24, 10, 0)[:12], dump=False, mid=0.6, optimize_points=0)
     synth_case("n2d8_24", s24, 200, 3, synth.genes_for(s24, 11, 0), dump=False, mid=0.6, nhood="2D8")
+
+    synth_case("cells24", s24, 200, 3, synth.genes_for(s24, 12, 0), dump=False, mid=0.6,
+               outs=("result", "cell_aps 0 3 17 250 100000"))
+    synth_case("exout24", s24, 200, 3, synth.genes_for(s24, 13, 0), dump=False, mid=0.6,
+               excitation_out="es_out.matrix")
+    # a sequence computed with other conduction delays ({2, 1, 3} ms), exported by the reference and
+    # loaded instead of the heart's own: the run uses the loaded (printed, 3-decimal) times
+    if not only or "exin24" in only:
+        wd = os.path.join(tmp, "exin24_src")
+        other = synth.HeartSpec(s24.n, s24.semi_axes, s24.wall, 3, [2, 1, 3], s24.n_leads, s24.lead_radius,
+                                n_stim=s24.n_stim, seed=s24.seed)
+        synth.make_workload(wd, other, 200, mid=0.6, excitation_out="es_other.matrix")
+        run_cli(ekgsim, wd, synth.genes_for(s24, 14, 0))
+        seq = open(os.path.join(wd, "es_other.matrix")).read()
+        synth_case("exin24", s24, 200, 3, synth.genes_for(s24, 14, 0), dump=False, mid=0.6,
+                   excitation_in="es_in.matrix", excitation_out="es_out.matrix", pre_files={"es_in.matrix": seq})
 
     if not args.skip_model24 and (not only or "model24" in only):
         wd = os.path.join(tmp, "model24")

@@ -44,6 +44,11 @@ def make_case(name, tmp_path):
     if "base_aps" in c:
         ini["base_aps"] = tuple(tuple(b) for b in c["base_aps"])
     synth.make_workload(str(tmp_path), spec, c["steps"], **ini)
+    if c.get("files"):
+        g = np.load(os.path.join(GOLD, f"{name}.npz"))
+        for fname in c["files"]:
+            with open(os.path.join(str(tmp_path), fname), "w") as f:
+                f.write(str(g["file_" + fname.replace(".", "_")]))
     return c
 
 
@@ -65,10 +70,11 @@ def run_cli(wd, genes, outs=("result",)):
 
 
 @pytest.mark.parametrize("name", ["tiny24", "c64", "layers10", "endoepi5", "extras24", "gate24", "rms24", "devlin24",
-                                  "vcorr24", "cube24", "n2d4_24", "start24", "k0_24", "fixed24", "n2d8_24"])
+                                  "vcorr24", "cube24", "n2d4_24", "start24", "k0_24", "fixed24", "n2d8_24",
+                                  "cells24", "exout24", "exin24"])
 def test_cli_matches_reference(name, tmp_path):
     c = make_case(name, tmp_path)
-    outs = ("result", "layer_aps") if name in ("layers10", "endoepi5") else ("result",)
+    outs = tuple(c.get("outs", ("result", "layer_aps") if name in ("layers10", "endoepi5") else ("result",)))
     r = run_cli(str(tmp_path), c["genes"], outs)
     assert r.returncode == 0
     m = re.search(r" criteria = <([^>]*)>, violation = (\S+)", r.stdout)
@@ -93,6 +99,18 @@ def test_cli_matches_reference(name, tmp_path):
         ref = g["layer_aps"]
         assert aps.shape == ref.shape
         assert np.all(np.abs(aps[:, 1:] - ref[:, 1:]) <= 2e-5 * np.abs(ref[:, 1:]) + 1e-9)
+    if "cell_aps" in g:
+        # cell APs by the reference's apIndex: header lines (k vectors printed with 6 digits) and values
+        head, aps = read_column(os.path.join(str(tmp_path), "cell_aps.column"))
+        assert head == [str(x) for x in g["cell_aps_head"]]
+        ref = g["cell_aps"]
+        assert aps.shape == ref.shape
+        assert np.all(np.abs(aps[:, 1:] - ref[:, 1:]) <= 2e-5 * np.abs(ref[:, 1:]) + 1e-9)
+    if "excitation_out" in g:
+        # [output files] excitation sequence: the same text as the reference's export
+        ini = c["ini"]
+        with open(os.path.join(str(tmp_path), ini["excitation_out"])) as f:
+            assert f.read() == str(g["excitation_out"])
 
 
 def test_cli_errors_print_and_exit_zero(tmp_path):
@@ -214,4 +232,91 @@ def test_served_admission_refused_and_bad_request_isolated(engine):
     L.check(L.load().ekg_server_set_free_bytes_provider(srv._h, None, None))
     r = srv.submit(hid, synth.genes_for(spec, 10, 5))
     assert srv.poll(r, hid, wait_ms=60000) is not None
+    srv.close()
+
+
+def test_served_c4_hearts_match_oracle(engine):
+    """The served configuration's four hearts (48^3, 96^3, 144^3, 192^3 scaled ellipsoids, 3 layers,
+    12 leads, 600 steps) through the served path: activation times bitwise per heart; per heart a
+    probe request alone and again inside a concurrent mix on all hearts, and one more request of the
+    mix, each against the FP64 oracle."""
+    from ekgsim_gb300.engine import Heart, Server
+    from oracle import oracle as O
+    cfg = synth.config(3)
+    steps = cfg["steps"]
+    hearts = []
+    for spec in cfg["hearts"]:
+        grid = synth.ellipsoid_heart(spec)
+        tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+        leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+        h = Heart.create(engine, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+        target = [t for t in synth.analytic_target(spec.n_leads, steps, spec.seed + 999)]
+        h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], target, mid_position=0.6)
+        hearts.append((h, spec, grid, tm, leads, target))
+    srv = Server(engine, max_batch=64, max_wait_us=1000)
+    ids = [srv.add_heart(x[0]) for x in hearts]
+    probes = [synth.genes_for(x[1], 900 + k, 3) for k, x in enumerate(hearts)]
+    alone = [srv.poll(srv.submit(ids[k], probes[k]), ids[k], wait_ms=120000, want_ecg=True) for k in range(4)]
+    reqs = []
+    lock = threading.Lock()
+
+    def client(c):
+        for j in range(8):
+            k = (c + j) % 4
+            g = synth.genes_for(hearts[k][1], 1000 + 37 * c + j, 3)
+            r = srv.submit(ids[k], g)
+            with lock:
+                reqs.append((r, k, g))
+
+    ths = [threading.Thread(target=client, args=(c,)) for c in range(4)]
+    for t in ths:
+        t.start()
+    mixed_ids = [srv.submit(ids[k], probes[k]) for k in range(4)]
+    for t in ths:
+        t.join()
+    mixed = [srv.poll(mixed_ids[k], ids[k], wait_ms=120000, want_ecg=True) for k in range(4)]
+    others = {}
+    for r, k, g in reqs:
+        out = srv.poll(r, ids[k], wait_ms=120000, want_ecg=True)
+        assert out is not None
+        others.setdefault(k, (g, out))
+    srv.close()
+    for k, (h, spec, grid, tm, leads, target) in enumerate(hearts):
+        at, layer = O.activation(grid, tm)
+        assert np.array_equal(h.activation().view(np.int64), at.view(np.int64)), spec.n
+        for g, out in ((probes[k], alone[k]), (probes[k], mixed[k]), others[k]):
+            lk = O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8],
+                             "endo-mid-epi", 0.6, g[:12])[0]
+            moved = O.move_leads(leads, g[12:].reshape(-1, 2))
+            ref = O.run(layer, at, lk, moved, "3D4", 0.0, float(steps), 1.0)
+            assert rel_l2(out[2], ref) <= TOL, spec.n
+            for l in range(spec.n_leads):
+                assert out[0][l] == pytest.approx(O.clamp(O.compare(2, ref[l], target[l])), abs=1e-4)
+        h.close()
+
+
+def test_served_many_and_criteria_only(engine):
+    """submit_many / poll_many hand over the same criteria as single submissions and polls; a server
+    without ECGs answers an ECG poll with an error; bad requests in a burst fail alone."""
+    from ekgsim_gb300.engine import EkgError, Server
+    hs = [_served_heart(engine, n, 60 + n) for n in (20, 28)]
+    srv = Server(engine, max_batch=32, max_wait_us=500, keep_ecg=False)
+    ids = [srv.add_heart(h) for h, _ in hs]
+    _, nc = hs[0][0].eval_shape()
+    genes = np.stack([synth.genes_for(hs[i % 2][1], 200 + i, 3) for i in range(24)])
+    hid = np.array([ids[i % 2] for i in range(24)], dtype=np.int32)
+    bad = genes.copy()
+    bad[5, 3] = np.nan
+    rids = srv.submit_many(hid, bad)
+    status, crit, viol, total, batch = srv.poll_many(rids, nc, wait_ms=120000)
+    assert status[5] == -1 and (np.delete(status, 5) == 0).all()
+    assert batch.max() > 1
+    for i in (0, 7, 23):
+        h = hs[i % 2][0]
+        c1, v1 = h.eval(genes[i])[:2]
+        assert np.allclose(crit[i], c1, rtol=0, atol=TOL)
+        assert viol[i] == v1
+    r = srv.submit(ids[0], genes[0])
+    with pytest.raises(EkgError):
+        srv.poll(r, ids[0], wait_ms=120000, want_ecg=True)
     srv.close()

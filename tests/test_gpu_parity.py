@@ -592,3 +592,52 @@ def test_queued_batches_match_synchronous(engine):
         for o in outs:
             for a in o:
                 E.host_unregister(a)
+
+
+def test_c3_batched_full_size(engine):
+    """The batched configuration at full size: 160^3 ellipsoid (wall 14, 3 layers), 12 leads, 600
+    steps, 256 distinct seeded vectors in one batched evaluation.  Activation times bitwise at
+    160^3; 8 results spread over the batch (first, last, middle, seeded random) against the FP64
+    oracle; every result against the per-simulation form of a second engine (batched form off)."""
+    from ekgsim_gb300.engine import Engine, Heart
+    c = synth.config(2)
+    spec, steps, batch = c["spec"], c["steps"], c["batch"]
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    target = [t for t in synth.analytic_target(spec.n_leads, steps, spec.seed + 999)]
+    h = Heart.create(engine, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+    at, layer = O.activation(grid, tm)
+    assert np.array_equal(h.activation().view(np.int64), at.view(np.int64))
+    h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], target, mid_position=0.6)
+    genes = np.stack([synth.genes_for(spec, r, 2) for r in range(batch)])
+    assert len({g.tobytes() for g in genes}) == batch
+    crit_b, viol_b, ecg_b = h.eval_batch(genes, want_ecg=True)
+    assert np.isfinite(ecg_b).all()
+    pick = sorted({0, batch // 2, batch - 1} | set(int(x) for x in np.random.Generator(np.random.PCG64(31)).choice(
+        np.arange(1, batch - 1), size=5, replace=False)))
+    assert len(pick) >= 8
+    for i in pick:
+        g = genes[i]
+        lk = O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], "endo-mid-epi",
+                         0.6, g[:12])[0]
+        moved = O.move_leads(leads, g[12:].reshape(-1, 2))
+        ref = O.run(layer, at, lk, moved, "3D4", 0.0, float(steps), 1.0)
+        assert rel_l2(ecg_b[i], ref) <= ECG_TOL, i
+        for l in range(spec.n_leads):
+            assert crit_b[i][l] == pytest.approx(O.clamp(O.compare(2, ref[l], target[l])), abs=1e-4)
+    h.close()
+    os.environ["EKG_BATCHED"] = "0"
+    try:
+        e2 = Engine(0)
+    finally:
+        os.environ.pop("EKG_BATCHED", None)
+    h2 = Heart.create(e2, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+    h2.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], target, mid_position=0.6)
+    crit_p, viol_p, ecg_p = h2.eval_batch(genes, want_ecg=True)
+    for i in range(batch):
+        assert rel_l2(ecg_b[i], ecg_p[i]) <= ECG_TOL, i
+    assert np.allclose(crit_b, crit_p, rtol=0, atol=1e-4)
+    assert np.array_equal(viol_b, viol_p)
+    h2.close()
+    e2.close()

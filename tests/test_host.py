@@ -216,3 +216,18 @@ def test_band_form_run_bounds():
     ts = 26.5 / c1
     e1 = np.exp2(-(c1 * ts)).astype(np.float32)
     assert np.all(np.float32(1.0) + e1 == np.float32(1.0))
+
+
+def test_oracle_naive_time_ranges_equal_whole_axis():
+    """The reference arm of the benchmark times the reference's per-voxel loop in slices of the time
+    axis; the slices give the same values as one pass over the whole axis (time advanced by += dt)."""
+    spec = synth.small_spec(16, n_leads=2)
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(3, spec.delays)
+    at, layer = O.activation(grid, tm)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    lk = O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], "endo-mid-epi", 0.6,
+                     synth.genes_for(spec, 0, 0)[:12])[0]
+    full = O.run_naive(layer, at, lk, leads, "3D4", 3.0, 80.0, 0.25)
+    parts = [O.run_naive_range(layer, at, lk, leads, "3D4", 3.0, 80.0, 0.25, k, k + 47) for k in range(0, 320, 47)]
+    assert np.array_equal(full, np.concatenate(parts, axis=1))

@@ -113,3 +113,53 @@ def test_reference_test_model_24_layers(tmp_path):
     assert printed_close(np.array([viol]), np.array([c["violation"]]))
     res = np.load(os.path.join(GOLD, "model24.npz"))["result"]
     assert printed_close(ecg.T, res[:, 1:])
+
+
+def _write_pre_files(name, tmp_path):
+    g = np.load(os.path.join(GOLD, f"{name}.npz"))
+    for fname in META["cases"][name].get("files", []):
+        with open(os.path.join(str(tmp_path), fname), "w") as f:
+            f.write(str(g["file_" + fname.replace(".", "_")]))
+    return g
+
+
+@pytest.mark.skipif("cells24" not in META["cases"], reason="no golden")
+def test_cell_aps_output(tmp_path):
+    """-out "cell_aps 0 3 17 250 100000": the cell APs with those reference apIndex numbers (first
+    appearance in raster order, simlib/simulator.cpp:570-590; the out-of-range one skipped), their
+    k vectors (k8 shifted by the activation time) in the header and their values at t = 0..699."""
+    c, s = make_case("cells24", tmp_path)
+    g = np.load(os.path.join(GOLD, "cells24.npz"))
+    crit, viol, ecg, lk, leads = O.evaluate(s, np.array(c["genes"]))
+    idx, al, aa = O.ap_indices(s.layer, s.at)
+    rows = g["cell_aps"]
+    assert rows.shape == (700, 5)
+    for j, a in enumerate((0, 3, 17, 250)):
+        k = lk[al[a] - 1].copy()
+        got = np.array([O.wohl(np.concatenate([k[:8], [k[8] - aa[a]]]), float(t) - aa[a]) for t in range(700)])
+        assert printed_close(got, rows[:, 1 + j], atol=1e-9), a
+
+
+@pytest.mark.skipif("exout24" not in META["cases"], reason="no golden")
+def test_excitation_sequence_export(tmp_path):
+    """[output files] excitation sequence: the exported text (simlib/simulator.cpp:71-106) equals
+    the reference's byte for byte."""
+    c, s = make_case("exout24", tmp_path)
+    g = np.load(os.path.join(GOLD, "exout24.npz"))
+    assert O.export_excitation(s.at) == str(g["excitation_out"])
+
+
+@pytest.mark.skipif("exin24" not in META["cases"], reason="no golden")
+def test_excitation_sequence_load(tmp_path):
+    """[model] excitation sequence: the run uses the loaded 3-decimal times (here a sequence of
+    other conduction delays) instead of the automaton's; criteria, printed ECG and the re-export
+    match the reference."""
+    c = META["cases"]["exin24"]
+    g = _write_pre_files("exin24", tmp_path)
+    c, s = make_case("exin24", tmp_path)
+    crit, viol, ecg, lk, leads = O.evaluate(s, np.array(c["genes"]))
+    assert printed_close(crit, np.array(c["criteria"]))
+    assert printed_close(ecg.T, g["result"][:, 1:])
+    assert O.export_excitation(s.at) == str(g["excitation_out"])
+    at_ca, _ = O.activation(s.raw, s.tm)
+    assert not np.array_equal(at_ca, s.at)  # the loaded sequence is not the heart's own
