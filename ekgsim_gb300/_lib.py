@@ -104,6 +104,12 @@ SIGNATURES = {
                                               P(c_uint64)]),
     "ekg_server_poll_many": (ctypes.c_int, [ctypes.c_void_p, c_int32, P(c_uint64), c_int32, c_int32, P(c_double),
                                             P(c_double), P(c_int32), P(RequestStats)]),
+    "ekg_heart_tune": (ctypes.c_int, [ctypes.c_void_p, c_int32, P(c_double), P(c_double), c_int32, P(c_double),
+                                      c_int32]),
+    "ekg_tune_candidates": (ctypes.c_int, [c_int32, c_int32, c_int32, P(c_int32), c_int32, P(c_int32)]),
+    "ekg_tune_cache_put": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, P(c_int32), c_double]),
+    "ekg_tune_cache_get": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, P(c_int32), P(c_double)]),
+    "ekg_selftest_bounded_wait": (ctypes.c_int, [c_int32, ctypes.c_uint32]),
     "ekg_server_set_free_bytes_provider": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "ekg_activation_noalloc": (ctypes.c_int, [c_int32, c_int32, c_int32, ctypes.c_void_p, c_int32, P(c_double),
                                               ctypes.c_void_p, P(c_int32)]),

@@ -1046,6 +1046,8 @@ void launch_gemm(cudaStream_t st, const BatchArgs &A) {
 
 // N of the band GEMM's row tiles: the smallest instance that holds the rows (one simulation's moved
 // leads fit 32), else the largest (256 with one basis, 128 with two).
+int small_operand_sims() { return SMALL_SIMS; }
+
 int batch_tile_rows(int two_bases, int rows_used) {
     if (rows_used <= 32) return 32;
     if (two_bases || rows_used <= 128) return 128;
@@ -1166,14 +1168,13 @@ void launch_sim_lead_field(cudaStream_t s, const HeartDev &h, const double *d_le
     EKG_CUDA(cudaGetLastError());
 }
 
-void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const float *k5l,
+void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, bool small, const float *k5l,
                              const float4 *hconst, const float4 *lrel, int nmove, int n_sims, const BandArgs &B,
                              uint8_t *Bt, int *work, int sm_count) {
     const int rows_used = n_sims * nmove;
     const int ngr = (rows_used + LF_THREADS * LF_ROWS - 1) / (LF_THREADS * LF_ROWS);
     const int nst = (int)(h.apad / BST);
     const bool diag = h.nhood == EKG_NHOOD_3D4;
-    const bool small = n_sims <= SMALL_SIMS;
     InteriorField ic;
     ic.A0 = h.interior_c[0];
     ic.A1 = h.interior_c[1];
@@ -1199,7 +1200,7 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, c
             nst, ngr, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p, \
             k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, B.stage_order, Bt, B.P1);      \
     } while (0)
-    switch (batch_tile_rows(two_bases, n_sims * nmove)) {
+    switch (tile_rows) {
     case 32:
         if (diag) EKG_LF(32, true);
         else EKG_LF(32, false);
@@ -1218,7 +1219,7 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, c
 
 void launch_batch_gemm(cudaStream_t s, const BatchArgs &A) {
     if (A.nitems == 0) return;
-    const int N = batch_tile_rows(A.two_bases, A.rows_used);
+    const int N = A.tile_rows > 0 ? A.tile_rows : batch_tile_rows(A.two_bases, A.rows_used);
     if (A.two_bases) {
         if (N == 32) launch_gemm<2, 32>(s, A);
         else launch_gemm<2, 128>(s, A);

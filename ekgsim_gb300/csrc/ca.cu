@@ -38,16 +38,16 @@ constexpr int MAX_LOCAL_ITERS = 64;
 __device__ __forceinline__ uint8_t layer_id(uint8_t v) { return v; }
 __device__ __forceinline__ uint8_t layer_id(int32_t v) { return (uint8_t)(v < 0 ? -v : v); }
 
+// One tile of a round (all threads of the block): stage, relax, write back, flag neighbours.
 template <typename LT>
-__global__ void k_ca_round(int nz, int ny, int nx, int ntz, int nty, int ntx, const LT *__restrict__ layers,
-                           const double *__restrict__ lag, int nl1, double *__restrict__ at,
-                           const int32_t *__restrict__ active, uint8_t *__restrict__ next_flag) {
+__device__ __forceinline__ void ca_tile(const int tile, int nz, int ny, int nx, int ntz, int nty, int ntx,
+                                        const LT *__restrict__ layers, const double *__restrict__ lag, int nl1,
+                                        double *__restrict__ at, uint8_t *__restrict__ next_flag) {
     __shared__ unsigned long long s_b[HS][HS][HS];  // activation-time bits
     __shared__ uint8_t s_l[HS][HS][HS];
     __shared__ uint8_t s_ch[2][HS][HS][HS];         // improved in the last sweep (tile interior)
     __shared__ uint32_t s_mark;  // 27-bit mask of neighbour tiles to flag (bit = (dz+1)*9+(dy+1)*3+(dx+1))
 
-    const int tile = active[blockIdx.x];
     const int tx0 = (tile % ntx) * TS;
     const int ty0 = ((tile / ntx) % nty) * TS;
     const int tz0 = (tile / (ntx * nty)) * TS;
@@ -193,6 +193,33 @@ __global__ void k_ca_round(int nz, int ny, int nx, int ntz, int nty, int ntx, co
     }
 }
 
+// A round with one block per active tile (the tile list's length is the grid).
+template <typename LT>
+__global__ void k_ca_round(int nz, int ny, int nx, int ntz, int nty, int ntx, const LT *__restrict__ layers,
+                           const double *__restrict__ lag, int nl1, double *__restrict__ at,
+                           const int32_t *__restrict__ active, uint8_t *__restrict__ next_flag) {
+    ca_tile<LT>(active[blockIdx.x], nz, ny, nx, ntz, nty, ntx, layers, lag, nl1, at, next_flag);
+}
+
+// A round over a device-resident tile list: a fixed grid walks the count_cur active tiles, so
+// rounds can be queued back to back without the host reading the count.  Block 0 clears the next
+// round's count, which only the compaction after this kernel adds to.
+__global__ void __launch_bounds__(CA_THREADS) k_ca_round_list(int nz, int ny, int nx, int ntz, int nty, int ntx,
+                                                              const uint8_t *__restrict__ layers,
+                                                              const double *__restrict__ lag, int nl1,
+                                                              double *__restrict__ at,
+                                                              const int32_t *__restrict__ active,
+                                                              const int32_t *__restrict__ count_cur,
+                                                              int32_t *__restrict__ count_next,
+                                                              uint8_t *__restrict__ next_flag) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *count_next = 0;
+    const int n = *count_cur;
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        ca_tile<uint8_t>(active[i], nz, ny, nx, ntz, nty, ntx, layers, lag, nl1, at, next_flag);
+        __syncthreads();  // the next tile restages the shared arrays
+    }
+}
+
 // next_flag -> compact list (order irrelevant); clears the flags.
 __global__ void k_ca_compact(int ntiles, uint8_t *__restrict__ flag, int32_t *__restrict__ list,
                              int32_t *__restrict__ count) {
@@ -225,53 +252,63 @@ __global__ void k_ca_finish(size_t n, double *__restrict__ at) {
 }  // namespace
 
 CaResult ca_run(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_layers, const uint8_t *d_start,
-                const std::vector<int32_t> &start_tiles, int nl1, const double *d_lag, double *d_at,
-                uint32_t *d_err) {
-    (void)d_err;
+                const std::vector<int32_t> &start_tiles, int nl1, const double *d_lag, double *d_at, int round_cap,
+                int sm_count) {
     CaResult res;
     const int ntz = (nz + TS - 1) / TS, nty = (ny + TS - 1) / TS, ntx = (nx + TS - 1) / TS;
     const int ntiles = ntz * nty * ntx;
     const size_t n = (size_t)nz * ny * nx;
-    DBuf<int32_t> list_a, list_b, count;
+    DBuf<int32_t> lists, count;
     DBuf<uint8_t> flag;
-    list_a.alloc(ntiles);
-    list_b.alloc(ntiles);
+    lists.alloc(2 * (size_t)ntiles);
     count.alloc(2);
     flag.alloc(ntiles);
+    int32_t *list[2] = {lists.p, lists.p + ntiles};
+    const int32_t n_start = (int32_t)start_tiles.size();
     EKG_CUDA(cudaMemsetAsync(flag.p, 0, ntiles, s));
-    EKG_CUDA(cudaMemcpyAsync(list_a.p, start_tiles.data(), start_tiles.size() * sizeof(int32_t),
+    EKG_CUDA(cudaMemcpyAsync(list[0], start_tiles.data(), start_tiles.size() * sizeof(int32_t),
                              cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(count.p, &n_start, sizeof(int32_t), cudaMemcpyHostToDevice, s));
     cudaEvent_t e0, e1;
     EKG_CUDA(cudaEventCreate(&e0));
     EKG_CUDA(cudaEventCreate(&e1));
     EKG_CUDA(cudaEventRecord(e0, s));
     k_ca_init<<<1024, 256, 0, s>>>(n, d_layers, d_start, d_at);
     EKG_CUDA(cudaGetLastError());
-    int n_active = (int)start_tiles.size();
     // Every round finalises at least the next tile along each shortest path; a path can
     // cross a tile boundary at most once per hop, so this cap is far above any real heart.
-    const int cap = 16 * (ntz + nty + ntx) + 4 * ntiles + 64;
-    int32_t *cur = list_a.p, *nxt = list_b.p;
+    const int cap = round_cap > 0 ? round_cap : 16 * (ntz + nty + ntx) + 4 * ntiles + 64;
+    // Rounds are queued in chunks (round over the device-resident list, then its compaction); the
+    // host reads the active count once per chunk.  Rounds after convergence find an empty list.
+    constexpr int CHUNK = 8;
+    int blocks_per_sm = 0;
+    EKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_ca_round_list, CA_THREADS, 0));
+    const int grid = std::max(1, std::min(ntiles, std::max(1, blocks_per_sm) * std::max(1, sm_count)));
     int32_t *h_count = nullptr;
     EKG_CUDA(cudaMallocHost(&h_count, sizeof(int32_t)));
+    int n_active = n_start, r = 0;
     while (n_active > 0) {
-        if (res.rounds >= cap) {
+        if (r >= cap) {
             cudaFreeHost(h_count);
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
             throw Error{EKG_ERR_CA_NOT_CONVERGED, "activation-time relaxation did not converge"};
         }
-        k_ca_round<uint8_t><<<n_active, CA_THREADS, 0, s>>>(nz, ny, nx, ntz, nty, ntx, d_layers, d_lag, nl1, d_at,
-                                                           cur, flag.p);
-        EKG_CUDA(cudaGetLastError());
-        EKG_CUDA(cudaMemsetAsync(count.p, 0, sizeof(int32_t), s));
-        k_ca_compact<<<(ntiles + 255) / 256, 256, 0, s>>>(ntiles, flag.p, nxt, count.p);
-        EKG_CUDA(cudaGetLastError());
-        EKG_CUDA(cudaMemcpyAsync(h_count, count.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        const int chunk = std::min(CHUNK, cap - r);
+        for (int k = 0; k < chunk; ++k, ++r) {
+            const int c = r & 1;
+            k_ca_round_list<<<grid, CA_THREADS, 0, s>>>(nz, ny, nx, ntz, nty, ntx, d_layers, d_lag, nl1, d_at,
+                                                       list[c], count.p + c, count.p + (c ^ 1), flag.p);
+            EKG_CUDA(cudaGetLastError());
+            k_ca_compact<<<(ntiles + 255) / 256, 256, 0, s>>>(ntiles, flag.p, list[c ^ 1], count.p + (c ^ 1));
+            EKG_CUDA(cudaGetLastError());
+        }
+        EKG_CUDA(cudaMemcpyAsync(h_count, count.p + (r & 1), sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         EKG_CUDA(cudaStreamSynchronize(s));
         n_active = *h_count;
-        std::swap(cur, nxt);
-        ++res.rounds;
     }
     cudaFreeHost(h_count);
+    res.rounds = r;
     k_ca_finish<<<1024, 256, 0, s>>>(n, d_at);
     EKG_CUDA(cudaGetLastError());
     EKG_CUDA(cudaEventRecord(e1, s));

@@ -18,6 +18,14 @@ struct ekg_engine {
     bool batched = true;  // separable batched form for multi-simulation passes (EKG_BATCHED=0 disables)
     int batch_ctas = 0;   // target CTAs of the moved-lead GEMM (0 = one wave)
     bool graphs = true;   // replay repeated passes as CUDA graphs (EKG_GRAPHS=0 disables)
+    // rounds after which the activation-time relaxation gives up with EKG_ERR_CA_NOT_CONVERGED
+    // (0 = the default bound from the grid size; EKG_CA_ROUND_CAP sets it, e.g. to test that error)
+    int ca_round_cap = 0;
+    // autotuning of the batched form's launch shapes: EKG_TUNE=1 tunes every new pass shape on its
+    // first pass (ekg_heart_tune does it on request); EKG_TUNE_CACHE names a file that keeps the
+    // choices across processes
+    bool tune = false;
+    std::string tune_cache;
 };
 
 namespace ekg {
@@ -65,11 +73,21 @@ struct BatchState {
     DBuf<float2> U, Up;                    // [rows][nl][max_ent] steady sums (U0, U1), per K part
     DBuf<float> partial;                   // [items][rows][128] raw accumulators (x2 with two bases)
 };
+// Launch shape of the batched form's moved-lead kernels, chosen by the autotuner (0 / -1 = the
+// built-in choice): the band GEMM's row tile (32, 128 or 256 rows of (simulation, moved lead)),
+// its work-item target in CTAs per SM, and the operand kernel's form (1: one thread per (AP,
+// simulation); 0: the persistent kernel with four rows per thread).
+struct TuneChoice {
+    int tile_rows = 0, cta_mult = 0, op_small = -1;
+    double ms = 0;        // device time of one pass with this shape (CUDA events)
+    int candidates = 0;   // shapes timed when it was chosen
+};
 // What one device pass does, decided on the host from the batch's layer APs and lead positions.
 struct PassPlan {
     bool batch = false;                    // separable batched form
     int n_sims = 0, nmove = 0, J = 0, two_bases = 0;
     int rows_used = 0, rows = 0, ntiles = 0, nitems = 0;
+    int tile_rows = 0, op_small = 0;       // launch shape (see TuneChoice)
     std::vector<double> k3;                // [S][nl]
     std::vector<int4> items;               // band GEMM work items, grouped by tile
     std::vector<int32_t> ti0, ti1;         // [ntt][nl] item range of each (tile, layer)
@@ -188,4 +206,7 @@ struct ekg_heart {
     bool any_k0 = false;              // some layer AP of the current pass has k0 != 0
     bool cpre_on = false;             // the current pass's repolarisation constants come from the host
     ekg::SimConfig cfg;
+    // autotuned launch shapes by pass shape (tune_key), and a shape forced while the tuner times it
+    std::map<std::string, ekg::TuneChoice> tuned;
+    const ekg::TuneChoice *tune_force = nullptr;
 };

@@ -129,8 +129,8 @@ struct CaResult {
 // layers_u8: stripped layer per cell; start flags in `is_start`; lag: [nl1][nl1][3] FP64 with
 // lag[s][d][k-1] = T[s][d] * sqrt(k).  at_out: FP64 per cell (0 for empty / unreachable).
 CaResult ca_run(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_layers, const uint8_t *d_start,
-                const std::vector<int32_t> &start_tiles, int nl1, const double *d_lag, double *d_at,
-                uint32_t *d_err);
+                const std::vector<int32_t> &start_tiles, int nl1, const double *d_lag, double *d_at, int round_cap,
+                int sm_count);
 
 // ------------------------------------------------------------------ ECG kernels (ecg.cu)
 // Heart-resident device arrays used by the simulation kernels.
@@ -247,7 +247,7 @@ void launch_contract_umma_args(cudaStream_t s, const ContractArgs &a);
 // ------------------------------------------------------------------ batched form (batch.cu)
 struct BatchArgs {
     int steps = 0, nl = 0, nkt = 0, rows = 0, rows_used = 0, nmove = 0, n_sims = 0, ntiles = 0, nitems = 0,
-        two_bases = 0;
+        two_bases = 0, tile_rows = 0;
     const float2 *t_hilo = nullptr, *at_hilo = nullptr;
     const int4 *items = nullptr;  // (t tile, first stage, end stage, layer), stages of 32 APs
     const float4 *hconst = nullptr;
@@ -276,6 +276,7 @@ struct BandArgs {
     float2 *ecg_ff = nullptr;
 };
 int batch_tile_rows(int two_bases, int rows_used);
+int small_operand_sims();  // passes up to this many simulations use the per-(AP, simulation) operand kernel
 void launch_taylor_w(cudaStream_t s, const HeartDev &h, const float *W0, int J, const double *centre,
                      const double *scale, float *Wt);
 void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int32_t *lc0, const int32_t *lc1,
@@ -283,7 +284,7 @@ void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int
 void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const float *F,
                            const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg,
                            float2 *ecg_ff);
-void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int two_bases, const float *k5l,
+void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, bool small, const float *k5l,
                              const float4 *hconst, const float4 *lrel, int nmove, int n_sims, const BandArgs &B,
                              uint8_t *Bt, int *work, int sm_count);
 void launch_batch_gemm(cudaStream_t s, const BatchArgs &a);

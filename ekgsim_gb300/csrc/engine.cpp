@@ -361,7 +361,8 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
         h->at_cells.alloc(n);
         EKG_CUDA(cudaMemcpyAsync(ds.p, st.data(), n, cudaMemcpyHostToDevice, s));
         EKG_CUDA(cudaMemcpyAsync(dlag.p, lag.data(), lag.size() * 8, cudaMemcpyHostToDevice, s));
-        CaResult r = ca_run(s, d->nz, d->ny, d->nx, dl.p, ds.p, start_tiles, nl1, dlag.p, h->at_cells.p, nullptr);
+        CaResult r = ca_run(s, d->nz, d->ny, d->nx, dl.p, ds.p, start_tiles, nl1, dlag.p, h->at_cells.p,
+                            h->eng->ca_round_cap, h->sm_count);
         h->ca_rounds = r.rounds;
         h->ca_ms = r.ms;
         EKG_CUDA(cudaStreamSynchronize(s));
@@ -745,6 +746,63 @@ void ensure_basis(ekg_heart *h, const std::vector<double> &key) {
     B.basis_ok = true;
 }
 
+// ------------------------------------------------------------------ autotuner (batched form)
+// A pass shape is the heart (grid, voxels, APs, leads, steps, neighbourhood, SM count) with the
+// pass's simulations, moved leads and bases; the tuner keeps one launch shape per pass shape.
+std::string tune_key(const ekg_heart *h, int n_sims, int nmove, int two_bases) {
+    std::ostringstream k;
+    k << "sm" << h->sm_count << ":" << h->nz << "x" << h->ny << "x" << h->nx << ":v" << h->nvox << ":a" << h->naps
+      << ":L" << h->dev.nleads << ":T" << h->dev.steps << ":nh" << h->nhood << ":S" << n_sims << ":m" << nmove
+      << ":b" << two_bases;
+    return k.str();
+}
+
+// Launch shapes worth timing: row tiles 32 / 128 / 256 (256 not with two bases; a tile at most
+// twice the rows used), GEMM work-item targets of 1, 2 and 4 CTAs per SM, and for passes of up to
+// 64 simulations both operand-kernel forms.
+std::vector<TuneChoice> tune_candidates(int two_bases, int rows_used, int n_sims) {
+    std::vector<TuneChoice> c;
+    for (int N : {32, 128, 256}) {
+        if (N == 256 && two_bases) continue;
+        if (N > 32 && N / 2 >= rows_used) continue;
+        for (int mult : {1, 2, 4})
+            for (int small : {1, 0}) {
+                if (small && n_sims > 64) continue;
+                TuneChoice t;
+                t.tile_rows = N;
+                t.cta_mult = mult;
+                t.op_small = small;
+                c.push_back(t);
+            }
+    }
+    return c;
+}
+
+// Cache file: one line per pass shape, "key tile_rows cta_mult op_small ms candidates"; later lines
+// win.
+void tune_cache_write(const std::string &path, const std::string &key, const TuneChoice &t) {
+    std::ofstream f(path, std::ios::app);
+    if (!f) throw Error{EKG_ERR_IO, "could not open autotuner cache " + path};
+    f << key << " " << t.tile_rows << " " << t.cta_mult << " " << t.op_small << " " << t.ms << " " << t.candidates
+      << "\n";
+}
+bool tune_cache_read(const std::string &path, const std::string &key, TuneChoice &out) {
+    std::ifstream f(path);
+    bool found = false;
+    for (std::string line; std::getline(f, line);) {
+        std::istringstream ss(line);
+        std::string k;
+        TuneChoice t;
+        if (!(ss >> k >> t.tile_rows >> t.cta_mult >> t.op_small >> t.ms >> t.candidates)) continue;
+        if (k != key) continue;
+        if (t.tile_rows != 32 && t.tile_rows != 128 && t.tile_rows != 256) continue;
+        if (t.cta_mult < 1 || t.cta_mult > 64 || t.op_small < 0 || t.op_small > 1) continue;
+        out = t;
+        found = true;
+    }
+    return found;
+}
+
 // Decide the pass: the batched (separable) form when the batch shares k1 and k4 per layer, no
 // layer has k0 != 0, exp(k5 at) has a short Taylor expansion and there are at least two sims.
 PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *leads) {
@@ -799,7 +857,20 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
                               (float)layer_k[9 * i + 3]);
     if (P.nmove > 0) {
         P.rows_used = n_sims * P.nmove;
-        const int N = batch_tile_rows(P.two_bases, P.rows_used);
+        // launch shape: the autotuner's choice for this pass shape, else the built-in one
+        const TuneChoice *tc = h->tune_force;
+        if (!tc) {
+            const std::string key = tune_key(h, n_sims, P.nmove, P.two_bases);
+            auto it = h->tuned.find(key);
+            if (it == h->tuned.end() && !h->eng->tune_cache.empty()) {
+                TuneChoice t;
+                if (tune_cache_read(h->eng->tune_cache, key, t)) it = h->tuned.emplace(key, t).first;
+            }
+            if (it != h->tuned.end()) tc = &it->second;
+        }
+        const int N = tc && tc->tile_rows > 0 ? tc->tile_rows : batch_tile_rows(P.two_bases, P.rows_used);
+        P.tile_rows = N;
+        P.op_small = tc && tc->op_small >= 0 ? tc->op_small : (n_sims <= small_operand_sims() ? 1 : 0);
         P.ntiles = (P.rows_used + N - 1) / N;
         P.rows = P.ntiles * N;
         // band work items: each (tile, layer) band cut into pieces of at most `per` stages, `per`
@@ -807,7 +878,8 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
         const int ntt = B.ntt;
         int64_t total = 0;
         for (size_t i = 0; i < B.band_s0.size(); ++i) total += B.band_s1[i] - B.band_s0[i];
-        const int target = std::max(1, h->eng->batch_ctas > 0 ? h->eng->batch_ctas : h->sm_count * (N <= 32 ? 2 : 1));
+        const int mult = tc && tc->cta_mult > 0 ? tc->cta_mult : (N <= 32 ? 2 : 1);
+        const int target = std::max(1, h->eng->batch_ctas > 0 ? h->eng->batch_ctas : h->sm_count * mult);
         int64_t per = std::max<int64_t>(1, (total * P.ntiles + target - 1) / target);
         for (;; ++per) {
             int64_t cnt = 0;
@@ -1014,8 +1086,8 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             U.ecg = E.ecg.p;
             U.ecg_ff = E.ecg_ff.p;
             if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[4], s));
-            launch_batch_lead_field(s, D, P.two_bases, in.k5l, in.hconst, in.lrel, nmove, n_sims, U, B.Bt.p,
-                                    B.work.p, h->sm_count);
+            launch_batch_lead_field(s, D, P.tile_rows, P.op_small != 0, in.k5l, in.hconst, in.lrel, nmove, n_sims, U,
+                                    B.Bt.p, B.work.p, h->sm_count);
             if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[5], s));
             if (fork) {
                 EKG_CUDA(cudaEventRecord(h->ev_op, s));
@@ -1036,6 +1108,7 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             A.ntiles = P.ntiles;
             A.nitems = P.nitems;
             A.two_bases = P.two_bases;
+            A.tile_rows = P.tile_rows;
             A.t_hilo = D.t_hilo.p;
             A.at_hilo = D.at_hilo.p;
             A.items = in.items;
@@ -1106,7 +1179,7 @@ std::vector<uint64_t> pass_signature(const ekg_heart *h, const PassPlan &P, int 
                                (uint64_t)P.two_bases, (uint64_t)P.rows, (uint64_t)P.rows_used, (uint64_t)P.ntiles,
                                (uint64_t)P.nitems, (uint64_t)ncl, (uint64_t)mode, (uint64_t)mark_static,
                                (uint64_t)h->cpre_on, (uint64_t)h->any_k0, (uint64_t)h->eng->contract, (uint64_t)B.J,
-                               (uint64_t)B.max_ent, (uint64_t)B.ntt};
+                               (uint64_t)B.max_ent, (uint64_t)B.ntt, (uint64_t)P.tile_rows, (uint64_t)P.op_small};
     const ekg_heart::PassInputs &in = h->in();
     for (const void *p : {(const void *)in.layer_k, (const void *)in.cpre, (const void *)in.leads, (const void *)in.k3,
                           (const void *)B.d_centre.p, (const void *)B.d_scale.p, (const void *)E.coef.p,
@@ -1175,6 +1248,8 @@ void run_pass(ekg_heart *h, const PassPlan &P, int ncl, int mode, bool mark_stat
 
 void assemble_criteria(const ekg_heart *h, const double *crit2, bool done, double approx_crit,
                        const std::vector<double> &approx, double endo_epi, double *out);
+TuneChoice tune_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *leads, int reps,
+                     double *builtin_ms);
 
 // Queues one device pass from the current staging buffer (h->cur): plan, upload, the pass (a graph
 // replay) and the copies of its outputs (ECG to ecg_host; criterion values and the error word to
@@ -1203,6 +1278,12 @@ void launch_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *
         pd.crit2_cap = 0;
         EKG_CUDA(cudaMallocHost(&pd.crit2, need * sizeof(double)));
         pd.crit2_cap = need;
+    }
+    if (h->eng->tune && n_sims > 1) {
+        // tune a new pass shape on its first pass (the choice is kept for the heart)
+        const PassPlan Pt = plan_pass(h, n_sims, layer_k, leads);
+        if (Pt.batch && Pt.nmove > 0 && !h->tuned.count(tune_key(h, n_sims, Pt.nmove, Pt.two_bases)))
+            tune_pass(h, n_sims, layer_k, leads, 3, nullptr);
     }
     const PassPlan P = plan_pass(h, n_sims, layer_k, leads);
     upload_inputs(h, P, layer_k, leads);
@@ -1324,7 +1405,7 @@ void benchmark(ekg_heart *h, int n_sims, const double *layer_k, const double *le
     if (op) {
         const HeartDev &D = h->dev;
         const BatchState &B = h->bs;
-        const int N = batch_tile_rows(P.two_bases, P.rows_used), nb = P.two_bases ? 2 : 1;
+        const int N = P.tile_rows, nb = P.two_bases ? 2 : 1;
         for (const int4 &it : P.items) gemm_flops += (double)(it.z - it.y) * P.ntiles * 128.0 * N * 32 * 2 * 3 * nb;
         std::vector<int32_t> nent(D.nlayers), esp((size_t)D.nlayers * 8), ls0(D.nlayers);
         EKG_CUDA(cudaMemcpy(nent.data(), B.nent.p, D.nlayers * 4, cudaMemcpyDeviceToHost));
@@ -1351,6 +1432,67 @@ void benchmark(ekg_heart *h, int n_sims, const double *layer_k, const double *le
     cudaEventDestroy(t1);
     EKG_CUDA(cudaMemcpy(h->err_host, h->ev.err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     if (*h->err_host) throw Error{EKG_ERR_TIMEOUT, "a bounded device wait ran out"};
+}
+
+// Times every candidate launch shape of the batched form for a pass of n_sims simulations with these
+// inputs (CUDA events on the heart's stream, `reps` passes each after one untimed pass), keeps the
+// fastest for this pass shape and appends it to the cache file.  out: the choice (with its ms and
+// the number of candidates) and the built-in shape's ms.  Passes without moved leads or outside the
+// batched form have nothing to tune (candidates = 0).  The caller holds the heart's lock.
+TuneChoice tune_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *leads, int reps,
+                     double *builtin_ms) {
+    drain_pending(h);
+    EKG_CUDA(cudaSetDevice(h->eng->device));
+    h->tune_force = nullptr;
+    const PassPlan P0 = plan_pass(h, n_sims, layer_k, leads);
+    TuneChoice best;
+    if (builtin_ms) *builtin_ms = 0;
+    if (!P0.batch || P0.nmove == 0) return best;
+    const std::string key = tune_key(h, n_sims, P0.nmove, P0.two_bases);
+    std::vector<TuneChoice> cands = tune_candidates(P0.two_bases, P0.rows_used, n_sims);
+    const int ncl = h->has_eval ? h->es.n_crit_leads : 0;
+    const int mode = h->has_eval ? h->es.comparison_mode : 2;
+    cudaStream_t s = h->stream;
+    cudaEvent_t a, b;
+    EKG_CUDA(cudaEventCreate(&a));
+    EKG_CUDA(cudaEventCreate(&b));
+    struct Restore {
+        ekg_heart *h;
+        cudaEvent_t a, b;
+        ~Restore() {
+            h->tune_force = nullptr;
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+    } restore{h, a, b};
+    double best_ms = 1e30;
+    for (TuneChoice &c : cands) {
+        h->tune_force = &c;
+        const PassPlan P = plan_pass(h, n_sims, layer_k, leads);
+        upload_inputs(h, P, layer_k, leads);
+        compute(h, P, ncl, mode, nullptr);
+        EKG_CUDA(cudaEventRecord(a, s));
+        for (int r = 0; r < reps; ++r) compute(h, P, ncl, mode, nullptr);
+        EKG_CUDA(cudaEventRecord(b, s));
+        EKG_CUDA(cudaEventSynchronize(b));
+        float ms = 0;
+        EKG_CUDA(cudaEventElapsedTime(&ms, a, b));
+        EKG_CUDA(cudaMemcpy(h->err_host, h->ev.err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        if (*h->err_host) throw Error{EKG_ERR_TIMEOUT, "a bounded device wait ran out (autotuner)"};
+        c.ms = ms / reps;
+        const int bN = batch_tile_rows(P0.two_bases, P0.rows_used);
+        const bool builtin = c.tile_rows == bN && c.op_small == (n_sims <= small_operand_sims() ? 1 : 0) &&
+                             c.cta_mult == (bN <= 32 ? 2 : 1);
+        if (builtin && builtin_ms) *builtin_ms = c.ms;
+        if (c.ms < best_ms) {
+            best_ms = c.ms;
+            best = c;
+        }
+    }
+    best.candidates = (int)cands.size();
+    h->tuned[key] = best;
+    if (!h->eng->tune_cache.empty()) tune_cache_write(h->eng->tune_cache, key, best);
+    return best;
 }
 
 // Per-simulation host part of SimImplementation::eval (sim.cpp:443-492): genes -> layer APs and
@@ -1647,6 +1789,9 @@ int ekg_engine_create(int device, ekg_engine **out) {
         if (const char *v = std::getenv("EKG_BATCHED")) e->batched = std::string(v) != "0";
         if (const char *v = std::getenv("EKG_BATCH_CTAS")) e->batch_ctas = std::atoi(v);
         if (const char *v = std::getenv("EKG_GRAPHS")) e->graphs = std::string(v) != "0";
+        if (const char *v = std::getenv("EKG_CA_ROUND_CAP")) e->ca_round_cap = std::max(0, std::atoi(v));
+        if (const char *v = std::getenv("EKG_TUNE")) e->tune = std::string(v) == "1";
+        if (const char *v = std::getenv("EKG_TUNE_CACHE")) e->tune_cache = v;
         EKG_CUDA(cudaSetDevice(device));
         EKG_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
         *out = e.release();
@@ -1879,6 +2024,63 @@ int ekg_heart_benchmark(ekg_heart *h, int32_t n_sims, const double *layer_k, con
             leads = lds.data();
         }
         benchmark(h, n_sims, layer_k, leads, warmup, iters, out, n_out);
+    });
+}
+
+int ekg_heart_tune(ekg_heart *h, int32_t n_sims, const double *layer_k, const double *leads, int32_t reps, double *out,
+                   int32_t n_out) {
+    return guard([&] {
+        EKG_CHECK(h && layer_k && out && n_sims >= 1 && reps >= 1, EKG_ERR_BAD_INPUT, "bad argument");
+        std::vector<double> lds;
+        if (!leads) {
+            for (int i = 0; i < n_sims; ++i) lds.insert(lds.end(), h->leads0.begin(), h->leads0.end());
+            leads = lds.data();
+        }
+        std::lock_guard<std::mutex> lk(h->mu);
+        double builtin = 0;
+        const TuneChoice t = tune_pass(h, n_sims, layer_k, leads, reps, &builtin);
+        const double v[6] = {(double)t.tile_rows, (double)t.cta_mult, (double)t.op_small, t.ms, builtin,
+                             (double)t.candidates};
+        for (int i = 0; i < n_out && i < 6; ++i) out[i] = v[i];
+    });
+}
+
+int ekg_tune_candidates(int32_t two_bases, int32_t rows_used, int32_t n_sims, int32_t *shapes_out, int32_t max_shapes,
+                        int32_t *n_out) {
+    return guard([&] {
+        EKG_CHECK(shapes_out && n_out && rows_used >= 1 && n_sims >= 1 && max_shapes >= 0, EKG_ERR_BAD_INPUT,
+                  "bad argument");
+        const std::vector<TuneChoice> c = tune_candidates(two_bases, rows_used, n_sims);
+        *n_out = (int32_t)c.size();
+        for (int i = 0; i < (int)c.size() && i < max_shapes; ++i) {
+            shapes_out[3 * i] = c[i].tile_rows;
+            shapes_out[3 * i + 1] = c[i].cta_mult;
+            shapes_out[3 * i + 2] = c[i].op_small;
+        }
+    });
+}
+
+int ekg_tune_cache_put(const char *path, const char *key, const int32_t *shape, double ms) {
+    return guard([&] {
+        EKG_CHECK(path && key && shape && std::strchr(key, ' ') == nullptr && *key, EKG_ERR_BAD_INPUT, "bad argument");
+        TuneChoice t;
+        t.tile_rows = shape[0];
+        t.cta_mult = shape[1];
+        t.op_small = shape[2];
+        t.ms = ms;
+        tune_cache_write(path, key, t);
+    });
+}
+
+int ekg_tune_cache_get(const char *path, const char *key, int32_t *shape_out, double *ms_out) {
+    return guard([&] {
+        EKG_CHECK(path && key && shape_out, EKG_ERR_BAD_INPUT, "bad argument");
+        TuneChoice t;
+        if (!tune_cache_read(path, key, t)) throw Error{EKG_ERR_NOT_FOUND, "no autotuner entry for that key"};
+        shape_out[0] = t.tile_rows;
+        shape_out[1] = t.cta_mult;
+        shape_out[2] = t.op_small;
+        if (ms_out) *ms_out = t.ms;
     });
 }
 

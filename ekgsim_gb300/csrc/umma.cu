@@ -373,4 +373,50 @@ void launch_contract_umma(cudaStream_t s, const HeartDev &h, const float *d_Wp, 
     launch_contract_umma_args(s, A);
 }
 
+// ------------------------------------------------------------------ bounded-wait self-test
+// One block does what a contraction CTA does around a wait that runs out: warp 0 takes tensor
+// memory, thread 0 waits on an mbarrier that nothing arrives on (the kernels' bounded wait with a
+// short poll limit), records KERR_MBAR_TIMEOUT in the error word, and warp 0 releases the tensor
+// memory before the block returns.  Nothing else waits, so the kernel always ends.
+__global__ void k_selftest_bounded_wait(uint32_t limit, uint32_t *err) {
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    const int warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        ptx::mbar_init(&bar, 1);
+        ptx::fence_barrier_init();
+    }
+    if (warp == 0) {
+        ptx::tmem_alloc(&tmem_base, 32);
+        ptx::tmem_relinquish();
+    }
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    if (threadIdx.x == 0 && !ptx::mbar_wait_n(&bar, 0, limit)) atomicOr(err, KERR_MBAR_TIMEOUT);
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    if (warp == 0) ptx::tmem_dealloc(tmem_base, 32);
+}
+
 }  // namespace ekg
+
+extern "C" int ekg_selftest_bounded_wait(int32_t device, uint32_t wait_limit) {
+    using namespace ekg;
+    return guard([&] {
+        EKG_CHECK(wait_limit >= 1 && wait_limit <= ptx::WAIT_LIMIT, EKG_ERR_BAD_INPUT,
+                  "wait limit must be in 1 .. the kernels' own limit");
+        EKG_CUDA(cudaSetDevice(device));
+        DBuf<uint32_t> err;
+        err.alloc(1);
+        EKG_CUDA(cudaMemset(err.p, 0, sizeof(uint32_t)));
+        k_selftest_bounded_wait<<<1, 128>>>(wait_limit, err.p);
+        EKG_CUDA(cudaGetLastError());
+        EKG_CUDA(cudaDeviceSynchronize());
+        uint32_t e = 0;
+        EKG_CUDA(cudaMemcpy(&e, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        if (e & KERR_MBAR_TIMEOUT)
+            throw Error{EKG_ERR_TIMEOUT, "a bounded device wait ran out (error word " + std::to_string(e) + ")"};
+    });
+}

@@ -140,6 +140,17 @@ class Heart:
                     operand_bytes=out[9], band_bytes=out[10], iters=iters, n_sims=n)
 
     # ------------------------------------------------------------------ evaluation
+    def tune(self, layer_k: np.ndarray, leads_zyx: Optional[np.ndarray] = None, reps: int = 3) -> dict:
+        """Autotune the batched form's launch shapes for passes like this one (ekg_heart_tune)."""
+        lk = np.ascontiguousarray(layer_k, dtype=np.float64)
+        n = lk.shape[0]
+        ld = None if leads_zyx is None else np.ascontiguousarray(leads_zyx, dtype=np.float64)
+        out = np.zeros(6)
+        check(self._lib.ekg_heart_tune(self._h, n, dptr(lk), dptr(ld), reps, dptr(out), 6))
+        return {"tile_rows": int(out[0]), "ctas_per_sm": int(out[1]), "operand_form":
+                "per-(AP, simulation)" if out[2] == 1 else "persistent", "ms": float(out[3]),
+                "builtin_ms": float(out[4]), "candidates": int(out[5])}
+
     def set_eval(self, base_aps, k_min, k_max, free_k, targets, target_offsets=None, **kw):
         """Evaluation settings (ekg_heart_set_eval); keyword arguments as ``eval_config``."""
         self._cfg = eval_config(base_aps, k_min, k_max, free_k, targets, target_offsets, **kw)

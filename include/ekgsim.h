@@ -133,6 +133,31 @@ int ekg_simulate(ekg_heart *h, const double *layer_k, const double *leads_zyx, d
 int ekg_heart_benchmark(ekg_heart *h, int32_t n_sims, const double *layer_k, const double *leads, int32_t warmup,
                         int32_t iters, double *out, int32_t n_out);
 
+/* Autotuner of the batched form's launch shapes (no counterpart in the reference, which has no
+ * device).  For a pass of n_sims simulations with these inputs (as ekg_heart_benchmark takes them)
+ * it times every candidate shape of the moved-lead kernels -- band GEMM row tile 32 / 128 / 256,
+ * GEMM work-item target of 1 / 2 / 4 CTAs per SM, and for up to 64 simulations the operand
+ * kernel's per-(AP, simulation) or persistent form -- with CUDA events on the heart's stream
+ * (`reps` passes each after one untimed pass), keeps the fastest for every later pass of this
+ * shape on this heart, and appends it to the file named by the EKG_TUNE_CACHE environment variable
+ * (read at engine creation; engines read it back for the same pass shape).  With EKG_TUNE=1 every
+ * new pass shape is tuned on its first batched pass.  out (up to 6 values): row tile, CTAs per SM,
+ * operand form (1 per-(AP, simulation), 0 persistent), ms per pass of the choice, ms per pass of
+ * the built-in shape, candidates timed (0: the pass has no moved leads or is not in the batched
+ * form, so there is nothing to tune).  Results of every shape are within the engine's tolerance of
+ * one another (the shapes change FP32 summation order only). */
+int ekg_heart_tune(ekg_heart *h, int32_t n_sims, const double *layer_k, const double *leads, int32_t reps,
+                   double *out, int32_t n_out);
+/* The candidate shapes the tuner times for a pass (host only): shapes_out receives up to
+ * max_shapes triples (row tile, CTAs per SM, operand form), *n_out their number. */
+int ekg_tune_candidates(int32_t two_bases, int32_t rows_used, int32_t n_sims, int32_t *shapes_out,
+                        int32_t max_shapes, int32_t *n_out);
+/* The tuner's cache file (host only): one line per pass shape, "key rows ctas form ms candidates",
+ * later lines winning.  _put appends a shape (triple as above) for `key` (no spaces); _get reads the
+ * last valid one (EKG_ERR_NOT_FOUND when there is none). */
+int ekg_tune_cache_put(const char *path, const char *key, const int32_t *shape, double ms);
+int ekg_tune_cache_get(const char *path, const char *key, int32_t *shape_out, double *ms_out);
+
 /* ------------------------------------------------------------------ evaluation */
 /* Everything SimImplementation reads from simulator.ini beyond the heart itself
  * (SimSettings, SimSettings.h:77-357) plus the loaded targets (sim.cpp:999-1042). */
@@ -270,6 +295,15 @@ int ekg_server_set_free_bytes_provider(ekg_server *s, uint64_t (*fn)(void *ctx),
  * serialised, and device work of two calls must not overlap (they share the array). */
 int ekg_activation_noalloc(int32_t nz, int32_t ny, int32_t nx, const int32_t *d_layers, int32_t n_transfer,
                            const double *transfer, double *d_at, int32_t *rounds_out);
+
+/* Self-test of the kernels' bounded device waits, for failure-detection tests that must not hang
+ * or fault the GPU.  No counterpart in the reference (it has no device).  One block takes tensor
+ * memory, waits on an mbarrier that nothing arrives on for at most wait_limit polls (the
+ * contraction kernels' own wait helper, whose limit is 2^22 polls), records the timeout bit in the
+ * error word, releases the tensor memory and returns; the host reads the word.  Returns
+ * EKG_ERR_TIMEOUT when the wait ran out (the expected outcome), after which the device stays
+ * usable. */
+int ekg_selftest_bounded_wait(int32_t device, uint32_t wait_limit);
 
 /* ------------------------------------------------------------------ files */
 /* Build a heart and its eval config from a simulator.ini and the files it names, as the

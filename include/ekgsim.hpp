@@ -68,7 +68,11 @@ public:
         std::vector<double> g((size_t)n * genes_), c((size_t)n * criteria_);
         violations.resize(n);
         for (int32_t i = 0; i < n; ++i) {
-            if ((int32_t)solutions[i].size() != genes_) throw std::runtime_error("Solution does not contain enough values");
+            // the reference's messages for too few and for a wrong number of genes (sim.cpp:458-459, :835-841)
+            if ((int32_t)solutions[i].size() < genes_) throw std::runtime_error("Solution does not contain enough values");
+            if ((int32_t)solutions[i].size() != genes_)
+                throw std::runtime_error("chromosome size does not agree with the combination of the number of free "
+                                         "Wohlfart parameters and the selected interpolation procedure");
             std::copy(solutions[i].begin(), solutions[i].end(), g.begin() + (size_t)i * genes_);
         }
         check(ekg_eval_batch(h_, n, g.data(), genes_, c.data(), violations.data(), nullptr));
@@ -80,7 +84,8 @@ public:
     // outputs must stay allocated until waitBatch returns
     int64_t submitBatch(const std::vector<double> &genes_flat, int32_t n, double *criteria, double *violations,
                         double *ecg = nullptr) const {
-        if ((int64_t)genes_flat.size() != (int64_t)n * genes_) throw std::runtime_error("Solution does not contain enough values");
+        if ((int64_t)genes_flat.size() != (int64_t)n * genes_)
+            throw std::runtime_error("genes_flat must hold n chromosomes of the heart's gene count");
         int64_t t = 0;
         check(ekg_eval_batch_submit(h_, n, genes_flat.data(), genes_, criteria, violations, ecg, &t));
         return t;

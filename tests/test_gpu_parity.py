@@ -641,3 +641,96 @@ def test_c3_batched_full_size(engine):
     assert np.array_equal(viol_b, viol_p)
     h2.close()
     e2.close()
+
+
+def test_bounded_wait_runs_out_and_device_stays_usable(engine):
+    """Failure detection without a GPU fault: a kernel waits on an mbarrier that nothing arrives on,
+    with the contraction kernels' bounded wait and a short poll limit; it records the timeout in
+    the error word, releases its tensor memory and returns, the call reports EKG_ERR_TIMEOUT, and
+    the device keeps working (a heart is created and simulated afterwards)."""
+    from ekgsim_gb300 import _lib as L
+    from ekgsim_gb300.engine import Heart
+    lib = L.load()
+    assert lib.ekg_selftest_bounded_wait(0, 1 << 12) == -5
+    assert "bounded device wait ran out" in lib.ekg_last_error().decode()
+    assert lib.ekg_selftest_bounded_wait(0, 0) == -1
+    spec = synth.small_spec(16)
+    h, grid, tm, leads = make_heart(engine, spec, steps=50)
+    at, layer = O.activation(grid, tm)
+    assert np.array_equal(h.activation().view(np.int64), at.view(np.int64))
+    lk = layer_k_for(spec)
+    assert rel_l2(h.simulate(lk), O.run(layer, at, lk, leads, "3D4", 0.0, 50.0, 1.0)) <= ECG_TOL
+
+
+def test_activation_round_cap_reports_not_converged():
+    """The activation-time relaxation gives up after its round cap with EKG_ERR_CA_NOT_CONVERGED
+    (the cap set low through EKG_CA_ROUND_CAP); an engine with the default cap converges on the same
+    heart, bit-exact against the oracle."""
+    from ekgsim_gb300.engine import EkgError, Engine, Heart
+    spec = synth.small_spec(40)
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(3, spec.delays)
+    os.environ["EKG_CA_ROUND_CAP"] = "2"
+    try:
+        e = Engine(0)
+    finally:
+        os.environ.pop("EKG_CA_ROUND_CAP", None)
+    with pytest.raises(EkgError) as err:
+        Heart.create(e, grid, tm, np.array([[60.0, 60.0, 60.0]]), "3D4", 0.0, 10.0, 1.0)
+    assert err.value.code == -3
+    e.close()
+    e2 = Engine(0)
+    h = Heart.create(e2, grid, tm, np.array([[60.0, 60.0, 60.0]]), "3D4", 0.0, 10.0, 1.0)
+    assert h.info.ca_rounds > 2
+    at, _ = O.activation(grid, tm)
+    assert np.array_equal(h.activation().view(np.int64), at.view(np.int64))
+    h.close()
+    e2.close()
+
+
+def test_autotuned_shape_keeps_parity(tmp_path):
+    """The autotuner times every candidate launch shape on the real heart and keeps the fastest;
+    batched results with the tuned shape match the FP64 oracle and the built-in shape's results
+    within the tolerance, the choice is written to the cache file, and a new engine reads it back
+    for the same pass shape (its results equal the tuned engine's bit for bit)."""
+    from ekgsim_gb300.engine import Engine, Heart
+    spec = synth.small_spec(48, n_leads=6, seed=23)
+    steps = 300
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(3, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    target = [t for t in synth.analytic_target(spec.n_leads, steps, 4)]
+    genes = np.stack([synth.genes_for(spec, 70 + r, 0) for r in range(96)])
+    cache = str(tmp_path / "tune.txt")
+    out = {}
+    for tag in ("builtin", "tuned", "cached"):
+        if tag != "builtin":
+            os.environ["EKG_TUNE_CACHE"] = cache
+        try:
+            e = Engine(0)
+        finally:
+            os.environ.pop("EKG_TUNE_CACHE", None)
+        h = Heart.create(e, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+        h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], target, mid_position=0.6)
+        if tag == "tuned":
+            lk = np.stack([O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8],
+                                       "endo-mid-epi", 0.6, g[:12])[0] for g in genes])
+            moved = np.stack([O.move_leads(leads, g[12:].reshape(-1, 2)) for g in genes])
+            t = h.tune(lk, moved, reps=2)
+            assert t["candidates"] >= 3 and t["tile_rows"] in (32, 128, 256) and t["ms"] > 0
+            assert t["ms"] <= t["builtin_ms"] * 1.0001
+            assert os.path.exists(cache)
+        out[tag] = h.eval_batch(genes, want_ecg=True)
+        h.close()
+        e.close()
+    at, layer = O.activation(grid, tm)
+    for i in (0, 50, 95):
+        g = genes[i]
+        lk = O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], "endo-mid-epi",
+                         0.6, g[:12])[0]
+        ref = O.run(layer, at, lk, O.move_leads(leads, g[12:].reshape(-1, 2)), "3D4", 0.0, float(steps), 1.0)
+        assert rel_l2(out["tuned"][2][i], ref) <= ECG_TOL
+        assert rel_l2(out["tuned"][2][i], out["builtin"][2][i]) <= ECG_TOL
+    assert np.allclose(out["tuned"][0], out["builtin"][0], rtol=0, atol=1e-4)
+    for a, b in zip(out["tuned"], out["cached"]):
+        assert np.array_equal(a, b)
