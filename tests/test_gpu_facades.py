@@ -108,4 +108,4 @@ def test_python_facades_match_reference(tmp_path):
     sim.run()
     ecg = np.stack([sim.getMeasurement(i) for i in range(sim.numMeasurements())])
     assert float(np.linalg.norm(ecg - ecg_ref) / np.linalg.norm(ecg_ref)) <= TOL
-    assert np.array_equal(sim.activationTimes().view(np.int64), s.at.view(np.int64))
+    assert np.array_equal(sim.activationTimes().ravel().view(np.int64), s.at.ravel().view(np.int64))
