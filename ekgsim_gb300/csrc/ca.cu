@@ -249,7 +249,202 @@ __global__ void k_ca_finish(size_t n, double *__restrict__ at) {
         if (isinf(at[i])) at[i] = 0.0;  // unreachable voxels keep excitationDelay 0
 }
 
+// ------------------------------------------------------------------ bucketed relaxation
+// Dijkstra by time buckets (delta-stepping with a bucket width just below the smallest lag): the
+// voxels whose time falls into bucket k = floor(t / delta) are final once every earlier bucket has
+// been relaxed, because each of their predecessors on a shortest path is at least one lag, so more
+// than delta, earlier.  Bucket k is one launch: a warp per queued voxel, one lane per neighbour,
+// offers fl(at(u) + lag) with a 64-bit atomicMin on the time bits; an improved neighbour is queued
+// in the bucket of its new time (a per-voxel mark drops repeats within one bucket; entries whose
+// voxel improved into an earlier bucket are skipped when their bucket comes).  Offers reach at
+// most ceil(max lag / delta) + 1 buckets ahead, so the lists form a ring of that many slots; the
+// slot of bucket k - 1 is emptied by bucket k's launch (nothing can still be queued there).
+struct BucketArgs {
+    int nz, ny, nx;
+    const uint8_t *layers;
+    const double *lag;  // [nl1][nl1][3]
+    int nl1;
+    unsigned long long *at;  // time bits per cell (non-negative doubles order like their bits)
+    int32_t *qmark;          // bucket a cell was last queued in
+    int32_t *lists;          // [ring][cap]
+    int32_t *counts;         // [ring]
+    int32_t *overflow;
+    int ring, cap;
+    double inv_delta;
+};
+
+__device__ __forceinline__ int bucket_of(double t, double inv_delta) {
+    return (int)floor(__dmul_rn(t, inv_delta));
+}
+
+__global__ void k_ca_bucket_init(size_t n, const uint8_t *__restrict__ layers, const uint8_t *__restrict__ start,
+                                 BucketArgs A) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        A.qmark[i] = -1;
+        double v = 0.0;
+        if (layers[i]) v = start[i] ? 1.0 : __longlong_as_double(0x7ff0000000000000LL);
+        A.at[i] = (unsigned long long)__double_as_longlong(v);
+        if (layers[i] && start[i]) {
+            const int b = bucket_of(1.0, A.inv_delta);
+            A.qmark[i] = b;
+            const int idx = atomicAdd(&A.counts[b % A.ring], 1);
+            if (idx < A.cap) A.lists[(size_t)(b % A.ring) * A.cap + idx] = (int32_t)i;
+            else atomicOr(A.overflow, 1);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_ca_bucket(int k, BucketArgs A) {
+    const int slot = k % A.ring;
+    if (blockIdx.x == 0 && threadIdx.x == 0) A.counts[(k + A.ring - 1) % A.ring] = 0;
+    const int n = min(A.counts[slot], A.cap);
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    // lane -> neighbour offset (26 of the 32 lanes)
+    int dz = 0, dy = 0, dx = 0, kind = 0;
+    const bool nb = lane < 26;
+    if (nb) {
+        const int c = lane < 13 ? lane : lane + 1;  // skip the centre of the 3x3x3 cube
+        dz = c / 9 - 1;
+        dy = (c / 3) % 3 - 1;
+        dx = c % 3 - 1;
+        kind = (dz != 0) + (dy != 0) + (dx != 0);
+    }
+    for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
+        const int u = A.lists[(size_t)slot * A.cap + e];
+        const unsigned long long bu = A.at[u];
+        const double au = __longlong_as_double((long long)bu);
+        if (bucket_of(au, A.inv_delta) != k) continue;  // improved into an earlier bucket since queued
+        if (!nb) continue;
+        const int x = u % A.nx, y = (u / A.nx) % A.ny, z = u / (A.nx * A.ny);
+        const int vz = z + dz, vy = y + dy, vx = x + dx;
+        if (vz < 0 || vz >= A.nz || vy < 0 || vy >= A.ny || vx < 0 || vx >= A.nx) continue;
+        const int v = (vz * A.ny + vy) * A.nx + vx;
+        const uint8_t lv = A.layers[v];
+        if (lv == 0) continue;
+        const unsigned long long bv = A.at[v];
+        if (bu >= bv) continue;  // lags are positive: an earlier voxel cannot improve
+        const uint8_t lu = A.layers[u];
+        const double c = __dadd_rn(au, A.lag[((size_t)lu * A.nl1 + lv) * 3 + (kind - 1)]);
+        const unsigned long long cb = (unsigned long long)__double_as_longlong(c);
+        if (cb >= bv) continue;
+        if (cb < atomicMin(&A.at[v], cb)) {
+            const int b = bucket_of(c, A.inv_delta);
+            if (atomicExch(&A.qmark[v], b) != b) {
+                const int idx = atomicAdd(&A.counts[b % A.ring], 1);
+                if (idx < A.cap) A.lists[(size_t)(b % A.ring) * A.cap + idx] = v;
+                else atomicOr(A.overflow, 1);
+            }
+        }
+    }
+}
+
+__global__ void k_ca_bucket_finish(size_t n, const unsigned long long *__restrict__ bits, double *__restrict__ at) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double v = __longlong_as_double((long long)bits[i]);
+        at[i] = isinf(v) ? 0.0 : v;  // unreachable voxels keep excitationDelay 0
+    }
+}
+
 }  // namespace
+
+// Bucketed relaxation when the smallest lag allows it (returns false to fall back to the tile
+// rounds: a zero lag, a time span of too many buckets, or a full bucket list).
+bool ca_run_buckets(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_layers, const uint8_t *d_start,
+                    const std::vector<double> &lag_h, int nl1, const double *d_lag, double *d_at, int64_t nvox,
+                    int round_cap, int sm_count, CaResult &res) {
+    double min_lag = INFINITY, max_lag = 0;
+    for (int a = 1; a < nl1; ++a)
+        for (int b = 1; b < nl1; ++b)
+            for (int k = 0; k < 3; ++k) {
+                const double l = lag_h[((size_t)a * nl1 + b) * 3 + k];
+                min_lag = std::min(min_lag, l);
+                max_lag = std::max(max_lag, l);
+            }
+    if (!(min_lag >= 0.05) || !std::isfinite(max_lag)) return false;
+    // a bucket width just below the smallest lag keeps a margin far above FP64 rounding
+    const double delta = min_lag * (1.0 - 1e-6);
+    const int ring = (int)std::ceil(max_lag / delta) + 3;
+    if (ring > 256) return false;
+    const size_t n = (size_t)nz * ny * nx;
+    // bucket indices stay far inside int: the latest time is below 1 + n * max_lag
+    if ((1.0 + (double)n * max_lag) / delta > 1e9) return false;
+    const int cap = (int)std::min<int64_t>(std::max<int64_t>(1024, nvox + 1024), INT32_MAX / 2);
+    DBuf<unsigned long long> bits;
+    DBuf<int32_t> qmark, lists, counts;
+    bits.alloc(n);
+    qmark.alloc(n);
+    lists.alloc((size_t)ring * cap);
+    counts.alloc(ring + 1);  // + the overflow flag
+    BucketArgs A;
+    A.nz = nz;
+    A.ny = ny;
+    A.nx = nx;
+    A.layers = d_layers;
+    A.lag = d_lag;
+    A.nl1 = nl1;
+    A.at = bits.p;
+    A.qmark = qmark.p;
+    A.lists = lists.p;
+    A.counts = counts.p;
+    A.overflow = counts.p + ring;
+    A.ring = ring;
+    A.cap = cap;
+    A.inv_delta = 1.0 / delta;
+    EKG_CUDA(cudaMemsetAsync(counts.p, 0, (ring + 1) * sizeof(int32_t), s));
+    cudaEvent_t e0, e1;
+    EKG_CUDA(cudaEventCreate(&e0));
+    EKG_CUDA(cudaEventCreate(&e1));
+    struct Events {
+        cudaEvent_t a, b;
+        ~Events() {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+    } ev{e0, e1};
+    EKG_CUDA(cudaEventRecord(e0, s));
+    k_ca_bucket_init<<<1024, 256, 0, s>>>(n, d_layers, d_start, A);
+    EKG_CUDA(cudaGetLastError());
+    // buckets before the first start time are empty
+    int k = (int)std::floor(1.0 * A.inv_delta);
+    const int grid = std::max(1, sm_count) * 8;
+    std::vector<int32_t> h(ring + 1);
+    int32_t *hc = nullptr;
+    EKG_CUDA(cudaMallocHost(&hc, (ring + 1) * sizeof(int32_t)));
+    struct Pinned {
+        int32_t *p;
+        ~Pinned() { cudaFreeHost(p); }
+    } pin{hc};
+    // every cell settles at most once per bucket it is queued in; more buckets than cells plus the
+    // ring means the queues never drain
+    const int64_t kmax = round_cap > 0 ? (int64_t)round_cap : (int64_t)n + 4LL * ring + 1024;
+    constexpr int CHUNK = 16;
+    int steps = 0;
+    for (;;) {
+        for (int i = 0; i < CHUNK; ++i, ++k, ++steps) {
+            if (steps >= kmax) throw Error{EKG_ERR_CA_NOT_CONVERGED, "activation-time relaxation did not converge"};
+            k_ca_bucket<<<grid, 256, 0, s>>>(k, A);
+            EKG_CUDA(cudaGetLastError());
+        }
+        EKG_CUDA(cudaMemcpyAsync(hc, counts.p, (ring + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        EKG_CUDA(cudaStreamSynchronize(s));
+        if (hc[ring]) return false;  // a bucket list overflowed: the tile rounds redo it
+        // the slot of the last bucket launched holds processed entries; any other non-empty slot
+        // is a bucket still to come
+        bool pending = false;
+        for (int r = 0; r < ring; ++r)
+            if (r != (k - 1) % ring && hc[r] > 0) pending = true;
+        if (!pending) break;
+    }
+    k_ca_bucket_finish<<<1024, 256, 0, s>>>(n, bits.p, d_at);
+    EKG_CUDA(cudaGetLastError());
+    EKG_CUDA(cudaEventRecord(e1, s));
+    EKG_CUDA(cudaEventSynchronize(e1));
+    EKG_CUDA(cudaEventElapsedTime(&res.ms, e0, e1));
+    res.rounds = steps;
+    res.buckets = true;
+    return true;
+}
 
 CaResult ca_run(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_layers, const uint8_t *d_start,
                 const std::vector<int32_t> &start_tiles, int nl1, const double *d_lag, double *d_at, int round_cap,

@@ -21,6 +21,9 @@ struct ekg_engine {
     // rounds after which the activation-time relaxation gives up with EKG_ERR_CA_NOT_CONVERGED
     // (0 = the default bound from the grid size; EKG_CA_ROUND_CAP sets it, e.g. to test that error)
     int ca_round_cap = 0;
+    // activation-time relaxation: 0 = by time buckets where the lags allow it (else tile rounds),
+    // 1 = tile rounds always (EKG_CA=tiles)
+    int ca_mode = 0;
     // autotuning of the batched form's launch shapes: EKG_TUNE=1 tunes every new pass shape on its
     // first pass (ekg_heart_tune does it on request); EKG_TUNE_CACHE names a file that keeps the
     // choices across processes

@@ -123,9 +123,14 @@ struct DBuf {
 
 // ------------------------------------------------------------------ CA (ca.cu)
 struct CaResult {
-    int rounds = 0;
+    int rounds = 0;        // tile rounds, or bucket launches of the bucketed relaxation
     float ms = 0.f;
+    bool buckets = false;  // the bucketed relaxation ran
 };
+// Bucketed relaxation (Dijkstra by time buckets); false when it does not apply and ca_run must run.
+bool ca_run_buckets(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_layers, const uint8_t *d_start,
+                    const std::vector<double> &lag_h, int nl1, const double *d_lag, double *d_at, int64_t nvox,
+                    int round_cap, int sm_count, CaResult &res);
 // layers_u8: stripped layer per cell; start flags in `is_start`; lag: [nl1][nl1][3] FP64 with
 // lag[s][d][k-1] = T[s][d] * sqrt(k).  at_out: FP64 per cell (0 for empty / unreachable).
 CaResult ca_run(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_layers, const uint8_t *d_start,

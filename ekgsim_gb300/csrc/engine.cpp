@@ -361,8 +361,14 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
         h->at_cells.alloc(n);
         EKG_CUDA(cudaMemcpyAsync(ds.p, st.data(), n, cudaMemcpyHostToDevice, s));
         EKG_CUDA(cudaMemcpyAsync(dlag.p, lag.data(), lag.size() * 8, cudaMemcpyHostToDevice, s));
-        CaResult r = ca_run(s, d->nz, d->ny, d->nx, dl.p, ds.p, start_tiles, nl1, dlag.p, h->at_cells.p,
-                            h->eng->ca_round_cap, h->sm_count);
+        int64_t nvox_h = 0;
+        for (int64_t i = 0; i < n; ++i) nvox_h += lay[i] != 0;
+        CaResult r;
+        if (h->eng->ca_mode == 1 ||
+            !ca_run_buckets(s, d->nz, d->ny, d->nx, dl.p, ds.p, lag, nl1, dlag.p, h->at_cells.p, nvox_h,
+                            h->eng->ca_round_cap, h->sm_count, r))
+            r = ca_run(s, d->nz, d->ny, d->nx, dl.p, ds.p, start_tiles, nl1, dlag.p, h->at_cells.p,
+                       h->eng->ca_round_cap, h->sm_count);
         h->ca_rounds = r.rounds;
         h->ca_ms = r.ms;
         EKG_CUDA(cudaStreamSynchronize(s));
@@ -1790,6 +1796,7 @@ int ekg_engine_create(int device, ekg_engine **out) {
         if (const char *v = std::getenv("EKG_BATCH_CTAS")) e->batch_ctas = std::atoi(v);
         if (const char *v = std::getenv("EKG_GRAPHS")) e->graphs = std::string(v) != "0";
         if (const char *v = std::getenv("EKG_CA_ROUND_CAP")) e->ca_round_cap = std::max(0, std::atoi(v));
+        if (const char *v = std::getenv("EKG_CA")) e->ca_mode = std::string(v) == "tiles" ? 1 : 0;
         if (const char *v = std::getenv("EKG_TUNE")) e->tune = std::string(v) == "1";
         if (const char *v = std::getenv("EKG_TUNE_CACHE")) e->tune_cache = v;
         EKG_CUDA(cudaSetDevice(device));

@@ -86,7 +86,8 @@ typedef struct {
     int32_t n_layers;          /* highest layer id */
     int32_t n_leads;
     int32_t steps;             /* ceil(length / dt) */
-    int32_t ca_rounds;         /* tile rounds the activation relaxation took */
+    int32_t ca_rounds;         /* steps of the activation relaxation: time buckets, or tile rounds
+                                * where the lags do not allow buckets (a zero lag) */
     int64_t device_bytes;      /* device memory held by this heart */
     double ca_ms;              /* device time of the activation relaxation */
     double setup_ms;           /* host wall time of ekg_heart_create */

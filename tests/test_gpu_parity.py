@@ -734,3 +734,25 @@ def test_autotuned_shape_keeps_parity(tmp_path):
     assert np.allclose(out["tuned"][0], out["builtin"][0], rtol=0, atol=1e-4)
     for a, b in zip(out["tuned"], out["cached"]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("n", [16, 40, 128])
+def test_activation_tile_rounds_and_buckets_agree(n):
+    """The two relaxations -- time buckets (default where the lags allow) and tile rounds
+    (EKG_CA=tiles, and the fallback) -- give the oracle's activation times bit for bit."""
+    from ekgsim_gb300.engine import Engine, Heart
+    spec = synth.small_spec(n) if n < 128 else synth.config(1)["spec"]
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(spec.n_layers, spec.delays)
+    at_ref, _ = O.activation(grid, tm)
+    for mode in ("tiles", "buckets"):
+        if mode == "tiles":
+            os.environ["EKG_CA"] = "tiles"
+        try:
+            e = Engine(0)
+        finally:
+            os.environ.pop("EKG_CA", None)
+        h = Heart.create(e, grid, tm, np.array([[n * 2.0, n * 2.0, n * 2.0]]), "3D4", 0.0, 10.0, 1.0)
+        assert np.array_equal(h.activation().view(np.int64), at_ref.view(np.int64)), mode
+        h.close()
+        e.close()
