@@ -253,20 +253,25 @@ __global__ void k_ca_finish(size_t n, double *__restrict__ at) {
 // Dijkstra by time buckets (delta-stepping with a bucket width just below the smallest lag): the
 // voxels whose time falls into bucket k = floor(t / delta) are final once every earlier bucket has
 // been relaxed, because each of their predecessors on a shortest path is at least one lag, so more
-// than delta, earlier.  Bucket k is one launch: a warp per queued voxel, one lane per neighbour,
-// offers fl(at(u) + lag) with a 64-bit atomicMin on the time bits; an improved neighbour is queued
-// in the bucket of its new time (a per-voxel mark drops repeats within one bucket; entries whose
-// voxel improved into an earlier bucket are skipped when their bucket comes).  Offers reach at
-// most ceil(max lag / delta) + 1 buckets ahead, so the lists form a ring of that many slots; the
-// slot of bucket k - 1 is emptied by bucket k's launch (nothing can still be queued there).
+// than delta, earlier.  Bucket k is one launch: a warp per queued entry (cell, layer, time), one
+// lane per neighbour, offers fl(at(u) + lag) with a 64-bit atomicMin on the time bits; an improved
+// neighbour is queued in the bucket of its new time with its new time (warp-aggregated appends per
+// bucket).  A cell can be queued more than once: an entry whose cell has improved since offers a
+// later time than the one already offered from the cell's better entry, which was relaxed in an
+// earlier bucket or in this one, so it changes nothing.  Offers reach at most
+// ceil(max lag / delta) + 1 buckets ahead, so the lists form a ring of that many slots; the slot
+// of bucket k - 1 is emptied by bucket k's launch (nothing can still be queued there).
+struct QEntry {
+    int32_t cell, layer;
+    unsigned long long bits;
+};
 struct BucketArgs {
     int nz, ny, nx;
     const uint8_t *layers;
     const double *lag;  // [nl1][nl1][3]
     int nl1;
     unsigned long long *at;  // time bits per cell (non-negative doubles order like their bits)
-    int32_t *qmark;          // bucket a cell was last queued in
-    int32_t *lists;          // [ring][cap]
+    QEntry *lists;           // [ring][cap]
     int32_t *counts;         // [ring]
     int32_t *overflow;
     int ring, cap;
@@ -280,15 +285,14 @@ __device__ __forceinline__ int bucket_of(double t, double inv_delta) {
 __global__ void k_ca_bucket_init(size_t n, const uint8_t *__restrict__ layers, const uint8_t *__restrict__ start,
                                  BucketArgs A) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        A.qmark[i] = -1;
         double v = 0.0;
         if (layers[i]) v = start[i] ? 1.0 : __longlong_as_double(0x7ff0000000000000LL);
-        A.at[i] = (unsigned long long)__double_as_longlong(v);
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+        A.at[i] = bits;
         if (layers[i] && start[i]) {
             const int b = bucket_of(1.0, A.inv_delta);
-            A.qmark[i] = b;
             const int idx = atomicAdd(&A.counts[b % A.ring], 1);
-            if (idx < A.cap) A.lists[(size_t)(b % A.ring) * A.cap + idx] = (int32_t)i;
+            if (idx < A.cap) A.lists[(size_t)(b % A.ring) * A.cap + idx] = QEntry{(int32_t)i, (int32_t)layers[i], bits};
             else atomicOr(A.overflow, 1);
         }
     }
@@ -301,7 +305,7 @@ __global__ void __launch_bounds__(256) k_ca_bucket(int k, BucketArgs A) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     // lane -> neighbour offset (26 of the 32 lanes)
-    int dz = 0, dy = 0, dx = 0, kind = 0;
+    int dz = 0, dy = 0, dx = 0, kind = 1;
     const bool nb = lane < 26;
     if (nb) {
         const int c = lane < 13 ? lane : lane + 1;  // skip the centre of the 3x3x3 cube
@@ -310,31 +314,38 @@ __global__ void __launch_bounds__(256) k_ca_bucket(int k, BucketArgs A) {
         dx = c % 3 - 1;
         kind = (dz != 0) + (dy != 0) + (dx != 0);
     }
+    // the loop bound is uniform over the warp, so every lane reaches the warp votes below
     for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
-        const int u = A.lists[(size_t)slot * A.cap + e];
-        const unsigned long long bu = A.at[u];
-        const double au = __longlong_as_double((long long)bu);
-        if (bucket_of(au, A.inv_delta) != k) continue;  // improved into an earlier bucket since queued
-        if (!nb) continue;
+        const QEntry q = A.lists[(size_t)slot * A.cap + e];
+        const int u = q.cell;
         const int x = u % A.nx, y = (u / A.nx) % A.ny, z = u / (A.nx * A.ny);
         const int vz = z + dz, vy = y + dy, vx = x + dx;
-        if (vz < 0 || vz >= A.nz || vy < 0 || vy >= A.ny || vx < 0 || vx >= A.nx) continue;
-        const int v = (vz * A.ny + vy) * A.nx + vx;
-        const uint8_t lv = A.layers[v];
-        if (lv == 0) continue;
-        const unsigned long long bv = A.at[v];
-        if (bu >= bv) continue;  // lags are positive: an earlier voxel cannot improve
-        const uint8_t lu = A.layers[u];
-        const double c = __dadd_rn(au, A.lag[((size_t)lu * A.nl1 + lv) * 3 + (kind - 1)]);
-        const unsigned long long cb = (unsigned long long)__double_as_longlong(c);
-        if (cb >= bv) continue;
-        if (cb < atomicMin(&A.at[v], cb)) {
-            const int b = bucket_of(c, A.inv_delta);
-            if (atomicExch(&A.qmark[v], b) != b) {
-                const int idx = atomicAdd(&A.counts[b % A.ring], 1);
-                if (idx < A.cap) A.lists[(size_t)(b % A.ring) * A.cap + idx] = v;
-                else atomicOr(A.overflow, 1);
-            }
+        const bool inside = nb && vz >= 0 && vz < A.nz && vy >= 0 && vy < A.ny && vx >= 0 && vx < A.nx;
+        const int v = inside ? (vz * A.ny + vy) * A.nx + vx : u;
+        const uint8_t lv = inside ? A.layers[v] : 0;
+        const unsigned long long bv = inside ? A.at[v] : 0ull;
+        bool improved = false;
+        double c = 0.0;
+        if (lv != 0 && q.bits < bv) {
+            c = __dadd_rn(__longlong_as_double((long long)q.bits),
+                          __ldg(A.lag + ((size_t)q.layer * A.nl1 + lv) * 3 + (kind - 1)));
+            const unsigned long long cb = (unsigned long long)__double_as_longlong(c);
+            improved = cb < bv && cb < atomicMin(&A.at[v], cb);
+        }
+        // queue the improved neighbours: one atomic per bucket and warp
+        const int b = improved ? bucket_of(c, A.inv_delta) : -1;
+        const unsigned same = __match_any_sync(0xffffffffu, b);
+        if (improved) {
+            const int leader = __ffs(same) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(&A.counts[b % A.ring], __popc(same));
+            base = __shfl_sync(same, base, leader);
+            const int idx = base + __popc(same & ((1u << lane) - 1u));
+            if (idx < A.cap)
+                A.lists[(size_t)(b % A.ring) * A.cap + idx] =
+                    QEntry{v, (int32_t)lv, (unsigned long long)__double_as_longlong(c)};
+            else
+                atomicOr(A.overflow, 1);
         }
     }
 }
@@ -369,11 +380,12 @@ bool ca_run_buckets(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_lay
     const size_t n = (size_t)nz * ny * nx;
     // bucket indices stay far inside int: the latest time is below 1 + n * max_lag
     if ((1.0 + (double)n * max_lag) / delta > 1e9) return false;
-    const int cap = (int)std::min<int64_t>(std::max<int64_t>(1024, nvox + 1024), INT32_MAX / 2);
+    // per bucket slot; a cell can be queued more than once, a full slot falls back to the tile rounds
+    const int cap = (int)std::min<int64_t>(std::max<int64_t>(65536, nvox / 2), INT32_MAX / 32);
     DBuf<unsigned long long> bits;
-    DBuf<int32_t> qmark, lists, counts;
+    DBuf<QEntry> lists;
+    DBuf<int32_t> counts;
     bits.alloc(n);
-    qmark.alloc(n);
     lists.alloc((size_t)ring * cap);
     counts.alloc(ring + 1);  // + the overflow flag
     BucketArgs A;
@@ -384,7 +396,6 @@ bool ca_run_buckets(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_lay
     A.lag = d_lag;
     A.nl1 = nl1;
     A.at = bits.p;
-    A.qmark = qmark.p;
     A.lists = lists.p;
     A.counts = counts.p;
     A.overflow = counts.p + ring;
