@@ -41,7 +41,7 @@ class HeartDesc(ctypes.Structure):
 class HeartInfo(ctypes.Structure):
     _fields_ = [("n_cells", c_int64), ("n_voxels", c_int64), ("n_aps", c_int64), ("n_layers", c_int32),
                 ("n_leads", c_int32), ("steps", c_int32), ("ca_rounds", c_int32), ("device_bytes", c_int64),
-                ("ca_ms", c_double), ("setup_ms", c_double)]
+                ("ca_ms", c_double), ("setup_ms", c_double), ("ca_buckets", c_int32)]
 
 
 class EvalConfig(ctypes.Structure):

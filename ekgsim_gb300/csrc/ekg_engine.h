@@ -188,6 +188,7 @@ struct ekg_heart {
     int64_t ncell = 0, nvox = 0, naps = 0;
     double start = 0, length = 0, dt = 1;
     int ca_rounds = 0;
+    bool ca_buckets = false;  // the relaxation ran by time buckets (else tile rounds)
     double ca_ms = 0, setup_ms = 0;
     std::vector<double> t;            // time axis
     std::vector<double> leads0;       // loaded lead positions (z,y,x)

@@ -371,6 +371,7 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
                        h->eng->ca_round_cap, h->sm_count);
         h->ca_rounds = r.rounds;
         h->ca_ms = r.ms;
+        h->ca_buckets = r.buckets;
         EKG_CUDA(cudaStreamSynchronize(s));
     }
     h->at_host.clear();  // copied to the host on first use (ensure_at_host)
@@ -1855,6 +1856,7 @@ int ekg_heart_get_info(ekg_heart *h, ekg_heart_info *info) {
         info->device_bytes = heart_device_bytes(h);
         info->ca_ms = h->ca_ms;
         info->setup_ms = h->setup_ms;
+        info->ca_buckets = h->ca_buckets ? 1 : 0;
     });
 }
 

@@ -91,6 +91,7 @@ typedef struct {
     int64_t device_bytes;      /* device memory held by this heart */
     double ca_ms;              /* device time of the activation relaxation */
     double setup_ms;           /* host wall time of ekg_heart_create */
+    int32_t ca_buckets;        /* 1: the relaxation ran by time buckets, 0: by tile rounds (or loaded) */
 } ekg_heart_info;
 
 /* Upload a heart, compute its activation times on the device (bit-exact FP64 equivalent of
@@ -253,7 +254,8 @@ typedef struct {
  * simulation fits). */
 int ekg_server_create(ekg_engine *e, const ekg_server_opts *opts, ekg_server **out);
 int ekg_server_destroy(ekg_server *s);
-/* Register a heart (with its eval config set); returns its id. */
+/* Register a heart (with its eval config set); returns its id.  The heart must outlive the server
+ * (destroy the server first), and its evaluation settings must not change while it is registered. */
 int ekg_server_add_heart(ekg_server *s, ekg_heart *h, int32_t *heart_id);
 int ekg_server_submit(ekg_server *s, int32_t heart_id, const double *genes, int32_t n_genes,
                       uint64_t *request_id);
