@@ -251,7 +251,7 @@ def served_stream(srv, ids, specs, rate: float, n: int, seed: int, n_crit: int):
             "mean_batch": float(np.mean(batch))}
 
 
-def served_run(rates=(500.0, 5e3, 5e4, 2e5, 1e6), seconds: float = 1.0, max_requests: int = 200_000,
+def served_run(rates=(500.0, 5e3, 5e4, 2e5, 4e5, 1e6), seconds: float = 1.0, max_requests: int = 200_000,
                seed: int = 3000, max_wait_us: int = 0):
     """Served configuration: Poisson streams of evaluation requests over four resident hearts,
     continuous batching in the engine's request loop (each heart's next pass is prepared and queued

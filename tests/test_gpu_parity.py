@@ -756,3 +756,49 @@ def test_activation_tile_rounds_and_buckets_agree(n):
         assert np.array_equal(h.activation().view(np.int64), at_ref.view(np.int64)), mode
         h.close()
         e.close()
+
+
+@pytest.mark.parametrize("case", ["single_voxel", "ragged", "plane", "zero_lag", "isolated_stimulus"])
+def test_activation_edge_shapes(case):
+    """Activation times bit-exact against the oracle on edge shapes, with both relaxations: a
+    one-voxel heart, extents that are not multiples of the 8-cell tiles, a one-cell-thick plane, a
+    conduction matrix with a zero delay (no time buckets: the tile rounds run), and a stimulus voxel
+    without non-empty neighbours next to an unreachable block; the ECG of the ragged heart too."""
+    from ekgsim_gb300.engine import Engine, Heart
+    rng = np.random.Generator(np.random.PCG64(41))
+    tm = synth.transfer_matrix(3, [1, 2, 2])
+    if case == "single_voxel":
+        grid = np.array([[[-1]]], dtype=np.int32)
+    elif case == "ragged":
+        grid = rng.integers(0, 4, size=(13, 17, 11)).astype(np.int32)
+        grid[6, 8, 5] = -2
+    elif case == "plane":
+        grid = rng.integers(1, 4, size=(1, 37, 29)).astype(np.int32)
+        grid[0, 3, 4] = -1
+    elif case == "zero_lag":
+        grid = rng.integers(1, 4, size=(12, 10, 14)).astype(np.int32)
+        grid[0, 0, 0] = -1
+        tm = tm.copy()
+        tm[2, 3] = 0.0
+    else:
+        grid = np.zeros((10, 10, 10), dtype=np.int32)
+        grid[1, 1, 1] = -1
+        grid[5:9, 5:9, 5:9] = 2
+    at_ref, layer = O.activation(grid, tm)
+    leads = np.array([[30.0, 25.0, 20.0], [-12.0, 4.0, 33.0]])
+    for mode in ("buckets", "tiles"):
+        if mode == "tiles":
+            os.environ["EKG_CA"] = "tiles"
+        try:
+            e = Engine(0)
+        finally:
+            os.environ.pop("EKG_CA", None)
+        h = Heart.create(e, grid, tm, leads, "3D4", 0.0, 60.0, 1.0)
+        assert np.array_equal(h.activation().view(np.int64), at_ref.view(np.int64)), mode
+        if case == "zero_lag":
+            assert h.info.ca_buckets == 0
+        if case == "ragged":
+            lk = layer_k_for(synth.small_spec(16), 3)
+            assert rel_l2(h.simulate(lk), O.run(layer, at_ref, lk, leads, "3D4", 0.0, 60.0, 1.0)) <= ECG_TOL
+        h.close()
+        e.close()
