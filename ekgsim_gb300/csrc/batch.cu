@@ -1168,7 +1168,8 @@ void launch_sim_lead_field(cudaStream_t s, const HeartDev &h, const double *d_le
     EKG_CUDA(cudaGetLastError());
 }
 
-void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, bool small, const float *k5l,
+void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, bool small, int blocks_per_sm,
+                             const float *k5l,
                              const float4 *hconst, const float4 *lrel, int nmove, int n_sims, const BandArgs &B,
                              uint8_t *Bt, int *work, int sm_count) {
     const int rows_used = n_sims * nmove;
@@ -1195,7 +1196,8 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, b
         if (!per_sm)                                                                                              \
             EKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_lead_field<NN, DG>,           \
                                                                    LF_THREADS, 0));                               \
-        const int grid = std::max(1, std::min(nst * ngr, std::max(1, per_sm) * sm_count));                       \
+        const int bps = blocks_per_sm > 0 ? std::min(blocks_per_sm, std::max(1, per_sm)) : std::max(1, per_sm);   \
+        const int grid = std::max(1, std::min(nst * ngr, bps * sm_count));                                       \
         k_batch_lead_field<NN, DG><<<grid, LF_THREADS, 0, s>>>(                                                   \
             nst, ngr, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p, \
             k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, B.stage_order, Bt, B.P1);      \

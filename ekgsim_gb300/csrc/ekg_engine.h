@@ -82,6 +82,7 @@ struct BatchState {
 // simulation); 0: the persistent kernel with four rows per thread).
 struct TuneChoice {
     int tile_rows = 0, cta_mult = 0, op_small = -1;
+    int op_bps = 0;       // persistent operand kernel: blocks per SM (0 = as many as fit)
     double ms = 0;        // device time of one pass with this shape (CUDA events)
     int candidates = 0;   // shapes timed when it was chosen
 };
@@ -90,7 +91,7 @@ struct PassPlan {
     bool batch = false;                    // separable batched form
     int n_sims = 0, nmove = 0, J = 0, two_bases = 0;
     int rows_used = 0, rows = 0, ntiles = 0, nitems = 0;
-    int tile_rows = 0, op_small = 0;       // launch shape (see TuneChoice)
+    int tile_rows = 0, op_small = 0, op_bps = 0;  // launch shape (see TuneChoice)
     std::vector<double> k3;                // [S][nl]
     std::vector<int4> items;               // band GEMM work items, grouped by tile
     std::vector<int32_t> ti0, ti1;         // [ntt][nl] item range of each (tile, layer)
@@ -213,4 +214,5 @@ struct ekg_heart {
     // autotuned launch shapes by pass shape (tune_key), and a shape forced while the tuner times it
     std::map<std::string, ekg::TuneChoice> tuned;
     const ekg::TuneChoice *tune_force = nullptr;
+    std::vector<ekg::TuneChoice> tune_last;  // every candidate of the last tuning, with its time
 };

@@ -289,7 +289,8 @@ void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int
 void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const float *F,
                            const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg,
                            float2 *ecg_ff);
-void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, bool small, const float *k5l,
+void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, bool small, int blocks_per_sm,
+                             const float *k5l,
                              const float4 *hconst, const float4 *lrel, int nmove, int n_sims, const BandArgs &B,
                              uint8_t *Bt, int *work, int sm_count);
 void launch_batch_gemm(cudaStream_t s, const BatchArgs &a);

@@ -765,8 +765,9 @@ std::string tune_key(const ekg_heart *h, int n_sims, int nmove, int two_bases) {
 }
 
 // Launch shapes worth timing: row tiles 32 / 128 / 256 (256 not with two bases; a tile at most
-// twice the rows used), GEMM work-item targets of 1, 2 and 4 CTAs per SM, and for passes of up to
-// 64 simulations both operand-kernel forms.
+// twice the rows used), GEMM work-item targets of 1, 2 and 4 CTAs per SM, for passes of up to 64
+// simulations both operand-kernel forms, and for the persistent operand kernel as many blocks per
+// SM as fit or 4 (a different balance of latency hiding and per-SM contention).
 std::vector<TuneChoice> tune_candidates(int two_bases, int rows_used, int n_sims) {
     std::vector<TuneChoice> c;
     for (int N : {32, 128, 256}) {
@@ -775,11 +776,15 @@ std::vector<TuneChoice> tune_candidates(int two_bases, int rows_used, int n_sims
         for (int mult : {1, 2, 4})
             for (int small : {1, 0}) {
                 if (small && n_sims > 64) continue;
-                TuneChoice t;
-                t.tile_rows = N;
-                t.cta_mult = mult;
-                t.op_small = small;
-                c.push_back(t);
+                for (int bps : {0, 4}) {
+                    if (small && bps) continue;
+                    TuneChoice t;
+                    t.tile_rows = N;
+                    t.cta_mult = mult;
+                    t.op_small = small;
+                    t.op_bps = bps;
+                    c.push_back(t);
+                }
             }
     }
     return c;
@@ -791,7 +796,7 @@ void tune_cache_write(const std::string &path, const std::string &key, const Tun
     std::ofstream f(path, std::ios::app);
     if (!f) throw Error{EKG_ERR_IO, "could not open autotuner cache " + path};
     f << key << " " << t.tile_rows << " " << t.cta_mult << " " << t.op_small << " " << t.ms << " " << t.candidates
-      << "\n";
+      << " " << t.op_bps << "\n";
 }
 bool tune_cache_read(const std::string &path, const std::string &key, TuneChoice &out) {
     std::ifstream f(path);
@@ -801,6 +806,8 @@ bool tune_cache_read(const std::string &path, const std::string &key, TuneChoice
         std::string k;
         TuneChoice t;
         if (!(ss >> k >> t.tile_rows >> t.cta_mult >> t.op_small >> t.ms >> t.candidates)) continue;
+        if (!(ss >> t.op_bps)) t.op_bps = 0;
+        if (t.op_bps < 0 || t.op_bps > 64) continue;
         if (k != key) continue;
         if (t.tile_rows != 32 && t.tile_rows != 128 && t.tile_rows != 256) continue;
         if (t.cta_mult < 1 || t.cta_mult > 64 || t.op_small < 0 || t.op_small > 1) continue;
@@ -878,6 +885,7 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
         const int N = tc && tc->tile_rows > 0 ? tc->tile_rows : batch_tile_rows(P.two_bases, P.rows_used);
         P.tile_rows = N;
         P.op_small = tc && tc->op_small >= 0 ? tc->op_small : (n_sims <= small_operand_sims() ? 1 : 0);
+        P.op_bps = tc ? tc->op_bps : 0;
         P.ntiles = (P.rows_used + N - 1) / N;
         P.rows = P.ntiles * N;
         // band work items: each (tile, layer) band cut into pieces of at most `per` stages, `per`
@@ -1093,8 +1101,8 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             U.ecg = E.ecg.p;
             U.ecg_ff = E.ecg_ff.p;
             if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[4], s));
-            launch_batch_lead_field(s, D, P.tile_rows, P.op_small != 0, in.k5l, in.hconst, in.lrel, nmove, n_sims, U,
-                                    B.Bt.p, B.work.p, h->sm_count);
+            launch_batch_lead_field(s, D, P.tile_rows, P.op_small != 0, P.op_bps, in.k5l, in.hconst, in.lrel, nmove,
+                                    n_sims, U, B.Bt.p, B.work.p, h->sm_count);
             if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[5], s));
             if (fork) {
                 EKG_CUDA(cudaEventRecord(h->ev_op, s));
@@ -1186,7 +1194,8 @@ std::vector<uint64_t> pass_signature(const ekg_heart *h, const PassPlan &P, int 
                                (uint64_t)P.two_bases, (uint64_t)P.rows, (uint64_t)P.rows_used, (uint64_t)P.ntiles,
                                (uint64_t)P.nitems, (uint64_t)ncl, (uint64_t)mode, (uint64_t)mark_static,
                                (uint64_t)h->cpre_on, (uint64_t)h->any_k0, (uint64_t)h->eng->contract, (uint64_t)B.J,
-                               (uint64_t)B.max_ent, (uint64_t)B.ntt, (uint64_t)P.tile_rows, (uint64_t)P.op_small};
+                               (uint64_t)B.max_ent, (uint64_t)B.ntt, (uint64_t)P.tile_rows, (uint64_t)P.op_small,
+                               (uint64_t)P.op_bps};
     const ekg_heart::PassInputs &in = h->in();
     for (const void *p : {(const void *)in.layer_k, (const void *)in.cpre, (const void *)in.leads, (const void *)in.k3,
                           (const void *)B.d_centre.p, (const void *)B.d_scale.p, (const void *)E.coef.p,
@@ -1489,7 +1498,7 @@ TuneChoice tune_pass(ekg_heart *h, int n_sims, const double *layer_k, const doub
         c.ms = ms / reps;
         const int bN = batch_tile_rows(P0.two_bases, P0.rows_used);
         const bool builtin = c.tile_rows == bN && c.op_small == (n_sims <= small_operand_sims() ? 1 : 0) &&
-                             c.cta_mult == (bN <= 32 ? 2 : 1);
+                             c.cta_mult == (bN <= 32 ? 2 : 1) && c.op_bps == 0;
         if (builtin && builtin_ms) *builtin_ms = c.ms;
         if (c.ms < best_ms) {
             best_ms = c.ms;
@@ -1497,6 +1506,7 @@ TuneChoice tune_pass(ekg_heart *h, int n_sims, const double *layer_k, const doub
         }
     }
     best.candidates = (int)cands.size();
+    h->tune_last = cands;
     h->tuned[key] = best;
     if (!h->eng->tune_cache.empty()) tune_cache_write(h->eng->tune_cache, key, best);
     return best;
@@ -2048,9 +2058,16 @@ int ekg_heart_tune(ekg_heart *h, int32_t n_sims, const double *layer_k, const do
         std::lock_guard<std::mutex> lk(h->mu);
         double builtin = 0;
         const TuneChoice t = tune_pass(h, n_sims, layer_k, leads, reps, &builtin);
-        const double v[6] = {(double)t.tile_rows, (double)t.cta_mult, (double)t.op_small, t.ms, builtin,
-                             (double)t.candidates};
-        for (int i = 0; i < n_out && i < 6; ++i) out[i] = v[i];
+        const double v[7] = {(double)t.tile_rows, (double)t.cta_mult, (double)t.op_small, t.ms, builtin,
+                             (double)t.candidates, (double)t.op_bps};
+        for (int i = 0; i < n_out && i < 7; ++i) out[i] = v[i];
+        // then every candidate: row tile, CTAs per SM, operand form, operand blocks per SM, ms
+        for (size_t c = 0; c < h->tune_last.size(); ++c) {
+            const TuneChoice &q = h->tune_last[c];
+            const double w[5] = {(double)q.tile_rows, (double)q.cta_mult, (double)q.op_small, (double)q.op_bps, q.ms};
+            for (int i = 0; i < 5; ++i)
+                if (7 + (int)c * 5 + i < n_out) out[7 + c * 5 + i] = w[i];
+        }
     });
 }
 
@@ -2062,9 +2079,10 @@ int ekg_tune_candidates(int32_t two_bases, int32_t rows_used, int32_t n_sims, in
         const std::vector<TuneChoice> c = tune_candidates(two_bases, rows_used, n_sims);
         *n_out = (int32_t)c.size();
         for (int i = 0; i < (int)c.size() && i < max_shapes; ++i) {
-            shapes_out[3 * i] = c[i].tile_rows;
-            shapes_out[3 * i + 1] = c[i].cta_mult;
-            shapes_out[3 * i + 2] = c[i].op_small;
+            shapes_out[4 * i] = c[i].tile_rows;
+            shapes_out[4 * i + 1] = c[i].cta_mult;
+            shapes_out[4 * i + 2] = c[i].op_small;
+            shapes_out[4 * i + 3] = c[i].op_bps;
         }
     });
 }
@@ -2076,6 +2094,7 @@ int ekg_tune_cache_put(const char *path, const char *key, const int32_t *shape, 
         t.tile_rows = shape[0];
         t.cta_mult = shape[1];
         t.op_small = shape[2];
+        t.op_bps = shape[3];
         t.ms = ms;
         tune_cache_write(path, key, t);
     });
@@ -2089,6 +2108,7 @@ int ekg_tune_cache_get(const char *path, const char *key, int32_t *shape_out, do
         shape_out[0] = t.tile_rows;
         shape_out[1] = t.cta_mult;
         shape_out[2] = t.op_small;
+        shape_out[3] = t.op_bps;
         if (ms_out) *ms_out = t.ms;
     });
 }

@@ -145,11 +145,16 @@ class Heart:
         lk = np.ascontiguousarray(layer_k, dtype=np.float64)
         n = lk.shape[0]
         ld = None if leads_zyx is None else np.ascontiguousarray(leads_zyx, dtype=np.float64)
-        out = np.zeros(6)
-        check(self._lib.ekg_heart_tune(self._h, n, dptr(lk), dptr(ld), reps, dptr(out), 6))
+        out = np.zeros(7 + 5 * 64)
+        check(self._lib.ekg_heart_tune(self._h, n, dptr(lk), dptr(ld), reps, dptr(out), out.size))
+        nc = int(out[5])
+        table = [{"tile_rows": int(out[7 + 5 * i]), "ctas_per_sm": int(out[8 + 5 * i]),
+                  "operand_form": "per-(AP, simulation)" if out[9 + 5 * i] == 1 else "persistent",
+                  "operand_blocks_per_sm": int(out[10 + 5 * i]), "ms": float(out[11 + 5 * i])}
+                 for i in range(min(nc, 64))]
         return {"tile_rows": int(out[0]), "ctas_per_sm": int(out[1]), "operand_form":
-                "per-(AP, simulation)" if out[2] == 1 else "persistent", "ms": float(out[3]),
-                "builtin_ms": float(out[4]), "candidates": int(out[5])}
+                "per-(AP, simulation)" if out[2] == 1 else "persistent", "operand_blocks_per_sm": int(out[6]),
+                "ms": float(out[3]), "builtin_ms": float(out[4]), "candidates": nc, "timings": table}
 
     def set_eval(self, base_aps, k_min, k_max, free_k, targets, target_offsets=None, **kw):
         """Evaluation settings (ekg_heart_set_eval); keyword arguments as ``eval_config``."""

@@ -138,25 +138,29 @@ int ekg_heart_benchmark(ekg_heart *h, int32_t n_sims, const double *layer_k, con
 /* Autotuner of the batched form's launch shapes (no counterpart in the reference, which has no
  * device).  For a pass of n_sims simulations with these inputs (as ekg_heart_benchmark takes them)
  * it times every candidate shape of the moved-lead kernels -- band GEMM row tile 32 / 128 / 256,
- * GEMM work-item target of 1 / 2 / 4 CTAs per SM, and for up to 64 simulations the operand
- * kernel's per-(AP, simulation) or persistent form -- with CUDA events on the heart's stream
+ * GEMM work-item target of 1 / 2 / 4 CTAs per SM, for up to 64 simulations the operand kernel's
+ * per-(AP, simulation) or persistent form, and the persistent form's blocks per SM (as many as fit,
+ * or 4) -- with CUDA events on the heart's stream
  * (`reps` passes each after one untimed pass), keeps the fastest for every later pass of this
  * shape on this heart, and appends it to the file named by the EKG_TUNE_CACHE environment variable
  * (read at engine creation; engines read it back for the same pass shape).  With EKG_TUNE=1 every
- * new pass shape is tuned on its first batched pass.  out (up to 6 values): row tile, CTAs per SM,
- * operand form (1 per-(AP, simulation), 0 persistent), ms per pass of the choice, ms per pass of
- * the built-in shape, candidates timed (0: the pass has no moved leads or is not in the batched
- * form, so there is nothing to tune).  Results of every shape are within the engine's tolerance of
+ * new pass shape is tuned on its first batched pass.  out (n_out values at most): [0] row tile,
+ * [1] CTAs per SM, [2] operand form (1 per-(AP, simulation), 0 persistent), [3] ms per pass of the
+ * choice, [4] ms per pass of the built-in shape, [5] candidates timed (0: the pass has no moved
+ * leads or is not in the batched form, so there is nothing to tune), [6] operand blocks per SM
+ * (0 = as many as fit); then per candidate five values: row tile, CTAs per SM, operand form,
+ * operand blocks per SM, ms per pass.  Results of every shape are within the engine's tolerance of
  * one another (the shapes change FP32 summation order only). */
 int ekg_heart_tune(ekg_heart *h, int32_t n_sims, const double *layer_k, const double *leads, int32_t reps,
                    double *out, int32_t n_out);
 /* The candidate shapes the tuner times for a pass (host only): shapes_out receives up to
- * max_shapes triples (row tile, CTAs per SM, operand form), *n_out their number. */
+ * max_shapes quadruples (row tile, CTAs per SM, operand form, operand blocks per SM), *n_out their
+ * number. */
 int ekg_tune_candidates(int32_t two_bases, int32_t rows_used, int32_t n_sims, int32_t *shapes_out,
                         int32_t max_shapes, int32_t *n_out);
-/* The tuner's cache file (host only): one line per pass shape, "key rows ctas form ms candidates",
- * later lines winning.  _put appends a shape (triple as above) for `key` (no spaces); _get reads the
- * last valid one (EKG_ERR_NOT_FOUND when there is none). */
+/* The tuner's cache file (host only): one line per pass shape, "key rows ctas form ms candidates
+ * blocks", later lines winning.  _put appends a shape (quadruple as above) for `key` (no spaces);
+ * _get reads the last valid one (EKG_ERR_NOT_FOUND when there is none). */
 int ekg_tune_cache_put(const char *path, const char *key, const int32_t *shape, double ms);
 int ekg_tune_cache_get(const char *path, const char *key, int32_t *shape_out, double *ms_out);
 

@@ -241,30 +241,31 @@ def test_tuner_candidates_and_cache(tmp_path):
     lib = L.load()
 
     def cands(two, rows, sims):
-        out = np.zeros(3 * 64, dtype=np.int32)
+        out = np.zeros(4 * 64, dtype=np.int32)
         n = ctypes.c_int32()
         L.check(lib.ekg_tune_candidates(two, rows, sims, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), 64,
                                         ctypes.byref(n)))
-        return [tuple(out[3 * i:3 * i + 3]) for i in range(n.value)]
+        return [tuple(out[4 * i:4 * i + 4]) for i in range(n.value)]
 
     big = cands(0, 512, 256)
     assert {c[0] for c in big} == {32, 128, 256} and {c[1] for c in big} == {1, 2, 4}
-    assert all(c[2] == 0 for c in big) and len(big) == 9
+    assert all(c[2] == 0 for c in big) and {c[3] for c in big} == {0, 4} and len(big) == 18
     assert {c[0] for c in cands(1, 512, 256)} == {32, 128}
     small = cands(0, 2, 1)
     assert {c[0] for c in small} == {32} and {c[2] for c in small} == {0, 1}
+    assert all(c[3] == 0 for c in small if c[2] == 1)
     path = str(tmp_path / "tune.txt").encode()
-    I3 = ctypes.c_int32 * 3
-    L.check(lib.ekg_tune_cache_put(path, b"k1", I3(128, 1, 0), 0.5))
-    L.check(lib.ekg_tune_cache_put(path, b"k2", I3(32, 2, 1), 0.25))
-    L.check(lib.ekg_tune_cache_put(path, b"k1", I3(256, 4, 0), 0.4))
+    I4 = ctypes.c_int32 * 4
+    L.check(lib.ekg_tune_cache_put(path, b"k1", I4(128, 1, 0, 0), 0.5))
+    L.check(lib.ekg_tune_cache_put(path, b"k2", I4(32, 2, 1, 0), 0.25))
+    L.check(lib.ekg_tune_cache_put(path, b"k1", I4(256, 4, 0, 4), 0.4))
     with open(path, "a") as f:
-        f.write("k1 77 1 0 0.1 9\n")  # not a row tile: ignored
-    got = I3()
+        f.write("k1 77 1 0 0.1 9 0\n")  # not a row tile: ignored
+    got = I4()
     ms = ctypes.c_double()
     L.check(lib.ekg_tune_cache_get(path, b"k1", got, ctypes.byref(ms)))
-    assert tuple(got) == (256, 4, 0) and ms.value == 0.4
+    assert tuple(got) == (256, 4, 0, 4) and ms.value == 0.4
     L.check(lib.ekg_tune_cache_get(path, b"k2", got, ctypes.byref(ms)))
-    assert tuple(got) == (32, 2, 1)
+    assert tuple(got) == (32, 2, 1, 0)
     assert lib.ekg_tune_cache_get(path, b"k3", got, ctypes.byref(ms)) == -9
-    assert lib.ekg_tune_cache_put(path, b"a b", I3(32, 1, 0), 1.0) == -1
+    assert lib.ekg_tune_cache_put(path, b"a b", I4(32, 1, 0, 0), 1.0) == -1
