@@ -298,14 +298,10 @@ __global__ void k_ca_bucket_init(size_t n, const uint8_t *__restrict__ layers, c
     }
 }
 
-// One bucket, by the whole grid.  Queue entries and counts are read through L2 (__ldcg): in the
-// single-launch form below other blocks wrote them in earlier buckets of the same launch, and a
-// line left in this SM's L1 from an earlier round of the ring would be stale.  Times read from L1
-// can only be stale upwards (they only decrease), which costs an extra atomic, never a wrong value.
-__device__ __forceinline__ void bucket_step(int k, const BucketArgs &A) {
+__global__ void __launch_bounds__(256) k_ca_bucket(int k, BucketArgs A) {
     const int slot = k % A.ring;
     if (blockIdx.x == 0 && threadIdx.x == 0) A.counts[(k + A.ring - 1) % A.ring] = 0;
-    const int n = min(__ldcg(A.counts + slot), A.cap);
+    const int n = min(A.counts[slot], A.cap);
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     // lane -> neighbour offset (26 of the 32 lanes)
@@ -320,9 +316,8 @@ __device__ __forceinline__ void bucket_step(int k, const BucketArgs &A) {
     }
     // the loop bound is uniform over the warp, so every lane reaches the warp votes below
     for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += warps) {
-        const int4 raw = __ldcg(reinterpret_cast<const int4 *>(A.lists + (size_t)slot * A.cap + e));
-        const int u = raw.x, lu = raw.y;
-        const unsigned long long qbits = ((unsigned long long)(uint32_t)raw.w << 32) | (uint32_t)raw.z;
+        const QEntry q = A.lists[(size_t)slot * A.cap + e];
+        const int u = q.cell;
         const int x = u % A.nx, y = (u / A.nx) % A.ny, z = u / (A.nx * A.ny);
         const int vz = z + dz, vy = y + dy, vx = x + dx;
         const bool inside = nb && vz >= 0 && vz < A.nz && vy >= 0 && vy < A.ny && vx >= 0 && vx < A.nx;
@@ -331,9 +326,9 @@ __device__ __forceinline__ void bucket_step(int k, const BucketArgs &A) {
         const unsigned long long bv = inside ? A.at[v] : 0ull;
         bool improved = false;
         double c = 0.0;
-        if (lv != 0 && qbits < bv) {
-            c = __dadd_rn(__longlong_as_double((long long)qbits),
-                          __ldg(A.lag + ((size_t)lu * A.nl1 + lv) * 3 + (kind - 1)));
+        if (lv != 0 && q.bits < bv) {
+            c = __dadd_rn(__longlong_as_double((long long)q.bits),
+                          __ldg(A.lag + ((size_t)q.layer * A.nl1 + lv) * 3 + (kind - 1)));
             const unsigned long long cb = (unsigned long long)__double_as_longlong(c);
             improved = cb < bv && cb < atomicMin(&A.at[v], cb);
         }
@@ -353,77 +348,6 @@ __device__ __forceinline__ void bucket_step(int k, const BucketArgs &A) {
                 atomicOr(A.overflow, 1);
         }
     }
-}
-
-// One launch per bucket (the host reads the counts every few buckets).
-__global__ void __launch_bounds__(256) k_ca_bucket(int k, BucketArgs A) { bucket_step(k, A); }
-
-// All buckets in one cooperative launch: a grid barrier between buckets replaces the launch
-// boundary.  After the barrier every block reads the counts of the slots still to come; appends
-// only add to them and the next bucket's appends happen after every block has read them, so all
-// blocks take the same decision to go on or stop.  The barrier's spin is bounded: a block that
-// gives up records status 2 and leaves, and the blocks still in the loop give up at the next
-// barrier.  Status 1: kmax buckets ran with cells still queued.
-struct CoopSync {
-    unsigned count, gen;
-    int status, steps;
-};
-constexpr unsigned COOP_SPIN_LIMIT = 1u << 24;  // polls of 64 ns or more: about a second at most
-
-__device__ __forceinline__ bool grid_barrier(CoopSync *cs) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int ok = 1;
-        volatile unsigned *gen = &cs->gen;
-        const unsigned g = *gen;
-        __threadfence();
-        if (atomicAdd(&cs->count, 1u) == gridDim.x - 1) {
-            atomicExch(&cs->count, 0u);
-            __threadfence();
-            atomicAdd(&cs->gen, 1u);
-        } else {
-            for (unsigned i = 0; *gen == g; ++i) {
-                if (i >= COOP_SPIN_LIMIT) {
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
-
-__global__ void __launch_bounds__(256) k_ca_bucket_coop(int k0, long long kmax, BucketArgs A, CoopSync *cs) {
-    __shared__ int s_pending;
-    int k = k0;
-    long long steps = 0;
-    for (;;) {
-        if (steps >= kmax) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&cs->status, 1);
-            break;
-        }
-        bucket_step(k, A);
-        ++k;
-        ++steps;
-        if (!grid_barrier(cs)) {
-            if (threadIdx.x == 0) atomicMax(&cs->status, 2);
-            break;
-        }
-        if (threadIdx.x == 0) {
-            int p = 0;
-            for (int r = 0; r < A.ring; ++r)
-                if (r != (k - 1) % A.ring && __ldcg(A.counts + r) > 0) p = 1;
-            s_pending = p;
-        }
-        __syncthreads();
-        if (!s_pending) break;
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) cs->steps = (int)steps;
 }
 
 __global__ void k_ca_bucket_finish(size_t n, const unsigned long long *__restrict__ bits, double *__restrict__ at) {
@@ -494,44 +418,6 @@ bool ca_run_buckets(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_lay
     EKG_CUDA(cudaGetLastError());
     // buckets before the first start time are empty
     int k = (int)std::floor(1.0 * A.inv_delta);
-    // every cell settles at most once per bucket it is queued in; more buckets than cells plus the
-    // ring means the queues never drain
-    const int64_t kmax = round_cap > 0 ? (int64_t)round_cap : (int64_t)n + 4LL * ring + 1024;
-    // one cooperative launch over all buckets when the device supports it (two blocks per SM)
-    int coop = 0, per_sm = 0;
-    {
-        int dev = 0;
-        EKG_CUDA(cudaGetDevice(&dev));
-        EKG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
-    }
-    EKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ca_bucket_coop, 256, 0));
-    if (coop && per_sm >= 1) {
-        DBuf<CoopSync> cs;
-        cs.alloc(1);
-        EKG_CUDA(cudaMemsetAsync(cs.p, 0, sizeof(CoopSync), s));
-        int k0 = k;
-        long long km = (long long)kmax;
-        BucketArgs Ac = A;
-        CoopSync *csp = cs.p;
-        void *args[] = {&k0, &km, &Ac, &csp};
-        const dim3 g((unsigned)(std::max(1, sm_count) * std::min(2, per_sm)));
-        EKG_CUDA(cudaLaunchCooperativeKernel((const void *)k_ca_bucket_coop, g, dim3(256), args, 0, s));
-        CoopSync hs{};
-        int32_t ovf = 0;
-        EKG_CUDA(cudaMemcpyAsync(&hs, cs.p, sizeof(CoopSync), cudaMemcpyDeviceToHost, s));
-        EKG_CUDA(cudaMemcpyAsync(&ovf, counts.p + ring, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-        EKG_CUDA(cudaStreamSynchronize(s));
-        if (ovf || hs.status == 2) return false;  // a full bucket list or a barrier that gave up: tile rounds
-        if (hs.status == 1) throw Error{EKG_ERR_CA_NOT_CONVERGED, "activation-time relaxation did not converge"};
-        k_ca_bucket_finish<<<1024, 256, 0, s>>>(n, bits.p, d_at);
-        EKG_CUDA(cudaGetLastError());
-        EKG_CUDA(cudaEventRecord(e1, s));
-        EKG_CUDA(cudaEventSynchronize(e1));
-        EKG_CUDA(cudaEventElapsedTime(&res.ms, e0, e1));
-        res.rounds = hs.steps;
-        res.buckets = true;
-        return true;
-    }
     const int grid = std::max(1, sm_count) * 8;
     std::vector<int32_t> h(ring + 1);
     int32_t *hc = nullptr;
@@ -540,6 +426,9 @@ bool ca_run_buckets(cudaStream_t s, int nz, int ny, int nx, const uint8_t *d_lay
         int32_t *p;
         ~Pinned() { cudaFreeHost(p); }
     } pin{hc};
+    // every cell settles at most once per bucket it is queued in; more buckets than cells plus the
+    // ring means the queues never drain
+    const int64_t kmax = round_cap > 0 ? (int64_t)round_cap : (int64_t)n + 4LL * ring + 1024;
     constexpr int CHUNK = 16;
     int steps = 0;
     for (;;) {
