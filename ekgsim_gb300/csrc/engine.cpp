@@ -818,7 +818,8 @@ bool tune_cache_read(const std::string &path, const std::string &key, TuneChoice
 }
 
 // Decide the pass: the batched (separable) form when the batch shares k1 and k4 per layer, no
-// layer has k0 != 0, exp(k5 at) has a short Taylor expansion and there are at least two sims.
+// layer's k0 differs from another's (per simulation), exp(k5 at) has a short Taylor expansion and
+// there are at least two sims.
 PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *leads) {
     PassPlan P;
     P.n_sims = n_sims;
@@ -840,7 +841,10 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
     for (int si = 0; si < n_sims; ++si)
         for (int i = 0; i < nl; ++i) {
             const double *k = layer_k + ((size_t)si * nl + i) * 9;
-            if (k[1] != key[2 * i] || k[4] != key[2 * i + 1] || k[0] != 0.0) return P;
+            // the resting potential k0 leaves sum_L k0_L sum_{a in L} W[l, a], which the batched form
+            // does not add: it vanishes when k0 is the same in every layer, since the AP differences
+            // of the dipoles make sum_a W[l, a] = 0 (simlib/simulator.cpp:509-525)
+            if (k[1] != key[2 * i] || k[4] != key[2 * i + 1] || k[0] != layer_k[(size_t)si * nl * 9]) return P;
             if (k[3] != layer_k[9 * i + 3]) k3_uniform = false;
         }
     // A single simulation takes the batched form once its (k1, k4) is settled: when the basis for it

@@ -802,3 +802,38 @@ def test_activation_edge_shapes(case):
             assert rel_l2(h.simulate(lk), O.run(layer, at_ref, lk, leads, "3D4", 0.0, 60.0, 1.0)) <= ECG_TOL
         h.close()
         e.close()
+
+
+def test_batched_form_uniform_resting_potential(engine):
+    """A resting potential k0 that is the same in every layer (-86 mV here) cancels in the dipoles
+    (sum_a W[l, a] = 0), so the batched form takes such batches; with k0 differing between layers
+    the batch takes the per-simulation form, which adds the constant term.  Both match the oracle."""
+    from ekgsim_gb300.engine import Heart
+    spec = synth.small_spec(40, n_leads=4, seed=29)
+    steps = 300
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(3, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    h = Heart.create(engine, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+    target = [t for t in synth.analytic_target(spec.n_leads, steps, 6)]
+    at, layer = O.activation(grid, tm)
+    genes = np.stack([synth.genes_for(spec, 80 + r, 0) for r in range(12)])
+    for k0s in ((-86.0, -86.0, -86.0), (-86.0, -80.0, -90.0)):
+        base = [[k0] + list(synth.BASE_AP[1:]) for k0 in k0s]
+        kmin, kmax = list(synth.K_MIN), list(synth.K_MAX)
+        kmin[0], kmax[0] = min(k0s), max(k0s)
+        h.set_eval(base, kmin, kmax, [5, 6, 7, 8], target, mid_position=0.6)
+        _, _, ecg_b = h.eval_batch(genes, want_ecg=True)
+        lks = np.stack([O.layer_aps(3, np.array(base), np.array(kmin), np.array(kmax), [5, 6, 7, 8], "endo-mid-epi",
+                                    0.6, g[:12])[0] for g in genes])
+        moveds = np.stack([O.move_leads(leads, g[12:].reshape(-1, 2)) for g in genes])
+        assert h.benchmark(lks, moveds, warmup=1, iters=1)["batched"] == (len(set(k0s)) == 1)
+        for i in (0, 11):
+            g = genes[i]
+            lk = O.layer_aps(3, np.array(base), np.array(kmin), np.array(kmax), [5, 6, 7, 8], "endo-mid-epi", 0.6,
+                             g[:12])[0]
+            assert np.allclose(lk[:, 0], k0s)
+            moved = O.move_leads(leads, g[12:].reshape(-1, 2))
+            ref = O.run(layer, at, lk, moved, "3D4", 0.0, float(steps), 1.0)
+            assert rel_l2(ecg_b[i], ref) <= ECG_TOL, (k0s, i)
+    h.close()
