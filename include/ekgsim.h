@@ -153,12 +153,12 @@ int ekg_heart_benchmark(ekg_heart *h, int32_t n_sims, const double *layer_k, con
  * one another (the shapes change FP32 summation order only). */
 int ekg_heart_tune(ekg_heart *h, int32_t n_sims, const double *layer_k, const double *leads, int32_t reps,
                    double *out, int32_t n_out);
-/* The candidate shapes the tuner times for a pass (host only): shapes_out receives up to
+/* The candidate shapes the tuner times for a pass (host only; no counterpart in the reference): shapes_out receives up to
  * max_shapes quadruples (row tile, CTAs per SM, operand form, operand blocks per SM), *n_out their
  * number. */
 int ekg_tune_candidates(int32_t two_bases, int32_t rows_used, int32_t n_sims, int32_t *shapes_out,
                         int32_t max_shapes, int32_t *n_out);
-/* The tuner's cache file (host only): one line per pass shape, "key rows ctas form ms candidates
+/* The tuner's cache file (host only; no counterpart in the reference): one line per pass shape, "key rows ctas form ms candidates
  * blocks", later lines winning.  _put appends a shape (quadruple as above) for `key` (no spaces);
  * _get reads the last valid one (EKG_ERR_NOT_FOUND when there is none). */
 int ekg_tune_cache_put(const char *path, const char *key, const int32_t *shape, double ms);
@@ -193,6 +193,9 @@ typedef struct {
     const double *disp_max;
 } ekg_eval_config;
 
+/* Set the evaluation settings of a heart: what SimImplementation's constructor takes from
+ * simulator.ini and the target file (sim.cpp:362-431, targets sim.cpp:999-1042).  Evaluations in
+ * flight complete with the settings they started with. */
 int ekg_heart_set_eval(ekg_heart *h, const ekg_eval_config *cfg);
 /* Number of genes and criteria (SimImplementation::getGeneParams, sim.cpp:523-580). */
 int ekg_eval_shape(ekg_heart *h, int32_t *n_genes, int32_t *n_criteria);
@@ -280,8 +283,9 @@ int ekg_server_poll_many(ekg_server *s, int32_t n, const uint64_t *request_ids, 
                          int32_t crit_stride, double *criteria_out, double *violation_out,
                          int32_t *status_out, ekg_request_stats *stats_out);
 
-/* Test hook: replace the free-device-memory query the admission check uses (fn returns free
- * bytes; NULL restores cudaMemGetInfo).  Lets tests refuse admission without filling the GPU. */
+/* Test hook (no counterpart in the reference): replace the free-device-memory query the admission
+ * check uses (fn returns free bytes; NULL restores cudaMemGetInfo).  Lets tests refuse admission
+ * without filling the GPU. */
 int ekg_server_set_free_bytes_provider(ekg_server *s, uint64_t (*fn)(void *ctx), void *ctx);
 
 /* Activation times without any device allocation, for callers that cannot call cudaMalloc (for
