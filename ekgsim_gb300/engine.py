@@ -5,13 +5,12 @@ These wrap include/ekgsim.h one to one; numpy arrays cross the boundary as plain
 from __future__ import annotations
 
 import ctypes
-import math
-from typing import Optional, Sequence
+from typing import Optional
 
 import numpy as np
 
 from . import _lib as L
-from ._lib import EkgError, check, dptr, i32ptr, i64ptr
+from ._lib import EkgError, check, dptr, i32ptr, i64ptr  # noqa: F401 (EkgError is part of this module's API)
 
 
 class Engine:
