@@ -325,7 +325,9 @@ __device__ __forceinline__ void few_w(const InteriorField &ic, const MSquares (&
 // voxels (padding, at the end of a layer) get 0.  Interior voxels use the closed form where the
 // lane's leads are at least 20 cells away (lanes normally agree), boundary voxels with few absent
 // neighbours the closed form minus those, the rest the exact sum.
-template <bool DIAG, int NP>
+// ALLFAR: every voxel of the chunk is known to be far from the lane's leads (the stage's bounding
+// box is), so the per-voxel distance test is skipped.
+template <bool DIAG, int NP, bool ALLFAR = false>
 __device__ __forceinline__ void chunk_w(int vb, int vend, const float4 *vox_pos, const float4 *vox_out,
                                         const float4 (&r)[NP], int nnb, const float *s_d, const InteriorField &ic,
                                         float (*s_w)[8][LF_THREADS], int tid) {
@@ -342,7 +344,7 @@ __device__ __forceinline__ void chunk_w(int vb, int vend, const float4 *vox_pos,
 #pragma unroll
         for (int k = 0; k < NP; ++k) {
             q[k] = msq(pos, r[k]);
-            far = far && q[k].s >= INTERIOR_S_MIN;
+            if (!ALLFAR) far = far && q[k].s >= INTERIOR_S_MIN;
         }
         if ((mi & VOX_INTERIOR) && far) {
 #pragma unroll
@@ -394,7 +396,8 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
     const float2 *__restrict__ at_hilo, const int32_t *__restrict__ a_layer, const float *__restrict__ k5l, int nl,
     const float4 *__restrict__ hconst, const float4 *__restrict__ lrel, int nmove, int n_sims,
     const float2 *__restrict__ tref, const int32_t *__restrict__ nent, const int32_t *__restrict__ esplit,
-    const int32_t *__restrict__ stage_order, uint8_t *__restrict__ Bt, float2 *__restrict__ P1) {
+    const int32_t *__restrict__ stage_order, const float4 *__restrict__ stage_box, uint8_t *__restrict__ Bt,
+    float2 *__restrict__ P1) {
     __shared__ float s_d[26 * 4];
     __shared__ float s_w[LF_ROWS][8][LF_THREADS];
     __shared__ float2 s_at[BST];  // the stage's activation times
@@ -439,6 +442,23 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
         __syncthreads();
         const float4 *vp = staged ? s_vpos : vox_pos, *vo = staged ? s_vout : vox_out;
         const int rb = (item % ngr) * (LF_THREADS * LF_ROWS) + tid * LF_ROWS;
+        // whether every voxel of the stage is far from every lead of the warp (squared distance from
+        // the lead to the stage's bounding box; a margin of one cell over the closed form's bound)
+        bool far_all = true;
+        if (rb < rows_used) {
+            const float4 lo = stage_box[2 * (size_t)st], hi = stage_box[2 * (size_t)st + 1];
+            const int nr0 = min(LF_ROWS, rows_used - rb);
+#pragma unroll
+            for (int q = 0; q < LF_ROWS; ++q) {
+                if (q >= nr0) break;
+                const float4 r = lrel[rb + q];
+                const float dz = fmaxf(fmaxf(lo.x - r.x, r.x - hi.x), 0.f);
+                const float dy = fmaxf(fmaxf(lo.y - r.y, r.y - hi.y), 0.f);
+                const float dx = fmaxf(fmaxf(lo.z - r.z, r.z - hi.z), 0.f);
+                far_all = far_all && dz * dz + dy * dy + dx * dx >= INTERIOR_S_MIN + 41.f;
+            }
+        }
+        far_all = __all_sync(0xffffffffu, far_all);
         if (rb >= rows_used) continue;
         const int nr = min(LF_ROWS, rows_used - rb);  // rows of this thread; the rest repeat its last row
         float k5[LF_ROWS], S0[LF_ROWS], S1[LF_ROWS];
@@ -455,7 +475,8 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
                 float4 r[LF_ROWS];
 #pragma unroll
                 for (int q = 0; q < LF_ROWS; ++q) r[q] = lrel[rb + min(q, nr - 1)];
-                chunk_w<DIAG, LF_ROWS>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
+                if (far_all) chunk_w<DIAG, LF_ROWS, true>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
+                else chunk_w<DIAG, LF_ROWS, false>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
             }
             const int col = (st & 1) * (BST / 8) + kc;  // 8-AP column within the 64-AP tile
 #pragma unroll
@@ -1200,7 +1221,8 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, b
         const int grid = std::max(1, std::min(nst * ngr, bps * sm_count));                                       \
         k_batch_lead_field<NN, DG><<<grid, LF_THREADS, 0, s>>>(                                                   \
             nst, ngr, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p, \
-            k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, B.stage_order, Bt, B.P1);      \
+            k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, B.stage_order, h.stage_box.p,  \
+            Bt, B.P1);                                                                                            \
     } while (0)
     switch (tile_rows) {
     case 32:

@@ -156,6 +156,7 @@ struct HeartDev {
     DBuf<uint32_t> vox_nbo; // [nvox] out-neighbour mask
     DBuf<float4> vox_pos;   // [nvox] bordered position relative to `centre` (z,y,x) + in-mask bits in .w
     DBuf<float4> vox_out;   // [nvox] sum of the out-neighbour offsets (z,y,x), .w = 1 if any
+    DBuf<float4> stage_box; // [2 * apad / 32] per 32-AP stage: lowest and highest voxel position (z,y,x)
     double centre[3] = {0, 0, 0};
     // K chunks
     DBuf<int32_t> chunk_a0, chunk_a1, chunk_layer;  // [nchunks]
@@ -192,6 +193,9 @@ void setup_voxels_device(cudaStream_t s, int nz, int ny, int nx, const uint8_t *
 void setup_ap_arrays_device(cudaStream_t s, const DedupResult &r, const double *d_at_cells, double *at,
                             float2 *at_hilo, int32_t *a_layer, int64_t *a_vb);
 // per-voxel records of the dipole kernels; returns the number of voxels flagged interior
+// Bounding box of each 32-AP stage's voxel positions (empty stages: an inverted box).
+void setup_stage_boxes_device(cudaStream_t s, int64_t apad, const int64_t *a_vox_begin, const float4 *vox_pos,
+                              float4 *stage_box);
 int64_t setup_voxel_records_device(cudaStream_t s, const DedupResult &r, int nz, int ny, int nx, const uint8_t *d_lay,
                                    const HeartDev &D, int few_max, int32_t *vzyx, uint32_t *vin, uint32_t *vout,
                                    float4 *vpos, float4 *vosum);

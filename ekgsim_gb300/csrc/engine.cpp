@@ -427,6 +427,8 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     const int few_max = D.nhood == EKG_NHOOD_3D4 ? 2 : D.nnb / 2;
     D.n_interior = setup_voxel_records_device(s, dd, d->nz, d->ny, d->nx, dl.p, D, few_max, D.vox_zyx.p, D.vox_nb.p,
                                               D.vox_nbo.p, D.vox_pos.p, D.vox_out.p);
+    D.stage_box.alloc((size_t)2 * (apad / 32));
+    setup_stage_boxes_device(s, apad, D.a_vox_begin.p, D.vox_pos.p, D.stage_box.p);
     // host copies of the sorted voxel cells and AP starts, for the reference's AP numbering
     h->vox_cell.resize(nv);
     h->vox_group_start.resize(na + 1);
@@ -459,7 +461,7 @@ int64_t heart_device_bytes(const ekg_heart *h) {
     const HeartDev &D = h->dev;
     int64_t b = D.at.bytes() + D.at_hilo.bytes() + D.a_layer.bytes() + D.a_vox_begin.bytes() + D.vox_zyx.bytes() +
                 D.vox_nb.bytes() + D.vox_nbo.bytes() + D.chunk_a0.bytes() * 3 + D.t.bytes() + D.t_hilo.bytes() +
-                h->W0.bytes() + h->at_cells.bytes();
+                h->W0.bytes() + h->at_cells.bytes() + D.vox_pos.bytes() + D.vox_out.bytes() + D.stage_box.bytes();
     const EvalDev &E = h->ev;
     b += (int64_t)h->stg[0].dev.bytes() + (int64_t)h->stg[1].dev.bytes() + E.layer_c.bytes() + E.F.bytes() + E.k0w.bytes() + E.W.bytes() +
          E.Wp.bytes() + E.partial.bytes() + E.ecg.bytes() + E.ecg_ff.bytes() + E.coef.bytes() + E.crit.bytes() + E.targets.bytes() +

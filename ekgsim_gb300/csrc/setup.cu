@@ -464,4 +464,53 @@ int64_t setup_voxel_records_device(cudaStream_t s, const DedupResult &r, int nz,
     return (int64_t)h;
 }
 
+// ------------------------------------------------------------------ stage bounding boxes
+// Block per 32-AP stage: the lowest and highest voxel position over the stage's voxels, so that the
+// operand kernel can tell for a whole stage whether every voxel is far from a lead.
+__global__ void k_stage_boxes(int64_t nst, const int64_t *__restrict__ a_vox_begin, const float4 *__restrict__ vox_pos,
+                              float4 *__restrict__ box) {
+    __shared__ float red[6][4];
+    const int64_t st = blockIdx.x;
+    const int64_t v0 = a_vox_begin[st * 32], v1 = a_vox_begin[st * 32 + 32];
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
+        const float4 p = vox_pos[v];
+        lo[0] = fminf(lo[0], p.x);
+        lo[1] = fminf(lo[1], p.y);
+        lo[2] = fminf(lo[2], p.z);
+        hi[0] = fmaxf(hi[0], p.x);
+        hi[1] = fmaxf(hi[1], p.y);
+        hi[2] = fmaxf(hi[2], p.z);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 3; ++k) {
+            red[k][w] = lo[k];
+            red[3 + k][w] = hi[k];
+        }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int j = 1; j < (int)(blockDim.x >> 5); ++j)
+            for (int k = 0; k < 3; ++k) {
+                red[k][0] = fminf(red[k][0], red[k][j]);
+                red[3 + k][0] = fmaxf(red[3 + k][0], red[3 + k][j]);
+            }
+        box[2 * st] = make_float4(red[0][0], red[1][0], red[2][0], 0.f);
+        box[2 * st + 1] = make_float4(red[3][0], red[4][0], red[5][0], 0.f);
+    }
+}
+
+void setup_stage_boxes_device(cudaStream_t s, int64_t apad, const int64_t *a_vox_begin, const float4 *vox_pos,
+                              float4 *stage_box) {
+    const int64_t nst = apad / 32;
+    if (nst <= 0) return;
+    k_stage_boxes<<<(unsigned)nst, 128, 0, s>>>(nst, a_vox_begin, vox_pos, stage_box);
+    EKG_CUDA(cudaGetLastError());
+}
+
 }  // namespace ekg
