@@ -838,3 +838,54 @@ def test_batched_form_uniform_resting_potential(engine):
             ref = O.run(layer, at, lk, moved, "3D4", 0.0, float(steps), 1.0)
             assert rel_l2(ecg_b[i], ref) <= ECG_TOL, (k0s, i)
     h.close()
+
+
+def test_batched_all_leads_moved_and_near_heart(engine):
+    """Every lead carries displacement genes (the reference's usual "optimize measuring points"
+    case, 12 + 2L genes), some of them moving leads to within a few cells of the heart, so that the
+    operand kernel takes both its closed-form path (stages far from every lead of a warp) and the
+    per-voxel exact path; a batch of 40 against the oracle."""
+    from ekgsim_gb300.engine import Heart
+    spec = synth.small_spec(48, n_leads=6, seed=33)
+    steps = 300
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(3, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    h = Heart.create(engine, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+    target = [t for t in synth.analytic_target(spec.n_leads, steps, 7)]
+    h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], target, mid_position=0.6)
+    rng = np.random.Generator(np.random.PCG64(71))
+    genes = np.stack([synth.genes_for(spec, 300 + r, 0) for r in range(40)])
+    genes[:, 12:] = rng.uniform(-50.0, 50.0, size=(40, 2 * spec.n_leads))
+    at, layer = O.activation(grid, tm)
+    nz = np.argwhere(layer > 0).astype(float) + 1.0  # bordered voxel coordinates (z, y, x)
+    mind = []
+    for g in genes:
+        moved = O.move_leads(leads, g[12:].reshape(-1, 2))
+        mind.append(min(np.sqrt(((nz - p) ** 2).sum(axis=1)).min() for p in moved))
+    assert min(mind) < 20.0 and max(mind) > 21.0  # both operand-kernel paths are taken
+    _, _, ecg_b = h.eval_batch(genes, want_ecg=True)
+    for i in (0, int(np.argmin(mind)), int(np.argmax(mind)), 39):
+        g = genes[i]
+        lk = O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], "endo-mid-epi",
+                         0.6, g[:12])[0]
+        ref = O.run(layer, at, lk, O.move_leads(leads, g[12:].reshape(-1, 2)), "3D4", 0.0, float(steps), 1.0)
+        assert rel_l2(ecg_b[i], ref) <= ECG_TOL, i
+    h.close()
+
+
+def test_c2_batched_twelve_leads(engine, tmp_path):
+    """The single-simulation configuration's heart (128^3, 12 leads, 600 steps) in the batched form:
+    a batch of 16 distinct vectors, 4 of them against the oracle."""
+    from ekgsim_gb300.engine import Heart
+    w, c = _workload(tmp_path, 1)
+    s = O.load_setup(str(tmp_path))
+    h = Heart.from_ini(engine, os.path.join(str(tmp_path), "simulator.ini"))
+    genes = np.stack([synth.genes_for(c["spec"], 20 + r, 1) for r in range(16)])
+    crit_b, viol_b, ecg_b = h.eval_batch(genes, want_ecg=True)
+    for i in (0, 5, 10, 15):
+        crit_ref, viol_ref, ecg_ref, _, _ = O.evaluate(s, genes[i])
+        assert rel_l2(ecg_b[i], ecg_ref) <= ECG_TOL, i
+        assert np.allclose(crit_b[i], crit_ref, rtol=0, atol=1e-4)
+        assert viol_b[i] == viol_ref
+    h.close()
