@@ -127,7 +127,8 @@ __global__ void __launch_bounds__(128) k_static_combine(int steps, int nleads, i
                                                         int n_sims, const float *__restrict__ F,
                                                         const float *__restrict__ coef, const double *__restrict__ k3,
                                                         const float *__restrict__ Q1, const float *__restrict__ Q2,
-                                                        double *__restrict__ ecg, float2 *__restrict__ ecg_ff) {
+                                                        double *__restrict__ ecg, float2 *__restrict__ ecg_ff,
+                                                        const double *__restrict__ cst) {
     __shared__ float s_c[SC_SIMS][11];  // [simulation][j < J: coefficient, 10: k3] of the current layer
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int l = nmove + blockIdx.y, s0 = blockIdx.z * SC_SIMS;
@@ -171,6 +172,7 @@ __global__ void __launch_bounds__(128) k_static_combine(int steps, int nleads, i
     for (int i = 0; i < SC_SIMS; ++i)
         if (i < ns) {
             const size_t o = ((size_t)(s0 + i) * nleads + l) * steps + t;
+            if (cst) acc[i] = ff_add(acc[i], ff_from_double(cst[(size_t)(s0 + i) * nleads + l]));
             ecg[o] = ff_to_double(acc[i]);
             ecg_ff[o] = acc[i];
         }
@@ -397,7 +399,7 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
     const float4 *__restrict__ hconst, const float4 *__restrict__ lrel, int nmove, int n_sims,
     const float2 *__restrict__ tref, const int32_t *__restrict__ nent, const int32_t *__restrict__ esplit,
     const int32_t *__restrict__ stage_order, const float4 *__restrict__ stage_box, uint8_t *__restrict__ Bt,
-    float2 *__restrict__ P1) {
+    float2 *__restrict__ P1, float *__restrict__ P2) {
     __shared__ float s_d[26 * 4];
     __shared__ float s_w[LF_ROWS][8][LF_THREADS];
     __shared__ float2 s_at[BST];  // the stage's activation times
@@ -507,6 +509,14 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
                 }
                 S0[q] += z0;
                 S1[q] += z1;
+                if (P2) {
+                    // the unscaled field sums of the 8 APs (the resting-potential term, k_k0_moved)
+                    float z2 = 0.f;
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) z2 += s_w[q][j][tid];
+                    const int s = row / nmove, l = row % nmove;
+                    P2[((size_t)st * 4 + kc) * rows_used + (size_t)l * n_sims + s] = z2;
+                }
             }
         }
         const int ne = nent[L];
@@ -533,7 +543,7 @@ __global__ void __launch_bounds__(128) k_batch_lead_field_small(
     const int32_t *__restrict__ a_layer, const float *__restrict__ k5l, int nl, const float4 *__restrict__ hconst,
     const float4 *__restrict__ lrel, int nmove, int n_sims, const float2 *__restrict__ tref,
     const int32_t *__restrict__ nent, const int32_t *__restrict__ esplit, uint8_t *__restrict__ Bt,
-    float2 *__restrict__ P1) {
+    float2 *__restrict__ P1, float *__restrict__ P2) {
     __shared__ float s_d[26 * 4];
     const int tid = threadIdx.x, lane = tid & 31;
     if (tid < nnb) {
@@ -580,6 +590,20 @@ __global__ void __launch_bounds__(128) k_batch_lead_field_small(
                         acc1 += DIAG ? voxel_w_diag(pos, mi, out, r1) : voxel_w_general(pos, mi, out, r1, nnb, s_d);
                 }
             }
+        if (P2 && valid) {
+            // unscaled field sums per 8-AP part of the stage (the resting-potential term): the warp
+            // is one stage, eight lanes one part
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                if (q >= np) break;
+                float z = q ? acc1 : acc0;  // every AP, activated or not (padding slots hold no voxels)
+                z += __shfl_xor_sync(0xffffffffu, z, 1);
+                z += __shfl_xor_sync(0xffffffffu, z, 2);
+                z += __shfl_xor_sync(0xffffffffu, z, 4);
+                if ((lane & 7) == 0)
+                    P2[((size_t)st * 4 + (lane >> 3)) * rows_used + (size_t)(l0 + q) * n_sims + s] = z;
+            }
+        }
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             if (q >= np) break;
@@ -929,7 +953,7 @@ __global__ void __launch_bounds__(256) k_reduce_band_w(int steps, int rows, int 
                                                      const float *__restrict__ partial, const float2 *__restrict__ U,
                                                      const float *__restrict__ E, const float *__restrict__ F,
                                                      const double *__restrict__ k3, double *__restrict__ ecg,
-                                                       float2 *__restrict__ ecg_ff) {
+                                                       float2 *__restrict__ ecg_ff, const double *__restrict__ cmov) {
     __shared__ float red[8][2][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int tt = blockIdx.x * 32 + lane;
@@ -978,6 +1002,7 @@ __global__ void __launch_bounds__(256) k_reduce_band_w(int steps, int rows, int 
     }
     if (w == 0 && on) {
         const size_t o = ((size_t)s * nleads + l) * steps + tt;
+        if (cmov) v = ff_add(v, ff_from_double(cmov[rp]));
         ecg[o] = ff_to_double(v);
         ecg_ff[o] = v;
     }
@@ -989,7 +1014,7 @@ __global__ void k_reduce_band(int steps, int rows, int nmove, int n_sims, int nl
                               const int32_t *__restrict__ ent, const float *__restrict__ partial,
                               const float2 *__restrict__ U, const float *__restrict__ E, const float *__restrict__ F,
                               const double *__restrict__ k3, double *__restrict__ ecg,
-                              float2 *__restrict__ ecg_ff) {
+                              float2 *__restrict__ ecg_ff, const double *__restrict__ cmov) {
     const int t0 = (blockIdx.x * blockDim.x + threadIdx.x) * RB_T;  // RB_T steps inside one 128-step tile
     if (t0 >= steps) return;
     const int r = blockIdx.y;
@@ -1039,11 +1064,13 @@ __global__ void k_reduce_band(int steps, int rows, int nmove, int n_sims, int nl
             v[k] = ff_add_f(v[k], F[((size_t)s * nl + L) * steps + tt] * x);
         }
     }
+    const float2 c = cmov ? ff_from_double(cmov[rp]) : make_float2(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < RB_T; ++k) {
         const int tt = t0 + k;
         if (tt >= steps) break;
         const size_t o = ((size_t)s * nleads + l) * steps + tt;
+        if (cmov) v[k] = ff_add(v[k], c);
         ecg[o] = ff_to_double(v[k]);
         ecg_ff[o] = v[k];
     }
@@ -1091,11 +1118,11 @@ void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int
 
 void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const float *F,
                            const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg,
-                           float2 *ecg_ff) {
+                           float2 *ecg_ff, const double *cst) {
     if (nmove >= h.nleads) return;
     dim3 grid((unsigned)((h.steps + 127) / 128), (unsigned)(h.nleads - nmove), (unsigned)((n_sims + SC_SIMS - 1) / SC_SIMS));
     k_static_combine<<<grid, 128, 0, s>>>(h.steps, h.nleads, h.nlayers, J, Jb, nmove, n_sims, F, coef, k3, Q1, Q2,
-                                          ecg, ecg_ff);
+                                          ecg, ecg_ff, cst);
     EKG_CUDA(cudaGetLastError());
 }
 
@@ -1210,7 +1237,7 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, b
             dim3 g((unsigned)((nst * BST + 127) / 128), (unsigned)n_sims);                                         \
             k_batch_lead_field_small<NN, DG><<<g, 128, 0, s>>>(                                                   \
                 nst, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p,    \
-                k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, Bt, B.P1);                 \
+                k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, Bt, B.P1, B.P2);           \
             break;                                                                                                \
         }                                                                                                         \
         static int per_sm = 0;                                                                                    \
@@ -1222,7 +1249,7 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, b
         k_batch_lead_field<NN, DG><<<grid, LF_THREADS, 0, s>>>(                                                   \
             nst, ngr, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p, \
             k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, B.stage_order, h.stage_box.p,  \
-            Bt, B.P1);                                                                                            \
+            Bt, B.P1, B.P2);                                                                                      \
     } while (0)
     switch (tile_rows) {
     case 32:
@@ -1254,6 +1281,80 @@ void launch_batch_gemm(cudaStream_t s, const BatchArgs &A) {
     }
 }
 
+// ------------------------------------------------------------------ resting-potential term
+// A layer's resting potential k0 adds k0_L sum_{a in L} W[l][a] to every sample of lead l (the AP
+// differences of the dipoles cancel it within a layer, simlib/simulator.cpp:509-525); the sum over
+// layers of sum_a W vanishes, so the term is taken relative to the first layer's k0.
+// Moved rows: thread per row' = l * S + s, the per-part unscaled sums P2 of each layer's stages
+// added in FP64 in a fixed order.
+__global__ void k_k0_moved(int rows_used, int n_sims, int nl, const int32_t *__restrict__ ls0,
+                           const int32_t *__restrict__ ls1, const float *__restrict__ P2,
+                           const double *__restrict__ layer_k, double *__restrict__ cmov) {
+    const int rp = blockIdx.x * blockDim.x + threadIdx.x;
+    if (rp >= rows_used) return;
+    const int s = rp % n_sims;
+    const double k00 = layer_k[(size_t)s * nl * 9];
+    double c = 0.0;
+    for (int L = 0; L < nl; ++L) {
+        double sw = 0.0;
+        for (int p = ls0[L] * 4; p < ls1[L] * 4; ++p) sw += (double)P2[(size_t)p * rows_used + rp];
+        c += (layer_k[((size_t)s * nl + L) * 9] - k00) * sw;
+    }
+    cmov[rp] = c;
+}
+
+// Static leads: K0s[L][l] = sum_{a in L} W0[l][a] in FP64, block per (lead, layer).
+__global__ void k_k0_static_sums(int nleads, int64_t apad, const int32_t *__restrict__ ls0,
+                                 const int32_t *__restrict__ ls1, const float *__restrict__ W0,
+                                 double *__restrict__ K0s) {
+    __shared__ double red[8];
+    const int l = blockIdx.x, L = blockIdx.y;
+    double v = 0.0;
+    for (int64_t a = (int64_t)ls0[L] * 32 + threadIdx.x; a < (int64_t)ls1[L] * 32; a += blockDim.x)
+        v += (double)W0[(size_t)l * apad + a];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        K0s[(size_t)L * nleads + l] = t;
+    }
+}
+
+// cst[s][l] = sum_L (k0_L - k0_0) K0s[L][l] for the static leads l >= nmove.
+__global__ void k_k0_static(int n_sims, int nleads, int nmove, int nl, const double *__restrict__ K0s,
+                            const double *__restrict__ layer_k, double *__restrict__ cst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_sims * nleads) return;
+    const int s = i / nleads, l = i % nleads;
+    if (l < nmove) return;
+    const double k00 = layer_k[(size_t)s * nl * 9];
+    double c = 0.0;
+    for (int L = 0; L < nl; ++L) c += (layer_k[((size_t)s * nl + L) * 9] - k00) * K0s[(size_t)L * nleads + l];
+    cst[i] = c;
+}
+
+void launch_k0_moved(cudaStream_t s, const BandArgs &A, const int32_t *ls0, const int32_t *ls1,
+                     const double *layer_k, double *cmov) {
+    k_k0_moved<<<(unsigned)((A.rows_used + 127) / 128), 128, 0, s>>>(A.rows_used, A.n_sims, A.nl, ls0, ls1, A.P2,
+                                                                     layer_k, cmov);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_k0_static_sums(cudaStream_t s, int nleads, int64_t apad, int nl, const int32_t *ls0, const int32_t *ls1,
+                           const float *W0, double *K0s) {
+    k_k0_static_sums<<<dim3((unsigned)nleads, (unsigned)nl), 256, 0, s>>>(nleads, apad, ls0, ls1, W0, K0s);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_k0_static(cudaStream_t s, int n_sims, int nleads, int nmove, int nl, const double *K0s,
+                      const double *layer_k, double *cst) {
+    const int n = n_sims * nleads;
+    k_k0_static<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n_sims, nleads, nmove, nl, K0s, layer_k, cst);
+    EKG_CUDA(cudaGetLastError());
+}
+
 int band_u_parts() { return BU_PARTS; }
 
 void launch_band_u(cudaStream_t s, const BandArgs &A) {
@@ -1269,12 +1370,12 @@ void launch_reduce_band(cudaStream_t s, const BandArgs &A) {
         dim3 grid((unsigned)((A.steps + 31) / 32), (unsigned)A.rows_used);
         k_reduce_band_w<<<grid, 256, 0, s>>>(A.steps, A.rows, A.nmove, A.n_sims, A.nleads, A.nl, A.ntt, A.max_ent,
                                              A.nb, A.ti0, A.ti1, A.ent, A.partial, A.U, A.E, A.F, A.k3, A.ecg,
-                                             A.ecg_ff);
+                                             A.ecg_ff, A.cmov);
     } else {
         dim3 grid((unsigned)((A.steps + 128 * RB_T - 1) / (128 * RB_T)), (unsigned)A.rows_used);
         k_reduce_band<<<grid, 128, 0, s>>>(A.steps, A.rows, A.nmove, A.n_sims, A.nleads, A.nl, A.ntt, A.max_ent,
                                            A.nb, A.ti0, A.ti1, A.ent, A.partial, A.U, A.E, A.F, A.k3, A.ecg,
-                                           A.ecg_ff);
+                                           A.ecg_ff, A.cmov);
     }
     EKG_CUDA(cudaGetLastError());
 }

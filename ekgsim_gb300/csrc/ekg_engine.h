@@ -75,6 +75,13 @@ struct BatchState {
     DBuf<int> work;                        // work counter of the operand kernel
     DBuf<float2> U, Up;                    // [rows][nl][max_ent] steady sums (U0, U1), per K part
     DBuf<float> partial;                   // [items][rows][128] raw accumulators (x2 with two bases)
+    // resting-potential term (k0 differing between layers): per-part unscaled field sums of the
+    // moved rows, the per-row and per-(simulation, static lead) constants, and per heart the
+    // layer sums of the resident lead field (K0s, valid while the band tables are)
+    DBuf<float> P2;                        // [stages * 4][rows_used]
+    DBuf<double> cmov, cst;                // [rows_used], [S][L]
+    DBuf<double> K0s;                      // [nl][L]
+    bool k0s_ok = false;
 };
 // Launch shape of the batched form's moved-lead kernels, chosen by the autotuner (0 / -1 = the
 // built-in choice): the band GEMM's row tile (32, 128 or 256 rows of (simulation, moved lead)),
@@ -92,6 +99,7 @@ struct PassPlan {
     int n_sims = 0, nmove = 0, J = 0, two_bases = 0;
     int rows_used = 0, rows = 0, ntiles = 0, nitems = 0;
     int tile_rows = 0, op_small = 0, op_bps = 0;  // launch shape (see TuneChoice)
+    bool k0 = false;                       // some simulation's k0 differs between layers
     std::vector<double> k3;                // [S][nl]
     std::vector<int4> items;               // band GEMM work items, grouped by tile
     std::vector<int32_t> ti0, ti1;         // [ntt][nl] item range of each (tile, layer)

@@ -279,6 +279,8 @@ struct BandArgs {
     const float *E = nullptr, *F = nullptr, *partial = nullptr;
     const double *k3 = nullptr;
     float2 *P1 = nullptr;            // [stages][rows] steady sums per 32-AP stage
+    float *P2 = nullptr;             // [stages * 4][rows] unscaled field sums per 8-AP part, or null
+    const double *cmov = nullptr;    // [rows'] resting-potential constant of each moved-lead row, or null
     float2 *Up = nullptr;            // [band_u_parts()][rows][nl][max_ent]
     float2 *U = nullptr;             // [rows][nl][max_ent]
     double *ecg = nullptr;
@@ -292,7 +294,7 @@ void launch_reduce_layers(cudaStream_t s, int steps, int rows, int nl, const int
                           const double *partial, float *Q);
 void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int nmove, int n_sims, const float *F,
                            const float *coef, const double *k3, const float *Q1, const float *Q2, double *ecg,
-                           float2 *ecg_ff);
+                           float2 *ecg_ff, const double *cst = nullptr);
 void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, bool small, int blocks_per_sm,
                              const float *k5l,
                              const float4 *hconst, const float4 *lrel, int nmove, int n_sims, const BandArgs &B,
@@ -300,6 +302,15 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, b
 void launch_batch_gemm(cudaStream_t s, const BatchArgs &a);
 int band_u_parts();
 void launch_band_u(cudaStream_t s, const BandArgs &a);
+// Resting-potential term of the batched form where k0 differs between layers:
+//   moved rows   cmov[l * S + s] = sum_L (k0_L - k0_0) sum_{a in L} W_s[l][a]   (from P2)
+//   static leads K0s[L][l] = sum_{a in L} W0[l][a] (per heart), cst[s][l] = sum_L (k0_L - k0_0) K0s[L][l]
+void launch_k0_moved(cudaStream_t s, const BandArgs &a, const int32_t *ls0, const int32_t *ls1,
+                     const double *layer_k, double *cmov);
+void launch_k0_static_sums(cudaStream_t s, int nleads, int64_t apad, int nl, const int32_t *ls0,
+                           const int32_t *ls1, const float *W0, double *K0s);
+void launch_k0_static(cudaStream_t s, int n_sims, int nleads, int nmove, int nl, const double *K0s,
+                      const double *layer_k, double *cst);
 void launch_reduce_band(cudaStream_t s, const BandArgs &a);
 void launch_reduce_ecg(cudaStream_t s, const HeartDev &h, const double *d_partial, const double *d_k0w,
                        int n_sims, double *d_ecg, float2 *d_ecg_ff);

@@ -623,6 +623,7 @@ void build_band(ekg_heart *h, const std::vector<double> &key, const std::vector<
     }
     if (gtab.empty()) gtab.push_back(0.f);
     B.max_ent = max_ent;
+    B.k0s_ok = false;  // the layer stage ranges are rebuilt below
     B.ls0.alloc(nl);
     B.ls1.alloc(nl);
     B.tref.alloc(nst);
@@ -819,9 +820,8 @@ bool tune_cache_read(const std::string &path, const std::string &key, TuneChoice
     return found;
 }
 
-// Decide the pass: the batched (separable) form when the batch shares k1 and k4 per layer, no
-// layer's k0 differs from another's (per simulation), exp(k5 at) has a short Taylor expansion and
-// there are at least two sims.
+// Decide the pass: the batched (separable) form when the batch shares k1 and k4 per layer and
+// exp(k5 at) has a short Taylor expansion (a single simulation once its k1, k4 are settled).
 PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double *leads) {
     PassPlan P;
     P.n_sims = n_sims;
@@ -843,10 +843,11 @@ PassPlan plan_pass(ekg_heart *h, int n_sims, const double *layer_k, const double
     for (int si = 0; si < n_sims; ++si)
         for (int i = 0; i < nl; ++i) {
             const double *k = layer_k + ((size_t)si * nl + i) * 9;
-            // the resting potential k0 leaves sum_L k0_L sum_{a in L} W[l, a], which the batched form
-            // does not add: it vanishes when k0 is the same in every layer, since the AP differences
-            // of the dipoles make sum_a W[l, a] = 0 (simlib/simulator.cpp:509-525)
-            if (k[1] != key[2 * i] || k[4] != key[2 * i + 1] || k[0] != layer_k[(size_t)si * nl * 9]) return P;
+            if (k[1] != key[2 * i] || k[4] != key[2 * i + 1]) return P;
+            // the resting potential k0 leaves sum_L k0_L sum_{a in L} W[l, a], which vanishes when k0
+            // is the same in every layer, since the AP differences of the dipoles make
+            // sum_a W[l, a] = 0 (simlib/simulator.cpp:509-525); otherwise the pass adds it
+            if (k[0] != layer_k[(size_t)si * nl * 9]) P.k0 = true;
             if (k[3] != layer_k[9 * i + 3]) k3_uniform = false;
         }
     // A single simulation takes the batched form once its (k1, k4) is settled: when the basis for it
@@ -1012,6 +1013,15 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
         BatchState &B = h->bs;
         const size_t nc = (size_t)n_sims * D.nlayers * std::max(1, P.J);
         if (h->ev.coef.n < nc) h->ev.coef.alloc(nc);
+        if (P.k0 && P.nmove < (int)D.nleads) {
+            if (B.cst.n < (size_t)n_sims * D.nleads) B.cst.alloc((size_t)n_sims * D.nleads);
+            if (!B.k0s_ok) {
+                // layer sums of the resident lead field, once per band tables (the layer ranges)
+                if (B.K0s.n < (size_t)D.nlayers * D.nleads) B.K0s.alloc((size_t)D.nlayers * D.nleads);
+                launch_k0_static_sums(h->stream, D.nleads, D.apad, D.nlayers, B.ls0.p, B.ls1.p, h->W0.p, B.K0s.p);
+                B.k0s_ok = true;
+            }
+        }
         if (P.nmove > 0) {
             const size_t bt = (size_t)P.rows * D.apad * 4;
             if (B.Bt.n < bt) B.Bt.alloc(bt);
@@ -1019,6 +1029,10 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
             if (B.partial.n < pb) B.partial.alloc(pb);
             const size_t p1 = (size_t)(D.apad / 32) * P.rows_used;
             if (B.P1.n < p1) B.P1.alloc(p1);
+            if (P.k0) {
+                if (B.P2.n < 4 * p1) B.P2.alloc(4 * p1);
+                if (B.cmov.n < (size_t)P.rows_used) B.cmov.alloc(P.rows_used);
+            }
             if (!B.work.p) B.work.alloc(1);
             const size_t ub = (size_t)P.rows_used * D.nlayers * B.max_ent;
             if (B.U.n < ub) {
@@ -1060,7 +1074,7 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
         BatchState &B = h->bs;
         auto static_part = [&]() {
             launch_static_combine(sx, D, P.J, B.J, nmove, n_sims, E.Ff.p, E.coef.p, in.k3, B.Q1.p, B.Q2.p, E.ecg.p,
-                                  E.ecg_ff.p);
+                                  E.ecg_ff.p, P.k0 ? B.cst.p : nullptr);
             launches += nmove < (int)L;
             if (mark_static) {
                 // inside a graph capture the record must be an external event node (the copy stream
@@ -1072,6 +1086,10 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
                                                                                       : cudaEventRecordDefault));
             }
         };
+        if (P.k0 && nmove < (int)L) {
+            launch_k0_static(sx, n_sims, (int)L, nmove, D.nlayers, B.K0s.p, in.layer_k, B.cst.p);
+            ++launches;
+        }
         static_part();
         if (nmove > 0) {
             if (P.rows_used < P.rows) EKG_CUDA(cudaMemsetAsync(B.Bt.p, 0, (size_t)P.rows * D.apad * 4, s));
@@ -1102,6 +1120,8 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             U.k3 = in.k3;
             U.partial = B.partial.p;
             U.P1 = B.P1.p;
+            U.P2 = P.k0 ? B.P2.p : nullptr;
+            U.cmov = P.k0 ? B.cmov.p : nullptr;
             U.U = B.U.p;
             U.Up = B.Up.p;
             U.ecg = E.ecg.p;
@@ -1115,6 +1135,10 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
                 EKG_CUDA(cudaStreamWaitEvent(sx, h->ev_op, 0));
             }
             launch_band_u(sx, U);
+            if (P.k0) {
+                launch_k0_moved(sx, U, B.ls0.p, B.ls1.p, in.layer_k, B.cmov.p);
+                ++launches;
+            }
             if (fork) EKG_CUDA(cudaEventRecord(h->ev_join, sx));
             launches += 2;
             if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[1], s));
@@ -1201,7 +1225,7 @@ std::vector<uint64_t> pass_signature(const ekg_heart *h, const PassPlan &P, int 
                                (uint64_t)P.nitems, (uint64_t)ncl, (uint64_t)mode, (uint64_t)mark_static,
                                (uint64_t)h->cpre_on, (uint64_t)h->any_k0, (uint64_t)h->eng->contract, (uint64_t)B.J,
                                (uint64_t)B.max_ent, (uint64_t)B.ntt, (uint64_t)P.tile_rows, (uint64_t)P.op_small,
-                               (uint64_t)P.op_bps};
+                               (uint64_t)P.op_bps, (uint64_t)P.k0};
     const ekg_heart::PassInputs &in = h->in();
     for (const void *p : {(const void *)in.layer_k, (const void *)in.cpre, (const void *)in.leads, (const void *)in.k3,
                           (const void *)B.d_centre.p, (const void *)B.d_scale.p, (const void *)E.coef.p,
@@ -1216,7 +1240,8 @@ std::vector<uint64_t> pass_signature(const ekg_heart *h, const PassPlan &P, int 
                           (const void *)B.Up.p, (const void *)B.partial.p,
                           (const void *)B.tref.p, (const void *)B.stage_order.p, (const void *)B.nent.p, (const void *)B.esplit.p, (const void *)B.ls0.p,
                           (const void *)B.ls1.p, (const void *)B.ent.p, (const void *)B.goff.p, (const void *)B.gtab.p,
-                          (const void *)B.E.p, (const void *)B.work.p, (const void *)h->W0.p})
+                          (const void *)B.E.p, (const void *)B.work.p, (const void *)h->W0.p, (const void *)B.P2.p,
+                          (const void *)B.cmov.p, (const void *)B.cst.p, (const void *)B.K0s.p})
         v.push_back(u(p));
     return v;
 }

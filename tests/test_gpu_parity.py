@@ -804,10 +804,13 @@ def test_activation_edge_shapes(case):
         e.close()
 
 
-def test_batched_form_uniform_resting_potential(engine):
-    """A resting potential k0 that is the same in every layer (-86 mV here) cancels in the dipoles
-    (sum_a W[l, a] = 0), so the batched form takes such batches; with k0 differing between layers
-    the batch takes the per-simulation form, which adds the constant term.  Both match the oracle."""
+def test_batched_form_resting_potential(engine):
+    """The resting potential k0 leaves sum_L k0_L sum_{a in L} W[l, a] on every sample.  With k0 the
+    same in every layer (-86 mV) it cancels in the dipoles (sum_a W[l, a] = 0); with k0 differing
+    between layers the batched form adds it, for the static leads (layer sums of the resident lead
+    field) and for the moved ones (per-part field sums written by the operand kernel).  Both batches
+    take the batched form and match the oracle and single evaluations, with two of four leads moved
+    (the static and moved terms, on two streams) and with all four moved (one stream)."""
     from ekgsim_gb300.engine import Heart
     spec = synth.small_spec(40, n_leads=4, seed=29)
     steps = 300
@@ -818,25 +821,31 @@ def test_batched_form_uniform_resting_potential(engine):
     target = [t for t in synth.analytic_target(spec.n_leads, steps, 6)]
     at, layer = O.activation(grid, tm)
     genes = np.stack([synth.genes_for(spec, 80 + r, 0) for r in range(12)])
+    genes_all = genes.copy()
+    genes_all[:, 16:] = np.random.Generator(np.random.PCG64(83)).uniform(-30.0, 30.0, size=(12, 4))
     for k0s in ((-86.0, -86.0, -86.0), (-86.0, -80.0, -90.0)):
         base = [[k0] + list(synth.BASE_AP[1:]) for k0 in k0s]
         kmin, kmax = list(synth.K_MIN), list(synth.K_MAX)
         kmin[0], kmax[0] = min(k0s), max(k0s)
         h.set_eval(base, kmin, kmax, [5, 6, 7, 8], target, mid_position=0.6)
-        _, _, ecg_b = h.eval_batch(genes, want_ecg=True)
-        lks = np.stack([O.layer_aps(3, np.array(base), np.array(kmin), np.array(kmax), [5, 6, 7, 8], "endo-mid-epi",
-                                    0.6, g[:12])[0] for g in genes])
-        moveds = np.stack([O.move_leads(leads, g[12:].reshape(-1, 2)) for g in genes])
-        assert h.benchmark(lks, moveds, warmup=1, iters=1)["batched"] == (len(set(k0s)) == 1)
-        for i in (0, 11):
-            g = genes[i]
-            lk = O.layer_aps(3, np.array(base), np.array(kmin), np.array(kmax), [5, 6, 7, 8], "endo-mid-epi", 0.6,
-                             g[:12])[0]
-            # the mid layer takes the last base AP's k0 (sim.cpp:856), so the layers get -86, -90, -90
-            assert (len(set(lk[:, 0])) == 1) == (len(set(k0s)) == 1)
-            moved = O.move_leads(leads, g[12:].reshape(-1, 2))
-            ref = O.run(layer, at, lk, moved, "3D4", 0.0, float(steps), 1.0)
-            assert rel_l2(ecg_b[i], ref) <= ECG_TOL, (k0s, i)
+        for gs in (genes, genes_all):
+            crit_b, viol_b, ecg_b = h.eval_batch(gs, want_ecg=True)
+            lks = np.stack([O.layer_aps(3, np.array(base), np.array(kmin), np.array(kmax), [5, 6, 7, 8],
+                                        "endo-mid-epi", 0.6, g[:12])[0] for g in gs])
+            moveds = np.stack([O.move_leads(leads, g[12:].reshape(-1, 2)) for g in gs])
+            assert h.benchmark(lks, moveds, warmup=1, iters=1)["batched"]
+            for i in (0, 11):
+                g = gs[i]
+                lk = lks[i]
+                # the mid layer takes the last base AP's k0 (sim.cpp:856), so the layers get -86, -90, -90
+                assert (len(set(lk[:, 0])) == 1) == (len(set(k0s)) == 1)
+                ref = O.run(layer, at, lk, moveds[i], "3D4", 0.0, float(steps), 1.0)
+                assert rel_l2(ecg_b[i], ref) <= ECG_TOL, (k0s, i)
+            # every simulation against its single evaluation
+            for i in range(len(gs)):
+                c1, v1, e1 = h.eval_batch(gs[i:i + 1], want_ecg=True)
+                assert rel_l2(ecg_b[i], e1[0]) <= ECG_TOL, (k0s, i)
+                assert np.allclose(crit_b[i], c1[0], rtol=0, atol=1e-4) and viol_b[i] == v1[0]
     h.close()
 
 
