@@ -1130,8 +1130,9 @@ void launch_static_combine(cudaStream_t s, const HeartDev &h, int J, int Jb, int
 // [0, nmove)) are evaluated in pairs that share the voxel loads, with the same field evaluation as
 // the batched form's operand kernel (closed form for interior voxels and for boundary voxels with
 // few absent neighbours where the leads are at least 20 cells away, exact sums otherwise); their
-// W is written for the k0 term and W' = W exp(k5_L at_a) for the contraction.  Leads at their
-// loaded position take the resident field W0, scaled the same way.  Lead positions are FP64
+// W is written for the k0 term and W' = W exp(k5_L at_a) for the contraction.  With static_rows the
+// leads at their loaded position take the resident field W0, scaled the same way (for the dense
+// contractions; the band contraction scales W0 itself).  Lead positions are FP64
 // [S][lead_stride][3] (z, y, x), made relative to the voxel centre in FP64 before the FP32 cast.
 template <bool DIAG>
 __global__ void __launch_bounds__(128) k_sim_lead_field(
@@ -1139,7 +1140,7 @@ __global__ void __launch_bounds__(128) k_sim_lead_field(
     const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs, const double *__restrict__ at,
     const int32_t *__restrict__ a_layer, const double *__restrict__ layer_k, int nl, const double *__restrict__ leads,
     int lead_stride, double cz, double cy, double cx, int nmove, int nleads, const float *__restrict__ W0,
-    float *__restrict__ W, float *__restrict__ Wp) {
+    float *__restrict__ W, float *__restrict__ Wp, int static_rows) {
     __shared__ float s_d[26 * 4];
     const int tid = threadIdx.x;
     if (tid < nnb) {
@@ -1190,14 +1191,123 @@ __global__ void __launch_bounds__(128) k_sim_lead_field(
             if (q >= np) break;
             const size_t o = ((size_t)s * nleads + l0 + q) * apad + a;
             W[o] = acc[q];
-            Wp[o] = acc[q] * f;
+            if (Wp) Wp[o] = acc[q] * f;
         }
     }
-    for (int l = nmove; l < nleads; ++l) Wp[((size_t)s * nleads + l) * apad + a] = W0[(size_t)l * apad + a] * f;
+    if (static_rows)
+        for (int l = nmove; l < nleads; ++l) Wp[((size_t)s * nleads + l) * apad + a] = W0[(size_t)l * apad + a] * f;
+}
+
+// Per-simulation form with many simulations: the moved rows' unscaled field W[s][l][a] (FP32) with
+// the batched operand kernel's work split -- items (32-AP stage, group of LF_THREADS * LF_ROWS
+// rows) taken from a counter, stages with the most voxels first, a stage's voxel records staged in
+// shared memory, LF_ROWS rows per thread sharing each voxel's loads and tests, the stage bounding-box
+// test -- instead of one thread per (AP, simulation), whose warps diverge over the APs' voxel
+// counts.  Row = s * nmove + l; lead positions FP64 [S][lead_stride][3] made relative to the voxel
+// centre in FP64 before the FP32 cast.  The band contraction scales W by exp(k5 at).
+template <bool DIAG>
+__global__ void __launch_bounds__(LF_THREADS, 8) k_sim_lead_field_rows(
+    int nst, int ngr, int *__restrict__ work, InteriorField ic, const int64_t *__restrict__ a_vox_begin,
+    const float4 *__restrict__ vox_pos, const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs,
+    const double *__restrict__ leads, int lead_stride, double cz, double cy, double cx, int nmove, int n_sims,
+    int nleads, int64_t apad, const int32_t *__restrict__ stage_order, const float4 *__restrict__ stage_box,
+    float *__restrict__ W) {
+    __shared__ float s_d[26 * 4];
+    __shared__ float s_w[LF_ROWS][8][LF_THREADS];
+    __shared__ int s_vb[BST / 8 + 1];
+    __shared__ float4 s_vpos[LF_VCAP], s_vout[LF_VCAP];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    if (tid < nnb) {
+        const float dz = difs[3 * tid], dy = difs[3 * tid + 1], dx = difs[3 * tid + 2];
+        s_d[4 * tid] = dz;
+        s_d[4 * tid + 1] = dy;
+        s_d[4 * tid + 2] = dx;
+        s_d[4 * tid + 3] = dz * dz + dy * dy + dx * dx;
+    }
+    const int rows_used = n_sims * nmove;
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_item = atomicAdd(work, 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= nst * ngr) break;
+        const int st = stage_order[item / ngr];
+        const int v0 = (int)a_vox_begin[(int64_t)st * BST], nv = (int)a_vox_begin[(int64_t)(st + 1) * BST] - v0;
+        const bool staged = nv <= LF_VCAP;
+        if (staged)
+            for (int i = tid; i < nv; i += LF_THREADS) {
+                s_vpos[i] = vox_pos[v0 + i];
+                s_vout[i] = vox_out[v0 + i];
+            }
+        if (tid < BST / 8 + 1) s_vb[tid] = (int)a_vox_begin[(int64_t)st * BST + tid * 8] - (staged ? v0 : 0);
+        __syncthreads();
+        const float4 *vp = staged ? s_vpos : vox_pos, *vo = staged ? s_vout : vox_out;
+        const int rb = (item % ngr) * (LF_THREADS * LF_ROWS) + tid * LF_ROWS;
+        const int nr = rb < rows_used ? min(LF_ROWS, rows_used - rb) : 0;  // the rest repeat the last row
+        float4 r[LF_ROWS];
+        bool far_all = true;
+        if (nr > 0) {
+            const float4 lo = stage_box[2 * (size_t)st], hi = stage_box[2 * (size_t)st + 1];
+#pragma unroll
+            for (int q = 0; q < LF_ROWS; ++q) {
+                const int row = rb + min(q, nr - 1);
+                const double *p = leads + ((size_t)(row / nmove) * lead_stride + row % nmove) * 3;
+                r[q] = make_float4((float)(p[0] - cz), (float)(p[1] - cy), (float)(p[2] - cx), 0.f);
+                const float dz = fmaxf(fmaxf(lo.x - r[q].x, r[q].x - hi.x), 0.f);
+                const float dy = fmaxf(fmaxf(lo.y - r[q].y, r[q].y - hi.y), 0.f);
+                const float dx = fmaxf(fmaxf(lo.z - r[q].z, r[q].z - hi.z), 0.f);
+                far_all = far_all && dz * dz + dy * dy + dx * dx >= INTERIOR_S_MIN + 41.f;
+            }
+        }
+        far_all = __all_sync(0xffffffffu, far_all);
+        if (nr == 0) continue;
+#pragma unroll 1
+        for (int kc = 0; kc < BST / 8; ++kc) {
+            if (far_all) chunk_w<DIAG, LF_ROWS, true>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
+            else chunk_w<DIAG, LF_ROWS, false>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
+#pragma unroll
+            for (int q = 0; q < LF_ROWS; ++q) {
+                if (q >= nr) break;
+                const int row = rb + q;
+                float4 *dst = reinterpret_cast<float4 *>(W + ((size_t)(row / nmove) * nleads + row % nmove) * apad +
+                                                         (size_t)st * BST + kc * 8);
+                dst[0] = make_float4(s_w[q][0][tid], s_w[q][1][tid], s_w[q][2][tid], s_w[q][3][tid]);
+                dst[1] = make_float4(s_w[q][4][tid], s_w[q][5][tid], s_w[q][6][tid], s_w[q][7][tid]);
+            }
+        }
+    }
+}
+
+void launch_sim_lead_field_rows(cudaStream_t s, const HeartDev &h, const double *d_leads, int nmove, int lead_stride,
+                                int n_sims, float *W, int *work, int sm_count) {
+    InteriorField ic;
+    ic.A0 = h.interior_c[0];
+    ic.A1 = h.interior_c[1];
+    ic.B0 = h.interior_c[2];
+    ic.B1 = h.interior_c[3];
+    ic.B2 = h.interior_c[4];
+    const int rows_used = n_sims * nmove;
+    const int ngr = (rows_used + LF_THREADS * LF_ROWS - 1) / (LF_THREADS * LF_ROWS);
+    const int nst = (int)(h.apad / BST);
+    const int items = nst * ngr;
+    const int grid = std::max(1, std::min(items, sm_count * 8));
+    EKG_CUDA(cudaMemsetAsync(work, 0, sizeof(int), s));
+    if (h.nhood == EKG_NHOOD_3D4)
+        k_sim_lead_field_rows<true><<<grid, LF_THREADS, 0, s>>>(
+            nst, ngr, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, d_leads, lead_stride,
+            h.centre[0], h.centre[1], h.centre[2], nmove, n_sims, h.nleads, h.apad, h.stage_order.p, h.stage_box.p, W);
+    else
+        k_sim_lead_field_rows<false><<<grid, LF_THREADS, 0, s>>>(
+            nst, ngr, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, d_leads, lead_stride,
+            h.centre[0], h.centre[1], h.centre[2], nmove, n_sims, h.nleads, h.apad, h.stage_order.p, h.stage_box.p, W);
+    EKG_CUDA(cudaGetLastError());
 }
 
 void launch_sim_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads, int nmove, int lead_stride,
-                           int n_sims, const double *d_layer_k, const float *W0, float *W, float *Wp) {
+                           int n_sims, const double *d_layer_k, const float *W0, float *W, float *Wp,
+                           bool static_rows) {
+    if (nmove == 0 && !static_rows) return;
     InteriorField ic;
     ic.A0 = h.interior_c[0];
     ic.A1 = h.interior_c[1];
@@ -1208,11 +1318,13 @@ void launch_sim_lead_field(cudaStream_t s, const HeartDev &h, const double *d_le
     if (h.nhood == EKG_NHOOD_3D4)
         k_sim_lead_field<true><<<g, 128, 0, s>>>(h.apad, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p,
                                                  h.at.p, h.a_layer.p, d_layer_k, h.nlayers, d_leads, lead_stride,
-                                                 h.centre[0], h.centre[1], h.centre[2], nmove, h.nleads, W0, W, Wp);
+                                                 h.centre[0], h.centre[1], h.centre[2], nmove, h.nleads, W0, W, Wp,
+                                                 static_rows ? 1 : 0);
     else
         k_sim_lead_field<false><<<g, 128, 0, s>>>(h.apad, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p,
                                                   h.at.p, h.a_layer.p, d_layer_k, h.nlayers, d_leads, lead_stride,
-                                                  h.centre[0], h.centre[1], h.centre[2], nmove, h.nleads, W0, W, Wp);
+                                                  h.centre[0], h.centre[1], h.centre[2], nmove, h.nleads, W0, W, Wp,
+                                                 static_rows ? 1 : 0);
     EKG_CUDA(cudaGetLastError());
 }
 
@@ -1248,7 +1360,7 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, b
         const int grid = std::max(1, std::min(nst * ngr, bps * sm_count));                                       \
         k_batch_lead_field<NN, DG><<<grid, LF_THREADS, 0, s>>>(                                                   \
             nst, ngr, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p, \
-            k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, B.stage_order, h.stage_box.p,  \
+            k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, h.stage_order.p, h.stage_box.p,  \
             Bt, B.P1, B.P2);                                                                                      \
     } while (0)
     switch (tile_rows) {
@@ -1322,14 +1434,15 @@ __global__ void k_k0_static_sums(int nleads, int64_t apad, const int32_t *__rest
     }
 }
 
-// cst[s][l] = sum_L (k0_L - k0_0) K0s[L][l] for the static leads l >= nmove.
+// cst[s][l] = sum_L (k0_L - k0_0) K0s[L][l] for the static leads l >= nmove (relative: the batched
+// form, whose other terms carry no k0), or sum_L k0_L K0s[L][l] (the per-simulation form's k0w).
 __global__ void k_k0_static(int n_sims, int nleads, int nmove, int nl, const double *__restrict__ K0s,
-                            const double *__restrict__ layer_k, double *__restrict__ cst) {
+                            const double *__restrict__ layer_k, double *__restrict__ cst, int relative) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_sims * nleads) return;
     const int s = i / nleads, l = i % nleads;
     if (l < nmove) return;
-    const double k00 = layer_k[(size_t)s * nl * 9];
+    const double k00 = relative ? layer_k[(size_t)s * nl * 9] : 0.0;
     double c = 0.0;
     for (int L = 0; L < nl; ++L) c += (layer_k[((size_t)s * nl + L) * 9] - k00) * K0s[(size_t)L * nleads + l];
     cst[i] = c;
@@ -1349,9 +1462,35 @@ void launch_k0_static_sums(cudaStream_t s, int nleads, int64_t apad, int nl, con
 }
 
 void launch_k0_static(cudaStream_t s, int n_sims, int nleads, int nmove, int nl, const double *K0s,
-                      const double *layer_k, double *cst) {
+                      const double *layer_k, double *cst, bool relative) {
     const int n = n_sims * nleads;
-    k_k0_static<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n_sims, nleads, nmove, nl, K0s, layer_k, cst);
+    k_k0_static<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n_sims, nleads, nmove, nl, K0s, layer_k, cst,
+                                                            relative ? 1 : 0);
+    EKG_CUDA(cudaGetLastError());
+}
+
+// out[L][l] = sum_{a: a_layer[a] == L} W0[l][a] in FP64, block per (lead, layer); padding APs hold
+// no voxels (W0 = 0).
+__global__ void k_w0_layer_sums(int64_t apad, int nleads, const float *__restrict__ W0,
+                                const int32_t *__restrict__ a_layer, double *__restrict__ out) {
+    __shared__ double red[8];
+    const int l = blockIdx.x, L = blockIdx.y;
+    double v = 0.0;
+    for (int64_t a = threadIdx.x; a < apad; a += blockDim.x)
+        if (a_layer[a] == L) v += (double)W0[(size_t)l * apad + a];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        out[(size_t)L * nleads + l] = t;
+    }
+}
+
+void launch_w0_layer_sums(cudaStream_t s, const HeartDev &h, const float *W0, double *out) {
+    k_w0_layer_sums<<<dim3((unsigned)h.nleads, (unsigned)h.nlayers), 256, 0, s>>>(h.apad, h.nleads, W0, h.a_layer.p,
+                                                                                  out);
     EKG_CUDA(cudaGetLastError());
 }
 

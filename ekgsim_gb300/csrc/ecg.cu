@@ -15,6 +15,7 @@
 // so the device evaluates H on the fly, folds exp(k5 at) into the lead field (W' = W exp(k5 at)),
 // and applies F_L in FP64 to each layer's partial sums.  k0 cancels inside every AP difference of
 // one layer; across layers it leaves the constant sum_L k0_L sum_{a in L} W[l,a].
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 
@@ -221,20 +222,22 @@ __global__ void __launch_bounds__(CC_T) k_contract_cuda(int steps, int nleads, i
 //           S0[l] = sum_a W'[l,a] 2^(-k4' (amax - at_a)), S1[l] = sum_a W'[l,a]  (k4' = k4 log2 e);
 //   band    the steps in between (the chunk's upstrokes, some 10 to 30 steps of 1 ms):
 //           P[t,l] = sum_a W'[l,a] H_a(t) evaluated directly in FP32, 32 (or 16) steps per pass.
-// APs with an infinite activation time (unreached cells, padding) contribute nothing.  Writes
-// partial[s][c][l][t] = P[t,l] F_L(t) in FP64 for every step, like the other contractions.
+// APs with an infinite activation time (unreached cells, padding) contribute nothing.  The block
+// writes only what the runs need: band[s][c][l][t] = P[t,l] (FP32) for the band steps,
+// csum[s][c][l] = (S0, S1) when the steady run is not empty, and cinfo[s][c] = (tb0, tb1, amax)
+// (first band step, first steady step, the FP32 bits of amax); k_reduce_chunks rebuilds the runs.
+// W'[l][a] = W[l][a] exp(k5 at_a) is formed here (the FP32 operations of the lead-field kernel's
+// W'), with W the moved rows' field Wm [S][L][apad] for l < wrows and the resident field
+// W0 [L][apad] for the others.
 constexpr int CB_THREADS = 256, CB_LB = 16, CB_CAP = CONTRACT_BAND_CAP;
 constexpr size_t CB_SMEM = (size_t)CB_CAP * CB_LB * 4 + (size_t)CB_CAP * 8 + (size_t)CB_THREADS * (CB_LB + 1) * 4;
-__global__ void __launch_bounds__(CB_THREADS, 4) k_contract_band(int steps, int nleads, int64_t apad, int nl,
-                                                             const float2 *__restrict__ t_hilo,
-                                                             const float2 *__restrict__ at_hilo,
-                                                             const int32_t *__restrict__ chunk_a0,
-                                                             const int32_t *__restrict__ chunk_a1,
-                                                             const int32_t *__restrict__ chunk_layer,
-                                                             const float *__restrict__ Wp,
-                                                             const float *__restrict__ layer_c,
-                                                             const double *__restrict__ F, int nchunks, int nlb,
-                                                             double *__restrict__ partial) {
+template <int NLB>
+__global__ void __launch_bounds__(CB_THREADS, 4) k_contract_band(
+    int steps, int nleads, int64_t apad, int nl, const float2 *__restrict__ t_hilo, const float2 *__restrict__ at_hilo,
+    const double *__restrict__ at, const int32_t *__restrict__ chunk_a0, const int32_t *__restrict__ chunk_a1,
+    const int32_t *__restrict__ chunk_layer, const float *__restrict__ Wm, int wrows, const float *__restrict__ W0,
+    const double *__restrict__ layer_k, const float *__restrict__ layer_c, int nchunks, int nlb,
+    float *__restrict__ band, float2 *__restrict__ csum, int4 *__restrict__ cinfo) {
     extern __shared__ __align__(16) uint8_t cb_smem[];
     float(*s_w)[CB_LB] = reinterpret_cast<float(*)[CB_LB]>(cb_smem);  // W'[a][l] of the chunk
     float2 *s_at = reinterpret_cast<float2 *>(cb_smem + (size_t)CB_CAP * CB_LB * 4);
@@ -248,21 +251,27 @@ __global__ void __launch_bounds__(CB_THREADS, 4) k_contract_band(int steps, int 
     const int a0 = chunk_a0[c], na = chunk_a1[c] - a0, L = chunk_layer[c];
     const int l0 = lb * CB_LB, nlh = min(CB_LB, nleads - l0);
     const float4 kc = reinterpret_cast<const float4 *>(layer_c)[(size_t)s * nl + L];
-    double *out = partial + ((size_t)s * nchunks + c) * nleads * (size_t)steps + (size_t)l0 * steps;
-    const double *Fl = F + ((size_t)s * nl + L) * steps;
+    float *out = band + ((size_t)s * nchunks + c) * nleads * (size_t)steps + (size_t)l0 * steps;
+    const double k5 = layer_k[((size_t)s * nl + L) * 9 + 5];
 
     // the chunk: activation times, W' transposed to [a][l], the extreme finite activation times
     float amin = INFINITY, amax = -INFINITY;
     for (int i = tid; i < na; i += CB_THREADS) {
-        const float2 at = at_hilo[a0 + i];
-        s_at[i] = at;
-        if (isfinite(at.x)) {
-            amin = fminf(amin, at.x);
-            amax = fmaxf(amax, at.x);
+        const float2 a2 = at_hilo[a0 + i];
+        s_at[i] = a2;
+        if (isfinite(a2.x)) {
+            amin = fminf(amin, a2.x);
+            amax = fmaxf(amax, a2.x);
         }
+        const double ad = at[a0 + i];
+        const float f = isinf(ad) ? 0.f : expf((float)(k5 * ad));
         float w[CB_LB];
 #pragma unroll
-        for (int l = 0; l < CB_LB; ++l) w[l] = l < nlh ? Wp[((size_t)s * nleads + l0 + l) * apad + a0 + i] : 0.f;
+        for (int l = 0; l < CB_LB; ++l) {
+            const int lg = l0 + l;
+            w[l] = l >= nlh ? 0.f
+                            : (lg < wrows ? Wm[((size_t)s * nleads + lg) * apad + a0 + i] : W0[(size_t)lg * apad + a0 + i]) * f;
+        }
 #pragma unroll
         for (int l = 0; l < CB_LB; l += 4)
             *reinterpret_cast<float4 *>(&s_w[i][l]) = make_float4(w[l], w[l + 1], w[l + 2], w[l + 3]);
@@ -298,22 +307,20 @@ __global__ void __launch_bounds__(CB_THREADS, 4) k_contract_band(int steps, int 
     }
     if (!any_finite) nzero = steps;
     const int tb0 = nzero, tb1 = steps - nsteady;  // band steps [tb0, tb1)
-
-    for (int t = tid; t < nzero; t += CB_THREADS)
-        for (int l = 0; l < nlh; ++l) out[(size_t)l * steps + t] = 0.0;
+    if (lb == 0 && tid == 0) cinfo[(size_t)s * nchunks + c] = make_int4(tb0, tb1, __float_as_int(amax), 0);
 
     if (nsteady > 0) {
         // S0, S1 per lead: each thread its APs, then a shuffle and a shared-memory reduction (eight
         // leads at a time, which keeps the accumulators in registers)
 #pragma unroll 1
-        for (int lh = 0; lh < CB_LB; lh += 8) {
+        for (int lh = 0; lh < NLB; lh += 8) {
             float u0[8], u1[8];
 #pragma unroll
             for (int l = 0; l < 8; ++l) u0[l] = u1[l] = 0.f;
             for (int i = tid; i < na; i += CB_THREADS) {
-                const float2 at = s_at[i];
-                if (!isfinite(at.x)) continue;
-                const float g = ex2_approx(-kc.y * ((amax - at.x) - at.y));
+                const float2 a2 = s_at[i];
+                if (!isfinite(a2.x)) continue;
+                const float g = ex2_approx(-kc.y * ((amax - a2.x) - a2.y));
 #pragma unroll
                 for (int l = 0; l < 8; ++l) {
                     const float w = s_w[i][lh + l];
@@ -344,50 +351,167 @@ __global__ void __launch_bounds__(CB_THREADS, 4) k_contract_band(int steps, int 
             s_sum[k][l] = v;
         }
         __syncthreads();
-        // thread per step: the step's factor once, then every lead (coalesced over the steps)
-        for (int t = tb1 + tid; t < steps; t += CB_THREADS) {
-            const float2 th = t_hilo[t];
-            const float e = kc.z * ex2_approx(-kc.y * ((th.x - amax) + th.y));
-            const double f = Fl[t];
-            for (int l = 0; l < nlh; ++l)
-                out[(size_t)l * steps + t] = (double)fmaf(e, s_sum[0][l], kc.w * s_sum[1][l]) * f;
-        }
+        if (tid < nlh) csum[((size_t)s * nchunks + c) * nleads + l0 + tid] = make_float2(s_sum[0][tid], s_sum[1][tid]);
     }
 
-    // band: passes of 32 steps (16 when at most 16 remain), lane = step.  The chunk's APs are dealt
-    // round-robin to 256 / rows slices (slice j takes APs j, j + nsl, ...): in 32-step passes a
-    // warp is one slice (broadcast reads of s_w), in 16-step passes its two slices read
-    // neighbouring rows (no bank conflict).
+    // band: passes of 32, 16 or 8 steps (the fewest steps that cover the run), lane = step.  The
+    // chunk's APs are dealt round-robin to 256 / rows slices (slice j takes APs j, j + nsl, ...);
+    // the 8 lanes of a quarter warp share one slice, so the W' reads are broadcasts.
+    // With T the chunk's first (smallest) activation time the two exponentials separate,
+    //     2^(-k' (t - at)) = 2^(-k' (t - T)) 2^(k' (at - T)),
+    // one factor per step and one per AP (replacing the AP time in shared memory), which leaves one
+    // SFU operation (the sigmoid's reciprocal) per (AP, step).  Taken while the per-AP factors stay
+    // below 2^64: the band steps end within 26.5 / k1' of amax, so the per-step factors stay above
+    // 2^-100 (no underflow) and the exponents' rounding stays that of the direct form's.
+    if (tb0 >= tb1) return;
+    const float2 T = s_at[0];
+    const bool sep = classify && kc.x * (amax - T.x) < 64.f && kc.y * (amax - T.x) < 64.f;
+    float2 *s_g = s_at;
+    if (sep) {
+        __syncthreads();  // every read of s_at above is done
+        for (int i = tid; i < na; i += CB_THREADS) {
+            const float2 a2 = s_at[i];
+            float2 g = make_float2(INFINITY, 0.f);  // H = 0 (no activation)
+            if (isfinite(a2.x)) {
+                const float d = (a2.x - T.x) + (a2.y - T.y);
+                g = make_float2(ex2_approx(kc.x * d), ex2_approx(kc.y * d));
+            }
+            s_g[i] = g;
+        }
+        __syncthreads();
+    }
     for (int tb = tb0; tb < tb1;) {
-        const int rows = tb1 - tb <= 16 ? 16 : 32;
+        const int rem = tb1 - tb;
+        const int rows = rem > 24 ? 32 : (rem > 8 ? 16 : 8);
         const int nsl = CB_THREADS / rows, r = lane & (rows - 1), sl = warp * (32 / rows) + lane / rows;
         const float2 th = t_hilo[min(tb + r, steps - 1)];
-        float acc[CB_LB];
+        float acc[NLB];
 #pragma unroll
-        for (int l = 0; l < CB_LB; ++l) acc[l] = 0.f;
-        for (int i = sl; i < na; i += nsl) {
-            const float2 at = s_at[i];
-            const float h = h_value(((th.x - at.x) + (th.y - at.y)), kc);
+        for (int l = 0; l < NLB; ++l) acc[l] = 0.f;
+        if (sep) {
+            const float d = (th.x - T.x) + (th.y - T.y);
+            const float E1 = ex2_approx(-kc.x * d), E4 = ex2_approx(-kc.y * d);
+            for (int i = sl; i < na; i += nsl) {
+                const float2 g = s_g[i];
+                const float sg = rcp_approx(fmaf(E1, g.x, 1.0f));
+                const float hv = sg * fmaf(kc.z, E4 * g.y, kc.w);
+                const float h = sg == 0.f ? 0.f : hv;
 #pragma unroll
-            for (int l = 0; l < CB_LB; l += 4) {
-                const float4 w = *reinterpret_cast<const float4 *>(&s_w[i][l]);
-                acc[l] = fmaf(w.x, h, acc[l]);
-                acc[l + 1] = fmaf(w.y, h, acc[l + 1]);
-                acc[l + 2] = fmaf(w.z, h, acc[l + 2]);
-                acc[l + 3] = fmaf(w.w, h, acc[l + 3]);
+                for (int l = 0; l < NLB; l += 4) {
+                    const float4 w = *reinterpret_cast<const float4 *>(&s_w[i][l]);
+                    acc[l] = fmaf(w.x, h, acc[l]);
+                    acc[l + 1] = fmaf(w.y, h, acc[l + 1]);
+                    acc[l + 2] = fmaf(w.z, h, acc[l + 2]);
+                    acc[l + 3] = fmaf(w.w, h, acc[l + 3]);
+                }
+            }
+        } else {
+            for (int i = sl; i < na; i += nsl) {
+                const float2 a2 = s_at[i];
+                const float h = h_value(((th.x - a2.x) + (th.y - a2.y)), kc);
+#pragma unroll
+                for (int l = 0; l < NLB; l += 4) {
+                    const float4 w = *reinterpret_cast<const float4 *>(&s_w[i][l]);
+                    acc[l] = fmaf(w.x, h, acc[l]);
+                    acc[l + 1] = fmaf(w.y, h, acc[l + 1]);
+                    acc[l + 2] = fmaf(w.z, h, acc[l + 2]);
+                    acc[l + 3] = fmaf(w.w, h, acc[l + 3]);
+                }
             }
         }
 #pragma unroll
-        for (int l = 0; l < CB_LB; ++l) s_red[sl * rows + r][l] = acc[l];
+        for (int l = 0; l < NLB; ++l) s_red[sl * rows + r][l] = acc[l];
         __syncthreads();
-        for (int i = tid; i < rows * CB_LB; i += CB_THREADS) {
+        for (int i = tid; i < rows * NLB; i += CB_THREADS) {
             const int l = i / rows, rr = i % rows, t = tb + rr;
             float v = 0.f;
             for (int w = 0; w < nsl; ++w) v += s_red[w * rows + rr][l];
-            if (t < tb1 && l < nlh) out[(size_t)l * steps + t] = (double)v * Fl[t];
+            if (t < tb1 && l < nlh) out[(size_t)l * steps + t] = v;
         }
         __syncthreads();
         tb += rows;
+    }
+}
+
+// ecg[s][l][t] = k0w[s][l] + sum_L F_L(t) sum_{c in L} P_c[l][t] from the band contraction's
+// compact outputs: warp per (simulation, lead, 32 steps), lane = step.  Within a layer the APs
+// ascend in activation time, so the chunks' tb0 and tb1 ascend with the chunk index.  Per layer:
+//   - the chunks steady over the whole tile (tb1 <= t0, a prefix of the layer's chunks) are
+//     summed once for the tile, lanes over chunks then a fixed-order tree,
+//         A = sum_c 2^(-k4'(t0 - amax_c)) S0_c,   B = sum_c S1_c,
+//     and enter step t as (1 - k3) 2^(-k4'(t - t0)) A + k3 B;
+//   - the following chunks are taken per step (band value, steady formula or zero) up to the
+//     first one whose zero run covers the tile (every later chunk's does too).
+// The layer's sum is float-float, times F_L(t) in FP64; the chunk order is fixed, so the result
+// does not depend on scheduling.  Also writes the float-float copy.
+__global__ void __launch_bounds__(512) k_reduce_chunks(
+    int steps, int nleads, int nl, int nchunks, const int32_t *__restrict__ layer_c0, const int32_t *__restrict__ layer_c1,
+    const float2 *__restrict__ t_hilo, const float *__restrict__ layer_c, const double *__restrict__ F,
+    const float *__restrict__ band, const float2 *__restrict__ csum, const int4 *__restrict__ cinfo,
+    const double *__restrict__ k0w, double *__restrict__ ecg, float2 *__restrict__ ecg_ff) {
+    const int lane = threadIdx.x & 31;
+    const int l = blockIdx.z * 16 + (threadIdx.x >> 5), s = blockIdx.y;
+    const int t0 = blockIdx.x * 32, t = t0 + lane;
+    if (l >= nleads) return;  // warps are independent: no block-wide barrier below
+    const bool valid = t < steps;
+    const float2 th0 = t_hilo[t0], th = t_hilo[valid ? t : steps - 1];
+    const int4 *ci = cinfo + (size_t)s * nchunks;
+    const float2 *cs = csum + (size_t)s * nchunks * nleads;
+    const float *bd = band + (size_t)s * nchunks * nleads * (size_t)steps + (size_t)l * steps;
+    double acc = 0.0;
+    for (int L = 0; L < nl; ++L) {
+        const int c0 = layer_c0[L], c1 = layer_c1[L];
+        if (c0 >= c1) continue;
+        const float4 kc = reinterpret_cast<const float4 *>(layer_c)[(size_t)s * nl + L];
+        // the steady prefix [c0, clo): clo = the first chunk with tb1 > t0
+        int clo = c1;
+        for (int cb = c0; cb < c1; cb += 32) {
+            const unsigned m = __ballot_sync(0xffffffffu, cb + lane < c1 && ci[cb + lane].y > t0);
+            if (m) {
+                clo = cb + __ffs(m) - 1;
+                break;
+            }
+        }
+        float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
+        for (int c = c0 + lane; c < clo; c += 32) {
+            const float2 sv = cs[(size_t)c * nleads + l];
+            const float g = ex2_approx(-kc.y * ((th0.x - __int_as_float(ci[c].z)) + th0.y));
+            A = ff_add_f(A, g * sv.x);
+            B = ff_add_f(B, sv.y);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float2 a2 = make_float2(__shfl_down_sync(0xffffffffu, A.x, o), __shfl_down_sync(0xffffffffu, A.y, o));
+            const float2 b2 = make_float2(__shfl_down_sync(0xffffffffu, B.x, o), __shfl_down_sync(0xffffffffu, B.y, o));
+            A = ff_add(A, a2);
+            B = ff_add(B, b2);
+        }
+        A = make_float2(__shfl_sync(0xffffffffu, A.x, 0), __shfl_sync(0xffffffffu, A.y, 0));
+        B = make_float2(__shfl_sync(0xffffffffu, B.x, 0), __shfl_sync(0xffffffffu, B.y, 0));
+        const float e0 = kc.z * ex2_approx(-kc.y * ((th.x - th0.x) + (th.y - th0.y)));
+        float2 sum = ff_add(ff_mul(make_float2(e0, 0.f), A), ff_mul(make_float2(kc.w, 0.f), B));
+        // the chunks after the prefix, per step
+        for (int c = clo; c < c1; ++c) {
+            const int4 in = ci[c];
+            if (in.x >= t0 + 32) break;
+            if (!valid || t < in.x) continue;
+            float v;
+            if (t < in.y) {
+                v = bd[(size_t)c * nleads * steps + t];
+            } else {
+                const float2 sv = cs[(size_t)c * nleads + l];
+                const float e = kc.z * ex2_approx(-kc.y * ((th.x - __int_as_float(in.z)) + th.y));
+                v = fmaf(e, sv.x, kc.w * sv.y);
+            }
+            sum = ff_add_f(sum, v);
+        }
+        if (valid) acc = fma(ff_to_double(sum), F[((size_t)s * nl + L) * steps + t], acc);
+    }
+    if (valid) {
+        const double r = k0w[(size_t)s * nleads + l] + acc;
+        const size_t o = ((size_t)s * nleads + l) * steps + t;
+        ecg[o] = r;
+        ecg_ff[o] = ff_from_double(r);
     }
 }
 
@@ -618,8 +742,8 @@ void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_lay
 }
 
 void launch_k0_term(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
-                    double *d_k0w) {
-    dim3 grid((unsigned)h.nleads, (unsigned)n_sims);
+                    double *d_k0w, int rows) {
+    dim3 grid((unsigned)rows, (unsigned)n_sims);
     k_k0_term<<<grid, 256, 0, s>>>(h.apad, h.nleads, d_W, h.a_layer.p, d_layer_k, h.nlayers, d_k0w);
     EKG_CUDA(cudaGetLastError());
 }
@@ -634,18 +758,41 @@ void launch_contract_cuda(cudaStream_t s, const HeartDev &h, const float *d_Wp, 
     EKG_CUDA(cudaGetLastError());
 }
 
-void launch_contract_band(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,
-                          const double *d_F, int n_sims, double *d_partial) {
+void launch_contract_band(cudaStream_t s, const HeartDev &h, const float *d_Wm, int wrows, const float *d_W0,
+                          const double *d_layer_k, const float *d_layer_c, int n_sims, float *d_band, float2 *d_csum,
+                          int4 *d_cinfo) {
     static bool attr = false;
     if (!attr) {
-        EKG_CUDA(cudaFuncSetAttribute(k_contract_band, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CB_SMEM));
+        EKG_CUDA(cudaFuncSetAttribute(k_contract_band<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CB_SMEM));
+        EKG_CUDA(cudaFuncSetAttribute(k_contract_band<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CB_SMEM));
+        EKG_CUDA(cudaFuncSetAttribute(k_contract_band<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CB_SMEM));
+        EKG_CUDA(cudaFuncSetAttribute(k_contract_band<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CB_SMEM));
         attr = true;
     }
     const int nlb = (h.nleads + CB_LB - 1) / CB_LB;
     dim3 grid((unsigned)h.nchunks, (unsigned)(n_sims * nlb));
-    k_contract_band<<<grid, CB_THREADS, CB_SMEM, s>>>(h.steps, h.nleads, h.apad, h.nlayers, h.t_hilo.p, h.at_hilo.p,
-                                                      h.chunk_a0.p, h.chunk_a1.p, h.chunk_layer.p, d_Wp, d_layer_c,
-                                                      d_F, h.nchunks, nlb, d_partial);
+    // leads per block rounded up to a multiple of 4 (one block when there are at most 16)
+    const int nlr = nlb > 1 ? 16 : (h.nleads + 3) / 4 * 4;
+    auto go = [&](auto kern) {
+        kern<<<grid, CB_THREADS, CB_SMEM, s>>>(h.steps, h.nleads, h.apad, h.nlayers, h.t_hilo.p, h.at_hilo.p, h.at.p,
+                                              h.chunk_a0.p, h.chunk_a1.p, h.chunk_layer.p, d_Wm, wrows, d_W0,
+                                              d_layer_k, d_layer_c, h.nchunks, nlb, d_band, d_csum, d_cinfo);
+    };
+    if (nlr == 4) go(k_contract_band<4>);
+    else if (nlr == 8) go(k_contract_band<8>);
+    else if (nlr == 12) go(k_contract_band<12>);
+    else go(k_contract_band<16>);
+    EKG_CUDA(cudaGetLastError());
+}
+
+void launch_reduce_chunks(cudaStream_t s, const HeartDev &h, const float *d_layer_c, const double *d_F,
+                          const float *d_band, const float2 *d_csum, const int4 *d_cinfo, const double *d_k0w,
+                          int n_sims, double *d_ecg, float2 *d_ecg_ff) {
+    const int nlb = (h.nleads + 15) / 16;
+    dim3 grid((unsigned)((h.steps + 31) / 32), (unsigned)n_sims, (unsigned)nlb);
+    k_reduce_chunks<<<grid, 32 * std::min(16, h.nleads), 0, s>>>(h.steps, h.nleads, h.nlayers, h.nchunks,
+                                                                 h.layer_c0.p, h.layer_c1.p, h.t_hilo.p, d_layer_c, d_F,
+                                                                 d_band, d_csum, d_cinfo, d_k0w, d_ecg, d_ecg_ff);
     EKG_CUDA(cudaGetLastError());
 }
 

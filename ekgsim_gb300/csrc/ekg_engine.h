@@ -64,7 +64,6 @@ struct BatchState {
     DBuf<int32_t> ls0, ls1;                // [nl] 32-AP stage range of each layer
     DBuf<int32_t> nent, esplit;            // [nl], [nl][8]: entries, steady prefix ends (stages)
     DBuf<float2> tref;                     // [stages] last finite activation time of the stage (hi, lo)
-    DBuf<int32_t> stage_order;             // [stages] by descending voxel count (operand kernel's item order)
     DBuf<int64_t> goff;                    // [nl][8] offsets into gtab
     DBuf<float> gtab;                      // exp(-k4 (t0_e - tref[st])) for the steady stages of entry e
     DBuf<int32_t> ent;                     // [nl][ntt] entry of each tile (-1: layer without APs)
@@ -212,6 +211,8 @@ struct ekg_heart {
     ekg::DBuf<double> at_cells;       // device activation times per cell
     ekg::DBuf<double> leads0_dev;
     ekg::DBuf<float> W0;              // [L][apad] lead field at the loaded positions
+    ekg::DBuf<double> W0_layer;       // [nl][L] per-layer sums of W0 (the per-simulation form's k0 term)
+    bool W0_layer_ok = false;
     ekg::EvalSettings es;
     ekg::BatchState bs;
     int sm_count = 152;

@@ -157,9 +157,11 @@ struct HeartDev {
     DBuf<float4> vox_pos;   // [nvox] bordered position relative to `centre` (z,y,x) + in-mask bits in .w
     DBuf<float4> vox_out;   // [nvox] sum of the out-neighbour offsets (z,y,x), .w = 1 if any
     DBuf<float4> stage_box; // [2 * apad / 32] per 32-AP stage: lowest and highest voxel position (z,y,x)
+    DBuf<int32_t> stage_order;  // [apad / 32] stages by descending voxel count (field kernels' item order)
     double centre[3] = {0, 0, 0};
     // K chunks
     DBuf<int32_t> chunk_a0, chunk_a1, chunk_layer;  // [nchunks]
+    DBuf<int32_t> layer_c0, layer_c1;               // [nlayers] chunk range of each layer (empty: 0, 0)
     // neighbourhood offsets (z,y,x) as int8 triples
     int nnb = 0;
     int8_t nb_dif[26 * 3];
@@ -209,7 +211,11 @@ struct EvalDev {
     DBuf<double> k0w;       // [S][L] constant k0 term
     DBuf<float> W;          // [S][L][apad] lead field for this eval's positions
     DBuf<float> Wp;         // [S][L][apad] W * exp(k5 at)
-    DBuf<double> partial;   // [S][nchunks][L][steps]
+    DBuf<double> partial;   // [S][nchunks][L][steps] (dense contractions)
+    DBuf<float> band;       // [S][nchunks][L][steps] band-step values (band contraction)
+    DBuf<float2> csum;      // [S][nchunks][L] steady sums (S0, S1)
+    DBuf<int4> cinfo;       // [S][nchunks] (first band step, first steady step, amax bits, 0)
+    DBuf<int> work;         // work-item counter of the moved-row field kernel
     DBuf<float> coef;       // [S][nl][J] static-lead Taylor coefficients (batched form)
     DBuf<double> ecg;       // [S][L][steps]
     DBuf<float2> ecg_ff;    // [S][L][steps] the same as float-float (hi, lo), read by the criteria
@@ -226,17 +232,33 @@ void launch_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads,
 void launch_layer_factors(cudaStream_t s, const HeartDev &h, const double *d_layer_k, const double *d_cpre,
                           int n_sims, double *d_F, float *d_Ff, float *d_layer_c, const double *d_centre = nullptr,
                           const double *d_scale = nullptr, int J = 0, float *d_coef = nullptr);
-// per-simulation form: W (moved rows) and W' = W exp(k5 at) (every row) from the lead positions (batch.cu)
+// per-simulation form: W and (Wp not null) W' = W exp(k5 at) of the moved rows from the lead
+// positions, and with static_rows W' of the other rows from the resident field W0 (batch.cu)
 void launch_sim_lead_field(cudaStream_t s, const HeartDev &h, const double *d_leads, int nmove, int lead_stride,
-                           int n_sims, const double *d_layer_k, const float *W0, float *W, float *Wp);
+                           int n_sims, const double *d_layer_k, const float *W0, float *W, float *Wp,
+                           bool static_rows);
+// the same W of the moved rows for many simulations, with the batched operand kernel's work split;
+// work: a device counter (zeroed here)
+void launch_sim_lead_field_rows(cudaStream_t s, const HeartDev &h, const double *d_leads, int nmove, int lead_stride,
+                                int n_sims, float *W, int *work, int sm_count);
+// k0w[s][l] = sum_a k0_{layer(a)} W[s][l][a] for the first `rows` leads
 void launch_k0_term(cudaStream_t s, const HeartDev &h, const float *d_W, const double *d_layer_k, int n_sims,
-                    double *d_k0w);
+                    double *d_k0w, int rows);
+// out[L][l] = sum_{a in layer L} W0[l][a] in FP64 (batch.cu)
+void launch_w0_layer_sums(cudaStream_t s, const HeartDev &h, const float *W0, double *out);
 void launch_contract_cuda(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,
                           const double *d_F, int n_sims, double *d_partial);
 // band form (zero / steady / band steps per chunk) for chunks of up to CONTRACT_BAND_CAP APs
 constexpr int CONTRACT_BAND_CAP = 512;
-void launch_contract_band(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,
-                          const double *d_F, int n_sims, double *d_partial);
+// band[S][nchunks][L][steps] (band steps only), csum[S][nchunks][L], cinfo[S][nchunks]; the field
+// is Wm [S][L][apad] (unscaled) for rows l < wrows and the resident W0 for the others
+void launch_contract_band(cudaStream_t s, const HeartDev &h, const float *d_Wm, int wrows, const float *d_W0,
+                          const double *d_layer_k, const float *d_layer_c, int n_sims, float *d_band, float2 *d_csum,
+                          int4 *d_cinfo);
+// ecg (and its float-float copy) from the band contraction's outputs plus k0w
+void launch_reduce_chunks(cudaStream_t s, const HeartDev &h, const float *d_layer_c, const double *d_F,
+                          const float *d_band, const float2 *d_csum, const int4 *d_cinfo, const double *d_k0w,
+                          int n_sims, double *d_ecg, float2 *d_ecg_ff);
 void launch_contract_umma(cudaStream_t s, const HeartDev &h, const float *d_Wp, const float *d_layer_c,
                           const double *d_F, int n_sims, double *d_partial, uint32_t *d_err);
 // Explicit-argument form: `rows` weight rows (leads) per simulation, Wp [S][rows][apad],
@@ -271,7 +293,7 @@ struct BandArgs {
     int max_ent = 1, nb = 1;
     const int32_t *ti0 = nullptr, *ti1 = nullptr;  // [ntt][nl] item range of (tile, layer)
     const float2 *tref = nullptr;                   // [stages] last finite activation time of each 32-AP stage
-    const int32_t *stage_order = nullptr;           // [stages] by descending voxel count
+    const int32_t *stage_order = nullptr;           // [stages] by descending voxel count (HeartDev's)
     const int32_t *nent = nullptr, *esplit = nullptr, *ls0 = nullptr, *ls1 = nullptr;  // stage units
     const int32_t *ent = nullptr;
     const int64_t *goff = nullptr;
@@ -309,8 +331,9 @@ void launch_k0_moved(cudaStream_t s, const BandArgs &a, const int32_t *ls0, cons
                      const double *layer_k, double *cmov);
 void launch_k0_static_sums(cudaStream_t s, int nleads, int64_t apad, int nl, const int32_t *ls0,
                            const int32_t *ls1, const float *W0, double *K0s);
+// cst[s][l] (l >= nmove) = sum_L (k0_L - k0_0) K0s[L][l], or sum_L k0_L K0s[L][l] when !relative
 void launch_k0_static(cudaStream_t s, int n_sims, int nleads, int nmove, int nl, const double *K0s,
-                      const double *layer_k, double *cst);
+                      const double *layer_k, double *cst, bool relative = true);
 void launch_reduce_band(cudaStream_t s, const BandArgs &a);
 void launch_reduce_ecg(cudaStream_t s, const HeartDev &h, const double *d_partial, const double *d_k0w,
                        int n_sims, double *d_ecg, float2 *d_ecg_ff);

@@ -429,6 +429,21 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
                                               D.vox_nbo.p, D.vox_pos.p, D.vox_out.p);
     D.stage_box.alloc((size_t)2 * (apad / 32));
     setup_stage_boxes_device(s, apad, D.a_vox_begin.p, D.vox_pos.p, D.stage_box.p);
+    {
+        // work items of the moved-lead field kernels: stages with the most voxels first
+        // (longest-first), ties by index
+        const int64_t nst = apad / 32;
+        std::vector<int64_t> vb(apad + 1);
+        EKG_CUDA(cudaMemcpyAsync(vb.data(), D.a_vox_begin.p, vb.size() * 8, cudaMemcpyDeviceToHost, s));
+        EKG_CUDA(cudaStreamSynchronize(s));
+        std::vector<int32_t> order(nst);
+        for (int64_t st = 0; st < nst; ++st) order[st] = (int32_t)st;
+        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+            return vb[32 * (a + 1)] - vb[32 * a] > vb[32 * (b + 1)] - vb[32 * b];
+        });
+        D.stage_order.alloc(nst);
+        EKG_CUDA(cudaMemcpy(D.stage_order.p, order.data(), nst * 4, cudaMemcpyHostToDevice));
+    }
     // host copies of the sorted voxel cells and AP starts, for the reference's AP numbering
     h->vox_cell.resize(nv);
     h->vox_group_start.resize(na + 1);
@@ -443,6 +458,17 @@ void heart_setup(ekg_heart *h, const ekg_heart_desc *d) {
     EKG_CUDA(cudaMemcpyAsync(D.chunk_a0.p, c0.data(), c0.size() * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.chunk_a1.p, c1.data(), c0.size() * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.chunk_layer.p, cl.data(), c0.size() * 4, cudaMemcpyHostToDevice, s));
+    // chunk range of each layer (a layer's chunks are contiguous)
+    std::vector<int32_t> lc0v(nl, 0), lc1v(nl, 0);
+    for (size_t k = 0; k < cl.size(); ++k) {
+        const int L = cl[k];
+        if (lc0v[L] == lc1v[L]) lc0v[L] = (int32_t)k;
+        lc1v[L] = (int32_t)k + 1;
+    }
+    D.layer_c0.alloc(nl);
+    D.layer_c1.alloc(nl);
+    EKG_CUDA(cudaMemcpyAsync(D.layer_c0.p, lc0v.data(), nl * 4, cudaMemcpyHostToDevice, s));
+    EKG_CUDA(cudaMemcpyAsync(D.layer_c1.p, lc1v.data(), nl * 4, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.difs.p, D.nb_dif, 3 * D.nnb, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.t.p, h->t.data(), steps * 8, cudaMemcpyHostToDevice, s));
     EKG_CUDA(cudaMemcpyAsync(D.t_hilo.p, th.data(), steps * 8, cudaMemcpyHostToDevice, s));
@@ -493,15 +519,31 @@ void ensure_eval_capacity(ekg_heart *h, int n_sims) {
     E.err.alloc(1);
     E.cap_sims = n_sims;
 }
+// moved rows (simulations x moved leads) from which the per-simulation form evaluates their field
+// with the persistent row kernel (below: one thread per (AP, simulation))
+constexpr int SIM_ROWS_PERSISTENT = 128;
+// whether the per-simulation form contracts with the band form (compact outputs)
+bool band_contraction(const ekg_heart *h) {
+    return h->eng->contract == EKG_CONTRACT_BAND && h->dev.chunk_max <= CONTRACT_BAND_CAP;
+}
 // buffers of the general (per-simulation AP) form
 void ensure_general_capacity(ekg_heart *h, int n_sims) {
     EvalDev &E = h->ev;
     const HeartDev &D = h->dev;
     const size_t S = (size_t)n_sims;
-    if (E.W.n >= S * D.nleads * D.apad && E.partial.n >= S * D.nchunks * D.nleads * D.steps) return;
-    E.W.alloc(S * D.nleads * D.apad);
-    E.Wp.alloc(S * D.nleads * D.apad);
-    E.partial.alloc(S * D.nchunks * D.nleads * D.steps);
+    const size_t nw = S * D.nleads * D.apad, np = S * D.nchunks * D.nleads * D.steps;
+    if (E.W.n < nw) {
+        E.W.alloc(nw);
+        E.Wp.alloc(nw);
+    }
+    if (E.work.n < 1) E.work.alloc(1);
+    if (band_contraction(h)) {
+        if (E.band.n < np) E.band.alloc(np);
+        if (E.csum.n < S * D.nchunks * D.nleads) E.csum.alloc(S * D.nchunks * D.nleads);
+        if (E.cinfo.n < S * D.nchunks) E.cinfo.alloc(S * D.nchunks);
+    } else if (E.partial.n < np) {
+        E.partial.alloc(np);
+    }
 }
 
 // Device pass for n_sims simulations, split into upload / compute / download so the benchmark
@@ -627,18 +669,6 @@ void build_band(ekg_heart *h, const std::vector<double> &key, const std::vector<
     B.ls0.alloc(nl);
     B.ls1.alloc(nl);
     B.tref.alloc(nst);
-    {
-        // operand kernel items: stages with the most voxels first (longest-first), ties by index
-        std::vector<int64_t> vb(D.apad + 1);
-        EKG_CUDA(cudaMemcpy(vb.data(), D.a_vox_begin.p, vb.size() * 8, cudaMemcpyDeviceToHost));
-        std::vector<int32_t> order(nst);
-        for (int64_t st = 0; st < nst; ++st) order[st] = (int32_t)st;
-        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
-            return vb[32 * (a + 1)] - vb[32 * a] > vb[32 * (b + 1)] - vb[32 * b];
-        });
-        B.stage_order.alloc(nst);
-        EKG_CUDA(cudaMemcpy(B.stage_order.p, order.data(), nst * 4, cudaMemcpyHostToDevice));
-    }
     B.nent.alloc(nl);
     B.esplit.alloc((size_t)nl * MAXE);
     B.goff.alloc((size_t)nl * MAXE);
@@ -1000,6 +1030,12 @@ void upload_inputs(ekg_heart *h, const PassPlan &P, const double *layer_k, const
     in.layer_k = reinterpret_cast<const double *>(dv + o_lk);
     in.cpre = h->cpre_on ? reinterpret_cast<const double *>(dv + o_cp) : nullptr;
     in.leads = P.nmove > 0 ? reinterpret_cast<const double *>(dv + o_ld) : nullptr;
+    if (!P.batch && h->any_k0 && band_contraction(h) && P.nmove < D.nleads && !h->W0_layer_ok) {
+        // per-layer sums of the resident lead field, once per heart
+        h->W0_layer.alloc((size_t)D.nlayers * D.nleads);
+        launch_w0_layer_sums(s, D, h->W0.p, h->W0_layer.p);
+        h->W0_layer_ok = true;
+    }
     if (P.batch) {
         in.k3 = reinterpret_cast<const double *>(dv + o_k3);
         in.hconst = reinterpret_cast<const float4 *>(dv + o_hc);
@@ -1104,7 +1140,7 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             U.nleads = (int)L;
             U.max_ent = B.max_ent;
             U.tref = B.tref.p;
-            U.stage_order = B.stage_order.p;
+            U.stage_order = D.stage_order.p;
             U.nent = B.nent.p;
             U.esplit = B.esplit.p;
             U.ls0 = B.ls0.p;
@@ -1180,30 +1216,51 @@ void compute(ekg_heart *h, const PassPlan &P, int n_crit_leads, int mode, PassTi
             EKG_CUDA(cudaEventRecord(tm->ev[2], s));
         }
     } else {
-        // lead field: recomputed rows for moved leads, the resident rows for leads at their loaded
-        // position (W, unscaled, is needed in full only for the k0 term)
-        if (h->any_k0)
+        // lead field: recomputed rows for moved leads; the leads at their loaded position take the
+        // resident field W0 (scaled inside the band contraction, or written out for the dense ones)
+        const bool band = band_contraction(h);
+        if (h->any_k0 && !band)
             for (size_t si = 0; si < S; ++si)
                 EKG_CUDA(cudaMemcpyAsync(E.W.p + si * L * D.apad, h->W0.p, L * D.apad * 4, cudaMemcpyDeviceToDevice, s));
-        launch_sim_lead_field(s, D, in.leads, nmove, (int)L, n_sims, in.layer_k, h->W0.p, E.W.p, E.Wp.p);
-        ++launches;
-        // k0 leaves a constant term only when some layer's k0 differs from zero (AP differences
-        // within a layer cancel it)
-        if (h->any_k0) {
-            launch_k0_term(s, D, E.W.p, in.layer_k, n_sims, E.k0w.p);
+        if (band && nmove > 0 && n_sims * nmove >= SIM_ROWS_PERSISTENT) {
+            launch_sim_lead_field_rows(s, D, in.leads, nmove, (int)L, n_sims, E.W.p, E.work.p, h->sm_count);
             ++launches;
+        } else if (nmove > 0 || !band) {
+            launch_sim_lead_field(s, D, in.leads, nmove, (int)L, n_sims, in.layer_k, h->W0.p, E.W.p,
+                                  band ? nullptr : E.Wp.p, !band);
+            ++launches;
+        }
+        // k0 leaves a constant term only when some layer's k0 differs from zero (AP differences
+        // within a layer cancel it): sum_a k0_{layer(a)} W[l, a], from W for the moved rows and from
+        // the layer sums of W0 for the others
+        if (h->any_k0) {
+            const int wrows = band ? nmove : (int)L;
+            if (wrows > 0) {
+                launch_k0_term(s, D, E.W.p, in.layer_k, n_sims, E.k0w.p, wrows);
+                ++launches;
+            }
+            if (wrows < (int)L) {
+                launch_k0_static(s, n_sims, (int)L, wrows, D.nlayers, h->W0_layer.p, in.layer_k, E.k0w.p, false);
+                ++launches;
+            }
         } else {
             EKG_CUDA(cudaMemsetAsync(E.k0w.p, 0, S * L * sizeof(double), s));
         }
         if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[1], s));
-        if (h->eng->contract == EKG_CONTRACT_BAND && D.chunk_max <= CONTRACT_BAND_CAP)
-            launch_contract_band(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p);
-        else if (h->eng->contract != EKG_CONTRACT_DENSE_CUDA)
-            launch_contract_umma(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p, E.err.p);
-        else
-            launch_contract_cuda(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p);
-        if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[2], s));
-        launch_reduce_ecg(s, D, E.partial.p, E.k0w.p, n_sims, E.ecg.p, E.ecg_ff.p);
+        if (band) {
+            launch_contract_band(s, D, E.W.p, nmove, h->W0.p, in.layer_k, E.layer_c.p, n_sims, E.band.p, E.csum.p,
+                                 E.cinfo.p);
+            if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[2], s));
+            launch_reduce_chunks(s, D, E.layer_c.p, E.F.p, E.band.p, E.csum.p, E.cinfo.p, E.k0w.p, n_sims, E.ecg.p,
+                                 E.ecg_ff.p);
+        } else {
+            if (h->eng->contract != EKG_CONTRACT_DENSE_CUDA)
+                launch_contract_umma(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p, E.err.p);
+            else
+                launch_contract_cuda(s, D, E.Wp.p, E.layer_c.p, E.F.p, n_sims, E.partial.p);
+            if (tm && tm->on) EKG_CUDA(cudaEventRecord(tm->ev[2], s));
+            launch_reduce_ecg(s, D, E.partial.p, E.k0w.p, n_sims, E.ecg.p, E.ecg_ff.p);
+        }
         launches += 2;
     }
     if (n_crit_leads > 0) {
@@ -1238,10 +1295,12 @@ std::vector<uint64_t> pass_signature(const ekg_heart *h, const PassPlan &P, int 
                           (const void *)B.Q1.p,
                           (const void *)B.Q2.p, (const void *)B.Bt.p, (const void *)B.P1.p, (const void *)B.U.p,
                           (const void *)B.Up.p, (const void *)B.partial.p,
-                          (const void *)B.tref.p, (const void *)B.stage_order.p, (const void *)B.nent.p, (const void *)B.esplit.p, (const void *)B.ls0.p,
+                          (const void *)B.tref.p, (const void *)h->dev.stage_order.p, (const void *)B.nent.p, (const void *)B.esplit.p, (const void *)B.ls0.p,
                           (const void *)B.ls1.p, (const void *)B.ent.p, (const void *)B.goff.p, (const void *)B.gtab.p,
                           (const void *)B.E.p, (const void *)B.work.p, (const void *)h->W0.p, (const void *)B.P2.p,
-                          (const void *)B.cmov.p, (const void *)B.cst.p, (const void *)B.K0s.p})
+                          (const void *)B.cmov.p, (const void *)B.cst.p, (const void *)B.K0s.p, (const void *)E.band.p,
+                          (const void *)E.csum.p, (const void *)E.cinfo.p, (const void *)h->W0_layer.p, (const void *)E.work.p,
+                          (const void *)h->dev.stage_order.p})
         v.push_back(u(p));
     return v;
 }
@@ -1464,12 +1523,20 @@ void benchmark(ekg_heart *h, int n_sims, const double *layer_k, const double *le
         op_bytes = (double)P.rows_used * D.apad * 4 + p1 * P.rows_used * 8 +
                    (double)D.nvox * 16 + (double)(D.nvox - D.n_interior) * 16 + (double)D.apad * 16;
     }
+    // bytes the band contraction of the per-simulation form has to move: the moved rows' W' and the
+    // activation times per simulation and lead block, the resident field once, and its compact
+    // outputs (run limits, steady sums, the band steps' values, counted from the run limits)
     double band_bytes = 0;
-    if (!P.batch && h->eng->contract == EKG_CONTRACT_BAND && h->dev.chunk_max <= CONTRACT_BAND_CAP) {
+    if (!P.batch && band_contraction(h)) {
         const HeartDev &D = h->dev;
         const int nlb = (D.nleads + 15) / 16;
-        band_bytes = (double)n_sims * ((double)D.nleads * D.apad * 4 + (double)D.nchunks * D.nleads * D.steps * 8 +
-                                       (double)nlb * D.apad * 8);
+        std::vector<int4> ci((size_t)n_sims * D.nchunks);
+        EKG_CUDA(cudaMemcpy(ci.data(), h->ev.cinfo.p, ci.size() * sizeof(int4), cudaMemcpyDeviceToHost));
+        double nband = 0;
+        for (const int4 &c : ci) nband += std::max(0, c.y - c.x);
+        band_bytes = (double)n_sims * ((double)P.nmove * D.apad * 4 + (double)nlb * D.apad * 16 +
+                                       (double)D.nchunks * (16 + (double)D.nleads * 8)) +
+                     nband * D.nleads * 4 + (double)(D.nleads - P.nmove) * D.apad * 4;
     }
     const double vals[11] = {total, contract, prep, tail, (double)g_launch_count, (double)P.nmove, P.batch ? 1.0 : 0.0,
                              operand, gemm_flops, op_bytes, band_bytes};

@@ -2,9 +2,11 @@
 
     python -m ekgsim_gb300.profile_case ca [--grid N]          heart set-up of an N^3 ellipsoid
                                                                (activation-time relaxation, de-duplication)
-    python -m ekgsim_gb300.profile_case batched [--sims S] [--passes P] [--moved-all]
+    python -m ekgsim_gb300.profile_case batched [--sims S] [--passes P] [--moved-all] [--free-k1]
                                                                S-simulation batched passes on the
                                                                160^3 heart of the batched workload
+                                                               (--free-k1: k1 differs between the
+                                                               simulations, the per-simulation form)
 
 The workloads are the seeded synthetic ones of ekgsim_gb300.synth.
 """
@@ -25,6 +27,7 @@ def main():
     ap.add_argument("--sims", type=int, default=256)
     ap.add_argument("--passes", type=int, default=3)
     ap.add_argument("--moved-all", action="store_true")
+    ap.add_argument("--free-k1", action="store_true")
     a = ap.parse_args()
     eng = E.Engine(0)
     if a.case == "ca":
@@ -53,9 +56,14 @@ def main():
             rng = np.random.Generator(np.random.PCG64(spec.seed + 77))
             genes[:, 12:] = -50.0 + 100.0 * rng.random((a.sims, 2 * spec.n_leads))
         lk = np.stack([E.layer_aps(h._cfg, spec.n_layers, g[:12])[0] for g in genes])
+        if a.free_k1:
+            lk[:, :, 1] *= 1.0 + 1e-3 * np.arange(a.sims)[:, None]  # k1 as a free gene
         moved = np.stack([E.move_leads(leads, g[12:].reshape(-1, 2)) for g in genes])
         bm = h.benchmark(lk, moved, warmup=1, iters=a.passes)
-        print(f"batched: {a.sims} sims, {bm['total_ms'] / a.passes:.3f} ms per pass")
+        it = a.passes
+        print(f"{'batched' if bm['batched'] else 'per-simulation'} form: {a.sims} sims, "
+              f"{bm['total_ms'] / it:.3f} ms per pass (prep {bm['prep_ms'] / it:.3f}, contract "
+              f"{bm['contract_ms'] / it:.3f}, tail {bm['tail_ms'] / it:.3f}, operand {bm['operand_ms'] / it:.3f})")
         h.close()
     eng.close()
 

@@ -382,6 +382,50 @@ def test_batched_two_bases_free_k3(engine):
         assert rel_l2(ecg_b[i], ref) <= ECG_TOL
 
 
+def test_per_simulation_form_many_moved_rows(engine):
+    """k1 free per simulation (the per-simulation form) with 70 simulations: 280 moved rows (all four
+    leads displaced, some to within a few cells of the heart) and 140 (two leads), which the
+    persistent row kernel evaluates; the band contraction scales the rows and the chunk reduction
+    rebuilds the zero and steady runs.  A spread of results against the oracle, every result against
+    its single evaluation (one simulation: the per-AP lead-field kernel)."""
+    from ekgsim_gb300.engine import Heart
+    spec = synth.small_spec(40, n_leads=4, seed=37)
+    steps = 300
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(3, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    h = Heart.create(engine, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+    free = [1, 5, 6, 7, 8]
+    h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, free,
+               [t for t in synth.analytic_target(spec.n_leads, steps, 9)], mid_position=0.6)
+    ng, _ = h.eval_shape()
+    lo, hi = h.gene_bounds()
+    rng = np.random.Generator(np.random.PCG64(41))
+    n = 70
+    genes = lo + (hi - lo) * rng.random((n, ng))
+    genes[:, 15:] = rng.uniform(-50.0, 50.0, size=(n, 2 * spec.n_leads))
+    at, layer = O.activation(grid, tm)
+    nz = np.argwhere(layer > 0).astype(float) + 1.0  # bordered voxel coordinates (z, y, x)
+    for nmoved in (4, 2):
+        gs = genes.copy()
+        gs[:, 15 + 2 * nmoved:] = 0.0
+        lks = np.stack([O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, free, "endo-mid-epi",
+                                    0.6, g[:15])[0] for g in gs])
+        moveds = np.stack([O.move_leads(leads, g[15:].reshape(-1, 2)) for g in gs])
+        assert not h.benchmark(lks, moveds, warmup=1, iters=1)["batched"]
+        mind = [min(np.sqrt(((nz - p) ** 2).sum(axis=1)).min() for p in m[:nmoved]) for m in moveds]
+        assert min(mind) < 20.0 and max(mind) > 21.0
+        crit_b, viol_b, ecg_b = h.eval_batch(gs, want_ecg=True)
+        for i in (0, 23, 47, 69):
+            ref = O.run(layer, at, lks[i], moveds[i], "3D4", 0.0, float(steps), 1.0)
+            assert rel_l2(ecg_b[i], ref) <= ECG_TOL, (nmoved, i)
+        for i in range(n):
+            c1, v1, e1 = h.eval_batch(gs[i:i + 1], want_ecg=True)
+            assert rel_l2(ecg_b[i], e1[0]) <= ECG_TOL, (nmoved, i)
+            assert np.allclose(crit_b[i], c1[0], rtol=0, atol=1e-4) and viol_b[i] == v1[0]
+    h.close()
+
+
 def test_single_simulation_batched_form(engine):
     """Repeated single evaluations with the same k1, k4 switch to the batched form (static-lead basis +
     32-row band GEMM); the first call uses the per-simulation form.  Both match the oracle."""
