@@ -349,6 +349,39 @@ def all_leads_moved(E, heart, leads_zyx, spec, steps, batch, cfg_index, grid, tm
             "ecg_rel_l2_max": max(rels), "checked_sims": len(rels)}
 
 
+def free_k1(E, heart, leads_zyx, spec, steps, batch, cfg_index, grid, tm, iters, target):
+    """The same workload with k1 (the upstroke rate) a free gene, so every simulation has its own
+    k1 and the batch takes the per-simulation form (moved leads' field, band contraction, chunk
+    reduction): device simulations/s with inputs resident, and two results against the FP64 oracle.
+    Leaves the heart's evaluation settings with k1 free."""
+    from ekgsim_gb300 import synth
+    from oracle import oracle as O
+    free = [1, 5, 6, 7, 8]
+    heart.set_eval([synth.BASE_AP] * spec.n_layers, synth.K_MIN, synth.K_MAX, free, [t for t in target],
+                   mid_position=0.6)
+    ng, _ = heart.eval_shape()
+    lo, hi = heart.gene_bounds()
+    rng = np.random.Generator(np.random.PCG64(spec.seed + 91))
+    genes = lo + (hi - lo) * rng.random((batch, ng))
+    genes[:, 15:] = np.stack([synth.genes_for(spec, r, cfg_index)[12:] for r in range(batch)])
+    cfg = heart._cfg
+    lk = np.stack([E.layer_aps(cfg, spec.n_layers, g[:15])[0] for g in genes])
+    moved = np.stack([E.move_leads(leads_zyx, g[15:].reshape(-1, 2)) for g in genes])
+    heart.benchmark(lk, moved, warmup=3, iters=1)
+    bm = heart.benchmark(lk, moved, warmup=0, iters=iters)
+    ms = bm["total_ms"] / iters
+    ecg = heart.eval_batch(genes, want_ecg=True)[2]
+    at, layer = O.activation(grid, tm)
+    rels = []
+    for i in (0, batch - 1):
+        ref = O.run(layer, at, lk[i], moved[i], "3D4", 0.0, float(steps), 1.0)
+        rels.append(float(np.linalg.norm(ecg[i] - ref) / np.linalg.norm(ref)))
+    return {"form": "batched" if bm["batched"] else "per-simulation", "free_k": free,
+            "moved_leads": int(bm["moved_leads"]), "sims_per_s": batch / (ms / 1000.0), "ms_per_step": ms,
+            "lead_field_ms": bm["prep_ms"] / iters, "contract_ms": bm["contract_ms"] / iters,
+            "tail_ms": bm["tail_ms"] / iters, "ecg_rel_l2_max": max(rels), "checked_sims": len(rels)}
+
+
 def host_cores() -> int:
     try:
         return len(os.sched_getaffinity(0))
@@ -592,6 +625,8 @@ def run_ours(args):
     if d.rank == 0 and not args.no_moved_all and args.workload == "batched":
         line["all_leads_moved"] = all_leads_moved(E, heart, leads_zyx, spec, steps, batch, cfg_index, grid, tm,
                                                   args.steps, args.no_tune)
+    if d.rank == 0 and not args.no_free_k1 and args.workload == "batched":
+        line["free_k1"] = free_k1(E, heart, leads_zyx, spec, steps, batch, cfg_index, grid, tm, args.steps, target)
     if d.rank == 0 and not args.no_served:
         line["served"] = served_run(max_wait_us=args.served_wait_us)
         line["served_over_plain"] = line["served"]["saturated"]["throughput_req_s"] / plain["sims_per_s"]
@@ -624,6 +659,7 @@ def main():
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the built-in launch shapes")
     ap.add_argument("--no-moved-all", action="store_true", help="skip the all-leads-moved variant")
+    ap.add_argument("--no-free-k1", action="store_true", help="skip the free-k1 (per-simulation form) variant")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":

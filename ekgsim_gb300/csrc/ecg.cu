@@ -230,26 +230,30 @@ __global__ void __launch_bounds__(CC_T) k_contract_cuda(int steps, int nleads, i
 // W'), with W the moved rows' field Wm [S][L][apad] for l < wrows and the resident field
 // W0 [L][apad] for the others.
 constexpr int CB_THREADS = 256, CB_LB = 16, CB_CAP = CONTRACT_BAND_CAP;
-constexpr size_t CB_SMEM = (size_t)CB_CAP * CB_LB * 4 + (size_t)CB_CAP * 8 + (size_t)CB_THREADS * (CB_LB + 1) * 4;
+// dynamic shared memory of a block with NLB leads: W' [CB_CAP][NLB], the activation times, the
+// band passes' partial sums [CB_THREADS][NLB + 1]; five blocks per SM fit up to 12 leads
+constexpr size_t cb_smem_bytes(int nlb) {
+    return (size_t)CB_CAP * nlb * 4 + (size_t)CB_CAP * 8 + (size_t)CB_THREADS * (nlb + 1) * 4;
+}
 template <int NLB>
-__global__ void __launch_bounds__(CB_THREADS, 4) k_contract_band(
+__global__ void __launch_bounds__(CB_THREADS, NLB <= 12 ? 5 : 4) k_contract_band(
     int steps, int nleads, int64_t apad, int nl, const float2 *__restrict__ t_hilo, const float2 *__restrict__ at_hilo,
     const double *__restrict__ at, const int32_t *__restrict__ chunk_a0, const int32_t *__restrict__ chunk_a1,
     const int32_t *__restrict__ chunk_layer, const float *__restrict__ Wm, int wrows, const float *__restrict__ W0,
     const double *__restrict__ layer_k, const float *__restrict__ layer_c, int nchunks, int nlb,
     float *__restrict__ band, float2 *__restrict__ csum, int4 *__restrict__ cinfo) {
     extern __shared__ __align__(16) uint8_t cb_smem[];
-    float(*s_w)[CB_LB] = reinterpret_cast<float(*)[CB_LB]>(cb_smem);  // W'[a][l] of the chunk
-    float2 *s_at = reinterpret_cast<float2 *>(cb_smem + (size_t)CB_CAP * CB_LB * 4);
-    float(*s_red)[CB_LB + 1] = reinterpret_cast<float(*)[CB_LB + 1]>(s_at + CB_CAP);  // [slice * rows + step]
+    float(*s_w)[NLB] = reinterpret_cast<float(*)[NLB]>(cb_smem);  // W'[a][l] of the chunk
+    float2 *s_at = reinterpret_cast<float2 *>(cb_smem + (size_t)CB_CAP * NLB * 4);
+    float(*s_red)[NLB + 1] = reinterpret_cast<float(*)[NLB + 1]>(s_at + CB_CAP);  // [slice * rows + step]
     __shared__ float s_ext[2][CB_THREADS / 32];
-    __shared__ float s_part[2][CB_THREADS / 32][CB_LB];
-    __shared__ float s_sum[2][CB_LB];
+    __shared__ float s_part[2][CB_THREADS / 32][(NLB + 7) / 8 * 8];
+    __shared__ float s_sum[2][NLB];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int c = blockIdx.x;
     const int s = blockIdx.y / nlb, lb = blockIdx.y % nlb;
     const int a0 = chunk_a0[c], na = chunk_a1[c] - a0, L = chunk_layer[c];
-    const int l0 = lb * CB_LB, nlh = min(CB_LB, nleads - l0);
+    const int l0 = lb * NLB, nlh = min(NLB, nleads - l0);
     const float4 kc = reinterpret_cast<const float4 *>(layer_c)[(size_t)s * nl + L];
     float *out = band + ((size_t)s * nchunks + c) * nleads * (size_t)steps + (size_t)l0 * steps;
     const double k5 = layer_k[((size_t)s * nl + L) * 9 + 5];
@@ -265,15 +269,15 @@ __global__ void __launch_bounds__(CB_THREADS, 4) k_contract_band(
         }
         const double ad = at[a0 + i];
         const float f = isinf(ad) ? 0.f : expf((float)(k5 * ad));
-        float w[CB_LB];
+        float w[NLB];
 #pragma unroll
-        for (int l = 0; l < CB_LB; ++l) {
+        for (int l = 0; l < NLB; ++l) {
             const int lg = l0 + l;
             w[l] = l >= nlh ? 0.f
                             : (lg < wrows ? Wm[((size_t)s * nleads + lg) * apad + a0 + i] : W0[(size_t)lg * apad + a0 + i]) * f;
         }
 #pragma unroll
-        for (int l = 0; l < CB_LB; l += 4)
+        for (int l = 0; l < NLB; l += 4)
             *reinterpret_cast<float4 *>(&s_w[i][l]) = make_float4(w[l], w[l + 1], w[l + 2], w[l + 3]);
     }
 #pragma unroll
@@ -323,29 +327,36 @@ __global__ void __launch_bounds__(CB_THREADS, 4) k_contract_band(
                 const float g = ex2_approx(-kc.y * ((amax - a2.x) - a2.y));
 #pragma unroll
                 for (int l = 0; l < 8; ++l) {
-                    const float w = s_w[i][lh + l];
+                    const float w = lh + l < NLB ? s_w[i][lh + l] : 0.f;
                     u0[l] = fmaf(w, g, u0[l]);
                     u1[l] += w;
                 }
             }
+            // the 16 warp sums by recursive halving: at each level a lane keeps half of its values
+            // (chosen by one lane bit) and adds its partner's copy of them; 16 shuffles instead of 80
+            float v[16];
 #pragma unroll
             for (int l = 0; l < 8; ++l) {
+                v[l] = u0[l];
+                v[8 + l] = u1[l];
+            }
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    u0[l] += __shfl_xor_sync(0xffffffffu, u0[l], o);
-                    u1[l] += __shfl_xor_sync(0xffffffffu, u1[l], o);
+            for (int o = 16, n = 8; o > 1; o >>= 1, n >>= 1) {
+                const bool up = lane & o;
+#pragma unroll
+                for (int j = 0; j < n; ++j) {
+                    const float keep = up ? v[j + n] : v[j], give = up ? v[j] : v[j + n];
+                    v[j] = keep + __shfl_xor_sync(0xffffffffu, give, o);
                 }
             }
-            if (lane == 0)
-#pragma unroll
-                for (int l = 0; l < 8; ++l) {
-                    s_part[0][warp][lh + l] = u0[l];
-                    s_part[1][warp][lh + l] = u1[l];
-                }
+            v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+            // lane holds value 8 b4 + 4 b3 + 2 b2 + b1 (b_i its lane bits): (S0 or S1, lead)
+            const int idx = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+            if (!(lane & 1)) s_part[idx >> 3][warp][lh + (idx & 7)] = v[0];
         }
         __syncthreads();
-        if (tid < 2 * CB_LB) {
-            const int k = tid / CB_LB, l = tid % CB_LB;
+        if (tid < 2 * NLB) {
+            const int k = tid / NLB, l = tid % NLB;
             float v = 0.f;
             for (int w = 0; w < CB_THREADS / 32; ++w) v += s_part[k][w][l];
             s_sum[k][l] = v;
@@ -763,25 +774,26 @@ void launch_contract_band(cudaStream_t s, const HeartDev &h, const float *d_Wm, 
                           int4 *d_cinfo) {
     static bool attr = false;
     if (!attr) {
-        EKG_CUDA(cudaFuncSetAttribute(k_contract_band<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CB_SMEM));
-        EKG_CUDA(cudaFuncSetAttribute(k_contract_band<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CB_SMEM));
-        EKG_CUDA(cudaFuncSetAttribute(k_contract_band<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CB_SMEM));
-        EKG_CUDA(cudaFuncSetAttribute(k_contract_band<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CB_SMEM));
+        EKG_CUDA(cudaFuncSetAttribute(k_contract_band<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cb_smem_bytes(4)));
+        EKG_CUDA(cudaFuncSetAttribute(k_contract_band<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cb_smem_bytes(8)));
+        EKG_CUDA(cudaFuncSetAttribute(k_contract_band<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cb_smem_bytes(12)));
+        EKG_CUDA(cudaFuncSetAttribute(k_contract_band<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cb_smem_bytes(16)));
         attr = true;
     }
-    const int nlb = (h.nleads + CB_LB - 1) / CB_LB;
+    // leads per block: all of them rounded up to a multiple of 4 when there are at most 16, else
+    // blocks of 16
+    const int nlr = h.nleads > CB_LB ? CB_LB : (h.nleads + 3) / 4 * 4;
+    const int nlb = (h.nleads + nlr - 1) / nlr;
     dim3 grid((unsigned)h.nchunks, (unsigned)(n_sims * nlb));
-    // leads per block rounded up to a multiple of 4 (one block when there are at most 16)
-    const int nlr = nlb > 1 ? 16 : (h.nleads + 3) / 4 * 4;
-    auto go = [&](auto kern) {
-        kern<<<grid, CB_THREADS, CB_SMEM, s>>>(h.steps, h.nleads, h.apad, h.nlayers, h.t_hilo.p, h.at_hilo.p, h.at.p,
+    auto go = [&](auto kern, int nl_block) {
+        kern<<<grid, CB_THREADS, cb_smem_bytes(nl_block), s>>>(h.steps, h.nleads, h.apad, h.nlayers, h.t_hilo.p, h.at_hilo.p, h.at.p,
                                               h.chunk_a0.p, h.chunk_a1.p, h.chunk_layer.p, d_Wm, wrows, d_W0,
                                               d_layer_k, d_layer_c, h.nchunks, nlb, d_band, d_csum, d_cinfo);
     };
-    if (nlr == 4) go(k_contract_band<4>);
-    else if (nlr == 8) go(k_contract_band<8>);
-    else if (nlr == 12) go(k_contract_band<12>);
-    else go(k_contract_band<16>);
+    if (nlr == 4) go(k_contract_band<4>, 4);
+    else if (nlr == 8) go(k_contract_band<8>, 8);
+    else if (nlr == 12) go(k_contract_band<12>, 12);
+    else go(k_contract_band<16>, 16);
     EKG_CUDA(cudaGetLastError());
 }
 
