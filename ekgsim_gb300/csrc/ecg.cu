@@ -501,20 +501,34 @@ __global__ void __launch_bounds__(512) k_reduce_chunks(
         B = make_float2(__shfl_sync(0xffffffffu, B.x, 0), __shfl_sync(0xffffffffu, B.y, 0));
         const float e0 = kc.z * ex2_approx(-kc.y * ((th.x - th0.x) + (th.y - th0.y)));
         float2 sum = ff_add(ff_mul(make_float2(e0, 0.f), A), ff_mul(make_float2(kc.w, 0.f), B));
-        // the chunks after the prefix, per step
-        for (int c = clo; c < c1; ++c) {
-            const int4 in = ci[c];
-            if (in.x >= t0 + 32) break;
-            if (!valid || t < in.x) continue;
-            float v;
-            if (t < in.y) {
-                v = bd[(size_t)c * nleads * steps + t];
-            } else {
-                const float2 sv = cs[(size_t)c * nleads + l];
-                const float e = kc.z * ex2_approx(-kc.y * ((th.x - __int_as_float(in.z)) + th.y));
-                v = fmaf(e, sv.x, kc.w * sv.y);
+        // the chunks after the prefix, per step; the lanes load 32 chunks' run limits and steady sums
+        // at once (one coalesced load each) and pass them round by shuffles
+        bool done = false;
+        for (int cb = clo; cb < c1 && !done; cb += 32) {
+            const int cc = cb + lane;
+            const int4 mine = cc < c1 ? ci[cc] : make_int4(steps, steps, 0, 0);
+            const float2 smine = cc < c1 ? cs[(size_t)cc * nleads + l] : make_float2(0.f, 0.f);
+            const int nj = min(32, c1 - cb);
+#pragma unroll 4
+            for (int j = 0; j < nj; ++j) {
+                const int tb0 = __shfl_sync(0xffffffffu, mine.x, j), tb1 = __shfl_sync(0xffffffffu, mine.y, j);
+                const float am = __int_as_float(__shfl_sync(0xffffffffu, mine.z, j));
+                const float s0 = __shfl_sync(0xffffffffu, smine.x, j), s1 = __shfl_sync(0xffffffffu, smine.y, j);
+                if (tb0 >= t0 + 32) {  // this chunk and every later one are zero over the tile
+                    done = true;
+                    break;
+                }
+                if (valid && t >= tb0) {
+                    float v;
+                    if (t < tb1) {
+                        v = bd[(size_t)(cb + j) * nleads * steps + t];
+                    } else {
+                        const float e = kc.z * ex2_approx(-kc.y * ((th.x - am) + th.y));
+                        v = fmaf(e, s0, kc.w * s1);
+                    }
+                    sum = ff_add_f(sum, v);
+                }
             }
-            sum = ff_add_f(sum, v);
         }
         if (valid) acc = fma(ff_to_double(sum), F[((size_t)s * nl + L) * steps + t], acc);
     }
