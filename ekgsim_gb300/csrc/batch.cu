@@ -1204,10 +1204,12 @@ __global__ void __launch_bounds__(128) k_sim_lead_field(
 // shared memory, LF_ROWS rows per thread sharing each voxel's loads and tests, the stage bounding-box
 // test -- instead of one thread per (AP, simulation), whose warps diverge over the APs' voxel
 // counts.  Row = s * nmove + l; lead positions FP64 [S][lead_stride][3] made relative to the voxel
-// centre in FP64 before the FP32 cast.  The band contraction scales W by exp(k5 at).
+// centre in FP64 before the FP32 cast.  The band contraction scales W by exp(k5 at).  With fewer
+// rows the block's warps split the stage's four 8-AP chunks: ksplit groups of LF_THREADS / ksplit
+// threads, group g taking chunks g, g + ksplit, ... of the item's stage.
 template <bool DIAG>
 __global__ void __launch_bounds__(LF_THREADS, 8) k_sim_lead_field_rows(
-    int nst, int ngr, int *__restrict__ work, InteriorField ic, const int64_t *__restrict__ a_vox_begin,
+    int nst, int ngr, int ksplit, int *__restrict__ work, InteriorField ic, const int64_t *__restrict__ a_vox_begin,
     const float4 *__restrict__ vox_pos, const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs,
     const double *__restrict__ leads, int lead_stride, double cz, double cy, double cx, int nmove, int n_sims,
     int nleads, int64_t apad, const int32_t *__restrict__ stage_order, const float4 *__restrict__ stage_box,
@@ -1243,7 +1245,8 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_sim_lead_field_rows(
         if (tid < BST / 8 + 1) s_vb[tid] = (int)a_vox_begin[(int64_t)st * BST + tid * 8] - (staged ? v0 : 0);
         __syncthreads();
         const float4 *vp = staged ? s_vpos : vox_pos, *vo = staged ? s_vout : vox_out;
-        const int rb = (item % ngr) * (LF_THREADS * LF_ROWS) + tid * LF_ROWS;
+        const int gthreads = LF_THREADS / ksplit, kg = tid / gthreads;
+        const int rb = (item % ngr) * (gthreads * LF_ROWS) + (tid % gthreads) * LF_ROWS;
         const int nr = rb < rows_used ? min(LF_ROWS, rows_used - rb) : 0;  // the rest repeat the last row
         float4 r[LF_ROWS];
         bool far_all = true;
@@ -1263,7 +1266,7 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_sim_lead_field_rows(
         far_all = __all_sync(0xffffffffu, far_all);
         if (nr == 0) continue;
 #pragma unroll 1
-        for (int kc = 0; kc < BST / 8; ++kc) {
+        for (int kc = kg; kc < BST / 8; kc += ksplit) {
             if (far_all) chunk_w<DIAG, LF_ROWS, true>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
             else chunk_w<DIAG, LF_ROWS, false>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
 #pragma unroll
@@ -1288,18 +1291,21 @@ void launch_sim_lead_field_rows(cudaStream_t s, const HeartDev &h, const double 
     ic.B1 = h.interior_c[3];
     ic.B2 = h.interior_c[4];
     const int rows_used = n_sims * nmove;
-    const int ngr = (rows_used + LF_THREADS * LF_ROWS - 1) / (LF_THREADS * LF_ROWS);
+    // warps split a stage's chunks when the rows fill fewer than all of them
+    const int ksplit = rows_used <= 32 * LF_ROWS ? 4 : (rows_used <= 64 * LF_ROWS ? 2 : 1);
+    const int grows = LF_THREADS / ksplit * LF_ROWS;
+    const int ngr = (rows_used + grows - 1) / grows;
     const int nst = (int)(h.apad / BST);
     const int items = nst * ngr;
     const int grid = std::max(1, std::min(items, sm_count * 8));
     EKG_CUDA(cudaMemsetAsync(work, 0, sizeof(int), s));
     if (h.nhood == EKG_NHOOD_3D4)
         k_sim_lead_field_rows<true><<<grid, LF_THREADS, 0, s>>>(
-            nst, ngr, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, d_leads, lead_stride,
+            nst, ngr, ksplit, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, d_leads, lead_stride,
             h.centre[0], h.centre[1], h.centre[2], nmove, n_sims, h.nleads, h.apad, h.stage_order.p, h.stage_box.p, W);
     else
         k_sim_lead_field_rows<false><<<grid, LF_THREADS, 0, s>>>(
-            nst, ngr, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, d_leads, lead_stride,
+            nst, ngr, ksplit, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, d_leads, lead_stride,
             h.centre[0], h.centre[1], h.centre[2], nmove, n_sims, h.nleads, h.apad, h.stage_order.p, h.stage_box.p, W);
     EKG_CUDA(cudaGetLastError());
 }

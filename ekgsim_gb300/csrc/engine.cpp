@@ -521,7 +521,7 @@ void ensure_eval_capacity(ekg_heart *h, int n_sims) {
 }
 // moved rows (simulations x moved leads) from which the per-simulation form evaluates their field
 // with the persistent row kernel (below: one thread per (AP, simulation))
-constexpr int SIM_ROWS_PERSISTENT = 128;
+constexpr int SIM_ROWS_PERSISTENT = 32;
 // whether the per-simulation form contracts with the band form (compact outputs)
 bool band_contraction(const ekg_heart *h) {
     return h->eng->contract == EKG_CONTRACT_BAND && h->dev.chunk_max <= CONTRACT_BAND_CAP;
