@@ -391,9 +391,9 @@ constexpr int BST = 32;     // APs per stage
 constexpr int LF_ROWS = 4;  // rows per thread
 constexpr int LF_VCAP = 256;  // voxel records of a stage staged in shared memory
 static_assert(LF_THREADS >= BST + BST / 8 + 1, "the stage tables are loaded one entry per thread");
-template <int N, bool DIAG>
+template <bool DIAG, int ROWS, bool SPLIT, bool K0>
 __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
-    int nst, int ngr, int *__restrict__ work, InteriorField ic, const int64_t *__restrict__ a_vox_begin,
+    int nlog, int nst, int ngr, int ksplit_arg, int *__restrict__ work, InteriorField ic, const int64_t *__restrict__ a_vox_begin,
     const float4 *__restrict__ vox_pos, const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs,
     const float2 *__restrict__ at_hilo, const int32_t *__restrict__ a_layer, const float *__restrict__ k5l, int nl,
     const float4 *__restrict__ hconst, const float4 *__restrict__ lrel, int nmove, int n_sims,
@@ -443,15 +443,21 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
         }
         __syncthreads();
         const float4 *vp = staged ? s_vpos : vox_pos, *vo = staged ? s_vout : vox_out;
-        const int rb = (item % ngr) * (LF_THREADS * LF_ROWS) + tid * LF_ROWS;
+        // with fewer rows than threads x ROWS the warps split the stage's four 8-AP chunks:
+        // ksplit groups of LF_THREADS / ksplit threads over the same rows, group g taking chunks
+        // g, g + ksplit, ...
+        const int ksplit = SPLIT ? ksplit_arg : 1;  // the unsplit instance compiles without the split
+        const int gthreads = LF_THREADS / ksplit, kg = tid / gthreads;
+        const int rb = (item % ngr) * (gthreads * ROWS) + (tid % gthreads) * ROWS;
+        const bool active = rb < rows_used;  // every thread stays for the barriers below
         // whether every voxel of the stage is far from every lead of the warp (squared distance from
         // the lead to the stage's bounding box; a margin of one cell over the closed form's bound)
         bool far_all = true;
-        if (rb < rows_used) {
+        if (active) {
             const float4 lo = stage_box[2 * (size_t)st], hi = stage_box[2 * (size_t)st + 1];
-            const int nr0 = min(LF_ROWS, rows_used - rb);
+            const int nr0 = min(ROWS, rows_used - rb);
 #pragma unroll
-            for (int q = 0; q < LF_ROWS; ++q) {
+            for (int q = 0; q < ROWS; ++q) {
                 if (q >= nr0) break;
                 const float4 r = lrel[rb + q];
                 const float dz = fmaxf(fmaxf(lo.x - r.x, r.x - hi.x), 0.f);
@@ -461,28 +467,27 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
             }
         }
         far_all = __all_sync(0xffffffffu, far_all);
-        if (rb >= rows_used) continue;
-        const int nr = min(LF_ROWS, rows_used - rb);  // rows of this thread; the rest repeat its last row
-        float k5[LF_ROWS], S0[LF_ROWS], S1[LF_ROWS];
+        const int nr = active ? min(ROWS, rows_used - rb) : 0;  // rows of this thread; the rest repeat its last row
+        float k5[ROWS], S0[ROWS], S1[ROWS];
 #pragma unroll
-        for (int q = 0; q < LF_ROWS; ++q) {
-            const int row = rb + min(q, nr - 1);
+        for (int q = 0; q < ROWS; ++q) {
+            const int row = active ? rb + min(q, nr - 1) : 0;
             k5[q] = k5l[(size_t)(row / nmove) * nl + L];
             S0[q] = S1[q] = 0.f;
         }
         const int kt = st >> 1;
 #pragma unroll 1
-        for (int kc = 0; kc < BST / 8; ++kc) {
+        for (int kc = active ? kg : BST / 8; kc < BST / 8; kc += ksplit) {
             {
-                float4 r[LF_ROWS];
+                float4 r[ROWS];
 #pragma unroll
-                for (int q = 0; q < LF_ROWS; ++q) r[q] = lrel[rb + min(q, nr - 1)];
-                if (far_all) chunk_w<DIAG, LF_ROWS, true>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
-                else chunk_w<DIAG, LF_ROWS, false>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
+                for (int q = 0; q < ROWS; ++q) r[q] = lrel[rb + min(q, nr - 1)];
+                if (far_all) chunk_w<DIAG, ROWS, true>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
+                else chunk_w<DIAG, ROWS, false>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
             }
             const int col = (st & 1) * (BST / 8) + kc;  // 8-AP column within the 64-AP tile
 #pragma unroll
-            for (int q = 0; q < LF_ROWS; ++q) {
+            for (int q = 0; q < ROWS; ++q) {
                 if (q >= nr) break;
                 float wv[8];
 #pragma unroll
@@ -496,11 +501,11 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
                 split2(wv[4], wv[5], hv.z, lv.z);
                 split2(wv[6], wv[7], hv.w, lv.w);
                 const int row = rb + q;
-                const int nt = row / N, n = row % N;
+                const int nt = row >> nlog, n = row & ((1 << nlog) - 1);
                 const size_t tile = ((size_t)nt * nkt + kt) * 2;
-                const size_t off = (size_t)(col * (N / 8) + n / 8) * 128 + (n % 8) * 16;
-                *reinterpret_cast<uint4 *>(Bt + tile * (N * 128) + off) = hv;
-                *reinterpret_cast<uint4 *>(Bt + (tile + 1) * (N * 128) + off) = lv;
+                const size_t off = ((size_t)(col << (nlog - 3)) + n / 8) * 128 + (n % 8) * 16;
+                *reinterpret_cast<uint4 *>(Bt + (tile << (nlog + 7)) + off) = hv;
+                *reinterpret_cast<uint4 *>(Bt + ((tile + 1) << (nlog + 7)) + off) = lv;
                 float z0 = 0.f, z1 = 0.f;
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
@@ -509,7 +514,7 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
                 }
                 S0[q] += z0;
                 S1[q] += z1;
-                if (P2) {
+                if (K0 && P2) {
                     // the unscaled field sums of the 8 APs (the resting-potential term, k_k0_moved)
                     float z2 = 0.f;
 #pragma unroll
@@ -520,9 +525,28 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
             }
         }
         const int ne = nent[L];
-        if (ne > 0 && st < esplit[L * MAXE + ne - 1])  // the last entry's steady prefix is the longest
+        const bool steady = ne > 0 && st < esplit[L * MAXE + ne - 1];  // the last entry's steady prefix is the longest
+        if (SPLIT && steady && ksplit > 1) {
+            // the other groups hand their steady sums to group 0 through the staging area (free once
+            // every group is past the voxel loop), added in group order
+            float2 *s_p1 = reinterpret_cast<float2 *>(s_vpos);  // [LF_THREADS][ROWS]
+            __syncthreads();
+            if (kg > 0 && active)
 #pragma unroll
-            for (int q = 0; q < LF_ROWS; ++q) {
+                for (int q = 0; q < ROWS; ++q) s_p1[tid * ROWS + q] = make_float2(S0[q], S1[q]);
+            __syncthreads();
+            if (kg == 0 && active)
+                for (int g = 1; g < ksplit; ++g)
+#pragma unroll
+                    for (int q = 0; q < ROWS; ++q) {
+                        const float2 v = s_p1[(g * gthreads + tid) * ROWS + q];
+                        S0[q] += v.x;
+                        S1[q] += v.y;
+                    }
+        }
+        if (steady && kg == 0 && active)
+#pragma unroll
+            for (int q = 0; q < ROWS; ++q) {
                 if (q >= nr) break;
                 const int row = rb + q, s = row / nmove, l = row % nmove;
                 P1[(size_t)st * rows_used + (size_t)l * n_sims + s] = make_float2(S0[q], S1[q]);
@@ -530,12 +554,14 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_batch_lead_field(
     }
 }
 
-// Small batches (up to SMALL_SIMS simulations): one thread per (AP, simulation), so the work spreads
+// Small batches (up to SMALL_SIMS simulations; above that the persistent kernel with one row per
+// thread is faster, measured at 160^3: 6 simulations 0.119 against 0.132 ms per pass, 16
+// simulations 0.128 against 0.237): one thread per (AP, simulation), so the work spreads
 // over the heart instead of over simulations.  A block is four 32-AP stages of one simulation, one
 // per warp; eight consecutive lanes are one 8-AP chunk and write its BF16 hi/lo row segment two
 // bytes each.  The steady sums of a stage are reduced by a shuffle butterfly within its warp.
 // Same outputs as k_batch_lead_field.
-constexpr int SMALL_SIMS = 16;
+constexpr int SMALL_SIMS = 4;
 template <int N, bool DIAG>
 __global__ void __launch_bounds__(128) k_batch_lead_field_small(
     int nst, InteriorField ic, const int64_t *__restrict__ a_vox_begin, const float4 *__restrict__ vox_pos,
@@ -1207,7 +1233,7 @@ __global__ void __launch_bounds__(128) k_sim_lead_field(
 // centre in FP64 before the FP32 cast.  The band contraction scales W by exp(k5 at).  With fewer
 // rows the block's warps split the stage's four 8-AP chunks: ksplit groups of LF_THREADS / ksplit
 // threads, group g taking chunks g, g + ksplit, ... of the item's stage.
-template <bool DIAG>
+template <bool DIAG, int ROWS>
 __global__ void __launch_bounds__(LF_THREADS, 8) k_sim_lead_field_rows(
     int nst, int ngr, int ksplit, int *__restrict__ work, InteriorField ic, const int64_t *__restrict__ a_vox_begin,
     const float4 *__restrict__ vox_pos, const float4 *__restrict__ vox_out, int nnb, const int8_t *__restrict__ difs,
@@ -1215,7 +1241,7 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_sim_lead_field_rows(
     int nleads, int64_t apad, const int32_t *__restrict__ stage_order, const float4 *__restrict__ stage_box,
     float *__restrict__ W) {
     __shared__ float s_d[26 * 4];
-    __shared__ float s_w[LF_ROWS][8][LF_THREADS];
+    __shared__ float s_w[LF_ROWS][8][LF_THREADS];  // rows [0, ROWS) used
     __shared__ int s_vb[BST / 8 + 1];
     __shared__ float4 s_vpos[LF_VCAP], s_vout[LF_VCAP];
     __shared__ int s_item;
@@ -1246,14 +1272,14 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_sim_lead_field_rows(
         __syncthreads();
         const float4 *vp = staged ? s_vpos : vox_pos, *vo = staged ? s_vout : vox_out;
         const int gthreads = LF_THREADS / ksplit, kg = tid / gthreads;
-        const int rb = (item % ngr) * (gthreads * LF_ROWS) + (tid % gthreads) * LF_ROWS;
-        const int nr = rb < rows_used ? min(LF_ROWS, rows_used - rb) : 0;  // the rest repeat the last row
-        float4 r[LF_ROWS];
+        const int rb = (item % ngr) * (gthreads * ROWS) + (tid % gthreads) * ROWS;
+        const int nr = rb < rows_used ? min(ROWS, rows_used - rb) : 0;  // the rest repeat the last row
+        float4 r[ROWS];
         bool far_all = true;
         if (nr > 0) {
             const float4 lo = stage_box[2 * (size_t)st], hi = stage_box[2 * (size_t)st + 1];
 #pragma unroll
-            for (int q = 0; q < LF_ROWS; ++q) {
+            for (int q = 0; q < ROWS; ++q) {
                 const int row = rb + min(q, nr - 1);
                 const double *p = leads + ((size_t)(row / nmove) * lead_stride + row % nmove) * 3;
                 r[q] = make_float4((float)(p[0] - cz), (float)(p[1] - cy), (float)(p[2] - cx), 0.f);
@@ -1267,10 +1293,10 @@ __global__ void __launch_bounds__(LF_THREADS, 8) k_sim_lead_field_rows(
         if (nr == 0) continue;
 #pragma unroll 1
         for (int kc = kg; kc < BST / 8; kc += ksplit) {
-            if (far_all) chunk_w<DIAG, LF_ROWS, true>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
-            else chunk_w<DIAG, LF_ROWS, false>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
+            if (far_all) chunk_w<DIAG, ROWS, true>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
+            else chunk_w<DIAG, ROWS, false>(s_vb[kc], s_vb[kc + 1], vp, vo, r, nnb, s_d, ic, s_w, tid);
 #pragma unroll
-            for (int q = 0; q < LF_ROWS; ++q) {
+            for (int q = 0; q < ROWS; ++q) {
                 if (q >= nr) break;
                 const int row = rb + q;
                 float4 *dst = reinterpret_cast<float4 *>(W + ((size_t)(row / nmove) * nleads + row % nmove) * apad +
@@ -1291,22 +1317,30 @@ void launch_sim_lead_field_rows(cudaStream_t s, const HeartDev &h, const double 
     ic.B1 = h.interior_c[3];
     ic.B2 = h.interior_c[4];
     const int rows_used = n_sims * nmove;
-    // warps split a stage's chunks when the rows fill fewer than all of them
-    const int ksplit = rows_used <= 32 * LF_ROWS ? 4 : (rows_used <= 64 * LF_ROWS ? 2 : 1);
-    const int grows = LF_THREADS / ksplit * LF_ROWS;
+    int rows_t = 4, ksplit = 1;  // the operand kernel's layouts (rows per thread, chunk split)
+    if (rows_used <= 32) rows_t = 1, ksplit = 4;
+    else if (rows_used <= 64) rows_t = 1, ksplit = 2;
+    else if (rows_used <= 128) rows_t = 1, ksplit = 1;
+    else if (rows_used <= 256) rows_t = 4, ksplit = 2;
+    const int grows = LF_THREADS / ksplit * rows_t;
     const int ngr = (rows_used + grows - 1) / grows;
     const int nst = (int)(h.apad / BST);
     const int items = nst * ngr;
     const int grid = std::max(1, std::min(items, sm_count * 8));
     EKG_CUDA(cudaMemsetAsync(work, 0, sizeof(int), s));
-    if (h.nhood == EKG_NHOOD_3D4)
-        k_sim_lead_field_rows<true><<<grid, LF_THREADS, 0, s>>>(
-            nst, ngr, ksplit, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, d_leads, lead_stride,
-            h.centre[0], h.centre[1], h.centre[2], nmove, n_sims, h.nleads, h.apad, h.stage_order.p, h.stage_box.p, W);
-    else
-        k_sim_lead_field_rows<false><<<grid, LF_THREADS, 0, s>>>(
-            nst, ngr, ksplit, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, d_leads, lead_stride,
-            h.centre[0], h.centre[1], h.centre[2], nmove, n_sims, h.nleads, h.apad, h.stage_order.p, h.stage_box.p, W);
+    auto go = [&](auto kern) {
+        kern<<<grid, LF_THREADS, 0, s>>>(nst, ngr, ksplit, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb,
+                                         h.difs.p, d_leads, lead_stride, h.centre[0], h.centre[1], h.centre[2], nmove,
+                                         n_sims, h.nleads, h.apad, h.stage_order.p, h.stage_box.p, W);
+    };
+    const bool diag = h.nhood == EKG_NHOOD_3D4;
+    if (rows_t == 1) {
+        if (diag) go(k_sim_lead_field_rows<true, 1>);
+        else go(k_sim_lead_field_rows<false, 1>);
+    } else {
+        if (diag) go(k_sim_lead_field_rows<true, 4>);
+        else go(k_sim_lead_field_rows<false, 4>);
+    }
     EKG_CUDA(cudaGetLastError());
 }
 
@@ -1339,7 +1373,6 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, b
                              const float4 *hconst, const float4 *lrel, int nmove, int n_sims, const BandArgs &B,
                              uint8_t *Bt, int *work, int sm_count) {
     const int rows_used = n_sims * nmove;
-    const int ngr = (rows_used + LF_THREADS * LF_ROWS - 1) / (LF_THREADS * LF_ROWS);
     const int nst = (int)(h.apad / BST);
     const bool diag = h.nhood == EKG_NHOOD_3D4;
     InteriorField ic;
@@ -1348,41 +1381,63 @@ void launch_batch_lead_field(cudaStream_t s, const HeartDev &h, int tile_rows, b
     ic.B0 = h.interior_c[2];
     ic.B1 = h.interior_c[3];
     ic.B2 = h.interior_c[4];
-    EKG_CUDA(cudaMemsetAsync(work, 0, sizeof(int), s));
-#define EKG_LF(NN, DG)                                                                                            \
-    do {                                                                                                          \
-        if (small) {                                                                                              \
-            dim3 g((unsigned)((nst * BST + 127) / 128), (unsigned)n_sims);                                         \
-            k_batch_lead_field_small<NN, DG><<<g, 128, 0, s>>>(                                                   \
-                nst, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p,    \
-                k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, Bt, B.P1, B.P2);           \
-            break;                                                                                                \
-        }                                                                                                         \
-        static int per_sm = 0;                                                                                    \
-        if (!per_sm)                                                                                              \
-            EKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_lead_field<NN, DG>,           \
-                                                                   LF_THREADS, 0));                               \
-        const int bps = blocks_per_sm > 0 ? std::min(blocks_per_sm, std::max(1, per_sm)) : std::max(1, per_sm);   \
-        const int grid = std::max(1, std::min(nst * ngr, bps * sm_count));                                       \
-        k_batch_lead_field<NN, DG><<<grid, LF_THREADS, 0, s>>>(                                                   \
-            nst, ngr, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p, \
-            k5l, h.nlayers, hconst, lrel, nmove, n_sims, B.tref, B.nent, B.esplit, h.stage_order.p, h.stage_box.p,  \
-            Bt, B.P1, B.P2);                                                                                      \
-    } while (0)
-    switch (tile_rows) {
-    case 32:
-        if (diag) EKG_LF(32, true);
-        else EKG_LF(32, false);
-        break;
-    case 128:
-        if (diag) EKG_LF(128, true);
-        else EKG_LF(128, false);
-        break;
-    default:
-        if (diag) EKG_LF(256, true);
-        else EKG_LF(256, false);
+    const int nlog = tile_rows == 32 ? 5 : (tile_rows == 128 ? 7 : 8);
+    if (small) {
+        dim3 g((unsigned)((nst * BST + 127) / 128), (unsigned)n_sims);
+#define EKG_LFS(NN, DG)                                                                                            \
+    k_batch_lead_field_small<NN, DG><<<g, 128, 0, s>>>(nst, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p, h.nnb,  \
+                                                       h.difs.p, h.at_hilo.p, h.a_layer.p, k5l, h.nlayers, hconst,  \
+                                                       lrel, nmove, n_sims, B.tref, B.nent, B.esplit, Bt, B.P1, B.P2)
+        if (tile_rows == 32) {
+            if (diag) EKG_LFS(32, true);
+            else EKG_LFS(32, false);
+        } else if (tile_rows == 128) {
+            if (diag) EKG_LFS(128, true);
+            else EKG_LFS(128, false);
+        } else {
+            if (diag) EKG_LFS(256, true);
+            else EKG_LFS(256, false);
+        }
+#undef EKG_LFS
+        EKG_CUDA(cudaGetLastError());
+        return;
     }
-#undef EKG_LF
+    // rows per thread and chunk split by the rows: a warp covers 32 lanes x rows, so few rows take
+    // one row per thread, and the block's warps split a stage's four 8-AP chunks when the rows fill
+    // fewer than all of them (measured at 160^3 against four rows per thread and four groups: 32
+    // simulations x 2 moved leads 0.208 against 0.288 ms per pass, 128 simulations 0.457 against 0.508)
+    int rows_t = 4, ksplit = 1;
+    if (rows_used <= 32) rows_t = 1, ksplit = 4;
+    else if (rows_used <= 64) rows_t = 1, ksplit = 2;
+    else if (rows_used <= 128) rows_t = 1, ksplit = 1;
+    else if (rows_used <= 256) rows_t = 4, ksplit = 2;
+    const int grows = LF_THREADS / ksplit * rows_t;
+    const int ngr = (rows_used + grows - 1) / grows;
+    EKG_CUDA(cudaMemsetAsync(work, 0, sizeof(int), s));
+    auto go = [&](auto kern) {
+        static int per_sm = 0;
+        if (!per_sm) EKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, LF_THREADS, 0));
+        const int bps = blocks_per_sm > 0 ? std::min(blocks_per_sm, std::max(1, per_sm)) : std::max(1, per_sm);
+        const int grid = std::max(1, std::min(nst * ngr, bps * sm_count));
+        kern<<<grid, LF_THREADS, 0, s>>>(nlog, nst, ngr, ksplit, work, ic, h.a_vox_begin.p, h.vox_pos.p, h.vox_out.p,
+                                         h.nnb, h.difs.p, h.at_hilo.p, h.a_layer.p, k5l, h.nlayers, hconst, lrel, nmove,
+                                         n_sims, B.tref, B.nent, B.esplit, h.stage_order.p, h.stage_box.p, Bt, B.P1,
+                                         B.P2);
+    };
+    // the resting-potential sums (P2) only where a pass needs them: the unsplit instance is compiled
+    // with and without them
+    const bool k0 = B.P2 != nullptr;
+    if (diag) {
+        if (rows_t == 1) go(k_batch_lead_field<true, 1, true, true>);
+        else if (ksplit > 1) go(k_batch_lead_field<true, 4, true, true>);
+        else if (k0) go(k_batch_lead_field<true, 4, false, true>);
+        else go(k_batch_lead_field<true, 4, false, false>);
+    } else {
+        if (rows_t == 1) go(k_batch_lead_field<false, 1, true, true>);
+        else if (ksplit > 1) go(k_batch_lead_field<false, 4, true, true>);
+        else if (k0) go(k_batch_lead_field<false, 4, false, true>);
+        else go(k_batch_lead_field<false, 4, false, false>);
+    }
     EKG_CUDA(cudaGetLastError());
 }
 
