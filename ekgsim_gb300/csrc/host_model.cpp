@@ -460,15 +460,23 @@ struct AP {
     double at = 0;
     double operator()(double t) const { return wohlfart(k, t - at); }
 };
+// The samples of a border AP at t = 0 .. 699 ms (the interpolation evaluator's curve) and its
+// apd90, computed once per distinct border AP (the mid AP borders both segments).
+struct Curve {
+    double k[9];
+    double y[701];
+    double apd = -1.0;
+};
 // WohlfartPlus::apd90 (simlib/Wohlfart.h:206-223): the last downward crossing of k0 + k2/10 among
 // the samples at 0 .. 999 ms, found by scanning from the end (the samples after it are the only
-// ones that decide that it is the last)
-double apd90(const double *k) {
-    const RepolConst rc = repol_const(k);
+// ones that decide that it is the last).  The samples below 700 ms are the curve's (the same
+// wohlfart_rc arguments, so the same doubles); the others are evaluated here.
+double apd90(const double *k, const RepolConst &rc, const double *y) {
     const double target = k[0] + k[2] * 0.1;
-    double next = wohlfart_rc(k, rc, 999.0);
+    auto sample = [&](int i) { return i < 700 ? y[i] : wohlfart_rc(k, rc, (double)i); };
+    double next = sample(999);
     for (int i = 999; i >= 1; --i) {
-        const double prev = wohlfart_rc(k, rc, (double)(i - 1));
+        const double prev = sample(i - 1);
         if (prev > target && next <= target) {
             const double a = i - 1, wa = prev - target, b = i, wb = target - next;
             return (a * wa + b * wb) / (wa + wb);
@@ -476,6 +484,14 @@ double apd90(const double *k) {
         next = prev;
     }
     return -1.0;
+}
+// the curve of a border AP (activation time 0)
+void make_curve(const double *k, Curve &c) {
+    std::copy(k, k + 9, c.k);
+    const RepolConst rc = repol_const(k);
+    for (size_t i = 0; i < 700; ++i) c.y[i] = wohlfart_rc(k, rc, (double)i);
+    c.y[700] = c.y[699];  // the reference reads one past its 700-sample buffer here; hold the last value
+    c.apd = apd90(k, rc, c.y);
 }
 // WohlfartInterpolationEvaluator (sim.cpp:91-313): connectors between two border APs, points
 // on them at a ratio, and the sum of squared distances of an AP from those points.
@@ -485,18 +501,11 @@ struct Evaluator {
     };
     std::vector<Conn> conns;
     std::vector<double> pts;
-    void set_border(const AP &a1, const AP &a2) {
+    void set_border(const Curve &c1, const Curve &c2) {
         conns.clear();
         const size_t numPoints = 15, startX = 10;
-        const double apd1 = apd90(a1.k), apd2 = apd90(a2.k);
-        double y1[701], y2[701];
-        const RepolConst rc1 = repol_const(a1.k), rc2 = repol_const(a2.k);
-        for (size_t i = 0; i < 700; ++i) {
-            y1[i] = wohlfart_rc(a1.k, rc1, (double)i - a1.at);
-            y2[i] = wohlfart_rc(a2.k, rc2, (double)i - a2.at);
-        }
-        y1[700] = y1[699];  // the reference reads one past its 700-sample buffer here; hold the last value
-        y2[700] = y2[699];
+        const double apd1 = c1.apd, apd2 = c2.apd;
+        const double *y1 = c1.y, *y2 = c2.y;
         const double xs = 0.1;
         const size_t e1 = apd1 < 0 ? 0 : std::min<size_t>(700, (size_t)std::ceil(apd1));
         const size_t e2 = apd2 < 0 ? 0 : std::min<size_t>(700, (size_t)std::ceil(apd2));
@@ -666,10 +675,22 @@ void layer_aps_run_fits(const LayerFitJob *jobs, size_t n) {
     AP d;
     std::copy(kd, kd + 9, d.k);
     // the interpolation evaluator (connectors between the two border APs) is rebuilt only when the
-    // border APs change from one fit to the next
+    // border APs change from one fit to the next; the border APs' curves come from a small cache
+    // (a simulation's mid AP borders both of its segments)
     Evaluator ev;
     double key[18];
     bool have = false;
+    Curve cache[4];
+    int ncache = 0, next_slot = 0;
+    auto curve = [&](const double *kk) -> const Curve & {
+        for (int i = 0; i < ncache; ++i)
+            if (std::memcmp(cache[i].k, kk, 72) == 0) return cache[i];
+        Curve &c = cache[next_slot];
+        next_slot = (next_slot + 1) % 4;
+        ncache = std::min(ncache + 1, 4);
+        make_curve(kk, c);
+        return c;
+    };
     for (size_t j = 0; j < n; ++j) {
         const LayerFit &f = jobs[j].fit;
         double *k = jobs[j].out_k;
@@ -677,7 +698,9 @@ void layer_aps_run_fits(const LayerFitJob *jobs, size_t n) {
         std::copy(k + 9 * (size_t)f.a, k + 9 * (size_t)f.a + 9, a.k);
         std::copy(k + 9 * (size_t)f.b, k + 9 * (size_t)f.b + 9, b.k);
         if (!have || std::memcmp(key, a.k, 72) != 0 || std::memcmp(key + 9, b.k, 72) != 0) {
-            ev.set_border(a, b);
+            const Curve &ca = curve(a.k);
+            const Curve &cb = curve(b.k);  // the cache holds four curves: this never evicts ca
+            ev.set_border(ca, cb);
             std::copy(a.k, a.k + 9, key);
             std::copy(b.k, b.k + 9, key + 9);
             have = true;
