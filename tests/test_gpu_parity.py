@@ -383,11 +383,13 @@ def test_batched_two_bases_free_k3(engine):
 
 
 def test_per_simulation_form_many_moved_rows(engine):
-    """k1 free per simulation (the per-simulation form) with 70 simulations: 280 moved rows (all four
-    leads displaced, some to within a few cells of the heart) and 140 (two leads), which the
-    persistent row kernel evaluates; the band contraction scales the rows and the chunk reduction
-    rebuilds the zero and steady runs.  A spread of results against the oracle, every result against
-    its single evaluation (one simulation: the per-AP lead-field kernel)."""
+    """k1 free per simulation (the per-simulation form): 70 simulations with 280 moved rows (all four
+    leads displaced, some to within a few cells of the heart) and 140 (two leads), 20 with 40 and 6
+    with 12, which the persistent row kernel evaluates in its layouts (four rows per thread, one row
+    per thread with the stage's chunks split over two and four warp groups); the band contraction
+    scales the rows and the chunk reduction rebuilds the zero and steady runs.  A spread of results
+    against the oracle, every result against its single evaluation (one simulation: the per-AP
+    lead-field kernel)."""
     from ekgsim_gb300.engine import Heart
     spec = synth.small_spec(40, n_leads=4, seed=37)
     steps = 300
@@ -406,22 +408,23 @@ def test_per_simulation_form_many_moved_rows(engine):
     genes[:, 15:] = rng.uniform(-50.0, 50.0, size=(n, 2 * spec.n_leads))
     at, layer = O.activation(grid, tm)
     nz = np.argwhere(layer > 0).astype(float) + 1.0  # bordered voxel coordinates (z, y, x)
-    for nmoved in (4, 2):
-        gs = genes.copy()
+    for nmoved, ns in ((4, 70), (2, 70), (2, 20), (2, 6)):
+        gs = genes[:ns].copy()
         gs[:, 15 + 2 * nmoved:] = 0.0
         lks = np.stack([O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, free, "endo-mid-epi",
                                     0.6, g[:15])[0] for g in gs])
         moveds = np.stack([O.move_leads(leads, g[15:].reshape(-1, 2)) for g in gs])
         assert not h.benchmark(lks, moveds, warmup=1, iters=1)["batched"]
-        mind = [min(np.sqrt(((nz - p) ** 2).sum(axis=1)).min() for p in m[:nmoved]) for m in moveds]
-        assert min(mind) < 20.0 and max(mind) > 21.0
+        if ns == n:
+            mind = [min(np.sqrt(((nz - p) ** 2).sum(axis=1)).min() for p in m[:nmoved]) for m in moveds]
+            assert min(mind) < 20.0 and max(mind) > 21.0
         crit_b, viol_b, ecg_b = h.eval_batch(gs, want_ecg=True)
-        for i in (0, 23, 47, 69):
+        for i in sorted({0, ns // 3, (2 * ns) // 3, ns - 1}):
             ref = O.run(layer, at, lks[i], moveds[i], "3D4", 0.0, float(steps), 1.0)
-            assert rel_l2(ecg_b[i], ref) <= ECG_TOL, (nmoved, i)
-        for i in range(n):
+            assert rel_l2(ecg_b[i], ref) <= ECG_TOL, (nmoved, ns, i)
+        for i in range(ns):
             c1, v1, e1 = h.eval_batch(gs[i:i + 1], want_ecg=True)
-            assert rel_l2(ecg_b[i], e1[0]) <= ECG_TOL, (nmoved, i)
+            assert rel_l2(ecg_b[i], e1[0]) <= ECG_TOL, (nmoved, ns, i)
             assert np.allclose(crit_b[i], c1[0], rtol=0, atol=1e-4) and viol_b[i] == v1[0]
     h.close()
 
@@ -890,6 +893,40 @@ def test_batched_form_resting_potential(engine):
                 c1, v1, e1 = h.eval_batch(gs[i:i + 1], want_ecg=True)
                 assert rel_l2(ecg_b[i], e1[0]) <= ECG_TOL, (k0s, i)
                 assert np.allclose(crit_b[i], c1[0], rtol=0, atol=1e-4) and viol_b[i] == v1[0]
+    h.close()
+
+
+def test_batched_operand_layouts(engine):
+    """The batched form's operand kernel picks its layout from the moved rows: the per-(AP, simulation)
+    kernel up to 4 simulations, one row per thread with a stage's chunks split over four, two or one
+    warp groups up to 128 rows, four rows per thread split over two groups up to 256, unsplit above.
+    The same gene vectors in batches of 3, 5, 30, 64, 100 and 130 simulations (2 moved leads) give
+    the same ECGs within the tolerance, and a spread of them matches the oracle."""
+    from ekgsim_gb300.engine import Heart
+    spec = synth.small_spec(40, n_leads=4, seed=43)
+    steps = 300
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(3, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    h = Heart.create(engine, grid, tm, leads, "3D4", 0.0, float(steps), 1.0)
+    h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8],
+               [t for t in synth.analytic_target(spec.n_leads, steps, 5)], mid_position=0.6)
+    genes = np.stack([synth.genes_for(spec, 500 + r, 0) for r in range(130)])
+    at, layer = O.activation(grid, tm)
+    first = None
+    for n in (3, 5, 30, 64, 100, 130):
+        lks = np.stack([O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8],
+                                    "endo-mid-epi", 0.6, g[:12])[0] for g in genes[:n]])
+        moveds = np.stack([O.move_leads(leads, g[12:].reshape(-1, 2)) for g in genes[:n]])
+        assert h.benchmark(lks, moveds, warmup=1, iters=1)["batched"]
+        crit, viol, ecg = h.eval_batch(genes[:n], want_ecg=True)
+        if first is None:
+            first = ecg[:3].copy()
+        for i in range(3):
+            assert rel_l2(ecg[i], first[i]) <= ECG_TOL, (n, i)
+        for i in sorted({0, n // 2, n - 1}):
+            ref = O.run(layer, at, lks[i], moveds[i], "3D4", 0.0, float(steps), 1.0)
+            assert rel_l2(ecg[i], ref) <= ECG_TOL, (n, i)
     h.close()
 
 
