@@ -54,12 +54,10 @@ __global__ void k_lead_field(int64_t apad, const int64_t *__restrict__ a_vox_beg
                              const double *__restrict__ leads, int nleads, int lead_stride,
                              float *__restrict__ W, int w_lead_stride) {
     __shared__ int8_t s_dif[26 * 3];
-    __shared__ float s_sout[3];
     if (threadIdx.x < nnb * 3) s_dif[threadIdx.x] = difs[threadIdx.x];
     __syncthreads();
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int l = blockIdx.y, s = blockIdx.z;
-    (void)s_sout;
     if (a >= apad || l >= nleads) return;
     const double *r = leads + ((size_t)s * lead_stride + l) * 3;
     const float rz = (float)r[0], ry = (float)r[1], rx = (float)r[2];
