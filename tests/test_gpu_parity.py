@@ -930,6 +930,59 @@ def test_batched_operand_layouts(engine):
     h.close()
 
 
+def test_cube_neighbourhood_moved_leads(engine):
+    """The general-neighbourhood instances of the moved-lead field kernels ("cube": 26 neighbours,
+    with its own closed-form interior coefficients): the batched form at 30 and 130 simulations
+    (one row per thread, four rows per thread) and the per-simulation form with k1 free at 20
+    simulations (the row kernel), against the oracle and against single evaluations."""
+    from ekgsim_gb300.engine import Heart
+    spec = synth.small_spec(32, n_leads=3, seed=47)
+    steps = 250
+    grid = synth.ellipsoid_heart(spec)
+    tm = synth.transfer_matrix(3, spec.delays)
+    leads = synth.leads(spec, np.random.Generator(np.random.PCG64(spec.seed)))[:, ::-1].copy()
+    h = Heart.create(engine, grid, tm, leads, "cube", 0.0, float(steps), 1.0)
+    target = [t for t in synth.analytic_target(spec.n_leads, steps, 3)]
+    at, layer = O.activation(grid, tm)
+    # batched form (k1, k4 shared)
+    h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, [5, 6, 7, 8], target, mid_position=0.6)
+    genes = np.stack([synth.genes_for(spec, 700 + r, 0) for r in range(130)])
+    first = None
+    for n in (30, 130):
+        lks = np.stack([O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, [5, 6, 7, 8],
+                                    "endo-mid-epi", 0.6, g[:12])[0] for g in genes[:n]])
+        moveds = np.stack([O.move_leads(leads, g[12:].reshape(-1, 2)) for g in genes[:n]])
+        assert h.benchmark(lks, moveds, warmup=1, iters=1)["batched"]
+        _, _, ecg = h.eval_batch(genes[:n], want_ecg=True)
+        if first is None:
+            first = ecg[:3].copy()
+        for i in range(3):
+            assert rel_l2(ecg[i], first[i]) <= ECG_TOL, (n, i)
+        for i in sorted({0, n // 2, n - 1}):
+            ref = O.run(layer, at, lks[i], moveds[i], "cube", 0.0, float(steps), 1.0)
+            assert rel_l2(ecg[i], ref) <= ECG_TOL, (n, i)
+    # per-simulation form (k1 free)
+    free = [1, 5, 6, 7, 8]
+    h.set_eval([synth.BASE_AP] * 3, synth.K_MIN, synth.K_MAX, free, target, mid_position=0.6)
+    ng, _ = h.eval_shape()
+    lo, hi = h.gene_bounds()
+    rng = np.random.Generator(np.random.PCG64(53))
+    g2 = lo + (hi - lo) * rng.random((20, ng))
+    g2[:, 15:] = np.stack([synth.genes_for(spec, 800 + r, 0)[12:] for r in range(20)])
+    lks = np.stack([O.layer_aps(3, np.array([synth.BASE_AP] * 3), synth.K_MIN, synth.K_MAX, free, "endo-mid-epi",
+                                0.6, g[:15])[0] for g in g2])
+    moveds = np.stack([O.move_leads(leads, g[15:].reshape(-1, 2)) for g in g2])
+    assert not h.benchmark(lks, moveds, warmup=1, iters=1)["batched"]
+    crit_b, viol_b, ecg_b = h.eval_batch(g2, want_ecg=True)
+    for i in (0, 10, 19):
+        ref = O.run(layer, at, lks[i], moveds[i], "cube", 0.0, float(steps), 1.0)
+        assert rel_l2(ecg_b[i], ref) <= ECG_TOL, i
+    for i in range(20):
+        c1, v1, e1 = h.eval_batch(g2[i:i + 1], want_ecg=True)
+        assert rel_l2(ecg_b[i], e1[0]) <= ECG_TOL, i
+    h.close()
+
+
 def test_batched_all_leads_moved_and_near_heart(engine):
     """Every lead carries displacement genes (the reference's usual "optimize measuring points"
     case, 12 + 2L genes), some of them moving leads to within a few cells of the heart, so that the
